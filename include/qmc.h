@@ -1,0 +1,143 @@
+/*
+ * qmc.h — C ABI of the GB300 (sm_103a) VMC inner loop: FermiNet log|psi|,
+ * forward-Laplacian local energy and the all-electron Metropolis-Hastings
+ * walker step, plus the walker-batch reductions and the parameter adjoint.
+ *
+ * Conventions
+ *  - Every array argument is caller-owned DEVICE memory unless the name ends
+ *    in `_host`.  Electrons are float32 (batch, n, 3), spin-up electrons first.
+ *  - Calls are stream-ordered on the given cudaStream_t and never synchronise
+ *    the device; results are valid once the stream reaches them.
+ *  - Scratch memory is a caller-provided workspace whose size comes from
+ *    qmc_workspace_size(); no entry point below allocates on the hot path.
+ *  - A model handle is thread-compatible, not thread-safe: one host thread
+ *    (or one serving slot) drives it at a time.
+ *  - Every entry point returns a qmc_status; qmc_last_error() gives the text of
+ *    the calling thread's last failure.  Kernels never trap: numerical trouble
+ *    is reported per walker in a flag array (QMC_FLAG_*).
+ */
+#ifndef QMC_H_
+#define QMC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int qmc_status;
+enum {
+  QMC_OK = 0,
+  QMC_ERR_ARG = 1,         /* bad pointer / value                         */
+  QMC_ERR_SHAPE = 2,       /* unsupported size (electrons, widths, batch) */
+  QMC_ERR_NUMERIC = 3,     /* reserved: hard numerical failure            */
+  QMC_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up          */
+  QMC_ERR_CUDA = 5,        /* a CUDA runtime call failed                  */
+  QMC_ERR_WORKSPACE = 6,   /* workspace smaller than qmc_workspace_size() */
+  QMC_ERR_UNSUPPORTED = 7  /* feature not built / not on this device      */
+};
+
+/* per-walker flag bits written by qmc_forward / qmc_local_energy / qmc_mh_steps */
+enum {
+  QMC_FLAG_NONFINITE = 1,  /* log|psi| or E_L is NaN/Inf                      */
+  QMC_FLAG_REFACTOR = 2,   /* a determinant was re-factorised in FP64          */
+  QMC_FLAG_SINGULAR = 4    /* a determinant has an exactly zero pivot          */
+};
+
+enum { QMC_PRECISION_FP32 = 0, QMC_PRECISION_MIXED_BF16 = 1 };
+enum { QMC_ENVELOPE_ISOTROPIC = 0, QMC_ENVELOPE_ABS_ISOTROPIC = 1 };
+enum { QMC_OP_FORWARD = 0, QMC_OP_LOCAL_ENERGY = 1, QMC_OP_MH = 2, QMC_OP_GRAD = 3 };
+
+#define QMC_MAX_LAYERS 8
+
+/* Hyper-parameters of FermiNetWavefunction
+ * (src/jaqmc/app/molecule/wavefunction/ferminet.py:44-50). */
+typedef struct {
+  int n_up, n_down;                     /* nspins                               */
+  int n_atoms;
+  int ndets;                            /* K                                    */
+  int n_layers;                         /* len(hidden_dims_single)              */
+  int hidden_single[QMC_MAX_LAYERS];
+  int hidden_double[QMC_MAX_LAYERS];
+  int envelope;                         /* QMC_ENVELOPE_*                       */
+  int orbitals_spin_split;              /* 0/1                                  */
+  int precision;                        /* QMC_PRECISION_*                      */
+} qmc_ferminet_config;
+
+typedef struct qmc_model qmc_model;
+
+/* Text of the calling thread's last error ("" if none). */
+const char* qmc_last_error(void);
+
+/* Library / device information; returns QMC_ERR_UNSUPPORTED when the current
+ * device is not an sm_103 part. */
+qmc_status qmc_device_check(int* sm_major, int* sm_minor, int* n_sms);
+
+/* Create a FermiNet model on the current device.  atoms_host (A*3, bohr) and
+ * charges_host (A) are host arrays.  Replaces the construction of
+ * FermiNetWavefunction + its wiring (src/jaqmc/app/molecule/workflow.py:119-136). */
+qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atoms_host,
+                               const float* charges_host, qmc_model** out);
+qmc_status qmc_model_destroy(qmc_model* m);
+
+/* Number of float32 entries of the flat parameter vector (leaf order:
+ * per layer single kernel, bias, [two-electron kernel, bias]; orbital kernels
+ * per spin channel; envelope pi, sigma per channel). */
+size_t qmc_param_count(const qmc_model* m);
+
+/* Load parameters from a flat float32 DEVICE vector (qmc_param_count entries)
+ * into the model's device arena (reordered, padded and, for the mixed form,
+ * converted to bf16).  Replaces the params pytree handed to
+ * Wavefunction.evaluate (src/jaqmc/wavefunction/base.py:94-104). */
+qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t stream);
+
+/* Switch between QMC_PRECISION_FP32 and QMC_PRECISION_MIXED_BF16. */
+qmc_status qmc_model_set_precision(qmc_model* m, int precision);
+
+/* Bytes of workspace needed by `op` (QMC_OP_*) for `batch` walkers. */
+size_t qmc_workspace_size(const qmc_model* m, int op, int batch);
+
+/* log|psi| and sign for a batch: the vmapped FermiNetWavefunction.evaluate /
+ * phase_logpsi (src/jaqmc/app/molecule/wavefunction/ferminet.py:76-122,
+ * src/jaqmc/wavefunction/output/logdet.py:53-80).
+ * logpsi, sign: (batch,) float32; flags: (batch,) uint8 or NULL. */
+qmc_status qmc_forward(qmc_model* m, int batch, const float* electrons, float* logpsi,
+                       float* sign, uint8_t* flags, void* workspace, size_t workspace_bytes,
+                       cudaStream_t stream);
+
+/* Local energy E_L = KE + V per walker with the forward-Laplacian kinetic
+ * energy KE = -1/2 (lap log|psi| + |grad log|psi||^2)
+ * (src/jaqmc/estimator/kinetic/euclidean.py:114-135, _common.py:61-73) and the
+ * Coulomb potential (src/jaqmc/app/molecule/hamiltonian.py:9-22).
+ * Outputs (batch,) float32 each; any of ke / pe / logpsi / flags may be NULL. */
+qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, float* e_local,
+                            float* ke, float* pe, float* logpsi, uint8_t* flags,
+                            void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* `steps` all-electron Gaussian MH updates (src/jaqmc/sampler/mcmc.py:96-199):
+ * x' = x + stddev * N(0,1); accept iff 2 log|psi(x')| - 2 log|psi(x)| > log u.
+ * Draws come from Philox4x32-10 keyed by `seed`, counter (step = counter + s,
+ * walker, block), unless inj_normals (steps,batch,n,3) / inj_uniforms
+ * (steps,batch) are given.  electrons is updated in place; log_prob (batch,)
+ * receives 2 log|psi| of the final walkers; accepts (batch,) uint32 receives the
+ * number of accepted moves per walker (added to its previous value). */
+qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t seed,
+                        uint64_t counter, float* electrons, float* log_prob, uint32_t* accepts,
+                        const float* inj_normals, const float* inj_uniforms, uint8_t* flags,
+                        void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* The draws qmc_mh_steps would use for (seed, counter, steps): normals
+ * (steps,batch,n,3) and uniforms (steps,batch), either may be NULL. */
+qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
+                        uint64_t counter, float* normals, float* uniforms, cudaStream_t stream);
+
+/* FP64 walker-batch mean and variance <x^2> - <x>^2 of a float32 vector,
+ * NaNs skipped (src/jaqmc/estimator/base.py:27-53).  mean_var: 2 doubles. */
+qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QMC_H_ */

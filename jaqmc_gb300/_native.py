@@ -1,0 +1,254 @@
+"""ctypes binding of ``libqmc.so`` (the C ABI declared in ``include/qmc.h``).
+
+The library is built in-tree by ``jaqmc_gb300.build``.  Loading fails loudly
+when it is missing or when no sm_103 device is present: there is no CPU
+fallback on the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+import torch
+
+LIB_PATH = Path(__file__).resolve().parent / "libqmc.so"
+
+QMC_OK = 0
+STATUS = {0: "OK", 1: "ARG", 2: "SHAPE", 3: "NUMERIC", 4: "TIMEOUT", 5: "CUDA", 6: "WORKSPACE",
+          7: "UNSUPPORTED"}
+PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 1}
+ENVELOPE = {"isotropic": 0, "abs_isotropic": 1}
+OP_FORWARD, OP_LOCAL_ENERGY, OP_MH, OP_GRAD = 0, 1, 2, 3
+FLAG_NONFINITE, FLAG_REFACTOR, FLAG_SINGULAR = 1, 2, 4
+MAX_LAYERS = 8
+
+
+class QmcError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"qmc status {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class FermiNetConfigC(C.Structure):
+    _fields_ = [("n_up", C.c_int), ("n_down", C.c_int), ("n_atoms", C.c_int), ("ndets", C.c_int),
+                ("n_layers", C.c_int), ("hidden_single", C.c_int * MAX_LAYERS),
+                ("hidden_double", C.c_int * MAX_LAYERS), ("envelope", C.c_int),
+                ("orbitals_spin_split", C.c_int), ("precision", C.c_int)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "qmc_last_error": (C.c_char_p, []),
+    "qmc_device_check": (C.c_int, [C.POINTER(C.c_int)] * 3),
+    "qmc_ferminet_create": (C.c_int, [C.POINTER(FermiNetConfigC), C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_void_p)]),
+    "qmc_model_destroy": (C.c_int, [C.c_void_p]),
+    "qmc_param_count": (C.c_size_t, [C.c_void_p]),
+    "qmc_model_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qmc_model_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
+    "qmc_workspace_size": (C.c_size_t, [C.c_void_p, C.c_int, C.c_int]),
+    "qmc_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "qmc_local_energy": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                   C.c_void_p]),
+    "qmc_mh_steps": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_uint64,
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "qmc_mh_draws": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p,
+                               C.c_void_p, C.c_void_p]),
+    "qmc_reduce_mean_var": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+
+def exported_symbols():
+    """Names the library must export (every entry point of include/qmc.h)."""
+    return list(_SIGS)
+
+
+def load(path: Path | None = None):
+    """Load ``libqmc.so`` (no device needed) and bind the signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = Path(path or LIB_PATH)
+        if not p.exists():
+            raise FileNotFoundError(
+                f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                "or `python -m jaqmc_gb300.build` (there is no CPU fallback)")
+        lib = C.CDLL(str(p))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(status: int):
+    if status != QMC_OK:
+        raise QmcError(status, load().qmc_last_error().decode())
+
+
+def ptr(t) -> int | None:
+    if t is None:
+        return None
+    if isinstance(t, torch.Tensor):
+        if not t.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if not t.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return t.data_ptr()
+    return int(t)
+
+
+def stream_handle(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def device_check():
+    lib = load()
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    check(lib.qmc_device_check(C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value
+
+
+class Workspace:
+    """Caller-owned scratch buffers, grown on demand (never inside a step)."""
+
+    def __init__(self, device):
+        self.device = device
+        self.buf = None
+
+    def get(self, nbytes: int) -> torch.Tensor:
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
+        return self.buf
+
+
+class NativeFermiNet:
+    """One ``qmc_model`` handle: a FermiNet for one molecule on one device."""
+
+    def __init__(self, cfg, atoms, charges, precision="fp32", device=None):
+        lib = load()
+        self.lib = lib
+        self.device = torch.device(device or "cuda")
+        torch.cuda.set_device(self.device)
+        if not torch.cuda.is_available():
+            raise RuntimeError("no CUDA device: the qmc library has no CPU fallback")
+        device_check()
+        c = FermiNetConfigC()
+        c.n_up, c.n_down = int(cfg.nspins[0]), int(cfg.nspins[1])
+        atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 3))
+        charges = np.ascontiguousarray(np.asarray(charges, np.float32).reshape(-1))
+        c.n_atoms = atoms.shape[0]
+        c.ndets = int(cfg.ndets)
+        L = len(cfg.hidden_dims_single)
+        c.n_layers = L
+        for i in range(L):
+            c.hidden_single[i] = int(cfg.hidden_dims_single[i])
+            c.hidden_double[i] = int(cfg.hidden_dims_double[i])
+        c.envelope = ENVELOPE[str(cfg.envelope)]
+        c.orbitals_spin_split = int(bool(cfg.orbitals_spin_split))
+        c.precision = PRECISION[precision]
+        if getattr(cfg, "use_last_layer", False):
+            raise QmcError(7, "use_last_layer=True is not supported")
+        h = C.c_void_p()
+        check(lib.qmc_ferminet_create(C.byref(c), atoms.ctypes.data, charges.ctypes.data, C.byref(h)))
+        self.h = h
+        self.n = c.n_up + c.n_down
+        self.precision = precision
+        self.ws = Workspace(self.device)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.qmc_model_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+    @property
+    def param_count(self) -> int:
+        return int(self.lib.qmc_param_count(self.h))
+
+    def set_precision(self, precision: str):
+        check(self.lib.qmc_model_set_precision(self.h, PRECISION[precision]))
+        self.precision = precision
+
+    def set_params(self, flat: torch.Tensor, stream=None):
+        flat = flat.to(device=self.device, dtype=torch.float32).contiguous()
+        if flat.numel() != self.param_count:
+            raise QmcError(2, f"expected {self.param_count} parameters, got {flat.numel()}")
+        check(self.lib.qmc_model_set_params(self.h, ptr(flat), stream_handle(stream)))
+        self._params = flat  # keep alive until the copy has run
+
+    def workspace(self, op: int, batch: int):
+        nb = int(self.lib.qmc_workspace_size(self.h, op, batch))
+        return self.ws.get(nb), nb
+
+    def _elec(self, electrons):
+        e = electrons
+        if e.dtype != torch.float32 or not e.is_cuda or not e.is_contiguous():
+            raise ValueError("electrons must be a contiguous float32 CUDA tensor (B, n, 3)")
+        if e.dim() != 3 or e.shape[1] != self.n or e.shape[2] != 3:
+            raise ValueError(f"electrons must have shape (B, {self.n}, 3), got {tuple(e.shape)}")
+        return e
+
+    def forward(self, electrons, stream=None):
+        e = self._elec(electrons)
+        B = e.shape[0]
+        lp = torch.empty(B, dtype=torch.float32, device=self.device)
+        sg = torch.empty_like(lp)
+        fl = torch.empty(B, dtype=torch.uint8, device=self.device)
+        ws, nb = self.workspace(OP_FORWARD, B)
+        check(self.lib.qmc_forward(self.h, B, ptr(e), ptr(lp), ptr(sg), ptr(fl), ptr(ws), ws.numel(),
+                                   stream_handle(stream)))
+        return lp, sg, fl
+
+    def local_energy(self, electrons, stream=None):
+        e = self._elec(electrons)
+        B = e.shape[0]
+        out = torch.empty((4, B), dtype=torch.float32, device=self.device)
+        fl = torch.empty(B, dtype=torch.uint8, device=self.device)
+        ws, nb = self.workspace(OP_LOCAL_ENERGY, B)
+        check(self.lib.qmc_local_energy(self.h, B, ptr(e), ptr(out[0]), ptr(out[1]), ptr(out[2]),
+                                        ptr(out[3]), ptr(fl), ptr(ws), ws.numel(), stream_handle(stream)))
+        return {"e_local": out[0], "kinetic": out[1], "potential": out[2], "logpsi": out[3], "flags": fl}
+
+    def mh_steps(self, electrons, steps, stddev, seed, counter, log_prob=None, accepts=None,
+                 normals=None, uniforms=None, stream=None):
+        e = self._elec(electrons)
+        B = e.shape[0]
+        if log_prob is None:
+            log_prob = torch.empty(B, dtype=torch.float32, device=self.device)
+        if accepts is None:
+            accepts = torch.zeros(B, dtype=torch.int32, device=self.device)
+        fl = torch.empty(B, dtype=torch.uint8, device=self.device)
+        ws, nb = self.workspace(OP_MH, B)
+        check(self.lib.qmc_mh_steps(self.h, B, int(steps), float(stddev), int(seed), int(counter), ptr(e),
+                                    ptr(log_prob), ptr(accepts), ptr(normals), ptr(uniforms), ptr(fl),
+                                    ptr(ws), ws.numel(), stream_handle(stream)))
+        return e, log_prob, accepts, fl
+
+    def mh_draws(self, batch, steps, seed, counter, stream=None):
+        nz = torch.empty((steps, batch, self.n, 3), dtype=torch.float32, device=self.device)
+        uz = torch.empty((steps, batch), dtype=torch.float32, device=self.device)
+        check(self.lib.qmc_mh_draws(self.h, int(batch), int(steps), int(seed), int(counter), ptr(nz),
+                                    ptr(uz), stream_handle(stream)))
+        return nz, uz
+
+
+def reduce_mean_var(x: torch.Tensor, stream=None):
+    out = torch.empty(2, dtype=torch.float64, device=x.device)
+    x = x.to(torch.float32).contiguous()
+    check(load().qmc_reduce_mean_var(x.numel(), ptr(x), ptr(out), stream_handle(stream)))
+    return out

@@ -1,0 +1,549 @@
+// C ABI (include/qmc.h): model arena, workspace planning and the drivers of
+// the forward pass, the forward-Laplacian local energy and the MH steps.
+#include <stdarg.h>
+#include <string.h>
+
+#include <cmath>
+#include <string>
+
+#include "common.cuh"
+#include "gemm_simt.cuh"
+#include "kernels.cuh"
+#include "stream_tc.cuh"
+
+namespace qmc {
+
+static thread_local std::string g_err;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+qmc_status cuda_status(cudaError_t e, const char* what) {
+  set_error("CUDA error in %s: %s", what, cudaGetErrorString(e));
+  return QMC_ERR_CUDA;
+}
+
+// ------------------------------------------------------------ layouts
+static qmc_status build_dims(const qmc_ferminet_config* c, Dims* d) {
+  memset(d, 0, sizeof *d);
+  if (c->n_up < 0 || c->n_down < 0 || c->n_up + c->n_down < 1) {
+    set_error("nspins must be non-negative with at least one electron");
+    return QMC_ERR_SHAPE;
+  }
+  d->n_up = c->n_up;
+  d->n_dn = c->n_down;
+  d->n = c->n_up + c->n_down;
+  if (d->n > 64) {
+    set_error("at most 64 electrons are supported (got %d)", d->n);
+    return QMC_ERR_SHAPE;
+  }
+  d->A = c->n_atoms;
+  if (d->A < 1 || d->A > kMaxAtoms) {
+    set_error("n_atoms must be in 1..%d", kMaxAtoms);
+    return QMC_ERR_SHAPE;
+  }
+  d->K = c->ndets;
+  if (d->K < 1 || d->K > 64) {
+    set_error("ndets must be in 1..64");
+    return QMC_ERR_SHAPE;
+  }
+  d->L = c->n_layers;
+  if (d->L < 1 || d->L > QMC_MAX_LAYERS) {
+    set_error("n_layers must be in 1..%d", QMC_MAX_LAYERS);
+    return QMC_ERR_SHAPE;
+  }
+  d->C = (d->n_up > 0) + (d->n_dn > 0);
+  d->split = c->orbitals_spin_split && d->n_up > 0 && d->n_dn > 0;
+  d->env_abs = c->envelope == QMC_ENVELOPE_ABS_ISOTROPIC;
+  if (c->envelope != QMC_ENVELOPE_ABS_ISOTROPIC && c->envelope != QMC_ENVELOPE_ISOTROPIC) {
+    set_error("unsupported envelope %d", c->envelope);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  int d1 = 4 * d->A, d2 = 4;
+  for (int l = 0; l < d->L; ++l) {
+    int s = c->hidden_single[l], t = c->hidden_double[l];
+    if (s < 8 || s % 8 || s > 1024 || t < 1 || t > 256 || 256 % t) {
+      set_error("layer %d: widths (%d, %d) unsupported (single: multiple of 8 up to 1024; "
+                "double: a divisor of 256)", l, s, t);
+      return QMC_ERR_SHAPE;
+    }
+    d->d1_in[l] = d1;
+    d->d2_in[l] = d2;
+    d->d1[l] = s;
+    d->d2[l] = t;
+    d->upd2[l] = l < d->L - 1;
+    d->d1_in_p[l] = round_up(d1, 8);
+    d->g1_p[l] = round_up(d->C * d1, 8);
+    d->g2_p[l] = round_up(d->C * d2, 8);
+    if (l == 0 && d1 == s) {
+      set_error("a residual connection on the first layer (4*n_atoms == width) is not supported");
+      return QMC_ERR_SHAPE;
+    }
+    d1 = s;
+    if (d->upd2[l]) d2 = t;
+  }
+  d->d_last = d1;
+  d->norb = d->K * d->n;
+  d->norb_p = round_up(d->norb, 4);
+  return QMC_OK;
+}
+
+static void build_param_layout(const Dims& d, ParamLayout* p) {
+  size_t o = 0;
+  for (int l = 0; l < d.L; ++l) {
+    int rows = d.d1_in[l] + d.C * d.d1_in[l] + d.C * d.d2_in[l];
+    p->dense1_k[l] = o; o += (size_t)rows * d.d1[l];
+    p->dense1_b[l] = o; o += d.d1[l];
+    if (d.upd2[l]) {
+      p->dense2_k[l] = o; o += (size_t)d.d2_in[l] * d.d2[l];
+      p->dense2_b[l] = o; o += d.d2[l];
+    }
+  }
+  int nch = d.split ? 2 : 1;
+  for (int s = 0; s < nch; ++s) { p->orb_k[s] = o; o += (size_t)d.d_last * d.norb; }
+  for (int s = 0; s < nch; ++s) {
+    p->env_pi[s] = o; o += (size_t)d.n * d.A * d.K;
+    p->env_sigma[s] = o; o += (size_t)d.n * d.A * d.K;
+  }
+  p->total = o;
+}
+
+static void build_arena(const Dims& d, ArenaLayout* a) {
+  size_t o = 0;
+  auto take = [&](size_t n) { size_t r = o; o += align_up(n, 64); return r; };
+  for (int l = 0; l < d.L; ++l) {
+    a->w_main[l] = take((size_t)(d.d1_in_p[l] + d.g2_p[l]) * d.d1[l]);
+    a->w_g1[l] = take((size_t)d.g1_p[l] * d.d1[l]);
+    a->b1[l] = take(d.d1[l]);
+    if (d.upd2[l]) {
+      a->w2[l] = take((size_t)d.d2_in[l] * d.d2[l]);
+      a->b2[l] = take(d.d2[l]);
+    }
+  }
+  int nch = d.split ? 2 : 1;
+  for (int s = 0; s < nch; ++s) a->w_orb[s] = take((size_t)d.d_last * d.norb_p);
+  for (int s = 0; s < nch; ++s) {
+    a->env_pi[s] = take((size_t)d.n * d.A * d.K);
+    a->env_sigma[s] = take((size_t)d.n * d.A * d.K);
+  }
+  a->atoms = take(3 * d.A);
+  a->charges = take(d.A);
+  a->total = o;
+  size_t b = 0;
+  auto takeb = [&](size_t n) { size_t r = b; b += align_up(n, 128); return r; };
+  for (int l = 0; l < d.L; ++l) {
+    a->t_main[l] = takeb((size_t)d.d1[l] * (d.d1_in_p[l] + d.g2_p[l]));
+    a->t_g1[l] = takeb((size_t)d.d1[l] * d.g1_p[l]);
+  }
+  for (int s = 0; s < nch; ++s) a->t_orb[s] = takeb((size_t)round_up(d.norb, 128) * d.d_last);
+  a->total_bf16 = b;
+}
+
+// ------------------------------------------------------------ workspace
+struct Plan {
+  int B, T, Tp, P2, K0p;
+  bool mixed;
+  size_t x0, h1[2], h2[2], g1, gb, g2, rae, aevec, amat, pe, lpsi, sgn, xp, lp, refac, total;
+  size_t act_bytes;  // element size of one-electron activations
+};
+
+static int tangent_count(const Dims& d, int op) { return op == QMC_OP_LOCAL_ENERGY ? 3 * d.n + 2 : 1; }
+
+// Padded tangent count: the tensor-core path tiles columns by whole groups
+// with a 16-column granularity.
+static int padded_tangents(const Dims& d, int T, bool mixed) {
+  if (T == 1) return 1;
+  return mixed ? tc_padded_tangents(T) : T;
+}
+
+static Plan make_plan(const qmc_model* m, int op, int B) {
+  const Dims& d = m->d;
+  Plan p{};
+  p.B = B;
+  p.mixed = m->precision == QMC_PRECISION_MIXED_BF16;
+  p.T = tangent_count(d, op);
+  p.Tp = padded_tangents(d, p.T, p.mixed);
+  p.P2 = p.T > 1 ? 5 : 1;
+  p.K0p = d.d1_in_p[0];
+  p.act_bytes = p.mixed ? 2 : 4;
+  const size_t rows = (size_t)B * d.n * p.Tp;
+  int dmax = 8, g1max = 8, g2max = 8, d2max = 4;
+  for (int l = 0; l < d.L; ++l) {
+    dmax = std::max(dmax, std::max(d.d1_in_p[l], d.d1[l]));
+    g1max = std::max(g1max, d.g1_p[l]);
+    g2max = std::max(g2max, d.g2_p[l]);
+    d2max = std::max(d2max, d.d2[l]);
+  }
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes, 256); return r; };
+  p.x0 = take(rows * p.K0p * 4);
+  p.h1[0] = take(rows * dmax * p.act_bytes);
+  p.h1[1] = take(rows * dmax * p.act_bytes);
+  size_t pairs = (size_t)B * d.n * d.n;
+  p.h2[0] = take(pairs * p.P2 * d2max * 4);
+  p.h2[1] = take(pairs * p.P2 * d2max * 4);
+  p.g1 = take((size_t)B * p.Tp * g1max * 4);
+  p.gb = take((size_t)B * p.Tp * dmax * 4);
+  p.g2 = take(rows * g2max * 4);
+  p.rae = take((size_t)B * d.n * d.A * 4);
+  p.aevec = take((size_t)B * d.n * d.A * 12);
+  p.amat = take((size_t)B * d.K * p.Tp * d.n * d.n * 4);
+  p.pe = take((size_t)B * 4);
+  p.lpsi = take((size_t)B * 4);
+  p.sgn = take((size_t)B * 4);
+  p.xp = take((size_t)B * d.n * 12);
+  p.lp = take((size_t)B * 4);
+  p.refac = take(16);
+  p.total = o;
+  return p;
+}
+
+template <typename T>
+static T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+
+// ------------------------------------------------------------ network
+// One-electron layer l: spin means, broadcast GEMM, main GEMM with the
+// tangent epilogue; then the two-electron update.
+template <typename ActT>
+static qmc_status run_backbone(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
+  const Dims& d = m->d;
+  const float* ar = m->arena;
+  const ArenaLayout& a = m->a;
+  const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
+  const RowMap rows_map{n, 0, n, Tp};
+  const RowMap wt_map{1, 0, 1, Tp};
+  const int ngroups = B * n;
+  int cur = 0, h2cur = 0;
+  for (int l = 0; l < d.L; ++l) {
+    const int din = d.d1_in[l], dinp = d.d1_in_p[l], dout = d.d1[l];
+    ActT* out = at<ActT>(ws, p.h1[l == 0 ? 0 : cur ^ 1]);
+    float* G1 = at<float>(ws, p.g1);
+    float* Gb = at<float>(ws, p.gb);
+    const float* H2 = at<float>(ws, p.h2[h2cur]);
+    // spin means of the one-electron input
+    if (l == 0) {
+      QMC_CUDA(launch_mean_h1<float>(s, B, n, d.n_up, d.C, Tp, din, dinp, at<float>(ws, p.x0),
+                                     d.g1_p[l], G1));
+    } else {
+      QMC_CUDA(launch_mean_h1<ActT>(s, B, n, d.n_up, d.C, Tp, din, dinp, at<ActT>(ws, p.h1[cur]),
+                                    d.g1_p[l], G1));
+    }
+    // broadcast term G = means @ W_g1, rows (walker, tangent)
+    QMC_CUDA(launch_gemm_simt<float>(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], (const float*)nullptr,
+                                     0, 0, ar + a.w_g1[l], dout, dout,
+                                     EpiStore{Gb, dout, nullptr}));
+    const bool use_tc = p.mixed && l > 0 && tc_layer_supported(dinp, d.g2_p[l], dout);
+    if (l == 0 || !p.mixed) {
+      float* G2 = at<float>(ws, p.g2);
+      QMC_CUDA(launch_mean_h2<float>(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l], G2));
+      EpiLayer<ActT> epi{Gb, ar + a.b1[l], nullptr, out, dout, T};
+      if (l == 0) {
+        QMC_CUDA(launch_gemm_simt<float>(s, ngroups, rows_map, at<float>(ws, p.x0), p.K0p, dinp, G2,
+                                         d.g2_p[l], d.g2_p[l], ar + a.w_main[l], dout, dout, epi));
+      } else {
+        // plain form (ActT == float here)
+        const ActT* in = at<ActT>(ws, p.h1[cur]);
+        if (din == dout) epi.resid = in;
+        QMC_CUDA(launch_gemm_simt<ActT>(s, ngroups, rows_map, in, dinp, dinp,
+                                        reinterpret_cast<const ActT*>(G2), d.g2_p[l], d.g2_p[l],
+                                        ar + a.w_main[l], dout, dout, epi));
+      }
+    } else {
+      ActT* G2 = at<ActT>(ws, p.g2);
+      QMC_CUDA(launch_mean_h2<ActT>(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l], G2));
+      const ActT* in = at<ActT>(ws, p.h1[cur]);
+      EpiLayer<ActT> epi{Gb, ar + a.b1[l], din == dout ? in : nullptr, out, dout, T};
+      if (use_tc) {
+        QMC_TRY(tc_stream_layer(s, ngroups, n, Tp, T, reinterpret_cast<const __nv_bfloat16*>(in), dinp,
+                                reinterpret_cast<const __nv_bfloat16*>(G2), d.g2_p[l],
+                                m->arena_bf16 + a.t_main[l], dout, Gb, ar + a.b1[l],
+                                din == dout, reinterpret_cast<__nv_bfloat16*>(out)));
+      } else {
+        QMC_CUDA(launch_gemm_simt<ActT>(s, ngroups, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
+                                        ar + a.w_main[l], dout, dout, epi));
+      }
+    }
+    if (d.upd2[l]) {
+      QMC_CUDA(launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l], ar + a.b2[l],
+                                 at<float>(ws, p.h2[h2cur ^ 1])));
+      h2cur ^= 1;
+    }
+    cur = (l == 0) ? 0 : cur ^ 1;
+  }
+  *out_buf = cur;
+  return QMC_OK;
+}
+
+template <typename ActT>
+static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
+  const Dims& d = m->d;
+  const ArenaLayout& a = m->a;
+  const float* ar = m->arena;
+  const ActT* h = at<ActT>(ws, p.h1[hb]);
+  int nch = d.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    int ns = d.split ? (c == 0 ? d.n_up : d.n_dn) : d.n;
+    int i0 = (d.split && c == 1) ? d.n_up : 0;
+    RowMap map{ns, i0, d.n, p.Tp};
+    EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec),
+                   ar + a.env_pi[c], ar + a.env_sigma[c], d.n, d.A, d.K, p.T, d.env_abs};
+    QMC_CUDA(launch_gemm_simt<ActT>(s, p.B * ns, map, h, d.d_last, d.d_last, (const ActT*)nullptr, 0, 0,
+                                    ar + a.w_orb[c], d.norb_p, d.norb, epi));
+  }
+  return QMC_OK;
+}
+
+// Full evaluation: features -> backbone -> orbitals -> determinants.
+static qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
+                           float* logpsi, float* sign, float* ke, float* el, uint8_t* flags,
+                           cudaStream_t s) {
+  const Dims& d = m->d;
+  const float* ar = m->arena;
+  float* pe = want_pe ? at<float>(ws, p.pe) : nullptr;
+  QMC_CUDA(launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
+                           ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
+                           at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe));
+  int hb = 0;
+  if (p.mixed) {
+    QMC_TRY(run_backbone<__nv_bfloat16>(m, p, ws, s, &hb));
+    QMC_TRY(run_orbitals<__nv_bfloat16>(m, p, ws, hb, s));
+  } else {
+    QMC_TRY(run_backbone<float>(m, p, ws, s, &hb));
+    QMC_TRY(run_orbitals<float>(m, p, ws, hb, s));
+  }
+  QMC_CUDA(launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
+                         flags, nullptr));
+  return QMC_OK;
+}
+
+static qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, int op) {
+  if (!m) { set_error("null model"); return QMC_ERR_ARG; }
+  if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
+  if (batch < 1) { set_error("batch must be >= 1"); return QMC_ERR_SHAPE; }
+  if (op == QMC_OP_LOCAL_ENERGY && make_plan(m, op, 1).Tp > 128) {
+    set_error("local energy supports at most 42 electrons (3n+2 <= 128 tangents per tile)");
+    return QMC_ERR_SHAPE;
+  }
+  size_t need = make_plan(m, op, batch).total;
+  if (!ws || ws_bytes < need) {
+    set_error("workspace too small: %zu bytes given, %zu needed", ws_bytes, need);
+    return QMC_ERR_WORKSPACE;
+  }
+  int dev;
+  QMC_CUDA(cudaGetDevice(&dev));
+  if (dev != m->device) {
+    set_error("model lives on device %d but device %d is current", m->device, dev);
+    return QMC_ERR_ARG;
+  }
+  return QMC_OK;
+}
+
+}  // namespace qmc
+
+using namespace qmc;
+
+extern "C" {
+
+const char* qmc_last_error(void) { return qmc::g_err.c_str(); }
+
+qmc_status qmc_device_check(int* major, int* minor, int* n_sms) {
+  int dev;
+  QMC_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp pr;
+  QMC_CUDA(cudaGetDeviceProperties(&pr, dev));
+  if (major) *major = pr.major;
+  if (minor) *minor = pr.minor;
+  if (n_sms) *n_sms = pr.multiProcessorCount;
+  if (!(pr.major == 10 && pr.minor == 3)) {
+    set_error("device %s is sm_%d%d; this library is built for sm_103a", pr.name, pr.major, pr.minor);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  return QMC_OK;
+}
+
+qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atoms_host,
+                               const float* charges_host, qmc_model** out) {
+  if (!cfg || !atoms_host || !charges_host || !out) {
+    set_error("null argument");
+    return QMC_ERR_ARG;
+  }
+  *out = nullptr;
+  qmc_model* m = new qmc_model();
+  qmc_status st = build_dims(cfg, &m->d);
+  if (st != QMC_OK) { delete m; return st; }
+  if (cfg->precision != QMC_PRECISION_FP32 && cfg->precision != QMC_PRECISION_MIXED_BF16) {
+    delete m;
+    set_error("unknown precision %d", cfg->precision);
+    return QMC_ERR_ARG;
+  }
+  m->precision = cfg->precision;
+  build_param_layout(m->d, &m->p);
+  build_arena(m->d, &m->a);
+  cudaError_t e = cudaGetDevice(&m->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->n_sms, cudaDevAttrMultiProcessorCount, m->device);
+  if (e == cudaSuccess) e = cudaMalloc(&m->arena, m->a.total * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->arena_bf16, m->a.total_bf16 * sizeof(__nv_bfloat16));
+  if (e == cudaSuccess) e = cudaMemset(m->arena, 0, m->a.total * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(m->arena_bf16, 0, m->a.total_bf16 * sizeof(__nv_bfloat16));
+  const int A = m->d.A;
+  memcpy(m->atoms_host, atoms_host, sizeof(float) * 3 * A);
+  memcpy(m->charges_host, charges_host, sizeof(float) * A);
+  double nuc = 0.0;
+  for (int I = 0; I < A; ++I)
+    for (int J = I + 1; J < A; ++J) {
+      double dx = atoms_host[3 * I] - atoms_host[3 * J], dy = atoms_host[3 * I + 1] - atoms_host[3 * J + 1],
+             dz = atoms_host[3 * I + 2] - atoms_host[3 * J + 2];
+      nuc += (double)charges_host[I] * charges_host[J] / std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  m->nuclear_repulsion = nuc;
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->arena + m->a.atoms, atoms_host, sizeof(float) * 3 * A, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->arena + m->a.charges, charges_host, sizeof(float) * A, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(m->arena);
+    cudaFree(m->arena_bf16);
+    delete m;
+    return cuda_status(e, "qmc_ferminet_create");
+  }
+  *out = m;
+  return QMC_OK;
+}
+
+qmc_status qmc_model_destroy(qmc_model* m) {
+  if (!m) return QMC_OK;
+  cudaFree(m->arena);
+  cudaFree(m->arena_bf16);
+  delete m;
+  return QMC_OK;
+}
+
+size_t qmc_param_count(const qmc_model* m) { return m ? m->p.total : 0; }
+
+qmc_status qmc_model_set_precision(qmc_model* m, int precision) {
+  if (!m) { set_error("null model"); return QMC_ERR_ARG; }
+  if (precision != QMC_PRECISION_FP32 && precision != QMC_PRECISION_MIXED_BF16) {
+    set_error("unknown precision %d", precision);
+    return QMC_ERR_ARG;
+  }
+  m->precision = precision;
+  return QMC_OK;
+}
+
+qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t s) {
+  if (!m || !params) { set_error("null argument"); return QMC_ERR_ARG; }
+  const Dims& d = m->d;
+  const ArenaLayout& a = m->a;
+  const ParamLayout& p = m->p;
+  float* ar = m->arena;
+  auto cp = [&](size_t dst, size_t src, size_t count) {
+    return cudaMemcpyAsync(ar + dst, params + src, count * sizeof(float), cudaMemcpyDeviceToDevice, s);
+  };
+  for (int l = 0; l < d.L; ++l) {
+    const int din = d.d1_in[l], dout = d.d1[l];
+    QMC_CUDA(cudaMemsetAsync(ar + a.w_main[l], 0, sizeof(float) * (d.d1_in_p[l] + d.g2_p[l]) * dout, s));
+    QMC_CUDA(cudaMemsetAsync(ar + a.w_g1[l], 0, sizeof(float) * d.g1_p[l] * dout, s));
+    size_t k = p.dense1_k[l];
+    // rows [h1 | g1 (C*din) | g2 (C*d2in)] of the reference kernel
+    QMC_CUDA(cp(a.w_main[l], k, (size_t)din * dout));
+    QMC_CUDA(cp(a.w_g1[l], k + (size_t)din * dout, (size_t)d.C * din * dout));
+    QMC_CUDA(cp(a.w_main[l] + (size_t)d.d1_in_p[l] * dout, k + (size_t)(din + d.C * din) * dout,
+                (size_t)d.C * d.d2_in[l] * dout));
+    QMC_CUDA(cp(a.b1[l], p.dense1_b[l], dout));
+    if (d.upd2[l]) {
+      QMC_CUDA(cp(a.w2[l], p.dense2_k[l], (size_t)d.d2_in[l] * d.d2[l]));
+      QMC_CUDA(cp(a.b2[l], p.dense2_b[l], d.d2[l]));
+    }
+  }
+  int nch = d.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    QMC_CUDA(cudaMemsetAsync(ar + a.w_orb[c], 0, sizeof(float) * d.d_last * d.norb_p, s));
+    QMC_CUDA(cudaMemcpy2DAsync(ar + a.w_orb[c], sizeof(float) * d.norb_p, params + p.orb_k[c],
+                               sizeof(float) * d.norb, sizeof(float) * d.norb, d.d_last,
+                               cudaMemcpyDeviceToDevice, s));
+    QMC_CUDA(cp(a.env_pi[c], p.env_pi[c], (size_t)d.n * d.A * d.K));
+    QMC_CUDA(cp(a.env_sigma[c], p.env_sigma[c], (size_t)d.n * d.A * d.K));
+  }
+  // bf16 K-major copies for the tensor-core path
+  for (int l = 0; l < d.L; ++l) {
+    int kmain = d.d1_in_p[l] + d.g2_p[l];
+    QMC_CUDA(launch_transpose_bf16(s, ar + a.w_main[l], kmain, d.d1[l], d.d1[l],
+                                   m->arena_bf16 + a.t_main[l], kmain, d.d1[l]));
+    QMC_CUDA(launch_transpose_bf16(s, ar + a.w_g1[l], d.g1_p[l], d.d1[l], d.d1[l],
+                                   m->arena_bf16 + a.t_g1[l], d.g1_p[l], d.d1[l]));
+  }
+  for (int c = 0; c < nch; ++c)
+    QMC_CUDA(launch_transpose_bf16(s, ar + a.w_orb[c], d.d_last, d.norb, d.norb_p,
+                                   m->arena_bf16 + a.t_orb[c], d.d_last, round_up(d.norb, 128)));
+  m->params_set = true;
+  return QMC_OK;
+}
+
+size_t qmc_workspace_size(const qmc_model* m, int op, int batch) {
+  if (!m || batch < 1) return 0;
+  return make_plan(m, op, batch).total;
+}
+
+qmc_status qmc_forward(qmc_model* m, int batch, const float* electrons, float* logpsi, float* sign,
+                       uint8_t* flags, void* ws, size_t ws_bytes, cudaStream_t s) {
+  QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_FORWARD));
+  if (!electrons || !logpsi) { set_error("null electrons/logpsi"); return QMC_ERR_ARG; }
+  Plan p = make_plan(m, QMC_OP_FORWARD, batch);
+  return evaluate(m, p, ws, electrons, false, logpsi, sign, nullptr, nullptr, flags, s);
+}
+
+qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, float* e_local, float* ke,
+                            float* pe, float* logpsi, uint8_t* flags, void* ws, size_t ws_bytes,
+                            cudaStream_t s) {
+  QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_LOCAL_ENERGY));
+  if (!electrons || !e_local) { set_error("null electrons/e_local"); return QMC_ERR_ARG; }
+  Plan p = make_plan(m, QMC_OP_LOCAL_ENERGY, batch);
+  QMC_TRY(evaluate(m, p, ws, electrons, true, logpsi ? logpsi : at<float>(ws, p.lpsi),
+                   at<float>(ws, p.sgn), ke, e_local, flags, s));
+  if (pe) QMC_CUDA(cudaMemcpyAsync(pe, at<float>(ws, p.pe), sizeof(float) * batch, cudaMemcpyDeviceToDevice, s));
+  return QMC_OK;
+}
+
+qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t seed, uint64_t counter,
+                        float* electrons, float* log_prob, uint32_t* accepts, const float* inj_normals,
+                        const float* inj_uniforms, uint8_t* flags, void* ws, size_t ws_bytes,
+                        cudaStream_t s) {
+  QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_MH));
+  if (!electrons || !log_prob || steps < 0) { set_error("bad electrons/log_prob/steps"); return QMC_ERR_ARG; }
+  Plan p = make_plan(m, QMC_OP_MH, batch);
+  const int n = m->d.n;
+  float* lpsi = at<float>(ws, p.lpsi);
+  // log_prob of the starting walkers (src/jaqmc/sampler/mcmc.py:166)
+  QMC_TRY(evaluate(m, p, ws, electrons, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, flags, s));
+  QMC_CUDA(launch_scale(s, batch, lpsi, 2.0f, log_prob));
+  float* xp = at<float>(ws, p.xp);
+  for (int st = 0; st < steps; ++st) {
+    const float* nz = inj_normals ? inj_normals + (size_t)st * batch * n * 3 : nullptr;
+    const float* uz = inj_uniforms ? inj_uniforms + (size_t)st * batch : nullptr;
+    QMC_CUDA(launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, nz));
+    QMC_TRY(evaluate(m, p, ws, xp, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, nullptr, s));
+    QMC_CUDA(launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, uz, accepts));
+  }
+  return QMC_OK;
+}
+
+qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed, uint64_t counter,
+                        float* normals, float* uniforms, cudaStream_t s) {
+  if (!m || batch < 1 || steps < 1) { set_error("bad arguments"); return QMC_ERR_ARG; }
+  QMC_CUDA(launch_mh_draws(s, batch, m->d.n, steps, seed, counter, normals, uniforms));
+  return QMC_OK;
+}
+
+qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t s) {
+  if (batch < 1 || !x || !mean_var) { set_error("bad arguments"); return QMC_ERR_ARG; }
+  QMC_CUDA(launch_reduce_mean_var(s, batch, x, mean_var));
+  return QMC_OK;
+}
+
+}  // extern "C"

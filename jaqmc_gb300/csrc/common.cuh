@@ -1,0 +1,149 @@
+// Internal declarations shared by the qmc CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/qmc.h"
+
+namespace qmc {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+qmc_status cuda_status(cudaError_t e, const char* what);
+
+#define QMC_CUDA(call)                                                     \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) return ::qmc::cuda_status(e_, #call);           \
+  } while (0)
+#define QMC_LAUNCH(what)                                                   \
+  do {                                                                     \
+    cudaError_t e_ = cudaGetLastError();                                   \
+    if (e_ != cudaSuccess) return ::qmc::cuda_status(e_, what);            \
+  } while (0)
+#define QMC_TRY(expr)                                                      \
+  do {                                                                     \
+    qmc_status s_ = (expr);                                                \
+    if (s_ != QMC_OK) return s_;                                           \
+  } while (0)
+
+__host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+__host__ __device__ inline size_t align_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+constexpr float kRsqrt2 = 0.70710678118654752440f;
+constexpr int kMaxAtoms = 64;
+
+// ---------------------------------------------------------------- model
+// Dimensions derived from qmc_ferminet_config.  Widths with a trailing `p`
+// are padded to a multiple of 8 (the K step of the SIMT GEMM); padded
+// activation columns and weight rows are kept at zero.
+struct Dims {
+  int n_up, n_dn, n, A, K, L, C;  // C: non-empty spin channels
+  int split;                      // per-spin orbitals/envelopes
+  int env_abs;
+  int d1_in[QMC_MAX_LAYERS], d2_in[QMC_MAX_LAYERS];
+  int d1[QMC_MAX_LAYERS], d2[QMC_MAX_LAYERS];
+  int upd2[QMC_MAX_LAYERS];
+  int d1_in_p[QMC_MAX_LAYERS];   // padded one-electron input width
+  int g1_p[QMC_MAX_LAYERS];      // padded width of the spin means of h1 (C*d1_in)
+  int g2_p[QMC_MAX_LAYERS];      // padded width of the spin means of h2 (C*d2_in)
+  int d_last;                    // width of the last one-electron layer
+  int norb;                      // K*n orbital columns per electron
+  int norb_p;                    // norb padded to a multiple of 4 (weight row stride)
+};
+
+// Device arena layout (float offsets) of the derived parameters.
+struct ArenaLayout {
+  size_t w_main[QMC_MAX_LAYERS];  // [(d1_in_p + g2_p) x d1]   rows: W_h ; W_g2
+  size_t w_g1[QMC_MAX_LAYERS];    // [g1_p x d1]
+  size_t b1[QMC_MAX_LAYERS];      // [d1]
+  size_t w2[QMC_MAX_LAYERS];      // [d2_in x d2]
+  size_t b2[QMC_MAX_LAYERS];      // [d2]
+  size_t w_orb[2];                // [d_last x norb_p] per channel (zero padded columns)
+  size_t env_pi[2], env_sigma[2]; // [n x A x K] per channel (reference layout)
+  size_t atoms, charges;          // [A x 3], [A]
+  size_t total;                   // floats
+  // bf16 arena (element offsets) for the mixed form: transposed weights
+  size_t t_main[QMC_MAX_LAYERS];  // [d1 x (d1_in_p + g2_p)] K-major
+  size_t t_g1[QMC_MAX_LAYERS];    // [d1 x g1_p]
+  size_t t_orb[2];                // [norb_p x d_last]
+  size_t total_bf16;
+};
+
+// Source offsets of each leaf in the flat parameter vector.
+struct ParamLayout {
+  size_t dense1_k[QMC_MAX_LAYERS], dense1_b[QMC_MAX_LAYERS];
+  size_t dense2_k[QMC_MAX_LAYERS], dense2_b[QMC_MAX_LAYERS];
+  size_t orb_k[2];
+  size_t env_pi[2], env_sigma[2];
+  size_t total;
+};
+
+}  // namespace qmc
+
+struct qmc_model {
+  qmc::Dims d;
+  qmc::ArenaLayout a;
+  qmc::ParamLayout p;
+  int precision;
+  int device;
+  float* arena = nullptr;          // derived fp32 parameters
+  __nv_bfloat16* arena_bf16 = nullptr;
+  float atoms_host[3 * qmc::kMaxAtoms];
+  float charges_host[qmc::kMaxAtoms];
+  double nuclear_repulsion = 0.0;  // sum_{I<J} Z_I Z_J / R_IJ
+  bool params_set = false;
+  int n_sms = 0;
+};
+
+namespace qmc {
+
+// ---------------------------------------------------------------- Philox
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11): 10 rounds of the
+// multiply/xor-swap round function with the published multipliers and Weyl
+// key increments.
+struct U4 { uint32_t x, y, z, w; };
+
+__host__ __device__ inline uint32_t mulhilo(uint32_t a, uint32_t b, uint32_t* hi) {
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  *hi = (uint32_t)(p >> 32);
+  return (uint32_t)p;
+}
+
+__host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, hi1;
+    uint32_t lo0 = mulhilo(M0, c.x, &hi0);
+    uint32_t lo1 = mulhilo(M1, c.z, &hi1);
+    U4 n;
+    n.x = hi1 ^ c.y ^ k0;
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ k1;
+    n.w = lo0;
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// Open-interval uniform from the top 24 bits: ((x >> 8) + 0.5) * 2^-24.
+__host__ __device__ inline float u01(uint32_t x) {
+  return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
+// Draw layout of one MH step for one walker: Philox blocks b = 0..nb-1 with
+// counter (b, walker, step_lo, step_hi) give 4 words each.  Words are
+// consumed in pairs by Box-Muller for the 3n normals (block 0 .. ceil(3n/4)-1);
+// the accept uniform is word x of block ceil(3n/4).
+__host__ __device__ inline int normal_blocks(int n) { return (3 * n + 3) / 4; }
+
+}  // namespace qmc

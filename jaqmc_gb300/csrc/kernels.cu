@@ -1,0 +1,797 @@
+// FermiNet features, two-electron stream, spin means, determinant stage,
+// Metropolis-Hastings and reductions for sm_103a.
+#include "kernels.cuh"
+
+namespace qmc {
+
+// =====================================================================
+// features (src/jaqmc/wavefunction/input/atomic.py:46-79,
+//           src/jaqmc/geometry/obc.py:7-88,
+//           src/jaqmc/app/molecule/hamiltonian.py:9-22)
+// =====================================================================
+__global__ void k_features(int n, int A, int Tp, int T, int K0p, const float* __restrict__ elec,
+                           const float* __restrict__ atoms, const float* __restrict__ charges,
+                           double nuc, float* __restrict__ X0, float* __restrict__ H2,
+                           float* __restrict__ rae_g, float* __restrict__ aevec_g,
+                           float* __restrict__ pe) {
+  extern __shared__ float sh[];
+  float* xs = sh;                // [n][3]
+  float* rs = xs + 3 * n;        // [n][A]
+  float* vs = rs + n * A;        // [n][A][3]
+  __shared__ double red[32];
+  const int w = blockIdx.x;
+  const float* ew = elec + (size_t)w * n * 3;
+  for (int e = threadIdx.x; e < 3 * n; e += blockDim.x) xs[e] = ew[e];
+  __syncthreads();
+  double vpot = 0.0;
+  for (int e = threadIdx.x; e < n * A; e += blockDim.x) {
+    int i = e / A, I = e % A;
+    float dx = xs[3 * i] - atoms[3 * I], dy = xs[3 * i + 1] - atoms[3 * I + 1],
+          dz = xs[3 * i + 2] - atoms[3 * I + 2];
+    float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    rs[e] = r;
+    vs[3 * e] = dx;
+    vs[3 * e + 1] = dy;
+    vs[3 * e + 2] = dz;
+    size_t gi = (size_t)w * n * A + e;
+    rae_g[gi] = r;
+    aevec_g[3 * gi] = dx;
+    aevec_g[3 * gi + 1] = dy;
+    aevec_g[3 * gi + 2] = dz;
+    vpot -= (double)charges[I] / (double)r;
+  }
+  __syncthreads();
+  // one-electron rows
+  const int A4 = 4 * A;
+  const size_t per_w = (size_t)n * Tp * K0p;
+  float* Xw = X0 + (size_t)w * per_w;
+  for (size_t e = threadIdx.x; e < per_w; e += blockDim.x) {
+    int f = (int)(e % K0p);
+    int t = (int)((e / K0p) % Tp);
+    int i = (int)(e / ((size_t)K0p * Tp));
+    float v = 0.f;
+    if (f < A4 && t < T) {
+      int I = f >> 2, comp = f & 3;
+      float r = rs[i * A + I];
+      const float* vec = vs + 3 * (i * A + I);
+      if (t == 0) {
+        v = comp == 0 ? r : vec[comp - 1];
+      } else if (t == 1) {
+        v = comp == 0 ? 2.0f / r : 0.f;
+      } else {
+        int d = t - 2, el = d / 3, c = d % 3;
+        if (el == i) v = comp == 0 ? vec[c] / r : (comp - 1 == c ? 1.f : 0.f);
+      }
+    }
+    Xw[e] = v;
+  }
+  // two-electron rows
+  const int P2 = T > 1 ? 5 : 1;
+  const size_t per_w2 = (size_t)n * n * P2 * 4;
+  float* Hw = H2 + (size_t)w * per_w2;
+  for (size_t e = threadIdx.x; e < per_w2; e += blockDim.x) {
+    int comp = (int)(e & 3);
+    int p = (int)((e >> 2) % P2);
+    int pr = (int)(e / (4 * P2));
+    int i = pr / n, j = pr % n;
+    float v = 0.f;
+    if (i != j) {
+      float d[3] = {xs[3 * i] - xs[3 * j], xs[3 * i + 1] - xs[3 * j + 1], xs[3 * i + 2] - xs[3 * j + 2]};
+      float r = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      if (p == 0) v = comp == 0 ? r : d[comp - 1];
+      else if (p == 1) v = comp == 0 ? 2.0f / r : 0.f;
+      else {
+        int c = p - 2;
+        v = comp == 0 ? d[c] / r : (comp - 1 == c ? 1.f : 0.f);
+      }
+      if (pe && p == 0 && comp == 0 && i < j) vpot += 1.0 / (double)r;
+    }
+    Hw[e] = v;
+  }
+  if (pe) {
+    // block reduction of the potential
+    for (int o = 16; o > 0; o >>= 1) vpot += __shfl_xor_sync(0xffffffffu, vpot, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vpot;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) pe[w] = (float)(v + nuc);
+    }
+  }
+}
+
+cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, int K0p,
+                            const float* electrons, const float* atoms, const float* charges,
+                            double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe) {
+  size_t sm = sizeof(float) * (3 * n + 4 * n * A);
+  k_features<<<B, 256, sm, s>>>(n, A, Tp, T, K0p, electrons, atoms, charges, nuc, X0, H2, rae,
+                                aevec, pe);
+  return cudaGetLastError();
+}
+
+// =====================================================================
+// two-electron layer (src/jaqmc/wavefunction/backbone/ferminet.py:55-63)
+// rows p: 0 value, 1 Laplacian wrt the pair difference, 2..4 its gradient.
+// =====================================================================
+__global__ void k_pair_layer(int npairs, int P2, int d_in, int d_out, const float* __restrict__ Hin,
+                             const float* __restrict__ W, const float* __restrict__ b,
+                             float* __restrict__ Hout) {
+  extern __shared__ float sh[];
+  float* Ws = sh;                     // [d_in][d_out]
+  float* Is = Ws + d_in * d_out;      // [ppb][P2][d_in]
+  const int ppb = blockDim.x / d_out;
+  const int p0 = blockIdx.x * ppb;
+  for (int e = threadIdx.x; e < d_in * d_out; e += blockDim.x) Ws[e] = W[e];
+  const int np = min(ppb, npairs - p0);
+  for (int e = threadIdx.x; e < np * P2 * d_in; e += blockDim.x)
+    Is[e] = Hin[(size_t)p0 * P2 * d_in + e];
+  __syncthreads();
+  const int lp = threadIdx.x / d_out, f = threadIdx.x % d_out;
+  if (lp >= np) return;
+  const float* in = Is + lp * P2 * d_in;
+  float z[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int k = 0; k < d_in; ++k) {
+    float wv = Ws[k * d_out + f];
+#pragma unroll
+    for (int p = 0; p < 5; ++p)
+      if (p < P2) z[p] = fmaf(in[p * d_in + k], wv, z[p]);
+  }
+  float h = tanhf(z[0] + b[f]);
+  float out[5];
+  out[0] = h;
+  if (P2 > 1) {
+    float d1 = 1.f - h * h, d2 = -2.f * h * d1;
+    float S = z[2] * z[2] + z[3] * z[3] + z[4] * z[4];
+    out[1] = d1 * z[1] + d2 * S;
+    out[2] = d1 * z[2];
+    out[3] = d1 * z[3];
+    out[4] = d1 * z[4];
+  }
+  const bool res = d_in == d_out;
+  float* o = Hout + ((size_t)(p0 + lp) * P2) * d_out + f;
+  for (int p = 0; p < P2; ++p) {
+    float v = out[p];
+    if (res) v = (v + in[p * d_in + f]) * kRsqrt2;
+    o[p * d_out] = v;
+  }
+}
+
+cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
+                              const float* Hin, const float* W, const float* b, float* Hout) {
+  int ppb = 256 / d_out;
+  if (ppb < 1) return cudaErrorInvalidValue;
+  size_t sm = sizeof(float) * (d_in * d_out + ppb * P2 * d_in);
+  k_pair_layer<<<(npairs + ppb - 1) / ppb, ppb * d_out, sm, s>>>(npairs, P2, d_in, d_out, Hin, W, b,
+                                                                  Hout);
+  return cudaGetLastError();
+}
+
+// =====================================================================
+// spin-channel means (src/jaqmc/wavefunction/backbone/ferminet.py:65-90)
+// =====================================================================
+__device__ __forceinline__ void channel_range(int s, int C, int n, int n_up, int* a0, int* a1) {
+  if (C == 1) { *a0 = 0; *a1 = n; return; }
+  *a0 = s == 0 ? 0 : n_up;
+  *a1 = s == 0 ? n_up : n;
+}
+
+template <typename InT>
+__global__ void k_mean_h1(int B, int n, int n_up, int C, int Tp, int d, int ld,
+                          const InT* __restrict__ X, int g1p, float* __restrict__ G1) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t total = (size_t)B * Tp * g1p;
+  if (e >= total) return;
+  int col = (int)(e % g1p);
+  size_t wt = e / g1p;
+  int t = (int)(wt % Tp);
+  int w = (int)(wt / Tp);
+  float v = 0.f;
+  if (col < C * d) {
+    int s = col / d, f = col % d, a0, a1;
+    channel_range(s, C, n, n_up, &a0, &a1);
+    float acc = 0.f;
+    for (int i = a0; i < a1; ++i) acc += (float)X[(((size_t)w * n + i) * Tp + t) * ld + f];
+    v = acc / (float)(a1 - a0);
+  }
+  G1[e] = v;
+}
+
+template <typename InT>
+cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, int ld,
+                           const InT* X, int g1p, float* G1) {
+  size_t total = (size_t)B * Tp * g1p;
+  k_mean_h1<InT><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, d, ld, X, g1p, G1);
+  return cudaGetLastError();
+}
+template cudaError_t launch_mean_h1<float>(cudaStream_t, int, int, int, int, int, int, int,
+                                           const float*, int, float*);
+template cudaError_t launch_mean_h1<__nv_bfloat16>(cudaStream_t, int, int, int, int, int, int, int,
+                                                   const __nv_bfloat16*, int, float*);
+
+// d/dr_e of h2[a, i] = (delta_{ae} - delta_{ie}) d/dDelta (pair (a,i), a != i);
+// the full Laplacian of a pair feature is twice its Laplacian in Delta.
+template <typename OutT>
+__global__ void k_mean_h2(int B, int n, int n_up, int C, int Tp, int T, int d2, int P2,
+                          const float* __restrict__ H2, int g2p, OutT* __restrict__ G2) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t total = (size_t)B * n * Tp * g2p;
+  if (e >= total) return;
+  int col = (int)(e % g2p);
+  size_t r = e / g2p;
+  int t = (int)(r % Tp);
+  size_t wi = r / Tp;
+  int i = (int)(wi % n);
+  int w = (int)(wi / n);
+  float v = 0.f;
+  if (col < C * d2 && t < T) {
+    int s = col / d2, f = col % d2, a0, a1;
+    channel_range(s, C, n, n_up, &a0, &a1);
+    const float inv = 1.0f / (float)(a1 - a0);
+    auto at = [&](int a, int p) { return H2[((((size_t)w * n + a) * n + i) * P2 + p) * d2 + f]; };
+    if (t == 0) {
+      float acc = 0.f;
+      for (int a = a0; a < a1; ++a) acc += at(a, 0);
+      v = acc * inv;
+    } else if (t == 1) {
+      float acc = 0.f;
+      for (int a = a0; a < a1; ++a) acc += at(a, 1);
+      v = 2.0f * acc * inv;
+    } else {
+      int dd = t - 2, el = dd / 3, c = dd % 3;
+      float acc = 0.f;
+      if (el == i) {
+        for (int a = a0; a < a1; ++a) acc -= at(a, 2 + c);
+      } else if (el >= a0 && el < a1) {
+        acc = at(el, 2 + c);
+      }
+      v = acc * inv;
+    }
+  }
+  G2[e] = (OutT)v;
+}
+
+template <typename OutT>
+cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d2,
+                           int P2, const float* H2, int g2p, OutT* G2) {
+  size_t total = (size_t)B * n * Tp * g2p;
+  k_mean_h2<OutT><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, T, d2, P2, H2,
+                                                                  g2p, G2);
+  return cudaGetLastError();
+}
+template cudaError_t launch_mean_h2<float>(cudaStream_t, int, int, int, int, int, int, int, int,
+                                           const float*, int, float*);
+template cudaError_t launch_mean_h2<__nv_bfloat16>(cudaStream_t, int, int, int, int, int, int, int,
+                                                   int, const float*, int, __nv_bfloat16*);
+
+// =====================================================================
+// determinant stage (src/jaqmc/wavefunction/output/logdet.py:53-80,
+//                    src/jaqmc/laplacian/primitives/slogdet.py:25-72,
+//                    src/jaqmc/estimator/kinetic/_common.py:61-73)
+// One CTA per walker; each warp factorises determinants k = warp, warp+nw, ...
+// =====================================================================
+constexpr float kRefactorRatio = 1e6f;
+
+__device__ __forceinline__ float warp_sum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct DetOut {
+  double ld;
+  float sgn;
+  float tL, t2, q;
+  int refactor, singular;
+};
+
+// LU with partial pivoting of the n x n matrix in S (row stride n+1) by one
+// warp; perm[i] = source row of pivoted row i.  Returns log|det|, sign and the
+// pivot ratio max|u_kk| / min|u_kk|.
+template <typename S>
+__device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* sgn, double* ratio,
+                        int* singular) {
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < n; i += 32) perm[i] = i;
+  __syncwarp();
+  double la = 0.0, pmax = 0.0, pmin = 1e300;
+  float sg = 1.f;
+  int sing = 0;
+  for (int k = 0; k < n; ++k) {
+    S best = (S)-1;
+    int bi = k;
+    for (int i = k + lane; i < n; i += 32) {
+      S v = fabs(LU[i * ld + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      S ob = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (bi != k) {
+      for (int j = lane; j < n; j += 32) {
+        S tmp = LU[k * ld + j];
+        LU[k * ld + j] = LU[bi * ld + j];
+        LU[bi * ld + j] = tmp;
+      }
+      if (lane == 0) {
+        int tp = perm[k];
+        perm[k] = perm[bi];
+        perm[bi] = tp;
+      }
+      sg = -sg;
+    }
+    __syncwarp();
+    S piv = LU[k * ld + k];
+    double ap = fabs((double)piv);
+    if (!(ap > 0.0)) { sing = 1; la = -INFINITY; break; }
+    la += log(ap);
+    if (piv < (S)0) sg = -sg;
+    pmax = fmax(pmax, ap);
+    pmin = fmin(pmin, ap);
+    S inv = (S)1 / piv;
+    for (int i = k + 1 + lane; i < n; i += 32) LU[i * ld + k] *= inv;
+    __syncwarp();
+    for (int j = k + 1 + lane; j < n; j += 32) {
+      S ukj = LU[k * ld + j];
+      for (int i = k + 1; i < n; ++i) LU[i * ld + j] -= LU[i * ld + k] * ukj;
+    }
+    __syncwarp();
+  }
+  *logabs = la;
+  *sgn = sg;
+  *ratio = sing ? INFINITY : pmax / pmin;
+  *singular = sing;
+}
+
+// Per-warp scratch for one determinant: LU and A^-1 (row stride ld), the
+// products M_t = A^-1 A_t (row stride ldm, odd, so that transposed reads are
+// bank-conflict free) and the staged A_t for the FP64 path.
+struct DetScratch {
+  int ld, ldm;
+  size_t bytes;  // per warp, FP64 worst case
+  __host__ __device__ DetScratch(int n) {
+    ld = (n + 3) / 4 * 4;
+    ldm = (n % 2 == 0) ? n + 1 : n + 2;
+    bytes = align_up((size_t)(2 * n * ld + 2 * n * ldm) * 8 + (size_t)n * 4, 16);
+  }
+};
+
+// A^-1 column by column (lane j solves L U x = P e_j in place in column j).
+template <typename S>
+__device__ void warp_inverse(const S* LU, S* Ainv, const int* perm, int n, int ld) {
+  const int lane = threadIdx.x & 31;
+  for (int j = lane; j < ld; j += 32) {
+    if (j >= n) {  // zero padding columns
+      for (int i = 0; i < n; ++i) Ainv[i * ld + j] = (S)0;
+      continue;
+    }
+    for (int i = 0; i < n; ++i) {
+      S v = perm[i] == j ? (S)1 : (S)0;
+      for (int m = 0; m < i; ++m) v -= LU[i * ld + m] * Ainv[m * ld + j];
+      Ainv[i * ld + j] = v;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      S v = Ainv[i * ld + j];
+      for (int m = i + 1; m < n; ++m) v -= LU[i * ld + m] * Ainv[m * ld + j];
+      Ainv[i * ld + j] = v / LU[i * ld + i];
+    }
+  }
+  __syncwarp();
+}
+
+// M = A^-1 A_t into Ms; returns tr(M) (warp-reduced).  FP32: columns of A_t
+// held in registers, rows of A^-1 read as float4 broadcasts.
+template <int NMAX>
+__device__ float warp_product_f32(const float* Ainv, const float* __restrict__ At, float* Ms, int n,
+                                  int ld, int ldm) {
+  const int lane = threadIdx.x & 31;
+  float tr = 0.f;
+  for (int j = lane; j < n; j += 32) {
+    float x[NMAX];
+#pragma unroll
+    for (int m = 0; m < NMAX; ++m) x[m] = m < n ? At[m * n + j] : 0.f;
+#pragma unroll 4
+    for (int i = 0; i < n; ++i) {
+      const float4* a4 = reinterpret_cast<const float4*>(Ainv + i * ld);
+      float acc = 0.f;
+#pragma unroll
+      for (int m4 = 0; m4 < NMAX / 4; ++m4) {
+        if (4 * m4 < n) {
+          float4 a = a4[m4];
+          acc = fmaf(a.x, x[4 * m4], acc);
+          acc = fmaf(a.y, x[4 * m4 + 1], acc);
+          acc = fmaf(a.z, x[4 * m4 + 2], acc);
+          acc = fmaf(a.w, x[4 * m4 + 3], acc);
+        }
+      }
+      Ms[i * ldm + j] = acc;
+      if (i == j) tr += acc;
+    }
+  }
+  tr = warp_sum(tr);
+  __syncwarp();
+  return tr;
+}
+
+// FP64 variant (re-factorised determinants only): A_t staged in shared memory.
+__device__ double warp_product_f64(const double* Ainv, const float* __restrict__ At, double* Ms,
+                                   double* Xs, int n, int ld, int ldm) {
+  const int lane = threadIdx.x & 31;
+  for (int e = lane; e < n * n; e += 32) Xs[(e / n) * ldm + (e % n)] = (double)At[e];
+  __syncwarp();
+  double tr = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    for (int i = 0; i < n; ++i) {
+      double acc = 0.0;
+      for (int m = 0; m < n; ++m) acc += Ainv[i * ld + m] * Xs[m * ldm + j];
+      Ms[i * ldm + j] = acc;
+      if (i == j) tr += acc;
+    }
+  }
+  tr = warp_sum(tr);
+  __syncwarp();
+  return tr;
+}
+
+template <typename S>
+__device__ S warp_trace_sq(const S* Ms, int n, int ldm) {
+  const int lane = threadIdx.x & 31;
+  S t2 = (S)0;
+  for (int j = lane; j < n; j += 32)
+    for (int i = 0; i < n; ++i) t2 += Ms[i * ldm + j] * Ms[j * ldm + i];
+  t2 = warp_sum(t2);
+  __syncwarp();
+  return t2;
+}
+
+// Factorise determinant k of a walker and, for T > 1, the slogdet traces
+//   tL = tr(A^-1 L_A),  t1_d = tr(A^-1 J_d A),  t2 = sum_d tr((A^-1 J_d A)^2),
+//   q = sum_d t1_d^2.
+template <typename S, int NMAX>
+__device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* scratch,
+                            float* t1s, bool fp64_pass) {
+  const int lane = threadIdx.x & 31;
+  const DetScratch sc(n);
+  const int ld = sc.ld, ldm = sc.ldm;
+  S* LU = reinterpret_cast<S*>(scratch);
+  S* Ainv = LU + n * ld;
+  S* Ms = Ainv + n * ld;
+  S* Xs = Ms + n * ldm;
+  int* perm = reinterpret_cast<int*>(scratch + (size_t)(2 * n * ld + 2 * n * ldm) * 8);
+  const size_t ts = (size_t)n * n;
+  DetOut o{};
+  for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (S)Ak[e];
+  __syncwarp();
+  double ratio;
+  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &ratio, &o.singular);
+  o.refactor = (!fp64_pass && !(ratio <= (double)kRefactorRatio)) ? 1 : 0;
+  if (T <= 1 || o.singular || o.refactor) return o;
+  warp_inverse<S>(LU, Ainv, perm, n, ld);
+  float t2acc = 0.f, qacc = 0.f;
+  for (int t = 1; t < T; ++t) {
+    const float* At = Ak + (size_t)t * ts;
+    S tr;
+    if constexpr (sizeof(S) == 4) tr = warp_product_f32<NMAX>(Ainv, At, Ms, n, ld, ldm);
+    else tr = warp_product_f64(Ainv, At, Ms, Xs, n, ld, ldm);
+    if (t == 1) {
+      o.tL = (float)tr;
+    } else {
+      S t2 = warp_trace_sq<S>(Ms, n, ldm);
+      if (lane == 0) t1s[t - 2] = (float)tr;
+      t2acc += (float)t2;
+      qacc += (float)(tr * tr);
+    }
+  }
+  o.t2 = t2acc;
+  o.q = qacc;
+  return o;
+}
+
+template <int NMAX>
+__global__ void k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
+                         const float* __restrict__ pe, float* __restrict__ logpsi,
+                         float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
+                         uint8_t* __restrict__ flags, int* __restrict__ n_refactor) {
+  extern __shared__ double shd[];
+  const int w = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  const int D = T > 1 ? T - 2 : 0;
+  // shared layout: per-det results, then per-warp scratch
+  double* lds = shd;                                    // [K]
+  float* sgs = reinterpret_cast<float*>(lds + K);       // [K]
+  float* tLs = sgs + K;                                 // [K]
+  float* t2s = tLs + K;                                 // [K]
+  float* qs = t2s + K;                                  // [K]
+  float* t1s = qs + K;                                  // [K][D]
+  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);  // flags [2]
+  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
+  const DetScratch sc(n);
+  char* scratch = reinterpret_cast<char*>(shd) + head + sc.bytes * warp;
+  if (threadIdx.x < 2) ints[threadIdx.x] = 0;
+  __syncthreads();
+  for (int k = warp; k < K; k += nw) {
+    const float* Ak = A + ((size_t)w * K + k) * Tp * n * n;
+    float* t1k = t1s + (size_t)k * D;
+    DetOut o = det_stage<float, NMAX>(Ak, n, T, scratch, t1k, false);
+    if (o.refactor) {
+      o = det_stage<double, NMAX>(Ak, n, T, scratch, t1k, true);
+      o.refactor = 1;
+    }
+    if (lane == 0) {
+      lds[k] = o.ld;
+      sgs[k] = o.singular ? 0.f : o.sgn;
+      tLs[k] = o.tL;
+      t2s[k] = o.t2;
+      qs[k] = o.q;
+      if (o.refactor) atomicOr(&ints[0], 1);
+      if (o.singular) atomicOr(&ints[1], 1);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  // FP64 signed log-sum-exp over determinants
+  double lmax = -INFINITY;
+  for (int k = 0; k < K; ++k)
+    if (sgs[k] != 0.f) lmax = fmax(lmax, lds[k]);
+  double Ssum = 0.0;
+  for (int k = 0; k < K; ++k)
+    if (sgs[k] != 0.f) Ssum += (double)sgs[k] * exp(lds[k] - lmax);
+  double lp = log(fabs(Ssum)) + lmax;
+  float sg = Ssum > 0 ? 1.f : (Ssum < 0 ? -1.f : 0.f);
+  bool bad = !isfinite(lp);
+  if (T > 1) {
+    // grad_d = sum_k w_k t1_kd ; lap = sum_k w_k (tL - t2 + q) - |grad|^2
+    double g2 = 0.0;
+    for (int d = lane; d < D; d += 32) {
+      double g = 0.0;
+      for (int k = 0; k < K; ++k)
+        if (sgs[k] != 0.f) g += (double)sgs[k] * exp(lds[k] - lmax) / Ssum * (double)t1s[(size_t)k * D + d];
+      g2 += g * g;
+    }
+    g2 = warp_sum(g2);
+    double lap = 0.0;
+    for (int k = 0; k < K; ++k)
+      if (sgs[k] != 0.f)
+        lap += (double)sgs[k] * exp(lds[k] - lmax) / Ssum * ((double)tLs[k] - (double)t2s[k] + (double)qs[k]);
+    lap -= g2;
+    double kin = -0.5 * (lap + g2);
+    if (lane == 0) {
+      if (ke) ke[w] = (float)kin;
+      if (el) el[w] = (float)(kin + (pe ? (double)pe[w] : 0.0));
+    }
+    bad = bad || !isfinite(kin);
+  }
+  if (lane == 0) {
+    if (logpsi) logpsi[w] = (float)lp;
+    if (sign) sign[w] = sg;
+    uint8_t f = (bad ? QMC_FLAG_NONFINITE : 0) | (ints[0] ? QMC_FLAG_REFACTOR : 0) |
+                (ints[1] ? QMC_FLAG_SINGULAR : 0);
+    if (flags) flags[w] = f;
+    if (ints[0] && n_refactor) atomicAdd(n_refactor, 1);
+  }
+}
+
+cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
+                          const float* pe, float* logpsi, float* sign, float* ke, float* el,
+                          uint8_t* flags, int* n_refactor) {
+  const int D = T > 1 ? T - 2 : 0;
+  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
+  const DetScratch sc(n);
+  int nw = (int)((200 * 1024 - head) / sc.bytes);
+  nw = nw < 1 ? 1 : nw;
+  nw = nw > 8 ? 8 : nw;
+  nw = nw > K ? K : nw;
+  size_t sm = head + sc.bytes * nw;
+  if (sm > 220 * 1024) return cudaErrorInvalidValue;
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+#define QMC_LD(NM)                                                                          \
+  {                                                                                         \
+    static int set_dev = -1;                                                                \
+    if (set_dev != dev) {                                                                   \
+      e = cudaFuncSetAttribute(k_logdet<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                               220 * 1024);                                                 \
+      if (e != cudaSuccess) return e;                                                       \
+      set_dev = dev;                                                                        \
+    }                                                                                       \
+    k_logdet<NM><<<B, 32 * nw, sm, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags,    \
+                                        n_refactor);                                        \
+  }
+  if (n <= 8) QMC_LD(8)
+  else if (n <= 16) QMC_LD(16)
+  else if (n <= 32) QMC_LD(32)
+  else if (n <= 64) QMC_LD(64)
+  else return cudaErrorInvalidValue;
+#undef QMC_LD
+  return cudaGetLastError();
+}
+
+// =====================================================================
+// Metropolis-Hastings (src/jaqmc/sampler/mcmc.py:53-54, 96-137)
+// =====================================================================
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
+  float u1 = u01(a), u2 = u01(b);
+  float rad = sqrtf(-2.0f * logf(u1));
+  float sn, cs;
+  sincospif(2.0f * u2, &sn, &cs);
+  *z0 = rad * cs;
+  *z1 = rad * sn;
+}
+
+__device__ __forceinline__ U4 draw_block(uint64_t seed, uint64_t step, int w, int b) {
+  U4 c{(uint32_t)b, (uint32_t)w, (uint32_t)step, (uint32_t)(step >> 32)};
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+__global__ void k_mh_propose(int B, int n, const float* __restrict__ x, float* __restrict__ xp,
+                             float stddev, uint64_t seed, uint64_t step,
+                             const float* __restrict__ inj) {
+  const int nb = normal_blocks(n);
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * nb) return;
+  int w = (int)(e / nb), b = (int)(e % nb);
+  float z[4];
+  if (inj) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int c = 4 * b + q;
+      z[q] = c < 3 * n ? inj[(size_t)w * 3 * n + c] : 0.f;
+    }
+  } else {
+    U4 r = draw_block(seed, step, w, b);
+    box_muller(r.x, r.y, &z[0], &z[1]);
+    box_muller(r.z, r.w, &z[2], &z[3]);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int c = 4 * b + q;
+    if (c < 3 * n) {
+      size_t o = (size_t)w * 3 * n + c;
+      xp[o] = x[o] + stddev * z[q];
+    }
+  }
+}
+
+cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
+                              float stddev, uint64_t seed, uint64_t ctr, const float* inj) {
+  size_t total = (size_t)B * normal_blocks(n);
+  k_mh_propose<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, x, xp, stddev, seed, ctr, inj);
+  return cudaGetLastError();
+}
+
+__global__ void k_mh_accept(int B, int n, float* __restrict__ x, const float* __restrict__ xp,
+                            float* __restrict__ lp, const float* __restrict__ logpsi_p,
+                            uint64_t seed, uint64_t step, const float* __restrict__ inj,
+                            uint32_t* __restrict__ accepts) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= B) return;
+  float u = inj ? inj[w] : u01(draw_block(seed, step, w, normal_blocks(n)).x);
+  float lp2 = 2.0f * logpsi_p[w];
+  float ratio = lp2 - lp[w];
+  bool cond = ratio > logf(u);
+  if (cond) {
+    for (int c = 0; c < 3 * n; ++c) x[(size_t)w * 3 * n + c] = xp[(size_t)w * 3 * n + c];
+    lp[w] = lp2;
+    if (accepts) accepts[w] += 1u;
+  }
+}
+
+cudaError_t launch_mh_accept(cudaStream_t s, int B, int n, float* x, const float* xp, float* lp,
+                             const float* logpsi_p, uint64_t seed, uint64_t ctr,
+                             const float* inj_uniforms, uint32_t* accepts) {
+  k_mh_accept<<<(B + 127) / 128, 128, 0, s>>>(B, n, x, xp, lp, logpsi_p, seed, ctr, inj_uniforms,
+                                              accepts);
+  return cudaGetLastError();
+}
+
+__global__ void k_mh_draws(int B, int n, int steps, uint64_t seed, uint64_t ctr,
+                           float* __restrict__ normals, float* __restrict__ uniforms) {
+  const int nb = normal_blocks(n);
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)steps * B * (nb + 1)) return;
+  int b = (int)(e % (nb + 1));
+  size_t sw = e / (nb + 1);
+  int w = (int)(sw % B), st = (int)(sw / B);
+  U4 r = draw_block(seed, ctr + st, w, b);
+  if (b == nb) {
+    if (uniforms) uniforms[(size_t)st * B + w] = u01(r.x);
+    return;
+  }
+  if (!normals) return;
+  float z[4];
+  box_muller(r.x, r.y, &z[0], &z[1]);
+  box_muller(r.z, r.w, &z[2], &z[3]);
+  for (int q = 0; q < 4; ++q) {
+    int c = 4 * b + q;
+    if (c < 3 * n) normals[((size_t)st * B + w) * 3 * n + c] = z[q];
+  }
+}
+
+cudaError_t launch_mh_draws(cudaStream_t s, int B, int n, int steps, uint64_t seed, uint64_t ctr,
+                            float* normals, float* uniforms) {
+  size_t total = (size_t)steps * B * (normal_blocks(n) + 1);
+  k_mh_draws<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, steps, seed, ctr, normals, uniforms);
+  return cudaGetLastError();
+}
+
+__global__ void k_scale(int B, const float* __restrict__ in, float c, float* __restrict__ out) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < B) out[w] = c * in[w];
+}
+cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float* out) {
+  k_scale<<<(B + 255) / 256, 256, 0, s>>>(B, in, c, out);
+  return cudaGetLastError();
+}
+
+// =====================================================================
+// FP64 batch mean / variance (src/jaqmc/estimator/base.py:27-53)
+// =====================================================================
+__global__ void k_reduce_mean_var(int B, const float* __restrict__ x, double* __restrict__ out) {
+  __shared__ double s1[32], s2[32];
+  __shared__ int sc[32];
+  double a = 0.0, b = 0.0;
+  int c = 0;
+  for (int i = threadIdx.x; i < B; i += blockDim.x) {
+    float v = x[i];
+    if (!isnan(v)) { a += v; b += (double)v * v; ++c; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  int wp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) { s1[wp] = a; s2[wp] = b; sc[wp] = c; }
+  __syncthreads();
+  if (wp == 0) {
+    int nw = blockDim.x >> 5;
+    a = ln < nw ? s1[ln] : 0.0;
+    b = ln < nw ? s2[ln] : 0.0;
+    c = ln < nw ? sc[ln] : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if (ln == 0) {
+      double m = c ? a / c : NAN;
+      out[0] = m;
+      out[1] = c ? b / c - m * m : NAN;
+    }
+  }
+}
+
+cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out) {
+  k_reduce_mean_var<<<1, 1024, 0, s>>>(B, x, out);
+  return cudaGetLastError();
+}
+
+// =====================================================================
+// parameter preparation
+// =====================================================================
+__global__ void k_transpose_bf16(const float* __restrict__ in, int rows, int cols, int ld_in,
+                                 __nv_bfloat16* __restrict__ out, int rows_p, int cols_p) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)rows_p * cols_p) return;
+  int r = (int)(e % rows_p), c = (int)(e / rows_p);  // out[c][r]
+  float v = (r < rows && c < cols) ? in[(size_t)r * ld_in + c] : 0.f;
+  out[e] = __float2bfloat16_rn(v);
+}
+
+cudaError_t launch_transpose_bf16(cudaStream_t s, const float* in, int rows, int cols, int ld_in,
+                                  __nv_bfloat16* out, int rows_p, int cols_p) {
+  size_t total = (size_t)rows_p * cols_p;
+  k_transpose_bf16<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(in, rows, cols, ld_in, out, rows_p,
+                                                                  cols_p);
+  return cudaGetLastError();
+}
+
+}  // namespace qmc

@@ -1,0 +1,56 @@
+// Declarations of the FermiNet / MH / reduction kernels (kernels.cu).
+#pragma once
+#include "common.cuh"
+
+namespace qmc {
+
+// Features of MoleculeFeatures (input/atomic.py:46-79) with tangents.
+//  X0    [(w*n+i)*Tp + t][K0p]   one-electron rows (ae features)
+//  H2    [(w*n+i)*n + j][P2][4]  two-electron rows, compact tangents
+//  rae   [w*n+i][A], aevec [w*n+i][A][3]
+//  pe    [w] Coulomb potential (may be null)
+// P2 = 5 (value, Laplacian wrt r_i-r_j, d/d(r_i-r_j)_{x,y,z}) when T > 1, else 1.
+cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, int K0p,
+                            const float* electrons, const float* atoms, const float* charges,
+                            double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe);
+
+// Two-electron layer h2' = residual(tanh(h2 W + b)) on compact tangent rows.
+cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
+                              const float* Hin, const float* W, const float* b, float* Hout);
+
+// Spin-channel means of the one-electron rows: G1[(w*Tp+t)][s*d + f].
+template <typename InT>
+cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, int ld,
+                           const InT* X, int g1p, float* G1);
+
+// Spin-channel means of the two-electron rows expanded to full tangents:
+// G2[(w*n+i)*Tp + t][s*d2 + f].
+template <typename OutT>
+cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d2,
+                           int P2, const float* H2, int g2p, OutT* G2);
+
+// Per-walker determinant stage: LU/log|det| of the K value matrices, FP64
+// signed log-sum-exp and, when T > 1, the slogdet forward-Laplacian traces
+// combined into the kinetic energy.  A: [w][k][Tp][n][n].
+cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
+                          const float* pe, float* logpsi, float* sign, float* ke, float* el,
+                          uint8_t* flags, int* n_refactor);
+
+// MH proposal x' = x + stddev * N(0,1) for update `step` of a call.
+cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
+                              float stddev, uint64_t seed, uint64_t ctr, const float* inj_normals);
+// Accept/reject with 2 log|psi| and the draw for update `ctr`.
+cudaError_t launch_mh_accept(cudaStream_t s, int B, int n, float* x, const float* xp, float* lp,
+                             const float* logpsi_p, uint64_t seed, uint64_t ctr,
+                             const float* inj_uniforms, uint32_t* accepts);
+cudaError_t launch_mh_draws(cudaStream_t s, int B, int n, int steps, uint64_t seed, uint64_t ctr,
+                            float* normals, float* uniforms);
+cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float* out);
+
+cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out);
+
+// fp32 [rows][cols] -> bf16 transposed [cols_p][rows_p] (zero padded)
+cudaError_t launch_transpose_bf16(cudaStream_t s, const float* in, int rows, int cols, int ld_in,
+                                  __nv_bfloat16* out, int rows_p, int cols_p);
+
+}  // namespace qmc

@@ -1,0 +1,171 @@
+"""Wavefunction hyper-parameters, parameter trees and the flat device layout.
+
+Parameter trees mirror the Flax trees of the reference so that a reference
+checkpoint's ``params`` can be loaded leaf by leaf:
+
+* FermiNet — ``src/jaqmc/app/molecule/wavefunction/ferminet.py:44-76``:
+  ``backbone_layer/Dense_k`` (single and two-electron Dense layers in creation
+  order, ``src/jaqmc/wavefunction/backbone/ferminet.py:37-63``),
+  ``orbital_layer/SplitChannelDense_0/DenseGeneral_s`` or
+  ``orbital_layer/DenseGeneral_0`` (``src/jaqmc/wavefunction/output/orbital.py:60-78``),
+  ``envelope_layer/_env_up|_env_down|_env`` with ``pi`` and ``sigma``
+  (``src/jaqmc/wavefunction/output/envelope.py:65-95,123-140``).
+
+Initialisation is fan-in scaled ``N(0, 1/fan_in)`` for kernels, zero biases,
+and ones for the envelope ``pi`` / ``sigma`` (their reference initialisers).
+
+``flatten`` orders the leaves for the C ABI (``include/qmc.h``): per layer the
+single-stream kernel and bias, then the two-electron kernel and bias when that
+layer updates the two-electron stream; then the orbital kernels (and biases)
+per spin channel; then ``pi`` and ``sigma`` per envelope channel.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class FermiNetConfig:
+    """Hyper-parameters of ``FermiNetWavefunction`` (same names and defaults)."""
+
+    nspins: tuple = (1, 1)
+    ndets: int = 16
+    hidden_dims_single: list = field(default_factory=lambda: [256] * 4)
+    hidden_dims_double: list = field(default_factory=lambda: [32] * 4)
+    use_last_layer: bool = False
+    envelope: str = "abs_isotropic"
+    orbitals_spin_split: bool = True
+    full_det: bool = True
+
+    @property
+    def n(self) -> int:
+        return int(sum(self.nspins))
+
+    @property
+    def channels(self) -> int:
+        """Number of non-empty spin channels (aggregation width multiplier)."""
+        return int(sum(1 for s in self.nspins if s > 0))
+
+    @property
+    def split(self) -> bool:
+        """Whether orbitals/envelopes are per spin channel."""
+        return bool(self.orbitals_spin_split and self.nspins[0] > 0 and self.nspins[1] > 0)
+
+    def layer_dims(self, n_atoms: int):
+        """``[(d1_in, d2_in, d1_out, d2_out, updates_two_electron)]`` per layer."""
+        out = []
+        d1, d2 = 4 * n_atoms, 4
+        L = len(self.hidden_dims_single)
+        for l, (s, dd) in enumerate(zip(self.hidden_dims_single, self.hidden_dims_double)):
+            upd = l < L - 1 or self.use_last_layer
+            out.append((d1, d2, s, dd, upd))
+            d1 = s
+            if upd:
+                d2 = dd
+        return out
+
+
+def _dense(rng, fan_in, fan_out, bias=True):
+    d = {"kernel": (rng.standard_normal((fan_in, fan_out)) / np.sqrt(fan_in)).astype(np.float32)}
+    if bias:
+        d["bias"] = np.zeros((fan_out,), np.float32)
+    return d
+
+
+def init_ferminet(cfg: FermiNetConfig, n_atoms: int, seed: int = 0):
+    """A Flax-shaped parameter tree (numpy float32) for ``cfg``."""
+    rng = np.random.default_rng(seed)
+    n, K, C = cfg.n, cfg.ndets, cfg.channels
+    bb, k = {}, 0
+    for (d1, d2, s, dd, upd) in cfg.layer_dims(n_atoms):
+        bb[f"Dense_{k}"] = _dense(rng, d1 + C * d1 + C * d2, s)
+        k += 1
+        if upd:
+            bb[f"Dense_{k}"] = _dense(rng, d2, dd)
+            k += 1
+    d_last = cfg.hidden_dims_single[-1]
+    if cfg.use_last_layer:
+        d_last = d_last + C * d_last + C * cfg.hidden_dims_double[-1]
+
+    def dg():
+        return {"kernel": (rng.standard_normal((d_last, K, n)) / np.sqrt(d_last)).astype(np.float32)}
+
+    if cfg.split:
+        orb = {"SplitChannelDense_0": {"DenseGeneral_0": dg(), "DenseGeneral_1": dg()}}
+    else:
+        orb = {"DenseGeneral_0": dg()}
+
+    def env():
+        return {"pi": np.ones((n, n_atoms, K), np.float32), "sigma": np.ones((n, n_atoms, K), np.float32)}
+
+    envl = {"_env_up": env(), "_env_down": env()} if cfg.split else {"_env": env()}
+    return {"params": {"backbone_layer": bb, "orbital_layer": orb, "envelope_layer": envl}}
+
+
+def ferminet_leaves(cfg: FermiNetConfig, n_atoms: int):
+    """``[(path, shape)]`` in C-ABI order."""
+    n, K, C = cfg.n, cfg.ndets, cfg.channels
+    out, k = [], 0
+    for (d1, d2, s, dd, upd) in cfg.layer_dims(n_atoms):
+        out.append((("backbone_layer", f"Dense_{k}", "kernel"), (d1 + C * d1 + C * d2, s)))
+        out.append((("backbone_layer", f"Dense_{k}", "bias"), (s,)))
+        k += 1
+        if upd:
+            out.append((("backbone_layer", f"Dense_{k}", "kernel"), (d2, dd)))
+            out.append((("backbone_layer", f"Dense_{k}", "bias"), (dd,)))
+            k += 1
+    if cfg.use_last_layer:
+        raise NotImplementedError("use_last_layer=True is not supported by the GPU path")
+    d_last = cfg.hidden_dims_single[-1]
+    if cfg.split:
+        for s in range(2):
+            out.append((("orbital_layer", "SplitChannelDense_0", f"DenseGeneral_{s}", "kernel"), (d_last, K, n)))
+    else:
+        out.append((("orbital_layer", "DenseGeneral_0", "kernel"), (d_last, K, n)))
+    names = ["_env_up", "_env_down"] if cfg.split else ["_env"]
+    for nm in names:
+        out.append((("envelope_layer", nm, "pi"), (n, n_atoms, K)))
+        out.append((("envelope_layer", nm, "sigma"), (n, n_atoms, K)))
+    return out
+
+
+def _get(tree, path):
+    t = tree["params"]
+    for p in path:
+        t = t[p]
+    return t
+
+
+def _set(tree, path, value):
+    t = tree.setdefault("params", {})
+    for p in path[:-1]:
+        t = t.setdefault(p, {})
+    t[path[-1]] = value
+
+
+def flatten(tree, leaves) -> np.ndarray:
+    parts = []
+    for path, shape in leaves:
+        a = np.asarray(_get(tree, path), dtype=np.float32)
+        if tuple(a.shape) != tuple(shape):
+            raise ValueError(f"{'/'.join(path)}: expected shape {shape}, got {a.shape}")
+        parts.append(a.reshape(-1))
+    return np.concatenate(parts) if parts else np.zeros((0,), np.float32)
+
+
+def unflatten(flat, leaves):
+    tree, off = {}, 0
+    flat = np.asarray(flat)
+    for path, shape in leaves:
+        size = int(np.prod(shape))
+        _set(tree, path, flat[off:off + size].reshape(shape).copy())
+        off += size
+    if off != flat.size:
+        raise ValueError(f"flat parameter vector has {flat.size} entries, layout needs {off}")
+    return tree
+
+
+def count(leaves) -> int:
+    return int(sum(int(np.prod(s)) for _, s in leaves))
