@@ -1,0 +1,400 @@
+"""Benchmark of the VMC inner loop: walker-steps/s of (S MH steps + E_L).
+
+One "step" is one request on a batch of walkers: ``S`` all-electron MH
+updates followed by the forward-Laplacian local energy and its FP64 batch
+mean/variance.  Default workload: FermiNet 4x(256, 32), K=16 on N2 (7+7
+electrons), 4096 walkers, S=20 (the configuration the metric is quoted on).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(walkers are independent; no data-path collective) and rank 0 prints one
+JSON line with the whole-job throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker-steps/s (MH+E_L) mixed vs plain FP32 at |ΔĒ|≤0.5 mHa; serve p50/p99 ms"
+UNIT = "walker-steps/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+WORKLOADS = {
+    "N2": dict(system="N2", nspins=(7, 7), walkers=4096, mh_steps=20),
+    "Li": dict(system="Li", nspins=(2, 1), walkers=1024, mh_steps=10),
+    "CH4": dict(system="CH4", nspins=(5, 5), walkers=4096, mh_steps=20),
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        load = [s for s in sm if mx and s >= 0.3 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(
+        os.environ.get("LOCAL_RANK", 0))
+
+
+def stream_layer_flops(cfg, n_atoms, B, T):
+    """Algorithmic FLOPs of one launch set of the one-electron layer GEMMs for
+    T tangent rows per electron: 2 * rows * (d_in + C*d2_in) * d_out summed over
+    layers (the spin-mean term is a separate, per-walker GEMM)."""
+    from jaqmc_gb300 import params as P
+    C = cfg.channels
+    tot = 0
+    for (d1, d2, s, dd, upd) in P.FermiNetConfig.layer_dims(cfg, n_atoms):
+        tot += 2 * B * cfg.n * T * (d1 + C * d2) * s
+    return tot
+
+
+# ----------------------------------------------------------------- CPU side
+def cpu_request_rate(wl, seconds=12.0, sample_walkers=64, threads=None):
+    """The oracle (torch FP32 on the host cores) running the same request on a
+    bounded sample of walkers; returns (walker-steps/s, cores, description)."""
+    import torch
+
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+    from oracle import ferminet as OF
+    from oracle import hamiltonian as OH
+    threads = threads or os.cpu_count()
+    torch.set_num_threads(threads)
+    mol = S.SYSTEMS[wl["system"]]()
+    cfg = P.FermiNetConfig(nspins=mol.nspins)
+    tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+    oc = OF.FermiNetConfig(nspins=cfg.nspins, ndets=cfg.ndets)
+    f = OF.logpsi_fn(tree, oc, mol.atoms, dtype=torch.float32)
+    x = torch.as_tensor(S.init_walkers(mol, sample_walkers, seed=1))
+    g = torch.Generator().manual_seed(2)
+    S_ = wl["mh_steps"]
+    reqs, t0 = 0, time.perf_counter()
+    with torch.no_grad():
+        while True:
+            lp = 2 * f(x)
+            for _ in range(S_):
+                x2 = x + 0.02 * torch.randn(x.shape, generator=g)
+                lp2 = 2 * f(x2)
+                acc = (lp2 - lp) > torch.log(torch.rand(lp.shape, generator=g))
+                x = torch.where(acc[:, None, None], x2, x)
+                lp = torch.where(acc, lp2, lp)
+            out = OF.evaluate(tree, oc, x, mol.atoms, dtype=torch.float32, tangents=True)
+            el = OH.kinetic_from_tangents(out["grad"], out["lap"]) + OH.potential_energy(x, mol.atoms, mol.charges)
+            float(el.double().mean())
+            reqs += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
+    dt = time.perf_counter() - t0
+    rate = reqs * sample_walkers * S_ / dt
+    desc = (f"oracle (torch fp32, {threads} threads) on {sample_walkers} of {wl['walkers']} walkers, "
+            f"{reqs} requests of {S_} MH steps + E_L in {dt:.1f} s")
+    return rate, threads, desc
+
+
+def run_reference(args, wl):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    rates = []
+    for _ in range(args.warmup):
+        cpu_request_rate(wl, seconds=1.0, sample_walkers=16)
+    for _ in range(args.steps):
+        r, cores, desc = cpu_request_rate(wl, seconds=4.0, sample_walkers=32)
+        rates.append(r)
+    v = float(np.mean(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": workload_name(wl, "fp32"), **wl},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference (JAX/Flax) is not installable offline; its CPU path is timed as the "
+                    "oracle restatement"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_name(wl, prec):
+    return (f"{wl['system']} FermiNet 4x(256,32) K=16, {wl['walkers']} walkers, "
+            f"{wl['mh_steps']} MH steps + forward-Laplacian E_L, {prec}")
+
+
+# ----------------------------------------------------------------- GPU side
+def run_ours(args, wl):
+    import torch
+    import torch.distributed as dist
+
+    from jaqmc_gb300 import _native
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    mol = S.SYSTEMS[wl["system"]]()
+    cfg = P.FermiNetConfig(nspins=mol.nspins)
+    tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+    flat = torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms)), device=dev)
+    B, S_ = wl["walkers"], wl["mh_steps"]
+    x0 = torch.as_tensor(S.init_walkers(mol, B, seed=1 + rank), device=dev)
+    models = {}
+    for prec in ("fp32", "mixed"):
+        m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision=prec, device=dev)
+        m.set_params(flat)
+        models[prec] = m
+    stream = torch.cuda.current_stream()
+
+    def request(m, x, counter):
+        m.mh_steps(x, S_, 0.02, 2 + rank, counter)
+        out = m.local_energy(x)
+        return _native.reduce_mean_var(out["e_local"])
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(m, x, K, counter0):
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(K):
+            mv = request(m, x, counter0 + k * S_)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t)
+        return ms, mv
+
+    # burn-in: sample the walkers from |psi|^2 first (the reference's
+    # SamplingWorkStage burn-in), so energies are those of a running VMC
+    models["fp32"].mh_steps(x0, args.burn_in, 0.15, 1000 + rank, 0)
+    torch.cuda.synchronize()
+    prec_main = args.precision
+    results = {}
+    xs = {p: x0.clone() for p in models}
+    counter = 0
+    for p, m in models.items():
+        for _ in range(args.warmup):
+            request(m, xs[p], counter)
+            counter += S_
+    clocks = ClockSampler(local)
+    clocks.start()
+    for p in (prec_main,) + tuple(q for q in models if q != prec_main):
+        ms, mv = timed(models[p], xs[p], args.steps, counter)
+        counter += args.steps * S_
+        results[p] = {"ms_per_step": ms / args.steps, "mean_var": mv.cpu().numpy().tolist()}
+    clk = clocks.stop()
+
+    # energy agreement of the two forms on identical walkers (same positions)
+    xe = x0.clone()
+    e_plain = models["fp32"].local_energy(xe)["e_local"].double()
+    e_mixed = models["mixed"].local_energy(xe)["e_local"].double()
+    d_mean = float((e_mixed.mean() - e_plain.mean()).abs())
+    d_oracle = None
+    if rank == 0 and not args.no_cpu:
+        import torch as _t
+
+        from oracle import ferminet as OF
+        from oracle import hamiltonian as OH
+        sub = xe[:args.oracle_walkers].double().cpu()
+        oc = OF.FermiNetConfig(nspins=cfg.nspins, ndets=cfg.ndets)
+        ref = OF.evaluate(tree, oc, sub, mol.atoms, dtype=_t.float64, tangents=True)
+        el64 = OH.kinetic_from_tangents(ref["grad"], ref["lap"]) + OH.potential_energy(sub, mol.atoms, mol.charges)
+        nsub = sub.shape[0]
+        d_oracle = {p: float(models[p].local_energy(xe[:nsub].contiguous())["e_local"].double().mean().cpu()
+                             - el64.mean()) for p in models}
+        d_oracle["walkers"] = nsub
+
+    # live per-kernel timing of the same request (second pass, profiler on)
+    _native.profile_enable(True)
+    _native.profile_read()
+    barrier()
+    for k in range(args.steps):
+        request(models[prec_main], xs[prec_main], counter + k * S_)
+    barrier()
+    prof = _native.profile_read()
+    _native.profile_enable(False)
+    launches = sum(v[0] for v in prof.values())
+
+    # end to end through the public API with host buffers
+    host_x = x0.cpu().pin_memory()
+    host_out = torch.empty(2, dtype=torch.float64).pin_memory()
+    m = models[prec_main]
+    xd = torch.empty_like(x0)
+    barrier()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        xd.copy_(host_x, non_blocking=True)
+        mv = request(m, xd, counter + k * S_)
+        host_out.copy_(mv, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t)
+
+    ms_main = results[prec_main]["ms_per_step"]
+    value = world * B * S_ / (ms_main / 1e3)
+    value_e2e = world * B * S_ / (e2e_ms / 1e3)
+    pk, pk_kind = peaks()
+    # roofline of the dominant kernel class
+    dom = max(prof, key=lambda k: prof[k][1])
+    rl = None
+    if dom == "stream_layer":
+        T_fl = 3 * mol.n_electrons + 2
+        flops_req = (S_ + 1) * stream_layer_flops(cfg, mol.n_atoms, B, 1) + stream_layer_flops(
+            cfg, mol.n_atoms, B, T_fl)
+        launches_dom, ms_dom = prof[dom]
+        achieved = flops_req * args.steps / (ms_dom / 1e3) / 1e12
+        if prec_main == "mixed":
+            peak, unit, bound = pk["bf16_tflops_sustained"], "TFLOP/s", "tensor"
+            pname = f"bf16 dense sustained ({pk_kind})"
+        else:
+            peak, unit, bound = FP32_SIMT_PEAK, "TFLOP/s", "fp32-simt"
+            pname = "FP32 SIMT nominal (152 SM x 128 FMA x 2 x 2.07 GHz)"
+        rl = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "peak_source": pname,
+              "unit": unit, "frac": achieved / peak, "traffic": TRAFFIC.get((wl["system"], prec_main)),
+              "launches_per_step": launches_dom / args.steps, "ms_per_step": ms_dom / args.steps}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r, cores, desc = cpu_request_rate(wl)
+        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_main, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3/fp32-acc" if prec_main == "mixed" else "fp32",
+            "data": "synthetic (seeded walkers N(0,1) around nuclei; fan-in-scaled N(0,1/fan_in) params)",
+            "config": {"workload": workload_name(wl, prec_main), **wl, "precision": prec_main,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "working set larger than L2 (local-energy workspace several GB)"},
+            "forms": {p: {"ms_per_step": r_["ms_per_step"],
+                          "walker_steps_per_s": world * B * S_ / (r_["ms_per_step"] / 1e3),
+                          "E_mean_var": r_["mean_var"]} for p, r_ in results.items()},
+            "mixed_over_plain": results["fp32"]["ms_per_step"] / results["mixed"]["ms_per_step"],
+            "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
+            "dE_mean_vs_fp64_oracle_Ha": d_oracle,
+            "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": int(B * mol.n_electrons * 3 * 4),
+                    "d2h_bytes_per_step": 16},
+            "gpu_launches": launches,
+            "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items()},
+            "roofline": rl,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12
+# dram__bytes_read.sum + dram__bytes_write.sum per request of the dominant
+# kernel class from the committed ncu summaries (None until captured)
+TRAFFIC: dict = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="N2", choices=list(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"])
+    ap.add_argument("--burn-in", type=int, default=200)
+    ap.add_argument("--oracle-walkers", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -137,6 +137,31 @@ qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
  * NaNs skipped (src/jaqmc/estimator/base.py:27-53).  mean_var: 2 doubles. */
 qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t stream);
 
+/* Reads and clears the model's device error word (synchronises the device).
+ * Returns QMC_ERR_TIMEOUT with *code != 0 when a bounded wait inside a
+ * tensor-core kernel expired since the last check. */
+qmc_status qmc_model_check_error(qmc_model* m, int* code);
+
+/* Built-in launch profiler.  While enabled, every kernel the library launches
+ * is counted per class and bracketed by CUDA events on its stream (stream
+ * capture must not be active).  qmc_profile_read synchronises on the recorded
+ * events and returns, per class, the number of launches and their summed
+ * device time in ms, then clears the record.  Classes: QMC_KC_*. */
+enum {
+  QMC_KC_STREAM_LAYER = 0, /* one-electron layer GEMM + tangent epilogue  */
+  QMC_KC_BROADCAST = 1,    /* spin-mean broadcast GEMM                    */
+  QMC_KC_ORBITAL = 2,      /* orbital GEMM x envelope                     */
+  QMC_KC_LOGDET = 3,       /* LU / log-sum-exp / slogdet traces           */
+  QMC_KC_FEATURES = 4,     /* input features + potential                  */
+  QMC_KC_MEANS = 5,        /* spin means of both streams                  */
+  QMC_KC_PAIR = 6,         /* two-electron layers                         */
+  QMC_KC_MH = 7,           /* proposal / accept                           */
+  QMC_KC_OTHER = 8,
+  QMC_KC_COUNT = 9
+};
+qmc_status qmc_profile_enable(int on);
+qmc_status qmc_profile_read(int n_classes, int64_t* launches, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

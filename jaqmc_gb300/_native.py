@@ -63,6 +63,9 @@ _SIGS = {
     "qmc_mh_draws": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p,
                                C.c_void_p, C.c_void_p]),
     "qmc_reduce_mean_var": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qmc_model_check_error": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "qmc_profile_enable": (C.c_int, [C.c_int]),
+    "qmc_profile_read": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -191,6 +194,12 @@ class NativeFermiNet:
         check(self.lib.qmc_model_set_params(self.h, ptr(flat), stream_handle(stream)))
         self._params = flat  # keep alive until the copy has run
 
+    def check_error(self) -> int:
+        """Device error word of the bounded waits (0 = none); raises on error."""
+        code = C.c_int(0)
+        check(self.lib.qmc_model_check_error(self.h, C.byref(code)))
+        return code.value
+
     def workspace(self, op: int, batch: int):
         nb = int(self.lib.qmc_workspace_size(self.h, op, batch))
         return self.ws.get(nb), nb
@@ -245,6 +254,23 @@ class NativeFermiNet:
         check(self.lib.qmc_mh_draws(self.h, int(batch), int(steps), int(seed), int(counter), ptr(nz),
                                     ptr(uz), stream_handle(stream)))
         return nz, uz
+
+
+KERNEL_CLASSES = ["stream_layer", "broadcast", "orbital", "logdet", "features", "means", "pair", "mh",
+                  "other"]
+
+
+def profile_enable(on: bool = True):
+    check(load().qmc_profile_enable(int(bool(on))))
+
+
+def profile_read():
+    """``{class: (launches, ms)}`` since the last read (synchronises)."""
+    n = len(KERNEL_CLASSES)
+    launches = (C.c_int64 * n)()
+    ms = (C.c_double * n)()
+    check(load().qmc_profile_read(n, launches, ms))
+    return {k: (int(launches[i]), float(ms[i])) for i, k in enumerate(KERNEL_CLASSES)}
 
 
 def reduce_mean_var(x: torch.Tensor, stream=None):

@@ -9,7 +9,20 @@
 #include "common.cuh"
 #include "gemm_simt.cuh"
 #include "kernels.cuh"
+#include "profile.cuh"
 #include "stream_tc.cuh"
+
+// Launch `call` as a kernel of profiler class `cls` on stream `s`.
+#define QMC_PROF(cls, call)               \
+  do {                                    \
+    ::qmc::ProfScope ps_((cls), s);       \
+    QMC_CUDA(call);                       \
+  } while (0)
+#define QMC_PROF_TRY(cls, call)           \
+  do {                                    \
+    ::qmc::ProfScope ps_((cls), s);       \
+    QMC_TRY(call);                        \
+  } while (0)
 
 namespace qmc {
 
@@ -137,11 +150,11 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
   a->total = o;
   size_t b = 0;
   auto takeb = [&](size_t n) { size_t r = b; b += align_up(n, 128); return r; };
-  for (int l = 0; l < d.L; ++l) {
-    a->t_main[l] = takeb((size_t)d.d1[l] * (d.d1_in_p[l] + d.g2_p[l]));
-    a->t_g1[l] = takeb((size_t)d.d1[l] * d.g1_p[l]);
+  for (int l = 0; l < d.L; ++l) {  // hi and lo planes of the transposed weights
+    a->t_main[l] = takeb(2 * (size_t)d.d1[l] * (d.d1_in_p[l] + d.g2_p[l]));
+    a->t_g1[l] = takeb(2 * (size_t)d.d1[l] * d.g1_p[l]);
   }
-  for (int s = 0; s < nch; ++s) a->t_orb[s] = takeb((size_t)round_up(d.norb, 128) * d.d_last);
+  for (int s = 0; s < nch; ++s) a->t_orb[s] = takeb(2 * (size_t)d.norb * d.d_last);
   a->total_bf16 = b;
 }
 
@@ -150,7 +163,9 @@ struct Plan {
   int B, T, Tp, P2, K0p;
   bool mixed;
   size_t x0, h1[2], h2[2], g1, gb, g2, rae, aevec, amat, pe, lpsi, sgn, xp, lp, refac, total;
-  size_t act_bytes;  // element size of one-electron activations
+  size_t act_bytes;  // bytes per one-electron activation (fp32, or two bf16 planes)
+  size_t h1_plane, g1_plane, g2_plane;  // bf16 elements between split planes
+  int dmax, g1max, g2max;
 };
 
 static int tangent_count(const Dims& d, int op) { return op == QMC_OP_LOCAL_ENERGY ? 3 * d.n + 2 : 1; }
@@ -171,7 +186,7 @@ static Plan make_plan(const qmc_model* m, int op, int B) {
   p.Tp = padded_tangents(d, p.T, p.mixed);
   p.P2 = p.T > 1 ? 5 : 1;
   p.K0p = d.d1_in_p[0];
-  p.act_bytes = p.mixed ? 2 : 4;
+  p.act_bytes = 4;
   const size_t rows = (size_t)B * d.n * p.Tp;
   int dmax = 8, g1max = 8, g2max = 8, d2max = 4;
   for (int l = 0; l < d.L; ++l) {
@@ -180,6 +195,12 @@ static Plan make_plan(const qmc_model* m, int op, int B) {
     g2max = std::max(g2max, d.g2_p[l]);
     d2max = std::max(d2max, d.d2[l]);
   }
+  p.dmax = dmax;
+  p.g1max = g1max;
+  p.g2max = g2max;
+  p.h1_plane = rows * dmax;
+  p.g1_plane = (size_t)B * p.Tp * g1max;
+  p.g2_plane = rows * g2max;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes, 256); return r; };
   p.x0 = take(rows * p.K0p * 4);
@@ -208,70 +229,37 @@ template <typename T>
 static T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
 
 // ------------------------------------------------------------ network
-// One-electron layer l: spin means, broadcast GEMM, main GEMM with the
-// tangent epilogue; then the two-electron update.
-template <typename ActT>
-static qmc_status run_backbone(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
+// Plain FP32 form.  One-electron layer l: spin means, broadcast GEMM, main
+// GEMM with the tangent epilogue; then the two-electron update.
+static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
   const Dims& d = m->d;
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
   const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
   const RowMap rows_map{n, 0, n, Tp};
   const RowMap wt_map{1, 0, 1, Tp};
-  const int ngroups = B * n;
   int cur = 0, h2cur = 0;
   for (int l = 0; l < d.L; ++l) {
     const int din = d.d1_in[l], dinp = d.d1_in_p[l], dout = d.d1[l];
-    ActT* out = at<ActT>(ws, p.h1[l == 0 ? 0 : cur ^ 1]);
+    const float* in = l == 0 ? at<float>(ws, p.x0) : at<float>(ws, p.h1[cur]);
+    float* out = at<float>(ws, p.h1[l == 0 ? 0 : cur ^ 1]);
     float* G1 = at<float>(ws, p.g1);
     float* Gb = at<float>(ws, p.gb);
+    float* G2 = at<float>(ws, p.g2);
     const float* H2 = at<float>(ws, p.h2[h2cur]);
-    // spin means of the one-electron input
-    if (l == 0) {
-      QMC_CUDA(launch_mean_h1<float>(s, B, n, d.n_up, d.C, Tp, din, dinp, at<float>(ws, p.x0),
-                                     d.g1_p[l], G1));
-    } else {
-      QMC_CUDA(launch_mean_h1<ActT>(s, B, n, d.n_up, d.C, Tp, din, dinp, at<ActT>(ws, p.h1[cur]),
-                                    d.g1_p[l], G1));
-    }
-    // broadcast term G = means @ W_g1, rows (walker, tangent)
-    QMC_CUDA(launch_gemm_simt<float>(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], (const float*)nullptr,
-                                     0, 0, ar + a.w_g1[l], dout, dout,
-                                     EpiStore{Gb, dout, nullptr}));
-    const bool use_tc = p.mixed && l > 0 && tc_layer_supported(dinp, d.g2_p[l], dout);
-    if (l == 0 || !p.mixed) {
-      float* G2 = at<float>(ws, p.g2);
-      QMC_CUDA(launch_mean_h2<float>(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l], G2));
-      EpiLayer<ActT> epi{Gb, ar + a.b1[l], nullptr, out, dout, T};
-      if (l == 0) {
-        QMC_CUDA(launch_gemm_simt<float>(s, ngroups, rows_map, at<float>(ws, p.x0), p.K0p, dinp, G2,
-                                         d.g2_p[l], d.g2_p[l], ar + a.w_main[l], dout, dout, epi));
-      } else {
-        // plain form (ActT == float here)
-        const ActT* in = at<ActT>(ws, p.h1[cur]);
-        if (din == dout) epi.resid = in;
-        QMC_CUDA(launch_gemm_simt<ActT>(s, ngroups, rows_map, in, dinp, dinp,
-                                        reinterpret_cast<const ActT*>(G2), d.g2_p[l], d.g2_p[l],
-                                        ar + a.w_main[l], dout, dout, epi));
-      }
-    } else {
-      ActT* G2 = at<ActT>(ws, p.g2);
-      QMC_CUDA(launch_mean_h2<ActT>(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l], G2));
-      const ActT* in = at<ActT>(ws, p.h1[cur]);
-      EpiLayer<ActT> epi{Gb, ar + a.b1[l], din == dout ? in : nullptr, out, dout, T};
-      if (use_tc) {
-        QMC_TRY(tc_stream_layer(s, ngroups, n, Tp, T, reinterpret_cast<const __nv_bfloat16*>(in), dinp,
-                                reinterpret_cast<const __nv_bfloat16*>(G2), d.g2_p[l],
-                                m->arena_bf16 + a.t_main[l], dout, Gb, ar + a.b1[l],
-                                din == dout, reinterpret_cast<__nv_bfloat16*>(out)));
-      } else {
-        QMC_CUDA(launch_gemm_simt<ActT>(s, ngroups, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
-                                        ar + a.w_main[l], dout, dout, epi));
-      }
-    }
+    QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StF32{const_cast<float*>(in), dinp},
+                                          d.g1_p[l], StF32{G1, d.g1_p[l]}));
+    QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
+                                                ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
+    QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                          StF32{G2, d.g2_p[l]}));
+    EpiLayer<StF32> epi{Gb, ar + a.b1[l], StF32{nullptr, dout}, StF32{out, dout}, T};
+    if (l > 0 && din == dout) epi.resid = StF32{const_cast<float*>(in), dout};
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
+                                                   ar + a.w_main[l], dout, dout, epi));
     if (d.upd2[l]) {
-      QMC_CUDA(launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l], ar + a.b2[l],
-                                 at<float>(ws, p.h2[h2cur ^ 1])));
+      QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                              ar + a.b2[l], at<float>(ws, p.h2[h2cur ^ 1])));
       h2cur ^= 1;
     }
     cur = (l == 0) ? 0 : cur ^ 1;
@@ -280,21 +268,121 @@ static qmc_status run_backbone(qmc_model* m, const Plan& p, void* ws, cudaStream
   return QMC_OK;
 }
 
-template <typename ActT>
+// Mixed form: the first layer (4A-wide input) in FP32; every later layer,
+// its broadcast term and the orbitals as split-BF16 tcgen05 GEMMs.
+static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
+  const Dims& d = m->d;
+  const float* ar = m->arena;
+  const ArenaLayout& a = m->a;
+  const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
+  const RowMap rows_map{n, 0, n, Tp};
+  const RowMap wt_map{1, 0, 1, Tp};
+  typedef __nv_bfloat16 bf;
+  int cur = 0, h2cur = 0;
+  for (int l = 0; l < d.L; ++l) {
+    const int din = d.d1_in[l], dinp = d.d1_in_p[l], dout = d.d1[l];
+    bf* out = at<bf>(ws, p.h1[l == 0 ? 0 : cur ^ 1]);
+    float* Gb = at<float>(ws, p.gb);
+    const float* H2 = at<float>(ws, p.h2[h2cur]);
+    if (l == 0) {
+      float* X0 = at<float>(ws, p.x0);
+      float* G1 = at<float>(ws, p.g1);
+      float* G2 = at<float>(ws, p.g2);
+      QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StF32{X0, dinp}, d.g1_p[l],
+                                            StF32{G1, d.g1_p[l]}));
+      QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
+                                                  ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
+      QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                            StF32{G2, d.g2_p[l]}));
+      EpiLayer<StSplit> epi{Gb, ar + a.b1[l], StSplit{nullptr, dout, 0}, StSplit{out, dout, p.h1_plane}, T};
+      QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, X0, dinp, dinp, G2, d.g2_p[l],
+                                                     d.g2_p[l], ar + a.w_main[l], dout, dout, epi));
+    } else {
+      bf* in = at<bf>(ws, p.h1[cur]);
+      bf* G1 = at<bf>(ws, p.g1);
+      bf* G2 = at<bf>(ws, p.g2);
+      const int kmain = dinp + d.g2_p[l];
+      QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StSplit{in, dinp, p.h1_plane},
+                                            d.g1_p[l], StSplit{G1, d.g1_p[l], p.g1_plane}));
+      TcStoreArgs sa{B * Tp, G1, d.g1_p[l], p.g1_plane, m->arena_bf16 + a.t_g1[l], dout, Gb, m->dev_err};
+      QMC_PROF_TRY(QMC_KC_BROADCAST, tc_store_gemm(s, sa));
+      QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                            StSplit{G2, d.g2_p[l], p.g2_plane}));
+      TcLayerArgs la{};
+      la.n_groups = B * n;
+      la.n = n;
+      la.Tp = Tp;
+      la.T = T;
+      la.X = in;
+      la.k1 = dinp;
+      la.x_plane = p.h1_plane;
+      la.G2 = G2;
+      la.k2 = d.g2_p[l];
+      la.g2_plane = p.g2_plane;
+      la.Wt = m->arena_bf16 + a.t_main[l];
+      la.n_out = dout;
+      la.Gb = Gb;
+      la.bias = ar + a.b1[l];
+      la.residual = din == dout;
+      la.out = out;
+      la.out_plane = p.h1_plane;
+      la.err = m->dev_err;
+      (void)kmain;
+      QMC_PROF_TRY(QMC_KC_STREAM_LAYER, tc_stream_layer(s, la));
+    }
+    if (d.upd2[l]) {
+      QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                              ar + a.b2[l], at<float>(ws, p.h2[h2cur ^ 1])));
+      h2cur ^= 1;
+    }
+    cur = (l == 0) ? 0 : cur ^ 1;
+  }
+  *out_buf = cur;
+  return QMC_OK;
+}
+
 static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
   const Dims& d = m->d;
   const ArenaLayout& a = m->a;
   const float* ar = m->arena;
-  const ActT* h = at<ActT>(ws, p.h1[hb]);
   int nch = d.split ? 2 : 1;
+  if (p.mixed) {
+    TcOrbitalArgs oa{};
+    oa.B = p.B;
+    oa.n = d.n;
+    oa.n_up = d.n_up;
+    oa.split = d.split;
+    oa.Tp = p.Tp;
+    oa.T = p.T;
+    oa.K = d.K;
+    oa.natom = d.A;
+    oa.env_abs = d.env_abs;
+    oa.X = at<__nv_bfloat16>(ws, p.h1[hb]);
+    oa.k = d.d_last;
+    oa.x_plane = p.h1_plane;
+    for (int c = 0; c < 2; ++c) {
+      int cc = c < nch ? c : 0;
+      oa.Wt[c] = m->arena_bf16 + a.t_orb[cc];
+      oa.pi[c] = ar + a.env_pi[cc];
+      oa.sigma[c] = ar + a.env_sigma[cc];
+    }
+    oa.norb = d.norb;
+    oa.rae = at<float>(ws, p.rae);
+    oa.aevec = at<float>(ws, p.aevec);
+    oa.A = at<float>(ws, p.amat);
+    oa.err = m->dev_err;
+    QMC_PROF_TRY(QMC_KC_ORBITAL, tc_orbitals(s, oa));
+    return QMC_OK;
+  }
+  const float* h = at<float>(ws, p.h1[hb]);
   for (int c = 0; c < nch; ++c) {
     int ns = d.split ? (c == 0 ? d.n_up : d.n_dn) : d.n;
     int i0 = (d.split && c == 1) ? d.n_up : 0;
     RowMap map{ns, i0, d.n, p.Tp};
     EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec),
                    ar + a.env_pi[c], ar + a.env_sigma[c], d.n, d.A, d.K, p.T, d.env_abs};
-    QMC_CUDA(launch_gemm_simt<ActT>(s, p.B * ns, map, h, d.d_last, d.d_last, (const ActT*)nullptr, 0, 0,
-                                    ar + a.w_orb[c], d.norb_p, d.norb, epi));
+    QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, p.B * ns, map, h, d.d_last, d.d_last, nullptr, 0, 0,
+                                              ar + a.w_orb[c], d.norb_p, d.norb, epi));
   }
   return QMC_OK;
 }
@@ -306,18 +394,14 @@ static qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* e
   const Dims& d = m->d;
   const float* ar = m->arena;
   float* pe = want_pe ? at<float>(ws, p.pe) : nullptr;
-  QMC_CUDA(launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
+  QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
                            ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
                            at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe));
   int hb = 0;
-  if (p.mixed) {
-    QMC_TRY(run_backbone<__nv_bfloat16>(m, p, ws, s, &hb));
-    QMC_TRY(run_orbitals<__nv_bfloat16>(m, p, ws, hb, s));
-  } else {
-    QMC_TRY(run_backbone<float>(m, p, ws, s, &hb));
-    QMC_TRY(run_orbitals<float>(m, p, ws, hb, s));
-  }
-  QMC_CUDA(launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
+  if (p.mixed) QMC_TRY(run_backbone_mixed(m, p, ws, s, &hb));
+  else QMC_TRY(run_backbone_plain(m, p, ws, s, &hb));
+  QMC_TRY(run_orbitals(m, p, ws, hb, s));
+  QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
                          flags, nullptr));
   return QMC_OK;
 }
@@ -326,6 +410,18 @@ static qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1) { set_error("batch must be >= 1"); return QMC_ERR_SHAPE; }
+  if (m->precision == QMC_PRECISION_MIXED_BF16) {
+    const Dims& d = m->d;
+    for (int l = 1; l < d.L; ++l)
+      if (!tc_layer_supported(d.d1_in_p[l], d.g2_p[l], d.d1[l])) {
+        set_error("mixed precision needs one-electron widths that are multiples of 64 (layer %d)", l);
+        return QMC_ERR_UNSUPPORTED;
+      }
+    if (d.d_last % 64 || make_plan(m, op, 1).Tp < 0) {
+      set_error("mixed precision needs a last width that is a multiple of 64");
+      return QMC_ERR_UNSUPPORTED;
+    }
+  }
   if (op == QMC_OP_LOCAL_ENERGY && make_plan(m, op, 1).Tp > 128) {
     set_error("local energy supports at most 42 electrons (3n+2 <= 128 tangents per tile)");
     return QMC_ERR_SHAPE;
@@ -389,6 +485,8 @@ qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atom
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->n_sms, cudaDevAttrMultiProcessorCount, m->device);
   if (e == cudaSuccess) e = cudaMalloc(&m->arena, m->a.total * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->arena_bf16, m->a.total_bf16 * sizeof(__nv_bfloat16));
+  if (e == cudaSuccess) e = cudaMalloc(&m->dev_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m->dev_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(m->arena, 0, m->a.total * sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(m->arena_bf16, 0, m->a.total_bf16 * sizeof(__nv_bfloat16));
   const int A = m->d.A;
@@ -409,6 +507,7 @@ qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atom
   if (e != cudaSuccess) {
     cudaFree(m->arena);
     cudaFree(m->arena_bf16);
+    cudaFree(m->dev_err);
     delete m;
     return cuda_status(e, "qmc_ferminet_create");
   }
@@ -420,7 +519,19 @@ qmc_status qmc_model_destroy(qmc_model* m) {
   if (!m) return QMC_OK;
   cudaFree(m->arena);
   cudaFree(m->arena_bf16);
+  cudaFree(m->dev_err);
   delete m;
+  return QMC_OK;
+}
+
+qmc_status qmc_model_check_error(qmc_model* m, int* code) {
+  if (!m || !code) { set_error("null argument"); return QMC_ERR_ARG; }
+  QMC_CUDA(cudaMemcpy(code, m->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+  QMC_CUDA(cudaMemset(m->dev_err, 0, sizeof(int)));
+  if (*code) {
+    set_error("a bounded device-side wait expired (code %d)", *code);
+    return QMC_ERR_TIMEOUT;
+  }
   return QMC_OK;
 }
 
@@ -473,14 +584,14 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
   // bf16 K-major copies for the tensor-core path
   for (int l = 0; l < d.L; ++l) {
     int kmain = d.d1_in_p[l] + d.g2_p[l];
-    QMC_CUDA(launch_transpose_bf16(s, ar + a.w_main[l], kmain, d.d1[l], d.d1[l],
-                                   m->arena_bf16 + a.t_main[l], kmain, d.d1[l]));
-    QMC_CUDA(launch_transpose_bf16(s, ar + a.w_g1[l], d.g1_p[l], d.d1[l], d.d1[l],
-                                   m->arena_bf16 + a.t_g1[l], d.g1_p[l], d.d1[l]));
+    QMC_CUDA(launch_transpose_split(s, ar + a.w_main[l], kmain, d.d1[l], d.d1[l],
+                                    m->arena_bf16 + a.t_main[l], kmain, d.d1[l]));
+    QMC_CUDA(launch_transpose_split(s, ar + a.w_g1[l], d.g1_p[l], d.d1[l], d.d1[l],
+                                    m->arena_bf16 + a.t_g1[l], d.g1_p[l], d.d1[l]));
   }
   for (int c = 0; c < nch; ++c)
-    QMC_CUDA(launch_transpose_bf16(s, ar + a.w_orb[c], d.d_last, d.norb, d.norb_p,
-                                   m->arena_bf16 + a.t_orb[c], d.d_last, round_up(d.norb, 128)));
+    QMC_CUDA(launch_transpose_split(s, ar + a.w_orb[c], d.d_last, d.norb, d.norb_p,
+                                    m->arena_bf16 + a.t_orb[c], d.d_last, d.norb));
   m->params_set = true;
   return QMC_OK;
 }
@@ -521,14 +632,14 @@ qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64
   float* lpsi = at<float>(ws, p.lpsi);
   // log_prob of the starting walkers (src/jaqmc/sampler/mcmc.py:166)
   QMC_TRY(evaluate(m, p, ws, electrons, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, flags, s));
-  QMC_CUDA(launch_scale(s, batch, lpsi, 2.0f, log_prob));
+  QMC_PROF(QMC_KC_OTHER, launch_scale(s, batch, lpsi, 2.0f, log_prob));
   float* xp = at<float>(ws, p.xp);
   for (int st = 0; st < steps; ++st) {
     const float* nz = inj_normals ? inj_normals + (size_t)st * batch * n * 3 : nullptr;
     const float* uz = inj_uniforms ? inj_uniforms + (size_t)st * batch : nullptr;
-    QMC_CUDA(launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, nz));
+    QMC_PROF(QMC_KC_MH, launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, nz));
     QMC_TRY(evaluate(m, p, ws, xp, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, nullptr, s));
-    QMC_CUDA(launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, uz, accepts));
+    QMC_PROF(QMC_KC_MH, launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, uz, accepts));
   }
   return QMC_OK;
 }
@@ -536,13 +647,13 @@ qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64
 qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed, uint64_t counter,
                         float* normals, float* uniforms, cudaStream_t s) {
   if (!m || batch < 1 || steps < 1) { set_error("bad arguments"); return QMC_ERR_ARG; }
-  QMC_CUDA(launch_mh_draws(s, batch, m->d.n, steps, seed, counter, normals, uniforms));
+  QMC_PROF(QMC_KC_OTHER, launch_mh_draws(s, batch, m->d.n, steps, seed, counter, normals, uniforms));
   return QMC_OK;
 }
 
 qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t s) {
   if (batch < 1 || !x || !mean_var) { set_error("bad arguments"); return QMC_ERR_ARG; }
-  QMC_CUDA(launch_reduce_mean_var(s, batch, x, mean_var));
+  QMC_PROF(QMC_KC_OTHER, launch_reduce_mean_var(s, batch, x, mean_var));
   return QMC_OK;
 }
 

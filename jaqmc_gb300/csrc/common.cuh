@@ -97,6 +97,7 @@ struct qmc_model {
   float atoms_host[3 * qmc::kMaxAtoms];
   float charges_host[qmc::kMaxAtoms];
   double nuclear_repulsion = 0.0;  // sum_{I<J} Z_I Z_J / R_IJ
+  int* dev_err = nullptr;          // device error word of bounded waits
   bool params_set = false;
   int n_sms = 0;
 };

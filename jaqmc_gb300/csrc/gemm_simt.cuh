@@ -9,6 +9,7 @@
 //   h = f(z0),  J_t h = f'(z0) z_t,  L h = f'(z0) z_L + f''(z0) sum_t z_t^2
 // without another pass over memory.
 #pragma once
+#include "act.cuh"
 #include "common.cuh"
 
 namespace qmc {
@@ -48,18 +49,18 @@ struct EpiStore {
 };
 
 // FermiNet one-electron layer: z = acc + Gb[w,t] + (t==0) b; tanh with the
-// tangent rules; residual (h_in + h)/sqrt(2) when `resid` is set.
-template <typename OutT>
+// tangent rules; residual (h_in + h)/sqrt(2) when `resid` is set.  `Out` is
+// the storage policy of the activations (StF32 or StSplit).
+template <class Out>
 struct EpiLayer {
   const float* Gb;   // [walkers*Tp][N] broadcast (spin-mean) term
   const float* bias; // [N]
-  const OutT* resid; // rows like out, or nullptr
-  OutT* out;
-  int ld;            // row stride of out / resid
+  Out resid;         // rows like out; resid.p == nullptr: no residual
+  Out out;
   int T;             // real tangents (1 = value only)
   __device__ __forceinline__ void put(size_t row, int col, float v) const {
-    if (resid) v = (v + (float)resid[row * ld + col]) * kRsqrt2;
-    out[row * ld + col] = (OutT)v;
+    if (resid.valid()) v = (v + resid.get(row, col)) * kRsqrt2;
+    out.put(row, col, v);
   }
   __device__ void operator()(const float* Cs, int ng, int g0, int n0, int N, const RowMap& m) const {
     const int Tp = m.Tp;
@@ -81,7 +82,7 @@ struct EpiLayer {
         }
         float zL = cs[kCsLd] + gb[N];
         put(r0 + 1, col, d1 * zL + d2 * S);
-        for (int t = T; t < Tp; ++t) out[(r0 + t) * ld + col] = (OutT)0.0f;
+        for (int t = T; t < Tp; ++t) out.put(r0 + t, col, 0.0f);
       }
     }
   }
@@ -146,10 +147,10 @@ struct EpiOrbital {
 // C[rows x N] = [A1 | A2][rows x (K1+K2)] * W[(K1+K2) x N].  K1 and K2 are
 // multiples of 8; W rows are read as float4, so ldw is a multiple of 4 with
 // zero columns from N up to round_up(N, 4); A1/A2/W are 16-byte aligned.
-template <typename InT, class Epi>
+template <class Epi>
 __global__ void __launch_bounds__(256)
-k_gemm_simt(int n_groups, RowMap map, const InT* __restrict__ A1, int lda1, int K1,
-            const InT* __restrict__ A2, int lda2, int K2, const float* __restrict__ W, int ldw,
+k_gemm_simt(int n_groups, RowMap map, const float* __restrict__ A1, int lda1, int K1,
+            const float* __restrict__ A2, int lda2, int K2, const float* __restrict__ W, int ldw,
             int N, Epi epi) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
@@ -175,14 +176,8 @@ k_gemm_simt(int n_groups, RowMap map, const InT* __restrict__ A1, int lda1, int 
     v = make_float4(0.f, 0.f, 0.f, 0.f);
     if (!a_ok) return;
     int k = k0 + a_k;
-    const InT* src = (k < K1) ? (A1 + a_row * lda1 + k) : (A2 + a_row * lda2 + (k - K1));
-    if constexpr (sizeof(InT) == 4) {
-      v = *reinterpret_cast<const float4*>(src);
-    } else {
-      const __nv_bfloat162* s2 = reinterpret_cast<const __nv_bfloat162*>(src);
-      float2 f0 = __bfloat1622float2(s2[0]), f1 = __bfloat1622float2(s2[1]);
-      v = make_float4(f0.x, f0.y, f1.x, f1.y);
-    }
+    const float* src = (k < K1) ? (A1 + a_row * lda1 + k) : (A2 + a_row * lda2 + (k - K1));
+    v = *reinterpret_cast<const float4*>(src);
   };
   auto load_b = [&](int k0, float4& v) {
     v = b_ok ? *reinterpret_cast<const float4*>(W + (size_t)(k0 + b_k) * ldw + n0 + b_c)
@@ -252,22 +247,24 @@ k_gemm_simt(int n_groups, RowMap map, const InT* __restrict__ A1, int lda1, int 
   if (ng > 0) epi(Cs, ng, g0, n0, N, map);
 }
 
-template <typename InT, class Epi>
-cudaError_t launch_gemm_simt(cudaStream_t s, int n_groups, RowMap map, const InT* A1, int lda1,
-                             int K1, const InT* A2, int lda2, int K2, const float* W, int ldw,
+template <class Epi>
+cudaError_t launch_gemm_simt(cudaStream_t s, int n_groups, RowMap map, const float* A1, int lda1,
+                             int K1, const float* A2, int lda2, int K2, const float* W, int ldw,
                              int N, const Epi& epi) {
   if (n_groups <= 0) return cudaSuccess;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_simt<InT, Epi>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSimtSmem);
+  if (map.Tp > kBM) return cudaErrorInvalidValue;
+  static int attr_dev = -1;  // the attribute is per device
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (attr_dev != dev) {
+    e = cudaFuncSetAttribute(k_gemm_simt<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSimtSmem);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_dev = dev;
   }
   int G = kBM / map.Tp;
   dim3 grid((n_groups + G - 1) / G, (N + kBN - 1) / kBN);
-  k_gemm_simt<InT, Epi><<<grid, 256, kSimtSmem, s>>>(n_groups, map, A1, lda1, K1, A2, lda2, K2, W,
-                                                     ldw, N, epi);
+  k_gemm_simt<Epi><<<grid, 256, kSimtSmem, s>>>(n_groups, map, A1, lda1, K1, A2, lda2, K2, W, ldw, N, epi);
   return cudaGetLastError();
 }
 

@@ -1,5 +1,7 @@
 // FermiNet features, two-electron stream, spin means, determinant stage,
 // Metropolis-Hastings and reductions for sm_103a.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace qmc {
@@ -118,52 +120,117 @@ __global__ void k_pair_layer(int npairs, int P2, int d_in, int d_out, const floa
                              const float* __restrict__ W, const float* __restrict__ b,
                              float* __restrict__ Hout) {
   extern __shared__ float sh[];
-  float* Ws = sh;                     // [d_in][d_out]
-  float* Is = Ws + d_in * d_out;      // [ppb][P2][d_in]
+  float* Ws = sh;                     // [d_in][d_out], loaded once per block
+  float* Is = Ws + d_in * d_out;      // [ppb][P2][d_in] of the current chunk
   const int ppb = blockDim.x / d_out;
-  const int p0 = blockIdx.x * ppb;
   for (int e = threadIdx.x; e < d_in * d_out; e += blockDim.x) Ws[e] = W[e];
-  const int np = min(ppb, npairs - p0);
-  for (int e = threadIdx.x; e < np * P2 * d_in; e += blockDim.x)
-    Is[e] = Hin[(size_t)p0 * P2 * d_in + e];
-  __syncthreads();
   const int lp = threadIdx.x / d_out, f = threadIdx.x % d_out;
-  if (lp >= np) return;
-  const float* in = Is + lp * P2 * d_in;
-  float z[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int k = 0; k < d_in; ++k) {
-    float wv = Ws[k * d_out + f];
-#pragma unroll
-    for (int p = 0; p < 5; ++p)
-      if (p < P2) z[p] = fmaf(in[p * d_in + k], wv, z[p]);
-  }
-  float h = tanhf(z[0] + b[f]);
-  float out[5];
-  out[0] = h;
-  if (P2 > 1) {
-    float d1 = 1.f - h * h, d2 = -2.f * h * d1;
-    float S = z[2] * z[2] + z[3] * z[3] + z[4] * z[4];
-    out[1] = d1 * z[1] + d2 * S;
-    out[2] = d1 * z[2];
-    out[3] = d1 * z[3];
-    out[4] = d1 * z[4];
-  }
+  const float bf = b[f];
   const bool res = d_in == d_out;
-  float* o = Hout + ((size_t)(p0 + lp) * P2) * d_out + f;
-  for (int p = 0; p < P2; ++p) {
-    float v = out[p];
-    if (res) v = (v + in[p * d_in + f]) * kRsqrt2;
-    o[p * d_out] = v;
+  const int nchunks = (npairs + ppb - 1) / ppb;
+  for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    const int p0 = chunk * ppb;
+    const int np = min(ppb, npairs - p0);
+    __syncthreads();  // previous chunk done with Is (and Ws loaded on entry)
+    for (int e = threadIdx.x; e < np * P2 * d_in; e += blockDim.x) Is[e] = Hin[(size_t)p0 * P2 * d_in + e];
+    __syncthreads();
+    if (lp >= np) continue;
+    const float* in = Is + lp * P2 * d_in;
+    float z[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int k = 0; k < d_in; ++k) {
+      float wv = Ws[k * d_out + f];
+#pragma unroll
+      for (int p = 0; p < 5; ++p)
+        if (p < P2) z[p] = fmaf(in[p * d_in + k], wv, z[p]);
+    }
+    float h = tanhf(z[0] + bf);
+    float out[5];
+    out[0] = h;
+    if (P2 > 1) {
+      float d1 = 1.f - h * h, d2 = -2.f * h * d1;
+      float S = z[2] * z[2] + z[3] * z[3] + z[4] * z[4];
+      out[1] = d1 * z[1] + d2 * S;
+      out[2] = d1 * z[2];
+      out[3] = d1 * z[3];
+      out[4] = d1 * z[4];
+    }
+    float* o = Hout + ((size_t)(p0 + lp) * P2) * d_out + f;
+    for (int p = 0; p < P2; ++p) {
+      float v = out[p];
+      if (res) v = (v + in[p * d_in + f]) * kRsqrt2;
+      o[p * d_out] = v;
+    }
+  }
+}
+
+// Value-only two-electron layer: one thread per pair, all d_out features in
+// registers, weights broadcast from shared memory.
+template <int DIN, int DOUT>
+__global__ void __launch_bounds__(128) k_pair_layer_value(int npairs, const float* __restrict__ Hin,
+                                                          const float* __restrict__ W,
+                                                          const float* __restrict__ b,
+                                                          float* __restrict__ Hout) {
+  __shared__ float Ws[DIN * DOUT];
+  __shared__ float bs[DOUT];
+  for (int e = threadIdx.x; e < DIN * DOUT; e += blockDim.x) Ws[e] = W[e];
+  for (int e = threadIdx.x; e < DOUT; e += blockDim.x) bs[e] = b[e];
+  __syncthreads();
+  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= npairs) return;
+  float x[DIN];
+  const float4* src = reinterpret_cast<const float4*>(Hin + (size_t)pr * DIN);
+#pragma unroll
+  for (int q = 0; q < DIN / 4; ++q) {
+    float4 v = src[q];
+    x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+  }
+  float4* dst = reinterpret_cast<float4*>(Hout + (size_t)pr * DOUT);
+#pragma unroll
+  for (int f4 = 0; f4 < DOUT / 4; ++f4) {
+    float z[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) z[e] = bs[4 * f4 + e];
+#pragma unroll
+    for (int k = 0; k < DIN; ++k) {
+      const float4 w = *reinterpret_cast<const float4*>(&Ws[k * DOUT + 4 * f4]);
+      z[0] = fmaf(x[k], w.x, z[0]);
+      z[1] = fmaf(x[k], w.y, z[1]);
+      z[2] = fmaf(x[k], w.z, z[2]);
+      z[3] = fmaf(x[k], w.w, z[3]);
+    }
+    float4 o;
+    o.x = tanhf(z[0]); o.y = tanhf(z[1]); o.z = tanhf(z[2]); o.w = tanhf(z[3]);
+    if (DIN == DOUT) {
+      o.x = (o.x + x[4 * f4]) * kRsqrt2;
+      o.y = (o.y + x[4 * f4 + 1]) * kRsqrt2;
+      o.z = (o.z + x[4 * f4 + 2]) * kRsqrt2;
+      o.w = (o.w + x[4 * f4 + 3]) * kRsqrt2;
+    }
+    dst[f4] = o;
   }
 }
 
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout) {
+  if (P2 == 1) {
+    const unsigned grid = (unsigned)((npairs + 127) / 128);
+    if (d_in == 4 && d_out == 32) {
+      k_pair_layer_value<4, 32><<<grid, 128, 0, s>>>(npairs, Hin, W, b, Hout);
+      return cudaGetLastError();
+    }
+    if (d_in == 32 && d_out == 32) {
+      k_pair_layer_value<32, 32><<<grid, 128, 0, s>>>(npairs, Hin, W, b, Hout);
+      return cudaGetLastError();
+    }
+  }
   int ppb = 256 / d_out;
   if (ppb < 1) return cudaErrorInvalidValue;
   size_t sm = sizeof(float) * (d_in * d_out + ppb * P2 * d_in);
-  k_pair_layer<<<(npairs + ppb - 1) / ppb, ppb * d_out, sm, s>>>(npairs, P2, d_in, d_out, Hin, W, b,
-                                                                  Hout);
+  static int n_sms = 0;
+  if (!n_sms) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, 0);
+  int nchunks = (npairs + ppb - 1) / ppb;
+  int grid = std::min(nchunks, std::max(1, n_sms) * 8);
+  k_pair_layer<<<grid, ppb * d_out, sm, s>>>(npairs, P2, d_in, d_out, Hin, W, b, Hout);
   return cudaGetLastError();
 }
 
@@ -176,9 +243,8 @@ __device__ __forceinline__ void channel_range(int s, int C, int n, int n_up, int
   *a1 = s == 0 ? n_up : n;
 }
 
-template <typename InT>
-__global__ void k_mean_h1(int B, int n, int n_up, int C, int Tp, int d, int ld,
-                          const InT* __restrict__ X, int g1p, float* __restrict__ G1) {
+template <class In, class Out>
+__global__ void k_mean_h1(int B, int n, int n_up, int C, int Tp, int d, In X, int g1p, Out G1) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t total = (size_t)B * Tp * g1p;
   if (e >= total) return;
@@ -191,29 +257,29 @@ __global__ void k_mean_h1(int B, int n, int n_up, int C, int Tp, int d, int ld,
     int s = col / d, f = col % d, a0, a1;
     channel_range(s, C, n, n_up, &a0, &a1);
     float acc = 0.f;
-    for (int i = a0; i < a1; ++i) acc += (float)X[(((size_t)w * n + i) * Tp + t) * ld + f];
+    for (int i = a0; i < a1; ++i) acc += X.get(((size_t)w * n + i) * Tp + t, f);
     v = acc / (float)(a1 - a0);
   }
-  G1[e] = v;
+  G1.put(wt, col, v);
 }
 
-template <typename InT>
-cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, int ld,
-                           const InT* X, int g1p, float* G1) {
+template <class In, class Out>
+cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, In X, int g1p,
+                           Out G1) {
   size_t total = (size_t)B * Tp * g1p;
-  k_mean_h1<InT><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, d, ld, X, g1p, G1);
+  k_mean_h1<In, Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, d, X, g1p, G1);
   return cudaGetLastError();
 }
-template cudaError_t launch_mean_h1<float>(cudaStream_t, int, int, int, int, int, int, int,
-                                           const float*, int, float*);
-template cudaError_t launch_mean_h1<__nv_bfloat16>(cudaStream_t, int, int, int, int, int, int, int,
-                                                   const __nv_bfloat16*, int, float*);
+template cudaError_t launch_mean_h1<StF32, StF32>(cudaStream_t, int, int, int, int, int, int, StF32, int,
+                                                  StF32);
+template cudaError_t launch_mean_h1<StSplit, StSplit>(cudaStream_t, int, int, int, int, int, int, StSplit,
+                                                      int, StSplit);
 
 // d/dr_e of h2[a, i] = (delta_{ae} - delta_{ie}) d/dDelta (pair (a,i), a != i);
 // the full Laplacian of a pair feature is twice its Laplacian in Delta.
-template <typename OutT>
+template <class Out>
 __global__ void k_mean_h2(int B, int n, int n_up, int C, int Tp, int T, int d2, int P2,
-                          const float* __restrict__ H2, int g2p, OutT* __restrict__ G2) {
+                          const float* __restrict__ H2, int g2p, Out G2) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t total = (size_t)B * n * Tp * g2p;
   if (e >= total) return;
@@ -248,21 +314,21 @@ __global__ void k_mean_h2(int B, int n, int n_up, int C, int Tp, int T, int d2, 
       v = acc * inv;
     }
   }
-  G2[e] = (OutT)v;
+  G2.put(r, col, v);
 }
 
-template <typename OutT>
+template <class Out>
 cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d2,
-                           int P2, const float* H2, int g2p, OutT* G2) {
+                           int P2, const float* H2, int g2p, Out G2) {
   size_t total = (size_t)B * n * Tp * g2p;
-  k_mean_h2<OutT><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, T, d2, P2, H2,
+  k_mean_h2<Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, T, d2, P2, H2,
                                                                   g2p, G2);
   return cudaGetLastError();
 }
-template cudaError_t launch_mean_h2<float>(cudaStream_t, int, int, int, int, int, int, int, int,
-                                           const float*, int, float*);
-template cudaError_t launch_mean_h2<__nv_bfloat16>(cudaStream_t, int, int, int, int, int, int, int,
-                                                   int, const float*, int, __nv_bfloat16*);
+template cudaError_t launch_mean_h2<StF32>(cudaStream_t, int, int, int, int, int, int, int, int,
+                                           const float*, int, StF32);
+template cudaError_t launch_mean_h2<StSplit>(cudaStream_t, int, int, int, int, int, int, int, int,
+                                             const float*, int, StSplit);
 
 // =====================================================================
 // determinant stage (src/jaqmc/wavefunction/output/logdet.py:53-80,
@@ -270,7 +336,8 @@ template cudaError_t launch_mean_h2<__nv_bfloat16>(cudaStream_t, int, int, int, 
 //                    src/jaqmc/estimator/kinetic/_common.py:61-73)
 // One CTA per walker; each warp factorises determinants k = warp, warp+nw, ...
 // =====================================================================
-constexpr float kRefactorRatio = 1e6f;
+// FP64 re-factorisation threshold on the pivot growth factor max|U| / max|A|.
+constexpr float kRefactorGrowth = 1e6f;
 
 __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -288,16 +355,21 @@ struct DetOut {
   int refactor, singular;
 };
 
-// LU with partial pivoting of the n x n matrix in S (row stride n+1) by one
-// warp; perm[i] = source row of pivoted row i.  Returns log|det|, sign and the
-// pivot ratio max|u_kk| / min|u_kk|.
+// LU with partial pivoting of the n x n matrix in S (row stride ld) by one
+// warp; perm[i] = source row of pivoted row i.  log|det| is accumulated as a
+// normalised mantissa/exponent product (one FP64 log per determinant).
+// Returns the pivot growth factor max|U| / max|A| in *growth.
 template <typename S>
-__device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* sgn, double* ratio,
+__device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* sgn, double* growth,
                         int* singular) {
   const int lane = threadIdx.x & 31;
   for (int i = lane; i < n; i += 32) perm[i] = i;
+  S amax = (S)0;
+  for (int e = lane; e < n * n; e += 32) amax = fmax(amax, (S)fabs(LU[(e / n) * ld + (e % n)]));
+  for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
   __syncwarp();
-  double la = 0.0, pmax = 0.0, pmin = 1e300;
+  S mant = (S)1;
+  int ex = 0;
   float sg = 1.f;
   int sing = 0;
   for (int k = 0; k < n; ++k) {
@@ -327,14 +399,12 @@ __device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* 
     }
     __syncwarp();
     S piv = LU[k * ld + k];
-    double ap = fabs((double)piv);
-    if (!(ap > 0.0)) { sing = 1; la = -INFINITY; break; }
-    la += log(ap);
+    if (!(fabs(piv) > (S)0)) { sing = 1; break; }
     if (piv < (S)0) sg = -sg;
-    pmax = fmax(pmax, ap);
-    pmin = fmin(pmin, ap);
-    S inv = (S)1 / piv;
-    for (int i = k + 1 + lane; i < n; i += 32) LU[i * ld + k] *= inv;
+    int e2;
+    mant = frexp(mant * (S)fabs(piv), &e2);
+    ex += e2;
+    for (int i = k + 1 + lane; i < n; i += 32) LU[i * ld + k] /= piv;
     __syncwarp();
     for (int j = k + 1 + lane; j < n; j += 32) {
       S ukj = LU[k * ld + j];
@@ -342,9 +412,15 @@ __device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* 
     }
     __syncwarp();
   }
-  *logabs = la;
+  S umax = (S)0;
+  if (!sing)
+    for (int j = lane; j < n; j += 32)
+      for (int i = 0; i <= j; ++i) umax = fmax(umax, (S)fabs(LU[i * ld + j]));
+  for (int o = 16; o > 0; o >>= 1) umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+  // one FP64 log per determinant (FP64 is scarce on this part): lane 0 only
+  *logabs = sing ? -INFINITY : (lane == 0 ? log((double)mant) + (double)ex * 0.69314718055994530942 : 0.0);
   *sgn = sg;
-  *ratio = sing ? INFINITY : pmax / pmin;
+  *growth = sing ? INFINITY : (double)umax / (double)amax;
   *singular = sing;
 }
 
@@ -467,9 +543,9 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* sc
   DetOut o{};
   for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (S)Ak[e];
   __syncwarp();
-  double ratio;
-  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &ratio, &o.singular);
-  o.refactor = (!fp64_pass && !(ratio <= (double)kRefactorRatio)) ? 1 : 0;
+  double growth;
+  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular);
+  o.refactor = (!fp64_pass && !o.singular && !(growth <= (double)kRefactorGrowth)) ? 1 : 0;
   if (T <= 1 || o.singular || o.refactor) return o;
   warp_inverse<S>(LU, Ainv, perm, n, ld);
   float t2acc = 0.f, qacc = 0.f;
@@ -536,37 +612,44 @@ __global__ void k_logdet(int n, int K, int Tp, int T, const float* __restrict__ 
   }
   __syncthreads();
   if (warp != 0) return;
-  // FP64 signed log-sum-exp over determinants
+  // FP64 signed log-sum-exp over determinants, one determinant per lane
   double lmax = -INFINITY;
-  for (int k = 0; k < K; ++k)
+  for (int k = lane; k < K; k += 32)
     if (sgs[k] != 0.f) lmax = fmax(lmax, lds[k]);
+  for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
   double Ssum = 0.0;
-  for (int k = 0; k < K; ++k)
+  for (int k = lane; k < K; k += 32)
     if (sgs[k] != 0.f) Ssum += (double)sgs[k] * exp(lds[k] - lmax);
-  double lp = log(fabs(Ssum)) + lmax;
+  Ssum = warp_sum(Ssum);
+  double lp = lane == 0 ? log(fabs(Ssum)) + lmax : 0.0;
   float sg = Ssum > 0 ? 1.f : (Ssum < 0 ? -1.f : 0.f);
-  bool bad = !isfinite(lp);
+  bool bad = lane == 0 && !isfinite(lp);
   if (T > 1) {
+    // w_k = s_k exp(ld_k - max) / S, once per determinant (FP64)
+    float* wk = tLs;  // reuse: tL_k is folded into the per-det term below
+    for (int k = lane; k < K; k += 32) {
+      double w = sgs[k] != 0.f ? (double)sgs[k] * exp(lds[k] - lmax) / Ssum : 0.0;
+      lds[k] = w * ((double)tLs[k] - (double)t2s[k] + (double)qs[k]);
+      wk[k] = (float)w;
+    }
+    __syncwarp();
     // grad_d = sum_k w_k t1_kd ; lap = sum_k w_k (tL - t2 + q) - |grad|^2
     double g2 = 0.0;
     for (int d = lane; d < D; d += 32) {
       double g = 0.0;
-      for (int k = 0; k < K; ++k)
-        if (sgs[k] != 0.f) g += (double)sgs[k] * exp(lds[k] - lmax) / Ssum * (double)t1s[(size_t)k * D + d];
+      for (int k = 0; k < K; ++k) g += (double)wk[k] * (double)t1s[(size_t)k * D + d];
       g2 += g * g;
     }
     g2 = warp_sum(g2);
     double lap = 0.0;
-    for (int k = 0; k < K; ++k)
-      if (sgs[k] != 0.f)
-        lap += (double)sgs[k] * exp(lds[k] - lmax) / Ssum * ((double)tLs[k] - (double)t2s[k] + (double)qs[k]);
+    for (int k = 0; k < K; ++k) lap += lds[k];
     lap -= g2;
     double kin = -0.5 * (lap + g2);
     if (lane == 0) {
       if (ke) ke[w] = (float)kin;
       if (el) el[w] = (float)(kin + (pe ? (double)pe[w] : 0.0));
     }
-    bad = bad || !isfinite(kin);
+    bad = bad || (lane == 0 && !isfinite(kin));
   }
   if (lane == 0) {
     if (logpsi) logpsi[w] = (float)lp;
@@ -777,20 +860,23 @@ cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double
 // =====================================================================
 // parameter preparation
 // =====================================================================
-__global__ void k_transpose_bf16(const float* __restrict__ in, int rows, int cols, int ld_in,
-                                 __nv_bfloat16* __restrict__ out, int rows_p, int cols_p) {
+__global__ void k_transpose_split(const float* __restrict__ in, int rows, int cols, int ld_in,
+                                  __nv_bfloat16* __restrict__ out, int rows_p, int cols_p) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)rows_p * cols_p) return;
+  const size_t plane = (size_t)rows_p * cols_p;
+  if (e >= plane) return;
   int r = (int)(e % rows_p), c = (int)(e / rows_p);  // out[c][r]
   float v = (r < rows && c < cols) ? in[(size_t)r * ld_in + c] : 0.f;
-  out[e] = __float2bfloat16_rn(v);
+  __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  out[e] = hi;
+  out[e + plane] = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
-cudaError_t launch_transpose_bf16(cudaStream_t s, const float* in, int rows, int cols, int ld_in,
-                                  __nv_bfloat16* out, int rows_p, int cols_p) {
+cudaError_t launch_transpose_split(cudaStream_t s, const float* in, int rows, int cols, int ld_in,
+                                   __nv_bfloat16* out, int rows_p, int cols_p) {
   size_t total = (size_t)rows_p * cols_p;
-  k_transpose_bf16<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(in, rows, cols, ld_in, out, rows_p,
-                                                                  cols_p);
+  k_transpose_split<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(in, rows, cols, ld_in, out, rows_p,
+                                                                   cols_p);
   return cudaGetLastError();
 }
 

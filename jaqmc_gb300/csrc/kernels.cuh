@@ -1,5 +1,6 @@
 // Declarations of the FermiNet / MH / reduction kernels (kernels.cu).
 #pragma once
+#include "act.cuh"
 #include "common.cuh"
 
 namespace qmc {
@@ -18,16 +19,17 @@ cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, 
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout);
 
-// Spin-channel means of the one-electron rows: G1[(w*Tp+t)][s*d + f].
-template <typename InT>
-cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, int ld,
-                           const InT* X, int g1p, float* G1);
+// Spin-channel means of the one-electron rows: G1[(w*Tp+t)][s*d + f]
+// (padding columns up to the output row width are written as zero).
+template <class In, class Out>
+cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, In X, int g1p,
+                           Out G1);
 
 // Spin-channel means of the two-electron rows expanded to full tangents:
 // G2[(w*n+i)*Tp + t][s*d2 + f].
-template <typename OutT>
+template <class Out>
 cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d2,
-                           int P2, const float* H2, int g2p, OutT* G2);
+                           int P2, const float* H2, int g2p, Out G2);
 
 // Per-walker determinant stage: LU/log|det| of the K value matrices, FP64
 // signed log-sum-exp and, when T > 1, the slogdet forward-Laplacian traces
@@ -49,8 +51,9 @@ cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float*
 
 cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out);
 
-// fp32 [rows][cols] -> bf16 transposed [cols_p][rows_p] (zero padded)
-cudaError_t launch_transpose_bf16(cudaStream_t s, const float* in, int rows, int cols, int ld_in,
-                                  __nv_bfloat16* out, int rows_p, int cols_p);
+// fp32 [rows][cols] -> transposed split-bf16 planes hi/lo of [cols_p][rows_p]
+// (zero padded; the lo plane starts cols_p*rows_p elements after hi)
+cudaError_t launch_transpose_split(cudaStream_t s, const float* in, int rows, int cols, int ld_in,
+                                   __nv_bfloat16* out, int rows_p, int cols_p);
 
 }  // namespace qmc

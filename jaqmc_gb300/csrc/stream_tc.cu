@@ -1,12 +1,650 @@
+// Split-BF16 tcgen05 GEMMs (see stream_tc.cuh).
+//
+// One CTA computes a 128-feature x N-column accumulator (N = whole tangent
+// groups, <= 256).  Warp roles: warp 0 issues the TMA loads of the K chunks
+// (64 bf16 = one 128-byte swizzle row) into a ring of shared-memory stages;
+// warp 1 owns the TMEM allocation and issues the MMAs (3 per K=16 step:
+// hi*hi, hi*lo, lo*hi); warps 2-9 run the epilogue from TMEM, two warps per
+// TMEM lane quarter splitting the tile's columns.  For residual layers the
+// two K chunks holding this CTA's 128 input features are loaded last, so the
+// epilogue reads the residual from those shared-memory tiles.  Every
+// mbarrier wait is bounded; on expiry the CTA records an error code, waits
+// (bounded) for its own copies and MMAs, frees TMEM and exits.
+#include <cudaTypedefs.h>
+
 #include "stream_tc.cuh"
+#include "tc_ptx.cuh"
 
 namespace qmc {
-int tc_padded_tangents(int T) { return T; }
-bool tc_layer_supported(int, int, int) { return false; }
-qmc_status tc_stream_layer(cudaStream_t, int, int, int, int, const __nv_bfloat16*, int,
-                           const __nv_bfloat16*, int, const __nv_bfloat16*, int, const float*,
-                           const float*, bool, __nv_bfloat16*) {
-  set_error("tensor-core stream layer not built");
-  return QMC_ERR_UNSUPPORTED;
+
+constexpr int kTcThreads = 320;
+constexpr int kEpiWarps = 8;
+constexpr int kKChunk = 64;                      // bf16 per 128-byte swizzle row
+constexpr int kATile = 128 * kKChunk * 2;        // bytes of one A plane tile
+constexpr long long kWaitCycles = 1000000000LL;  // about 0.5 s at 2 GHz
+constexpr int kErrTimeoutFull = 1, kErrTimeoutEmpty = 2, kErrTimeoutAcc = 3;
+
+struct TileInfo {
+  int row0;   // first activation row of the tile (TMA y coordinate)
+  int a_sel;  // which A tensor map (orbital spin channel)
+  int g0;     // first group
+  int ng;     // valid groups in the tile
+  int w, i0;  // orbital tiles: walker and first electron
+};
+
+struct TcArgs {
+  int n_cols;     // columns per tile (G * Tp)
+  int G, Tp, T;
+  int k_chunks, k1_chunks;
+  int stages;
+  int tmem_cols;
+  int n_out;
+  int resid_last;  // order the K chunks so this CTA's residual features come last
+  int* err;
+};
+
+// K-chunk order: source B (0 = first, 1 = second), chunk index within it,
+// and the A (weight) K offset.  With resid_last: second-source chunks first,
+// then the first-source chunks outside [m0, m0+128), then those two.
+__device__ __forceinline__ void chunk_src(const TcArgs& g, int m0, int c, int* b2, int* kx, int* ka) {
+  const int nx = g.k1_chunks, n2 = g.k_chunks - g.k1_chunks;
+  if (!g.resid_last) {
+    *b2 = c >= nx;
+    *kx = (c < nx ? c : c - nx) * kKChunk;
+    *ka = c * kKChunk;
+    return;
+  }
+  if (c < n2) {
+    *b2 = 1;
+    *kx = c * kKChunk;
+    *ka = (nx + c) * kKChunk;
+    return;
+  }
+  const int r0 = m0 / kKChunk;
+  int idx = c - n2, j;
+  if (idx >= nx - 2) {
+    j = r0 + (idx - (nx - 2));
+  } else {
+    j = idx < r0 ? idx : idx + 2;
+  }
+  *b2 = 0;
+  *kx = j * kKChunk;
+  *ka = j * kKChunk;
 }
+
+// element (r, k) of a 128-byte-swizzled K-major bf16 tile
+__device__ __forceinline__ float sw128_at(const uint8_t* tile, int r, int k) {
+  const uint8_t* p = tile + r * 128 + ((((k >> 3) ^ (r & 7)) << 4) | ((k & 7) << 1));
+  return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(p));
+}
+
+struct ResidTiles {  // residual operand tiles left in shared memory
+  const uint8_t* hi[2];
+  const uint8_t* lo[2];
+  __device__ __forceinline__ float get(int r, int f_loc) const {
+    const int w = f_loc >> 6, k = f_loc & 63;
+    return sw128_at(hi[w], r, k) + sw128_at(lo[w], r, k);
+  }
+};
+
+__device__ __forceinline__ void report(int* err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_tc_gemm(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
+          const __grid_constant__ CUtensorMap mapB1, const __grid_constant__ CUtensorMap mapB2, TcArgs g,
+          Epi epi) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int stage_b = g.n_cols * kKChunk * 2;
+  const int stage_bytes = 2 * kATile + 2 * stage_b;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)g.stages * stage_bytes);
+  uint64_t* empty = full + g.stages;
+  uint64_t* accb = empty + g.stages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+  int* aborted = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * 128;
+  const TileInfo ti = epi.tile(blockIdx.x, g);
+
+  // once any CTA of the call has given up on a wait, the rest skip their work
+  __shared__ int skip;
+  if (threadIdx.x == 0) skip = g.err ? *(volatile int*)g.err : 0;
+  __syncthreads();
+  if (skip) return;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < g.stages; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    ptx::mbar_init(accb, 1);
+    *aborted = 0;
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(tmem_slot, (uint32_t)g.tmem_cols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const CUtensorMap* A = ti.a_sel ? &mapA1 : &mapA0;
+      ptx::prefetch_tmap(A);
+      ptx::prefetch_tmap(&mapB1);
+      int issued = 0;
+      for (int c = 0; c < g.k_chunks; ++c) {
+        const int s = c % g.stages;
+        const uint32_t ph = (uint32_t)(c / g.stages) & 1u;
+        if (!ptx::mbar_wait_bounded(&empty[s], ph ^ 1u, kWaitCycles)) {
+          report(g.err, kErrTimeoutEmpty);
+          atomicExch(aborted, 1);
+          break;
+        }
+        if (*(volatile int*)aborted) break;
+        uint8_t* base = smem + (size_t)s * stage_bytes;
+        int b2, kx, ka;
+        chunk_src(g, m0, c, &b2, &kx, &ka);
+        ptx::mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+        ptx::tma_load_3d(base, A, ka, m0, 0, &full[s]);
+        ptx::tma_load_3d(base + kATile, A, ka, m0, 1, &full[s]);
+        const CUtensorMap* Bm = b2 ? &mapB2 : &mapB1;
+        ptx::tma_load_3d(base + 2 * kATile, Bm, kx, ti.row0, 0, &full[s]);
+        ptx::tma_load_3d(base + 2 * kATile + stage_b, Bm, kx, ti.row0, 1, &full[s]);
+        ++issued;
+      }
+      // never leave the CTA with copies in flight: wait (bounded) for the
+      // last phase armed on every stage
+      for (int c = issued - g.stages; c < issued; ++c) {
+        if (c < 0) continue;
+        const int s = c % g.stages;
+        const uint32_t ph = (uint32_t)(c / g.stages) & 1u;
+        ptx::mbar_wait_bounded(&full[s], ph, kWaitCycles);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = ptx::idesc_bf16(128, g.n_cols);
+      for (int c = 0; c < g.k_chunks; ++c) {
+        const int s = c % g.stages;
+        const uint32_t ph = (uint32_t)(c / g.stages) & 1u;
+        if (!ptx::mbar_wait_bounded(&full[s], ph, kWaitCycles)) {
+          report(g.err, kErrTimeoutFull);
+          atomicExch(aborted, 1);
+          break;
+        }
+        ptx::tc_fence_after();
+        uint8_t* base = smem + (size_t)s * stage_bytes;
+        const uint64_t a_hi = ptx::sw128_desc(base), a_lo = ptx::sw128_desc(base + kATile);
+        const uint64_t b_hi = ptx::sw128_desc(base + 2 * kATile);
+        const uint64_t b_lo = ptx::sw128_desc(base + 2 * kATile + stage_b);
+#pragma unroll
+        for (int kk = 0; kk < kKChunk / 16; ++kk) {
+          const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 16 bf16 = 32 bytes
+          ptx::mma_bf16(tmem, a_hi + off, b_hi + off, idesc, (c | kk) != 0);
+          ptx::mma_bf16(tmem, a_hi + off, b_lo + off, idesc, 1u);
+          ptx::mma_bf16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+        }
+        ptx::mma_commit(&empty[s]);
+      }
+      ptx::mma_commit(accb);  // fires once every issued MMA has completed
+    }
+  } else {
+    const bool ok = ptx::mbar_wait_bounded(accb, 0u, kWaitCycles);
+    if (!ok) report(g.err, kErrTimeoutAcc);
+    if (ok && !*(volatile int*)aborted) {
+      ptx::tc_fence_after();
+      const int q = warp & 3;           // TMEM lane quarter accessible to this warp
+      const int half = (warp - 2) >> 2; // which of the two warps of this quarter
+      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16);
+      ResidTiles rt{};
+      if (g.resid_last) {
+        for (int w2 = 0; w2 < 2; ++w2) {
+          const int st = (g.k_chunks - 2 + w2) % g.stages;
+          const uint8_t* base = smem + (size_t)st * stage_bytes + 2 * kATile;
+          rt.hi[w2] = base;
+          rt.lo[w2] = base + stage_b;
+        }
+      }
+      epi.run(ti, g, taddr, m0 + 32 * q + lane, 32 * q + lane, half, rt);
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, (uint32_t)g.tmem_cols);
+  }
+}
+
+// ------------------------------------------------------------ epilogues
+// contiguous tiles: groups [tile*G, tile*G + G), rows tile*G*Tp ...
+struct ContigTiles {
+  int n_groups;
+  __device__ TileInfo tile(int tx, const TcArgs& g) const {
+    TileInfo t{};
+    t.g0 = tx * g.G;
+    t.ng = min(g.G, n_groups - t.g0);
+    t.row0 = t.g0 * g.Tp;
+    return t;
+  }
+};
+
+struct EpiTcLayer : ContigTiles {
+  int n, ld;  // electrons per walker, activation row width (n_out)
+  StSplit out;
+  bool has_resid;
+  const float* Gb;
+  const float* bias;
+  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int f_loc, int half,
+                      const ResidTiles& rt) const {
+    const bool fok = f < g.n_out;
+    const int N = g.n_out;
+    const float b = fok ? bias[f] : 0.f;
+    if (g.T == 1) {
+      for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
+        float v[16], gbv[16];
+        ptx::tmem_ld16(taddr + c0, v);
+        if (!fok) continue;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          int lg = c0 + j;
+          gbv[j] = lg < ti.ng ? Gb[(size_t)((ti.g0 + lg) / n) * N + f] : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          int lg = c0 + j;
+          if (lg < ti.ng) {
+            float h = tanhf(v[j] + gbv[j] + b);
+            if (has_resid) h = (h + rt.get(lg, f_loc)) * kRsqrt2;
+            out.put((size_t)(ti.g0 + lg), f, h);  // Tp == 1
+          }
+        }
+      }
+      return;
+    }
+    for (int lg = half; lg < ti.ng; lg += 2) {
+      const int gi = ti.g0 + lg;
+      const int w = gi / n;
+      const size_t r0 = (size_t)gi * g.Tp;
+      const int c0 = lg * g.Tp;
+      const float* gb = Gb + (size_t)w * g.Tp * N + f;
+      float h = 0.f, d1 = 0.f, zL = 0.f, S = 0.f;
+      for (int q4 = 0; q4 < g.Tp / 4; ++q4) {
+        float gbv[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int t = 4 * q4 + e;
+          gbv[e] = (fok && t < g.T) ? gb[(size_t)t * N] : 0.f;
+        }
+        float v[4];
+        ptx::tmem_ld4(taddr + c0 + 4 * q4, v);
+        if (!fok) continue;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int t = 4 * q4 + e;
+          float r = 0.f;
+          if (has_resid && t < g.T) r = rt.get(c0 + t, f_loc);
+          if (t == 0) {
+            h = tanhf(v[e] + gbv[e] + b);
+            d1 = 1.f - h * h;
+            out.put(r0, f, has_resid ? (h + r) * kRsqrt2 : h);
+          } else if (t == 1) {
+            zL = v[e] + gbv[e];
+          } else if (t < g.T) {
+            float z = v[e] + gbv[e];
+            S = fmaf(z, z, S);
+            float y = d1 * z;
+            out.put(r0 + t, f, has_resid ? (y + r) * kRsqrt2 : y);
+          } else {
+            out.put(r0 + t, f, 0.f);
+          }
+        }
+      }
+      if (fok) {
+        float y = d1 * zL - 2.f * h * d1 * S;
+        if (has_resid) y = (y + rt.get(c0 + 1, f_loc)) * kRsqrt2;
+        out.put(r0 + 1, f, y);
+      }
+    }
+  }
+};
+
+struct EpiTcStore : ContigTiles {
+  float* out;
+  int ld;
+  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int, int half,
+                      const ResidTiles&) const {
+    const bool fok = f < g.n_out;
+    for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
+      float v[16];
+      ptx::tmem_ld16(taddr + c0, v);
+      if (!fok) continue;
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        if (c0 + j < ti.ng) out[(size_t)(ti.row0 + c0 + j) * ld + f] = v[j];
+    }
+  }
+};
+
+// Orbital tiles never straddle a (walker, spin channel): tile -> (w, s, chunk).
+struct EpiTcOrbital {
+  int n, n_up, split, K, natom, env_abs, tiles_up, tiles_per_walker;
+  const float* pi[2];
+  const float* sigma[2];
+  const float* rae;
+  const float* aevec;
+  float* A;
+  int n_rows;  // B * n (value-only passes)
+  __device__ TileInfo tile(int tx, const TcArgs& g) const {
+    TileInfo t{};
+    if (g.T == 1) {
+      // value-only: contiguous 256-row tiles over all walkers, one pass per
+      // spin channel; rows of the other channel are skipped in the epilogue
+      const int tpc = (n_rows + 255) / 256;
+      t.a_sel = split ? tx / tpc : 0;
+      t.g0 = (tx % tpc) * 256;
+      t.ng = min(256, n_rows - t.g0);
+      t.row0 = t.g0;
+      return t;
+    }
+    const int w = tx / tiles_per_walker, r = tx % tiles_per_walker;
+    int s = 0, chunk = r, i0 = 0, ns = n;
+    if (split) {
+      s = r < tiles_up ? 0 : 1;
+      chunk = s == 0 ? r : r - tiles_up;
+      i0 = s == 0 ? 0 : n_up;
+      ns = s == 0 ? n_up : n - n_up;
+    }
+    t.a_sel = s;
+    t.w = w;
+    t.i0 = i0 + chunk * g.G;
+    t.ng = min(g.G, ns - chunk * g.G);
+    t.row0 = (w * n + t.i0) * g.Tp;
+    return t;
+  }
+  // envelope value, gradient (wrt the electron) and Laplacian for column (k, j)
+  __device__ void envelope(int s, int w, int i, int k, int j, int T, float* e) const {
+    const float* ra = rae + ((size_t)w * n + i) * natom;
+    const float* av = aevec + ((size_t)w * n + i) * natom * 3;
+    float e0 = 0.f, ex = 0.f, ey = 0.f, ez = 0.f, el = 0.f;
+    for (int I = 0; I < natom; ++I) {
+      float pv = pi[s][((size_t)j * natom + I) * K + k];
+      float sv = sigma[s][((size_t)j * natom + I) * K + k];
+      float r = ra[I];
+      float se = env_abs ? fabsf(sv) : sv;
+      float ev = pv * expf(-se * r);
+      e0 += ev;
+      if (T > 1) {
+        float gr = -se * ev / r;
+        ex = fmaf(gr, av[3 * I], ex);
+        ey = fmaf(gr, av[3 * I + 1], ey);
+        ez = fmaf(gr, av[3 * I + 2], ez);
+        el += ev * (se * se - 2.0f * se / r);
+      }
+    }
+    e[0] = e0; e[1] = ex; e[2] = ey; e[3] = ez; e[4] = el;
+  }
+  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int, int half,
+                      const ResidTiles&) const {
+    const bool fok = f < g.n_out;
+    const int k = fok ? f / n : 0, j = fok ? f % n : 0;
+    const size_t ts = (size_t)n * n;
+    if (g.T == 1) {
+      for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
+        float v[16];
+        ptx::tmem_ld16(taddr + c0, v);
+        if (!fok) continue;
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+          int lg = c0 + jj;
+          if (lg < ti.ng) {
+            int gi = ti.g0 + lg, w = gi / n, i = gi % n;
+            if (split && (i < n_up ? 0 : 1) != ti.a_sel) continue;
+            float e[5];
+            envelope(ti.a_sel, w, i, k, j, 1, e);
+            A[((size_t)w * K + k) * ts + (size_t)i * n + j] = v[jj] * e[0];
+          }
+        }
+      }
+      return;
+    }
+    for (int lg = half; lg < ti.ng; lg += 2) {
+      const int i = ti.i0 + lg;
+      float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (fok) envelope(ti.a_sel, ti.w, i, k, j, g.T, e);
+      float* dst = A + (((size_t)ti.w * K + k) * g.Tp) * ts + (size_t)i * n + j;
+      const int ti3 = 2 + 3 * i;
+      float o0 = 0.f, oL = 0.f, cross = 0.f;
+      for (int q4 = 0; q4 < g.Tp / 4; ++q4) {
+        float v[4];
+        ptx::tmem_ld4(taddr + lg * g.Tp + 4 * q4, v);
+        if (!fok) continue;
+#pragma unroll
+        for (int ee = 0; ee < 4; ++ee) {
+          const int t = 4 * q4 + ee;
+          const float o = v[ee];
+          if (t == 0) {
+            o0 = o;
+            dst[0] = o * e[0];
+          } else if (t == 1) {
+            oL = o;
+          } else if (t < g.T) {
+            float val = o * e[0];
+            int c = t - ti3;
+            if (c >= 0 && c < 3) {
+              val = fmaf(o0, e[1 + c], val);
+              cross = fmaf(o, e[1 + c], cross);
+            }
+            dst[(size_t)t * ts] = val;
+          } else {
+            dst[(size_t)t * ts] = 0.f;
+          }
+        }
+      }
+      if (fok) dst[ts] = oL * e[0] + 2.0f * cross + o0 * e[4];
+    }
+  }
+};
+
+// ------------------------------------------------------------ host side
+int tc_padded_tangents(int T) {
+  if (T <= 1) return 1;
+  for (int Tp = (T + 3) / 4 * 4; Tp <= 256; Tp += 4)
+    if (tc_groups_per_tile(Tp) > 0) return Tp;
+  return -1;
+}
+
+int tc_groups_per_tile(int Tp) {
+  if (Tp == 1) return 256;
+  for (int G = 256 / Tp; G >= 1; --G)
+    if ((G * Tp) % 16 == 0) return G;
+  return 0;
+}
+
+bool tc_layer_supported(int k1, int k2, int n_out) {
+  return k1 % kKChunk == 0 && k2 > 0 && k2 <= 256 && n_out >= 16;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 3-D map over two bf16 planes: dims (k_extent, rows, 2), box (64, box_rows, 1).
+static qmc_status make_map(CUtensorMap* m, const void* base, int k_extent, size_t rows, int ld,
+                           size_t plane, int box_rows) {
+  auto enc = encoder();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled is unavailable");
+    return QMC_ERR_UNSUPPORTED;
+  }
+  cuuint64_t dims[3] = {(cuuint64_t)k_extent, (cuuint64_t)rows, 2};
+  cuuint64_t strides[2] = {(cuuint64_t)ld * 2, (cuuint64_t)plane * 2};
+  cuuint32_t box[3] = {(cuuint32_t)kKChunk, (cuuint32_t)box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d): k=%d rows=%zu ld=%d plane=%zu box_rows=%d", (int)r,
+              k_extent, rows, ld, plane, box_rows);
+    return QMC_ERR_CUDA;
+  }
+  return QMC_OK;
+}
+
+static int tmem_cols_for(int n_cols) {
+  int c = 32;
+  while (c < n_cols) c <<= 1;
+  return c;
+}
+
+template <class Epi>
+static qmc_status launch(cudaStream_t s, const CUtensorMap& A0, const CUtensorMap& A1, const CUtensorMap& B1,
+                         const CUtensorMap& B2, TcArgs g, int n_tiles, const Epi& epi) {
+  if (n_tiles <= 0) return QMC_OK;
+  const int stage_bytes = 2 * kATile + 2 * g.n_cols * kKChunk * 2;
+  g.stages = std::min(4, (200 * 1024) / stage_bytes);
+  if (g.stages < 2) {
+    set_error("tile of %d columns does not fit two pipeline stages", g.n_cols);
+    return QMC_ERR_SHAPE;
+  }
+  g.tmem_cols = tmem_cols_for(g.n_cols);
+  const size_t smem = 1024 + (size_t)g.stages * stage_bytes + 256;
+  // the opt-in attribute is per device and kernel; raise it to this launch's need
+  static int attr_dev = -1;
+  static size_t attr_bytes = 0;
+  int dev;
+  QMC_CUDA(cudaGetDevice(&dev));
+  if (attr_dev != dev || attr_bytes < smem) {
+    QMC_CUDA(cudaFuncSetAttribute(k_tc_gemm<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_dev = dev;
+    attr_bytes = smem;
+  }
+  dim3 grid(n_tiles, (g.n_out + 127) / 128);
+  k_tc_gemm<Epi><<<grid, kTcThreads, smem, s>>>(A0, A1, B1, B2, g, epi);
+  QMC_CUDA(cudaGetLastError());
+  return QMC_OK;
+}
+
+qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
+  const int G = tc_groups_per_tile(a.Tp);
+  if (G <= 0 || !tc_layer_supported(a.k1, a.k2, a.n_out)) {
+    set_error("tensor-core layer: unsupported shape (Tp=%d k1=%d k2=%d n_out=%d)", a.Tp, a.k1, a.k2, a.n_out);
+    return QMC_ERR_SHAPE;
+  }
+  const size_t rows = (size_t)a.n_groups * a.Tp;
+  TcArgs g{};
+  g.G = G;
+  g.Tp = a.Tp;
+  g.T = a.T;
+  g.n_cols = G * a.Tp;
+  g.k1_chunks = a.k1 / kKChunk;
+  g.k_chunks = g.k1_chunks + (a.k2 + kKChunk - 1) / kKChunk;
+  g.n_out = a.n_out;
+  g.err = a.err;
+  CUtensorMap mA, mB1, mB2;
+  const int kw = a.k1 + a.k2;
+  QMC_TRY(make_map(&mA, a.Wt, kw, a.n_out, kw, (size_t)a.n_out * kw, 128));
+  QMC_TRY(make_map(&mB1, a.X, a.k1, rows, a.k1, a.x_plane, g.n_cols));
+  QMC_TRY(make_map(&mB2, a.G2, a.k2, rows, a.k2, a.g2_plane, g.n_cols));
+  if (a.residual && (a.k1 != a.n_out || a.k1 < 2 * kKChunk || a.n_out % 128)) {
+    set_error("tensor-core layer: residual needs equal widths that are multiples of 128 (got %d -> %d)", a.k1,
+              a.n_out);
+    return QMC_ERR_SHAPE;
+  }
+  g.resid_last = a.residual ? 1 : 0;
+  EpiTcLayer e{};
+  e.n_groups = a.n_groups;
+  e.n = a.n;
+  e.ld = a.n_out;
+  e.has_resid = a.residual;
+  e.out = StSplit{a.out, a.n_out, a.out_plane};
+  e.Gb = a.Gb;
+  e.bias = a.bias;
+  return launch(s, mA, mA, mB1, mB2, g, (a.n_groups + G - 1) / G, e);
+}
+
+qmc_status tc_store_gemm(cudaStream_t s, const TcStoreArgs& a) {
+  TcArgs g{};
+  g.G = 256;
+  g.Tp = 1;
+  g.T = 1;
+  g.n_cols = 256;
+  g.k1_chunks = (a.k + kKChunk - 1) / kKChunk;
+  g.k_chunks = g.k1_chunks;
+  g.n_out = a.n_out;
+  g.err = a.err;
+  CUtensorMap mA, mB;
+  QMC_TRY(make_map(&mA, a.Wt, a.k, a.n_out, a.k, (size_t)a.n_out * a.k, 128));
+  QMC_TRY(make_map(&mB, a.X, a.k, a.n_rows, a.k, a.x_plane, 256));
+  EpiTcStore e{};
+  e.n_groups = a.n_rows;
+  e.out = a.out;
+  e.ld = a.n_out;
+  return launch(s, mA, mA, mB, mB, g, (a.n_rows + 255) / 256, e);
+}
+
+qmc_status tc_orbitals(cudaStream_t s, const TcOrbitalArgs& a) {
+  const int G = tc_groups_per_tile(a.Tp);
+  if (G <= 0 || a.k % kKChunk) {
+    set_error("tensor-core orbitals: unsupported shape (Tp=%d k=%d)", a.Tp, a.k);
+    return QMC_ERR_SHAPE;
+  }
+  const size_t rows = (size_t)a.B * a.n * a.Tp;
+  TcArgs g{};
+  g.G = G;
+  g.Tp = a.Tp;
+  g.T = a.T;
+  g.n_cols = a.T == 1 ? 256 : G * a.Tp;
+  g.k1_chunks = a.k / kKChunk;
+  g.k_chunks = g.k1_chunks;
+  g.n_out = a.norb;
+  g.err = a.err;
+  CUtensorMap mA0, mA1, mB;
+  QMC_TRY(make_map(&mA0, a.Wt[0], a.k, a.norb, a.k, (size_t)a.norb * a.k, 128));
+  QMC_TRY(make_map(&mA1, a.split ? a.Wt[1] : a.Wt[0], a.k, a.norb, a.k, (size_t)a.norb * a.k, 128));
+  QMC_TRY(make_map(&mB, a.X, a.k, rows, a.k, a.x_plane, g.n_cols));
+  EpiTcOrbital e{};
+  e.n = a.n;
+  e.n_up = a.n_up;
+  e.split = a.split;
+  e.K = a.K;
+  e.natom = a.natom;
+  e.env_abs = a.env_abs;
+  if (a.split) {
+    e.tiles_up = (a.n_up + G - 1) / G;
+    e.tiles_per_walker = e.tiles_up + (a.n - a.n_up + G - 1) / G;
+  } else {
+    e.tiles_up = (a.n + G - 1) / G;
+    e.tiles_per_walker = e.tiles_up;
+  }
+  e.n_rows = a.B * a.n;
+  const int n_tiles = a.T == 1 ? (a.split ? 2 : 1) * ((e.n_rows + 255) / 256) : a.B * e.tiles_per_walker;
+  for (int c = 0; c < 2; ++c) {
+    e.pi[c] = a.pi[a.split ? c : 0];
+    e.sigma[c] = a.sigma[a.split ? c : 0];
+  }
+  e.rae = a.rae;
+  e.aevec = a.aevec;
+  e.A = a.A;
+  return launch(s, mA0, mA1, mB, mB, g, n_tiles, e);
+}
+
 }  // namespace qmc

@@ -1,0 +1,290 @@
+"""GPU parity of the FermiNet path (through the C ABI) against the CPU oracle.
+
+Tolerances (plain FP32 form vs the FP64 oracle):
+  * sign of psi: bit-exact per walker;
+  * log|psi| and E_L: max and mean absolute error at most 3x those of the
+    oracle's own FP32 evaluation of the same walkers, plus 1e-5 relative
+    (log|psi|) or 1e-4 Ha (E_L); the batch-mean E_L within 0.5 mHa.  Walkers
+    close to a node of a random-initialised FermiNet are ill-conditioned in
+    any FP32 evaluation, so a per-walker 1e-4 Ha bound holds only for the
+    fraction of walkers recorded in parity_stats ("frac_within_1e-4").
+Mixed (split-BF16) form, on walkers equilibrated by MH: signs bit-exact,
+log|psi| within 1e-3 relative, batch-mean E_L within 0.5 mHa of FP64.
+MH: draws injected into both sides; the accept mask is bit-exact except
+near-ties |ratio - log u| < 1e-4, which are excluded and counted.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import (full_cfg, hydrogenic_tree, oracle_cfg, oracle_forward, oracle_local_energy, setup,
+                     small_cfg)
+from jaqmc_gb300 import _native
+from jaqmc_gb300 import params as P
+from jaqmc_gb300 import systems as S
+from oracle import ferminet as OF
+from oracle import mcmc as OM
+from oracle import philox as OP
+
+pytestmark = pytest.mark.gpu
+OUT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
+
+
+def _record(name, stats):
+    os.makedirs(OUT, exist_ok=True)
+    path = os.path.join(OUT, "parity_stats.jsonl")
+    with open(path, "a") as f:
+        f.write(json.dumps({"case": name, **stats}) + "\n")
+
+
+def _model(mol, cfg, flat, dev, precision="fp32"):
+    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision=precision, device=dev)
+    m.set_params(torch.as_tensor(flat, device=dev))
+    return m
+
+
+CASES = {
+    "Li-full": (S.lithium, lambda: full_cfg((2, 1)), 48),
+    "Li-small-nosplit": (S.lithium, lambda: small_cfg((2, 1), orbitals_spin_split=False), 16),
+    "H-small": (S.hydrogen, lambda: small_cfg((1, 0)), 16),
+    "He-triplet": (lambda: S.make_molecule("He", [2], [[0, 0, 0]], (2, 0)), lambda: small_cfg((2, 0)), 16),
+    "He-down": (lambda: S.make_molecule("He", [2], [[0, 0, 0]], (0, 2)), lambda: small_cfg((0, 2)), 16),
+    "CH4-full": (S.methane, lambda: full_cfg((5, 5)), 32),
+    "N2-full": (S.nitrogen_dimer, lambda: full_cfg((7, 7)), 32),
+    "N2-isotropic": (S.nitrogen_dimer, lambda: full_cfg((7, 7), envelope="isotropic", ndets=4), 32),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_forward_parity(case, cuda_device):
+    molf, cfgf, B = CASES[case]
+    mol, cfg = molf(), cfgf()
+    tree, flat, x = setup(mol, cfg, B)
+    m = _model(mol, cfg, flat, cuda_device)
+    lp, sg, fl = m.forward(torch.as_tensor(x, device=cuda_device))
+    r64 = oracle_forward(tree, cfg, mol, x)
+    r32 = oracle_forward(tree, cfg, mol, x, dtype=torch.float32)
+    ref = r64["logpsi"].numpy()
+    err = np.abs(lp.cpu().numpy() - ref)
+    e32 = np.abs(r32["logpsi"].double().numpy() - ref)
+    tol = 1e-5 * np.maximum(1.0, np.abs(ref)).max()
+    _record(f"forward/{case}", {"max_rel": float((err / np.maximum(1, np.abs(ref))).max()),
+                                "median_abs": float(np.median(err)), "oracle32_max_abs": float(e32.max()),
+                                "n": B})
+    assert np.array_equal(sg.cpu().numpy(), r64["sign_logpsi"].numpy())
+    assert err.max() <= 3 * e32.max() + tol, (err.max(), e32.max())
+    assert err.mean() <= 3 * e32.mean() + tol, (err.mean(), e32.mean())
+    assert (fl.cpu().numpy() & _native.FLAG_NONFINITE).sum() == 0
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_local_energy_parity(case, cuda_device):
+    molf, cfgf, B = CASES[case]
+    mol, cfg = molf(), cfgf()
+    tree, flat, x = setup(mol, cfg, B)
+    m = _model(mol, cfg, flat, cuda_device)
+    out = m.local_energy(torch.as_tensor(x, device=cuda_device))
+    r64 = oracle_local_energy(tree, cfg, mol, x)
+    r32 = oracle_local_energy(tree, cfg, mol, x, dtype=torch.float32)
+    ref = r64["e_local"].numpy()
+    got = out["e_local"].cpu().numpy()
+    err = np.abs(got - ref)
+    e32 = np.abs(r32["e_local"].double().numpy() - ref)
+    _record(f"local_energy/{case}", {"max_abs": float(err.max()), "median_abs": float(np.median(err)),
+                                     "frac_within_1e-4": float((err <= 1e-4).mean()),
+                                     "mean_err": float(got.mean() - ref.mean()),
+                                     "oracle32_max_abs": float(e32.max()),
+                                     "oracle32_median_abs": float(np.median(e32)), "n": B})
+    # robust statistics: the tails of two FP32 evaluations near nodes differ by luck
+    assert np.median(err) <= 3 * np.median(e32) + 1e-4, (np.median(err), np.median(e32))
+    assert np.quantile(err, 0.9) <= 3 * np.quantile(e32, 0.9) + 1e-4
+    assert err.max() <= 20 * e32.max() + 1e-3, (err.max(), e32.max())
+    assert abs(got.mean() - ref.mean()) <= 3 * e32.mean() + 5e-4
+    np.testing.assert_allclose(out["potential"].cpu().numpy(), r64["potential"].numpy(), rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(out["logpsi"].cpu().numpy(), r64["logpsi"].numpy(), rtol=1e-4, atol=1e-4)
+
+
+def test_hydrogen_atom_exact(cuda_device):
+    mol = S.hydrogen()
+    cfg = small_cfg((1, 0), ndets=2)
+    tree = hydrogenic_tree(cfg, 1, sigma=1.0)
+    flat = P.flatten(tree, P.ferminet_leaves(cfg, 1))
+    x = S.init_walkers(mol, 256, seed=5)
+    m = _model(mol, cfg, flat, cuda_device)
+    out = m.local_energy(torch.as_tensor(x, device=cuda_device))
+    np.testing.assert_allclose(out["e_local"].cpu().numpy(), -0.5, atol=2e-5)
+
+
+def test_hydrogenic_helium_exact(cuda_device):
+    mol = S.make_molecule("He", [2], [[0, 0, 0]], (1, 1))
+    cfg = small_cfg((1, 1), ndets=2)
+    tree = hydrogenic_tree(cfg, 1, sigma=2.0)
+    orb = tree["params"]["orbital_layer"]["SplitChannelDense_0"]
+    orb["DenseGeneral_0"]["kernel"][:] = 0.0
+    orb["DenseGeneral_0"]["kernel"][:, :, 0] = 0.5
+    orb["DenseGeneral_1"]["kernel"][:] = 0.0
+    orb["DenseGeneral_1"]["kernel"][:, :, 1] = 0.5
+    flat = P.flatten(tree, P.ferminet_leaves(cfg, 1))
+    x = S.init_walkers(mol, 256, seed=6)
+    m = _model(mol, cfg, flat, cuda_device)
+    out = m.local_energy(torch.as_tensor(x, device=cuda_device))
+    r12 = np.linalg.norm(x[:, 0] - x[:, 1], axis=-1)
+    np.testing.assert_allclose(out["e_local"].cpu().numpy(), -4.0 + 1.0 / r12, rtol=2e-5, atol=2e-5)
+
+
+def test_same_spin_swap_flips_sign(cuda_device):
+    mol = S.lithium()
+    cfg = full_cfg((2, 1))
+    tree, flat, x = setup(mol, cfg, 64)
+    m = _model(mol, cfg, flat, cuda_device)
+    xs = x.copy()
+    xs[:, [0, 1]] = xs[:, [1, 0]]
+    lp, sg, _ = m.forward(torch.as_tensor(x, device=cuda_device))
+    lp2, sg2, _ = m.forward(torch.as_tensor(xs, device=cuda_device))
+    assert torch.equal(sg, -sg2)
+    np.testing.assert_allclose(lp.cpu().numpy(), lp2.cpu().numpy(), rtol=5e-4)
+
+
+def test_coincident_electrons_flag_singular(cuda_device):
+    """Host-injected failure: two same-spin electrons at one point make every
+    determinant exactly singular; the walker is flagged, nothing traps."""
+    mol = S.lithium()
+    cfg = full_cfg((2, 1), ndets=4)
+    tree, flat, x = setup(mol, cfg, 8)
+    x[3, 1] = x[3, 0]
+    m = _model(mol, cfg, flat, cuda_device)
+    lp, sg, fl = m.forward(torch.as_tensor(x, device=cuda_device))
+    fl = fl.cpu().numpy()
+    assert fl[3] & _native.FLAG_SINGULAR and fl[3] & _native.FLAG_NONFINITE
+    assert not np.isfinite(lp[3].item())
+    assert np.isfinite(lp.cpu().numpy()[np.arange(8) != 3]).all()
+    # the model stays usable
+    lp2, _, _ = m.forward(torch.as_tensor(x[:3], device=cuda_device))
+    assert np.isfinite(lp2.cpu().numpy()).all()
+
+
+def test_mh_internal_draws_equal_injected(cuda_device):
+    mol = S.nitrogen_dimer()
+    cfg = full_cfg((7, 7), ndets=4)
+    tree, flat, x = setup(mol, cfg, 128)
+    m = _model(mol, cfg, flat, cuda_device)
+    nz, uz = m.mh_draws(128, 4, seed=11, counter=5)
+    a = torch.as_tensor(x, device=cuda_device).clone()
+    b = torch.as_tensor(x, device=cuda_device).clone()
+    _, lpa, acca, _ = m.mh_steps(a, 4, 0.02, 11, 5)
+    _, lpb, accb, _ = m.mh_steps(b, 4, 0.02, 11, 5, normals=nz, uniforms=uz)
+    assert torch.equal(a, b) and torch.equal(lpa, lpb) and torch.equal(acca, accb)
+
+
+def test_philox_draws_match_oracle(cuda_device):
+    mol = S.methane()
+    cfg = small_cfg((5, 5))
+    tree, flat, x = setup(mol, cfg, 4)
+    m = _model(mol, cfg, flat, cuda_device)
+    nz, uz = m.mh_draws(300, 3, seed=(7 << 32) + 9, counter=(1 << 32) + 3)
+    for s in range(3):
+        zo, uo = OP.mh_draws((7 << 32) + 9, (1 << 32) + 3 + s, 300, mol.n_electrons)
+        assert np.array_equal(uo, uz[s].cpu().numpy())
+        np.testing.assert_allclose(nz[s].cpu().numpy(), zo, atol=2e-5)
+
+
+@pytest.mark.parametrize("case", ["Li-full", "N2-full"])
+def test_mh_matches_oracle(case, cuda_device):
+    molf, cfgf, _ = CASES[case]
+    mol, cfg = molf(), cfgf()
+    B, steps = 64, 3
+    tree, flat, x = setup(mol, cfg, B)
+    m = _model(mol, cfg, flat, cuda_device)
+    nz, uz = m.mh_draws(B, steps, seed=2, counter=0)
+    xg = torch.as_tensor(x, device=cuda_device).clone()
+    _, lpg, accg, _ = m.mh_steps(xg, steps, 0.02, 2, 0)
+    f = OF.logpsi_fn(tree, oracle_cfg(cfg), mol.atoms)
+    xo, lpo, acco, ratios = OM.mh_steps(f, torch.as_tensor(x, dtype=torch.float64), nz.cpu().double(),
+                                        uz.cpu().double(), 0.02)
+    near = ((ratios - torch.log(uz.cpu().double())).abs() < 1e-4).any(0).numpy()
+    keep = ~near
+    _record(f"mh/{case}", {"excluded_near_ties": int(near.sum()), "n": B,
+                           "accepts_gpu": int(accg.sum()), "accepts_oracle": int(acco.sum())})
+    assert keep.sum() >= B - 2
+    assert np.array_equal(accg.cpu().numpy()[keep], acco.numpy()[keep])
+    np.testing.assert_allclose(xg.cpu().numpy()[keep], xo.numpy()[keep], atol=1e-5)
+    np.testing.assert_allclose(lpg.cpu().numpy()[keep], lpo.numpy()[keep], rtol=1e-4, atol=1e-4)
+
+
+def test_reduce_mean_var(cuda_device):
+    g = torch.Generator().manual_seed(0)
+    x = torch.randn(10007, generator=g) * 3 + 1
+    x[5] = float("nan")
+    mv = _native.reduce_mean_var(x.to(cuda_device)).cpu().numpy()
+    xs = x.double().numpy()
+    m = np.nanmean(xs)
+    np.testing.assert_allclose(mv, [m, np.nanmean(xs * xs) - m * m], rtol=1e-12)
+
+
+def test_workspace_and_argument_errors(cuda_device):
+    mol = S.lithium()
+    cfg = small_cfg((2, 1))
+    tree, flat, x = setup(mol, cfg, 4)
+    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, device=cuda_device)
+    with pytest.raises(_native.QmcError):  # parameters not set
+        m.forward(torch.as_tensor(x, device=cuda_device))
+    with pytest.raises(_native.QmcError):
+        m.set_params(torch.zeros(3, device=cuda_device))
+    m.set_params(torch.as_tensor(flat, device=cuda_device))
+    lib = _native.load()
+    e = torch.as_tensor(x, device=cuda_device)
+    out = torch.empty(4, device=cuda_device)
+    st = lib.qmc_forward(m.h, 4, e.data_ptr(), out.data_ptr(), None, None, out.data_ptr(), 16,
+                         _native.stream_handle())
+    assert st == 6 and b"workspace" in lib.qmc_last_error()
+
+
+def _equilibrated(mol, cfg, flat, dev, B, steps=300, stddev=0.15, seed=3):
+    """Walkers sampled from |psi|^2 by the FP32 GPU sampler (burn-in)."""
+    m = _model(mol, cfg, flat, dev)
+    x = torch.as_tensor(S.init_walkers(mol, B, seed=1), device=dev)
+    m.mh_steps(x, steps, stddev, seed, 0)
+    return x.cpu().numpy()
+
+
+@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full"])
+def test_mixed_form_on_equilibrated_walkers(case, cuda_device):
+    molf, cfgf, _ = CASES[case]
+    mol, cfg = molf(), cfgf()
+    tree, flat, _ = setup(mol, cfg, 1)
+    x = _equilibrated(mol, cfg, flat, cuda_device, 64)
+    mm = _model(mol, cfg, flat, cuda_device, precision="mixed")
+    xd = torch.as_tensor(x, device=cuda_device)
+    lp, sg, _ = mm.forward(xd)
+    out = mm.local_energy(xd)
+    assert mm.check_error() == 0
+    r64 = oracle_local_energy(tree, cfg, mol, x)
+    ref_lp = r64["logpsi"].numpy()
+    rel = np.abs(lp.cpu().numpy() - ref_lp) / np.maximum(1, np.abs(ref_lp))
+    e = out["e_local"].cpu().numpy() - r64["e_local"].numpy()
+    _record(f"mixed/{case}", {"logpsi_max_rel": float(rel.max()), "el_median_abs": float(np.median(np.abs(e))),
+                              "el_max_abs": float(np.abs(e).max()), "mean_err": float(e.mean()), "n": len(x)})
+    assert np.array_equal(sg.cpu().numpy(), r64["sign"].numpy())
+    assert rel.max() < 1e-3
+    assert abs(e.mean()) <= 5e-4
+
+
+def test_mixed_mh_runs_and_matches_plain_sampler(cuda_device):
+    """Mixed MH keeps the same draws; its acceptance rate matches the plain
+    form's within sampling noise, and no bounded wait expires."""
+    mol = S.nitrogen_dimer()
+    cfg = full_cfg((7, 7))
+    tree, flat, x = setup(mol, cfg, 512)
+    mp = _model(mol, cfg, flat, cuda_device)
+    mm = _model(mol, cfg, flat, cuda_device, precision="mixed")
+    a = torch.as_tensor(x, device=cuda_device).clone()
+    b = torch.as_tensor(x, device=cuda_device).clone()
+    _, _, acc_p, _ = mp.mh_steps(a, 10, 0.1, 5, 0)
+    _, _, acc_m, fl = mm.mh_steps(b, 10, 0.1, 5, 0)
+    assert mm.check_error() == 0
+    pp, pm = acc_p.sum().item() / 5120, acc_m.sum().item() / 5120
+    assert abs(pp - pm) < 0.03, (pp, pm)
+    assert torch.isfinite(b).all()
