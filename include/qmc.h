@@ -107,6 +107,18 @@ qmc_status qmc_forward(qmc_model* m, int batch, const float* electrons, float* l
                        float* sign, uint8_t* flags, void* workspace, size_t workspace_bytes,
                        cudaStream_t stream);
 
+/* The same forward pass as qmc_forward, for callers that may not allocate
+ * device memory while they run (for example code executing inside another
+ * framework's step or a serving loop that reserves all memory up front).  The
+ * intermediate buffers live in a 64 MiB device array inside this library;
+ * batches whose forward pass needs more are rejected with QMC_ERR_WORKSPACE.
+ * The array is shared by all calls on a device: calls whose GPU work overlaps
+ * race, so serialise them.  The first call on a device resolves the array's
+ * address; make it before any stream capture.  This entry point has no
+ * counterpart in the reference. */
+qmc_status qmc_forward_noalloc(qmc_model* m, int batch, const float* electrons, float* logpsi,
+                               float* sign, uint8_t* flags, cudaStream_t stream);
+
 /* Local energy E_L = KE + V per walker with the forward-Laplacian kinetic
  * energy KE = -1/2 (lap log|psi| + |grad log|psi||^2)
  * (src/jaqmc/estimator/kinetic/euclidean.py:114-135, _common.py:61-73) and the

@@ -10,6 +10,7 @@
 #include "gemm_simt.cuh"
 #include "kernels.cuh"
 #include "profile.cuh"
+#include "plan.cuh"
 #include "stream_tc.cuh"
 
 // Launch `call` as a kernel of profiler class `cls` on stream `s`.
@@ -159,15 +160,6 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
 }
 
 // ------------------------------------------------------------ workspace
-struct Plan {
-  int B, T, Tp, P2, K0p;
-  bool mixed;
-  size_t x0, h1[2], h2[2], g1, gb, g2, rae, aevec, amat, pe, lpsi, sgn, xp, lp, refac, total;
-  size_t act_bytes;  // bytes per one-electron activation (fp32, or two bf16 planes)
-  size_t h1_plane, g1_plane, g2_plane;  // bf16 elements between split planes
-  int dmax, g1max, g2max;
-};
-
 static int tangent_count(const Dims& d, int op) { return op == QMC_OP_LOCAL_ENERGY ? 3 * d.n + 2 : 1; }
 
 // Padded tangent count: the tensor-core path tiles columns by whole groups
@@ -177,7 +169,7 @@ static int padded_tangents(const Dims& d, int T, bool mixed) {
   return mixed ? tc_padded_tangents(T) : T;
 }
 
-static Plan make_plan(const qmc_model* m, int op, int B) {
+Plan make_plan(const qmc_model* m, int op, int B) {
   const Dims& d = m->d;
   Plan p{};
   p.B = B;
@@ -388,7 +380,7 @@ static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cu
 }
 
 // Full evaluation: features -> backbone -> orbitals -> determinants.
-static qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
+qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
                            float* logpsi, float* sign, float* ke, float* el, uint8_t* flags,
                            cudaStream_t s) {
   const Dims& d = m->d;
@@ -406,7 +398,7 @@ static qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* e
   return QMC_OK;
 }
 
-static qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, int op) {
+qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, int op) {
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1) { set_error("batch must be >= 1"); return QMC_ERR_SHAPE; }

@@ -1,0 +1,29 @@
+// Workspace plan and evaluation driver shared by the C-ABI entry points.
+#pragma once
+#include "common.cuh"
+
+namespace qmc {
+
+// Byte offsets of every scratch buffer of one call inside the workspace.
+struct Plan {
+  int B, T, Tp, P2, K0p;
+  bool mixed;
+  size_t x0, h1[2], h2[2], g1, gb, g2, rae, aevec, amat, pe, lpsi, sgn, xp, lp, refac, total;
+  size_t act_bytes;  // bytes per one-electron activation (fp32, or two bf16 planes)
+  size_t h1_plane, g1_plane, g2_plane;  // bf16 elements between split planes
+  int dmax, g1max, g2max;
+};
+
+
+Plan make_plan(const qmc_model* m, int op, int B);
+
+// Validates a call: parameters set, batch >= 1, workspace large enough,
+// supported shapes, model on the current device.
+qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, int op);
+
+// features -> backbone -> orbitals -> determinants for p.B walkers using the
+// scratch buffers of plan p inside ws.
+qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
+                    float* logpsi, float* sign, float* ke, float* el, uint8_t* flags, cudaStream_t s);
+
+}  // namespace qmc
