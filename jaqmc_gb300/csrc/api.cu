@@ -221,10 +221,25 @@ template <typename T>
 static T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
 
 // ------------------------------------------------------------ network
+// Value-only passes fuse each two-electron layer with the next layer's spin
+// means of h2 (and the first layer's means with the features) when the
+// widths and the per-walker pair block fit the fused kernel.
+static bool pair_fused(const Dims& d, int T) {
+  if (T != 1) return false;
+  for (int l = 0; l < d.L; ++l) {
+    if (!d.upd2[l]) continue;
+    const bool w_ok = (d.d2_in[l] == 4 && d.d2[l] == 32) || (d.d2_in[l] == 32 && d.d2[l] == 32);
+    if (!w_ok || (size_t)4 * ((size_t)d.n * d.n * d.d2[l] + (size_t)d.d2_in[l] * d.d2[l]) > 200 * 1024)
+      return false;
+  }
+  return true;
+}
+
 // Plain FP32 form.  One-electron layer l: spin means, broadcast GEMM, main
 // GEMM with the tangent epilogue; then the two-electron update.
 static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
   const Dims& d = m->d;
+  const bool fused = pair_fused(d, p.T);
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
   const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
@@ -243,15 +258,21 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
                                           d.g1_p[l], StF32{G1, d.g1_p[l]}));
     QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
                                                 ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
-    QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
-                                          StF32{G2, d.g2_p[l]}));
+    if (!fused)
+      QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                            StF32{G2, d.g2_p[l]}));
     EpiLayer<StF32> epi{Gb, ar + a.b1[l], StF32{nullptr, dout}, StF32{out, dout}, T};
     if (l > 0 && din == dout) epi.resid = StF32{const_cast<float*>(in), dout};
     QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
                                                    ar + a.w_main[l], dout, dout, epi));
     if (d.upd2[l]) {
-      QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
-                                              ar + a.b2[l], at<float>(ws, p.h2[h2cur ^ 1])));
+      float* h2o = at<float>(ws, p.h2[h2cur ^ 1]);
+      if (fused)
+        QMC_PROF(QMC_KC_PAIR, launch_pair_layer_mean(s, B, n, d.n_up, d.C, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                                     ar + a.b2[l], h2o, d.g2_p[l + 1], StF32{G2, d.g2_p[l + 1]}));
+      else
+        QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                                ar + a.b2[l], h2o));
       h2cur ^= 1;
     }
     cur = (l == 0) ? 0 : cur ^ 1;
@@ -264,6 +285,7 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
 // its broadcast term and the orbitals as split-BF16 tcgen05 GEMMs.
 static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
   const Dims& d = m->d;
+  const bool fused = pair_fused(d, p.T);
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
   const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
@@ -284,8 +306,9 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
                                             StF32{G1, d.g1_p[l]}));
       QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
                                                   ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
-      QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
-                                            StF32{G2, d.g2_p[l]}));
+      if (!fused)
+        QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                              StF32{G2, d.g2_p[l]}));
       EpiLayer<StSplit> epi{Gb, ar + a.b1[l], StSplit{nullptr, dout, 0}, StSplit{out, dout, p.h1_plane}, T};
       QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, X0, dinp, dinp, G2, d.g2_p[l],
                                                      d.g2_p[l], ar + a.w_main[l], dout, dout, epi));
@@ -298,8 +321,9 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
                                             d.g1_p[l], StSplit{G1, d.g1_p[l], p.g1_plane}));
       TcStoreArgs sa{B * Tp, G1, d.g1_p[l], p.g1_plane, m->arena_bf16 + a.t_g1[l], dout, Gb, m->dev_err};
       QMC_PROF_TRY(QMC_KC_BROADCAST, tc_store_gemm(s, sa));
-      QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
-                                            StSplit{G2, d.g2_p[l], p.g2_plane}));
+      if (!fused)
+        QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                              StSplit{G2, d.g2_p[l], p.g2_plane}));
       TcLayerArgs la{};
       la.n_groups = B * n;
       la.n = n;
@@ -323,8 +347,14 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
       QMC_PROF_TRY(QMC_KC_STREAM_LAYER, tc_stream_layer(s, la));
     }
     if (d.upd2[l]) {
-      QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
-                                              ar + a.b2[l], at<float>(ws, p.h2[h2cur ^ 1])));
+      float* h2o = at<float>(ws, p.h2[h2cur ^ 1]);
+      if (fused)  // next layer (>= 1) reads its G2 as split bf16
+        QMC_PROF(QMC_KC_PAIR, launch_pair_layer_mean(s, B, n, d.n_up, d.C, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                                     ar + a.b2[l], h2o, d.g2_p[l + 1],
+                                                     StSplit{at<bf>(ws, p.g2), d.g2_p[l + 1], p.g2_plane}));
+      else
+        QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                                ar + a.b2[l], h2o));
       h2cur ^= 1;
     }
     cur = (l == 0) ? 0 : cur ^ 1;
@@ -386,9 +416,11 @@ qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electron
   const Dims& d = m->d;
   const float* ar = m->arena;
   float* pe = want_pe ? at<float>(ws, p.pe) : nullptr;
+  const bool fused = pair_fused(d, p.T);
   QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
                            ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
-                           at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe));
+                           at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe,
+                           d.n_up, d.C, d.g2_p[0], fused ? at<float>(ws, p.g2) : nullptr));
   int hb = 0;
   if (p.mixed) QMC_TRY(run_backbone_mixed(m, p, ws, s, &hb));
   else QMC_TRY(run_backbone_plain(m, p, ws, s, &hb));

@@ -107,9 +107,16 @@ struct EpiOrbital {
       const float* ra = rae + ((size_t)w * n + i) * natom;
       const float* av = aevec + (((size_t)w * n + i) * natom) * 3;
       float e0 = 0.f, ex = 0.f, ey = 0.f, ez = 0.f, el = 0.f;
+      // all atoms' parameters first, so their loads are in flight together
+      float pvs[8], svs[8];
+#pragma unroll
+      for (int I = 0; I < 8; ++I) {
+        pvs[I] = I < natom ? pi[((size_t)j * natom + I) * K + k] : 0.f;
+        svs[I] = I < natom ? sigma[((size_t)j * natom + I) * K + k] : 0.f;
+      }
       for (int I = 0; I < natom; ++I) {
-        float pv = pi[((size_t)j * natom + I) * K + k];
-        float sv = sigma[((size_t)j * natom + I) * K + k];
+        float pv = I < 8 ? pvs[I] : pi[((size_t)j * natom + I) * K + k];
+        float sv = I < 8 ? svs[I] : sigma[((size_t)j * natom + I) * K + k];
         float r = ra[I];
         float se = env_abs ? fabsf(sv) : sv;
         float ev = pv * expf(-se * r);

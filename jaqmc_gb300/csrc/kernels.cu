@@ -15,7 +15,7 @@ __global__ void k_features(int n, int A, int Tp, int T, int K0p, const float* __
                            const float* __restrict__ atoms, const float* __restrict__ charges,
                            double nuc, float* __restrict__ X0, float* __restrict__ H2,
                            float* __restrict__ rae_g, float* __restrict__ aevec_g,
-                           float* __restrict__ pe) {
+                           float* __restrict__ pe, int n_up, int C, int g2p, float* __restrict__ G2) {
   extern __shared__ float sh[];
   float* xs = sh;                // [n][3]
   float* rs = xs + 3 * n;        // [n][A]
@@ -90,6 +90,26 @@ __global__ void k_features(int n, int A, int Tp, int T, int K0p, const float* __
     }
     Hw[e] = v;
   }
+  if (G2 && T == 1) {
+    // spin means of the ee features over the first electron index:
+    // G2[w*n+i][s*4 + comp] = mean_{a in s} ee[a, i, comp]
+    for (int e = threadIdx.x; e < n * g2p; e += blockDim.x) {
+      const int i = e / g2p, col = e % g2p;
+      float v = 0.f;
+      if (col < 4 * C) {
+        const int sc = col / 4, comp = col % 4;
+        const int a0 = C == 1 ? 0 : (sc == 0 ? 0 : n_up), a1 = C == 1 ? n : (sc == 0 ? n_up : n);
+        float acc = 0.f;
+        for (int a = a0; a < a1; ++a) {
+          if (a == i) continue;
+          float d0 = xs[3 * a] - xs[3 * i], d1 = xs[3 * a + 1] - xs[3 * i + 1], d2 = xs[3 * a + 2] - xs[3 * i + 2];
+          acc += comp == 0 ? sqrtf(d0 * d0 + d1 * d1 + d2 * d2) : (comp == 1 ? d0 : (comp == 2 ? d1 : d2));
+        }
+        v = acc / (float)(a1 - a0);
+      }
+      G2[((size_t)w * n + i) * g2p + col] = v;
+    }
+  }
   if (pe) {
     // block reduction of the potential
     for (int o = 16; o > 0; o >>= 1) vpot += __shfl_xor_sync(0xffffffffu, vpot, o);
@@ -105,10 +125,11 @@ __global__ void k_features(int n, int A, int Tp, int T, int K0p, const float* __
 
 cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, int K0p,
                             const float* electrons, const float* atoms, const float* charges,
-                            double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe) {
+                            double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe,
+                            int n_up, int C, int g2p, float* G2) {
   size_t sm = sizeof(float) * (3 * n + 4 * n * A);
   k_features<<<B, 256, sm, s>>>(n, A, Tp, T, K0p, electrons, atoms, charges, nuc, X0, H2, rae,
-                                aevec, pe);
+                                aevec, pe, n_up, C, g2p, G2);
   return cudaGetLastError();
 }
 
@@ -209,6 +230,102 @@ __global__ void __launch_bounds__(128) k_pair_layer_value(int npairs, const floa
     dst[f4] = o;
   }
 }
+
+// Value-only two-electron layer fused with the spin means of its output (the
+// next layer's <h2>): one block per walker.  Outputs are staged in shared
+// memory and reduced in a fixed order, so the means are deterministic.
+template <int DIN, int DOUT, class Out>
+__global__ void __launch_bounds__(256) k_pair_layer_mean(int n, int n_up, int C, const float* __restrict__ Hin,
+                                                         const float* __restrict__ W, const float* __restrict__ b,
+                                                         float* __restrict__ Hout, int g2p, Out G2) {
+  extern __shared__ float shp[];
+  float* Ws = shp;                  // [DIN][DOUT]
+  float* Os = Ws + DIN * DOUT;      // [n*n][DOUT]
+  for (int e = threadIdx.x; e < DIN * DOUT; e += blockDim.x) Ws[e] = W[e];
+  __syncthreads();
+  const int w = blockIdx.x;
+  const int np = n * n;
+  for (int pr = threadIdx.x; pr < np; pr += blockDim.x) {
+    const size_t gp = (size_t)w * np + pr;
+    float x[DIN];
+    const float4* src = reinterpret_cast<const float4*>(Hin + gp * DIN);
+#pragma unroll
+    for (int q = 0; q < DIN / 4; ++q) {
+      float4 v = src[q];
+      x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+    }
+    float4* dst = reinterpret_cast<float4*>(Hout + gp * DOUT);
+#pragma unroll
+    for (int f4 = 0; f4 < DOUT / 4; ++f4) {
+      float z[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) z[e] = b[4 * f4 + e];
+#pragma unroll
+      for (int k = 0; k < DIN; ++k) {
+        const float4 wv = *reinterpret_cast<const float4*>(&Ws[k * DOUT + 4 * f4]);
+        z[0] = fmaf(x[k], wv.x, z[0]);
+        z[1] = fmaf(x[k], wv.y, z[1]);
+        z[2] = fmaf(x[k], wv.z, z[2]);
+        z[3] = fmaf(x[k], wv.w, z[3]);
+      }
+      float4 o;
+      o.x = tanhf(z[0]); o.y = tanhf(z[1]); o.z = tanhf(z[2]); o.w = tanhf(z[3]);
+      if (DIN == DOUT) {
+        o.x = (o.x + x[4 * f4]) * kRsqrt2;
+        o.y = (o.y + x[4 * f4 + 1]) * kRsqrt2;
+        o.z = (o.z + x[4 * f4 + 2]) * kRsqrt2;
+        o.w = (o.w + x[4 * f4 + 3]) * kRsqrt2;
+      }
+      dst[f4] = o;
+      *reinterpret_cast<float4*>(&Os[pr * DOUT + 4 * f4]) = o;
+    }
+  }
+  __syncthreads();
+  // <h2>_s[i] = mean over a in channel s of h2[a, i]  (first index averaged)
+  for (int e = threadIdx.x; e < n * g2p; e += blockDim.x) {
+    const int i = e / g2p, col = e % g2p;
+    float v = 0.f;
+    if (col < C * DOUT) {
+      const int sc = col / DOUT, f = col % DOUT;
+      const int a0 = C == 1 ? 0 : (sc == 0 ? 0 : n_up), a1 = C == 1 ? n : (sc == 0 ? n_up : n);
+      float acc = 0.f;
+      for (int a = a0; a < a1; ++a) acc += Os[(a * n + i) * DOUT + f];
+      v = acc / (float)(a1 - a0);
+    }
+    G2.put((size_t)w * n + i, col, v);
+  }
+}
+
+template <class Out>
+cudaError_t launch_pair_layer_mean(cudaStream_t s, int B, int n, int n_up, int C, int d_in, int d_out,
+                                   const float* Hin, const float* W, const float* b, float* Hout, int g2p,
+                                   Out G2) {
+  const size_t sm = sizeof(float) * ((size_t)d_in * d_out + (size_t)n * n * d_out);
+  if (sm > 200 * 1024) return cudaErrorNotSupported;
+  static int attr_dev = -1;
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+#define QMC_PLM(DI, DO)                                                                              \
+  if (d_in == DI && d_out == DO) {                                                                   \
+    if (attr_dev != dev) {                                                                           \
+      e = cudaFuncSetAttribute(k_pair_layer_mean<DI, DO, Out>,                                       \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);             \
+      if (e != cudaSuccess) return e;                                                                \
+    }                                                                                                \
+    k_pair_layer_mean<DI, DO, Out><<<B, 256, sm, s>>>(n, n_up, C, Hin, W, b, Hout, g2p, G2);         \
+    attr_dev = dev;                                                                                  \
+    return cudaGetLastError();                                                                       \
+  }
+  QMC_PLM(4, 32)
+  QMC_PLM(32, 32)
+#undef QMC_PLM
+  return cudaErrorNotSupported;
+}
+template cudaError_t launch_pair_layer_mean<StF32>(cudaStream_t, int, int, int, int, int, int, const float*,
+                                                   const float*, const float*, float*, int, StF32);
+template cudaError_t launch_pair_layer_mean<StSplit>(cudaStream_t, int, int, int, int, int, int, const float*,
+                                                     const float*, const float*, float*, int, StSplit);
 
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout) {
@@ -661,9 +778,163 @@ __global__ void k_logdet(int n, int K, int Tp, int T, const float* __restrict__ 
   }
 }
 
+// Value-only determinant stage (MH passes): LU in registers.  A segment of
+// SEG lanes factorises one matrix, lane i holding row i (rows >= n are
+// identity rows), so a warp works on 32/SEG matrices at once.  Pivot search,
+// row exchange and pivot-row broadcast are segment shuffles; the multipliers
+// are not kept (only U's diagonal is needed).  Matrices whose pivot growth
+// exceeds the threshold are re-factorised in FP64 afterwards by warp 0.
+template <int SEG>
+__global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int WB, const float* __restrict__ A,
+                                                      float* __restrict__ logpsi, float* __restrict__ sign,
+                                                      uint8_t* __restrict__ flags) {
+  extern __shared__ double shv[];
+  const int nmat = WB * K;
+  double* lds = shv;                                       // [nmat]
+  float* sgs = reinterpret_cast<float*>(lds + nmat);       // [nmat]
+  int* redo = reinterpret_cast<int*>(sgs + nmat);          // [nmat] re-factorise flags
+  int* singular = redo + nmat;                             // [nmat]
+  char* scratch = reinterpret_cast<char*>(shv) + align_up((size_t)nmat * 16 + 16, 16);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / SEG, i = lane % SEG;
+  const unsigned seg_mask = (SEG == 32) ? 0xffffffffu : (((1u << SEG) - 1u) << (sub * SEG));
+  const int w0 = blockIdx.x * WB;
+  const int mpw = 32 / SEG;
+  for (int base = warp * mpw; base < nmat; base += 8 * mpw) {
+    const int mloc = base + sub;
+    const int w = w0 + mloc / K;
+    const bool active = mloc < nmat && w < B;
+    float r[SEG];
+    const float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
+#pragma unroll
+    for (int j = 0; j < SEG; ++j) r[j] = (active && i < n && j < n) ? Am[i * n + j] : (j == i ? 1.f : 0.f);
+    float amax = 0.f;
+#pragma unroll
+    for (int j = 0; j < SEG; ++j) amax = fmaxf(amax, (i < n) ? fabsf(r[j]) : 0.f);
+#pragma unroll
+    for (int o = SEG / 2; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o, SEG));
+    float sg = 1.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+      if (k < n) {
+        float v = (i >= k && i < n) ? fabsf(r[k]) : -1.f;
+        int vi = i;
+#pragma unroll
+        for (int o = SEG / 2; o > 0; o >>= 1) {
+          float ov = __shfl_xor_sync(0xffffffffu, v, o, SEG);
+          int oi = __shfl_xor_sync(0xffffffffu, vi, o, SEG);
+          if (ov > v || (ov == v && oi < vi)) { v = ov; vi = oi; }
+        }
+        const int p = vi;
+        if (p != k) sg = -sg;
+        const int src = (i == k) ? p : ((i == p) ? k : i);
+#pragma unroll
+        for (int j = 0; j < SEG; ++j)
+          if (j >= k) r[j] = __shfl_sync(0xffffffffu, r[j], src, SEG);
+        float u[SEG];
+#pragma unroll
+        for (int j = 0; j < SEG; ++j)
+          if (j >= k) u[j] = __shfl_sync(0xffffffffu, r[j], k, SEG);
+        if (i > k && i < n && u[k] != 0.f) {
+          const float l = r[k] / u[k];
+#pragma unroll
+          for (int j = 0; j < SEG; ++j)
+            if (j > k) r[j] = fmaf(-l, u[j], r[j]);
+        }
+      }
+    }
+    // diagonal of U sits in r[i] of lane i
+    float d = (i < n) ? r[i] : 1.f;
+    float umax = 0.f;
+#pragma unroll
+    for (int j = 0; j < SEG; ++j)
+      if (j >= i && i < n) umax = fmaxf(umax, fabsf(r[j]));
+    double la = (d != 0.f) ? (double)logf(fabsf(d)) : 0.0;
+    int neg = d < 0.f ? 1 : 0, zero = d == 0.f ? 1 : 0;
+#pragma unroll
+    for (int o = SEG / 2; o > 0; o >>= 1) {
+      umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o, SEG));
+      la += __shfl_xor_sync(0xffffffffu, la, o, SEG);
+      neg += __shfl_xor_sync(0xffffffffu, neg, o, SEG);
+      zero += __shfl_xor_sync(0xffffffffu, zero, o, SEG);
+    }
+    (void)seg_mask;
+    if (active && i == 0) {
+      const bool sing = zero > 0;
+      lds[mloc] = sing ? -INFINITY : la;
+      sgs[mloc] = sing ? 0.f : ((neg & 1) ? -sg : sg);
+      singular[mloc] = sing;
+      redo[mloc] = (!sing && !(umax <= kRefactorGrowth * amax)) ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  // rare: FP64 re-factorisation of matrices with large pivot growth
+  if (warp == 0) {
+    for (int mloc = 0; mloc < nmat; ++mloc) {
+      const int w = w0 + mloc / K;
+      if (w >= B || !redo[mloc]) continue;
+      const float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
+      DetOut o = det_stage<double, 16>(Am, n, 1, scratch, nullptr, true);
+      if (lane == 0) {
+        lds[mloc] = o.ld;
+        sgs[mloc] = o.singular ? 0.f : o.sgn;
+        singular[mloc] = o.singular;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // FP64 signed log-sum-exp per walker, one warp per walker
+  for (int wl = warp; wl < WB; wl += 8) {
+    const int w = w0 + wl;
+    if (w >= B) break;
+    const double* ldw = lds + wl * K;
+    const float* sgw = sgs + wl * K;
+    double lmax = -INFINITY;
+    for (int k = lane; k < K; k += 32)
+      if (sgw[k] != 0.f) lmax = fmax(lmax, ldw[k]);
+    for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    double S = 0.0;
+    int anyredo = 0, anysing = 0;
+    for (int k = lane; k < K; k += 32) {
+      if (sgw[k] != 0.f) S += (double)sgw[k] * exp(ldw[k] - lmax);
+      anyredo |= redo[wl * K + k];
+      anysing |= singular[wl * K + k];
+    }
+    S = warp_sum(S);
+    anyredo = __any_sync(0xffffffffu, anyredo);
+    anysing = __any_sync(0xffffffffu, anysing);
+    if (lane == 0) {
+      double lp = log(fabs(S)) + lmax;
+      if (logpsi) logpsi[w] = (float)lp;
+      if (sign) sign[w] = S > 0 ? 1.f : (S < 0 ? -1.f : 0.f);
+      if (flags)
+        flags[w] = (!isfinite(lp) ? QMC_FLAG_NONFINITE : 0) | (anyredo ? QMC_FLAG_REFACTOR : 0) |
+                   (anysing ? QMC_FLAG_SINGULAR : 0);
+    }
+  }
+}
+
+static cudaError_t launch_logdet_value(cudaStream_t s, int B, int n, int K, const float* A, float* logpsi,
+                                       float* sign, uint8_t* flags) {
+  const int seg = n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32;
+  const int per_pass = 8 * (32 / seg);
+  const int WB = std::max(1, per_pass / K);
+  const size_t sm = align_up((size_t)WB * K * 16 + 16, 16) + DetScratch(n).bytes;
+  const unsigned grid = (unsigned)((B + WB - 1) / WB);
+  switch (seg) {
+    case 4: k_logdet_value<4><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
+    case 8: k_logdet_value<8><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
+    case 16: k_logdet_value<16><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
+    default: k_logdet_value<32><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor) {
+  if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, A, logpsi, sign, flags);
   const int D = T > 1 ? T - 2 : 0;
   const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
   const DetScratch sc(n);

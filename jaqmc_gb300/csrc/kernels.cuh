@@ -13,11 +13,20 @@ namespace qmc {
 // P2 = 5 (value, Laplacian wrt r_i-r_j, d/d(r_i-r_j)_{x,y,z}) when T > 1, else 1.
 cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, int K0p,
                             const float* electrons, const float* atoms, const float* charges,
-                            double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe);
+                            double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe,
+                            int n_up = 0, int C = 0, int g2p = 0, float* G2 = nullptr);
 
 // Two-electron layer h2' = residual(tanh(h2 W + b)) on compact tangent rows.
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout);
+
+// Value-only two-electron layer fused with the spin means of its output
+// (written as the next layer's G2 rows [w*n+i][s*d_out + f]); returns
+// cudaErrorNotSupported for widths or electron counts it does not cover.
+template <class Out>
+cudaError_t launch_pair_layer_mean(cudaStream_t s, int B, int n, int n_up, int C, int d_in, int d_out,
+                                   const float* Hin, const float* W, const float* b, float* Hout, int g2p,
+                                   Out G2);
 
 // Spin-channel means of the one-electron rows: G1[(w*Tp+t)][s*d + f]
 // (padding columns up to the output row width are written as zero).

@@ -23,6 +23,7 @@ constexpr int kKChunk = 64;                      // bf16 per 128-byte swizzle ro
 constexpr int kATile = 128 * kKChunk * 2;        // bytes of one A plane tile
 constexpr long long kWaitCycles = 1000000000LL;  // about 0.5 s at 2 GHz
 constexpr int kErrTimeoutFull = 1, kErrTimeoutEmpty = 2, kErrTimeoutAcc = 3;
+constexpr int kEnvRegs = 8;  // atoms whose envelope parameters stay in registers
 
 struct TileInfo {
   int row0;   // first activation row of the tile (TMA y coordinate)
@@ -370,16 +371,40 @@ struct EpiTcOrbital {
     t.row0 = (w * n + t.i0) * g.Tp;
     return t;
   }
+  // envelope parameters of column (k, j) for the first kEnvRegs atoms, held
+  // in registers across the tile's rows
+  struct EnvParams {
+    float pv[kEnvRegs], se[kEnvRegs];
+  };
+  __device__ void load_params(int s, int k, int j, EnvParams& ep) const {
+#pragma unroll
+    for (int I = 0; I < kEnvRegs; ++I) {
+      float pv = 0.f, se = 0.f;
+      if (I < natom) {
+        pv = pi[s][((size_t)j * natom + I) * K + k];
+        float sv = sigma[s][((size_t)j * natom + I) * K + k];
+        se = env_abs ? fabsf(sv) : sv;
+      }
+      ep.pv[I] = pv;
+      ep.se[I] = se;
+    }
+  }
   // envelope value, gradient (wrt the electron) and Laplacian for column (k, j)
-  __device__ void envelope(int s, int w, int i, int k, int j, int T, float* e) const {
+  __device__ void envelope(int s, int w, int i, int k, int j, int T, float* e, const EnvParams& ep) const {
     const float* ra = rae + ((size_t)w * n + i) * natom;
     const float* av = aevec + ((size_t)w * n + i) * natom * 3;
     float e0 = 0.f, ex = 0.f, ey = 0.f, ez = 0.f, el = 0.f;
     for (int I = 0; I < natom; ++I) {
-      float pv = pi[s][((size_t)j * natom + I) * K + k];
-      float sv = sigma[s][((size_t)j * natom + I) * K + k];
+      float pv, se;
+      if (I < kEnvRegs) {
+        pv = ep.pv[I];
+        se = ep.se[I];
+      } else {
+        pv = pi[s][((size_t)j * natom + I) * K + k];
+        float sv = sigma[s][((size_t)j * natom + I) * K + k];
+        se = env_abs ? fabsf(sv) : sv;
+      }
       float r = ra[I];
-      float se = env_abs ? fabsf(sv) : sv;
       float ev = pv * expf(-se * r);
       e0 += ev;
       if (T > 1) {
@@ -397,6 +422,8 @@ struct EpiTcOrbital {
     const bool fok = f < g.n_out;
     const int k = fok ? f / n : 0, j = fok ? f % n : 0;
     const size_t ts = (size_t)n * n;
+    EnvParams ep;
+    load_params(ti.a_sel, k, j, ep);
     if (g.T == 1) {
       for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
         float v[16];
@@ -409,7 +436,7 @@ struct EpiTcOrbital {
             int gi = ti.g0 + lg, w = gi / n, i = gi % n;
             if (split && (i < n_up ? 0 : 1) != ti.a_sel) continue;
             float e[5];
-            envelope(ti.a_sel, w, i, k, j, 1, e);
+            envelope(ti.a_sel, w, i, k, j, 1, e, ep);
             A[((size_t)w * K + k) * ts + (size_t)i * n + j] = v[jj] * e[0];
           }
         }
@@ -419,7 +446,7 @@ struct EpiTcOrbital {
     for (int lg = half; lg < ti.ng; lg += 2) {
       const int i = ti.i0 + lg;
       float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      if (fok) envelope(ti.a_sel, ti.w, i, k, j, g.T, e);
+      if (fok) envelope(ti.a_sel, ti.w, i, k, j, g.T, e, ep);
       float* dst = A + (((size_t)ti.w * K + k) * g.Tp) * ts + (size_t)i * n + j;
       const int ti3 = 2 + 3 * i;
       float o0 = 0.f, oL = 0.f, cross = 0.f;
