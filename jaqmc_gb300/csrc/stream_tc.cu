@@ -5,12 +5,15 @@
 // (64 bf16 = one 128-byte swizzle row) into a ring of shared-memory stages;
 // warp 1 owns the TMEM allocation and issues the MMAs (3 per K=16 step:
 // hi*hi, hi*lo, lo*hi); warps 2-9 run the epilogue from TMEM, two warps per
-// TMEM lane quarter splitting the tile's columns.  For residual layers the
-// two K chunks holding this CTA's 128 input features are loaded last, so the
-// epilogue reads the residual from those shared-memory tiles.  Every
+// TMEM lane quarter splitting the tile's columns.  The kernel is persistent:
+// one CTA per SM walks a static list of (column tile, 128-feature block) work
+// items with two TMEM accumulators, so the epilogue of one item overlaps the
+// loads and MMAs of the next.  Every
 // mbarrier wait is bounded; on expiry the CTA records an error code, waits
 // (bounded) for its own copies and MMAs, frees TMEM and exits.
 #include <cudaTypedefs.h>
+
+#include <algorithm>
 
 #include "stream_tc.cuh"
 #include "tc_ptx.cuh"
@@ -34,6 +37,7 @@ struct TileInfo {
 };
 
 struct TcArgs {
+  int n_tiles, n_mblocks;  // work items: (column tile, 128-feature block)
   int n_cols;     // columns per tile (G * Tp)
   int G, Tp, T;
   int k_chunks, k1_chunks;
@@ -41,6 +45,7 @@ struct TcArgs {
   int tmem_cols;
   int n_out;
   int resid_last;  // order the K chunks so this CTA's residual features come last
+  int ebuf_bytes;  // epilogue staging bytes per half (0: unused)
   int* err;
 };
 
@@ -73,21 +78,6 @@ __device__ __forceinline__ void chunk_src(const TcArgs& g, int m0, int c, int* b
   *ka = j * kKChunk;
 }
 
-// element (r, k) of a 128-byte-swizzled K-major bf16 tile
-__device__ __forceinline__ float sw128_at(const uint8_t* tile, int r, int k) {
-  const uint8_t* p = tile + r * 128 + ((((k >> 3) ^ (r & 7)) << 4) | ((k & 7) << 1));
-  return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(p));
-}
-
-struct ResidTiles {  // residual operand tiles left in shared memory
-  const uint8_t* hi[2];
-  const uint8_t* lo[2];
-  __device__ __forceinline__ float get(int r, int f_loc) const {
-    const int w = f_loc >> 6, k = f_loc & 63;
-    return sw128_at(hi[w], r, k) + sw128_at(lo[w], r, k);
-  }
-};
-
 __device__ __forceinline__ void report(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
@@ -103,13 +93,17 @@ k_tc_gemm(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUt
   const int stage_bytes = 2 * kATile + 2 * stage_b;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)g.stages * stage_bytes);
   uint64_t* empty = full + g.stages;
-  uint64_t* accb = empty + g.stages;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+  uint64_t* tfull = empty + g.stages;   // [2] accumulator ready
+  uint64_t* tempty = tfull + 2;         // [2] accumulator drained by the epilogue
+  uint64_t* done = tempty + 2;          // all MMAs of this CTA complete
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   int* aborted = reinterpret_cast<int*>(tmem_slot + 1);
+  // per epilogue half: a staging tile of [2 planes][rows][128 features] bf16
+  uint8_t* ebuf0 = smem + (size_t)g.stages * stage_bytes + 256;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * 128;
-  const TileInfo ti = epi.tile(blockIdx.x, g);
+  const int n_items = g.n_tiles * g.n_mblocks;
+  const int acc_cols = g.tmem_cols / 2;  // column offset of the second accumulator
 
   // once any CTA of the call has given up on a wait, the rest skip their work
   __shared__ int skip;
@@ -122,7 +116,11 @@ k_tc_gemm(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUt
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], 1);
     }
-    ptx::mbar_init(accb, 1);
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&tfull[b], 1);
+      ptx::mbar_init(&tempty[b], kEpiWarps);
+    }
+    ptx::mbar_init(done, 1);
     *aborted = 0;
     ptx::fence_mbar_init();
   }
@@ -137,84 +135,105 @@ k_tc_gemm(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUt
 
   if (warp == 0) {
     if (lane == 0) {
-      const CUtensorMap* A = ti.a_sel ? &mapA1 : &mapA0;
-      ptx::prefetch_tmap(A);
+      ptx::prefetch_tmap(&mapA0);
       ptx::prefetch_tmap(&mapB1);
-      int issued = 0;
-      for (int c = 0; c < g.k_chunks; ++c) {
-        const int s = c % g.stages;
-        const uint32_t ph = (uint32_t)(c / g.stages) & 1u;
-        if (!ptx::mbar_wait_bounded(&empty[s], ph ^ 1u, kWaitCycles)) {
-          report(g.err, kErrTimeoutEmpty);
-          atomicExch(aborted, 1);
-          break;
+      int cg = 0;  // chunks issued by this CTA
+      for (int it = blockIdx.x; it < n_items && !*(volatile int*)aborted; it += gridDim.x) {
+        const int mb = it % g.n_mblocks, m0 = mb * 128;
+        const TileInfo ti = epi.tile(it / g.n_mblocks, g);
+        const CUtensorMap* A = ti.a_sel ? &mapA1 : &mapA0;
+        for (int c = 0; c < g.k_chunks; ++c, ++cg) {
+          const int s = cg % g.stages;
+          const uint32_t ph = (uint32_t)(cg / g.stages) & 1u;
+          if (!ptx::mbar_wait_bounded(&empty[s], ph ^ 1u, kWaitCycles)) {
+            report(g.err, kErrTimeoutEmpty);
+            atomicExch(aborted, 1);
+            break;
+          }
+          uint8_t* base = smem + (size_t)s * stage_bytes;
+          int b2, kx, ka;
+          chunk_src(g, m0, c, &b2, &kx, &ka);
+          ptx::mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+          ptx::tma_load_3d(base, A, ka, m0, 0, &full[s]);
+          ptx::tma_load_3d(base + kATile, A, ka, m0, 1, &full[s]);
+          const CUtensorMap* Bm = b2 ? &mapB2 : &mapB1;
+          ptx::tma_load_3d(base + 2 * kATile, Bm, kx, ti.row0, 0, &full[s]);
+          ptx::tma_load_3d(base + 2 * kATile + stage_b, Bm, kx, ti.row0, 1, &full[s]);
         }
-        if (*(volatile int*)aborted) break;
-        uint8_t* base = smem + (size_t)s * stage_bytes;
-        int b2, kx, ka;
-        chunk_src(g, m0, c, &b2, &kx, &ka);
-        ptx::mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
-        ptx::tma_load_3d(base, A, ka, m0, 0, &full[s]);
-        ptx::tma_load_3d(base + kATile, A, ka, m0, 1, &full[s]);
-        const CUtensorMap* Bm = b2 ? &mapB2 : &mapB1;
-        ptx::tma_load_3d(base + 2 * kATile, Bm, kx, ti.row0, 0, &full[s]);
-        ptx::tma_load_3d(base + 2 * kATile + stage_b, Bm, kx, ti.row0, 1, &full[s]);
-        ++issued;
       }
-      // never leave the CTA with copies in flight: wait (bounded) for the
-      // last phase armed on every stage
-      for (int c = issued - g.stages; c < issued; ++c) {
+      // never leave with copies in flight: wait (bounded) for the last phase
+      // armed on every stage
+      for (int c = cg - g.stages; c < cg; ++c) {
         if (c < 0) continue;
-        const int s = c % g.stages;
-        const uint32_t ph = (uint32_t)(c / g.stages) & 1u;
-        ptx::mbar_wait_bounded(&full[s], ph, kWaitCycles);
+        ptx::mbar_wait_bounded(&full[c % g.stages], (uint32_t)(c / g.stages) & 1u, kWaitCycles);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = ptx::idesc_bf16(128, g.n_cols);
-      for (int c = 0; c < g.k_chunks; ++c) {
-        const int s = c % g.stages;
-        const uint32_t ph = (uint32_t)(c / g.stages) & 1u;
-        if (!ptx::mbar_wait_bounded(&full[s], ph, kWaitCycles)) {
-          report(g.err, kErrTimeoutFull);
+      int cg = 0, j = 0;
+      for (int it = blockIdx.x; it < n_items && !*(volatile int*)aborted; it += gridDim.x, ++j) {
+        const int buf = j & 1;
+        const uint32_t use = (uint32_t)(j >> 1);
+        if (!ptx::mbar_wait_bounded(&tempty[buf], (use & 1u) ^ 1u, kWaitCycles)) {
+          report(g.err, kErrTimeoutAcc);
           atomicExch(aborted, 1);
           break;
         }
         ptx::tc_fence_after();
-        uint8_t* base = smem + (size_t)s * stage_bytes;
-        const uint64_t a_hi = ptx::sw128_desc(base), a_lo = ptx::sw128_desc(base + kATile);
-        const uint64_t b_hi = ptx::sw128_desc(base + 2 * kATile);
-        const uint64_t b_lo = ptx::sw128_desc(base + 2 * kATile + stage_b);
+        const uint32_t acc = tmem + (uint32_t)(buf * acc_cols);
+        bool ok = true;
+        for (int c = 0; c < g.k_chunks; ++c, ++cg) {
+          const int s = cg % g.stages;
+          const uint32_t ph = (uint32_t)(cg / g.stages) & 1u;
+          if (!ptx::mbar_wait_bounded(&full[s], ph, kWaitCycles)) {
+            report(g.err, kErrTimeoutFull);
+            atomicExch(aborted, 1);
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          uint8_t* base = smem + (size_t)s * stage_bytes;
+          const uint64_t a_hi = ptx::sw128_desc(base), a_lo = ptx::sw128_desc(base + kATile);
+          const uint64_t b_hi = ptx::sw128_desc(base + 2 * kATile);
+          const uint64_t b_lo = ptx::sw128_desc(base + 2 * kATile + stage_b);
 #pragma unroll
-        for (int kk = 0; kk < kKChunk / 16; ++kk) {
-          const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 16 bf16 = 32 bytes
-          ptx::mma_bf16(tmem, a_hi + off, b_hi + off, idesc, (c | kk) != 0);
-          ptx::mma_bf16(tmem, a_hi + off, b_lo + off, idesc, 1u);
-          ptx::mma_bf16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+          for (int kk = 0; kk < kKChunk / 16; ++kk) {
+            const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 16 bf16 = 32 bytes
+            ptx::mma_bf16(acc, a_hi + off, b_hi + off, idesc, (c | kk) != 0);
+            ptx::mma_bf16(acc, a_hi + off, b_lo + off, idesc, 1u);
+            ptx::mma_bf16(acc, a_lo + off, b_hi + off, idesc, 1u);
+          }
+          ptx::mma_commit(&empty[s]);
         }
-        ptx::mma_commit(&empty[s]);
+        if (!ok) break;
+        ptx::mma_commit(&tfull[buf]);
       }
-      ptx::mma_commit(accb);  // fires once every issued MMA has completed
+      ptx::mma_commit(done);  // fires once every MMA issued here has completed
+      ptx::mbar_wait_bounded(done, 0u, kWaitCycles);
     }
   } else {
-    const bool ok = ptx::mbar_wait_bounded(accb, 0u, kWaitCycles);
-    if (!ok) report(g.err, kErrTimeoutAcc);
-    if (ok && !*(volatile int*)aborted) {
-      ptx::tc_fence_after();
-      const int q = warp & 3;           // TMEM lane quarter accessible to this warp
-      const int half = (warp - 2) >> 2; // which of the two warps of this quarter
-      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16);
-      ResidTiles rt{};
-      if (g.resid_last) {
-        for (int w2 = 0; w2 < 2; ++w2) {
-          const int st = (g.k_chunks - 2 + w2) % g.stages;
-          const uint8_t* base = smem + (size_t)st * stage_bytes + 2 * kATile;
-          rt.hi[w2] = base;
-          rt.lo[w2] = base + stage_b;
-        }
+    const int q = warp & 3;            // TMEM lane quarter accessible to this warp
+    const int half = (warp - 2) >> 2;  // which of the two warps of this quarter
+    int j = 0;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++j) {
+      const int buf = j & 1;
+      const uint32_t use = (uint32_t)(j >> 1);
+      if (!ptx::mbar_wait_bounded(&tfull[buf], use & 1u, kWaitCycles)) {
+        report(g.err, kErrTimeoutAcc);
+        atomicExch(aborted, 1);
+        break;
       }
-      epi.run(ti, g, taddr, m0 + 32 * q + lane, 32 * q + lane, half, rt);
+      if (*(volatile int*)aborted) break;
+      ptx::tc_fence_after();
+      const int mb = it % g.n_mblocks, m0 = mb * 128;
+      const TileInfo ti = epi.tile(it / g.n_mblocks, g);
+      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * acc_cols);
+      epi.run(ti, g, taddr, m0 + 32 * q + lane, half, ebuf0 + (size_t)half * g.ebuf_bytes);
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(ptx::smem_u32(&tempty[buf]))
+                                  : "memory");
     }
   }
   ptx::tc_fence_before();
@@ -238,82 +257,156 @@ struct ContigTiles {
   }
 };
 
+__device__ __forceinline__ void half_sync(int half) {
+  // the 4 epilogue warps of one half (128 threads) on named barrier 1 + half
+  asm volatile("bar.sync %0, 128;" ::"r"(1 + half) : "memory");
+}
+
+// One-electron layer epilogue.  Row blocks (one tangent group, or 16 rows of
+// a value-only tile) are staged through shared memory: the residual rows are
+// read with 16-byte vector loads, each thread updates its feature column in
+// place, and the block is written back with 16-byte vector stores.
 struct EpiTcLayer : ContigTiles {
   int n, ld;  // electrons per walker, activation row width (n_out)
-  StSplit out;
+  StSplit resid, out;
   bool has_resid;
   const float* Gb;
   const float* bias;
-  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int f_loc, int half,
-                      const ResidTiles& rt) const {
+
+  // rows [row0, row0 + nrows) x features [m0, m0 + 128) of `st` <-> staging tile
+  // all loads of a batch are issued before any shared-memory store
+  __device__ void load_block(const StSplit& st, size_t row0, int nrows, int m0, int lt, __nv_bfloat16* eb) const {
+    const int nv = nrows * 2 * 16;
+    for (int v0 = 0; v0 < nv; v0 += 128 * 12) {
+      uint4 r[12];
+#pragma unroll
+      for (int u = 0; u < 12; ++u) {
+        const int v = v0 + lt + 128 * u;
+        if (v < nv) {
+          const int pl = v / (nrows * 16), rr = (v / 16) % nrows, q = v % 16;
+          r[u] = __ldg(reinterpret_cast<const uint4*>(st.p + pl * st.plane + (row0 + rr) * (size_t)st.ld + m0 + 8 * q));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 12; ++u) {
+        const int v = v0 + lt + 128 * u;
+        if (v < nv) {
+          const int pl = v / (nrows * 16), rr = (v / 16) % nrows, q = v % 16;
+          *reinterpret_cast<uint4*>(eb + ((size_t)pl * nrows + rr) * 128 + 8 * q) = r[u];
+        }
+      }
+    }
+  }
+  __device__ void store_block(const StSplit& st, size_t row0, int nrows, int m0, int lt, int n_out,
+                              const __nv_bfloat16* eb) const {
+    const int nv = nrows * 2 * 16;
+    for (int v = lt; v < nv; v += 128) {
+      const int pl = v / (nrows * 16), rr = (v / 16) % nrows, q = v % 16;
+      if (m0 + 8 * q >= n_out) continue;
+      uint4* dst = reinterpret_cast<uint4*>(st.p + pl * st.plane + (row0 + rr) * (size_t)st.ld + m0 + 8 * q);
+      *dst = *reinterpret_cast<const uint4*>(eb + ((size_t)pl * nrows + rr) * 128 + 8 * q);
+    }
+  }
+  __device__ __forceinline__ float eb_get(const __nv_bfloat16* eb, int nrows, int rr, int fl) const {
+    return __bfloat162float(eb[(size_t)rr * 128 + fl]) + __bfloat162float(eb[((size_t)nrows + rr) * 128 + fl]);
+  }
+  __device__ __forceinline__ void eb_put(__nv_bfloat16* eb, int nrows, int rr, int fl, float y) const {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(y);
+    eb[(size_t)rr * 128 + fl] = hi;
+    eb[((size_t)nrows + rr) * 128 + fl] = __float2bfloat16_rn(y - __bfloat162float(hi));
+  }
+
+  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t* ebuf) const {
+    __nv_bfloat16* eb = reinterpret_cast<__nv_bfloat16*>(ebuf);
     const bool fok = f < g.n_out;
     const int N = g.n_out;
-    const float b = fok ? bias[f] : 0.f;
+    const int fc = fok ? f : 0;  // clamped column for speculative loads
+    const int fl = f & 127, m0 = f - fl;
+    const int lt = fl;           // thread index within this half (= local feature)
+    const float b = bias[fc];
     if (g.T == 1) {
       for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
+        const int nrows = min(16, ti.ng - c0);  // uniform across the half
+        if (nrows <= 0) break;
+        const size_t row0 = (size_t)(ti.g0 + c0);
+        if (has_resid) load_block(resid, row0, nrows, m0, lt, eb);
         float v[16], gbv[16];
-        ptx::tmem_ld16(taddr + c0, v);
-        if (!fok) continue;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          int lg = c0 + j;
-          gbv[j] = lg < ti.ng ? Gb[(size_t)((ti.g0 + lg) / n) * N + f] : 0.f;
+          const int gi = ti.g0 + c0 + min(j, nrows - 1);
+          gbv[j] = __ldg(Gb + (size_t)(gi / n) * N + fc);
         }
+        ptx::tmem_ld16(taddr + c0, v);
+        half_sync(half);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          int lg = c0 + j;
-          if (lg < ti.ng) {
+          if (j < nrows) {
             float h = tanhf(v[j] + gbv[j] + b);
-            if (has_resid) h = (h + rt.get(lg, f_loc)) * kRsqrt2;
-            out.put((size_t)(ti.g0 + lg), f, h);  // Tp == 1
+            if (has_resid) h = (h + eb_get(eb, nrows, j, fl)) * kRsqrt2;
+            eb_put(eb, nrows, j, fl, h);
           }
         }
+        half_sync(half);
+        store_block(out, row0, nrows, m0, lt, N, eb);
+        half_sync(half);
       }
       return;
     }
+    const int Tp = g.Tp;
     for (int lg = half; lg < ti.ng; lg += 2) {
       const int gi = ti.g0 + lg;
       const int w = gi / n;
-      const size_t r0 = (size_t)gi * g.Tp;
-      const int c0 = lg * g.Tp;
-      const float* gb = Gb + (size_t)w * g.Tp * N + f;
+      const size_t r0 = (size_t)gi * Tp;
+      const int c0 = lg * Tp;
+      const float* gb = Gb + (size_t)w * Tp * N + fc;
+      if (has_resid) load_block(resid, r0, Tp, m0, lt, eb);
+      half_sync(half);
       float h = 0.f, d1 = 0.f, zL = 0.f, S = 0.f;
-      for (int q4 = 0; q4 < g.Tp / 4; ++q4) {
-        float gbv[4];
+      float nxt[8];  // broadcast terms of the next chunk, loaded one chunk ahead
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int t = 4 * q4 + e;
-          gbv[e] = (fok && t < g.T) ? gb[(size_t)t * N] : 0.f;
+      for (int e = 0; e < 8; ++e) nxt[e] = e < g.T ? __ldg(gb + (size_t)e * N) : 0.f;
+      for (int t0 = 0; t0 < Tp; t0 += 8) {
+        const bool two = t0 + 4 < Tp;  // uniform
+        float gbv[8], v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          gbv[e] = nxt[e];
+          const int t = t0 + 8 + e;
+          nxt[e] = t < g.T ? __ldg(gb + (size_t)t * N) : 0.f;
         }
-        float v[4];
-        ptx::tmem_ld4(taddr + c0 + 4 * q4, v);
-        if (!fok) continue;
+        ptx::tmem_ld4(taddr + c0 + t0, v);
+        if (two) ptx::tmem_ld4(taddr + c0 + t0 + 4, v + 4);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int t = 4 * q4 + e;
-          float r = 0.f;
-          if (has_resid && t < g.T) r = rt.get(c0 + t, f_loc);
+        for (int e = 0; e < 8; ++e) {
+          const int t = t0 + e;
+          if (e >= 4 && !two) break;
+          if (t == 1) {
+            zL = v[e] + gbv[e];
+            continue;
+          }
+          float y;
           if (t == 0) {
             h = tanhf(v[e] + gbv[e] + b);
             d1 = 1.f - h * h;
-            out.put(r0, f, has_resid ? (h + r) * kRsqrt2 : h);
-          } else if (t == 1) {
-            zL = v[e] + gbv[e];
+            y = h;
           } else if (t < g.T) {
-            float z = v[e] + gbv[e];
+            const float z = v[e] + gbv[e];
             S = fmaf(z, z, S);
-            float y = d1 * z;
-            out.put(r0 + t, f, has_resid ? (y + r) * kRsqrt2 : y);
+            y = d1 * z;
           } else {
-            out.put(r0 + t, f, 0.f);
+            eb_put(eb, Tp, t, fl, 0.f);
+            continue;
           }
+          if (has_resid) y = (y + eb_get(eb, Tp, t, fl)) * kRsqrt2;
+          eb_put(eb, Tp, t, fl, y);
         }
       }
-      if (fok) {
-        float y = d1 * zL - 2.f * h * d1 * S;
-        if (has_resid) y = (y + rt.get(c0 + 1, f_loc)) * kRsqrt2;
-        out.put(r0 + 1, f, y);
-      }
+      float y = d1 * zL - 2.f * h * d1 * S;
+      if (has_resid) y = (y + eb_get(eb, Tp, 1, fl)) * kRsqrt2;
+      eb_put(eb, Tp, 1, fl, y);
+      half_sync(half);
+      store_block(out, r0, Tp, m0, lt, N, eb);
+      half_sync(half);
     }
   }
 };
@@ -321,8 +414,7 @@ struct EpiTcLayer : ContigTiles {
 struct EpiTcStore : ContigTiles {
   float* out;
   int ld;
-  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int, int half,
-                      const ResidTiles&) const {
+  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t*) const {
     const bool fok = f < g.n_out;
     for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
       float v[16];
@@ -417,8 +509,7 @@ struct EpiTcOrbital {
     }
     e[0] = e0; e[1] = ex; e[2] = ey; e[3] = ez; e[4] = el;
   }
-  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int, int half,
-                      const ResidTiles&) const {
+  __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t*) const {
     const bool fok = f < g.n_out;
     const int k = fok ? f / n : 0, j = fok ? f % n : 0;
     const size_t ts = (size_t)n * n;
@@ -547,13 +638,20 @@ static qmc_status launch(cudaStream_t s, const CUtensorMap& A0, const CUtensorMa
                          const CUtensorMap& B2, TcArgs g, int n_tiles, const Epi& epi) {
   if (n_tiles <= 0) return QMC_OK;
   const int stage_bytes = 2 * kATile + 2 * g.n_cols * kKChunk * 2;
-  g.stages = std::min(4, (200 * 1024) / stage_bytes);
+  const size_t avail = 227 * 1024 - 1024 - 256 - 2 * (size_t)g.ebuf_bytes - 64;
+  g.stages = std::min<int>(4, (int)(avail / stage_bytes));
   if (g.stages < 2) {
     set_error("tile of %d columns does not fit two pipeline stages", g.n_cols);
     return QMC_ERR_SHAPE;
   }
-  g.tmem_cols = tmem_cols_for(g.n_cols);
-  const size_t smem = 1024 + (size_t)g.stages * stage_bytes + 256;
+  g.tmem_cols = 2 * tmem_cols_for(g.n_cols);  // two accumulators
+  if (g.tmem_cols > 512) {
+    set_error("tile of %d columns does not fit two TMEM accumulators", g.n_cols);
+    return QMC_ERR_SHAPE;
+  }
+  g.n_tiles = n_tiles;
+  g.n_mblocks = (g.n_out + 127) / 128;
+  const size_t smem = 1024 + (size_t)g.stages * stage_bytes + 256 + 2 * (size_t)g.ebuf_bytes;
   // the opt-in attribute is per device and kernel; raise it to this launch's need
   static int attr_dev = -1;
   static size_t attr_bytes = 0;
@@ -564,8 +662,10 @@ static qmc_status launch(cudaStream_t s, const CUtensorMap& A0, const CUtensorMa
     attr_dev = dev;
     attr_bytes = smem;
   }
-  dim3 grid(n_tiles, (g.n_out + 127) / 128);
-  k_tc_gemm<Epi><<<grid, kTcThreads, smem, s>>>(A0, A1, B1, B2, g, epi);
+  static int n_sms = 0;
+  if (!n_sms) QMC_CUDA(cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev));
+  const int n_items = g.n_tiles * g.n_mblocks;
+  k_tc_gemm<Epi><<<std::min(n_items, n_sms), kTcThreads, smem, s>>>(A0, A1, B1, B2, g, epi);
   QMC_CUDA(cudaGetLastError());
   return QMC_OK;
 }
@@ -596,11 +696,17 @@ qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
               a.n_out);
     return QMC_ERR_SHAPE;
   }
-  g.resid_last = a.residual ? 1 : 0;
+  g.resid_last = 0;
+  g.ebuf_bytes = 2 * 128 * 2 * (a.T == 1 ? 16 : a.Tp);  // two planes x rows x 128 bf16
+  if (a.n_out % 8) {
+    set_error("tensor-core layer: output width %d is not a multiple of 8", a.n_out);
+    return QMC_ERR_SHAPE;
+  }
   EpiTcLayer e{};
   e.n_groups = a.n_groups;
   e.n = a.n;
   e.ld = a.n_out;
+  e.resid = StSplit{const_cast<__nv_bfloat16*>(a.X), a.k1, a.x_plane};
   e.has_resid = a.residual;
   e.out = StSplit{a.out, a.n_out, a.out_plane};
   e.Gb = a.Gb;
