@@ -145,6 +145,22 @@ qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64
 qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
                         uint64_t counter, float* normals, float* uniforms, cudaStream_t stream);
 
+/* Parameter adjoint of log|psi| (FP32), replacing the per-walker
+ * jax.value_and_grad of LossAndGrad (src/jaqmc/estimator/loss_grad.py:70-91)
+ * and its gradient algebra (:113-128):
+ *   per_walker (batch x qmc_param_count, may be NULL): row w = d log|psi_w| / d theta
+ *     in the flat parameter layout of qmc_model_set_params;
+ *   grad (qmc_param_count doubles, may be NULL): sum_w weights[w] * d log|psi_w| / d theta,
+ *     e.g. weights = 2 (E_c,w - <E_c>) / batch for the VMC energy gradient;
+ *   logpsi (batch, may be NULL).
+ * Walkers are processed in chunks sized by the gradient budget; every chunk
+ * recomputes its forward activations.  Workspace: qmc_workspace_size(m, QMC_OP_GRAD, batch). */
+qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
+                    double* grad, float* logpsi, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* Byte budget of the adjoint's workspace (default 8 GiB); sets the chunk size. */
+qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes);
+
 /* FP64 walker-batch mean and variance <x^2> - <x>^2 of a float32 vector,
  * NaNs skipped (src/jaqmc/estimator/base.py:27-53).  mean_var: 2 doubles. */
 qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t stream);

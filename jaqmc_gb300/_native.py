@@ -65,6 +65,9 @@ _SIGS = {
     "qmc_mh_draws": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p,
                                C.c_void_p, C.c_void_p]),
     "qmc_reduce_mean_var": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qmc_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                           C.c_void_p, C.c_size_t, C.c_void_p]),
+    "qmc_model_set_grad_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
     "qmc_model_check_error": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qmc_profile_enable": (C.c_int, [C.c_int]),
     "qmc_profile_read": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p]),
@@ -249,6 +252,27 @@ class NativeFermiNet:
                                     ptr(log_prob), ptr(accepts), ptr(normals), ptr(uniforms), ptr(fl),
                                     ptr(ws), ws.numel(), stream_handle(stream)))
         return e, log_prob, accepts, fl
+
+    def set_grad_budget(self, nbytes: int):
+        check(self.lib.qmc_model_set_grad_budget(self.h, int(nbytes)))
+
+    def grad(self, electrons, weights=None, per_walker=False, stream=None):
+        """Adjoint of log|psi|: returns ``(per_walker (B,P) or None, grad (P,) float64 or
+        None, logpsi (B,))``; ``grad = sum_w weights[w] d log|psi_w|/d theta``."""
+        e = self._elec(electrons)
+        B = e.shape[0]
+        P = self.param_count
+        J = torch.empty((B, P), dtype=torch.float32, device=self.device) if per_walker else None
+        g = None
+        w = None
+        if weights is not None:
+            w = weights.to(device=self.device, dtype=torch.float64).contiguous()
+            g = torch.empty(P, dtype=torch.float64, device=self.device)
+        lp = torch.empty(B, dtype=torch.float32, device=self.device)
+        ws, nb = self.workspace(OP_GRAD, B)
+        check(self.lib.qmc_grad(self.h, B, ptr(e), ptr(w), ptr(J), ptr(g), ptr(lp), ptr(ws), ws.numel(),
+                                stream_handle(stream)))
+        return J, g, lp
 
     def mh_draws(self, batch, steps, seed, counter, stream=None):
         nz = torch.empty((steps, batch, self.n, 3), dtype=torch.float32, device=self.device)

@@ -1,0 +1,475 @@
+// Hand-written adjoint of log|psi| with respect to the FermiNet parameters
+// (FP32).  Replaces the per-walker jax.value_and_grad of LossAndGrad
+// (src/jaqmc/estimator/loss_grad.py:70-91) and the VMC gradient algebra
+// (:113-128): per-walker Jacobian rows d log|psi_w| / d theta in the flat
+// parameter layout of qmc_model_set_params, and sum_w c_w d log|psi_w|/d theta.
+//
+// Walkers are processed in chunks sized to a byte budget; each chunk re-runs
+// the forward pass keeping every layer's activations, then runs the backward
+// pass (recomputation instead of storing activations for the whole batch).
+#include <algorithm>
+
+#include "gemm_simt.cuh"
+#include "kernels.cuh"
+#include "plan.cuh"
+#include "profile.cuh"
+
+namespace qmc {
+
+template <typename T>
+static T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+
+// ------------------------------------------------------------ kernels
+// y = tanh(z) saved next to the layer output (value-only one-electron layer)
+struct EpiLayerSave {
+  const float* Gb;
+  const float* bias;
+  const float* resid;  // nullptr: no residual
+  float* out;
+  float* y;
+  int ld;
+  __device__ void operator()(const float* Cs, int ng, int g0, int n0, int N, const RowMap& m) const {
+    for (int p = threadIdx.x; p < ng * kBN; p += blockDim.x) {
+      int lg = p / kBN, c = p % kBN, col = n0 + c;
+      if (col >= N) continue;
+      int g = g0 + lg;
+      size_t r = m.row(g, 0);
+      float h = tanhf(Cs[lg * kCsLd + c] + Gb[(size_t)m.w(g) * N + col] + bias[col]);
+      y[r * ld + col] = h;
+      out[r * ld + col] = resid ? (h + resid[r * ld + col]) * kRsqrt2 : h;
+    }
+  }
+};
+
+// two-electron layer with saved tanh outputs
+__global__ void k_pair_fwd_save(int npairs, int d_in, int d_out, const float* __restrict__ Hin,
+                                const float* __restrict__ W, const float* __restrict__ b, float* __restrict__ Hout,
+                                float* __restrict__ Y) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)npairs * d_out) return;
+  const int f = (int)(e % d_out);
+  const size_t pr = e / d_out;
+  const float* x = Hin + pr * d_in;
+  float z = b[f];
+  for (int k = 0; k < d_in; ++k) z = fmaf(x[k], W[k * d_out + f], z);
+  const float y = tanhf(z);
+  Y[e] = y;
+  Hout[e] = d_in == d_out ? (y + x[f]) * kRsqrt2 : y;
+}
+
+// orbital / envelope cotangents from Abar (value-only pass)
+__global__ void k_orb_bwd(int B, int n, int n_up, int split, int K, int natom, int env_abs, int norb_p,
+                          const float* __restrict__ Abar, const float* __restrict__ orb,
+                          const float* __restrict__ rae, const float* __restrict__ pi0,
+                          const float* __restrict__ sg0, const float* __restrict__ pi1,
+                          const float* __restrict__ sg1, float* __restrict__ orbbar, float* __restrict__ envbar) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * n * norb_p) return;
+  const int col = (int)(e % norb_p);
+  const size_t wi = e / norb_p;
+  const int i = (int)(wi % n), w = (int)(wi / n);
+  if (col >= K * n) {
+    orbbar[e] = 0.f;
+    return;
+  }
+  const int k = col / n, j = col % n;
+  const bool c1 = split && i >= n_up;
+  const float* pi = c1 ? pi1 : pi0;
+  const float* sg = c1 ? sg1 : sg0;
+  float env = 0.f;
+  for (int I = 0; I < natom; ++I) {
+    float sv = sg[((size_t)j * natom + I) * K + k];
+    float se = env_abs ? fabsf(sv) : sv;
+    env += pi[((size_t)j * natom + I) * K + k] * expf(-se * rae[wi * natom + I]);
+  }
+  const size_t ai = (((size_t)w * K + k) * n + i) * n + j;
+  const float ab = Abar[ai];
+  orbbar[e] = ab * env;
+  envbar[ai] = ab * orb[ai];
+}
+
+// envelope parameter rows of the Jacobian: d/dpi, d/dsigma for channel c
+__global__ void k_env_jac(int B, int n, int i0, int ns, int K, int natom, int env_abs, const float* __restrict__ envbar,
+                          const float* __restrict__ rae, const float* __restrict__ pi, const float* __restrict__ sg,
+                          float* __restrict__ J, size_t P, size_t off_pi, size_t off_sg) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t per_w = (size_t)n * natom * K;
+  if (e >= (size_t)B * per_w) return;
+  const int w = (int)(e / per_w);
+  const size_t q = e % per_w;  // (j, I, k) in the reference layout
+  const int k = (int)(q % K), I = (int)((q / K) % natom), j = (int)(q / ((size_t)K * natom));
+  const float pv = pi[q], sv = sg[q];
+  const float se = env_abs ? fabsf(sv) : sv;
+  const float dse = env_abs ? (sv > 0.f ? 1.f : (sv < 0.f ? -1.f : 0.f)) : 1.f;
+  float dpi = 0.f, dsg = 0.f;
+  for (int i = i0; i < i0 + ns; ++i) {
+    const float r = rae[((size_t)w * n + i) * natom + I];
+    const float ex = expf(-se * r);
+    const float eb = envbar[(((size_t)w * K + k) * n + i) * n + j];
+    dpi = fmaf(eb, ex, dpi);
+    dsg = fmaf(eb, -pv * ex * r * dse, dsg);
+  }
+  J[(size_t)w * P + off_pi + q] = dpi;
+  J[(size_t)w * P + off_sg + q] = dsg;
+}
+
+// Jacobian block of a dense layer: J[w][off + kx*N + c] =
+//   sum_{r<R} X[w*Rs + row0 + r][kx] * Z[w*Rs + row0 + r][c]
+__global__ void k_jac_outer(int B, int R, int Rs, int row0, const float* __restrict__ X, int ldx, int Kx,
+                            const float* __restrict__ Z, int ldz, int N, float* __restrict__ J, size_t P,
+                            size_t off) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t per_w = (size_t)Kx * N;
+  if (e >= (size_t)B * per_w) return;
+  const int w = (int)(e / per_w);
+  const int kx = (int)((e % per_w) / N), c = (int)(e % N);
+  const size_t base = (size_t)w * Rs + row0;
+  float acc = 0.f;
+  for (int r = 0; r < R; ++r) acc = fmaf(X[(base + r) * ldx + kx], Z[(base + r) * ldz + c], acc);
+  J[(size_t)w * P + off + (size_t)kx * N + c] = acc;
+}
+
+// per-walker column sums Zs[w][c] = sum_{r<R} Z[w*R + r][c]; optionally also
+// written as Jacobian rows (bias gradients)
+__global__ void k_colsum(int B, int R, const float* __restrict__ Z, int ldz, int N, float* __restrict__ Zs,
+                         float* __restrict__ J, size_t P, size_t off) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * N) return;
+  const int w = (int)(e / N), c = (int)(e % N);
+  float acc = 0.f;
+  for (int r = 0; r < R; ++r) acc += Z[((size_t)w * R + r) * ldz + c];
+  if (Zs) Zs[e] = acc;
+  if (J) J[(size_t)w * P + off + c] = acc;
+}
+
+// z = hbar * s * (1 - y^2), hres = hbar * s (residual path)
+__global__ void k_tanh_bwd(size_t count, float s, const float* __restrict__ hbar, const float* __restrict__ y,
+                           float* __restrict__ zbar) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  const float v = y[e];
+  zbar[e] = hbar[e] * s * (1.f - v * v);
+}
+
+// hbar_in[w,i,f] = T[w,i,f] + res * hbar_out[w,i,f] / sqrt(2) + g1bar[w][s(i)*din + f] / n_s
+__global__ void k_input_grad(int B, int n, int n_up, int C, int din, const float* __restrict__ Tm, int ldt,
+                             const float* __restrict__ hbar_out, int residual, const float* __restrict__ g1bar,
+                             int g1p, float* __restrict__ hbar_in) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * n * din) return;
+  const int f = (int)(e % din);
+  const size_t wi = e / din;
+  const int i = (int)(wi % n), w = (int)(wi / n);
+  const int sc = (C == 2 && i >= n_up) ? 1 : 0;
+  const int ns = C == 1 ? n : (sc == 0 ? n_up : n - n_up);
+  float v = Tm[wi * ldt + f] + g1bar[(size_t)w * g1p + sc * din + f] / (float)ns;
+  if (residual) v += hbar_out[wi * din + f] * kRsqrt2;
+  hbar_in[e] = v;
+}
+
+// h2bar[w,a,i,f] (+)= g2bar[w,i][s(a)*d2 + f] / n_{s(a)}  (G2 averages over the first index)
+__global__ void k_h2_from_g2(int B, int n, int n_up, int C, int d2, const float* __restrict__ Tm, int ldt,
+                             int col0, float* __restrict__ h2bar, int accumulate) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * n * n * d2) return;
+  const int f = (int)(e % d2);
+  const size_t pr = e / d2;
+  const int i = (int)(pr % n), a = (int)((pr / n) % n), w = (int)(pr / ((size_t)n * n));
+  const int sc = (C == 2 && a >= n_up) ? 1 : 0;
+  const int ns = C == 1 ? n : (sc == 0 ? n_up : n - n_up);
+  const float v = Tm[((size_t)w * n + i) * ldt + col0 + sc * d2 + f] / (float)ns;
+  h2bar[e] = accumulate ? h2bar[e] + v : v;
+}
+
+// two-electron layer backward data path: h2bar_in = z2bar W2^T (+ residual)
+__global__ void k_pair_bwd_data(size_t npairs, int d_in, int d_out, const float* __restrict__ z2bar,
+                                const float* __restrict__ Wt, const float* __restrict__ h2bar_out,
+                                float* __restrict__ h2bar_in) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= npairs * d_in) return;
+  const int k = (int)(e % d_in);
+  const size_t pr = e / d_in;
+  float acc = 0.f;
+  for (int f = 0; f < d_out; ++f) acc = fmaf(z2bar[pr * d_out + f], Wt[(size_t)f * d_in + k], acc);
+  if (d_in == d_out) acc += h2bar_out[pr * d_out + k] * kRsqrt2;
+  h2bar_in[e] = acc;
+}
+
+// grad[p] += sum_w c_w J[w][p]  (FP64 accumulation)
+__global__ void k_weighted_sum(int B, size_t P, const float* __restrict__ J, const double* __restrict__ c,
+                               double* __restrict__ grad) {
+  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double acc = 0.0;
+  for (int w = 0; w < B; ++w) acc += c[w] * (double)J[(size_t)w * P + p];
+  grad[p] += acc;
+}
+
+static inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// ------------------------------------------------------------ plan
+struct GradPlan {
+  int B;
+  size_t x0, h1[QMC_MAX_LAYERS], y1[QMC_MAX_LAYERS], g1m[QMC_MAX_LAYERS], G2[QMC_MAX_LAYERS], gb;
+  size_t h2[QMC_MAX_LAYERS], y2[QMC_MAX_LAYERS], amat, orb, abar, envbar, rae, aevec, lpsi;
+  size_t hbar[2], zbar, tmp, zsum, g1bar, h2bar[2], z2bar, orbbar, J, total;
+};
+
+static GradPlan make_grad_plan(const qmc_model* m, int B) {
+  const Dims& d = m->d;
+  GradPlan p{};
+  p.B = B;
+  size_t o = 0;
+  auto take = [&](size_t floats) { size_t r = o; o += align_up(floats * 4, 256); return r; };
+  const size_t rows = (size_t)B * d.n, pairs = rows * d.n;
+  int dmax = 8, kmax = 8, g1max = 8, d2max = 4;
+  p.x0 = take(rows * d.d1_in_p[0]);
+  for (int l = 0; l < d.L; ++l) {
+    p.h1[l] = take(rows * d.d1[l]);
+    p.y1[l] = take(rows * d.d1[l]);
+    p.g1m[l] = take((size_t)B * d.g1_p[l]);
+    p.G2[l] = take(rows * d.g2_p[l]);
+    p.h2[l] = take(pairs * d.d2_in[l]);
+    if (d.upd2[l]) p.y2[l] = take(pairs * d.d2[l]);
+    dmax = std::max(dmax, std::max(d.d1[l], d.d1_in_p[l]));
+    kmax = std::max(kmax, d.d1_in_p[l] + d.g2_p[l]);
+    g1max = std::max(g1max, d.g1_p[l]);
+    d2max = std::max(d2max, std::max(d.d2[l], d.d2_in[l]));
+  }
+  p.gb = take((size_t)B * dmax);
+  const size_t am = (size_t)B * d.K * d.n * d.n;
+  p.amat = take(am);
+  p.orb = take(am);
+  p.abar = take(am);
+  p.envbar = take(am);
+  p.rae = take(rows * d.A);
+  p.aevec = take(rows * d.A * 3);
+  p.lpsi = take(B);
+  p.hbar[0] = take(rows * dmax);
+  p.hbar[1] = take(rows * dmax);
+  p.zbar = take(rows * dmax);
+  p.tmp = take(rows * std::max(kmax, d.norb_p));
+  p.zsum = take((size_t)B * dmax);
+  p.g1bar = take((size_t)B * g1max);
+  p.h2bar[0] = take(pairs * d2max);
+  p.h2bar[1] = take(pairs * d2max);
+  p.z2bar = take(pairs * d2max);
+  p.orbbar = take(rows * d.norb_p);
+  p.J = take((size_t)B * m->p.total);
+  p.total = o;
+  return p;
+}
+
+// walkers per chunk under the model's byte budget
+static int grad_chunk(const qmc_model* m, int B) {
+  const size_t one = make_grad_plan(m, 1).total;
+  const size_t two = make_grad_plan(m, 2).total;
+  const size_t per = two > one ? two - one : one;
+  size_t c = m->grad_budget > one ? 1 + (m->grad_budget - one) / per : 1;
+  return (int)std::max<size_t>(1, std::min<size_t>(c, (size_t)B));
+}
+
+size_t grad_workspace(const qmc_model* m, int B) { return make_grad_plan(m, grad_chunk(m, B)).total; }
+
+#define QMC_PROF(cls, call)         \
+  do {                              \
+    ::qmc::ProfScope ps_((cls), s); \
+    QMC_CUDA(call);                 \
+  } while (0)
+
+// Forward pass of `B` walkers keeping every layer's activations.
+static qmc_status forward_save(qmc_model* m, const GradPlan& p, void* ws, const float* electrons, cudaStream_t s) {
+  const Dims& d = m->d;
+  const ArenaLayout& a = m->a;
+  const float* ar = m->arena;
+  const int B = p.B, n = d.n;
+  const RowMap rows_map{n, 0, n, 1};
+  const RowMap w_map{1, 0, 1, 1};
+  QMC_PROF(QMC_KC_FEATURES, launch_features(s, B, n, d.A, 1, 1, d.d1_in_p[0], electrons, ar + a.atoms, ar + a.charges,
+                                            m->nuclear_repulsion, at<float>(ws, p.x0), at<float>(ws, p.h2[0]),
+                                            at<float>(ws, p.rae), at<float>(ws, p.aevec), nullptr));
+  for (int l = 0; l < d.L; ++l) {
+    const int din = d.d1_in[l], dinp = d.d1_in_p[l], dout = d.d1[l];
+    const float* in = l == 0 ? at<float>(ws, p.x0) : at<float>(ws, p.h1[l - 1]);
+    float* g1m = at<float>(ws, p.g1m[l]);
+    float* G2 = at<float>(ws, p.G2[l]);
+    float* Gb = at<float>(ws, p.gb);
+    QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, 1, din, StF32{const_cast<float*>(in), dinp}, d.g1_p[l],
+                                          StF32{g1m, d.g1_p[l]}));
+    QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, w_map, g1m, d.g1_p[l], d.g1_p[l], nullptr, 0, 0, ar + a.w_g1[l],
+                                                dout, dout, EpiStore{Gb, dout, nullptr}));
+    QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, 1, 1, d.d2_in[l], 1, at<float>(ws, p.h2[l]), d.g2_p[l],
+                                          StF32{G2, d.g2_p[l]}));
+    EpiLayerSave epi{Gb, ar + a.b1[l], (l > 0 && din == dout) ? in : nullptr, at<float>(ws, p.h1[l]),
+                     at<float>(ws, p.y1[l]), dout};
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
+                                                   ar + a.w_main[l], dout, dout, epi));
+    if (d.upd2[l]) {
+      const size_t np = (size_t)B * n * n;
+      ::qmc::ProfScope ps_(QMC_KC_PAIR, s);
+      k_pair_fwd_save<<<blocks(np * d.d2[l]), 256, 0, s>>>((int)np, d.d2_in[l], d.d2[l], at<float>(ws, p.h2[l]),
+                                                            ar + a.w2[l], ar + a.b2[l], at<float>(ws, p.h2[l + 1]),
+                                                            at<float>(ws, p.y2[l]));
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  const int nch = d.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    const int ns = d.split ? (c == 0 ? d.n_up : d.n_dn) : d.n;
+    const int i0 = (d.split && c == 1) ? d.n_up : 0;
+    RowMap map{ns, i0, n, 1};
+    EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + a.env_pi[c],
+                   ar + a.env_sigma[c], n, d.A, d.K, 1, d.env_abs};
+    epi.orb = at<float>(ws, p.orb);
+    QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, at<float>(ws, p.h1[d.L - 1]), d.d_last, d.d_last, nullptr,
+                                              0, 0, ar + a.w_orb[c], d.norb_p, d.norb, epi));
+  }
+  return QMC_OK;
+}
+
+// Backward pass of one chunk: per-walker Jacobian rows into J (row stride P).
+static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, float* logpsi, cudaStream_t s) {
+  const Dims& d = m->d;
+  const ArenaLayout& a = m->a;
+  const ParamLayout& pl = m->p;
+  const float* ar = m->arena;
+  const int B = p.B, n = d.n;
+  const size_t P = pl.total, rows = (size_t)B * n, pairs = rows * n;
+  const RowMap rows_map{n, 0, n, 1};
+  const RowMap w_map{1, 0, 1, 1};
+  QMC_PROF(QMC_KC_LOGDET, launch_logdet_bwd(s, B, n, d.K, at<float>(ws, p.amat), at<float>(ws, p.abar), logpsi));
+  const int nch = d.split ? 2 : 1;
+  {
+    ::qmc::ProfScope ps_(QMC_KC_ORBITAL, s);
+    k_orb_bwd<<<blocks(rows * d.norb_p), 256, 0, s>>>(
+        B, n, d.n_up, d.split, d.K, d.A, d.env_abs, d.norb_p, at<float>(ws, p.abar), at<float>(ws, p.orb),
+        at<float>(ws, p.rae), ar + a.env_pi[0], ar + a.env_sigma[0], ar + a.env_pi[nch - 1],
+        ar + a.env_sigma[nch - 1], at<float>(ws, p.orbbar), at<float>(ws, p.envbar));
+    QMC_CUDA(cudaGetLastError());
+  }
+  float* hbar = at<float>(ws, p.hbar[0]);
+  for (int c = 0; c < nch; ++c) {
+    const int ns = d.split ? (c == 0 ? d.n_up : d.n_dn) : d.n;
+    const int i0 = (d.split && c == 1) ? d.n_up : 0;
+    {
+      ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
+      k_env_jac<<<blocks((size_t)B * n * d.A * d.K), 256, 0, s>>>(B, n, i0, ns, d.K, d.A, d.env_abs,
+                                                                 at<float>(ws, p.envbar), at<float>(ws, p.rae),
+                                                                 ar + a.env_pi[c], ar + a.env_sigma[c], J, P,
+                                                                 pl.env_pi[c], pl.env_sigma[c]);
+      QMC_CUDA(cudaGetLastError());
+      k_jac_outer<<<blocks((size_t)B * d.d_last * d.norb), 256, 0, s>>>(
+          B, ns, n, i0, at<float>(ws, p.h1[d.L - 1]), d.d_last, d.d_last, at<float>(ws, p.orbbar), d.norb_p, d.norb, J,
+          P, pl.orb_k[c]);
+      QMC_CUDA(cudaGetLastError());
+    }
+    // hbar of the last layer's rows of this channel = orbbar W_orb^T
+    RowMap map{ns, i0, n, 1};
+    QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, at<float>(ws, p.orbbar), d.norb_p, d.norb_p, nullptr, 0, 0,
+                                              ar + a.wt_orb[c], d.d_last, d.d_last, EpiStore{hbar, d.d_last, nullptr}));
+  }
+  int hb = 0, h2b = 0;
+  for (int l = d.L - 1; l >= 0; --l) {
+    const int din = d.d1_in[l], dinp = d.d1_in_p[l], dout = d.d1[l];
+    const bool res = l > 0 && din == dout;
+    const float* in = l == 0 ? at<float>(ws, p.x0) : at<float>(ws, p.h1[l - 1]);
+    float* hb_out = at<float>(ws, p.hbar[hb]);
+    float* zbar = at<float>(ws, p.zbar);
+    float* zsum = at<float>(ws, p.zsum);
+    {
+      ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
+      k_tanh_bwd<<<blocks(rows * dout), 256, 0, s>>>(rows * dout, res ? kRsqrt2 : 1.f, hb_out, at<float>(ws, p.y1[l]),
+                                                     zbar);
+      QMC_CUDA(cudaGetLastError());
+      const size_t k0 = pl.dense1_k[l];
+      k_jac_outer<<<blocks((size_t)B * din * dout), 256, 0, s>>>(B, n, n, 0, in, dinp, din, zbar, dout, dout, J, P, k0);
+      QMC_CUDA(cudaGetLastError());
+      k_jac_outer<<<blocks((size_t)B * d.C * d.d2_in[l] * dout), 256, 0, s>>>(
+          B, n, n, 0, at<float>(ws, p.G2[l]), d.g2_p[l], d.C * d.d2_in[l], zbar, dout, dout, J, P,
+          k0 + (size_t)(din + d.C * din) * dout);
+      QMC_CUDA(cudaGetLastError());
+      k_colsum<<<blocks((size_t)B * dout), 256, 0, s>>>(B, n, zbar, dout, dout, zsum, J, P, pl.dense1_b[l]);
+      QMC_CUDA(cudaGetLastError());
+      k_jac_outer<<<blocks((size_t)B * d.C * din * dout), 256, 0, s>>>(B, 1, 1, 0, at<float>(ws, p.g1m[l]), d.g1_p[l],
+                                                                      d.C * din, zsum, dout, dout, J, P,
+                                                                      k0 + (size_t)din * dout);
+      QMC_CUDA(cudaGetLastError());
+    }
+    float* tmp = at<float>(ws, p.tmp);
+    const int kmain = dinp + d.g2_p[l];
+    if (l > 0) {
+      // [h | g2] input cotangents = zbar W_main^T ; spin-mean cotangent = zsum W_g1^T
+      QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, zbar, dout, dout, nullptr, 0, 0,
+                                                     ar + a.wt_main[l], kmain, kmain, EpiStore{tmp, kmain, nullptr}));
+      float* g1bar = at<float>(ws, p.g1bar);
+      QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, w_map, zsum, dout, dout, nullptr, 0, 0, ar + a.wt_g1[l],
+                                                  d.g1_p[l], d.g1_p[l], EpiStore{g1bar, d.g1_p[l], nullptr}));
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_input_grad<<<blocks(rows * din), 256, 0, s>>>(B, n, d.n_up, d.C, din, tmp, kmain, hb_out, res ? 1 : 0, g1bar,
+                                                      d.g1_p[l], at<float>(ws, p.hbar[hb ^ 1]));
+      QMC_CUDA(cudaGetLastError());
+    }
+    // two-electron stream: h2[l+1] = pair_l(h2[l]) for l < L-1; G2[l] = means of h2[l]
+    {
+      ::qmc::ProfScope ps_(QMC_KC_PAIR, s);
+      float* h2b_next = at<float>(ws, p.h2bar[h2b]);  // cotangent of h2[l+1]
+      float* h2b_cur = at<float>(ws, p.h2bar[h2b ^ 1]);
+      bool have_cur = false;
+      if (d.upd2[l]) {
+        float* z2 = at<float>(ws, p.z2bar);
+        k_tanh_bwd<<<blocks(pairs * d.d2[l]), 256, 0, s>>>(pairs * d.d2[l], d.d2_in[l] == d.d2[l] ? kRsqrt2 : 1.f,
+                                                          h2b_next, at<float>(ws, p.y2[l]), z2);
+        QMC_CUDA(cudaGetLastError());
+        k_jac_outer<<<blocks((size_t)B * d.d2_in[l] * d.d2[l]), 256, 0, s>>>(
+            B, n * n, n * n, 0, at<float>(ws, p.h2[l]), d.d2_in[l], d.d2_in[l], z2, d.d2[l], d.d2[l], J, P,
+            pl.dense2_k[l]);
+        QMC_CUDA(cudaGetLastError());
+        k_colsum<<<blocks((size_t)B * d.d2[l]), 256, 0, s>>>(B, n * n, z2, d.d2[l], d.d2[l], nullptr, J, P,
+                                                             pl.dense2_b[l]);
+        QMC_CUDA(cudaGetLastError());
+        if (l > 0) {
+          k_pair_bwd_data<<<blocks(pairs * d.d2_in[l]), 256, 0, s>>>(pairs, d.d2_in[l], d.d2[l], z2, ar + a.wt2[l],
+                                                                    h2b_next, h2b_cur);
+          QMC_CUDA(cudaGetLastError());
+          have_cur = true;
+        }
+      }
+      if (l > 0) {
+        k_h2_from_g2<<<blocks(pairs * d.d2_in[l]), 256, 0, s>>>(B, n, d.n_up, d.C, d.d2_in[l], tmp, kmain, dinp, h2b_cur,
+                                                               have_cur ? 1 : 0);
+        QMC_CUDA(cudaGetLastError());
+        h2b ^= 1;
+      }
+    }
+    hb ^= 1;
+  }
+  return QMC_OK;
+}
+
+qmc_status run_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
+                    double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
+  const int chunk = grad_chunk(m, batch);
+  const GradPlan p = make_grad_plan(m, chunk);
+  if (ws_bytes < p.total) {
+    set_error("workspace too small for the adjoint: %zu bytes given, %zu needed", ws_bytes, p.total);
+    return QMC_ERR_WORKSPACE;
+  }
+  const size_t P = m->p.total;
+  if (grad) QMC_CUDA(cudaMemsetAsync(grad, 0, P * sizeof(double), s));
+  for (int w0 = 0; w0 < batch; w0 += chunk) {
+    const int B = std::min(chunk, batch - w0);
+    GradPlan q = make_grad_plan(m, B);
+    // the chunk's plan lays out fewer walkers inside the same workspace
+    float* J = per_walker ? per_walker + (size_t)w0 * P : at<float>(ws, q.J);
+    QMC_TRY(forward_save(m, q, ws, electrons + (size_t)w0 * m->d.n * 3, s));
+    QMC_TRY(backward(m, q, ws, J, logpsi ? logpsi + w0 : nullptr, s));
+    if (grad && weights) {
+      ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
+      k_weighted_sum<<<blocks(P), 256, 0, s>>>(B, P, J, weights + w0, grad);
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  return QMC_OK;
+}
+
+}  // namespace qmc

@@ -104,7 +104,7 @@ static qmc_status build_dims(const qmc_ferminet_config* c, Dims* d) {
   }
   d->d_last = d1;
   d->norb = d->K * d->n;
-  d->norb_p = round_up(d->norb, 4);
+  d->norb_p = round_up(d->norb, 8);
   return QMC_OK;
 }
 
@@ -148,6 +148,12 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
   }
   a->atoms = take(3 * d.A);
   a->charges = take(d.A);
+  for (int l = 0; l < d.L; ++l) {
+    a->wt_main[l] = take((size_t)d.d1[l] * (d.d1_in_p[l] + d.g2_p[l]));
+    a->wt_g1[l] = take((size_t)d.d1[l] * d.g1_p[l]);
+    if (d.upd2[l]) a->wt2[l] = take((size_t)d.d2[l] * d.d2_in[l]);
+  }
+  for (int s = 0; s < nch; ++s) a->wt_orb[s] = take((size_t)d.norb_p * d.d_last);
   a->total = o;
   size_t b = 0;
   auto takeb = [&](size_t n) { size_t r = b; b += align_up(n, 128); return r; };
@@ -605,6 +611,17 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
     QMC_CUDA(cp(a.env_pi[c], p.env_pi[c], (size_t)d.n * d.A * d.K));
     QMC_CUDA(cp(a.env_sigma[c], p.env_sigma[c], (size_t)d.n * d.A * d.K));
   }
+  // FP32 transposes for the adjoint
+  for (int l = 0; l < d.L; ++l) {
+    const int kmain = d.d1_in_p[l] + d.g2_p[l];
+    QMC_CUDA(launch_transpose_f32(s, ar + a.w_main[l], kmain, d.d1[l], d.d1[l], ar + a.wt_main[l]));
+    QMC_CUDA(launch_transpose_f32(s, ar + a.w_g1[l], d.g1_p[l], d.d1[l], d.d1[l], ar + a.wt_g1[l]));
+    if (d.upd2[l]) QMC_CUDA(launch_transpose_f32(s, ar + a.w2[l], d.d2_in[l], d.d2[l], d.d2[l], ar + a.wt2[l]));
+  }
+  for (int c = 0; c < nch; ++c) {
+    QMC_CUDA(cudaMemsetAsync(ar + a.wt_orb[c], 0, sizeof(float) * d.norb_p * d.d_last, s));
+    QMC_CUDA(launch_transpose_f32(s, ar + a.w_orb[c], d.d_last, d.norb, d.norb_p, ar + a.wt_orb[c]));
+  }
   // bf16 K-major copies for the tensor-core path
   for (int l = 0; l < d.L; ++l) {
     int kmain = d.d1_in_p[l] + d.g2_p[l];
@@ -622,7 +639,25 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
 
 size_t qmc_workspace_size(const qmc_model* m, int op, int batch) {
   if (!m || batch < 1) return 0;
+  if (op == QMC_OP_GRAD) return grad_workspace(m, batch);
   return make_plan(m, op, batch).total;
+}
+
+qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes) {
+  if (!m || bytes == 0) { set_error("null model or zero budget"); return QMC_ERR_ARG; }
+  m->grad_budget = bytes;
+  return QMC_OK;
+}
+
+qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
+                    double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (!m) { set_error("null model"); return QMC_ERR_ARG; }
+  if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
+  if (batch < 1 || !electrons) { set_error("bad batch/electrons"); return QMC_ERR_ARG; }
+  if (!per_walker && !grad) { set_error("nothing to compute: per_walker and grad are both null"); return QMC_ERR_ARG; }
+  if (grad && !weights) { set_error("grad needs per-walker weights"); return QMC_ERR_ARG; }
+  if (!ws) { set_error("null workspace"); return QMC_ERR_WORKSPACE; }
+  return run_grad(m, batch, electrons, weights, per_walker, grad, logpsi, ws, ws_bytes, s);
 }
 
 qmc_status qmc_forward(qmc_model* m, int batch, const float* electrons, float* logpsi, float* sign,

@@ -54,7 +54,7 @@ struct Dims {
   int g2_p[QMC_MAX_LAYERS];      // padded width of the spin means of h2 (C*d2_in)
   int d_last;                    // width of the last one-electron layer
   int norb;                      // K*n orbital columns per electron
-  int norb_p;                    // norb padded to a multiple of 4 (weight row stride)
+  int norb_p;                    // norb padded to a multiple of 8 (weight row stride)
 };
 
 // Device arena layout (float offsets) of the derived parameters.
@@ -67,6 +67,11 @@ struct ArenaLayout {
   size_t w_orb[2];                // [d_last x norb_p] per channel (zero padded columns)
   size_t env_pi[2], env_sigma[2]; // [n x A x K] per channel (reference layout)
   size_t atoms, charges;          // [A x 3], [A]
+  // FP32 transposes for the adjoint's input-gradient GEMMs
+  size_t wt_main[QMC_MAX_LAYERS]; // [d1 x (d1_in_p + g2_p)]
+  size_t wt_g1[QMC_MAX_LAYERS];   // [d1 x g1_p]
+  size_t wt2[QMC_MAX_LAYERS];     // [d2 x d2_in]
+  size_t wt_orb[2];               // [norb_p x d_last]
   size_t total;                   // floats
   // bf16 arena (element offsets) for the mixed form: transposed weights
   size_t t_main[QMC_MAX_LAYERS];  // [d1 x (d1_in_p + g2_p)] K-major
@@ -99,6 +104,7 @@ struct qmc_model {
   double nuclear_repulsion = 0.0;  // sum_{I<J} Z_I Z_J / R_IJ
   int* dev_err = nullptr;          // device error word of bounded waits
   bool params_set = false;
+  size_t grad_budget = (size_t)8 << 30;  // bytes for the adjoint's chunked workspace
   int n_sms = 0;
 };
 

@@ -97,6 +97,7 @@ struct EpiOrbital {
   const float* pi;     // this spin channel: [n][A][K]
   const float* sigma;  // [n][A][K]
   int n, natom, K, T, env_abs;
+  float* orb = nullptr;  // value-only passes: also store the orbitals before the envelope
   __device__ void operator()(const float* Cs, int ng, int g0, int n0, int N, const RowMap& m) const {
     const int Tp = m.Tp;
     for (int p = threadIdx.x; p < ng * kBN; p += blockDim.x) {
@@ -134,6 +135,7 @@ struct EpiOrbital {
       const size_t ts = (size_t)n * n;
       float o0 = cs[0];
       dst[0] = o0 * e0;
+      if (orb) orb[(((size_t)w * K + k) * Tp) * n * n + (size_t)i * n + j] = o0;
       if (T > 1) {
         int ti = 2 + 3 * i;
         for (int t = 2; t < T; ++t) {
@@ -150,6 +152,11 @@ struct EpiOrbital {
     }
   }
 };
+
+// The kernel and its launcher have internal linkage: every translation unit
+// that includes this header owns its own instantiations, and with them its own
+// record of which device already has the shared-memory opt-in set.
+namespace {
 
 // C[rows x N] = [A1 | A2][rows x (K1+K2)] * W[(K1+K2) x N].  K1 and K2 are
 // multiples of 8; W rows are read as float4, so ldw is a multiple of 4 with
@@ -274,5 +281,7 @@ cudaError_t launch_gemm_simt(cudaStream_t s, int n_groups, RowMap map, const flo
   k_gemm_simt<Epi><<<grid, 256, kSimtSmem, s>>>(n_groups, map, A1, lda1, K1, A2, lda2, K2, W, ldw, N, epi);
   return cudaGetLastError();
 }
+
+}  // namespace
 
 }  // namespace qmc

@@ -969,6 +969,109 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
 }
 
 // =====================================================================
+// determinant backward: dlog|psi| / dA_k = w_k A_k^{-T}, w_k = D_k / psi
+// (the cotangent of slogdet + signed log-sum-exp,
+//  src/jaqmc/wavefunction/output/logdet.py:53-80)
+// =====================================================================
+template <typename S>
+__device__ void det_inverse(const float* __restrict__ Ak, int n, char* scratch, double* ld, float* sg, int* sing,
+                            double* growth) {
+  const int lane = threadIdx.x & 31;
+  const DetScratch sc(n);
+  S* LU = reinterpret_cast<S*>(scratch);
+  S* Ainv = LU + n * sc.ld;
+  int* perm = reinterpret_cast<int*>(scratch + (size_t)(2 * n * sc.ld + 2 * n * sc.ldm) * 8);
+  for (int e = lane; e < n * n; e += 32) LU[(e / n) * sc.ld + (e % n)] = (S)Ak[e];
+  __syncwarp();
+  warp_lu<S>(LU, n, sc.ld, perm, ld, sg, growth, sing);
+  if (!*sing) warp_inverse<S>(LU, Ainv, perm, n, sc.ld);
+}
+
+__global__ void k_logdet_bwd(int n, int K, const float* __restrict__ A, float* __restrict__ Abar,
+                             float* __restrict__ logpsi) {
+  extern __shared__ double shb[];
+  const int w = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  double* lds = shb;                                   // [K]
+  float* sgs = reinterpret_cast<float*>(lds + K);      // [K]
+  int* dbl = reinterpret_cast<int*>(sgs + K);          // [K] factorise in FP64
+  float* wk = reinterpret_cast<float*>(dbl + K);       // [K]
+  const DetScratch sc(n);
+  char* scratch = reinterpret_cast<char*>(shb) + align_up((size_t)K * 20 + 16, 16) + sc.bytes * warp;
+  const size_t ts = (size_t)n * n;
+  for (int k = warp; k < K; k += nw) {
+    const float* Ak = A + ((size_t)w * K + k) * ts;
+    double ld, growth;
+    float sg;
+    int sing;
+    det_inverse<float>(Ak, n, scratch, &ld, &sg, &sing, &growth);
+    int use64 = !sing && !(growth <= (double)kRefactorGrowth);
+    if (use64) det_inverse<double>(Ak, n, scratch, &ld, &sg, &sing, &growth);
+    if (lane == 0) {
+      lds[k] = ld;
+      sgs[k] = sing ? 0.f : sg;
+      dbl[k] = use64;
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (warp == 0) {
+    double lmax = -INFINITY;
+    for (int k = lane; k < K; k += 32)
+      if (sgs[k] != 0.f) lmax = fmax(lmax, lds[k]);
+    for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    double S = 0.0;
+    for (int k = lane; k < K; k += 32)
+      if (sgs[k] != 0.f) S += (double)sgs[k] * exp(lds[k] - lmax);
+    S = warp_sum(S);
+    for (int k = lane; k < K; k += 32) wk[k] = sgs[k] != 0.f ? (float)((double)sgs[k] * exp(lds[k] - lmax) / S) : 0.f;
+    if (lane == 0 && logpsi) logpsi[w] = (float)(log(fabs(S)) + lmax);
+  }
+  __syncthreads();
+  // second pass: A_k^{-1} again (the scratch holds one determinant per warp)
+  for (int k = warp; k < K; k += nw) {
+    const float* Ak = A + ((size_t)w * K + k) * ts;
+    float* Bk = Abar + ((size_t)w * K + k) * ts;
+    if (sgs[k] == 0.f) {
+      for (int e = lane; e < n * n; e += 32) Bk[e] = 0.f;
+      continue;
+    }
+    double ld, growth;
+    float sg;
+    int sing;
+    if (dbl[k]) {
+      det_inverse<double>(Ak, n, scratch, &ld, &sg, &sing, &growth);
+      const double* Ainv = reinterpret_cast<const double*>(scratch) + n * sc.ld;
+      for (int e = lane; e < n * n; e += 32) Bk[e] = (float)((double)wk[k] * Ainv[(e % n) * sc.ld + e / n]);
+    } else {
+      det_inverse<float>(Ak, n, scratch, &ld, &sg, &sing, &growth);
+      const float* Ainv = reinterpret_cast<const float*>(scratch) + n * sc.ld;
+      for (int e = lane; e < n * n; e += 32) Bk[e] = wk[k] * Ainv[(e % n) * sc.ld + e / n];
+    }
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_logdet_bwd(cudaStream_t s, int B, int n, int K, const float* A, float* Abar, float* logpsi) {
+  const DetScratch sc(n);
+  const size_t head = align_up((size_t)K * 20 + 16, 16);
+  int nw = (int)((200 * 1024 - head) / sc.bytes);
+  nw = std::max(1, std::min(std::min(nw, 8), K));
+  const size_t sm = head + sc.bytes * nw;
+  static int attr_dev = -1;
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (attr_dev != dev) {
+    e = cudaFuncSetAttribute(k_logdet_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_dev = dev;
+  }
+  k_logdet_bwd<<<B, 32 * nw, sm, s>>>(n, K, A, Abar, logpsi);
+  return cudaGetLastError();
+}
+
+// =====================================================================
 // Metropolis-Hastings (src/jaqmc/sampler/mcmc.py:53-54, 96-137)
 // =====================================================================
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
@@ -1131,6 +1234,20 @@ cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double
 // =====================================================================
 // parameter preparation
 // =====================================================================
+__global__ void k_transpose_f32(const float* __restrict__ in, int rows, int cols, int ld_in,
+                                float* __restrict__ out) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)rows * cols) return;
+  int r = (int)(e % rows), c = (int)(e / rows);  // out[c][r]
+  out[e] = in[(size_t)r * ld_in + c];
+}
+
+cudaError_t launch_transpose_f32(cudaStream_t s, const float* in, int rows, int cols, int ld_in, float* out) {
+  size_t total = (size_t)rows * cols;
+  k_transpose_f32<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(in, rows, cols, ld_in, out);
+  return cudaGetLastError();
+}
+
 __global__ void k_transpose_split(const float* __restrict__ in, int rows, int cols, int ld_in,
                                   __nv_bfloat16* __restrict__ out, int rows_p, int cols_p) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -47,6 +47,10 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor);
 
+// Cotangent of log|psi| with respect to the value orbital matrices:
+// Abar[w][k] = w_k A_k^{-T}; also writes log|psi| (may be null).
+cudaError_t launch_logdet_bwd(cudaStream_t s, int B, int n, int K, const float* A, float* Abar, float* logpsi);
+
 // MH proposal x' = x + stddev * N(0,1) for update `step` of a call.
 cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
                               float stddev, uint64_t seed, uint64_t ctr, const float* inj_normals);
@@ -59,6 +63,9 @@ cudaError_t launch_mh_draws(cudaStream_t s, int B, int n, int steps, uint64_t se
 cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float* out);
 
 cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out);
+
+// fp32 [rows][cols] (row stride ld_in) -> fp32 transposed [cols][rows]
+cudaError_t launch_transpose_f32(cudaStream_t s, const float* in, int rows, int cols, int ld_in, float* out);
 
 // fp32 [rows][cols] -> transposed split-bf16 planes hi/lo of [cols_p][rows_p]
 // (zero padded; the lo plane starts cols_p*rows_p elements after hi)

@@ -26,4 +26,10 @@ qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, 
 qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
                     float* logpsi, float* sign, float* ke, float* el, uint8_t* flags, cudaStream_t s);
 
+// Adjoint (adjoint.cu): workspace bytes for `batch` walkers under the model's
+// gradient budget, and the chunked forward + backward driver.
+size_t grad_workspace(const qmc_model* m, int batch);
+qmc_status run_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
+                    double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s);
+
 }  // namespace qmc

@@ -64,3 +64,36 @@ def hydrogenic_tree(cfg: P.FermiNetConfig, n_atoms: int, sigma: float, seed=0):
         leaf["sigma"][:] = sigma
         leaf["pi"][:] = 1.0
     return tree
+
+
+def oracle_param_jacobian(flat, cfg, mol, x):
+    """(B, P) float64 d log|psi_w| / d theta by torch autograd on the oracle
+    (the role of the reference's jax.grad), in the flat leaf order."""
+    leaves = P.ferminet_leaves(cfg, mol.n_atoms)
+    ts = []
+    tree = {}
+    off = 0
+    for path, shape in leaves:
+        size = int(np.prod(shape))
+        t = torch.tensor(np.asarray(flat[off:off + size], np.float64).reshape(shape), requires_grad=True)
+        off += size
+        ts.append(t)
+        node = tree.setdefault("params", {})
+        for k in path[:-1]:
+            node = node.setdefault(k, {})
+        node[path[-1]] = t
+    out = OF.evaluate(tree, oracle_cfg(cfg), torch.as_tensor(x, dtype=torch.float64), mol.atoms,
+                      dtype=torch.float64)
+    lp = out["logpsi"]
+    rows = []
+    for w in range(lp.shape[0]):
+        g = torch.autograd.grad(lp[w], ts, retain_graph=True, allow_unused=True)
+        rows.append(torch.cat([(gi if gi is not None else torch.zeros_like(t)).reshape(-1)
+                               for gi, t in zip(g, ts)]))
+    return torch.stack(rows).numpy(), lp.detach().numpy()
+
+
+def oracle_logpsi_flat(flat, cfg, mol, x):
+    tree = P.unflatten(np.asarray(flat, np.float64), P.ferminet_leaves(cfg, mol.n_atoms))
+    return OF.evaluate(tree, oracle_cfg(cfg), torch.as_tensor(x, dtype=torch.float64), mol.atoms,
+                       dtype=torch.float64)["logpsi"].numpy()
