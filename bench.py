@@ -191,6 +191,32 @@ def workload_name(wl, prec):
             f"{wl['mh_steps']} MH steps + forward-Laplacian E_L, {prec}")
 
 
+# ----------------------------------------------------------------- serving
+def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
+    """Poisson(rate) arrivals of neutral-atom jobs (Z ~ U{2..18}, Hund spins,
+    walkers ~ U{256..4096}), each ``requests`` requests of 20 MH steps + E_L
+    mean/variance in the mixed form, served with ``slots`` concurrent slots."""
+    from jaqmc_gb300 import serving as SV
+    be = SV.CudaBackend(precision="mixed", mh_steps=20, stddev=0.02, device=dev)
+    warm = SV.Server(be, n_slots=2, hbm_budget=budget_gb << 30)
+    warm.run_arrivals(SV.atom_job_specs(3, rate=0.0, seed=10_000, requests=2, walker_choices=(256,)))
+    srv = SV.Server(be, n_slots=slots, hbm_budget=budget_gb << 30)
+    specs = SV.atom_job_specs(n_jobs, rate, seed=seed, requests=requests)
+    srv.run_arrivals(specs)
+    first = min(sp.arrival for sp in specs)
+    span = max(st.finished for st in srv.finished_jobs) - first
+    lat, jl = srv.request_latencies_ms(), srv.job_latencies_ms()
+    ws = sum(sp.walkers * 20 * requests for sp in specs)
+    bad = [st.spec.job_id for st in srv.finished_jobs if not np.all(np.isfinite(np.stack(st.results)[:, :2]))]
+    return {"arrival_rate_jobs_per_s": rate, "jobs": n_jobs, "requests_per_job": requests, "slots": slots,
+            "hbm_budget_gb": budget_gb, "jobs_per_s": n_jobs / span, "requests_per_s": n_jobs * requests / span,
+            "walker_steps_per_s": ws / span, "request_p50_ms": float(np.percentile(lat, 50)),
+            "request_p99_ms": float(np.percentile(lat, 99)), "job_p50_ms": float(np.percentile(jl, 50)),
+            "job_p99_ms": float(np.percentile(jl, 99)), "peak_hbm_gb": srv.peak_used / 1e9,
+            "graph_replays": int(sum(r.graph for r in srv.finished)), "nonfinite_jobs": bad,
+            "span_s": span}
+
+
 # ----------------------------------------------------------------- GPU side
 def run_ours(args, wl):
     import torch
@@ -337,6 +363,9 @@ def run_ours(args, wl):
         rl = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "peak_source": pname,
               "unit": unit, "frac": achieved / peak, "traffic": TRAFFIC.get((wl["system"], prec_main)),
               "launches_per_step": launches_dom / args.steps, "ms_per_step": ms_dom / args.steps}
+    serve = None
+    if not args.no_serve:
+        serve = run_serving(dev, args.serve_rate, args.serve_jobs, args.serve_requests, slots=args.serve_slots)
     cpu = None
     if rank == 0 and not args.no_cpu:
         r, cores, desc = cpu_request_rate(wl)
@@ -361,6 +390,7 @@ def run_ours(args, wl):
             "gpu_launches": launches,
             "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items()},
             "roofline": rl,
+            "serving": serve,
             "cpu_baseline": cpu,
             "clocks": clk,
         }
@@ -387,7 +417,19 @@ def main():
     ap.add_argument("--burn-in", type=int, default=200)
     ap.add_argument("--oracle-walkers", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-only", action="store_true", help="print only the serving measurement")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrival rate (jobs/s)")
+    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--serve-requests", type=int, default=2)
+    ap.add_argument("--serve-slots", type=int, default=8)
     args = ap.parse_args()
+    if args.serve_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_serving(torch.device("cuda", 0), args.serve_rate, args.serve_jobs,
+                                     args.serve_requests, slots=args.serve_slots)), flush=True)
+        return 0
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     wl = WORKLOADS[args.workload]

@@ -140,6 +140,19 @@ qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64
                         const float* inj_normals, const float* inj_uniforms, uint8_t* flags,
                         void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+/* qmc_mh_steps with the Philox update counter resident in device memory:
+ * update s of the call uses step = *counter + s, and *counter is advanced by
+ * `steps` on the stream when the call's work is done.  Nothing on the host
+ * depends on the counter, so a request (this call, qmc_local_energy and
+ * qmc_reduce_mean_var on fixed buffers) can be captured once into a CUDA graph
+ * and replayed: every replay continues the job's random stream.  No draw
+ * injection.  Reference counterpart: the sampler state's PRNG key threaded
+ * through MCMCSampler.step (src/jaqmc/sampler/mcmc.py:160-199). */
+qmc_status qmc_mh_steps_resident(qmc_model* m, int batch, int steps, float stddev, uint64_t seed,
+                                 uint64_t* counter, float* electrons, float* log_prob, uint32_t* accepts,
+                                 uint8_t* flags, void* workspace, size_t workspace_bytes,
+                                 cudaStream_t stream);
+
 /* The draws qmc_mh_steps would use for (seed, counter, steps): normals
  * (steps,batch,n,3) and uniforms (steps,batch), either may be NULL. */
 qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,

@@ -62,6 +62,9 @@ _SIGS = {
     "qmc_mh_steps": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_uint64,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "qmc_mh_steps_resident": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_size_t, C.c_void_p]),
     "qmc_mh_draws": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p,
                                C.c_void_p, C.c_void_p]),
     "qmc_reduce_mean_var": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -147,10 +150,13 @@ class NativeFermiNet:
     def __init__(self, cfg, atoms, charges, precision="fp32", device=None):
         lib = load()
         self.lib = lib
-        self.device = torch.device(device or "cuda")
-        torch.cuda.set_device(self.device)
         if not torch.cuda.is_available():
             raise RuntimeError("no CUDA device: the qmc library has no CPU fallback")
+        dev = torch.device(device or "cuda")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        torch.cuda.set_device(self.device)
         device_check()
         c = FermiNetConfigC()
         c.n_up, c.n_down = int(cfg.nspins[0]), int(cfg.nspins[1])
@@ -252,6 +258,21 @@ class NativeFermiNet:
                                     ptr(log_prob), ptr(accepts), ptr(normals), ptr(uniforms), ptr(fl),
                                     ptr(ws), ws.numel(), stream_handle(stream)))
         return e, log_prob, accepts, fl
+
+    def mh_steps_resident(self, electrons, steps, stddev, seed, counter, log_prob, accepts, flags=None,
+                          ws=None, stream=None):
+        """MH updates with the Philox counter in device memory (uint64 tensor of
+        one element, advanced by ``steps``); no host synchronisation."""
+        e = self._elec(electrons)
+        B = e.shape[0]
+        if counter.dtype != torch.uint64 and counter.dtype != torch.int64:
+            raise ValueError("counter must be a one-element 64-bit integer CUDA tensor")
+        if ws is None:
+            ws, _ = self.workspace(OP_MH, B)
+        check(self.lib.qmc_mh_steps_resident(self.h, B, int(steps), float(stddev), int(seed), ptr(counter),
+                                             ptr(e), ptr(log_prob), ptr(accepts), ptr(flags), ptr(ws),
+                                             ws.numel(), stream_handle(stream)))
+        return e, log_prob, accepts
 
     def set_grad_budget(self, nbytes: int):
         check(self.lib.qmc_model_set_grad_budget(self.h, int(nbytes)))

@@ -470,6 +470,32 @@ qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, 
   return QMC_OK;
 }
 
+// Body of qmc_mh_steps / qmc_mh_steps_resident: the update index of step st is
+// counter + st (+ *ctr_dev when ctr_dev is set).
+qmc_status mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t seed, uint64_t counter,
+                    const uint64_t* ctr_dev, float* electrons, float* log_prob, uint32_t* accepts,
+                    const float* inj_normals, const float* inj_uniforms, uint8_t* flags, void* ws,
+                    size_t ws_bytes, cudaStream_t s) {
+  QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_MH));
+  if (!electrons || !log_prob || steps < 0) { set_error("bad electrons/log_prob/steps"); return QMC_ERR_ARG; }
+  Plan p = make_plan(m, QMC_OP_MH, batch);
+  const int n = m->d.n;
+  float* lpsi = at<float>(ws, p.lpsi);
+  // log_prob of the starting walkers (src/jaqmc/sampler/mcmc.py:166)
+  QMC_TRY(evaluate(m, p, ws, electrons, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, flags, s));
+  QMC_PROF(QMC_KC_OTHER, launch_scale(s, batch, lpsi, 2.0f, log_prob));
+  float* xp = at<float>(ws, p.xp);
+  for (int st = 0; st < steps; ++st) {
+    const float* nz = inj_normals ? inj_normals + (size_t)st * batch * n * 3 : nullptr;
+    const float* uz = inj_uniforms ? inj_uniforms + (size_t)st * batch : nullptr;
+    QMC_PROF(QMC_KC_MH, launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, ctr_dev, nz));
+    QMC_TRY(evaluate(m, p, ws, xp, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, nullptr, s));
+    QMC_PROF(QMC_KC_MH, launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, ctr_dev,
+                                         uz, accepts));
+  }
+  return QMC_OK;
+}
+
 }  // namespace qmc
 
 using namespace qmc;
@@ -684,22 +710,17 @@ qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64
                         float* electrons, float* log_prob, uint32_t* accepts, const float* inj_normals,
                         const float* inj_uniforms, uint8_t* flags, void* ws, size_t ws_bytes,
                         cudaStream_t s) {
-  QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_MH));
-  if (!electrons || !log_prob || steps < 0) { set_error("bad electrons/log_prob/steps"); return QMC_ERR_ARG; }
-  Plan p = make_plan(m, QMC_OP_MH, batch);
-  const int n = m->d.n;
-  float* lpsi = at<float>(ws, p.lpsi);
-  // log_prob of the starting walkers (src/jaqmc/sampler/mcmc.py:166)
-  QMC_TRY(evaluate(m, p, ws, electrons, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, flags, s));
-  QMC_PROF(QMC_KC_OTHER, launch_scale(s, batch, lpsi, 2.0f, log_prob));
-  float* xp = at<float>(ws, p.xp);
-  for (int st = 0; st < steps; ++st) {
-    const float* nz = inj_normals ? inj_normals + (size_t)st * batch * n * 3 : nullptr;
-    const float* uz = inj_uniforms ? inj_uniforms + (size_t)st * batch : nullptr;
-    QMC_PROF(QMC_KC_MH, launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, nz));
-    QMC_TRY(evaluate(m, p, ws, xp, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, nullptr, s));
-    QMC_PROF(QMC_KC_MH, launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, uz, accepts));
-  }
+  return qmc::mh_steps(m, batch, steps, stddev, seed, counter, nullptr, electrons, log_prob, accepts,
+                       inj_normals, inj_uniforms, flags, ws, ws_bytes, s);
+}
+
+qmc_status qmc_mh_steps_resident(qmc_model* m, int batch, int steps, float stddev, uint64_t seed,
+                                 uint64_t* counter, float* electrons, float* log_prob, uint32_t* accepts,
+                                 uint8_t* flags, void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (!counter) { set_error("null device counter"); return QMC_ERR_ARG; }
+  QMC_TRY(qmc::mh_steps(m, batch, steps, stddev, seed, 0, counter, electrons, log_prob, accepts, nullptr,
+                        nullptr, flags, ws, ws_bytes, s));
+  QMC_PROF(QMC_KC_OTHER, launch_counter_add(s, counter, (uint64_t)steps));
   return QMC_OK;
 }
 

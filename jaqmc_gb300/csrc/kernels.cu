@@ -1090,10 +1090,11 @@ __device__ __forceinline__ U4 draw_block(uint64_t seed, uint64_t step, int w, in
 
 __global__ void k_mh_propose(int B, int n, const float* __restrict__ x, float* __restrict__ xp,
                              float stddev, uint64_t seed, uint64_t step,
-                             const float* __restrict__ inj) {
+                             const uint64_t* __restrict__ ctr_dev, const float* __restrict__ inj) {
   const int nb = normal_blocks(n);
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (size_t)B * nb) return;
+  if (ctr_dev) step += *ctr_dev;
   int w = (int)(e / nb), b = (int)(e % nb);
   float z[4];
   if (inj) {
@@ -1118,18 +1119,20 @@ __global__ void k_mh_propose(int B, int n, const float* __restrict__ x, float* _
 }
 
 cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
-                              float stddev, uint64_t seed, uint64_t ctr, const float* inj) {
+                              float stddev, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
+                              const float* inj) {
   size_t total = (size_t)B * normal_blocks(n);
-  k_mh_propose<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, x, xp, stddev, seed, ctr, inj);
+  k_mh_propose<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, x, xp, stddev, seed, ctr, ctr_dev, inj);
   return cudaGetLastError();
 }
 
 __global__ void k_mh_accept(int B, int n, float* __restrict__ x, const float* __restrict__ xp,
                             float* __restrict__ lp, const float* __restrict__ logpsi_p,
-                            uint64_t seed, uint64_t step, const float* __restrict__ inj,
-                            uint32_t* __restrict__ accepts) {
+                            uint64_t seed, uint64_t step, const uint64_t* __restrict__ ctr_dev,
+                            const float* __restrict__ inj, uint32_t* __restrict__ accepts) {
   int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= B) return;
+  if (ctr_dev) step += *ctr_dev;
   float u = inj ? inj[w] : u01(draw_block(seed, step, w, normal_blocks(n)).x);
   float lp2 = 2.0f * logpsi_p[w];
   float ratio = lp2 - lp[w];
@@ -1142,10 +1145,19 @@ __global__ void k_mh_accept(int B, int n, float* __restrict__ x, const float* __
 }
 
 cudaError_t launch_mh_accept(cudaStream_t s, int B, int n, float* x, const float* xp, float* lp,
-                             const float* logpsi_p, uint64_t seed, uint64_t ctr,
+                             const float* logpsi_p, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
                              const float* inj_uniforms, uint32_t* accepts) {
-  k_mh_accept<<<(B + 127) / 128, 128, 0, s>>>(B, n, x, xp, lp, logpsi_p, seed, ctr, inj_uniforms,
+  k_mh_accept<<<(B + 127) / 128, 128, 0, s>>>(B, n, x, xp, lp, logpsi_p, seed, ctr, ctr_dev, inj_uniforms,
                                               accepts);
+  return cudaGetLastError();
+}
+
+__global__ void k_counter_add(uint64_t* ctr, uint64_t inc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *ctr += inc;
+}
+
+cudaError_t launch_counter_add(cudaStream_t s, uint64_t* ctr, uint64_t inc) {
+  k_counter_add<<<1, 32, 0, s>>>(ctr, inc);
   return cudaGetLastError();
 }
 

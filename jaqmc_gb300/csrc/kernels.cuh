@@ -52,12 +52,16 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
 cudaError_t launch_logdet_bwd(cudaStream_t s, int B, int n, int K, const float* A, float* Abar, float* logpsi);
 
 // MH proposal x' = x + stddev * N(0,1) for update `step` of a call.
+// The update index is ctr (+ *ctr_dev when ctr_dev is not null).
 cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
-                              float stddev, uint64_t seed, uint64_t ctr, const float* inj_normals);
-// Accept/reject with 2 log|psi| and the draw for update `ctr`.
+                              float stddev, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
+                              const float* inj_normals);
+// Accept/reject with 2 log|psi| and the draw for update `ctr` (+ *ctr_dev).
 cudaError_t launch_mh_accept(cudaStream_t s, int B, int n, float* x, const float* xp, float* lp,
-                             const float* logpsi_p, uint64_t seed, uint64_t ctr,
+                             const float* logpsi_p, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
                              const float* inj_uniforms, uint32_t* accepts);
+// *ctr += inc on the stream.
+cudaError_t launch_counter_add(cudaStream_t s, uint64_t* ctr, uint64_t inc);
 cudaError_t launch_mh_draws(cudaStream_t s, int B, int n, int steps, uint64_t seed, uint64_t ctr,
                             float* normals, float* uniforms);
 cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float* out);

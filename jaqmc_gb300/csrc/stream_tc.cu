@@ -580,10 +580,21 @@ int tc_padded_tangents(int T) {
   return -1;
 }
 
+// Pipeline stages that fit next to two epilogue staging buffers.
+static int tc_stages_fitting(int n_cols, int ebuf_bytes) {
+  const int stage_bytes = 2 * kATile + 2 * n_cols * kKChunk * 2;
+  const long avail = 227L * 1024 - 1024 - 256 - 2L * ebuf_bytes - 64;
+  return (int)std::min<long>(4, avail / stage_bytes);
+}
+
+// Epilogue staging bytes per half of a tangent layer tile: two planes x Tp
+// rows x 128 bf16 (16 rows when Tp == 1).
+static int tc_layer_ebuf(int Tp) { return 2 * 128 * 2 * (Tp == 1 ? 16 : Tp); }
+
 int tc_groups_per_tile(int Tp) {
   if (Tp == 1) return 256;
   for (int G = 256 / Tp; G >= 1; --G)
-    if ((G * Tp) % 16 == 0) return G;
+    if ((G * Tp) % 16 == 0 && tc_stages_fitting(G * Tp, tc_layer_ebuf(Tp)) >= 2) return G;
   return 0;
 }
 
@@ -638,8 +649,7 @@ static qmc_status launch(cudaStream_t s, const CUtensorMap& A0, const CUtensorMa
                          const CUtensorMap& B2, TcArgs g, int n_tiles, const Epi& epi) {
   if (n_tiles <= 0) return QMC_OK;
   const int stage_bytes = 2 * kATile + 2 * g.n_cols * kKChunk * 2;
-  const size_t avail = 227 * 1024 - 1024 - 256 - 2 * (size_t)g.ebuf_bytes - 64;
-  g.stages = std::min<int>(4, (int)(avail / stage_bytes));
+  g.stages = tc_stages_fitting(g.n_cols, g.ebuf_bytes);
   if (g.stages < 2) {
     set_error("tile of %d columns does not fit two pipeline stages", g.n_cols);
     return QMC_ERR_SHAPE;
@@ -697,7 +707,7 @@ qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
     return QMC_ERR_SHAPE;
   }
   g.resid_last = 0;
-  g.ebuf_bytes = 2 * 128 * 2 * (a.T == 1 ? 16 : a.Tp);  // two planes x rows x 128 bf16
+  g.ebuf_bytes = tc_layer_ebuf(a.T == 1 ? 1 : a.Tp);
   if (a.n_out % 8) {
     set_error("tensor-core layer: output width %d is not a multiple of 8", a.n_out);
     return QMC_ERR_SHAPE;

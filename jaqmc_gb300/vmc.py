@@ -1,0 +1,342 @@
+"""Host-side mirror of the reference's wavefunction / sampler / estimator
+protocols, backed by the GB300 library (``libqmc.so``).
+
+Each class keeps the reference's name, fields, method signatures and stats
+keys so that a workflow written against the reference drops onto this
+implementation:
+
+* :class:`MoleculeData`, :class:`BatchedData` — ``src/jaqmc/app/molecule/data.py:13-28``,
+  ``src/jaqmc/data.py`` (electrons batched on axis 0).
+* :class:`FermiNetWavefunction` — ``src/jaqmc/app/molecule/wavefunction/ferminet.py:21-137``
+  (``init_params``, ``evaluate``, ``logpsi``, ``phase_logpsi``); evaluation is
+  batched (the reference's callers ``vmap`` a single-walker function).
+* :class:`MCMCSampler` — ``src/jaqmc/sampler/mcmc.py:58-199`` (``init``, ``step``,
+  width adaptation, ``pmove``).
+* :class:`EuclideanKinetic`, :func:`potential_energy`, :class:`TotalEnergy`,
+  :class:`LossAndGrad`, :func:`mean_reduce` — ``src/jaqmc/estimator/kinetic/euclidean.py:29-135``,
+  ``src/jaqmc/app/molecule/hamiltonian.py:9-22``, ``src/jaqmc/estimator/total_energy.py:16-70``,
+  ``src/jaqmc/estimator/loss_grad.py:25-128``, ``src/jaqmc/estimator/base.py:27-53``.
+
+Everything numerical runs on the GPU through the C ABI; there is no CPU path.
+"""
+from __future__ import annotations
+
+import dataclasses
+from dataclasses import dataclass, field
+from typing import Any, NamedTuple
+
+import numpy as np
+import torch
+
+from . import _native
+from . import params as P
+
+
+# ----------------------------------------------------------------- data
+@dataclass
+class MoleculeData:
+    electrons: Any  # (n, 3) or (B, n, 3)
+    atoms: Any      # (A, 3)
+    charges: Any    # (A,)
+
+    def merge(self, other: dict) -> "MoleculeData":
+        return dataclasses.replace(self, **other)
+
+    def subset(self, keys):
+        return {k: getattr(self, k) for k in keys}
+
+    def __getitem__(self, key):
+        return getattr(self, key)
+
+
+@dataclass
+class BatchedData:
+    data: MoleculeData
+    fields_with_batch: list = field(default_factory=lambda: ["electrons"])
+
+    @property
+    def batch_size(self) -> int:
+        return int(self.data.electrons.shape[0])
+
+
+def _device_electrons(e, device) -> torch.Tensor:
+    t = torch.as_tensor(e)
+    if t.dim() == 2:
+        t = t.unsqueeze(0)
+    return t.to(device=device, dtype=torch.float32).contiguous()
+
+
+# ----------------------------------------------------------------- wavefunction
+class DeviceParams:
+    """A parameter tree plus its flat float32 copy on the device (the layout of
+    ``qmc_model_set_params``).  Optimisers may update ``flat`` in place; call
+    :meth:`touch` afterwards so the model reloads it."""
+
+    def __init__(self, tree, leaves, device):
+        self.leaves = leaves
+        self.flat = torch.as_tensor(P.flatten(tree, leaves), device=device)
+        self.version = 0
+
+    def touch(self):
+        self.version += 1
+
+    def tree(self):
+        return P.unflatten(self.flat.detach().cpu().numpy(), self.leaves)
+
+
+@dataclass
+class FermiNetWavefunction:
+    """FermiNet ansatz (same hyper-parameters and defaults as the reference)
+    evaluated by the GB300 library.  ``precision`` selects the plain FP32 or the
+    split-BF16 tensor-core form."""
+
+    nspins: tuple = (1, 1)
+    ndets: int = 16
+    hidden_dims_single: list = field(default_factory=lambda: [256] * 4)
+    hidden_dims_double: list = field(default_factory=lambda: [32] * 4)
+    use_last_layer: bool = False
+    envelope: str = "abs_isotropic"
+    orbitals_spin_split: bool = True
+    full_det: bool = True
+    precision: str = "fp32"
+    device: Any = None
+
+    def __post_init__(self):
+        self._models = {}
+        self._loaded = {}
+
+    @property
+    def config(self) -> P.FermiNetConfig:
+        return P.FermiNetConfig(nspins=tuple(self.nspins), ndets=self.ndets,
+                                hidden_dims_single=list(self.hidden_dims_single),
+                                hidden_dims_double=list(self.hidden_dims_double),
+                                use_last_layer=self.use_last_layer, envelope=self.envelope,
+                                orbitals_spin_split=self.orbitals_spin_split)
+
+    def _dev(self):
+        dev = torch.device(self.device or "cuda")
+        return dev if dev.index is not None else torch.device("cuda", torch.cuda.current_device())
+
+    # -- protocol ------------------------------------------------------
+    def init_params(self, data: MoleculeData, rngs=0) -> DeviceParams:
+        seed = int(rngs) if np.isscalar(rngs) else int(np.asarray(rngs).ravel()[0])
+        atoms = np.asarray(data.atoms, np.float64).reshape(-1, 3)
+        tree = P.init_ferminet(self.config, atoms.shape[0], seed=seed)
+        return DeviceParams(tree, P.ferminet_leaves(self.config, atoms.shape[0]), self._dev())
+
+    def model(self, data: MoleculeData, params: DeviceParams) -> _native.NativeFermiNet:
+        atoms = np.asarray(torch.as_tensor(data.atoms).cpu(), np.float32).reshape(-1, 3)
+        charges = np.asarray(torch.as_tensor(data.charges).cpu(), np.float32).reshape(-1)
+        key = (atoms.tobytes(), charges.tobytes(), self.precision)
+        m = self._models.get(key)
+        if m is None:
+            m = _native.NativeFermiNet(self.config, atoms, charges, precision=self.precision,
+                                       device=self._dev())
+            self._models[key] = m
+        stamp = (id(params), params.version)
+        if self._loaded.get(key) != stamp:
+            m.set_params(params.flat)
+            self._loaded[key] = stamp
+        return m
+
+    def evaluate(self, params: DeviceParams, data: MoleculeData) -> dict:
+        m = self.model(data, params)
+        lp, sg, fl = m.forward(_device_electrons(data.electrons, self._dev()))
+        return {"logpsi": lp, "sign_logpsi": sg, "flags": fl}
+
+    def logpsi(self, params, data):
+        return self.evaluate(params, data)["logpsi"]
+
+    def phase_logpsi(self, params, data):
+        out = self.evaluate(params, data)
+        return out["sign_logpsi"], out["logpsi"]
+
+    def orbitals(self, params, data):
+        raise NotImplementedError("orbital matrices are internal to the GPU path (pretraining is out of scope)")
+
+    def batch_log_prob(self, params: DeviceParams, data: MoleculeData) -> "BoundLogProb":
+        """The ``2 log|psi|`` callable that :class:`MCMCSampler` runs on the GPU."""
+        return BoundLogProb(self, params, data)
+
+
+@dataclass
+class BoundLogProb:
+    """``x -> 2 log|psi(x)|`` bound to a wavefunction, parameters and system."""
+
+    wf: FermiNetWavefunction
+    params: DeviceParams
+    data: MoleculeData
+
+    def __call__(self, electrons):
+        return 2.0 * self.wf.logpsi(self.params, self.data.merge({"electrons": electrons}))
+
+
+# ----------------------------------------------------------------- sampler
+class MCMCState(NamedTuple):
+    stddev: float
+    pmoves: np.ndarray
+    counter: int
+    rng_counter: int
+    seed: int
+
+
+@dataclass
+class MCMCSampler:
+    """All-electron Gaussian Metropolis-Hastings sampler (Philox draws on the GPU)."""
+
+    steps: int = 10
+    initial_width: float = 0.1
+    adapt_frequency: int = 100
+    pmove_range: tuple = (0.5, 0.55)
+
+    def init(self, data, rngs=0) -> MCMCState:
+        seed = int(rngs) if np.isscalar(rngs) else int(np.asarray(rngs).ravel()[0])
+        return MCMCState(float(self.initial_width), np.zeros(self.adapt_frequency), 0, 0, seed)
+
+    def step(self, batch_log_prob: BoundLogProb, data, state: MCMCState, rngs=None):
+        if not isinstance(batch_log_prob, BoundLogProb):
+            raise TypeError("MCMCSampler.step needs the BoundLogProb of a GB300 wavefunction "
+                            "(FermiNetWavefunction.batch_log_prob)")
+        if self.steps == 0:
+            return data, {"pmove": 0.0}, state
+        wf, params, system = batch_log_prob.wf, batch_log_prob.params, batch_log_prob.data
+        electrons = data["electrons"] if isinstance(data, dict) else data.electrons
+        x = _device_electrons(electrons, wf._dev()).clone()
+        m = wf.model(system, params)
+        accepts = torch.zeros(x.shape[0], dtype=torch.int32, device=x.device)
+        m.mh_steps(x, self.steps, state.stddev, state.seed, state.rng_counter, accepts=accepts)
+        pmove = float(accepts.sum().item()) / (self.steps * x.shape[0])
+        # width adaptation (src/jaqmc/sampler/mcmc.py:182-197)
+        counter = state.counter + 1
+        t = counter % self.adapt_frequency
+        pmoves = state.pmoves.copy()
+        pmoves[t] = pmove
+        stddev = state.stddev
+        if t == 0:
+            mean = float(np.mean(pmoves))
+            if mean > self.pmove_range[1]:
+                stddev = stddev * 1.1
+            elif mean < self.pmove_range[0]:
+                stddev = stddev / 1.1
+        new_state = MCMCState(stddev, pmoves, counter, state.rng_counter + self.steps, state.seed)
+        new_data = {"electrons": x} if isinstance(data, dict) else data.merge({"electrons": x})
+        return new_data, {"pmove": pmove}, new_state
+
+
+# ----------------------------------------------------------------- estimators
+def mean_reduce(walker_stats: dict, include_variance: bool = True) -> dict:
+    """FP64 walker-batch mean and variance on the GPU (NaNs skipped)."""
+    out = {}
+    for k, v in walker_stats.items():
+        mv = _native.reduce_mean_var(torch.as_tensor(v).reshape(-1)).cpu().numpy()
+        out[k] = float(mv[0])
+        if include_variance:
+            out[f"{k}_var"] = float(mv[1])
+    return out
+
+
+class _EnergyCache:
+    """Local energies of the last (params, walkers) evaluated, shared by the
+    kinetic and potential estimators so one GPU pass serves both."""
+
+    def __init__(self):
+        self.key = None
+        self.value = None
+
+    def get(self, wf, params, data):
+        e = data.electrons
+        key = (id(wf), id(params), params.version, id(e), getattr(e, "_version", None))
+        if self.key != key:
+            m = wf.model(data, params)
+            self.value = m.local_energy(_device_electrons(e, wf._dev()))
+            self.key = key
+        return self.value
+
+
+_energy_cache = _EnergyCache()
+
+
+@dataclass
+class EuclideanKinetic:
+    """Forward-Laplacian kinetic energy ``-1/2 (lap log|psi| + |grad log|psi||^2)``."""
+
+    f_log_psi: Any = None  # the FermiNetWavefunction
+    data_field: str = "electrons"
+
+    def init(self, data, rngs=None):
+        return None
+
+    def evaluate_batch_walkers(self, params, batched_data: BatchedData, prev_walker_stats, state, rngs=None):
+        out = _energy_cache.get(self.f_log_psi, params, batched_data.data)
+        return {"energy:kinetic": out["kinetic"]}, state
+
+    def reduce(self, walker_stats):
+        return mean_reduce(walker_stats)
+
+
+def potential_energy(params, batched_data: BatchedData, prev_walker_stats, state, rngs=None, wf=None):
+    """Coulomb potential per walker (computed in the same GPU pass as E_L)."""
+    out = _energy_cache.get(wf, params, batched_data.data)
+    return {"energy:potential": out["potential"]}, state
+
+
+@dataclass
+class TotalEnergy:
+    output_name: str = "total_energy"
+    components: list | None = None
+
+    def evaluate_batch_walkers(self, params, batched_data, prev_walker_stats, state, rngs=None):
+        keys = self.components or [k for k in prev_walker_stats if k.startswith("energy:")]
+        total = None
+        for k in keys:
+            total = prev_walker_stats[k] if total is None else total + prev_walker_stats[k]
+        return {self.output_name: total}, state
+
+    def reduce(self, walker_stats):
+        return mean_reduce(walker_stats)
+
+
+def clip_observable(x: torch.Tensor, method: str = "mad", scale: float = 5.0) -> torch.Tensor:
+    """MAD / IQR clipping window (``src/jaqmc/utils/clip.py:11-68``), on the device."""
+    if method == "none":
+        return x
+    finite = x[torch.isfinite(x)]
+    if method == "mad":
+        med = finite.median()
+        dev = (finite - med).abs().median()
+        return x.clamp(med - scale * dev, med + scale * dev)
+    if method == "iqr":
+        q = torch.quantile(finite.double(), torch.tensor([0.25, 0.75], dtype=torch.float64, device=x.device))
+        iqr = q[1] - q[0]
+        return x.clamp(float(q[0] - scale * iqr), float(q[1] + scale * iqr))
+    raise ValueError(f"Unknown clip method {method!r}.")
+
+
+@dataclass
+class LossAndGrad:
+    """VMC energy gradient ``2 (<E_c g> - <E_c><g>)`` through the GPU adjoint;
+    the per-walker gradients are contracted on the device instead of being
+    materialised (``per_walker=True`` keeps them, e.g. for SR)."""
+
+    loss_key: str = "total_energy"
+    clip_method: str = "mad"
+    clip_scale: float = 5.0
+    f_log_psi: Any = None
+    per_walker: bool = False
+
+    def evaluate_batch_walkers(self, params, batched_data, prev_walker_stats, state, rngs=None):
+        return {"loss": prev_walker_stats[self.loss_key]}, state
+
+    def gradient(self, params, batched_data: BatchedData, loss: torch.Tensor):
+        wf = self.f_log_psi
+        loss = torch.as_tensor(loss).to(wf._dev()).double()
+        ec = clip_observable(loss, self.clip_method, self.clip_scale)
+        B = loss.shape[0]
+        weights = 2.0 * (ec - ec.mean()) / B
+        m = wf.model(batched_data.data, params)
+        J, g, _ = m.grad(_device_electrons(batched_data.data.electrons, wf._dev()), weights=weights,
+                         per_walker=self.per_walker)
+        stats = {"loss": float(loss.mean()), "clipped_loss": float(ec.mean()), "grads": g}
+        if J is not None:
+            stats["grad_logpsi"] = J
+        return stats

@@ -251,9 +251,17 @@ def _equilibrated(mol, cfg, flat, dev, B, steps=300, stddev=0.15, seed=3):
     return x.cpu().numpy()
 
 
-@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full"])
+# atoms whose tangent tiles take fewer groups per tensor-core tile (P: 48
+# tangent rows per electron, 4 groups; Ar: 56 rows, 2 groups)
+MIXED_EXTRA = {
+    "P-full": (lambda: S.atom(15), lambda: full_cfg(S.atom(15).nspins), 64),
+    "Ar-full": (lambda: S.atom(18), lambda: full_cfg(S.atom(18).nspins), 64),
+}
+
+
+@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full", "P-full", "Ar-full"])
 def test_mixed_form_on_equilibrated_walkers(case, cuda_device):
-    molf, cfgf, _ = CASES[case]
+    molf, cfgf, _ = {**CASES, **MIXED_EXTRA}[case]
     mol, cfg = molf(), cfgf()
     tree, flat, _ = setup(mol, cfg, 1)
     x = _equilibrated(mol, cfg, flat, cuda_device, 64)

@@ -1,0 +1,95 @@
+"""End-to-end use of the reference-shaped host API on the GPU.
+
+* VMC training of the hydrogen atom with FermiNet through FermiNetWavefunction,
+  MCMCSampler, the energy estimators and LossAndGrad (Adam on the flat
+  parameters) reaches -0.5 Ha (tests/hydrogen/atom_test.py:38-52 asserts the
+  same for its own ansatz).
+* The estimator pipeline's kinetic + potential equals qmc_local_energy.
+* The torch.autograd.Function and the torch.library custom op give the adjoint
+  gradient.
+"""
+import numpy as np
+import pytest
+import torch
+
+from jaqmc_gb300 import _native, torch_ops
+from jaqmc_gb300 import systems as S
+from jaqmc_gb300 import vmc
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(mol, walkers, seed=1):
+    x = torch.as_tensor(S.init_walkers(mol, walkers, seed=seed), device="cuda")
+    return vmc.MoleculeData(x, mol.atoms, mol.charges)
+
+
+def test_hydrogen_training_reaches_exact_energy(cuda_device):
+    mol = S.hydrogen()
+    wf = vmc.FermiNetWavefunction(nspins=(1, 0), ndets=2, hidden_dims_single=[16, 16], hidden_dims_double=[4, 4])
+    data = _system(mol, 1024)
+    params = wf.init_params(data, 0)
+    sampler = vmc.MCMCSampler(steps=10, initial_width=0.3)
+    state = sampler.init(data, 7)
+    kin = vmc.EuclideanKinetic(f_log_psi=wf)
+    tot = vmc.TotalEnergy()
+    lg = vmc.LossAndGrad(f_log_psi=wf)
+    opt = torch.optim.Adam([params.flat], lr=2e-2)
+    for _ in range(5):  # burn-in
+        d, _, state = sampler.step(wf.batch_log_prob(params, data), data, state)
+        data = data.merge({"electrons": d.electrons})
+    energies = []
+    for it in range(400):
+        d, stats, state = sampler.step(wf.batch_log_prob(params, data), data, state)
+        data = data.merge({"electrons": d.electrons})
+        bd = vmc.BatchedData(data)
+        ws = {}
+        ws.update(vmc.potential_energy(params, bd, ws, None, wf=wf)[0])
+        ws.update(kin.evaluate_batch_walkers(params, bd, ws, None)[0])
+        ws.update(tot.evaluate_batch_walkers(params, bd, ws, None)[0])
+        g = lg.gradient(params, bd, ws["total_energy"])
+        energies.append(vmc.mean_reduce({"e": ws["total_energy"]})["e"])
+        opt.zero_grad()
+        params.flat.grad = g["grads"].to(torch.float32)
+        opt.step()
+        params.touch()
+    e = float(np.mean(energies[-20:]))
+    assert abs(e + 0.5) < 5e-3, energies[-20:]
+    assert 0.3 < stats["pmove"] < 1.0
+
+
+def test_estimators_match_local_energy(cuda_device):
+    mol = S.methane()
+    wf = vmc.FermiNetWavefunction(nspins=mol.nspins)
+    data = _system(mol, 64)
+    params = wf.init_params(data, 0)
+    bd = vmc.BatchedData(data)
+    ws = {}
+    ws.update(vmc.potential_energy(params, bd, ws, None, wf=wf)[0])
+    ws.update(vmc.EuclideanKinetic(f_log_psi=wf).evaluate_batch_walkers(params, bd, ws, None)[0])
+    ws.update(vmc.TotalEnergy().evaluate_batch_walkers(params, bd, ws, None)[0])
+    m = wf.model(data, params)
+    ref = m.local_energy(data.electrons)
+    torch.testing.assert_close(ws["total_energy"], ref["e_local"])
+    red = vmc.mean_reduce({"total_energy": ws["total_energy"]})
+    assert set(red) == {"total_energy", "total_energy_var"}
+
+
+def test_autograd_function_and_custom_op(cuda_device):
+    mol = S.lithium()
+    wf = vmc.FermiNetWavefunction(nspins=mol.nspins, ndets=3, hidden_dims_single=[8, 8], hidden_dims_double=[4, 4])
+    data = _system(mol, 16)
+    params = wf.init_params(data, 0)
+    m = wf.model(data, params)
+    w = torch.linspace(-1, 1, 16, device="cuda")
+    flat = params.flat.clone().requires_grad_(True)
+    lp = torch_ops.ferminet_logpsi(flat, data.electrons, m)
+    (lp * w).sum().backward()
+    _, g, _ = m.grad(data.electrons, weights=w.double())
+    torch.testing.assert_close(flat.grad, g.float(), rtol=1e-5, atol=1e-6)
+    h = torch_ops.register(m)
+    flat2 = params.flat.clone().requires_grad_(True)
+    lp2 = torch.ops.qmc_gb300.ferminet_logpsi(flat2, data.electrons, h)
+    torch.testing.assert_close(lp2, lp.detach())
+    (lp2 * w).sum().backward()
+    torch.testing.assert_close(flat2.grad, flat.grad)
