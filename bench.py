@@ -217,6 +217,48 @@ def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
             "span_s": span}
 
 
+def run_request_only(args, wl):
+    """W warm-up and K timed requests (or only their E_L / MH part) of one
+    form, nothing else: the command line profiled by ncu."""
+    import torch
+
+    from jaqmc_gb300 import _native
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    mol = S.SYSTEMS[wl["system"]]()
+    cfg = P.FermiNetConfig(nspins=mol.nspins)
+    tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+    flat = torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms)), device=dev)
+    B, S_ = wl["walkers"], wl["mh_steps"]
+    x = torch.as_tensor(S.init_walkers(mol, B, seed=1), device=dev)
+    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision=args.precision, device=dev)
+    m.set_params(flat)
+    if args.burn_in:
+        m.mh_steps(x, args.burn_in, 0.15, 1000, 0)
+
+    def one(k):
+        if args.op in ("request", "mh"):
+            m.mh_steps(x, S_, 0.02, 2, k * S_)
+        if args.op in ("request", "el"):
+            _native.reduce_mean_var(m.local_energy(x)["e_local"])
+
+    for k in range(args.warmup):
+        one(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(args.steps):
+        one(args.warmup + k)
+    e1.record()
+    torch.cuda.synchronize()
+    assert m.check_error() == 0
+    print(json.dumps({"op": args.op, "precision": args.precision, "walkers": B, "system": wl["system"],
+                      "ms_per_step": e0.elapsed_time(e1) / args.steps}), flush=True)
+    return 0
+
+
 # ----------------------------------------------------------------- GPU side
 def run_ours(args, wl):
     import torch
@@ -418,6 +460,11 @@ def main():
     ap.add_argument("--oracle-walkers", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--walkers", type=int, default=None, help="override the workload's walker count")
+    ap.add_argument("--request-only", action="store_true",
+                    help="only W warm-up + K timed requests of --precision (for profiler runs)")
+    ap.add_argument("--op", default="request", choices=["request", "el", "mh"],
+                    help="with --request-only: the whole request, only E_L, or only the MH steps")
     ap.add_argument("--serve-only", action="store_true", help="print only the serving measurement")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrival rate (jobs/s)")
     ap.add_argument("--serve-jobs", type=int, default=48)
@@ -432,7 +479,11 @@ def main():
         return 0
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.walkers:
+        wl["walkers"] = args.walkers
+    if args.request_only:
+        return run_request_only(args, wl)
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -82,6 +82,8 @@ __device__ __forceinline__ void report(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
+// 10 warps share the SM's four 16K-register sub-partitions (three warps on
+// two of them), which caps a thread at 168 registers.
 template <class Epi>
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_tc_gemm(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
@@ -257,15 +259,22 @@ struct ContigTiles {
   }
 };
 
-__device__ __forceinline__ void half_sync(int half) {
-  // the 4 epilogue warps of one half (128 threads) on named barrier 1 + half
-  asm volatile("bar.sync %0, 128;" ::"r"(1 + half) : "memory");
+// Split value <-> one 32-bit word: bf16 hi in the low half, bf16 lo above.
+__device__ __forceinline__ float word_value(uint32_t w) {
+  return __uint_as_float(w << 16) + __uint_as_float(w & 0xffff0000u);
+}
+__device__ __forceinline__ uint32_t value_word(float y) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn(y);
+  const float hf = __bfloat162float(hi);
+  const __nv_bfloat162 p = __floats2bfloat162_rn(hf, y - hf);  // .x (low) = hi exactly
+  return *reinterpret_cast<const uint32_t*>(&p);
 }
 
-// One-electron layer epilogue.  Row blocks (one tangent group, or 16 rows of
-// a value-only tile) are staged through shared memory: the residual rows are
-// read with 16-byte vector loads, each thread updates its feature column in
-// place, and the block is written back with 16-byte vector stores.
+// One-electron layer epilogue.  Each warp owns 32 features of the tile and
+// stages its rows through a private shared-memory block of 32-bit words
+// (hi | lo << 16, one word per feature and row), so the residual is read and
+// the output written with 16-byte global accesses and no barrier wider than
+// the warp.  A thread holds one feature (its TMEM lane) and walks the rows.
 struct EpiTcLayer : ContigTiles {
   int n, ld;  // electrons per walker, activation row width (n_out)
   StSplit resid, out;
@@ -273,140 +282,161 @@ struct EpiTcLayer : ContigTiles {
   const float* Gb;
   const float* bias;
 
-  // rows [row0, row0 + nrows) x features [m0, m0 + 128) of `st` <-> staging tile
-  // all loads of a batch are issued before any shared-memory store
-  __device__ void load_block(const StSplit& st, size_t row0, int nrows, int m0, int lt, __nv_bfloat16* eb) const {
-    const int nv = nrows * 2 * 16;
-    for (int v0 = 0; v0 < nv; v0 += 128 * 12) {
-      uint4 r[12];
+  // rows [row0, row0 + R) x features [col0, col0 + 32) of `st` -> wb[R][32]
+  // (8 rows per pass: lane = 4 * row + 8-feature vector)
+  __device__ __forceinline__ void warp_load(const StSplit& st, size_t row0, int R, int col0, int nvec, int lane,
+                                            uint32_t* wb) const {
+    const int vq = lane & 3, rl = lane >> 2;
+    if (vq >= nvec) return;
+    for (int rb = 0; rb < R; rb += 16) {
+      uint4 h[2], l[2];
 #pragma unroll
-      for (int u = 0; u < 12; ++u) {
-        const int v = v0 + lt + 128 * u;
-        if (v < nv) {
-          const int pl = v / (nrows * 16), rr = (v / 16) % nrows, q = v % 16;
-          r[u] = __ldg(reinterpret_cast<const uint4*>(st.p + pl * st.plane + (row0 + rr) * (size_t)st.ld + m0 + 8 * q));
+      for (int p = 0; p < 2; ++p) {
+        const int r = rb + 8 * p + rl;
+        if (r < R) {
+          const __nv_bfloat16* src = st.p + (row0 + r) * (size_t)st.ld + col0 + 8 * vq;
+          h[p] = __ldg(reinterpret_cast<const uint4*>(src));
+          l[p] = __ldg(reinterpret_cast<const uint4*>(src + st.plane));
         }
       }
 #pragma unroll
-      for (int u = 0; u < 12; ++u) {
-        const int v = v0 + lt + 128 * u;
-        if (v < nv) {
-          const int pl = v / (nrows * 16), rr = (v / 16) % nrows, q = v % 16;
-          *reinterpret_cast<uint4*>(eb + ((size_t)pl * nrows + rr) * 128 + 8 * q) = r[u];
+      for (int p = 0; p < 2; ++p) {
+        const int r = rb + 8 * p + rl;
+        if (r < R) {
+          uint4 a, b;
+          a.x = __byte_perm(h[p].x, l[p].x, 0x5410);
+          a.y = __byte_perm(h[p].x, l[p].x, 0x7632);
+          a.z = __byte_perm(h[p].y, l[p].y, 0x5410);
+          a.w = __byte_perm(h[p].y, l[p].y, 0x7632);
+          b.x = __byte_perm(h[p].z, l[p].z, 0x5410);
+          b.y = __byte_perm(h[p].z, l[p].z, 0x7632);
+          b.z = __byte_perm(h[p].w, l[p].w, 0x5410);
+          b.w = __byte_perm(h[p].w, l[p].w, 0x7632);
+          uint4* d = reinterpret_cast<uint4*>(wb + r * 32 + 8 * vq);
+          d[0] = a;
+          d[1] = b;
         }
       }
     }
   }
-  __device__ void store_block(const StSplit& st, size_t row0, int nrows, int m0, int lt, int n_out,
-                              const __nv_bfloat16* eb) const {
-    const int nv = nrows * 2 * 16;
-    for (int v = lt; v < nv; v += 128) {
-      const int pl = v / (nrows * 16), rr = (v / 16) % nrows, q = v % 16;
-      if (m0 + 8 * q >= n_out) continue;
-      uint4* dst = reinterpret_cast<uint4*>(st.p + pl * st.plane + (row0 + rr) * (size_t)st.ld + m0 + 8 * q);
-      *dst = *reinterpret_cast<const uint4*>(eb + ((size_t)pl * nrows + rr) * 128 + 8 * q);
+  // wb[R][32] -> rows [row0, row0 + R) x features [col0, col0 + 32) of `st`
+  __device__ __forceinline__ void warp_store(const StSplit& st, size_t row0, int R, int col0, int nvec, int lane,
+                                             const uint32_t* wb) const {
+    const int vq = lane & 3, rl = lane >> 2;
+    if (vq >= nvec) return;
+    for (int r = rl; r < R; r += 8) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(wb + r * 32 + 8 * vq);
+      const uint4 a = s4[0], b = s4[1];
+      uint4 h, l;
+      h.x = __byte_perm(a.x, a.y, 0x5410);
+      l.x = __byte_perm(a.x, a.y, 0x7632);
+      h.y = __byte_perm(a.z, a.w, 0x5410);
+      l.y = __byte_perm(a.z, a.w, 0x7632);
+      h.z = __byte_perm(b.x, b.y, 0x5410);
+      l.z = __byte_perm(b.x, b.y, 0x7632);
+      h.w = __byte_perm(b.z, b.w, 0x5410);
+      l.w = __byte_perm(b.z, b.w, 0x7632);
+      __nv_bfloat16* dst = st.p + (row0 + r) * (size_t)st.ld + col0 + 8 * vq;
+      *reinterpret_cast<uint4*>(dst) = h;
+      *reinterpret_cast<uint4*>(dst + st.plane) = l;
     }
-  }
-  __device__ __forceinline__ float eb_get(const __nv_bfloat16* eb, int nrows, int rr, int fl) const {
-    return __bfloat162float(eb[(size_t)rr * 128 + fl]) + __bfloat162float(eb[((size_t)nrows + rr) * 128 + fl]);
-  }
-  __device__ __forceinline__ void eb_put(__nv_bfloat16* eb, int nrows, int rr, int fl, float y) const {
-    const __nv_bfloat16 hi = __float2bfloat16_rn(y);
-    eb[(size_t)rr * 128 + fl] = hi;
-    eb[((size_t)nrows + rr) * 128 + fl] = __float2bfloat16_rn(y - __bfloat162float(hi));
   }
 
   __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t* ebuf) const {
-    __nv_bfloat16* eb = reinterpret_cast<__nv_bfloat16*>(ebuf);
-    const bool fok = f < g.n_out;
     const int N = g.n_out;
-    const int fc = fok ? f : 0;  // clamped column for speculative loads
-    const int fl = f & 127, m0 = f - fl;
-    const int lt = fl;           // thread index within this half (= local feature)
+    const int lane = f & 31, col0 = f - lane;
+    const int q = (f & 127) >> 5;
+    const int nvec = max(0, min(4, (N - col0) / 8));
+    const int fc = f < N ? f : 0;  // clamped feature for loads of parameters
     const float b = bias[fc];
     if (g.T == 1) {
-      for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
-        const int nrows = min(16, ti.ng - c0);  // uniform across the half
-        if (nrows <= 0) break;
+      uint32_t* wb = reinterpret_cast<uint32_t*>(ebuf) + q * 32 * 16;
+      for (int c0 = 16 * half; c0 < ti.ng; c0 += 32) {
+        const int nrows = min(16, ti.ng - c0);
         const size_t row0 = (size_t)(ti.g0 + c0);
-        if (has_resid) load_block(resid, row0, nrows, m0, lt, eb);
-        float v[16], gbv[16];
+        if (has_resid) warp_load(resid, row0, nrows, col0, nvec, lane, wb);
+        uint32_t r[16];
+        ptx::tmem_ld16_nw(taddr + c0, r);
+        float gbv[16];
+        int w = (int)(row0 / n), e = (int)(row0 % n);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int gi = ti.g0 + c0 + min(j, nrows - 1);
-          gbv[j] = __ldg(Gb + (size_t)(gi / n) * N + fc);
+          gbv[j] = __ldg(Gb + (size_t)w * N + fc);
+          if (++e == n) {
+            e = 0;
+            ++w;
+          }
         }
-        ptx::tmem_ld16(taddr + c0, v);
-        half_sync(half);
+        ptx::tmem_wait16(r);
+        __syncwarp();
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           if (j < nrows) {
-            float h = tanhf(v[j] + gbv[j] + b);
-            if (has_resid) h = (h + eb_get(eb, nrows, j, fl)) * kRsqrt2;
-            eb_put(eb, nrows, j, fl, h);
+            float y = tanhf(__uint_as_float(r[j]) + gbv[j] + b);
+            if (has_resid) y = (y + word_value(wb[j * 32 + lane])) * kRsqrt2;
+            wb[j * 32 + lane] = value_word(y);
           }
         }
-        half_sync(half);
-        store_block(out, row0, nrows, m0, lt, N, eb);
-        half_sync(half);
+        __syncwarp();
+        warp_store(out, row0, nrows, col0, nvec, lane, wb);
+        __syncwarp();
       }
       return;
     }
-    const int Tp = g.Tp;
+    const int Tp = g.Tp, T = g.T;
+    uint32_t* wb = reinterpret_cast<uint32_t*>(ebuf) + q * 32 * Tp;
     for (int lg = half; lg < ti.ng; lg += 2) {
       const int gi = ti.g0 + lg;
-      const int w = gi / n;
       const size_t r0 = (size_t)gi * Tp;
-      const int c0 = lg * Tp;
-      const float* gb = Gb + (size_t)w * Tp * N + fc;
-      if (has_resid) load_block(resid, r0, Tp, m0, lt, eb);
-      half_sync(half);
+      const uint32_t tcol = taddr + (uint32_t)(lg * Tp);
+      const float* gb = Gb + (size_t)(gi / n) * Tp * N + fc;
+      if (has_resid) warp_load(resid, r0, Tp, col0, nvec, lane, wb);
       float h = 0.f, d1 = 0.f, zL = 0.f, S = 0.f;
-      float nxt[8];  // broadcast terms of the next chunk, loaded one chunk ahead
+      for (int t0 = 0; t0 < Tp; t0 += 16) {
+        const int cs = min(16, Tp - t0);  // a multiple of 4, uniform
+        uint32_t r[16];
+        if (cs == 16) {
+          ptx::tmem_ld16_nw(tcol + t0, r);
+        } else {
 #pragma unroll
-      for (int e = 0; e < 8; ++e) nxt[e] = e < g.T ? __ldg(gb + (size_t)e * N) : 0.f;
-      for (int t0 = 0; t0 < Tp; t0 += 8) {
-        const bool two = t0 + 4 < Tp;  // uniform
-        float gbv[8], v[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          gbv[e] = nxt[e];
-          const int t = t0 + 8 + e;
-          nxt[e] = t < g.T ? __ldg(gb + (size_t)t * N) : 0.f;
+          for (int k = 0; k < 4; ++k)
+            if (4 * k < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * k, r + 4 * k);
         }
-        ptx::tmem_ld4(taddr + c0 + t0, v);
-        if (two) ptx::tmem_ld4(taddr + c0 + t0 + 4, v + 4);
+        float gbv[16];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
+        for (int e = 0; e < 16; ++e) gbv[e] = t0 + e < T ? __ldg(gb + (size_t)(t0 + e) * N) : 0.f;
+        ptx::tmem_wait16(r);
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
           const int t = t0 + e;
-          if (e >= 4 && !two) break;
-          if (t == 1) {
-            zL = v[e] + gbv[e];
-            continue;
-          }
+          if (e >= cs) break;
+          const float z = __uint_as_float(r[e]) + gbv[e];
           float y;
           if (t == 0) {
-            h = tanhf(v[e] + gbv[e] + b);
+            h = tanhf(z + b);
             d1 = 1.f - h * h;
             y = h;
-          } else if (t < g.T) {
-            const float z = v[e] + gbv[e];
+          } else if (t == 1) {
+            zL = z;
+            continue;
+          } else if (t < T) {
             S = fmaf(z, z, S);
             y = d1 * z;
           } else {
-            eb_put(eb, Tp, t, fl, 0.f);
+            wb[t * 32 + lane] = 0u;
             continue;
           }
-          if (has_resid) y = (y + eb_get(eb, Tp, t, fl)) * kRsqrt2;
-          eb_put(eb, Tp, t, fl, y);
+          if (has_resid) y = (y + word_value(wb[t * 32 + lane])) * kRsqrt2;
+          wb[t * 32 + lane] = value_word(y);
         }
       }
       float y = d1 * zL - 2.f * h * d1 * S;
-      if (has_resid) y = (y + eb_get(eb, Tp, 1, fl)) * kRsqrt2;
-      eb_put(eb, Tp, 1, fl, y);
-      half_sync(half);
-      store_block(out, r0, Tp, m0, lt, N, eb);
-      half_sync(half);
+      if (has_resid) y = (y + word_value(wb[32 + lane])) * kRsqrt2;
+      wb[32 + lane] = value_word(y);
+      __syncwarp();
+      warp_store(out, r0, Tp, col0, nvec, lane, wb);
+      __syncwarp();
     }
   }
 };
