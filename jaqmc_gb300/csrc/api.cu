@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <string>
+#include <type_traits>
 
 #include "common.cuh"
 #include "gemm_simt.cuh"
@@ -241,11 +242,58 @@ static bool pair_fused(const Dims& d, int T) {
   return true;
 }
 
+// Value-only forwards run the whole two-electron stream in one kernel
+// (launch_pair_stream_value) when its layers are 32 wide, a walker's pair
+// activations fit in shared memory and the per-layer means fit the second
+// pair buffer, which that path leaves unused.
+static bool pair_stream(const Dims& d, const Plan& p) {
+  if (p.T != 1 || d.L < 2 || d.L - 1 > kPairStreamMax) return false;
+  for (int l = 0; l < d.L; ++l) {
+    if (d.upd2[l] != (l < d.L - 1)) return false;
+    if (l < d.L - 1 && (d.d2[l] != 32 || (d.d2_in[l] != 4 && d.d2_in[l] != 32))) return false;
+  }
+  if (pair_stream_smem(d.n, d.L - 1) > 200 * 1024) return false;
+  return (size_t)(d.L - 1) * p.g2_plane * 4 <= p.g1 - p.h2[1];
+}
+
+// The means after pair layer l - 1 (input of one-electron layer l >= 1) on
+// the fused two-electron path: f32 [B*n][g2_p[l]], or two bf16 planes.
+static size_t stream_g2(const Plan& p, int l) { return p.h2[1] + (size_t)(l - 1) * p.g2_plane * 4; }
+
+template <class Out>
+static qmc_status run_pair_stream(qmc_model* m, const Plan& p, void* ws, cudaStream_t s) {
+  const Dims& d = m->d;
+  const float* ar = m->arena;
+  PairStreamArgs a{};
+  PairStreamOut<Out> o{};
+  a.n = d.n;
+  a.n_up = d.n_up;
+  a.C = d.C;
+  a.nl = d.L - 1;
+  a.H0 = reinterpret_cast<const float*>(static_cast<char*>(ws) + p.h2[0]);
+  for (int l = 0; l < a.nl; ++l) {
+    a.din[l] = d.d2_in[l];
+    a.W[l] = ar + m->a.w2[l];
+    a.b[l] = ar + m->a.b2[l];
+    a.g2p[l] = d.g2_p[l + 1];
+    char* base = static_cast<char*>(ws) + stream_g2(p, l + 1);
+    if constexpr (std::is_same<Out, StSplit>::value) {
+      o.G2[l] = StSplit{reinterpret_cast<__nv_bfloat16*>(base), d.g2_p[l + 1], p.g2_plane};
+    } else {
+      o.G2[l] = StF32{reinterpret_cast<float*>(base), d.g2_p[l + 1]};
+    }
+  }
+  QMC_PROF(QMC_KC_PAIR, launch_pair_stream_value(s, p.B, a, o));
+  return QMC_OK;
+}
+
 // Plain FP32 form.  One-electron layer l: spin means, broadcast GEMM, main
 // GEMM with the tangent epilogue; then the two-electron update.
 static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
   const Dims& d = m->d;
   const bool fused = pair_fused(d, p.T);
+  const bool stream = pair_stream(d, p);
+  if (stream) QMC_TRY(run_pair_stream<StF32>(m, p, ws, s));
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
   const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
@@ -258,20 +306,20 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
     float* out = at<float>(ws, p.h1[l == 0 ? 0 : cur ^ 1]);
     float* G1 = at<float>(ws, p.g1);
     float* Gb = at<float>(ws, p.gb);
-    float* G2 = at<float>(ws, p.g2);
+    float* G2 = at<float>(ws, stream && l > 0 ? stream_g2(p, l) : p.g2);
     const float* H2 = at<float>(ws, p.h2[h2cur]);
     QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StF32{const_cast<float*>(in), dinp},
                                           d.g1_p[l], StF32{G1, d.g1_p[l]}));
     QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
                                                 ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
-    if (!fused)
+    if (!fused && !stream)
       QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
                                             StF32{G2, d.g2_p[l]}));
     EpiLayer<StF32> epi{Gb, ar + a.b1[l], StF32{nullptr, dout}, StF32{out, dout}, T};
     if (l > 0 && din == dout) epi.resid = StF32{const_cast<float*>(in), dout};
     QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
                                                    ar + a.w_main[l], dout, dout, epi));
-    if (d.upd2[l]) {
+    if (d.upd2[l] && !stream) {
       float* h2o = at<float>(ws, p.h2[h2cur ^ 1]);
       if (fused)
         QMC_PROF(QMC_KC_PAIR, launch_pair_layer_mean(s, B, n, d.n_up, d.C, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
@@ -292,6 +340,8 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
 static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cudaStream_t s, int* out_buf) {
   const Dims& d = m->d;
   const bool fused = pair_fused(d, p.T);
+  const bool stream = pair_stream(d, p);
+  if (stream) QMC_TRY(run_pair_stream<StSplit>(m, p, ws, s));
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
   const int B = p.B, Tp = p.Tp, T = p.T, n = d.n;
@@ -321,13 +371,13 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
     } else {
       bf* in = at<bf>(ws, p.h1[cur]);
       bf* G1 = at<bf>(ws, p.g1);
-      bf* G2 = at<bf>(ws, p.g2);
+      bf* G2 = at<bf>(ws, stream ? stream_g2(p, l) : p.g2);
       const int kmain = dinp + d.g2_p[l];
       QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StSplit{in, dinp, p.h1_plane},
                                             d.g1_p[l], StSplit{G1, d.g1_p[l], p.g1_plane}));
       TcStoreArgs sa{B * Tp, G1, d.g1_p[l], p.g1_plane, m->arena_bf16 + a.t_g1[l], dout, Gb, m->dev_err};
       QMC_PROF_TRY(QMC_KC_BROADCAST, tc_store_gemm(s, sa));
-      if (!fused)
+      if (!fused && !stream)
         QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
                                               StSplit{G2, d.g2_p[l], p.g2_plane}));
       TcLayerArgs la{};
@@ -352,7 +402,7 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
       (void)kmain;
       QMC_PROF_TRY(QMC_KC_STREAM_LAYER, tc_stream_layer(s, la));
     }
-    if (d.upd2[l]) {
+    if (d.upd2[l] && !stream) {
       float* h2o = at<float>(ws, p.h2[h2cur ^ 1]);
       if (fused)  // next layer (>= 1) reads its G2 as split bf16
         QMC_PROF(QMC_KC_PAIR, launch_pair_layer_mean(s, B, n, d.n_up, d.C, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
@@ -398,6 +448,17 @@ static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cu
     oa.rae = at<float>(ws, p.rae);
     oa.aevec = at<float>(ws, p.aevec);
     oa.A = at<float>(ws, p.amat);
+    oa.env = nullptr;
+    // value-only passes: envelopes by a full-occupancy kernel into the (now
+    // unused) two-electron buffer, when it is large enough
+    const size_t env_bytes = (size_t)p.B * d.K * d.n * d.n * sizeof(float);
+    if (p.T == 1 && p.h2[1] - p.h2[0] >= env_bytes) {
+      float* env = at<float>(ws, p.h2[0]);
+      QMC_PROF(QMC_KC_ORBITAL, launch_envelope_value(s, p.B, d.n, d.n_up, d.split, d.K, d.A, d.env_abs,
+                                                     oa.pi[0], oa.sigma[0], oa.pi[1], oa.sigma[1],
+                                                     at<float>(ws, p.rae), env));
+      oa.env = env;
+    }
     oa.err = m->dev_err;
     QMC_PROF_TRY(QMC_KC_ORBITAL, tc_orbitals(s, oa));
     return QMC_OK;

@@ -133,6 +133,45 @@ cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, 
   return cudaGetLastError();
 }
 
+// Envelope factor of every value-only orbital matrix element (walker w,
+// determinant k, electron i, orbital j): sum_I pi[j,I,k] exp(-s r_iI) with
+// s = |sigma[j,I,k]| (abs_isotropic) or sigma (isotropic), per spin channel
+// of electron i (src/jaqmc/wavefunction/output/envelope.py:98-140).  Same
+// terms, same order as the tangent epilogues, so the product is unchanged.
+__global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A, int env_abs,
+                                 const float* __restrict__ pi0, const float* __restrict__ sg0,
+                                 const float* __restrict__ pi1, const float* __restrict__ sg1,
+                                 const float* __restrict__ rae, float* __restrict__ env) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * K * n * n) return;
+  const int j = (int)(e % n);
+  size_t r = e / n;
+  const int i = (int)(r % n);
+  r /= n;
+  const int k = (int)(r % K);
+  const int w = (int)(r / K);
+  const bool s1 = split && i >= n_up;
+  const float* pi = s1 ? pi1 : pi0;
+  const float* sg = s1 ? sg1 : sg0;
+  const float* ra = rae + ((size_t)w * n + i) * A;
+  float acc = 0.f;
+  for (int I = 0; I < A; ++I) {
+    const size_t q = ((size_t)j * A + I) * K + k;
+    const float sv = __ldg(sg + q);
+    acc += __ldg(pi + q) * expf(-(env_abs ? fabsf(sv) : sv) * __ldg(ra + I));
+  }
+  env[e] = acc;
+}
+
+cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
+                                  const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                  const float* rae, float* env) {
+  const size_t total = (size_t)B * K * n * n;
+  k_envelope_value<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, split, K, A, env_abs, pi0, sg0,
+                                                                    pi1, sg1, rae, env);
+  return cudaGetLastError();
+}
+
 // =====================================================================
 // two-electron layer (src/jaqmc/wavefunction/backbone/ferminet.py:55-63)
 // rows p: 0 value, 1 Laplacian wrt the pair difference, 2..4 its gradient.
@@ -296,6 +335,122 @@ __global__ void __launch_bounds__(256) k_pair_layer_mean(int n, int n_up, int C,
   }
 }
 
+// Whole value-only two-electron stream of one walker per block: every pair
+// layer h2 <- tanh(W2 h2 + b2) (+ residual) with the activations kept in
+// shared memory, and after each layer the spin means over the first electron
+// index that the next one-electron layer reads (G2 of layers 1..nl).  Pair
+// activations never leave the SM.  Widths: input 4 or 32, output 32.
+template <class Out>
+__global__ void __launch_bounds__(256) k_pair_stream_value(PairStreamArgs a, PairStreamOut<Out> o) {
+  extern __shared__ float shs[];
+  constexpr int DO = 32, RS = 36;  // row stride 36 floats: conflict-free 16-byte accesses
+  float* Ws = shs;                         // [nl][32][32]
+  float* bs = Ws + a.nl * DO * DO;         // [nl][32]
+  float* Os = bs + a.nl * DO;              // [n*n][RS]
+  for (int l = 0; l < a.nl; ++l) {
+    for (int e = threadIdx.x; e < a.din[l] * DO; e += blockDim.x) Ws[l * DO * DO + e] = a.W[l][e];
+    for (int e = threadIdx.x; e < DO; e += blockDim.x) bs[l * DO + e] = a.b[l][e];
+  }
+  __syncthreads();
+  const int n = a.n, np = n * n, w = blockIdx.x;
+  for (int l = 0; l < a.nl; ++l) {
+    const float* Wl = Ws + l * DO * DO;
+    const float* bl = bs + l * DO;
+    const int din = a.din[l];
+    for (int pr = threadIdx.x; pr < np; pr += blockDim.x) {
+      float x[DO];
+      float* row = Os + pr * RS;
+      if (l == 0) {
+        const float4* src = reinterpret_cast<const float4*>(a.H0 + ((size_t)w * np + pr) * din);
+#pragma unroll
+        for (int q = 0; q < DO / 4; ++q) {
+          const float4 v = q < din / 4 ? __ldg(src + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+          x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < DO / 4; ++q) {
+          const float4 v = *reinterpret_cast<const float4*>(row + 4 * q);
+          x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int f4 = 0; f4 < DO / 4; ++f4) {
+        float z[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) z[e] = bl[4 * f4 + e];
+        if (din == 4) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float4 wv = *reinterpret_cast<const float4*>(&Wl[k * DO + 4 * f4]);
+            z[0] = fmaf(x[k], wv.x, z[0]);
+            z[1] = fmaf(x[k], wv.y, z[1]);
+            z[2] = fmaf(x[k], wv.z, z[2]);
+            z[3] = fmaf(x[k], wv.w, z[3]);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < DO; ++k) {
+            const float4 wv = *reinterpret_cast<const float4*>(&Wl[k * DO + 4 * f4]);
+            z[0] = fmaf(x[k], wv.x, z[0]);
+            z[1] = fmaf(x[k], wv.y, z[1]);
+            z[2] = fmaf(x[k], wv.z, z[2]);
+            z[3] = fmaf(x[k], wv.w, z[3]);
+          }
+        }
+        float4 v;
+        v.x = tanhf(z[0]); v.y = tanhf(z[1]); v.z = tanhf(z[2]); v.w = tanhf(z[3]);
+        if (din == DO) {
+          v.x = (v.x + x[4 * f4]) * kRsqrt2;
+          v.y = (v.y + x[4 * f4 + 1]) * kRsqrt2;
+          v.z = (v.z + x[4 * f4 + 2]) * kRsqrt2;
+          v.w = (v.w + x[4 * f4 + 3]) * kRsqrt2;
+        }
+        *reinterpret_cast<float4*>(row + 4 * f4) = v;
+      }
+    }
+    __syncthreads();
+    // <h2>_s[i] = mean over a in channel s of h2[a, i]  (first index averaged)
+    const int g2p = a.g2p[l];
+    for (int e = threadIdx.x; e < n * g2p; e += blockDim.x) {
+      const int i = e / g2p, col = e % g2p;
+      float v = 0.f;
+      if (col < a.C * DO) {
+        const int sc = col / DO, f = col % DO;
+        const int a0 = a.C == 1 ? 0 : (sc == 0 ? 0 : a.n_up), a1 = a.C == 1 ? n : (sc == 0 ? a.n_up : n);
+        float acc = 0.f;
+        for (int aa = a0; aa < a1; ++aa) acc += Os[(aa * n + i) * RS + f];
+        v = acc / (float)(a1 - a0);
+      }
+      o.G2[l].put((size_t)w * n + i, col, v);
+    }
+    __syncthreads();
+  }
+}
+
+size_t pair_stream_smem(int n, int nl) { return sizeof(float) * ((size_t)nl * (32 * 32 + 32) + (size_t)n * n * 36); }
+
+template <class Out>
+cudaError_t launch_pair_stream_value(cudaStream_t s, int B, const PairStreamArgs& a, const PairStreamOut<Out>& o) {
+  const size_t sm = pair_stream_smem(a.n, a.nl);
+  if (sm > 200 * 1024 || a.nl < 1 || a.nl > kPairStreamMax) return cudaErrorNotSupported;
+  static int attr_dev = -1;
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (attr_dev != dev) {
+    e = cudaFuncSetAttribute(k_pair_stream_value<Out>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_dev = dev;
+  }
+  k_pair_stream_value<Out><<<B, 256, sm, s>>>(a, o);
+  return cudaGetLastError();
+}
+template cudaError_t launch_pair_stream_value<StF32>(cudaStream_t, int, const PairStreamArgs&,
+                                                     const PairStreamOut<StF32>&);
+template cudaError_t launch_pair_stream_value<StSplit>(cudaStream_t, int, const PairStreamArgs&,
+                                                       const PairStreamOut<StSplit>&);
+
 template <class Out>
 cudaError_t launch_pair_layer_mean(cudaStream_t s, int B, int n, int n_up, int C, int d_in, int d_out,
                                    const float* Hin, const float* W, const float* b, float* Hout, int g2p,
@@ -380,9 +535,90 @@ __global__ void k_mean_h1(int B, int n, int n_up, int C, int Tp, int d, In X, in
   G1.put(wt, col, v);
 }
 
+// 8 consecutive features of one row (16-byte aligned) <-> registers.
+__device__ __forceinline__ void load8(const StF32& X, size_t r, int c, float* v) {
+  const float4* p = reinterpret_cast<const float4*>(X.p + r * X.ld + c);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void load8(const StSplit& X, size_t r, int c, float* v) {
+  const __nv_bfloat16* p = X.p + r * X.ld + c;
+  const uint4 h = __ldg(reinterpret_cast<const uint4*>(p));
+  const uint4 l = __ldg(reinterpret_cast<const uint4*>(p + X.plane));
+  const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[2 * k] = __uint_as_float(hw[k] << 16) + __uint_as_float(lw[k] << 16);
+    v[2 * k + 1] = __uint_as_float(hw[k] & 0xffff0000u) + __uint_as_float(lw[k] & 0xffff0000u);
+  }
+}
+__device__ __forceinline__ void store8(const StF32& Y, size_t r, int c, const float* v) {
+  float4* p = reinterpret_cast<float4*>(Y.p + r * Y.ld + c);
+  p[0] = make_float4(v[0], v[1], v[2], v[3]);
+  p[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+__device__ __forceinline__ void store8(const StSplit& Y, size_t r, int c, const float* v) {
+  uint32_t hw[4], lw[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(v[2 * k] - __low2float(hi), v[2 * k + 1] - __high2float(hi));
+    hw[k] = *reinterpret_cast<const uint32_t*>(&hi);
+    lw[k] = *reinterpret_cast<const uint32_t*>(&lo);
+  }
+  __nv_bfloat16* p = Y.p + r * Y.ld + c;
+  *reinterpret_cast<uint4*>(p) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+  *reinterpret_cast<uint4*>(p + Y.plane) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+}
+static bool vec8_ok(const StF32& X) { return ((uintptr_t)X.p & 15) == 0 && X.ld % 4 == 0; }
+static bool vec8_ok(const StSplit& X) {
+  return ((uintptr_t)X.p & 15) == 0 && X.ld % 8 == 0 && X.plane % 8 == 0;
+}
+
+// Spin means of 8 features per thread: all electron rows of a batch are
+// loaded (16-byte vectors) before they are summed.
+template <class In, class Out>
+__global__ void k_mean_h1_vec(int B, int n, int n_up, int C, int Tp, int d, In X, int g1p, Out G1) {
+  const int nv = g1p / 8;
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * Tp * nv) return;
+  const int col = 8 * (int)(e % nv);
+  const size_t wt = e / nv;
+  const int t = (int)(wt % Tp);
+  const int w = (int)(wt / Tp);
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (col < C * d) {
+    const int s = col / d, f = col % d;
+    int a0, a1;
+    channel_range(s, C, n, n_up, &a0, &a1);
+    for (int i0 = a0; i0 < a1; i0 += 4) {
+      float v[4][8];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (i0 + k < a1) load8(X, ((size_t)w * n + i0 + k) * Tp + t, f, v[k]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (i0 + k < a1) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[j] += v[k][j];
+        }
+    }
+    const float inv = 1.0f / (float)(a1 - a0);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] *= inv;
+  }
+  store8(G1, wt, col, acc);
+}
+
 template <class In, class Out>
 cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, In X, int g1p,
                            Out G1) {
+  if (d % 8 == 0 && g1p % 8 == 0 && vec8_ok(X) && vec8_ok(G1)) {
+    const size_t total = (size_t)B * Tp * (g1p / 8);
+    k_mean_h1_vec<In, Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, d, X, g1p, G1);
+    return cudaGetLastError();
+  }
   size_t total = (size_t)B * Tp * g1p;
   k_mean_h1<In, Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, d, X, g1p, G1);
   return cudaGetLastError();

@@ -51,6 +51,29 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
 // Abar[w][k] = w_k A_k^{-T}; also writes log|psi| (may be null).
 cudaError_t launch_logdet_bwd(cudaStream_t s, int B, int n, int K, const float* A, float* Abar, float* logpsi);
 
+// Value-only two-electron stream fused over all its layers (see kernels.cu).
+constexpr int kPairStreamMax = 8;
+struct PairStreamArgs {
+  int n, n_up, C, nl;
+  int din[kPairStreamMax];                  // 4 or 32; outputs are 32 wide
+  const float* W[kPairStreamMax];           // [din][32]
+  const float* b[kPairStreamMax];           // [32]
+  const float* H0;                          // [B][n][n][din[0]] pair features
+  int g2p[kPairStreamMax];                  // padded width of the means after layer l
+};
+template <class Out>
+struct PairStreamOut {
+  Out G2[kPairStreamMax];                   // means after pair layer l (input of layer l+1)
+};
+size_t pair_stream_smem(int n, int nl);
+template <class Out>
+cudaError_t launch_pair_stream_value(cudaStream_t s, int B, const PairStreamArgs& a, const PairStreamOut<Out>& o);
+
+// Envelopes [w][k][i][j] of the value-only orbital matrices.
+cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
+                                  const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                  const float* rae, float* env);
+
 // MH proposal x' = x + stddev * N(0,1) for update `step` of a call.
 // The update index is ctr (+ *ctr_dev when ctr_dev is not null).
 cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,

@@ -465,6 +465,7 @@ struct EpiTcOrbital {
   const float* rae;
   const float* aevec;
   float* A;
+  const float* env;  // value-only passes: precomputed envelopes laid out like A, or null
   int n_rows;  // B * n (value-only passes)
   __device__ TileInfo tile(int tx, const TcArgs& g) const {
     TileInfo t{};
@@ -549,16 +550,26 @@ struct EpiTcOrbital {
       for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
         float v[16];
         ptx::tmem_ld16(taddr + c0, v);
-        if (!fok) continue;
+        if (!fok || c0 >= ti.ng) continue;
+        const int gi0 = ti.g0 + c0;
+        int w = gi0 / n, i = gi0 - w * n;
 #pragma unroll
         for (int jj = 0; jj < 16; ++jj) {
-          int lg = c0 + jj;
-          if (lg < ti.ng) {
-            int gi = ti.g0 + lg, w = gi / n, i = gi % n;
-            if (split && (i < n_up ? 0 : 1) != ti.a_sel) continue;
-            float e[5];
-            envelope(ti.a_sel, w, i, k, j, 1, e, ep);
-            A[((size_t)w * K + k) * ts + (size_t)i * n + j] = v[jj] * e[0];
+          if (c0 + jj < ti.ng && (!split || (i < n_up ? 0 : 1) == ti.a_sel)) {
+            const size_t idx = ((size_t)w * K + k) * ts + (size_t)i * n + j;
+            float ev;
+            if (env) {
+              ev = __ldg(env + idx);
+            } else {
+              float e[5];
+              envelope(ti.a_sel, w, i, k, j, 1, e, ep);
+              ev = e[0];
+            }
+            A[idx] = v[jj] * ev;
+          }
+          if (++i == n) {
+            i = 0;
+            ++w;
           }
         }
       }
@@ -817,6 +828,7 @@ qmc_status tc_orbitals(cudaStream_t s, const TcOrbitalArgs& a) {
   e.rae = a.rae;
   e.aevec = a.aevec;
   e.A = a.A;
+  e.env = a.T == 1 ? a.env : nullptr;
   return launch(s, mA0, mA1, mB, mB, g, n_tiles, e);
 }
 
