@@ -387,24 +387,18 @@ def run_ours(args, wl):
     value = world * B * S_ / (ms_main / 1e3)
     value_e2e = world * B * S_ / (e2e_ms / 1e3)
     pk, pk_kind = peaks()
-    # roofline of the dominant kernel class
-    dom = max(prof, key=lambda k: prof[k][1])
-    rl = None
-    if dom == "stream_layer":
-        T_fl = 3 * mol.n_electrons + 2
-        flops_req = (S_ + 1) * stream_layer_flops(cfg, mol.n_atoms, B, 1) + stream_layer_flops(
-            cfg, mol.n_atoms, B, T_fl)
-        launches_dom, ms_dom = prof[dom]
-        achieved = flops_req * args.steps / (ms_dom / 1e3) / 1e12
-        if prec_main == "mixed":
-            peak, unit, bound = pk["bf16_tflops_sustained"], "TFLOP/s", "tensor"
-            pname = f"bf16 dense sustained ({pk_kind})"
-        else:
-            peak, unit, bound = FP32_SIMT_PEAK, "TFLOP/s", "fp32-simt"
-            pname = "FP32 SIMT nominal (152 SM x 128 FMA x 2 x 2.07 GHz)"
-        rl = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "peak_source": pname,
-              "unit": unit, "frac": achieved / peak, "traffic": TRAFFIC.get((wl["system"], prec_main)),
-              "launches_per_step": launches_dom / args.steps, "ms_per_step": ms_dom / args.steps}
+    # roofline of the dominant kernel: the one-electron layer kernel (layers
+    # >= 1) in its forward-Laplacian launches, timed live on E_L-only passes
+    _native.profile_enable(True)
+    _native.profile_read()
+    barrier()
+    for _ in range(args.steps):
+        models[prec_main].local_energy(xs[prec_main])
+    barrier()
+    prof_el = _native.profile_read()
+    _native.profile_enable(False)
+    Tp_fl = models[prec_main].tangent_rows(_native.OP_LOCAL_ENERGY)
+    rl, rl_t = fl_layer_roofline(cfg, mol, B, Tp_fl, prec_main, prof_el, pk, pk_kind)
     serve = None
     if not args.no_serve:
         serve = run_serving(dev, args.serve_rate, args.serve_jobs, args.serve_requests, slots=args.serve_slots)
@@ -432,6 +426,7 @@ def run_ours(args, wl):
             "gpu_launches": launches,
             "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items()},
             "roofline": rl,
+            "roofline_tensor": rl_t,
             "serving": serve,
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -443,9 +438,47 @@ def run_ours(args, wl):
 
 
 FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12
-# dram__bytes_read.sum + dram__bytes_write.sum per request of the dominant
-# kernel class from the committed ncu summaries (None until captured)
-TRAFFIC: dict = {}
+# dram__bytes_read.sum + dram__bytes_write.sum of one forward-Laplacian launch
+# of the one-electron layer kernel, from the committed ncu capture at 512
+# walkers, scaled to the workload's walkers (traffic grows with the rows)
+TRAFFIC_PER_WALKER: dict = {}
+
+
+def fl_layer_bytes_flops(cfg, mol, B, Tp):
+    """Algorithmic HBM bytes and FLOPs of one launch of a one-electron layer
+    l >= 1 with Tp tangent rows per electron: activations in (k1), spin means
+    of the pair stream (k2) and output (n_out) at 4 bytes per element (FP32,
+    or hi+lo bf16), plus the per-walker broadcast term; FLOPs 2 rows k n_out."""
+    from jaqmc_gb300 import params as P
+    dims = P.FermiNetConfig.layer_dims(cfg, mol.n_atoms)
+    d1_in, d2_in, d_out, _, _ = dims[1]
+    k1, k2 = d1_in, cfg.channels * d2_in
+    rows = B * mol.n_electrons * Tp
+    nbytes = rows * (k1 + k2 + d_out) * 4 + B * Tp * d_out * 4
+    flops = 2 * rows * (k1 + k2) * d_out
+    return nbytes, flops
+
+
+def fl_layer_roofline(cfg, mol, B, Tp, prec, prof_el, pk, pk_kind):
+    launches, ms = prof_el["stream_layer"]
+    if not launches:
+        return None, None
+    nbytes, flops = fl_layer_bytes_flops(cfg, mol, B, Tp)
+    t = ms / launches / 1e3
+    gbs = nbytes / t / 1e9
+    kern = ("k_tc_gemm<EpiTcLayer>" if prec == "mixed" else "k_gemm_simt<EpiLayer<StF32>>")
+    tpw = TRAFFIC_PER_WALKER.get((mol.name, prec))
+    rl = {"kernel": f"{kern}: forward-Laplacian launch of a 256-wide layer, {B} walkers",
+          "bound": "hbm", "achieved": gbs, "peak": pk["hbm_gbs"], "peak_source": f"hbm_gbs ({pk_kind})",
+          "unit": "GB/s", "frac": gbs / pk["hbm_gbs"], "traffic": tpw * B if tpw else None,
+          "algorithmic_bytes": nbytes, "ms_per_launch": t * 1e3, "launches": launches}
+    if prec == "mixed":
+        peak, src = pk["bf16_tflops_sustained"], f"bf16 dense sustained ({pk_kind})"
+    else:
+        peak, src = FP32_SIMT_PEAK, "FP32 SIMT nominal (152 SM x 128 FMA x 2 x 2.07 GHz)"
+    rl_t = {"bound": "tensor" if prec == "mixed" else "fp32-simt", "achieved": flops / t / 1e12, "peak": peak,
+            "peak_source": src, "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak, "algorithmic_flops": flops}
+    return rl, rl_t
 
 
 def main():

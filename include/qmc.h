@@ -128,6 +128,13 @@ qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, flo
                             float* ke, float* pe, float* logpsi, uint8_t* flags,
                             void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+/* Rows per electron that `op` propagates: 1 for QMC_OP_FORWARD / QMC_OP_MH,
+ * the 3n+2 forward-Laplacian tangents (padded to the tensor-core tile in the
+ * mixed form) for QMC_OP_LOCAL_ENERGY; -1 for an invalid model or op.  No
+ * counterpart in the reference (its tangents live inside the jaxpr
+ * interpreter, src/jaqmc/laplacian/interpreter.py:392-438). */
+int qmc_tangent_rows(const qmc_model* m, int op);
+
 /* `steps` all-electron Gaussian MH updates (src/jaqmc/sampler/mcmc.py:96-199):
  * x' = x + stddev * N(0,1); accept iff 2 log|psi(x')| - 2 log|psi(x)| > log u.
  * Draws come from Philox4x32-10 keyed by `seed`, counter (step = counter + s,
@@ -189,7 +196,7 @@ qmc_status qmc_model_check_error(qmc_model* m, int* code);
  * events and returns, per class, the number of launches and their summed
  * device time in ms, then clears the record.  Classes: QMC_KC_*. */
 enum {
-  QMC_KC_STREAM_LAYER = 0, /* one-electron layer GEMM + tangent epilogue  */
+  QMC_KC_STREAM_LAYER = 0, /* one-electron layers >= 1: GEMM + tangent epilogue */
   QMC_KC_BROADCAST = 1,    /* spin-mean broadcast GEMM                    */
   QMC_KC_ORBITAL = 2,      /* orbital GEMM x envelope                     */
   QMC_KC_LOGDET = 3,       /* LU / log-sum-exp / slogdet traces           */
@@ -198,7 +205,8 @@ enum {
   QMC_KC_PAIR = 6,         /* two-electron layers                         */
   QMC_KC_MH = 7,           /* proposal / accept                           */
   QMC_KC_OTHER = 8,
-  QMC_KC_COUNT = 9
+  QMC_KC_LAYER0 = 9,       /* first one-electron layer (4A-wide input)    */
+  QMC_KC_COUNT = 10
 };
 qmc_status qmc_profile_enable(int on);
 qmc_status qmc_profile_read(int n_classes, int64_t* launches, double* ms);

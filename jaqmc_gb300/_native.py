@@ -65,6 +65,7 @@ _SIGS = {
     "qmc_mh_steps_resident": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_size_t, C.c_void_p]),
+    "qmc_tangent_rows": (C.c_int, [C.c_void_p, C.c_int]),
     "qmc_mh_draws": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p,
                                C.c_void_p, C.c_void_p]),
     "qmc_reduce_mean_var": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -274,6 +275,10 @@ class NativeFermiNet:
                                              ws.numel(), stream_handle(stream)))
         return e, log_prob, accepts
 
+    def tangent_rows(self, op: int) -> int:
+        """Rows per electron that ``op`` propagates (padded tangents for E_L)."""
+        return int(self.lib.qmc_tangent_rows(self.h, int(op)))
+
     def set_grad_budget(self, nbytes: int):
         check(self.lib.qmc_model_set_grad_budget(self.h, int(nbytes)))
 
@@ -304,7 +309,7 @@ class NativeFermiNet:
 
 
 KERNEL_CLASSES = ["stream_layer", "broadcast", "orbital", "logdet", "features", "means", "pair", "mh",
-                  "other"]
+                  "other", "layer0"]
 
 
 def profile_enable(on: bool = True):

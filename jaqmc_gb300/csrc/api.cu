@@ -317,8 +317,9 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
                                             StF32{G2, d.g2_p[l]}));
     EpiLayer<StF32> epi{Gb, ar + a.b1[l], StF32{nullptr, dout}, StF32{out, dout}, T};
     if (l > 0 && din == dout) epi.resid = StF32{const_cast<float*>(in), dout};
-    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l],
-                                                   ar + a.w_main[l], dout, dout, epi));
+    QMC_PROF(l == 0 ? QMC_KC_LAYER0 : QMC_KC_STREAM_LAYER,
+             launch_gemm_simt(s, B * n, rows_map, in, dinp, dinp, G2, d.g2_p[l], d.g2_p[l], ar + a.w_main[l], dout,
+                              dout, epi));
     if (d.upd2[l] && !stream) {
       float* h2o = at<float>(ws, p.h2[h2cur ^ 1]);
       if (fused)
@@ -366,7 +367,7 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
         QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
                                               StF32{G2, d.g2_p[l]}));
       EpiLayer<StSplit> epi{Gb, ar + a.b1[l], StSplit{nullptr, dout, 0}, StSplit{out, dout, p.h1_plane}, T};
-      QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rows_map, X0, dinp, dinp, G2, d.g2_p[l],
+      QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, B * n, rows_map, X0, dinp, dinp, G2, d.g2_p[l],
                                                      d.g2_p[l], ar + a.w_main[l], dout, dout, epi));
     } else {
       bf* in = at<bf>(ws, p.h1[cur]);
@@ -765,6 +766,11 @@ qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, flo
                    at<float>(ws, p.sgn), ke, e_local, flags, s));
   if (pe) QMC_CUDA(cudaMemcpyAsync(pe, at<float>(ws, p.pe), sizeof(float) * batch, cudaMemcpyDeviceToDevice, s));
   return QMC_OK;
+}
+
+int qmc_tangent_rows(const qmc_model* m, int op) {
+  if (!m || op < QMC_OP_FORWARD || op > QMC_OP_GRAD) return -1;
+  return make_plan(m, op, 1).Tp;
 }
 
 qmc_status qmc_mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t seed, uint64_t counter,

@@ -259,87 +259,54 @@ struct ContigTiles {
   }
 };
 
-// Split value <-> one 32-bit word: bf16 hi in the low half, bf16 lo above.
-__device__ __forceinline__ float word_value(uint32_t w) {
-  return __uint_as_float(w << 16) + __uint_as_float(w & 0xffff0000u);
-}
-__device__ __forceinline__ uint32_t value_word(float y) {
-  const __nv_bfloat16 hi = __float2bfloat16_rn(y);
-  const float hf = __bfloat162float(hi);
-  const __nv_bfloat162 p = __floats2bfloat162_rn(hf, y - hf);  // .x (low) = hi exactly
-  return *reinterpret_cast<const uint32_t*>(&p);
-}
-
-// One-electron layer epilogue.  Each warp owns 32 features of the tile and
-// stages its rows through a private shared-memory block of 32-bit words
-// (hi | lo << 16, one word per feature and row), so the residual is read and
-// the output written with 16-byte global accesses and no barrier wider than
-// the warp.  A thread holds one feature (its TMEM lane) and walks the rows.
+// One-electron layer epilogue.  A thread holds one feature (its TMEM lane)
+// and walks the rows of its tile in chunks of 16.  Each warp owns 32 features
+// and two shared-memory chunk buffers of [2 planes][16 rows][32 features]
+// bf16: the residual rows of the next chunk are copied in with cp.async while
+// the current chunk is computed, outputs replace the residual in place, and a
+// chunk leaves with 16-byte stores per plane.  No barrier is wider than the
+// warp.  Tangent rows past T come out as zeros (their inputs are zero rows).
 struct EpiTcLayer : ContigTiles {
+  static constexpr int kCR = 16;                 // rows per chunk
+  static constexpr int kBuf = 2 * kCR * 32;      // bf16 per chunk buffer
   int n, ld;  // electrons per walker, activation row width (n_out)
   StSplit resid, out;
   bool has_resid;
   const float* Gb;
   const float* bias;
 
-  // rows [row0, row0 + R) x features [col0, col0 + 32) of `st` -> wb[R][32]
-  // (8 rows per pass: lane = 4 * row + 8-feature vector)
-  __device__ __forceinline__ void warp_load(const StSplit& st, size_t row0, int R, int col0, int nvec, int lane,
-                                            uint32_t* wb) const {
-    const int vq = lane & 3, rl = lane >> 2;
-    if (vq >= nvec) return;
-    for (int rb = 0; rb < R; rb += 16) {
-      uint4 h[2], l[2];
+  // rows [row0, row0 + nrows) x features [col0, col0 + 32) of `st` -> buf
+  __device__ __forceinline__ void fetch(const StSplit& st, size_t row0, int nrows, int col0, int nvec, int lane,
+                                        __nv_bfloat16* buf) const {
 #pragma unroll
-      for (int p = 0; p < 2; ++p) {
-        const int r = rb + 8 * p + rl;
-        if (r < R) {
-          const __nv_bfloat16* src = st.p + (row0 + r) * (size_t)st.ld + col0 + 8 * vq;
-          h[p] = __ldg(reinterpret_cast<const uint4*>(src));
-          l[p] = __ldg(reinterpret_cast<const uint4*>(src + st.plane));
-        }
-      }
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
+      if (r < nrows && vq < nvec)
+        ptx::cp_async16(buf + (pl * kCR + r) * 32 + 8 * vq,
+                        st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq);
+    }
+    ptx::cp_async_commit();
+  }
+  // buf -> rows [row0, row0 + nrows) of `st`, except row `skip`
+  __device__ __forceinline__ void store(const StSplit& st, size_t row0, int nrows, int skip, int col0, int nvec,
+                                        int lane, const __nv_bfloat16* buf) const {
 #pragma unroll
-      for (int p = 0; p < 2; ++p) {
-        const int r = rb + 8 * p + rl;
-        if (r < R) {
-          uint4 a, b;
-          a.x = __byte_perm(h[p].x, l[p].x, 0x5410);
-          a.y = __byte_perm(h[p].x, l[p].x, 0x7632);
-          a.z = __byte_perm(h[p].y, l[p].y, 0x5410);
-          a.w = __byte_perm(h[p].y, l[p].y, 0x7632);
-          b.x = __byte_perm(h[p].z, l[p].z, 0x5410);
-          b.y = __byte_perm(h[p].z, l[p].z, 0x7632);
-          b.z = __byte_perm(h[p].w, l[p].w, 0x5410);
-          b.w = __byte_perm(h[p].w, l[p].w, 0x7632);
-          uint4* d = reinterpret_cast<uint4*>(wb + r * 32 + 8 * vq);
-          d[0] = a;
-          d[1] = b;
-        }
-      }
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
+      if (r < nrows && r != skip && vq < nvec)
+        *reinterpret_cast<uint4*>(st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq) =
+            *reinterpret_cast<const uint4*>(buf + (pl * kCR + r) * 32 + 8 * vq);
     }
   }
-  // wb[R][32] -> rows [row0, row0 + R) x features [col0, col0 + 32) of `st`
-  __device__ __forceinline__ void warp_store(const StSplit& st, size_t row0, int R, int col0, int nvec, int lane,
-                                             const uint32_t* wb) const {
-    const int vq = lane & 3, rl = lane >> 2;
-    if (vq >= nvec) return;
-    for (int r = rl; r < R; r += 8) {
-      const uint4* s4 = reinterpret_cast<const uint4*>(wb + r * 32 + 8 * vq);
-      const uint4 a = s4[0], b = s4[1];
-      uint4 h, l;
-      h.x = __byte_perm(a.x, a.y, 0x5410);
-      l.x = __byte_perm(a.x, a.y, 0x7632);
-      h.y = __byte_perm(a.z, a.w, 0x5410);
-      l.y = __byte_perm(a.z, a.w, 0x7632);
-      h.z = __byte_perm(b.x, b.y, 0x5410);
-      l.z = __byte_perm(b.x, b.y, 0x7632);
-      h.w = __byte_perm(b.z, b.w, 0x5410);
-      l.w = __byte_perm(b.z, b.w, 0x7632);
-      __nv_bfloat16* dst = st.p + (row0 + r) * (size_t)st.ld + col0 + 8 * vq;
-      *reinterpret_cast<uint4*>(dst) = h;
-      *reinterpret_cast<uint4*>(dst + st.plane) = l;
-    }
+  __device__ __forceinline__ float get(const __nv_bfloat16* buf, int r, int lane) const {
+    return __bfloat162float(buf[r * 32 + lane]) + __bfloat162float(buf[(kCR + r) * 32 + lane]);
+  }
+  __device__ __forceinline__ void put(__nv_bfloat16* buf, int r, int lane, float y) const {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(y);
+    buf[r * 32 + lane] = hi;
+    buf[(kCR + r) * 32 + lane] = __float2bfloat16_rn(y - __bfloat162float(hi));
   }
 
   __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t* ebuf) const {
@@ -349,12 +316,18 @@ struct EpiTcLayer : ContigTiles {
     const int nvec = max(0, min(4, (N - col0) / 8));
     const int fc = f < N ? f : 0;  // clamped feature for loads of parameters
     const float b = bias[fc];
+    __nv_bfloat16* buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * 2 * kBuf;
     if (g.T == 1) {
-      uint32_t* wb = reinterpret_cast<uint32_t*>(ebuf) + q * 32 * 16;
-      for (int c0 = 16 * half; c0 < ti.ng; c0 += 32) {
+      int c0 = 16 * half, k = 0;
+      if (c0 >= ti.ng) return;
+      if (has_resid) fetch(resid, (size_t)(ti.g0 + c0), min(16, ti.ng - c0), col0, nvec, lane, buf0);
+      for (; c0 < ti.ng; c0 += 32, k ^= 1) {
+        __nv_bfloat16* buf = buf0 + k * kBuf;
         const int nrows = min(16, ti.ng - c0);
         const size_t row0 = (size_t)(ti.g0 + c0);
-        if (has_resid) warp_load(resid, row0, nrows, col0, nvec, lane, wb);
+        const bool more = c0 + 32 < ti.ng;
+        if (has_resid && more)
+          fetch(resid, row0 + 32, min(16, ti.ng - c0 - 32), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
         uint32_t r[16];
         ptx::tmem_ld16_nw(taddr + c0, r);
         float gbv[16];
@@ -368,75 +341,85 @@ struct EpiTcLayer : ContigTiles {
           }
         }
         ptx::tmem_wait16(r);
+        if (more) ptx::cp_async_wait<1>();
+        else ptx::cp_async_wait<0>();
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           if (j < nrows) {
             float y = tanhf(__uint_as_float(r[j]) + gbv[j] + b);
-            if (has_resid) y = (y + word_value(wb[j * 32 + lane])) * kRsqrt2;
-            wb[j * 32 + lane] = value_word(y);
+            if (has_resid) y = (y + get(buf, j, lane)) * kRsqrt2;
+            put(buf, j, lane, y);
           }
         }
         __syncwarp();
-        warp_store(out, row0, nrows, col0, nvec, lane, wb);
+        store(out, row0, nrows, -1, col0, nvec, lane, buf);
         __syncwarp();
       }
       return;
     }
     const int Tp = g.Tp, T = g.T;
-    uint32_t* wb = reinterpret_cast<uint32_t*>(ebuf) + q * 32 * Tp;
     for (int lg = half; lg < ti.ng; lg += 2) {
       const int gi = ti.g0 + lg;
       const size_t r0 = (size_t)gi * Tp;
       const uint32_t tcol = taddr + (uint32_t)(lg * Tp);
       const float* gb = Gb + (size_t)(gi / n) * Tp * N + fc;
-      if (has_resid) warp_load(resid, r0, Tp, col0, nvec, lane, wb);
-      float h = 0.f, d1 = 0.f, zL = 0.f, S = 0.f;
-      for (int t0 = 0; t0 < Tp; t0 += 16) {
+      if (has_resid) fetch(resid, r0, min(16, Tp), col0, nvec, lane, buf0);
+      float h = 0.f, d1 = 0.f, zL = 0.f, S = 0.f, res1 = 0.f;
+      int k = 0;
+      for (int t0 = 0; t0 < Tp; t0 += 16, k ^= 1) {
+        __nv_bfloat16* buf = buf0 + k * kBuf;
         const int cs = min(16, Tp - t0);  // a multiple of 4, uniform
+        const bool more = t0 + 16 < Tp;
+        if (has_resid && more) fetch(resid, r0 + t0 + 16, min(16, Tp - t0 - 16), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
         uint32_t r[16];
         if (cs == 16) {
           ptx::tmem_ld16_nw(tcol + t0, r);
         } else {
 #pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (4 * k < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * k, r + 4 * k);
+          for (int kk = 0; kk < 4; ++kk)
+            if (4 * kk < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * kk, r + 4 * kk);
         }
         float gbv[16];
 #pragma unroll
         for (int e = 0; e < 16; ++e) gbv[e] = t0 + e < T ? __ldg(gb + (size_t)(t0 + e) * N) : 0.f;
         ptx::tmem_wait16(r);
+        if (more) ptx::cp_async_wait<1>();
+        else ptx::cp_async_wait<0>();
         __syncwarp();
+        int e0 = 0;
+        if (t0 == 0) {  // value row and Laplacian row
+          h = tanhf(__uint_as_float(r[0]) + gbv[0] + b);
+          d1 = 1.f - h * h;
+          float y = h;
+          if (has_resid) y = (y + get(buf, 0, lane)) * kRsqrt2;
+          put(buf, 0, lane, y);
+          zL = __uint_as_float(r[1]) + gbv[1];
+          if (has_resid) res1 = get(buf, 1, lane);
+          e0 = 2;
+        }
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
-          const int t = t0 + e;
-          if (e >= cs) break;
-          const float z = __uint_as_float(r[e]) + gbv[e];
-          float y;
-          if (t == 0) {
-            h = tanhf(z + b);
-            d1 = 1.f - h * h;
-            y = h;
-          } else if (t == 1) {
-            zL = z;
-            continue;
-          } else if (t < T) {
-            S = fmaf(z, z, S);
-            y = d1 * z;
-          } else {
-            wb[t * 32 + lane] = 0u;
-            continue;
-          }
-          if (has_resid) y = (y + word_value(wb[t * 32 + lane])) * kRsqrt2;
-          wb[t * 32 + lane] = value_word(y);
+          if (e < e0 || e >= cs) continue;
+          const bool real = t0 + e < T;
+          const float z = real ? __uint_as_float(r[e]) + gbv[e] : 0.f;
+          S = fmaf(z, z, S);
+          float y = d1 * z;
+          if (has_resid) y = (y + get(buf, e, lane)) * kRsqrt2;
+          put(buf, e, lane, real ? y : 0.f);
         }
+        __syncwarp();
+        store(out, r0 + t0, cs, t0 == 0 ? 1 : -1, col0, nvec, lane, buf);
+        __syncwarp();
       }
-      float y = d1 * zL - 2.f * h * d1 * S;
-      if (has_resid) y = (y + word_value(wb[32 + lane])) * kRsqrt2;
-      wb[32 + lane] = value_word(y);
-      __syncwarp();
-      warp_store(out, r0, Tp, col0, nvec, lane, wb);
-      __syncwarp();
+      float y1 = d1 * zL - 2.f * h * d1 * S;
+      if (has_resid) y1 = (y1 + res1) * kRsqrt2;
+      if (f < N) {
+        const __nv_bfloat16 hi = __float2bfloat16_rn(y1);
+        __nv_bfloat16* o = out.p + (r0 + 1) * (size_t)out.ld + f;
+        o[0] = hi;
+        o[out.plane] = __float2bfloat16_rn(y1 - __bfloat162float(hi));
+      }
     }
   }
 };
@@ -628,9 +611,9 @@ static int tc_stages_fitting(int n_cols, int ebuf_bytes) {
   return (int)std::min<long>(4, avail / stage_bytes);
 }
 
-// Epilogue staging bytes per half of a tangent layer tile: two planes x Tp
-// rows x 128 bf16 (16 rows when Tp == 1).
-static int tc_layer_ebuf(int Tp) { return 2 * 128 * 2 * (Tp == 1 ? 16 : Tp); }
+// Epilogue staging bytes per half of a layer tile: four warps x two chunk
+// buffers x [2 planes][16 rows][32 features] bf16.
+static int tc_layer_ebuf(int) { return 4 * 2 * 2 * 16 * 32 * 2; }
 
 int tc_groups_per_tile(int Tp) {
   if (Tp == 1) return 256;

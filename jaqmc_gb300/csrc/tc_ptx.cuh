@@ -124,6 +124,17 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
   v[2] = __uint_as_float(r2);
   v[3] = __uint_as_float(r3);
 }
+// 16-byte global -> shared copy that bypasses the registers (and L1).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most N of this thread's committed groups are still in flight
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // Loads without the wait: the registers become valid at tmem_wait32, which
 // names them as operands so no use can be scheduled before it.
 __device__ __forceinline__ void tmem_ld4_nw(uint32_t taddr, uint32_t* r) {
