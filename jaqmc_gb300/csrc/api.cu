@@ -420,6 +420,16 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
   return QMC_OK;
 }
 
+// Value-only mixed passes take the envelope factor out of the tensor-core
+// epilogue (too few warps to hide its exponentials): a full-occupancy kernel
+// writes the factors into the two-electron buffer, unused by then, and the LU
+// kernel multiplies them in as it loads the matrices.
+static bool env_in_lu(const Dims& d, const Plan& p) {
+  const bool params_fit = (size_t)8 * (d.split ? 2 : 1) * d.A * d.K * d.n <= 48 * 1024;
+  return p.mixed && p.T == 1 && d.n <= 32 && params_fit &&
+         p.h2[1] - p.h2[0] >= (size_t)p.B * d.K * d.n * d.n * sizeof(float);
+}
+
 static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
   const Dims& d = m->d;
   const ArenaLayout& a = m->a;
@@ -449,17 +459,7 @@ static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cu
     oa.rae = at<float>(ws, p.rae);
     oa.aevec = at<float>(ws, p.aevec);
     oa.A = at<float>(ws, p.amat);
-    oa.env = nullptr;
-    // value-only passes: envelopes by a full-occupancy kernel into the (now
-    // unused) two-electron buffer, when it is large enough
-    const size_t env_bytes = (size_t)p.B * d.K * d.n * d.n * sizeof(float);
-    if (p.T == 1 && p.h2[1] - p.h2[0] >= env_bytes) {
-      float* env = at<float>(ws, p.h2[0]);
-      QMC_PROF(QMC_KC_ORBITAL, launch_envelope_value(s, p.B, d.n, d.n_up, d.split, d.K, d.A, d.env_abs,
-                                                     oa.pi[0], oa.sigma[0], oa.pi[1], oa.sigma[1],
-                                                     at<float>(ws, p.rae), env));
-      oa.env = env;
-    }
+    oa.raw = env_in_lu(d, p);
     oa.err = m->dev_err;
     QMC_PROF_TRY(QMC_KC_ORBITAL, tc_orbitals(s, oa));
     return QMC_OK;
@@ -493,8 +493,17 @@ qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electron
   if (p.mixed) QMC_TRY(run_backbone_mixed(m, p, ws, s, &hb));
   else QMC_TRY(run_backbone_plain(m, p, ws, s, &hb));
   QMC_TRY(run_orbitals(m, p, ws, hb, s));
+  EnvArgs env{};
+  if (env_in_lu(d, p)) {
+    const int c1 = d.split ? 1 : 0;
+    env.env = at<float>(ws, p.h2[0]);
+    QMC_PROF(QMC_KC_ORBITAL, launch_envelope_value(s, p.B, d.n, d.n_up, d.split, d.K, d.A, d.env_abs,
+                                                   ar + m->a.env_pi[0], ar + m->a.env_sigma[0],
+                                                   ar + m->a.env_pi[c1], ar + m->a.env_sigma[c1],
+                                                   at<float>(ws, p.rae), const_cast<float*>(env.env)));
+  }
   QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
-                         flags, nullptr));
+                                        flags, nullptr, env_in_lu(d, p) ? &env : nullptr));
   return QMC_OK;
 }
 

@@ -137,38 +137,49 @@ cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, 
 // determinant k, electron i, orbital j): sum_I pi[j,I,k] exp(-s r_iI) with
 // s = |sigma[j,I,k]| (abs_isotropic) or sigma (isotropic), per spin channel
 // of electron i (src/jaqmc/wavefunction/output/envelope.py:98-140).  Same
-// terms, same order as the tangent epilogues, so the product is unchanged.
-__global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A, int env_abs,
+// terms in the same order as the tangent epilogues.  One block per walker,
+// thread (i, j); the parameters are staged as [channel][I][k][j] so a warp
+// reads consecutive j.
+__global__ void k_envelope_value(int n, int n_up, int split, int K, int A, int env_abs,
                                  const float* __restrict__ pi0, const float* __restrict__ sg0,
                                  const float* __restrict__ pi1, const float* __restrict__ sg1,
                                  const float* __restrict__ rae, float* __restrict__ env) {
-  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)B * K * n * n) return;
-  const int j = (int)(e % n);
-  size_t r = e / n;
-  const int i = (int)(r % n);
-  r /= n;
-  const int k = (int)(r % K);
-  const int w = (int)(r / K);
-  const bool s1 = split && i >= n_up;
-  const float* pi = s1 ? pi1 : pi0;
-  const float* sg = s1 ? sg1 : sg0;
-  const float* ra = rae + ((size_t)w * n + i) * A;
-  float acc = 0.f;
-  for (int I = 0; I < A; ++I) {
+  extern __shared__ float she[];
+  const int nch = split ? 2 : 1, per = A * K * n;
+  float* ps = she;               // [nch][A][K][n]
+  float* ss = she + nch * per;   // [nch][A][K][n], already |sigma| when env_abs
+  for (int e = threadIdx.x; e < nch * per; e += blockDim.x) {
+    const int c = e / per, rem = e % per;
+    const int I = rem / (K * n), k = (rem / n) % K, j = rem % n;
     const size_t q = ((size_t)j * A + I) * K + k;
-    const float sv = __ldg(sg + q);
-    acc += __ldg(pi + q) * expf(-(env_abs ? fabsf(sv) : sv) * __ldg(ra + I));
+    ps[e] = (c ? pi1 : pi0)[q];
+    const float sv = (c ? sg1 : sg0)[q];
+    ss[e] = env_abs ? fabsf(sv) : sv;
   }
-  env[e] = acc;
+  __syncthreads();
+  const int w = blockIdx.x;
+  const int i = threadIdx.x / n, j = threadIdx.x % n;
+  if (i >= n) return;
+  const int c = split && i >= n_up ? 1 : 0;
+  const float* ra = rae + ((size_t)w * n + i) * A;
+  float* out = env + (size_t)w * K * n * n + i * n + j;
+  for (int k = 0; k < K; ++k) {
+    float acc = 0.f;
+    for (int I = 0; I < A; ++I) {
+      const int o = ((c * A + I) * K + k) * n + j;
+      acc += ps[o] * expf(-ss[o] * __ldg(ra + I));
+    }
+    out[(size_t)k * n * n] = acc;
+  }
 }
 
 cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,
                                   const float* rae, float* env) {
-  const size_t total = (size_t)B * K * n * n;
-  k_envelope_value<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, split, K, A, env_abs, pi0, sg0,
-                                                                    pi1, sg1, rae, env);
+  const size_t sm = sizeof(float) * 2 * (split ? 2 : 1) * (size_t)A * K * n;
+  if (n * n > 1024 || sm > 48 * 1024) return cudaErrorNotSupported;
+  const int threads = (n * n + 31) / 32 * 32;
+  k_envelope_value<<<B, threads, sm, s>>>(n, n_up, split, K, A, env_abs, pi0, sg0, pi1, sg1, rae, env);
   return cudaGetLastError();
 }
 
@@ -670,9 +681,59 @@ __global__ void k_mean_h2(int B, int n, int n_up, int C, int Tp, int T, int d2, 
   G2.put(r, col, v);
 }
 
+// k_mean_h2 with 8 features per thread (16-byte loads and stores).
+template <class Out>
+__global__ void k_mean_h2_vec(int B, int n, int n_up, int C, int Tp, int T, int d2, int P2,
+                              const float* __restrict__ H2, int g2p, Out G2) {
+  const int nv = g2p / 8;
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * n * Tp * nv) return;
+  const int col = 8 * (int)(e % nv);
+  const size_t r = e / nv;
+  const int t = (int)(r % Tp);
+  const size_t wi = r / Tp;
+  const int i = (int)(wi % n);
+  const int w = (int)(wi / n);
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (col < C * d2 && t < T) {
+    const int sc = col / d2, f = col % d2;
+    int a0, a1;
+    channel_range(sc, C, n, n_up, &a0, &a1);
+    const float inv = 1.0f / (float)(a1 - a0);
+    // row of pair (a, i), tangent slot p
+    auto row = [&](int a, int p) { return ((((size_t)w * n + a) * n + i) * P2 + p) * d2 + f; };
+    auto add8 = [&](size_t o, float sgn) {
+      const float4 x = __ldg(reinterpret_cast<const float4*>(H2 + o));
+      const float4 y = __ldg(reinterpret_cast<const float4*>(H2 + o + 4));
+      acc[0] += sgn * x.x; acc[1] += sgn * x.y; acc[2] += sgn * x.z; acc[3] += sgn * x.w;
+      acc[4] += sgn * y.x; acc[5] += sgn * y.y; acc[6] += sgn * y.z; acc[7] += sgn * y.w;
+    };
+    float scale = inv;
+    if (t <= 1) {
+      for (int a = a0; a < a1; ++a) add8(row(a, t), 1.f);
+      if (t == 1) scale = 2.0f * inv;
+    } else {
+      const int dd = t - 2, el = dd / 3, c = dd % 3;
+      if (el == i) {
+        for (int a = a0; a < a1; ++a) add8(row(a, 2 + c), -1.f);
+      } else if (el >= a0 && el < a1) {
+        add8(row(el, 2 + c), 1.f);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] *= scale;
+  }
+  store8(G2, r, col, acc);
+}
+
 template <class Out>
 cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d2,
                            int P2, const float* H2, int g2p, Out G2) {
+  if (d2 % 8 == 0 && g2p % 8 == 0 && ((uintptr_t)H2 & 15) == 0 && vec8_ok(G2)) {
+    const size_t total = (size_t)B * n * Tp * (g2p / 8);
+    k_mean_h2_vec<Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, T, d2, P2, H2, g2p, G2);
+    return cudaGetLastError();
+  }
   size_t total = (size_t)B * n * Tp * g2p;
   k_mean_h2<Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, T, d2, P2, H2,
                                                                   g2p, G2);
@@ -1021,9 +1082,9 @@ __global__ void k_logdet(int n, int K, int Tp, int T, const float* __restrict__ 
 // are not kept (only U's diagonal is needed).  Matrices whose pivot growth
 // exceeds the threshold are re-factorised in FP64 afterwards by warp 0.
 template <int SEG>
-__global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int WB, const float* __restrict__ A,
+__global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int WB, float* __restrict__ A,
                                                       float* __restrict__ logpsi, float* __restrict__ sign,
-                                                      uint8_t* __restrict__ flags) {
+                                                      uint8_t* __restrict__ flags, EnvArgs env) {
   extern __shared__ double shv[];
   const int nmat = WB * K;
   double* lds = shv;                                       // [nmat]
@@ -1041,9 +1102,15 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
     const int w = w0 + mloc / K;
     const bool active = mloc < nmat && w < B;
     float r[SEG];
-    const float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
+    float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
 #pragma unroll
     for (int j = 0; j < SEG; ++j) r[j] = (active && i < n && j < n) ? Am[i * n + j] : (j == i ? 1.f : 0.f);
+    if (env.env && active && i < n) {  // envelope factors of row i
+      const float* Em = env.env + ((size_t)w * K + (mloc % K)) * n * n;
+#pragma unroll
+      for (int j = 0; j < SEG; ++j)
+        if (j < n) r[j] *= __ldg(Em + i * n + j);
+    }
     float amax = 0.f;
 #pragma unroll
     for (int j = 0; j < SEG; ++j) amax = fmaxf(amax, (i < n) ? fabsf(r[j]) : 0.f);
@@ -1109,7 +1176,12 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
     for (int mloc = 0; mloc < nmat; ++mloc) {
       const int w = w0 + mloc / K;
       if (w >= B || !redo[mloc]) continue;
-      const float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
+      float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
+      if (env.env) {  // the FP64 pass reads the matrix with its envelope factors
+        const float* Em = env.env + ((size_t)w * K + (mloc % K)) * n * n;
+        for (int e = lane; e < n * n; e += 32) Am[e] *= Em[e];
+        __syncwarp();
+      }
       DetOut o = det_stage<double, 16>(Am, n, 1, scratch, nullptr, true);
       if (lane == 0) {
         lds[mloc] = o.ld;
@@ -1151,26 +1223,29 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
   }
 }
 
-static cudaError_t launch_logdet_value(cudaStream_t s, int B, int n, int K, const float* A, float* logpsi,
-                                       float* sign, uint8_t* flags) {
+static cudaError_t launch_logdet_value(cudaStream_t s, int B, int n, int K, float* A, float* logpsi,
+                                       float* sign, uint8_t* flags, const EnvArgs* envp) {
+  EnvArgs env{};
+  if (envp) env = *envp;
   const int seg = n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32;
   const int per_pass = 8 * (32 / seg);
   const int WB = std::max(1, per_pass / K);
   const size_t sm = align_up((size_t)WB * K * 16 + 16, 16) + DetScratch(n).bytes;
   const unsigned grid = (unsigned)((B + WB - 1) / WB);
   switch (seg) {
-    case 4: k_logdet_value<4><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
-    case 8: k_logdet_value<8><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
-    case 16: k_logdet_value<16><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
-    default: k_logdet_value<32><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags); break;
+    case 4: k_logdet_value<4><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags, env); break;
+    case 8: k_logdet_value<8><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags, env); break;
+    case 16: k_logdet_value<16><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags, env); break;
+    default: k_logdet_value<32><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags, env); break;
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
-                          uint8_t* flags, int* n_refactor) {
-  if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, A, logpsi, sign, flags);
+                          uint8_t* flags, int* n_refactor, const EnvArgs* env) {
+  if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, const_cast<float*>(A), logpsi, sign, flags, env);
+  if (env) return cudaErrorInvalidValue;  // tangent passes take enveloped matrices
   const int D = T > 1 ? T - 2 : 0;
   const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
   const DetScratch sc(n);

@@ -5,6 +5,18 @@
 
 namespace qmc {
 
+// Value-only determinant passes whose orbital matrices arrive without the
+// envelope factor: the factors (launch_envelope_value, laid out like the
+// matrices) are multiplied in, and written back, as the matrices are loaded.
+struct EnvArgs {
+  const float* env;  // [B][K][n][n]
+};
+// Envelopes [w][k][i][j] of the value-only orbital matrices.
+cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
+                                  const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                  const float* rae, float* env);
+
+
 // Features of MoleculeFeatures (input/atomic.py:46-79) with tangents.
 //  X0    [(w*n+i)*Tp + t][K0p]   one-electron rows (ae features)
 //  H2    [(w*n+i)*n + j][P2][4]  two-electron rows, compact tangents
@@ -45,7 +57,7 @@ cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp
 // combined into the kinetic energy.  A: [w][k][Tp][n][n].
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
-                          uint8_t* flags, int* n_refactor);
+                          uint8_t* flags, int* n_refactor, const EnvArgs* env = nullptr);
 
 // Cotangent of log|psi| with respect to the value orbital matrices:
 // Abar[w][k] = w_k A_k^{-T}; also writes log|psi| (may be null).
@@ -69,10 +81,6 @@ size_t pair_stream_smem(int n, int nl);
 template <class Out>
 cudaError_t launch_pair_stream_value(cudaStream_t s, int B, const PairStreamArgs& a, const PairStreamOut<Out>& o);
 
-// Envelopes [w][k][i][j] of the value-only orbital matrices.
-cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
-                                  const float* pi0, const float* sg0, const float* pi1, const float* sg1,
-                                  const float* rae, float* env);
 
 // MH proposal x' = x + stddev * N(0,1) for update `step` of a call.
 // The update index is ctr (+ *ctr_dev when ctr_dev is not null).

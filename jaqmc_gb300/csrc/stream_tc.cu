@@ -448,7 +448,7 @@ struct EpiTcOrbital {
   const float* rae;
   const float* aevec;
   float* A;
-  const float* env;  // value-only passes: precomputed envelopes laid out like A, or null
+  int raw;           // value-only passes: store orbitals without the envelope factor
   int n_rows;  // B * n (value-only passes)
   __device__ TileInfo tile(int tx, const TcArgs& g) const {
     TileInfo t{};
@@ -540,15 +540,13 @@ struct EpiTcOrbital {
         for (int jj = 0; jj < 16; ++jj) {
           if (c0 + jj < ti.ng && (!split || (i < n_up ? 0 : 1) == ti.a_sel)) {
             const size_t idx = ((size_t)w * K + k) * ts + (size_t)i * n + j;
-            float ev;
-            if (env) {
-              ev = __ldg(env + idx);
+            if (raw) {
+              A[idx] = v[jj];
             } else {
               float e[5];
               envelope(ti.a_sel, w, i, k, j, 1, e, ep);
-              ev = e[0];
+              A[idx] = v[jj] * e[0];
             }
-            A[idx] = v[jj] * ev;
           }
           if (++i == n) {
             i = 0;
@@ -811,7 +809,7 @@ qmc_status tc_orbitals(cudaStream_t s, const TcOrbitalArgs& a) {
   e.rae = a.rae;
   e.aevec = a.aevec;
   e.A = a.A;
-  e.env = a.T == 1 ? a.env : nullptr;
+  e.raw = a.T == 1 ? a.raw : 0;
   return launch(s, mA0, mA1, mB, mB, g, n_tiles, e);
 }
 

@@ -51,7 +51,7 @@ struct TcOrbitalArgs {
   const float* pi[2]; const float* sigma[2];        // per channel [n][A][K]
   const float* rae; const float* aevec;
   float* A;                                         // [w][k][Tp][n][n]
-  const float* env;  // T == 1: envelopes [w][k][n][n] from launch_envelope_value, or null
+  int raw;           // T == 1: store orbitals without the envelope (applied by the LU pass)
   int* err;
 };
 // orbital projection x envelope with the product rule.
