@@ -108,6 +108,17 @@ def dist_env():
         os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(ms: float, device) -> float:
+    """The slowest rank's time (every rank calls this after its timed region)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
 def stream_layer_flops(cfg, n_atoms, B, T):
     """Algorithmic FLOPs of one launch set of the one-electron layer GEMMs for
     T tangent rows per electron: 2 * rows * (d_in + C*d2_in) * d_out summed over
@@ -304,12 +315,7 @@ def run_ours(args, wl):
             mv = request(m, x, counter0 + k * S_)
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t)
-        return ms, mv
+        return max_over_ranks(e0.elapsed_time(e1), dev), mv
 
     # burn-in: sample the walkers from |psi|^2 first (the reference's
     # SamplingWorkStage burn-in), so energies are those of a running VMC
@@ -377,11 +383,7 @@ def run_ours(args, wl):
         host_out.copy_(mv, non_blocking=True)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
 
     ms_main = results[prec_main]["ms_per_step"]
     value = world * B * S_ / (ms_main / 1e3)

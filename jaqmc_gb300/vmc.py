@@ -27,6 +27,7 @@ from typing import Any, NamedTuple
 
 import numpy as np
 import torch
+import torch.distributed
 
 from . import _native
 from . import params as P
@@ -223,15 +224,71 @@ class MCMCSampler:
         return new_data, {"pmove": pmove}, new_state
 
 
+# ------------------------------------------------------- data-parallel ranks
+# Walkers are sharded across ranks (one GPU each) with no data-path
+# collective; the reference's per-step exchanges are host-side reductions of a
+# few numbers: the pmean of the energy statistics (src/jaqmc/estimator/base.py:
+# 43-48), the all-gather of the clip window (src/jaqmc/utils/clip.py:21,38)
+# and the pmean of the gradient.  They run over torch.distributed when a
+# process group with more than one rank is initialised, and are identities
+# otherwise.
+def _ranks(group=None) -> int:
+    d = torch.distributed
+    return d.get_world_size(group) if d.is_available() and d.is_initialized() else 1
+
+
+def combine_moments(mean: float, var: float, count: int, group=None):
+    """Global (mean, variance, count) from each rank's FP64 batch moments,
+    weighting ranks by their walker counts."""
+    if _ranks(group) == 1:
+        return mean, var, count
+    t = torch.tensor([count * mean, count * (var + mean * mean), float(count)], dtype=torch.float64,
+                     device=_collective_device(group))
+    torch.distributed.all_reduce(t, group=group)
+    n = float(t[2])
+    m = float(t[0]) / n
+    return m, float(t[1]) / n - m * m, int(n)
+
+
+def _collective_device(group=None):
+    backend = torch.distributed.get_backend(group)
+    return torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" else torch.device("cpu")
+
+
+def gather_walkers(x: torch.Tensor, group=None) -> torch.Tensor:
+    """All ranks' per-walker values concatenated in rank order (equal batch
+    sizes per rank, as the reference's all_gather assumes)."""
+    if _ranks(group) == 1:
+        return x
+    dev = _collective_device(group)
+    xl = x.detach().to(dev)
+    parts = [torch.empty_like(xl) for _ in range(_ranks(group))]
+    torch.distributed.all_gather(parts, xl, group=group)
+    return torch.cat(parts).to(x.device)
+
+
+def allreduce_sum(x: torch.Tensor, group=None) -> torch.Tensor:
+    if _ranks(group) == 1:
+        return x
+    dev = _collective_device(group)
+    t = x.detach().to(dev).clone()
+    torch.distributed.all_reduce(t, group=group)
+    return t.to(x.device)
+
+
 # ----------------------------------------------------------------- estimators
-def mean_reduce(walker_stats: dict, include_variance: bool = True) -> dict:
-    """FP64 walker-batch mean and variance on the GPU (NaNs skipped)."""
+def mean_reduce(walker_stats: dict, include_variance: bool = True, group=None) -> dict:
+    """FP64 walker-batch mean and variance on the GPU (NaNs skipped), combined
+    across ranks."""
     out = {}
     for k, v in walker_stats.items():
-        mv = _native.reduce_mean_var(torch.as_tensor(v).reshape(-1)).cpu().numpy()
-        out[k] = float(mv[0])
+        x = torch.as_tensor(v).reshape(-1)
+        mv = _native.reduce_mean_var(x).cpu().numpy()
+        count = int(torch.isfinite(x).sum()) if _ranks(group) > 1 else x.numel()
+        m, var, _ = combine_moments(float(mv[0]), float(mv[1]), count, group)
+        out[k] = m
         if include_variance:
-            out[f"{k}_var"] = float(mv[1])
+            out[f"{k}_var"] = var
     return out
 
 
@@ -296,20 +353,35 @@ class TotalEnergy:
         return mean_reduce(walker_stats)
 
 
-def clip_observable(x: torch.Tensor, method: str = "mad", scale: float = 5.0) -> torch.Tensor:
-    """MAD / IQR clipping window (``src/jaqmc/utils/clip.py:11-68``), on the device."""
+def clip_observable(x: torch.Tensor, method: str = "mad", scale: float = 5.0, group=None) -> torch.Tensor:
+    """MAD / IQR clipping window over all ranks' walkers (``src/jaqmc/utils/clip.py:11-68``):
+    medians and quartiles as ``nanmedian`` / ``nanquantile`` (the two middle
+    values averaged for an even count)."""
     if method == "none":
         return x
-    finite = x[torch.isfinite(x)]
+    if method not in ("mad", "iqr"):
+        raise ValueError(f"Unknown clip method {method!r}.")
+    allx = gather_walkers(x, group).double()
     if method == "mad":
-        med = finite.median()
-        dev = (finite - med).abs().median()
-        return x.clamp(med - scale * dev, med + scale * dev)
-    if method == "iqr":
-        q = torch.quantile(finite.double(), torch.tensor([0.25, 0.75], dtype=torch.float64, device=x.device))
+        med = torch.nanquantile(allx, 0.5)
+        dev = torch.nanquantile((allx - med).abs(), 0.5)
+        lo, hi = med - scale * dev, med + scale * dev
+    else:
+        q = torch.nanquantile(allx, torch.tensor([0.25, 0.75], dtype=torch.float64, device=allx.device))
         iqr = q[1] - q[0]
-        return x.clamp(float(q[0] - scale * iqr), float(q[1] + scale * iqr))
-    raise ValueError(f"Unknown clip method {method!r}.")
+        lo, hi = q[0] - scale * iqr, q[1] + scale * iqr
+    return x.clamp(lo.to(x.dtype).item(), hi.to(x.dtype).item())
+
+
+def energy_gradient_weights(loss: torch.Tensor, clip_method: str = "mad", clip_scale: float = 5.0, group=None):
+    """c_w = 2 (E_c,w - <E_c>) / B_total with the clipped local energies of all
+    ranks (``src/jaqmc/estimator/loss_grad.py:96-128``); the gradient is then
+    sum_w c_w d log|psi_w| / d theta summed over ranks."""
+    ec = clip_observable(loss.double(), clip_method, clip_scale, group)
+    tot = allreduce_sum(torch.stack([ec.sum(), torch.tensor(float(ec.numel()), dtype=torch.float64,
+                                                             device=ec.device)]), group)
+    mean, B = tot[0] / tot[1], tot[1]
+    return 2.0 * (ec - mean) / B, ec
 
 
 @dataclass
@@ -327,15 +399,14 @@ class LossAndGrad:
     def evaluate_batch_walkers(self, params, batched_data, prev_walker_stats, state, rngs=None):
         return {"loss": prev_walker_stats[self.loss_key]}, state
 
-    def gradient(self, params, batched_data: BatchedData, loss: torch.Tensor):
+    def gradient(self, params, batched_data: BatchedData, loss: torch.Tensor, group=None):
         wf = self.f_log_psi
         loss = torch.as_tensor(loss).to(wf._dev()).double()
-        ec = clip_observable(loss, self.clip_method, self.clip_scale)
-        B = loss.shape[0]
-        weights = 2.0 * (ec - ec.mean()) / B
+        weights, ec = energy_gradient_weights(loss, self.clip_method, self.clip_scale, group)
         m = wf.model(batched_data.data, params)
         J, g, _ = m.grad(_device_electrons(batched_data.data.electrons, wf._dev()), weights=weights,
                          per_walker=self.per_walker)
+        g = allreduce_sum(g, group)
         stats = {"loss": float(loss.mean()), "clipped_loss": float(ec.mean()), "grads": g}
         if J is not None:
             stats["grad_logpsi"] = J
