@@ -443,7 +443,10 @@ FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12
 # dram__bytes_read.sum + dram__bytes_write.sum of one forward-Laplacian launch
 # of the one-electron layer kernel, from the committed ncu capture at 512
 # walkers, scaled to the workload's walkers (traffic grows with the rows)
-TRAFFIC_PER_WALKER: dict = {}
+TRAFFIC_PER_WALKER: dict = {
+    # ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch at 512 walkers
+    ("N2", "mixed"): (449.865472e6 + 283.921408e6) / 512,
+}
 
 
 def fl_layer_bytes_flops(cfg, mol, B, Tp):
