@@ -169,3 +169,98 @@ def unflatten(flat, leaves):
 
 def count(leaves) -> int:
     return int(sum(int(np.prod(s)) for _, s in leaves))
+
+
+# ------------------------------------------------------------------ Psiformer
+@dataclass
+class PsiformerConfig:
+    """Hyper-parameters of ``PsiformerWavefunction``
+    (src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94): same names and
+    defaults; Pre-LN layers, biases on, abs_isotropic envelope, SimpleEE
+    Jastrow, log-rescaled input features."""
+
+    nspins: tuple = (1, 1)
+    ndets: int = 16
+    num_layers: int = 4
+    num_heads: int = 4
+    heads_dim: int = 64
+    mlp_hidden_dims: list = field(default_factory=lambda: [256])
+    envelope: str = "abs_isotropic"
+    orbitals_spin_split: bool = True
+    jastrow: str = "simple_ee"
+    jastrow_alpha_init: float = 1.0
+    rescale: bool = True
+    full_det: bool = True
+
+    @property
+    def n(self) -> int:
+        return int(sum(self.nspins))
+
+    @property
+    def dim(self) -> int:
+        return self.num_heads * self.heads_dim
+
+    @property
+    def split(self) -> bool:
+        return bool(self.orbitals_spin_split and self.nspins[0] > 0 and self.nspins[1] > 0)
+
+
+def psiformer_leaves(cfg: PsiformerConfig, n_atoms: int):
+    """``[(path, shape)]`` in C-ABI order (the network's order)."""
+    n, K, D, H, Dh = cfg.n, cfg.ndets, cfg.dim, cfg.num_heads, cfg.heads_dim
+    out = [(("backbone_layer", "Dense_0", "kernel"), (4 * n_atoms + 1, D)),
+           (("backbone_layer", "Dense_0", "bias"), (D,))]
+    for l in range(cfg.num_layers):
+        base = ("backbone_layer", f"PsiformerLayer_{l}")
+        out.append((base + ("LayerNorm_0", "scale"), (D,)))
+        out.append((base + ("LayerNorm_0", "bias"), (D,)))
+        mha = base + ("MultiHeadDotProductAttention_0",)
+        for nm in ("query", "key", "value"):
+            out.append((mha + (nm, "kernel"), (D, H, Dh)))
+            out.append((mha + (nm, "bias"), (H, Dh)))
+        out.append((mha + ("out", "kernel"), (H, Dh, D)))
+        out.append((mha + ("out", "bias"), (D,)))
+        out.append((base + ("LayerNorm_1", "scale"), (D,)))
+        out.append((base + ("LayerNorm_1", "bias"), (D,)))
+        dims = list(cfg.mlp_hidden_dims) + [D]
+        din = D
+        for k, dout in enumerate(dims):
+            out.append((base + (f"Dense_{k}", "kernel"), (din, dout)))
+            out.append((base + (f"Dense_{k}", "bias"), (dout,)))
+            din = dout
+    if cfg.split:
+        for s in range(2):
+            out.append((("orbital_layer", "SplitChannelDense_0", f"DenseGeneral_{s}", "kernel"), (D, K, n)))
+    else:
+        out.append((("orbital_layer", "DenseGeneral_0", "kernel"), (D, K, n)))
+    for nm in (["_env_up", "_env_down"] if cfg.split else ["_env"]):
+        out.append((("envelope_layer", nm, "pi"), (n, n_atoms, K)))
+        out.append((("envelope_layer", nm, "sigma"), (n, n_atoms, K)))
+    if cfg.jastrow == "simple_ee":
+        out.append((("jastrow_layer", "alpha_par"), (1,)))
+        out.append((("jastrow_layer", "alpha_anti"), (1,)))
+    return out
+
+
+def init_psiformer(cfg: PsiformerConfig, n_atoms: int, seed: int = 0):
+    """A Flax-shaped parameter tree: fan-in-scaled N(0, 1/fan_in) kernels, zero
+    biases, LayerNorm scale 1 / bias 0, envelope pi = sigma = 1, Jastrow alphas
+    at ``jastrow_alpha_init``."""
+    rng = np.random.default_rng(seed)
+    tree = {}
+    for path, shape in psiformer_leaves(cfg, n_atoms):
+        name = path[-1]
+        if name == "kernel":
+            if path[-2] == "out":
+                fan_in = shape[0] * shape[1]
+            else:
+                fan_in = shape[0]
+            v = (rng.standard_normal(shape) / np.sqrt(fan_in)).astype(np.float32)
+        elif name == "scale" or name in ("pi", "sigma"):
+            v = np.ones(shape, np.float32)
+        elif name in ("alpha_par", "alpha_anti"):
+            v = np.full(shape, cfg.jastrow_alpha_init, np.float32)
+        else:
+            v = np.zeros(shape, np.float32)
+        _set(tree, path, v)
+    return tree
