@@ -66,6 +66,26 @@ typedef struct {
   int precision;                        /* QMC_PRECISION_*                      */
 } qmc_ferminet_config;
 
+/* Psiformer with the SimpleEE Jastrow (PsiformerWavefunction,
+ * src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94): Pre-LN layers,
+ * biased attention projections and input layer, log-rescaled input features,
+ * no orbital bias.  Value path only: qmc_forward, qmc_mh_steps(_resident) and
+ * qmc_mh_draws; qmc_local_energy and qmc_grad return QMC_ERR_UNSUPPORTED. */
+typedef struct {
+  int n_up, n_down, n_atoms;
+  int ndets;                            /* K                                    */
+  int n_layers;                         /* <= 8                                 */
+  int n_heads, head_dim;                /* attention width n_heads*head_dim     */
+  int n_mlp;                            /* hidden MLP widths per layer (<= 4)   */
+  int mlp_dims[4];
+  int envelope;                         /* QMC_ENVELOPE_*                       */
+  int orbitals_spin_split;              /* 0/1                                  */
+  int jastrow;                          /* 0 none, 1 SimpleEE                   */
+  int precision;                        /* QMC_PRECISION_*                      */
+} qmc_psiformer_config;
+
+enum { QMC_KIND_FERMINET = 0, QMC_KIND_PSIFORMER = 1 };
+
 typedef struct qmc_model qmc_model;
 
 /* Text of the calling thread's last error ("" if none). */
@@ -80,6 +100,11 @@ qmc_status qmc_device_check(int* sm_major, int* sm_minor, int* n_sms);
  * FermiNetWavefunction + its wiring (src/jaqmc/app/molecule/workflow.py:119-136). */
 qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atoms_host,
                                const float* charges_host, qmc_model** out);
+/* Create a Psiformer model on the current device (see qmc_psiformer_config).
+ * Replaces the construction of PsiformerWavefunction + its wiring
+ * (src/jaqmc/app/molecule/workflow.py:119-136). */
+qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, const float* atoms_host,
+                                const float* charges_host, qmc_model** out);
 qmc_status qmc_model_destroy(qmc_model* m);
 
 /* Number of float32 entries of the flat parameter vector (leaf order:

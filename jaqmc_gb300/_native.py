@@ -38,6 +38,13 @@ class FermiNetConfigC(C.Structure):
                 ("orbitals_spin_split", C.c_int), ("precision", C.c_int)]
 
 
+class PsiformerConfigC(C.Structure):
+    _fields_ = [("n_up", C.c_int), ("n_down", C.c_int), ("n_atoms", C.c_int), ("ndets", C.c_int),
+                ("n_layers", C.c_int), ("n_heads", C.c_int), ("head_dim", C.c_int), ("n_mlp", C.c_int),
+                ("mlp_dims", C.c_int * 4), ("envelope", C.c_int), ("orbitals_spin_split", C.c_int),
+                ("jastrow", C.c_int), ("precision", C.c_int)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -47,6 +54,8 @@ _SIGS = {
     "qmc_device_check": (C.c_int, [C.POINTER(C.c_int)] * 3),
     "qmc_ferminet_create": (C.c_int, [C.POINTER(FermiNetConfigC), C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_void_p)]),
+    "qmc_psiformer_create": (C.c_int, [C.POINTER(PsiformerConfigC), C.c_void_p, C.c_void_p,
+                                       C.POINTER(C.c_void_p)]),
     "qmc_model_destroy": (C.c_int, [C.c_void_p]),
     "qmc_param_count": (C.c_size_t, [C.c_void_p]),
     "qmc_model_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -148,9 +157,8 @@ class Workspace:
 class NativeFermiNet:
     """One ``qmc_model`` handle: a FermiNet for one molecule on one device."""
 
-    def __init__(self, cfg, atoms, charges, precision="fp32", device=None):
-        lib = load()
-        self.lib = lib
+    def _open(self, device):
+        self.lib = load()
         if not torch.cuda.is_available():
             raise RuntimeError("no CUDA device: the qmc library has no CPU fallback")
         dev = torch.device(device or "cuda")
@@ -159,6 +167,10 @@ class NativeFermiNet:
         self.device = dev
         torch.cuda.set_device(self.device)
         device_check()
+
+    def __init__(self, cfg, atoms, charges, precision="fp32", device=None):
+        self._open(device)
+        lib = self.lib
         c = FermiNetConfigC()
         c.n_up, c.n_down = int(cfg.nspins[0]), int(cfg.nspins[1])
         atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 3))
@@ -177,8 +189,11 @@ class NativeFermiNet:
             raise QmcError(7, "use_last_layer=True is not supported")
         h = C.c_void_p()
         check(lib.qmc_ferminet_create(C.byref(c), atoms.ctypes.data, charges.ctypes.data, C.byref(h)))
+        self._finish(h, c.n_up + c.n_down, precision)
+
+    def _finish(self, h, n, precision):
         self.h = h
-        self.n = c.n_up + c.n_down
+        self.n = n
         self.precision = precision
         self.ws = Workspace(self.device)
 
@@ -306,6 +321,34 @@ class NativeFermiNet:
         check(self.lib.qmc_mh_draws(self.h, int(batch), int(steps), int(seed), int(counter), ptr(nz),
                                     ptr(uz), stream_handle(stream)))
         return nz, uz
+
+
+class NativePsiformer(NativeFermiNet):
+    """A ``qmc_model`` handle for a Psiformer (+ SimpleEE Jastrow): the value
+    path (``forward``, ``mh_steps``, ``mh_steps_resident``, ``mh_draws``);
+    ``local_energy`` and ``grad`` raise QMC_ERR_UNSUPPORTED."""
+
+    def __init__(self, cfg, atoms, charges, precision="mixed", device=None):
+        self._open(device)
+        c = PsiformerConfigC()
+        c.n_up, c.n_down = int(cfg.nspins[0]), int(cfg.nspins[1])
+        atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 3))
+        charges = np.ascontiguousarray(np.asarray(charges, np.float32).reshape(-1))
+        c.n_atoms = atoms.shape[0]
+        c.ndets = int(cfg.ndets)
+        c.n_layers = int(cfg.num_layers)
+        c.n_heads = int(cfg.num_heads)
+        c.head_dim = int(cfg.heads_dim)
+        c.n_mlp = len(cfg.mlp_hidden_dims)
+        for k, v in enumerate(cfg.mlp_hidden_dims):
+            c.mlp_dims[k] = int(v)
+        c.envelope = ENVELOPE[str(cfg.envelope)]
+        c.orbitals_spin_split = int(bool(cfg.orbitals_spin_split))
+        c.jastrow = 1 if cfg.jastrow == "simple_ee" else 0
+        c.precision = PRECISION[precision]
+        h = C.c_void_p()
+        check(self.lib.qmc_psiformer_create(C.byref(c), atoms.ctypes.data, charges.ctypes.data, C.byref(h)))
+        self._finish(h, c.n_up + c.n_down, precision)
 
 
 KERNEL_CLASSES = ["stream_layer", "broadcast", "orbital", "logdet", "features", "means", "pair", "mh",

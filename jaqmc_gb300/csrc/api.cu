@@ -12,6 +12,7 @@
 #include "kernels.cuh"
 #include "profile.cuh"
 #include "plan.cuh"
+#include "psiformer.cuh"
 #include "stream_tc.cuh"
 
 // Launch `call` as a kernel of profiler class `cls` on stream `s`.
@@ -430,7 +431,7 @@ static bool env_in_lu(const Dims& d, const Plan& p) {
          p.h2[1] - p.h2[0] >= (size_t)p.B * d.K * d.n * d.n * sizeof(float);
 }
 
-static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
+qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
   const Dims& d = m->d;
   const ArenaLayout& a = m->a;
   const float* ar = m->arena;
@@ -477,22 +478,13 @@ static qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cu
   return QMC_OK;
 }
 
-// Full evaluation: features -> backbone -> orbitals -> determinants.
-qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
-                           float* logpsi, float* sign, float* ke, float* el, uint8_t* flags,
-                           cudaStream_t s) {
+// Determinant stage: LU (with the value-only envelope factors when the
+// orbital epilogue left them out), log-sum-exp, and for tangent passes the
+// kinetic and local energy.
+qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, float* logpsi, float* sign,
+                      float* ke, float* el, uint8_t* flags, cudaStream_t s) {
   const Dims& d = m->d;
   const float* ar = m->arena;
-  float* pe = want_pe ? at<float>(ws, p.pe) : nullptr;
-  const bool fused = pair_fused(d, p.T);
-  QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
-                           ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
-                           at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe,
-                           d.n_up, d.C, d.g2_p[0], fused ? at<float>(ws, p.g2) : nullptr));
-  int hb = 0;
-  if (p.mixed) QMC_TRY(run_backbone_mixed(m, p, ws, s, &hb));
-  else QMC_TRY(run_backbone_plain(m, p, ws, s, &hb));
-  QMC_TRY(run_orbitals(m, p, ws, hb, s));
   EnvArgs env{};
   if (env_in_lu(d, p)) {
     const int c1 = d.split ? 1 : 0;
@@ -507,10 +499,51 @@ qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electron
   return QMC_OK;
 }
 
+// Full evaluation: features -> backbone -> orbitals -> determinants.
+qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
+                           float* logpsi, float* sign, float* ke, float* el, uint8_t* flags,
+                           cudaStream_t s) {
+  if (m->kind != QMC_KIND_FERMINET) {
+    set_error("this entry point evaluates FermiNet models only");
+    return QMC_ERR_UNSUPPORTED;
+  }
+  const Dims& d = m->d;
+  const float* ar = m->arena;
+  float* pe = want_pe ? at<float>(ws, p.pe) : nullptr;
+  const bool fused = pair_fused(d, p.T);
+  QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
+                           ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
+                           at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe,
+                           d.n_up, d.C, d.g2_p[0], fused ? at<float>(ws, p.g2) : nullptr));
+  int hb = 0;
+  if (p.mixed) QMC_TRY(run_backbone_mixed(m, p, ws, s, &hb));
+  else QMC_TRY(run_backbone_plain(m, p, ws, s, &hb));
+  QMC_TRY(run_orbitals(m, p, ws, hb, s));
+  return run_logdet(m, p, ws, pe, logpsi, sign, ke, el, flags, s);
+}
+
 qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, int op) {
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1) { set_error("batch must be >= 1"); return QMC_ERR_SHAPE; }
+  if (m->kind == QMC_KIND_PSIFORMER) {
+    if (op != QMC_OP_FORWARD && op != QMC_OP_MH) {
+      set_error("Psiformer models support the value path only (forward, MH steps)");
+      return QMC_ERR_UNSUPPORTED;
+    }
+    const size_t need = psi_make_plan(m, batch).base.total;
+    if (!ws || ws_bytes < need) {
+      set_error("workspace too small: %zu bytes given, %zu needed", ws_bytes, need);
+      return QMC_ERR_WORKSPACE;
+    }
+    int dev;
+    QMC_CUDA(cudaGetDevice(&dev));
+    if (dev != m->device) {
+      set_error("model lives on device %d but device %d is current", m->device, dev);
+      return QMC_ERR_ARG;
+    }
+    return QMC_OK;
+  }
   if (m->precision == QMC_PRECISION_MIXED_BF16) {
     const Dims& d = m->d;
     for (int l = 1; l < d.L; ++l)
@@ -549,18 +582,24 @@ qmc_status mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t s
                     size_t ws_bytes, cudaStream_t s) {
   QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_MH));
   if (!electrons || !log_prob || steps < 0) { set_error("bad electrons/log_prob/steps"); return QMC_ERR_ARG; }
-  Plan p = make_plan(m, QMC_OP_MH, batch);
+  const bool psi = m->kind == QMC_KIND_PSIFORMER;
+  const PsiPlan pp = psi ? psi_make_plan(m, batch) : PsiPlan{};
+  const Plan p = psi ? pp.base : make_plan(m, QMC_OP_MH, batch);
+  auto forward = [&](const float* x, float* lp, uint8_t* fl) -> qmc_status {
+    if (psi) return psi_evaluate(m, pp, ws, x, lp, at<float>(ws, p.sgn), fl, s);
+    return evaluate(m, p, ws, x, false, lp, at<float>(ws, p.sgn), nullptr, nullptr, fl, s);
+  };
   const int n = m->d.n;
   float* lpsi = at<float>(ws, p.lpsi);
   // log_prob of the starting walkers (src/jaqmc/sampler/mcmc.py:166)
-  QMC_TRY(evaluate(m, p, ws, electrons, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, flags, s));
+  QMC_TRY(forward(electrons, lpsi, flags));
   QMC_PROF(QMC_KC_OTHER, launch_scale(s, batch, lpsi, 2.0f, log_prob));
   float* xp = at<float>(ws, p.xp);
   for (int st = 0; st < steps; ++st) {
     const float* nz = inj_normals ? inj_normals + (size_t)st * batch * n * 3 : nullptr;
     const float* uz = inj_uniforms ? inj_uniforms + (size_t)st * batch : nullptr;
     QMC_PROF(QMC_KC_MH, launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, ctr_dev, nz));
-    QMC_TRY(evaluate(m, p, ws, xp, false, lpsi, at<float>(ws, p.sgn), nullptr, nullptr, nullptr, s));
+    QMC_TRY(forward(xp, lpsi, nullptr));
     QMC_PROF(QMC_KC_MH, launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, ctr_dev,
                                          uz, accepts));
   }
@@ -644,6 +683,7 @@ qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atom
 
 qmc_status qmc_model_destroy(qmc_model* m) {
   if (!m) return QMC_OK;
+  delete m->psi;
   cudaFree(m->arena);
   cudaFree(m->arena_bf16);
   cudaFree(m->dev_err);
@@ -662,7 +702,10 @@ qmc_status qmc_model_check_error(qmc_model* m, int* code) {
   return QMC_OK;
 }
 
-size_t qmc_param_count(const qmc_model* m) { return m ? m->p.total : 0; }
+size_t qmc_param_count(const qmc_model* m) {
+  if (!m) return 0;
+  return m->kind == QMC_KIND_PSIFORMER ? m->psi->p.total : m->p.total;
+}
 
 qmc_status qmc_model_set_precision(qmc_model* m, int precision) {
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
@@ -676,6 +719,7 @@ qmc_status qmc_model_set_precision(qmc_model* m, int precision) {
 
 qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t s) {
   if (!m || !params) { set_error("null argument"); return QMC_ERR_ARG; }
+  if (m->kind == QMC_KIND_PSIFORMER) return psi_set_params(m, params, s);
   const Dims& d = m->d;
   const ArenaLayout& a = m->a;
   const ParamLayout& p = m->p;
@@ -736,6 +780,8 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
 
 size_t qmc_workspace_size(const qmc_model* m, int op, int batch) {
   if (!m || batch < 1) return 0;
+  if (m->kind == QMC_KIND_PSIFORMER)
+    return op == QMC_OP_FORWARD || op == QMC_OP_MH ? psi_make_plan(m, batch).base.total : 0;
   if (op == QMC_OP_GRAD) return grad_workspace(m, batch);
   return make_plan(m, op, batch).total;
 }
@@ -749,6 +795,10 @@ qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes) {
 qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                     double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
+  if (m->kind != QMC_KIND_FERMINET) {
+    set_error("the parameter adjoint is built for FermiNet models only");
+    return QMC_ERR_UNSUPPORTED;
+  }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1 || !electrons) { set_error("bad batch/electrons"); return QMC_ERR_ARG; }
   if (!per_walker && !grad) { set_error("nothing to compute: per_walker and grad are both null"); return QMC_ERR_ARG; }
@@ -761,6 +811,7 @@ qmc_status qmc_forward(qmc_model* m, int batch, const float* electrons, float* l
                        uint8_t* flags, void* ws, size_t ws_bytes, cudaStream_t s) {
   QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_FORWARD));
   if (!electrons || !logpsi) { set_error("null electrons/logpsi"); return QMC_ERR_ARG; }
+  if (m->kind == QMC_KIND_PSIFORMER) return psi_evaluate(m, psi_make_plan(m, batch), ws, electrons, logpsi, sign, flags, s);
   Plan p = make_plan(m, QMC_OP_FORWARD, batch);
   return evaluate(m, p, ws, electrons, false, logpsi, sign, nullptr, nullptr, flags, s);
 }
@@ -779,6 +830,7 @@ qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, flo
 
 int qmc_tangent_rows(const qmc_model* m, int op) {
   if (!m || op < QMC_OP_FORWARD || op > QMC_OP_GRAD) return -1;
+  if (m->kind == QMC_KIND_PSIFORMER) return op == QMC_OP_FORWARD || op == QMC_OP_MH ? 1 : -1;
   return make_plan(m, op, 1).Tp;
 }
 

@@ -91,7 +91,13 @@ struct ParamLayout {
 
 }  // namespace qmc
 
+namespace qmc {
+struct PsiModel;
+}
+
 struct qmc_model {
+  int kind = 0;                    // QMC_KIND_FERMINET or QMC_KIND_PSIFORMER
+  qmc::PsiModel* psi = nullptr;    // Psiformer dims and layouts (kind == PSIFORMER)
   qmc::Dims d;
   qmc::ArenaLayout a;
   qmc::ParamLayout p;

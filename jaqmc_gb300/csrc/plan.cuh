@@ -26,6 +26,12 @@ qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, 
 qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electrons, bool want_pe,
                     float* logpsi, float* sign, float* ke, float* el, uint8_t* flags, cudaStream_t s);
 
+// The orbital (x envelope) stage reading the backbone output in h1[hb], and the
+// determinant stage; shared by the FermiNet and Psiformer drivers.
+qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s);
+qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, float* logpsi, float* sign,
+                      float* ke, float* el, uint8_t* flags, cudaStream_t s);
+
 // Adjoint (adjoint.cu): workspace bytes for `batch` walkers under the model's
 // gradient budget, and the chunked forward + backward driver.
 size_t grad_workspace(const qmc_model* m, int batch);

@@ -1,0 +1,592 @@
+// Psiformer + SimpleEE Jastrow, value path: log|psi| of a walker batch and,
+// through the shared MH driver, the all-electron Metropolis-Hastings step.
+//
+//   features (rescaled ae features + spin)      k_psi_features
+//   x = Dense(features)                          GEMM + k_psi_row
+//   per layer (Pre-LN, backbone/psiformer.py:61-99):
+//     xn = LN0(x)                                (fused into the previous row kernel)
+//     qkv = xn Wqkv                              one GEMM, 3D outputs
+//     att = MHA(qkv + bqkv)                      k_psi_attention, one block per (walker, head)
+//     x += att Wo + bo ; xn = LN1(x)             GEMM + k_psi_row
+//     h = tanh(xn W_k + b_k) ... ; x += h        GEMMs + k_psi_row
+//   orbitals x envelope, LU, log-sum-exp         shared with FermiNet
+//   log|psi| += Jastrow                          k_psi_add
+//
+// GEMMs are plain stores: split-BF16 tcgen05 (mixed form) or FP32 SIMT; bias,
+// tanh, residual, LayerNorm and the operand format of the next GEMM are one
+// warp-per-row kernel.
+#include <algorithm>
+#include <cmath>
+#include <utility>
+
+#include "gemm_simt.cuh"
+#include "kernels.cuh"
+#include "profile.cuh"
+#include "psiformer.cuh"
+#include "stream_tc.cuh"
+
+#define QMC_PROF(cls, call)         \
+  do {                              \
+    ::qmc::ProfScope ps_((cls), s); \
+    QMC_CUDA(call);                 \
+  } while (0)
+#define QMC_PROF_TRY(cls, call)     \
+  do {                              \
+    ::qmc::ProfScope ps_((cls), s); \
+    QMC_TRY(call);                  \
+  } while (0)
+
+namespace qmc {
+
+template <typename T>
+static T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+
+// ------------------------------------------------------------------ kernels
+// One block (256 threads) per walker.  X0 row (w, i): per atom
+// [log(1+r), vec * log(1+r) / r] (src/jaqmc/wavefunction/input/atomic.py:58-66),
+// then the spin (+1 up, -1 down, backbone/psiformer.py:170-176), zeros up to
+// K0p.  rae / aevec feed the envelope.  jas[w] is the SimpleEE Jastrow
+// (src/jaqmc/wavefunction/jastrow.py:48-122), reduced in a fixed order.
+__global__ void __launch_bounds__(256) k_psi_features(int n, int n_up, int A, int K0p, const float* __restrict__ x,
+                                                      const float* __restrict__ atoms,
+                                                      const float* __restrict__ alpha, float* __restrict__ X0,
+                                                      float* __restrict__ rae, float* __restrict__ aevec,
+                                                      float* __restrict__ jas) {
+  __shared__ float red[256];
+  extern __shared__ float xs[];  // [n][3]
+  const int w = blockIdx.x;
+  for (int e = threadIdx.x; e < 3 * n; e += blockDim.x) xs[e] = x[(size_t)w * 3 * n + e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * K0p; e += blockDim.x) {
+    const int i = e / K0p, c = e % K0p;
+    float v = 0.f;
+    if (c < 4 * A) {
+      const int I = c >> 2, q = c & 3;
+      const float dx = xs[3 * i] - atoms[3 * I], dy = xs[3 * i + 1] - atoms[3 * I + 1],
+                  dz = xs[3 * i + 2] - atoms[3 * I + 2];
+      const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+      const float lr = log1pf(r);
+      v = q == 0 ? lr : (q == 1 ? dx : q == 2 ? dy : dz) * lr / r;
+    } else if (c == 4 * A) {
+      v = i < n_up ? 1.f : -1.f;
+    }
+    X0[((size_t)w * n + i) * K0p + c] = v;
+  }
+  for (int e = threadIdx.x; e < n * A; e += blockDim.x) {
+    const int i = e / A, I = e % A;
+    const float dx = xs[3 * i] - atoms[3 * I], dy = xs[3 * i + 1] - atoms[3 * I + 1],
+                dz = xs[3 * i + 2] - atoms[3 * I + 2];
+    const size_t o = (size_t)w * n * A + e;
+    rae[o] = sqrtf(dx * dx + dy * dy + dz * dz);
+    aevec[3 * o] = dx;
+    aevec[3 * o + 1] = dy;
+    aevec[3 * o + 2] = dz;
+  }
+  float acc = 0.f;
+  if (alpha) {
+    const float ap = alpha[0], aa = alpha[1];
+    for (int p = threadIdx.x; p < n * n; p += blockDim.x) {
+      const int i = p / n, j = p % n;
+      if (j <= i) continue;
+      const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
+      const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+      const bool same = (i < n_up) == (j < n_up);
+      acc += same ? -(0.25f * ap * ap) / (ap + r) : -(0.5f * aa * aa) / (aa + r);
+    }
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) jas[w] = red[0];
+}
+
+// One warp per row of D <= 512 features (multiple of 32):
+//   v = z + bias; v = tanh(v) if act; v += x if resid; x = v if write_x;
+//   out = LayerNorm(v) (eps 1e-5, biased two-pass variance) if ln_s, else v.
+template <class Out>
+__global__ void k_psi_row(int rows, int D, const float* __restrict__ z, int ldz, const float* __restrict__ bias,
+                          int act, float* __restrict__ x, int resid, int write_x, const float* __restrict__ ln_s,
+                          const float* __restrict__ ln_b, Out out) {
+  constexpr int kMax = 16;
+  const int lane = threadIdx.x & 31;
+  const size_t row = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= (size_t)rows) return;
+  const int per = D >> 5;
+  float v[kMax];
+  float sum = 0.f;
+#pragma unroll
+  for (int k = 0; k < kMax; ++k) {
+    if (k < per) {
+      const int f = lane + 32 * k;
+      float t = z[row * ldz + f] + bias[f];
+      if (act) t = tanhf(t);
+      if (resid) t += x[row * D + f];
+      if (write_x) x[row * D + f] = t;
+      v[k] = t;
+      sum += t;
+    }
+  }
+  if (!ln_s) {
+#pragma unroll
+    for (int k = 0; k < kMax; ++k)
+      if (k < per) out.put(row, lane + 32 * k, v[k]);
+    return;
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  const float mean = sum / (float)D;
+  float sq = 0.f;
+#pragma unroll
+  for (int k = 0; k < kMax; ++k)
+    if (k < per) sq += (v[k] - mean) * (v[k] - mean);
+  for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  const float inv = rsqrtf(sq / (float)D + 1e-5f);
+#pragma unroll
+  for (int k = 0; k < kMax; ++k) {
+    if (k < per) {
+      const int f = lane + 32 * k;
+      out.put(row, f, (v[k] - mean) * inv * ln_s[f] + ln_b[f]);
+    }
+  }
+}
+
+// Multi-head dot-product attention of one (walker, head) per block
+// (flax MultiHeadDotProductAttention semantics, backbone/psiformer.py:74-81):
+// q, k, v = projections + biases, q / sqrt(Dh), softmax over keys, o = p v.
+template <class Out>
+__global__ void k_psi_attention(int n, int H, int Dh, const float* __restrict__ qkv, const float* __restrict__ bqkv,
+                                Out out) {
+  extern __shared__ float sa[];
+  const int ld = Dh + 1, lds = n + 1;
+  float* Q = sa;
+  float* Kt = Q + n * ld;
+  float* V = Kt + n * ld;
+  float* S = V + n * ld;
+  const int w = blockIdx.x / H, h = blockIdx.x % H;
+  const int D = H * Dh;
+  const float scale = 1.0f / sqrtf((float)Dh);
+  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
+    const int i = e / Dh, d = e % Dh;
+    const float* r = qkv + ((size_t)w * n + i) * 3 * D + h * Dh + d;
+    const int c = h * Dh + d;
+    Q[i * ld + d] = (r[0] + bqkv[c]) * scale;
+    Kt[i * ld + d] = r[D] + bqkv[D + c];
+    V[i * ld + d] = r[2 * D] + bqkv[2 * D + c];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    float acc = 0.f;
+    for (int d = 0; d < Dh; ++d) acc = fmaf(Q[i * ld + d], Kt[j * ld + d], acc);
+    S[i * lds + j] = acc;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int i = threadIdx.x >> 5; i < n; i += nw) {
+    float mx = -INFINITY;
+    for (int j = lane; j < n; j += 32) mx = fmaxf(mx, S[i * lds + j]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    float sum = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      const float e = expf(S[i * lds + j] - mx);
+      S[i * lds + j] = e;
+      sum += e;
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    const float inv = 1.0f / sum;
+    for (int j = lane; j < n; j += 32) S[i * lds + j] *= inv;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
+    const int i = e / Dh, d = e % Dh;
+    float acc = 0.f;
+    for (int j = 0; j < n; ++j) acc = fmaf(S[i * lds + j], V[j * ld + d], acc);
+    out.put((size_t)w * n + i, h * Dh + d, acc);
+  }
+}
+
+__global__ void k_psi_add(int B, float* __restrict__ lp, const float* __restrict__ jas) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < B) lp[w] += jas[w];
+}
+
+static size_t attention_smem(int n, int Dh) { return sizeof(float) * ((size_t)3 * n * (Dh + 1) + (size_t)n * (n + 1)); }
+
+// ------------------------------------------------------------------ host side
+PsiPlan psi_make_plan(const qmc_model* m, int B) {
+  const PsiDims& d = m->psi->d;
+  PsiPlan pp{};
+  Plan& p = pp.base;
+  p.B = B;
+  p.T = 1;
+  p.Tp = 1;
+  p.P2 = 1;
+  p.K0p = d.K0p;
+  p.mixed = m->precision == QMC_PRECISION_MIXED_BF16;
+  p.act_bytes = 4;
+  const size_t rows = (size_t)B * d.n;
+  int W = d.D;
+  for (int k = 0; k < d.n_dense; ++k) W = std::max(W, d.mlp[k]);
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes, 256); return r; };
+  p.x0 = take(rows * d.K0p * 4);
+  p.h1[0] = p.h1[1] = take(rows * d.D * 4);
+  p.h1_plane = rows * d.D;
+  const size_t env = (size_t)B * d.K * d.n * d.n * 4;
+  p.h2[0] = take(env);  // envelope factors of the value-only LU path
+  p.h2[1] = p.g1 = p.gb = p.g2 = o;
+  p.rae = take(rows * d.A * 4);
+  p.aevec = take(rows * d.A * 12);
+  p.amat = take(env);
+  p.pe = take((size_t)B * 4);
+  p.lpsi = take((size_t)B * 4);
+  p.sgn = take((size_t)B * 4);
+  p.xp = take(rows * 12);
+  p.lp = take((size_t)B * 4);
+  p.refac = take(16);
+  pp.x = take(rows * d.D * 4);
+  pp.in_plane = rows * W;
+  pp.xn = take(rows * W * 4);
+  pp.att = take(rows * W * 4);
+  pp.z = take(rows * std::max(3 * d.D, W) * 4);
+  pp.jas = take((size_t)B * 4);
+  p.dmax = d.D;
+  p.total = o;
+  return pp;
+}
+
+// z[rows][n_out] = X[rows][k] W[k][n_out] (X: GEMM-input buffer at `xoff`)
+static qmc_status psi_gemm(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s, size_t xoff, int k,
+                           size_t w_f32, size_t t_bf16, int n_out) {
+  const int rows = pp.base.B * m->psi->d.n;
+  float* z = at<float>(ws, pp.z);
+  if (pp.base.mixed) {
+    TcStoreArgs a{rows, at<__nv_bfloat16>(ws, xoff), k, pp.in_plane, m->arena_bf16 + t_bf16, n_out, z, m->dev_err};
+    QMC_PROF_TRY(QMC_KC_STREAM_LAYER, tc_store_gemm(s, a));
+  } else {
+    const RowMap map{1, 0, 1, 1};
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, rows, map, at<float>(ws, xoff), k, k, nullptr, 0, 0,
+                                                   m->arena + w_f32, n_out, n_out, EpiStore{z, n_out, nullptr}));
+  }
+  return QMC_OK;
+}
+
+template <class Out>
+static cudaError_t launch_row(cudaStream_t s, int rows, int D, const float* z, int ldz, const float* bias, int act,
+                              float* x, int resid, int write_x, const float* ln_s, const float* ln_b, Out out) {
+  const int wpb = 8;
+  k_psi_row<Out><<<(unsigned)((rows + wpb - 1) / wpb), 32 * wpb, 0, s>>>(rows, D, z, ldz, bias, act, x, resid,
+                                                                        write_x, ln_s, ln_b, out);
+  return cudaGetLastError();
+}
+
+template <class Out>
+static cudaError_t launch_attention(cudaStream_t s, int B, int n, int H, int Dh, const float* qkv,
+                                    const float* bqkv, Out out) {
+  const size_t sm = attention_smem(n, Dh);
+  static int attr_dev = -1;
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (sm > 48 * 1024 && attr_dev != dev) {
+    e = cudaFuncSetAttribute(k_psi_attention<Out>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_dev = dev;
+  }
+  k_psi_attention<Out><<<(unsigned)(B * H), 256, sm, s>>>(n, H, Dh, qkv, bqkv, out);
+  return cudaGetLastError();
+}
+
+template <class Out>
+static qmc_status psi_backbone(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s,
+                               Out (*fmt)(void*, const PsiPlan&, size_t, int)) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const float* ar = m->arena;
+  const int B = pp.base.B, rows = B * d.n, D = d.D;
+  float* x = at<float>(ws, pp.x);
+  float* z = at<float>(ws, pp.z);
+  // input Dense (FP32 SIMT in both forms: K = 4A + 1 is small)
+  {
+    const RowMap map{1, 0, 1, 1};
+    QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, rows, map, at<float>(ws, pp.base.x0), d.K0p, d.K0p, nullptr, 0, 0,
+                                             ar + a.w_in, D, D, EpiStore{z, D, nullptr}));
+  }
+  QMC_PROF(QMC_KC_LAYER0, launch_row(s, rows, D, z, D, ar + P.in_b, 0, x, 0, 1, ar + P.ln0_s[0], ar + P.ln0_b[0],
+                                     fmt(ws, pp, pp.xn, D)));
+  for (int l = 0; l < d.L; ++l) {
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, a.w_qkv[l], a.t_qkv[l], 3 * D));
+    QMC_PROF(QMC_KC_PAIR, launch_attention(s, B, d.n, d.H, d.Dh, z, ar + a.b_qkv[l], fmt(ws, pp, pp.att, D)));
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.att, D, P.o_k[l], a.t_o[l], D));
+    QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, D, z, D, ar + P.o_b[l], 0, x, 1, 1, ar + P.ln1_s[l], ar + P.ln1_b[l],
+                                      fmt(ws, pp, pp.xn, D)));
+    size_t in = pp.xn, other = pp.att;
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      const int dout = d.mlp[k];
+      QMC_TRY(psi_gemm(m, pp, ws, s, in, din, P.mlp_k[l][k], a.t_mlp[l][k], dout));
+      if (k + 1 < d.n_dense) {
+        QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, dout, z, dout, ar + P.mlp_b[l][k], 1, x, 0, 0, nullptr, nullptr,
+                                          fmt(ws, pp, other, dout)));
+        std::swap(in, other);
+        din = dout;
+      } else if (l + 1 < d.L) {
+        QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, D, z, D, ar + P.mlp_b[l][k], 1, x, 1, 1, ar + P.ln0_s[l + 1],
+                                          ar + P.ln0_b[l + 1], fmt(ws, pp, pp.xn, D)));
+      } else {  // backbone output, in the orbital GEMM's operand format
+        QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, D, z, D, ar + P.mlp_b[l][k], 1, x, 1, 1, nullptr, nullptr,
+                                          fmt(ws, pp, pp.base.h1[0], D)));
+      }
+    }
+  }
+  return QMC_OK;
+}
+
+static StSplit fmt_split(void* ws, const PsiPlan& pp, size_t off, int ld) {
+  return StSplit{at<__nv_bfloat16>(ws, off), ld, off == pp.base.h1[0] ? pp.base.h1_plane : pp.in_plane};
+}
+static StF32 fmt_f32(void* ws, const PsiPlan&, size_t off, int ld) { return StF32{at<float>(ws, off), ld}; }
+
+qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* electrons, float* logpsi,
+                        float* sign, uint8_t* flags, cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const Plan& p = pp.base;
+  const size_t sm = sizeof(float) * 3 * d.n;
+  QMC_PROF(QMC_KC_FEATURES,
+           (k_psi_features<<<p.B, 256, sm, s>>>(d.n, d.n_up, d.A, d.K0p, electrons, m->arena + m->a.atoms,
+                                                d.jastrow ? m->arena + P.alpha_par : nullptr, at<float>(ws, p.x0),
+                                                at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, pp.jas)),
+            cudaGetLastError()));
+  if (p.mixed) QMC_TRY(psi_backbone<StSplit>(m, pp, ws, s, fmt_split));
+  else QMC_TRY(psi_backbone<StF32>(m, pp, ws, s, fmt_f32));
+  QMC_TRY(run_orbitals(m, p, ws, 0, s));
+  QMC_TRY(run_logdet(m, p, ws, nullptr, logpsi, sign, nullptr, nullptr, flags, s));
+  QMC_PROF(QMC_KC_OTHER, (k_psi_add<<<(p.B + 255) / 256, 256, 0, s>>>(p.B, logpsi, at<float>(ws, pp.jas)),
+                          cudaGetLastError()));
+  return QMC_OK;
+}
+
+qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const ArenaLayout& oa = m->a;
+  float* ar = m->arena;
+  __nv_bfloat16* ab = m->arena_bf16;
+  const int D = d.D;
+  QMC_CUDA(cudaMemcpyAsync(ar, params, P.total * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  // input kernel [K0][D] zero-padded to [K0p][D]
+  QMC_CUDA(cudaMemsetAsync(ar + a.w_in, 0, sizeof(float) * d.K0p * D, s));
+  QMC_CUDA(cudaMemcpyAsync(ar + a.w_in, params + P.in_k, sizeof(float) * d.K0 * D, cudaMemcpyDeviceToDevice, s));
+  for (int l = 0; l < d.L; ++l) {
+    const size_t src[3] = {P.q_k[l], P.k_k[l], P.v_k[l]}, bsrc[3] = {P.q_b[l], P.k_b[l], P.v_b[l]};
+    for (int c = 0; c < 3; ++c) {
+      QMC_CUDA(cudaMemcpy2DAsync(ar + a.w_qkv[l] + (size_t)c * D, sizeof(float) * 3 * D, params + src[c],
+                                 sizeof(float) * D, sizeof(float) * D, D, cudaMemcpyDeviceToDevice, s));
+      QMC_CUDA(cudaMemcpyAsync(ar + a.b_qkv[l] + (size_t)c * D, params + bsrc[c], sizeof(float) * D,
+                               cudaMemcpyDeviceToDevice, s));
+    }
+    QMC_CUDA(launch_transpose_split(s, ar + a.w_qkv[l], D, 3 * D, 3 * D, ab + a.t_qkv[l], D, 3 * D));
+    QMC_CUDA(launch_transpose_split(s, ar + P.o_k[l], D, D, D, ab + a.t_o[l], D, D));
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      QMC_CUDA(launch_transpose_split(s, ar + P.mlp_k[l][k], din, d.mlp[k], d.mlp[k], ab + a.t_mlp[l][k], din,
+                                      d.mlp[k]));
+      din = d.mlp[k];
+    }
+  }
+  const int nch = d.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    QMC_CUDA(cudaMemsetAsync(ar + oa.w_orb[c], 0, sizeof(float) * D * m->d.norb_p, s));
+    QMC_CUDA(cudaMemcpy2DAsync(ar + oa.w_orb[c], sizeof(float) * m->d.norb_p, params + P.orb_k[c],
+                               sizeof(float) * m->d.norb, sizeof(float) * m->d.norb, D, cudaMemcpyDeviceToDevice,
+                               s));
+    QMC_CUDA(cudaMemcpyAsync(ar + oa.env_pi[c], params + P.env_pi[c], sizeof(float) * d.n * d.A * d.K,
+                             cudaMemcpyDeviceToDevice, s));
+    QMC_CUDA(cudaMemcpyAsync(ar + oa.env_sigma[c], params + P.env_sigma[c], sizeof(float) * d.n * d.A * d.K,
+                             cudaMemcpyDeviceToDevice, s));
+    QMC_CUDA(launch_transpose_split(s, ar + oa.w_orb[c], D, m->d.norb, m->d.norb_p, ab + oa.t_orb[c], D,
+                                    m->d.norb));
+  }
+  m->params_set = true;
+  return QMC_OK;
+}
+
+}  // namespace qmc
+
+using namespace qmc;
+
+extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, const float* atoms_host,
+                                           const float* charges_host, qmc_model** out) {
+  if (!cfg || !atoms_host || !charges_host || !out) {
+    set_error("null argument");
+    return QMC_ERR_ARG;
+  }
+  *out = nullptr;
+  const int n = cfg->n_up + cfg->n_down, A = cfg->n_atoms;
+  if (cfg->n_up < 0 || cfg->n_down < 0 || n < 1 || n > 64 || A < 1 || A > kMaxAtoms || cfg->ndets < 1 ||
+      cfg->n_layers < 1 || cfg->n_layers > kPsiMaxLayers || cfg->n_heads < 1 || cfg->head_dim < 1 ||
+      cfg->n_mlp < 0 || cfg->n_mlp > kPsiMaxMlp) {
+    set_error("psiformer: bad sizes (n=%d atoms=%d layers=%d mlp=%d)", n, A, cfg->n_layers, cfg->n_mlp);
+    return QMC_ERR_SHAPE;
+  }
+  const int D = cfg->n_heads * cfg->head_dim;
+  bool widths_ok = D % 64 == 0 && D <= 512;
+  for (int k = 0; k < cfg->n_mlp; ++k) widths_ok = widths_ok && cfg->mlp_dims[k] % 64 == 0 && cfg->mlp_dims[k] <= 512;
+  if (!widths_ok) {
+    set_error("psiformer: attention and MLP widths must be multiples of 64, at most 512");
+    return QMC_ERR_UNSUPPORTED;
+  }
+  if (attention_smem(n, cfg->head_dim) > 200 * 1024) {
+    set_error("psiformer: %d electrons x head width %d exceed the attention kernel's shared memory", n,
+              cfg->head_dim);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  if (cfg->precision != QMC_PRECISION_FP32 && cfg->precision != QMC_PRECISION_MIXED_BF16) {
+    set_error("unknown precision %d", cfg->precision);
+    return QMC_ERR_ARG;
+  }
+  qmc_model* m = new qmc_model();
+  m->kind = QMC_KIND_PSIFORMER;
+  m->psi = new PsiModel();
+  PsiDims& d = m->psi->d;
+  d.n = n;
+  d.n_up = cfg->n_up;
+  d.n_dn = cfg->n_down;
+  d.A = A;
+  d.K = cfg->ndets;
+  d.L = cfg->n_layers;
+  d.H = cfg->n_heads;
+  d.Dh = cfg->head_dim;
+  d.D = D;
+  d.n_dense = cfg->n_mlp + 1;
+  for (int k = 0; k < cfg->n_mlp; ++k) d.mlp[k] = cfg->mlp_dims[k];
+  d.mlp[cfg->n_mlp] = D;
+  d.split = cfg->orbitals_spin_split && cfg->n_up > 0 && cfg->n_down > 0;
+  d.env_abs = cfg->envelope == QMC_ENVELOPE_ABS_ISOTROPIC;
+  d.jastrow = cfg->jastrow != 0;
+  d.K0 = 4 * A + 1;
+  d.K0p = (d.K0 + 7) / 8 * 8;  // the SIMT GEMM walks K in steps of 8
+  // flat parameter offsets (reference leaf order)
+  PsiParams& P = m->psi->p;
+  size_t o = 0;
+  auto take = [&](size_t count) { size_t r = o; o += count; return r; };
+  P.in_k = take((size_t)d.K0 * D);
+  P.in_b = take(D);
+  for (int l = 0; l < d.L; ++l) {
+    P.ln0_s[l] = take(D);
+    P.ln0_b[l] = take(D);
+    P.q_k[l] = take((size_t)D * D);
+    P.q_b[l] = take(D);
+    P.k_k[l] = take((size_t)D * D);
+    P.k_b[l] = take(D);
+    P.v_k[l] = take((size_t)D * D);
+    P.v_b[l] = take(D);
+    P.o_k[l] = take((size_t)D * D);
+    P.o_b[l] = take(D);
+    P.ln1_s[l] = take(D);
+    P.ln1_b[l] = take(D);
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      P.mlp_k[l][k] = take((size_t)din * d.mlp[k]);
+      P.mlp_b[l][k] = take(d.mlp[k]);
+      din = d.mlp[k];
+    }
+  }
+  const int nch = d.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) P.orb_k[c] = take((size_t)D * d.K * n);
+  for (int c = 0; c < nch; ++c) {
+    P.env_pi[c] = take((size_t)n * A * d.K);
+    P.env_sigma[c] = take((size_t)n * A * d.K);
+  }
+  if (nch == 1) {
+    P.orb_k[1] = P.orb_k[0];
+    P.env_pi[1] = P.env_pi[0];
+    P.env_sigma[1] = P.env_sigma[0];
+  }
+  if (d.jastrow) {
+    P.alpha_par = take(1);
+    P.alpha_anti = take(1);
+  }
+  P.total = o;
+  // arena: verbatim params, then derived fp32 parameters, each block 64-byte
+  // aligned (vector loads and TMA need 16-byte aligned bases)
+  PsiArena& a = m->psi->a;
+  o = align_up(P.total, 64);
+  auto takea = [&](size_t count) { size_t r = o; o += align_up(count, 16); return r; };
+  a.w_in = takea((size_t)d.K0p * D);
+  for (int l = 0; l < d.L; ++l) {
+    a.w_qkv[l] = takea((size_t)D * 3 * D);
+    a.b_qkv[l] = takea((size_t)3 * D);
+  }
+  // FermiNet-shared orbital / envelope fields of the model
+  Dims& fd = m->d;
+  fd.n = n;
+  fd.n_up = d.n_up;
+  fd.n_dn = d.n_dn;
+  fd.A = A;
+  fd.K = d.K;
+  fd.L = 0;
+  fd.C = (d.n_up > 0) + (d.n_dn > 0);
+  fd.split = d.split;
+  fd.env_abs = d.env_abs;
+  fd.d_last = D;
+  fd.norb = d.K * n;
+  fd.norb_p = align_up(fd.norb, 8);
+  ArenaLayout& fa = m->a;
+  for (int c = 0; c < 2; ++c) {
+    if (c < nch) {
+      fa.w_orb[c] = takea((size_t)D * fd.norb_p);
+      fa.env_pi[c] = takea((size_t)n * A * d.K);
+      fa.env_sigma[c] = takea((size_t)n * A * d.K);
+    } else {
+      fa.w_orb[1] = fa.w_orb[0];
+      fa.env_pi[1] = fa.env_pi[0];
+      fa.env_sigma[1] = fa.env_sigma[0];
+    }
+  }
+  fa.atoms = takea((size_t)3 * A);
+  fa.charges = takea(A);
+  a.total = fa.total = o;
+  size_t ob = 0;
+  auto takeb = [&](size_t count) { size_t r = ob; ob += align_up(count, 64); return r; };
+  for (int l = 0; l < d.L; ++l) {
+    a.t_qkv[l] = takeb((size_t)2 * D * 3 * D);
+    a.t_o[l] = takeb((size_t)2 * D * D);
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      a.t_mlp[l][k] = takeb((size_t)2 * din * d.mlp[k]);
+      din = d.mlp[k];
+    }
+  }
+  for (int c = 0; c < 2; ++c) fa.t_orb[c] = c < nch ? takeb((size_t)2 * fd.norb_p * D) : fa.t_orb[0];
+  a.total_bf16 = fa.total_bf16 = ob;
+  m->precision = cfg->precision;
+  cudaError_t e = cudaGetDevice(&m->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->n_sms, cudaDevAttrMultiProcessorCount, m->device);
+  if (e == cudaSuccess) e = cudaMalloc(&m->arena, fa.total * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->arena_bf16, fa.total_bf16 * sizeof(__nv_bfloat16));
+  if (e == cudaSuccess) e = cudaMalloc(&m->dev_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m->dev_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m->arena, 0, fa.total * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(m->arena_bf16, 0, fa.total_bf16 * sizeof(__nv_bfloat16));
+  memcpy(m->atoms_host, atoms_host, sizeof(float) * 3 * A);
+  memcpy(m->charges_host, charges_host, sizeof(float) * A);
+  if (e == cudaSuccess) e = cudaMemcpy(m->arena + fa.atoms, atoms_host, sizeof(float) * 3 * A, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->arena + fa.charges, charges_host, sizeof(float) * A, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(m->arena);
+    cudaFree(m->arena_bf16);
+    cudaFree(m->dev_err);
+    delete m->psi;
+    delete m;
+    return cuda_status(e, "qmc_psiformer_create");
+  }
+  *out = m;
+  return QMC_OK;
+}

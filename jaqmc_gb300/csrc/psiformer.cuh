@@ -1,0 +1,72 @@
+// Psiformer + SimpleEE Jastrow (value path): layouts shared by psiformer.cu
+// and the entry points of api.cu.
+#pragma once
+#include "common.cuh"
+#include "plan.cuh"
+
+namespace qmc {
+
+constexpr int kPsiMaxLayers = 8;
+constexpr int kPsiMaxMlp = 4;  // hidden MLP widths per layer (plus the final one back to D)
+
+struct PsiDims {
+  int n, n_up, n_dn, A, K;
+  int L, H, Dh, D;                // layers, heads, head width, attention width H*Dh
+  int n_dense;                    // MLP dense layers per block (hidden widths + 1)
+  int mlp[kPsiMaxMlp + 1];        // output widths of the MLP dense layers (last = D)
+  int split, env_abs, jastrow;
+  int K0, K0p;                    // 4A + 1 input features, padded to a multiple of 8
+};
+
+// Offsets (floats) of each leaf in the flat parameter vector (reference leaf
+// order of PsiformerWavefunction); the arena starts with a verbatim copy.
+struct PsiParams {
+  size_t in_k, in_b;
+  size_t ln0_s[kPsiMaxLayers], ln0_b[kPsiMaxLayers];
+  size_t q_k[kPsiMaxLayers], q_b[kPsiMaxLayers], k_k[kPsiMaxLayers], k_b[kPsiMaxLayers];
+  size_t v_k[kPsiMaxLayers], v_b[kPsiMaxLayers], o_k[kPsiMaxLayers], o_b[kPsiMaxLayers];
+  size_t ln1_s[kPsiMaxLayers], ln1_b[kPsiMaxLayers];
+  size_t mlp_k[kPsiMaxLayers][kPsiMaxMlp + 1], mlp_b[kPsiMaxLayers][kPsiMaxMlp + 1];
+  size_t orb_k[2], env_pi[2], env_sigma[2];
+  size_t alpha_par, alpha_anti;
+  size_t total;
+};
+
+// Derived parameters after the verbatim copy (float offsets into the arena)
+// and the split-bf16 K-major copies of the GEMM weights (bf16 offsets).
+struct PsiArena {
+  size_t w_in;                    // [K0p][D] input kernel, zero rows past K0
+  size_t w_qkv[kPsiMaxLayers];    // [D][3D]: query | key | value kernels side by side
+  size_t b_qkv[kPsiMaxLayers];    // [3D]
+  size_t total;
+  size_t t_qkv[kPsiMaxLayers];    // [3D][D]
+  size_t t_o[kPsiMaxLayers];      // [D][D]
+  size_t t_mlp[kPsiMaxLayers][kPsiMaxMlp + 1];
+  size_t total_bf16;
+};
+
+struct PsiModel {
+  PsiDims d;
+  PsiParams p;
+  PsiArena a;
+};
+
+// Workspace of a Psiformer value pass: the shared fields of Plan (orbital
+// matrices, envelope scratch, MH buffers, the backbone output in h1[0]) plus
+// the backbone's own buffers.
+struct PsiPlan {
+  Plan base;
+  size_t x;     // [rows][D] f32 residual stream
+  size_t xn;    // [rows][D] GEMM input (f32, or two bf16 planes)
+  size_t z;     // [rows][max(3D, mlp)] f32 GEMM output
+  size_t att;   // [rows][D] attention output, GEMM input
+  size_t jas;   // [B] Jastrow
+  size_t in_plane;  // bf16 elements between planes of xn / att / h1[0]
+};
+
+PsiPlan psi_make_plan(const qmc_model* m, int B);
+qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* electrons, float* logpsi,
+                        float* sign, uint8_t* flags, cudaStream_t s);
+qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s);
+
+}  // namespace qmc

@@ -1,0 +1,115 @@
+"""Psiformer + SimpleEE Jastrow value path on the GPU against the FP64 oracle
+(oracle/psiformer.py) on the same parameters, walkers and draws: sign exact,
+log|psi| within 1e-5 relative (FP32 form) / 1e-3 relative (split-BF16 form),
+MH accept masks bit-exact away from near ties, the antiparallel cusp 1/2, and
+the ops the value path does not provide."""
+import numpy as np
+import pytest
+import torch
+
+from jaqmc_gb300 import _native
+from jaqmc_gb300 import params as P
+from jaqmc_gb300 import systems as S
+from oracle import mcmc as OM
+from oracle import psiformer as OP
+
+pytestmark = pytest.mark.gpu
+
+
+def _ocfg(cfg):
+    return OP.PsiformerConfig(nspins=cfg.nspins, ndets=cfg.ndets, num_layers=cfg.num_layers,
+                              num_heads=cfg.num_heads, heads_dim=cfg.heads_dim,
+                              mlp_hidden_dims=list(cfg.mlp_hidden_dims), envelope=cfg.envelope,
+                              orbitals_spin_split=cfg.orbitals_spin_split, jastrow=cfg.jastrow)
+
+
+def _setup(mol, cfg, B, dev, precision, seed=0):
+    tree = P.init_psiformer(cfg, mol.n_atoms, seed=seed)
+    flat = P.flatten(tree, P.psiformer_leaves(cfg, mol.n_atoms))
+    m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision=precision, device=dev)
+    assert m.param_count == flat.size
+    m.set_params(torch.as_tensor(flat, device=dev))
+    x = S.init_walkers(mol, B, seed=1)
+    return m, tree, x
+
+
+SMALL = dict(ndets=3, num_layers=2, num_heads=4, heads_dim=16, mlp_hidden_dims=[64])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("mixed", 1e-3)])
+@pytest.mark.parametrize("system", ["Li", "CH4"])
+def test_forward_matches_oracle(system, precision, tol, cuda_device):
+    mol = S.SYSTEMS[system]()
+    cfg = P.PsiformerConfig(nspins=mol.nspins, **SMALL)
+    m, tree, x = _setup(mol, cfg, 32, cuda_device, precision)
+    lp, sg, fl = m.forward(torch.as_tensor(x, device=cuda_device))
+    ref = OP.evaluate(tree, _ocfg(cfg), torch.as_tensor(x, dtype=torch.float64), mol.atoms)
+    rel = np.abs(lp.cpu().numpy() - ref["logpsi"].numpy()) / np.maximum(1.0, np.abs(ref["logpsi"].numpy()))
+    assert np.array_equal(sg.cpu().numpy(), ref["sign_logpsi"].numpy())
+    assert rel.max() < tol, rel.max()
+
+
+def test_benzene_full_config(cuda_device):
+    """The benzene configuration: 21+21 electrons, 12 atoms, 4 layers of 4 x 64
+    heads, MLP 256, K = 16, split-BF16 GEMMs."""
+    mol = S.benzene()
+    cfg = P.PsiformerConfig(nspins=mol.nspins)
+    m, tree, x = _setup(mol, cfg, 8, cuda_device, "mixed")
+    lp, sg, fl = m.forward(torch.as_tensor(x, device=cuda_device))
+    ref = OP.evaluate(tree, _ocfg(cfg), torch.as_tensor(x, dtype=torch.float64), mol.atoms)
+    rel = np.abs(lp.cpu().numpy() - ref["logpsi"].numpy()) / np.abs(ref["logpsi"].numpy())
+    assert np.array_equal(sg.cpu().numpy(), ref["sign_logpsi"].numpy())
+    assert rel.max() < 1e-3, rel
+    assert m.check_error() == 0
+
+
+def test_mh_matches_oracle(cuda_device):
+    mol = S.lithium()
+    cfg = P.PsiformerConfig(nspins=mol.nspins, **SMALL)
+    B, steps = 64, 3
+    m, tree, x = _setup(mol, cfg, B, cuda_device, "fp32")
+    nz, uz = m.mh_draws(B, steps, seed=4, counter=0)
+    xg = torch.as_tensor(x, device=cuda_device).clone()
+    _, lpg, accg, _ = m.mh_steps(xg, steps, 0.05, 4, 0)
+    f = OP.logpsi_fn(tree, _ocfg(cfg), torch.as_tensor(mol.atoms, dtype=torch.float64))
+    xo, lpo, acco, ratios = OM.mh_steps(f, torch.as_tensor(x, dtype=torch.float64), nz.cpu().double(),
+                                        uz.cpu().double(), 0.05)
+    near = ((ratios - torch.log(uz.cpu().double())).abs() < 1e-4).any(0).numpy()
+    keep = ~near
+    assert keep.sum() >= B - 2
+    assert np.array_equal(accg.cpu().numpy()[keep], acco.numpy()[keep])
+    np.testing.assert_allclose(lpg.cpu().numpy()[keep], lpo.numpy()[keep], rtol=1e-4, atol=1e-4)
+
+
+def test_antiparallel_cusp_on_gpu(cuda_device):
+    """Central differences of the GPU log|psi| along the up-down separation at
+    r = 0.01 bohr average to the cusp value 1/2 (+-0.1), as in
+    tests/wavefunction/molecule_wavefunction_test.py:538-607."""
+    mol = S.make_molecule("He", [2], [[0.0, 0.0, 0.0]], (1, 1))
+    cfg = P.PsiformerConfig(nspins=(1, 1), ndets=4, num_layers=1, num_heads=4, heads_dim=16, mlp_hidden_dims=[64])
+    m, tree, _ = _setup(mol, cfg, 1, cuda_device, "fp32")
+    g = torch.Generator().manual_seed(3)
+    d = torch.randn(200, 3, generator=g, dtype=torch.float64)
+    d = d / d.norm(dim=1, keepdim=True)
+    center = torch.tensor([2.0, 0.0, 0.0], dtype=torch.float64)
+    h, r = 2e-3, 0.01
+
+    def at(dist):
+        x = torch.zeros(200, 2, 3, dtype=torch.float64)
+        x[:, 0] = center
+        x[:, 1] = center + dist * d
+        return m.forward(x.float().to(cuda_device).contiguous())[0].double().cpu()
+    radial = (at(r + h) - at(r - h)) / (2 * h)
+    assert float(radial.mean()) == pytest.approx(0.5, abs=0.1)
+
+
+def test_value_path_only(cuda_device):
+    mol = S.lithium()
+    cfg = P.PsiformerConfig(nspins=mol.nspins, **SMALL)
+    m, _, x = _setup(mol, cfg, 4, cuda_device, "mixed")
+    xd = torch.as_tensor(x, device=cuda_device)
+    with pytest.raises(_native.QmcError, match="UNSUPPORTED"):
+        m.local_energy(xd)
+    with pytest.raises(_native.QmcError, match="UNSUPPORTED"):
+        m.grad(xd, weights=torch.ones(4, dtype=torch.float64, device=cuda_device))
+    assert m.tangent_rows(_native.OP_LOCAL_ENERGY) == -1
