@@ -36,6 +36,7 @@ WORKLOADS = {
     "N2": dict(system="N2", nspins=(7, 7), walkers=4096, mh_steps=20),
     "Li": dict(system="Li", nspins=(2, 1), walkers=1024, mh_steps=10),
     "CH4": dict(system="CH4", nspins=(5, 5), walkers=4096, mh_steps=20),
+    "C6H6": dict(system="C6H6", nspins=(21, 21), walkers=4096, mh_steps=10, model="psiformer"),
 }
 
 
@@ -200,6 +201,68 @@ def run_reference(args, wl):
 def workload_name(wl, prec):
     return (f"{wl['system']} FermiNet 4x(256,32) K=16, {wl['walkers']} walkers, "
             f"{wl['mh_steps']} MH steps + forward-Laplacian E_L, {prec}")
+
+
+# ----------------------------------------------------------------- Psiformer
+def psiformer_forward_flops(cfg, n, A):
+    """Dense FLOPs of one Psiformer log|psi| per walker: input layer, per layer
+    QKV / output / MLP GEMMs and the two attention contractions, orbitals."""
+    D, L = cfg.dim, cfg.num_layers
+    mlp = list(cfg.mlp_hidden_dims) + [D]
+    per_row = (4 * A + 1) * D
+    layer = 3 * D * D + D * D
+    din = D
+    for dout in mlp:
+        layer += din * dout
+        din = dout
+    per_row += L * layer + D * cfg.ndets * n
+    attn = L * 2 * n * n * D
+    return 2 * (n * per_row + attn)
+
+
+def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10):
+    """Benzene Psiformer (4 layers, 4 x 64 heads, MLP 256, K = 16, SimpleEE
+    Jastrow), split-BF16 GEMMs: walker-steps/s of ``mh_steps`` MH updates."""
+    import torch
+
+    from jaqmc_gb300 import _native
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+    mol = S.benzene()
+    cfg = P.PsiformerConfig(nspins=mol.nspins)
+    flat = torch.as_tensor(P.flatten(P.init_psiformer(cfg, mol.n_atoms, seed=0),
+                                     P.psiformer_leaves(cfg, mol.n_atoms)), device=dev)
+    m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision="mixed", device=dev)
+    m.set_params(flat)
+    x = torch.as_tensor(S.init_walkers(mol, walkers, seed=1), device=dev)
+    for k in range(warmup):
+        m.mh_steps(x, mh_steps, 0.02, 2, k * mh_steps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(steps):
+        m.mh_steps(x, mh_steps, 0.02, 2, (warmup + k) * mh_steps)
+    e1.record()
+    torch.cuda.synchronize()
+    assert m.check_error() == 0
+    ms = e0.elapsed_time(e1) / steps
+    _native.profile_enable(True)
+    _native.profile_read()
+    m.mh_steps(x, mh_steps, 0.02, 2, (warmup + steps) * mh_steps)
+    prof = _native.profile_read()
+    _native.profile_enable(False)
+    names = {"stream_layer": "gemm", "pair": "attention", "means": "bias_act_residual_layernorm",
+             "layer0": "input_layer", "orbital": "orbital", "logdet": "logdet", "features": "features_jastrow",
+             "mh": "mh", "other": "other", "broadcast": "broadcast"}
+    flops = psiformer_forward_flops(cfg, mol.n_electrons, mol.n_atoms) * walkers * (mh_steps + 1)
+    pk, kind = peaks()
+    return {"workload": f"C6H6 Psiformer 4x(4x64), MLP 256, K=16, SimpleEE Jastrow, {walkers} walkers, "
+                        f"{mh_steps} MH steps, split-BF16",
+            "walker_steps_per_s": walkers * mh_steps / (ms / 1e3), "ms_per_call": ms,
+            "tflops": flops / (ms / 1e3) / 1e12,
+            "frac_of_bf16_sustained": flops / (ms / 1e3) / 1e12 / pk["bf16_tflops_sustained"],
+            "kernel_ms_per_call": {names.get(k, k): v[1] for k, v in prof.items() if v[0]},
+            "local_energy": "not built (value path only)"}
 
 
 # ----------------------------------------------------------------- serving
@@ -401,6 +464,9 @@ def run_ours(args, wl):
     _native.profile_enable(False)
     Tp_fl = models[prec_main].tangent_rows(_native.OP_LOCAL_ENERGY)
     rl, rl_t = fl_layer_roofline(cfg, mol, B, Tp_fl, prec_main, prof_el, pk, pk_kind)
+    psi = None
+    if not args.no_psiformer:
+        psi = run_psiformer(dev, max(1, args.steps // 2), 1)
     serve = None
     if not args.no_serve:
         serve = run_serving(dev, args.serve_rate, args.serve_jobs, args.serve_requests, slots=args.serve_slots)
@@ -430,6 +496,7 @@ def run_ours(args, wl):
             "roofline": rl,
             "roofline_tensor": rl_t,
             "serving": serve,
+            "psiformer": psi,
             "cpu_baseline": cpu,
             "clocks": clk,
         }
@@ -498,6 +565,7 @@ def main():
     ap.add_argument("--oracle-walkers", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-psiformer", action="store_true")
     ap.add_argument("--walkers", type=int, default=None, help="override the workload's walker count")
     ap.add_argument("--request-only", action="store_true",
                     help="only W warm-up + K timed requests of --precision (for profiler runs)")
@@ -520,8 +588,18 @@ def main():
     wl = dict(WORKLOADS[args.workload])
     if args.walkers:
         wl["walkers"] = args.walkers
+    if args.request_only and wl.get("model") == "psiformer":
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_psiformer(torch.device("cuda", 0), args.steps, args.warmup, walkers=wl["walkers"],
+                                       mh_steps=wl["mh_steps"])), flush=True)
+        return 0
     if args.request_only:
         return run_request_only(args, wl)
+    if wl.get("model") == "psiformer":
+        print("the Psiformer workload runs with --request-only (MH only: its local energy is not built)",
+              file=sys.stderr)
+        return 2
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -431,6 +431,17 @@ static bool env_in_lu(const Dims& d, const Plan& p) {
          p.h2[1] - p.h2[0] >= (size_t)p.B * d.K * d.n * d.n * sizeof(float);
 }
 
+// Where the value-only mixed passes apply the envelope: 1 = factors from
+// launch_envelope_value multiplied in by the register LU (n <= 32), 2 = raw
+// orbitals multiplied in place by launch_envelope_apply before the LU;
+// 0 = inside the orbital epilogue (FP32 form and tangent passes).
+static int env_mode(const Dims& d, const Plan& p) {
+  if (!p.mixed || p.T != 1) return 0;
+  if (env_in_lu(d, p)) return 1;
+  const bool fits = (size_t)4 * (2 * (d.split ? 2 : 1) * d.A * d.n + d.n * d.A) <= 48 * 1024;
+  return d.n <= 64 && fits ? 2 : 0;
+}
+
 qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
   const Dims& d = m->d;
   const ArenaLayout& a = m->a;
@@ -460,7 +471,7 @@ qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStrea
     oa.rae = at<float>(ws, p.rae);
     oa.aevec = at<float>(ws, p.aevec);
     oa.A = at<float>(ws, p.amat);
-    oa.raw = env_in_lu(d, p);
+    oa.raw = env_mode(d, p) != 0;
     oa.err = m->dev_err;
     QMC_PROF_TRY(QMC_KC_ORBITAL, tc_orbitals(s, oa));
     return QMC_OK;
@@ -486,16 +497,22 @@ qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, fl
   const Dims& d = m->d;
   const float* ar = m->arena;
   EnvArgs env{};
-  if (env_in_lu(d, p)) {
-    const int c1 = d.split ? 1 : 0;
+  const int mode = env_mode(d, p);
+  const int c1 = d.split ? 1 : 0;
+  if (mode == 1) {
     env.env = at<float>(ws, p.h2[0]);
     QMC_PROF(QMC_KC_ORBITAL, launch_envelope_value(s, p.B, d.n, d.n_up, d.split, d.K, d.A, d.env_abs,
                                                    ar + m->a.env_pi[0], ar + m->a.env_sigma[0],
                                                    ar + m->a.env_pi[c1], ar + m->a.env_sigma[c1],
                                                    at<float>(ws, p.rae), const_cast<float*>(env.env)));
+  } else if (mode == 2) {
+    QMC_PROF(QMC_KC_ORBITAL, launch_envelope_apply(s, p.B, d.n, d.n_up, d.split, d.K, d.A, d.env_abs,
+                                                   ar + m->a.env_pi[0], ar + m->a.env_sigma[0],
+                                                   ar + m->a.env_pi[c1], ar + m->a.env_sigma[c1],
+                                                   at<float>(ws, p.rae), at<float>(ws, p.amat)));
   }
   QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
-                                        flags, nullptr, env_in_lu(d, p) ? &env : nullptr));
+                                        flags, nullptr, mode == 1 ? &env : nullptr));
   return QMC_OK;
 }
 

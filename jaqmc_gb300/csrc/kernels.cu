@@ -183,6 +183,51 @@ cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int sp
   return cudaGetLastError();
 }
 
+// The same factors multiplied into raw value-only orbital matrices in place:
+// one block per (walker, determinant k), the parameters of k staged as
+// [channel][I][j] and the walker's electron-atom distances in shared memory.
+__global__ void k_envelope_apply(int n, int n_up, int split, int K, int A, int env_abs,
+                                 const float* __restrict__ pi0, const float* __restrict__ sg0,
+                                 const float* __restrict__ pi1, const float* __restrict__ sg1,
+                                 const float* __restrict__ rae, float* __restrict__ Amat) {
+  extern __shared__ float sha[];
+  const int nch = split ? 2 : 1, per = A * n;
+  float* ps = sha;                  // [nch][A][n]
+  float* ss = ps + nch * per;       // [nch][A][n]
+  float* ra = ss + nch * per;       // [n][A]
+  const int w = blockIdx.x / K, k = blockIdx.x % K;
+  for (int e = threadIdx.x; e < nch * per; e += blockDim.x) {
+    const int c = e / per, I = (e / n) % A, j = e % n;
+    const size_t q = ((size_t)j * A + I) * K + k;
+    ps[e] = (c ? pi1 : pi0)[q];
+    const float sv = (c ? sg1 : sg0)[q];
+    ss[e] = env_abs ? fabsf(sv) : sv;
+  }
+  for (int e = threadIdx.x; e < n * A; e += blockDim.x) ra[e] = rae[(size_t)w * n * A + e];
+  __syncthreads();
+  float* Am = Amat + ((size_t)w * K + k) * n * n;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    const int c = split && i >= n_up ? 1 : 0;
+    float acc = 0.f;
+    for (int I = 0; I < A; ++I) {
+      const int o = (c * A + I) * n + j;
+      acc += ps[o] * expf(-ss[o] * ra[i * A + I]);
+    }
+    Am[e] *= acc;
+  }
+}
+
+cudaError_t launch_envelope_apply(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
+                                  const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                  const float* rae, float* Amat) {
+  const size_t sm = sizeof(float) * ((size_t)2 * (split ? 2 : 1) * A * n + (size_t)n * A);
+  if (sm > 48 * 1024) return cudaErrorNotSupported;
+  k_envelope_apply<<<(unsigned)((size_t)B * K), 256, sm, s>>>(n, n_up, split, K, A, env_abs, pi0, sg0, pi1, sg1,
+                                                               rae, Amat);
+  return cudaGetLastError();
+}
+
 // =====================================================================
 // two-electron layer (src/jaqmc/wavefunction/backbone/ferminet.py:55-63)
 // rows p: 0 value, 1 Laplacian wrt the pair difference, 2..4 its gradient.
@@ -1091,7 +1136,7 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
   float* sgs = reinterpret_cast<float*>(lds + nmat);       // [nmat]
   int* redo = reinterpret_cast<int*>(sgs + nmat);          // [nmat] re-factorise flags
   int* singular = redo + nmat;                             // [nmat]
-  char* scratch = reinterpret_cast<char*>(shv) + align_up((size_t)nmat * 16 + 16, 16);
+  char* scratch = reinterpret_cast<char*>(shv) + align_up((size_t)nmat * 20, 16);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / SEG, i = lane % SEG;
   const unsigned seg_mask = (SEG == 32) ? 0xffffffffu : (((1u << SEG) - 1u) << (sub * SEG));
@@ -1230,7 +1275,7 @@ static cudaError_t launch_logdet_value(cudaStream_t s, int B, int n, int K, floa
   const int seg = n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32;
   const int per_pass = 8 * (32 / seg);
   const int WB = std::max(1, per_pass / K);
-  const size_t sm = align_up((size_t)WB * K * 16 + 16, 16) + DetScratch(n).bytes;
+  const size_t sm = align_up((size_t)WB * K * 20, 16) + DetScratch(n).bytes;
   const unsigned grid = (unsigned)((B + WB - 1) / WB);
   switch (seg) {
     case 4: k_logdet_value<4><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags, env); break;
@@ -1241,10 +1286,113 @@ static cudaError_t launch_logdet_value(cudaStream_t s, int B, int n, int K, floa
   return cudaGetLastError();
 }
 
+// Value-only determinants for 32 < n <= 64: one block per walker, one warp
+// per matrix at a time, FP32 LU in shared memory (warp_lu, partial pivoting),
+// matrices with pivot growth above the threshold re-factorised in FP64 by
+// warp 0, then the FP64 signed log-sum-exp.  Shared memory holds one FP32
+// matrix per warp, so blocks stay small (the tangent kernel k_logdet sizes
+// its scratch for the FP64 inverse and products).
+constexpr int kLuWarps = 8;
+__global__ void __launch_bounds__(kLuWarps * 32) k_logdet_value_smem(int n, int K, const float* __restrict__ A,
+                                                                     float* __restrict__ logpsi,
+                                                                     float* __restrict__ sign,
+                                                                     uint8_t* __restrict__ flags) {
+  extern __shared__ double sml[];
+  const int ld = (n + 3) / 4 * 4;
+  double* lds = sml;                                         // [K]
+  float* sgs = reinterpret_cast<float*>(lds + K);            // [K]
+  int* redo = reinterpret_cast<int*>(sgs + K);               // [K]
+  int* sing = redo + K;                                      // [K]
+  char* base = reinterpret_cast<char*>(sml) + align_up((size_t)K * 20, 16);  // lds, sgs, redo, sing
+  const size_t per_warp = align_up((size_t)n * ld * 4 + (size_t)n * 4, 16);
+  const int w = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* LU = reinterpret_cast<float*>(base + per_warp * warp);
+  int* perm = reinterpret_cast<int*>(LU + (size_t)n * ld);
+  for (int k = warp; k < K; k += kLuWarps) {
+    const float* Ak = A + ((size_t)w * K + k) * n * n;
+    for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = Ak[e];
+    __syncwarp();
+    double la, growth;
+    float sg;
+    int sgl = 0;
+    warp_lu<float>(LU, n, ld, perm, &la, &sg, &growth, &sgl);
+    if (lane == 0) {
+      lds[k] = sgl ? -INFINITY : la;
+      sgs[k] = sgl ? 0.f : sg;
+      sing[k] = sgl;
+      redo[k] = (!sgl && !(growth <= (double)kRefactorGrowth)) ? 1 : 0;
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  double* LU64 = reinterpret_cast<double*>(base + per_warp * kLuWarps);
+  int* perm64 = reinterpret_cast<int*>(LU64 + (size_t)n * ld);
+  for (int k = 0; k < K; ++k) {
+    if (!redo[k]) continue;
+    const float* Ak = A + ((size_t)w * K + k) * n * n;
+    for (int e = lane; e < n * n; e += 32) LU64[(e / n) * ld + (e % n)] = (double)Ak[e];
+    __syncwarp();
+    double la, growth;
+    float sg;
+    int sgl = 0;
+    warp_lu<double>(LU64, n, ld, perm64, &la, &sg, &growth, &sgl);
+    if (lane == 0) {
+      lds[k] = sgl ? -INFINITY : la;
+      sgs[k] = sgl ? 0.f : sg;
+      sing[k] = sgl;
+    }
+    __syncwarp();
+  }
+  double lmax = -INFINITY;
+  int anyredo = 0, anysing = 0;
+  for (int k = lane; k < K; k += 32) {
+    if (sgs[k] != 0.f) lmax = fmax(lmax, lds[k]);
+    anyredo |= redo[k];
+    anysing |= sing[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  double S = 0.0;
+  for (int k = lane; k < K; k += 32)
+    if (sgs[k] != 0.f) S += (double)sgs[k] * exp(lds[k] - lmax);
+  S = warp_sum(S);
+  anyredo = __any_sync(0xffffffffu, anyredo);
+  anysing = __any_sync(0xffffffffu, anysing);
+  if (lane == 0) {
+    const double lp = log(fabs(S)) + lmax;
+    if (logpsi) logpsi[w] = (float)lp;
+    if (sign) sign[w] = S > 0 ? 1.f : (S < 0 ? -1.f : 0.f);
+    if (flags)
+      flags[w] = (isfinite(lp) ? 0 : QMC_FLAG_NONFINITE) | (anyredo ? QMC_FLAG_REFACTOR : 0) |
+                 (anysing ? QMC_FLAG_SINGULAR : 0);
+  }
+}
+
+static cudaError_t launch_logdet_value_smem(cudaStream_t s, int B, int n, int K, const float* A, float* logpsi,
+                                            float* sign, uint8_t* flags) {
+  const size_t ld = (n + 3) / 4 * 4;
+  const size_t per_warp = align_up((size_t)n * ld * 4 + (size_t)n * 4, 16);
+  const size_t sm = align_up((size_t)K * 20, 16) + per_warp * kLuWarps + (size_t)n * ld * 8 + (size_t)n * 4;
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  static int attr_dev = -1;
+  int dev;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (attr_dev != dev) {
+    e = cudaFuncSetAttribute(k_logdet_value_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_dev = dev;
+  }
+  k_logdet_value_smem<<<B, kLuWarps * 32, sm, s>>>(n, K, A, logpsi, sign, flags);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor, const EnvArgs* env) {
   if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, const_cast<float*>(A), logpsi, sign, flags, env);
+  if (T == 1 && n <= 64 && !env) return launch_logdet_value_smem(s, B, n, K, A, logpsi, sign, flags);
   if (env) return cudaErrorInvalidValue;  // tangent passes take enveloped matrices
   const int D = T > 1 ? T - 2 : 0;
   const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);

@@ -11,6 +11,10 @@ namespace qmc {
 struct EnvArgs {
   const float* env;  // [B][K][n][n]
 };
+// Multiply raw value-only orbital matrices [w][k][i][j] by their envelopes in place.
+cudaError_t launch_envelope_apply(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
+                                  const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                  const float* rae, float* Amat);
 // Envelopes [w][k][i][j] of the value-only orbital matrices.
 cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,

@@ -161,6 +161,50 @@ class FermiNetWavefunction:
 
 
 @dataclass
+class PsiformerWavefunction(FermiNetWavefunction):
+    """Psiformer ansatz with the SimpleEE Jastrow (hyper-parameters and
+    defaults of ``src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94``),
+    evaluated by the GB300 library: log|psi| and the MH sampler.  Its local
+    energy is not provided by the library (value path only)."""
+
+    num_layers: int = 4
+    num_heads: int = 4
+    heads_dim: int = 64
+    mlp_hidden_dims: list = field(default_factory=lambda: [256])
+    jastrow: str = "simple_ee"
+    jastrow_alpha_init: float = 1.0
+    precision: str = "mixed"
+
+    @property
+    def config(self) -> P.PsiformerConfig:
+        return P.PsiformerConfig(nspins=tuple(self.nspins), ndets=self.ndets, num_layers=self.num_layers,
+                                 num_heads=self.num_heads, heads_dim=self.heads_dim,
+                                 mlp_hidden_dims=list(self.mlp_hidden_dims), envelope=self.envelope,
+                                 orbitals_spin_split=self.orbitals_spin_split, jastrow=self.jastrow,
+                                 jastrow_alpha_init=self.jastrow_alpha_init)
+
+    def init_params(self, data: MoleculeData, rngs=0) -> DeviceParams:
+        seed = int(rngs) if np.isscalar(rngs) else int(np.asarray(rngs).ravel()[0])
+        A = np.asarray(data.atoms, np.float64).reshape(-1, 3).shape[0]
+        tree = P.init_psiformer(self.config, A, seed=seed)
+        return DeviceParams(tree, P.psiformer_leaves(self.config, A), self._dev())
+
+    def model(self, data: MoleculeData, params: DeviceParams) -> _native.NativePsiformer:
+        atoms = np.asarray(torch.as_tensor(data.atoms).cpu(), np.float32).reshape(-1, 3)
+        charges = np.asarray(torch.as_tensor(data.charges).cpu(), np.float32).reshape(-1)
+        key = (atoms.tobytes(), charges.tobytes(), self.precision)
+        m = self._models.get(key)
+        if m is None:
+            m = _native.NativePsiformer(self.config, atoms, charges, precision=self.precision, device=self._dev())
+            self._models[key] = m
+        stamp = (id(params), params.version)
+        if self._loaded.get(key) != stamp:
+            m.set_params(params.flat)
+            self._loaded[key] = stamp
+        return m
+
+
+@dataclass
 class BoundLogProb:
     """``x -> 2 log|psi(x)|`` bound to a wavefunction, parameters and system."""
 

@@ -113,3 +113,19 @@ def test_value_path_only(cuda_device):
     with pytest.raises(_native.QmcError, match="UNSUPPORTED"):
         m.grad(xd, weights=torch.ones(4, dtype=torch.float64, device=cuda_device))
     assert m.tangent_rows(_native.OP_LOCAL_ENERGY) == -1
+
+
+def test_host_mirror_sampler(cuda_device):
+    """PsiformerWavefunction + MCMCSampler of the host mirror: the sampler
+    moves walkers with a sane acceptance rate and log|psi| stays finite."""
+    from jaqmc_gb300 import vmc
+    mol = S.lithium()
+    wf = vmc.PsiformerWavefunction(nspins=mol.nspins, **SMALL)
+    x = torch.as_tensor(S.init_walkers(mol, 256, seed=1), device=cuda_device)
+    data = vmc.MoleculeData(x, mol.atoms, mol.charges)
+    params = wf.init_params(data, 0)
+    sampler = vmc.MCMCSampler(steps=10, initial_width=0.1)
+    state = sampler.init(data, 3)
+    d, stats, state = sampler.step(wf.batch_log_prob(params, data), data, state)
+    assert 0.05 < stats["pmove"] < 1.0
+    assert torch.isfinite(wf.logpsi(params, d)).all()
