@@ -155,32 +155,79 @@ __global__ void k_psi_row(int rows, int D, const float* __restrict__ z, int ldz,
 // Multi-head dot-product attention of one (walker, head) per block
 // (flax MultiHeadDotProductAttention semantics, backbone/psiformer.py:74-81):
 // q, k, v = projections + biases, q / sqrt(Dh), softmax over keys, o = p v.
+// Scores and outputs are computed in 2 x 4 register tiles from 16-byte shared
+// loads.  A thread's four keys (and its two query rows) are strided, so the
+// eight lanes of a 16-byte access phase read consecutive rows and distinct
+// banks.  Rows past n are zero.
+struct AttnShape {
+  int n, Dh, n2, np, ld, lds;
+  __host__ __device__ AttnShape(int n_, int Dh_) : n(n_), Dh(Dh_) {
+    n2 = (n + 1) / 2 * 2;  // query rows padded to pairs
+    np = (n + 3) / 4 * 4;  // key / value rows padded to quads
+    ld = Dh + 4;           // row stride (16-byte aligned rows)
+    lds = np + 1;          // score row stride
+  }
+  __host__ __device__ size_t floats() const {
+    return (size_t)(n2 + 2 * np) * ld + (size_t)n2 * lds;
+  }
+};
+
 template <class Out>
-__global__ void k_psi_attention(int n, int H, int Dh, const float* __restrict__ qkv, const float* __restrict__ bqkv,
-                                Out out) {
-  extern __shared__ float sa[];
-  const int ld = Dh + 1, lds = n + 1;
+__global__ void __launch_bounds__(128) k_psi_attention(int n, int H, int Dh, const float* __restrict__ qkv,
+                                                       const float* __restrict__ bqkv, Out out) {
+  extern __shared__ __align__(16) float sa[];
+  const AttnShape sh(n, Dh);
+  const int ld = sh.ld, lds = sh.lds, n2 = sh.n2, np = sh.np;
   float* Q = sa;
-  float* Kt = Q + n * ld;
-  float* V = Kt + n * ld;
-  float* S = V + n * ld;
+  float* Kt = Q + (size_t)n2 * ld;
+  float* V = Kt + (size_t)np * ld;
+  float* S = V + (size_t)np * ld;
   const int w = blockIdx.x / H, h = blockIdx.x % H;
   const int D = H * Dh;
   const float scale = 1.0f / sqrtf((float)Dh);
-  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
-    const int i = e / Dh, d = e % Dh;
-    const float* r = qkv + ((size_t)w * n + i) * 3 * D + h * Dh + d;
-    const int c = h * Dh + d;
-    Q[i * ld + d] = (r[0] + bqkv[c]) * scale;
-    Kt[i * ld + d] = r[D] + bqkv[D + c];
-    V[i * ld + d] = r[2 * D] + bqkv[2 * D + c];
+  // 16-byte loads of q, k, v (Dh, D and the row strides are multiples of 4)
+  const int dq = Dh / 4;
+#pragma unroll 2
+  for (int e = threadIdx.x; e < np * dq; e += blockDim.x) {
+    const int i = e / dq, d = 4 * (e % dq);
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f), k = q, v = q;
+    if (i < n) {
+      const float* r = qkv + ((size_t)w * n + i) * 3 * D + h * Dh + d;
+      const int c = h * Dh + d;
+      const float4 rq = *reinterpret_cast<const float4*>(r), rk = *reinterpret_cast<const float4*>(r + D),
+                   rv = *reinterpret_cast<const float4*>(r + 2 * D);
+      const float4 bq = *reinterpret_cast<const float4*>(bqkv + c),
+                   bk = *reinterpret_cast<const float4*>(bqkv + D + c),
+                   bv = *reinterpret_cast<const float4*>(bqkv + 2 * D + c);
+      q = make_float4((rq.x + bq.x) * scale, (rq.y + bq.y) * scale, (rq.z + bq.z) * scale, (rq.w + bq.w) * scale);
+      k = make_float4(rk.x + bk.x, rk.y + bk.y, rk.z + bk.z, rk.w + bk.w);
+      v = make_float4(rv.x + bv.x, rv.y + bv.y, rv.z + bv.z, rv.w + bv.w);
+    }
+    if (i < n2) *reinterpret_cast<float4*>(Q + i * ld + d) = q;
+    *reinterpret_cast<float4*>(Kt + i * ld + d) = k;
+    *reinterpret_cast<float4*>(V + i * ld + d) = v;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    const int i = e / n, j = e % n;
-    float acc = 0.f;
-    for (int d = 0; d < Dh; ++d) acc = fmaf(Q[i * ld + d], Kt[j * ld + d], acc);
-    S[i * lds + j] = acc;
+  // scores: thread (ti, tj) -> rows {ti, ti + n2/2} x keys {tj + c * np/4}
+  const int hi = n2 / 2, hj = np / 4;
+  for (int t = threadIdx.x; t < hi * hj; t += blockDim.x) {
+    const int ti = t / hj, tj = t % hj;
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    for (int d = 0; d < Dh; d += 4) {
+      const float4 q0 = *reinterpret_cast<const float4*>(Q + ti * ld + d);
+      const float4 q1 = *reinterpret_cast<const float4*>(Q + (ti + hi) * ld + d);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float4 kk = *reinterpret_cast<const float4*>(Kt + (tj + c * hj) * ld + d);
+        acc[0][c] = fmaf(q0.x, kk.x, fmaf(q0.y, kk.y, fmaf(q0.z, kk.z, fmaf(q0.w, kk.w, acc[0][c]))));
+        acc[1][c] = fmaf(q1.x, kk.x, fmaf(q1.y, kk.y, fmaf(q1.z, kk.z, fmaf(q1.w, kk.w, acc[1][c]))));
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      S[ti * lds + tj + c * hj] = acc[0][c];
+      S[(ti + hi) * lds + tj + c * hj] = acc[1][c];
+    }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -199,11 +246,30 @@ __global__ void k_psi_attention(int n, int H, int Dh, const float* __restrict__ 
     for (int j = lane; j < n; j += 32) S[i * lds + j] *= inv;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
-    const int i = e / Dh, d = e % Dh;
-    float acc = 0.f;
-    for (int j = 0; j < n; ++j) acc = fmaf(S[i * lds + j], V[j * ld + d], acc);
-    out.put((size_t)w * n + i, h * Dh + d, acc);
+  // outputs: thread (ti, td) -> rows {ti, ti + n2/2} x features 4 td .. 4 td + 3
+  const int hd = Dh / 4;
+  for (int t = threadIdx.x; t < hi * hd; t += blockDim.x) {
+    const int ti = t / hd, d0 = 4 * (t % hd);
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    for (int j = 0; j < n; ++j) {
+      const float p0 = S[ti * lds + j], p1 = S[(ti + hi) * lds + j];
+      const float4 v = *reinterpret_cast<const float4*>(V + j * ld + d0);
+      acc[0][0] = fmaf(p0, v.x, acc[0][0]);
+      acc[0][1] = fmaf(p0, v.y, acc[0][1]);
+      acc[0][2] = fmaf(p0, v.z, acc[0][2]);
+      acc[0][3] = fmaf(p0, v.w, acc[0][3]);
+      acc[1][0] = fmaf(p1, v.x, acc[1][0]);
+      acc[1][1] = fmaf(p1, v.y, acc[1][1]);
+      acc[1][2] = fmaf(p1, v.z, acc[1][2]);
+      acc[1][3] = fmaf(p1, v.w, acc[1][3]);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      const int i = ti + a * hi;
+      if (i < n)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) out.put((size_t)w * n + i, h * Dh + d0 + c, acc[a][c]);
+    }
   }
 }
 
@@ -212,7 +278,7 @@ __global__ void k_psi_add(int B, float* __restrict__ lp, const float* __restrict
   if (w < B) lp[w] += jas[w];
 }
 
-static size_t attention_smem(int n, int Dh) { return sizeof(float) * ((size_t)3 * n * (Dh + 1) + (size_t)n * (n + 1)); }
+static size_t attention_smem(int n, int Dh) { return sizeof(float) * AttnShape(n, Dh).floats(); }
 
 // ------------------------------------------------------------------ host side
 PsiPlan psi_make_plan(const qmc_model* m, int B) {
@@ -295,7 +361,7 @@ static cudaError_t launch_attention(cudaStream_t s, int B, int n, int H, int Dh,
     if (e != cudaSuccess) return e;
     attr_dev = dev;
   }
-  k_psi_attention<Out><<<(unsigned)(B * H), 256, sm, s>>>(n, H, Dh, qkv, bqkv, out);
+  k_psi_attention<Out><<<(unsigned)(B * H), 128, sm, s>>>(n, H, Dh, qkv, bqkv, out);
   return cudaGetLastError();
 }
 
@@ -435,10 +501,10 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
     return QMC_ERR_SHAPE;
   }
   const int D = cfg->n_heads * cfg->head_dim;
-  bool widths_ok = D % 64 == 0 && D <= 512;
+  bool widths_ok = D % 64 == 0 && D <= 512 && cfg->head_dim % 4 == 0;
   for (int k = 0; k < cfg->n_mlp; ++k) widths_ok = widths_ok && cfg->mlp_dims[k] % 64 == 0 && cfg->mlp_dims[k] <= 512;
   if (!widths_ok) {
-    set_error("psiformer: attention and MLP widths must be multiples of 64, at most 512");
+    set_error("psiformer: attention and MLP widths must be multiples of 64 (at most 512), head width a multiple of 4");
     return QMC_ERR_UNSUPPORTED;
   }
   if (attention_smem(n, cfg->head_dim) > 200 * 1024) {
