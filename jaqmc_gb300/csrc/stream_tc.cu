@@ -266,12 +266,12 @@ struct ContigTiles {
 // the current chunk is computed, outputs replace the residual in place, and a
 // chunk leaves with 16-byte stores per plane.  No barrier is wider than the
 // warp.  Tangent rows past T come out as zeros (their inputs are zero rows).
+template <bool RESID>
 struct EpiTcLayer : ContigTiles {
   static constexpr int kCR = 16;                 // rows per chunk
   static constexpr int kBuf = 2 * kCR * 32;      // bf16 per chunk buffer
   int n, ld;  // electrons per walker, activation row width (n_out)
   StSplit resid, out;
-  bool has_resid;
   const float* Gb;
   const float* bias;
 
@@ -320,13 +320,13 @@ struct EpiTcLayer : ContigTiles {
     if (g.T == 1) {
       int c0 = 16 * half, k = 0;
       if (c0 >= ti.ng) return;
-      if (has_resid) fetch(resid, (size_t)(ti.g0 + c0), min(16, ti.ng - c0), col0, nvec, lane, buf0);
+      if (RESID) fetch(resid, (size_t)(ti.g0 + c0), min(16, ti.ng - c0), col0, nvec, lane, buf0);
       for (; c0 < ti.ng; c0 += 32, k ^= 1) {
         __nv_bfloat16* buf = buf0 + k * kBuf;
         const int nrows = min(16, ti.ng - c0);
         const size_t row0 = (size_t)(ti.g0 + c0);
         const bool more = c0 + 32 < ti.ng;
-        if (has_resid && more)
+        if (RESID && more)
           fetch(resid, row0 + 32, min(16, ti.ng - c0 - 32), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
         uint32_t r[16];
         ptx::tmem_ld16_nw(taddr + c0, r);
@@ -348,7 +348,7 @@ struct EpiTcLayer : ContigTiles {
         for (int j = 0; j < 16; ++j) {
           if (j < nrows) {
             float y = tanhf(__uint_as_float(r[j]) + gbv[j] + b);
-            if (has_resid) y = (y + get(buf, j, lane)) * kRsqrt2;
+            if (RESID) y = (y + get(buf, j, lane)) * kRsqrt2;
             put(buf, j, lane, y);
           }
         }
@@ -364,62 +364,80 @@ struct EpiTcLayer : ContigTiles {
       const size_t r0 = (size_t)gi * Tp;
       const uint32_t tcol = taddr + (uint32_t)(lg * Tp);
       const float* gb = Gb + (size_t)(gi / n) * Tp * N + fc;
-      if (has_resid) fetch(resid, r0, min(16, Tp), col0, nvec, lane, buf0);
-      float h = 0.f, d1 = 0.f, zL = 0.f, S = 0.f, res1 = 0.f;
+      if (RESID) fetch(resid, r0, min(16, Tp), col0, nvec, lane, buf0);
+      FlState st{};
       int k = 0;
       for (int t0 = 0; t0 < Tp; t0 += 16, k ^= 1) {
         __nv_bfloat16* buf = buf0 + k * kBuf;
         const int cs = min(16, Tp - t0);  // a multiple of 4, uniform
         const bool more = t0 + 16 < Tp;
-        if (has_resid && more) fetch(resid, r0 + t0 + 16, min(16, Tp - t0 - 16), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
-        uint32_t r[16];
-        if (cs == 16) {
-          ptx::tmem_ld16_nw(tcol + t0, r);
+        if (RESID && more) fetch(resid, r0 + t0 + 16, min(16, Tp - t0 - 16), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
+        const bool full = cs == 16 && t0 + 16 <= T;  // every row of the chunk a real tangent
+        if (t0 == 0) {
+          if (full) chunk<true, true>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
+          else chunk<true, false>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
         } else {
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            if (4 * kk < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * kk, r + 4 * kk);
-        }
-        float gbv[16];
-#pragma unroll
-        for (int e = 0; e < 16; ++e) gbv[e] = t0 + e < T ? __ldg(gb + (size_t)(t0 + e) * N) : 0.f;
-        ptx::tmem_wait16(r);
-        if (more) ptx::cp_async_wait<1>();
-        else ptx::cp_async_wait<0>();
-        __syncwarp();
-        int e0 = 0;
-        if (t0 == 0) {  // value row and Laplacian row
-          h = tanhf(__uint_as_float(r[0]) + gbv[0] + b);
-          d1 = 1.f - h * h;
-          float y = h;
-          if (has_resid) y = (y + get(buf, 0, lane)) * kRsqrt2;
-          put(buf, 0, lane, y);
-          zL = __uint_as_float(r[1]) + gbv[1];
-          if (has_resid) res1 = get(buf, 1, lane);
-          e0 = 2;
-        }
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          if (e < e0 || e >= cs) continue;
-          const bool real = t0 + e < T;
-          const float z = real ? __uint_as_float(r[e]) + gbv[e] : 0.f;
-          S = fmaf(z, z, S);
-          float y = d1 * z;
-          if (has_resid) y = (y + get(buf, e, lane)) * kRsqrt2;
-          put(buf, e, lane, real ? y : 0.f);
+          if (full) chunk<false, true>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
+          else chunk<false, false>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
         }
         __syncwarp();
         store(out, r0 + t0, cs, t0 == 0 ? 1 : -1, col0, nvec, lane, buf);
         __syncwarp();
       }
-      float y1 = d1 * zL - 2.f * h * d1 * S;
-      if (has_resid) y1 = (y1 + res1) * kRsqrt2;
+      float y1 = st.d1 * st.zL - 2.f * st.h * st.d1 * st.S;
+      if (RESID) y1 = (y1 + st.res1) * kRsqrt2;
       if (f < N) {
         const __nv_bfloat16 hi = __float2bfloat16_rn(y1);
         __nv_bfloat16* o = out.p + (r0 + 1) * (size_t)out.ld + f;
         o[0] = hi;
         o[out.plane] = __float2bfloat16_rn(y1 - __bfloat162float(hi));
       }
+    }
+  }
+
+  // running forward-Laplacian state of one (group, feature)
+  struct FlState {
+    float h, d1, zL, S, res1;
+  };
+  // One chunk of tangent rows t0 .. t0 + cs - 1.  FIRST: the chunk holds the
+  // value row (t = 0) and the Laplacian row (t = 1, finished after the last
+  // chunk).  FULL: all 16 rows are real tangents (no size or padding checks).
+  template <bool FIRST, bool FULL>
+  __device__ __forceinline__ void chunk(FlState& st, uint32_t tcol, const float* gb, int t0, int cs, int T, int N,
+                                        float b, bool more, int lane, __nv_bfloat16* buf) const {
+    uint32_t r[16];
+    if (FULL || cs == 16) {
+      ptx::tmem_ld16_nw(tcol + t0, r);
+    } else {
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        if (4 * kk < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * kk, r + 4 * kk);
+    }
+    float gbv[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) gbv[e] = (FULL || t0 + e < T) ? __ldg(gb + (size_t)(t0 + e) * N) : 0.f;
+    ptx::tmem_wait16(r);
+    if (more) ptx::cp_async_wait<1>();
+    else ptx::cp_async_wait<0>();
+    __syncwarp();
+    if (FIRST) {  // value row and Laplacian row
+      st.h = tanhf(__uint_as_float(r[0]) + gbv[0] + b);
+      st.d1 = 1.f - st.h * st.h;
+      float y = st.h;
+      if (RESID) y = (y + get(buf, 0, lane)) * kRsqrt2;
+      put(buf, 0, lane, y);
+      st.zL = __uint_as_float(r[1]) + gbv[1];
+      if (RESID) st.res1 = get(buf, 1, lane);
+    }
+#pragma unroll
+    for (int e = FIRST ? 2 : 0; e < 16; ++e) {
+      if (!FULL && e >= cs) break;
+      const bool real = FULL || t0 + e < T;
+      const float z = real ? __uint_as_float(r[e]) + gbv[e] : 0.f;
+      st.S = fmaf(z, z, st.S);
+      float y = st.d1 * z;
+      if (RESID) y = (y + get(buf, e, lane)) * kRsqrt2;
+      put(buf, e, lane, real ? y : 0.f);
     }
   }
 };
@@ -734,15 +752,22 @@ qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
     set_error("tensor-core layer: output width %d is not a multiple of 8", a.n_out);
     return QMC_ERR_SHAPE;
   }
-  EpiTcLayer e{};
-  e.n_groups = a.n_groups;
-  e.n = a.n;
-  e.ld = a.n_out;
-  e.resid = StSplit{const_cast<__nv_bfloat16*>(a.X), a.k1, a.x_plane};
-  e.has_resid = a.residual;
-  e.out = StSplit{a.out, a.n_out, a.out_plane};
-  e.Gb = a.Gb;
-  e.bias = a.bias;
+  auto fill = [&](auto& e) {
+    e.n_groups = a.n_groups;
+    e.n = a.n;
+    e.ld = a.n_out;
+    e.resid = StSplit{const_cast<__nv_bfloat16*>(a.X), a.k1, a.x_plane};
+    e.out = StSplit{a.out, a.n_out, a.out_plane};
+    e.Gb = a.Gb;
+    e.bias = a.bias;
+  };
+  if (a.residual) {
+    EpiTcLayer<true> e{};
+    fill(e);
+    return launch(s, mA, mA, mB1, mB2, g, (a.n_groups + G - 1) / G, e);
+  }
+  EpiTcLayer<false> e{};
+  fill(e);
   return launch(s, mA, mA, mB1, mB2, g, (a.n_groups + G - 1) / G, e);
 }
 
