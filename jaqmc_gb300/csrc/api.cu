@@ -156,6 +156,8 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
     if (d.upd2[l]) a->wt2[l] = take((size_t)d.d2[l] * d.d2_in[l]);
   }
   for (int s = 0; s < nch; ++s) a->wt_orb[s] = take((size_t)d.norb_p * d.d_last);
+  a->k0w = 64 * ((d.d1_in_p[0] + 63) / 64 + (d.g2_p[0] + 63) / 64);
+  a->w0_pad = take((size_t)a->k0w * d.d1[0]);
   a->total = o;
   size_t b = 0;
   auto takeb = [&](size_t n) { size_t r = b; b += align_up(n, 128); return r; };
@@ -164,6 +166,7 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
     a->t_g1[l] = takeb(2 * (size_t)d.d1[l] * d.g1_p[l]);
   }
   for (int s = 0; s < nch; ++s) a->t_orb[s] = takeb(2 * (size_t)d.norb * d.d_last);
+  a->t0_pad = takeb(2 * (size_t)d.d1[0] * a->k0w);
   a->total_bf16 = b;
 }
 
@@ -204,6 +207,9 @@ Plan make_plan(const qmc_model* m, int op, int B) {
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes, 256); return r; };
   p.x0 = take(rows * p.K0p * 4);
+  // split-bf16 copies of the first layer's operands (mixed form)
+  p.x0s = take(p.mixed ? rows * p.K0p * 4 : 0);
+  p.g2s0 = take(p.mixed ? rows * d.g2_p[0] * 4 : 0);
   p.h1[0] = take(rows * dmax * p.act_bytes);
   p.h1[1] = take(rows * dmax * p.act_bytes);
   size_t pairs = (size_t)B * d.n * d.n;
@@ -357,19 +363,45 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
     float* Gb = at<float>(ws, p.gb);
     const float* H2 = at<float>(ws, p.h2[h2cur]);
     if (l == 0) {
+      // first layer (4A-wide features): spin means and broadcast term in FP32,
+      // the main GEMM on the tensor cores from split-bf16 copies of the
+      // features and pair means, with the chunk-padded kernel
       float* X0 = at<float>(ws, p.x0);
       float* G1 = at<float>(ws, p.g1);
-      float* G2 = at<float>(ws, p.g2);
+      const size_t rows = (size_t)B * n * Tp;
+      bf* X0s = at<bf>(ws, p.x0s);
+      bf* G2s = at<bf>(ws, p.g2s0);
       QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StF32{X0, dinp}, d.g1_p[l],
                                             StF32{G1, d.g1_p[l]}));
       QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
                                                   ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
       if (!fused)
         QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
-                                              StF32{G2, d.g2_p[l]}));
-      EpiLayer<StSplit> epi{Gb, ar + a.b1[l], StSplit{nullptr, dout, 0}, StSplit{out, dout, p.h1_plane}, T};
-      QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, B * n, rows_map, X0, dinp, dinp, G2, d.g2_p[l],
-                                                     d.g2_p[l], ar + a.w_main[l], dout, dout, epi));
+                                              StSplit{G2s, d.g2_p[l], rows * d.g2_p[l]}));
+      else
+        QMC_PROF(QMC_KC_LAYER0, launch_to_split(s, rows * d.g2_p[l], at<float>(ws, p.g2), G2s, rows * d.g2_p[l]));
+      QMC_PROF(QMC_KC_LAYER0, launch_to_split(s, rows * dinp, X0, X0s, rows * dinp));
+      TcLayerArgs la{};
+      la.n_groups = B * n;
+      la.n = n;
+      la.Tp = Tp;
+      la.T = T;
+      la.X = X0s;
+      la.k1 = dinp;
+      la.x_plane = rows * dinp;
+      la.G2 = G2s;
+      la.k2 = d.g2_p[l];
+      la.g2_plane = rows * d.g2_p[l];
+      la.Wt = m->arena_bf16 + a.t0_pad;
+      la.w_ld = a.k0w;
+      la.n_out = dout;
+      la.Gb = Gb;
+      la.bias = ar + a.b1[l];
+      la.residual = false;
+      la.out = out;
+      la.out_plane = p.h1_plane;
+      la.err = m->dev_err;
+      QMC_PROF_TRY(QMC_KC_LAYER0, tc_stream_layer(s, la));
     } else {
       bf* in = at<bf>(ws, p.h1[cur]);
       bf* G1 = at<bf>(ws, p.g1);
@@ -564,7 +596,7 @@ qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, 
   if (m->precision == QMC_PRECISION_MIXED_BF16) {
     const Dims& d = m->d;
     for (int l = 1; l < d.L; ++l)
-      if (!tc_layer_supported(d.d1_in_p[l], d.g2_p[l], d.d1[l])) {
+      if (d.d1_in_p[l] % 64 || !tc_layer_supported(d.d1_in_p[l], d.g2_p[l], d.d1[l])) {
         set_error("mixed precision needs one-electron widths that are multiples of 64 (layer %d)", l);
         return QMC_ERR_UNSUPPORTED;
       }
@@ -791,6 +823,16 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
   for (int c = 0; c < nch; ++c)
     QMC_CUDA(launch_transpose_split(s, ar + a.w_orb[c], d.d_last, d.norb, d.norb_p,
                                     m->arena_bf16 + a.t_orb[c], d.d_last, d.norb));
+  // first-layer kernel with per-source chunk padding: feature rows at 0,
+  // pair-mean rows at the next multiple of 64
+  {
+    const int d1 = d.d1[0], kx = d.d1_in_p[0], k2 = d.g2_p[0], o2 = 64 * ((kx + 63) / 64);
+    QMC_CUDA(cudaMemsetAsync(ar + a.w0_pad, 0, sizeof(float) * a.k0w * d1, s));
+    QMC_CUDA(cudaMemcpyAsync(ar + a.w0_pad, ar + a.w_main[0], sizeof(float) * kx * d1, cudaMemcpyDeviceToDevice, s));
+    QMC_CUDA(cudaMemcpyAsync(ar + a.w0_pad + (size_t)o2 * d1, ar + a.w_main[0] + (size_t)kx * d1,
+                             sizeof(float) * k2 * d1, cudaMemcpyDeviceToDevice, s));
+    QMC_CUDA(launch_transpose_split(s, ar + a.w0_pad, a.k0w, d1, d1, m->arena_bf16 + a.t0_pad, a.k0w, d1));
+  }
   m->params_set = true;
   return QMC_OK;
 }

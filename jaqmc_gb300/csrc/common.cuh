@@ -77,6 +77,11 @@ struct ArenaLayout {
   size_t t_main[QMC_MAX_LAYERS];  // [d1 x (d1_in_p + g2_p)] K-major
   size_t t_g1[QMC_MAX_LAYERS];    // [d1 x g1_p]
   size_t t_orb[2];                // [norb_p x d_last]
+  // first layer on the tensor cores: its kernel with each source (features,
+  // pair means) padded to whole 64-column chunks, as fp32 [k0w][d1] and as
+  // bf16 planes [d1][k0w]
+  size_t w0_pad, t0_pad;
+  int k0w;
   size_t total_bf16;
 };
 

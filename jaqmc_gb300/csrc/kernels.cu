@@ -228,6 +228,21 @@ cudaError_t launch_envelope_apply(cudaStream_t s, int B, int n, int n_up, int sp
   return cudaGetLastError();
 }
 
+// hi = bf16(v), lo = bf16(v - hi) for n contiguous values (planes `plane` apart).
+__global__ void k_to_split(size_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, size_t plane) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float v = src[e];
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  dst[e] = hi;
+  dst[e + plane] = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+cudaError_t launch_to_split(cudaStream_t s, size_t n, const float* src, __nv_bfloat16* dst, size_t plane) {
+  k_to_split<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, dst, plane);
+  return cudaGetLastError();
+}
+
 // =====================================================================
 // two-electron layer (src/jaqmc/wavefunction/backbone/ferminet.py:55-63)
 // rows p: 0 value, 1 Laplacian wrt the pair difference, 2..4 its gradient.

@@ -11,6 +11,9 @@ namespace qmc {
 struct EnvArgs {
   const float* env;  // [B][K][n][n]
 };
+// Split n contiguous fp32 values into bf16 hi / lo planes (`plane` elements apart).
+cudaError_t launch_to_split(cudaStream_t s, size_t n, const float* src, __nv_bfloat16* dst, size_t plane);
+
 // Multiply raw value-only orbital matrices [w][k][i][j] by their envelopes in place.
 cudaError_t launch_envelope_apply(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,

@@ -722,8 +722,13 @@ static qmc_status launch(cudaStream_t s, const CUtensorMap& A0, const CUtensorMa
 
 qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
   const int G = tc_groups_per_tile(a.Tp);
-  if (G <= 0 || !tc_layer_supported(a.k1, a.k2, a.n_out)) {
-    set_error("tensor-core layer: unsupported shape (Tp=%d k1=%d k2=%d n_out=%d)", a.Tp, a.k1, a.k2, a.n_out);
+  const int c1 = (a.k1 + kKChunk - 1) / kKChunk, c2 = (a.k2 + kKChunk - 1) / kKChunk;
+  // a first source narrower than whole chunks needs the chunk-padded weights;
+  // rows of both sources are read with 16-byte aligned strides
+  const bool shape_ok = a.w_ld ? (a.w_ld == kKChunk * (c1 + c2)) : tc_layer_supported(a.k1, a.k2, a.n_out);
+  if (G <= 0 || !shape_ok || a.k1 % 8 || a.k2 % 8 || a.k2 <= 0 || a.k2 > 256 || a.n_out < 16) {
+    set_error("tensor-core layer: unsupported shape (Tp=%d k1=%d k2=%d n_out=%d w_ld=%d)", a.Tp, a.k1, a.k2,
+              a.n_out, a.w_ld);
     return QMC_ERR_SHAPE;
   }
   const size_t rows = (size_t)a.n_groups * a.Tp;
@@ -732,12 +737,12 @@ qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
   g.Tp = a.Tp;
   g.T = a.T;
   g.n_cols = G * a.Tp;
-  g.k1_chunks = a.k1 / kKChunk;
-  g.k_chunks = g.k1_chunks + (a.k2 + kKChunk - 1) / kKChunk;
+  g.k1_chunks = c1;
+  g.k_chunks = c1 + c2;
   g.n_out = a.n_out;
   g.err = a.err;
   CUtensorMap mA, mB1, mB2;
-  const int kw = a.k1 + a.k2;
+  const int kw = a.w_ld ? a.w_ld : a.k1 + a.k2;
   QMC_TRY(make_map(&mA, a.Wt, kw, a.n_out, kw, (size_t)a.n_out * kw, 128));
   QMC_TRY(make_map(&mB1, a.X, a.k1, rows, a.k1, a.x_plane, g.n_cols));
   QMC_TRY(make_map(&mB2, a.G2, a.k2, rows, a.k2, a.g2_plane, g.n_cols));

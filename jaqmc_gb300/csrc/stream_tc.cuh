@@ -24,7 +24,9 @@ struct TcLayerArgs {
   int n_groups, n, Tp, T;
   const __nv_bfloat16* X; int k1; size_t x_plane;   // [rows][k1] split planes
   const __nv_bfloat16* G2; int k2; size_t g2_plane; // [rows][k2] split planes
-  const __nv_bfloat16* Wt; int n_out;               // [n_out][k1+k2] split planes
+  const __nv_bfloat16* Wt; int n_out;               // [n_out][w_ld] split planes
+  int w_ld;  // weight row: 0 = k1 + k2 (k1 a multiple of 64); else 64 * (chunks of k1 + chunks of k2),
+             // the second source's weights starting at column 64 * ceil(k1 / 64)
   const float* Gb; const float* bias;
   bool residual;
   __nv_bfloat16* out; size_t out_plane;             // [rows][n_out] split planes
