@@ -632,7 +632,7 @@ static int tc_stages_fitting(int n_cols, int ebuf_bytes) {
 static int tc_layer_ebuf(int) { return 4 * 2 * 2 * 16 * 32 * 2; }
 
 int tc_groups_per_tile(int Tp) {
-  if (Tp == 1) return 256;
+  if (Tp == 1) return 128;  // value-only tiles: 128 rows, so short launches spread over all SMs
   for (int G = 256 / Tp; G >= 1; --G)
     if ((G * Tp) % 16 == 0 && tc_stages_fitting(G * Tp, tc_layer_ebuf(Tp)) >= 2) return G;
   return 0;
@@ -777,23 +777,24 @@ qmc_status tc_stream_layer(cudaStream_t s, const TcLayerArgs& a) {
 }
 
 qmc_status tc_store_gemm(cudaStream_t s, const TcStoreArgs& a) {
+  constexpr int kRows = 128;  // rows per tile
   TcArgs g{};
-  g.G = 256;
+  g.G = kRows;
   g.Tp = 1;
   g.T = 1;
-  g.n_cols = 256;
+  g.n_cols = kRows;
   g.k1_chunks = (a.k + kKChunk - 1) / kKChunk;
   g.k_chunks = g.k1_chunks;
   g.n_out = a.n_out;
   g.err = a.err;
   CUtensorMap mA, mB;
   QMC_TRY(make_map(&mA, a.Wt, a.k, a.n_out, a.k, (size_t)a.n_out * a.k, 128));
-  QMC_TRY(make_map(&mB, a.X, a.k, a.n_rows, a.k, a.x_plane, 256));
+  QMC_TRY(make_map(&mB, a.X, a.k, a.n_rows, a.k, a.x_plane, kRows));
   EpiTcStore e{};
   e.n_groups = a.n_rows;
   e.out = a.out;
   e.ld = a.n_out;
-  return launch(s, mA, mA, mB, mB, g, (a.n_rows + 255) / 256, e);
+  return launch(s, mA, mA, mB, mB, g, (a.n_rows + kRows - 1) / kRows, e);
 }
 
 qmc_status tc_orbitals(cudaStream_t s, const TcOrbitalArgs& a) {
