@@ -137,10 +137,11 @@ cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, 
 // determinant k, electron i, orbital j): sum_I pi[j,I,k] exp(-s r_iI) with
 // s = |sigma[j,I,k]| (abs_isotropic) or sigma (isotropic), per spin channel
 // of electron i (src/jaqmc/wavefunction/output/envelope.py:98-140).  Same
-// terms in the same order as the tangent epilogues.  One block per walker,
-// thread (i, j); the parameters are staged as [channel][I][k][j] so a warp
-// reads consecutive j.
-__global__ void k_envelope_value(int n, int n_up, int split, int K, int A, int env_abs,
+// terms in the same order as the tangent epilogues.  One block per
+// kEnvWalkers walkers, thread (walker, i, j); the parameters are staged once
+// per block as [channel][I][k][j] so a warp reads consecutive j.
+constexpr int kEnvWalkers = 8;
+__global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A, int env_abs,
                                  const float* __restrict__ pi0, const float* __restrict__ sg0,
                                  const float* __restrict__ pi1, const float* __restrict__ sg1,
                                  const float* __restrict__ rae, float* __restrict__ env) {
@@ -157,19 +158,22 @@ __global__ void k_envelope_value(int n, int n_up, int split, int K, int A, int e
     ss[e] = env_abs ? fabsf(sv) : sv;
   }
   __syncthreads();
-  const int w = blockIdx.x;
-  const int i = threadIdx.x / n, j = threadIdx.x % n;
-  if (i >= n) return;
-  const int c = split && i >= n_up ? 1 : 0;
-  const float* ra = rae + ((size_t)w * n + i) * A;
-  float* out = env + (size_t)w * K * n * n + i * n + j;
-  for (int k = 0; k < K; ++k) {
-    float acc = 0.f;
-    for (int I = 0; I < A; ++I) {
-      const int o = ((c * A + I) * K + k) * n + j;
-      acc += ps[o] * expf(-ss[o] * __ldg(ra + I));
+  const int nn = n * n;
+  for (int e = threadIdx.x; e < kEnvWalkers * nn; e += blockDim.x) {
+    const int w = blockIdx.x * kEnvWalkers + e / nn;
+    if (w >= B) break;
+    const int i = (e % nn) / n, j = e % n;
+    const int c = split && i >= n_up ? 1 : 0;
+    const float* ra = rae + ((size_t)w * n + i) * A;
+    float* out = env + (size_t)w * K * nn + i * n + j;
+    for (int k = 0; k < K; ++k) {
+      float acc = 0.f;
+      for (int I = 0; I < A; ++I) {
+        const int o = ((c * A + I) * K + k) * n + j;
+        acc += ps[o] * expf(-ss[o] * __ldg(ra + I));
+      }
+      out[(size_t)k * nn] = acc;
     }
-    out[(size_t)k * n * n] = acc;
   }
 }
 
@@ -177,9 +181,9 @@ cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int sp
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,
                                   const float* rae, float* env) {
   const size_t sm = sizeof(float) * 2 * (split ? 2 : 1) * (size_t)A * K * n;
-  if (n * n > 1024 || sm > 48 * 1024) return cudaErrorNotSupported;
-  const int threads = (n * n + 31) / 32 * 32;
-  k_envelope_value<<<B, threads, sm, s>>>(n, n_up, split, K, A, env_abs, pi0, sg0, pi1, sg1, rae, env);
+  if (sm > 48 * 1024) return cudaErrorNotSupported;
+  k_envelope_value<<<(unsigned)((B + kEnvWalkers - 1) / kEnvWalkers), 256, sm, s>>>(B, n, n_up, split, K, A, env_abs,
+                                                                                 pi0, sg0, pi1, sg1, rae, env);
   return cudaGetLastError();
 }
 
