@@ -270,6 +270,7 @@ template <bool RESID>
 struct EpiTcLayer : ContigTiles {
   static constexpr int kCR = 16;                 // rows per chunk
   static constexpr int kBuf = 2 * kCR * 32;      // bf16 per chunk buffer
+  static constexpr int kGbuf = kCR * 32;         // floats per broadcast-term chunk
   int n, ld;  // electrons per walker, activation row width (n_out)
   StSplit resid, out;
   const float* Gb;
@@ -287,6 +288,17 @@ struct EpiTcLayer : ContigTiles {
                         st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq);
     }
     ptx::cp_async_commit();
+  }
+  // rows [t0, t0 + nrows) x features [col0, col0 + 32) of a walker's broadcast
+  // terms (fp32, row stride N) -> gbuf[16][32]; committed with the next fetch
+  __device__ __forceinline__ void fetch_gb(const float* gbrow, int nrows, int col0, int N, int lane,
+                                           float* gbuf) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int r = v >> 3, c = 4 * (v & 7);
+      if (r < nrows && col0 + c + 4 <= N) ptx::cp_async16(gbuf + r * 32 + c, gbrow + (size_t)r * N + col0 + c);
+    }
   }
   // buf -> rows [row0, row0 + nrows) of `st`, except row `skip`
   __device__ __forceinline__ void store(const StSplit& st, size_t row0, int nrows, int skip, int col0, int nvec,
@@ -316,7 +328,7 @@ struct EpiTcLayer : ContigTiles {
     const int nvec = max(0, min(4, (N - col0) / 8));
     const int fc = f < N ? f : 0;  // clamped feature for loads of parameters
     const float b = bias[fc];
-    __nv_bfloat16* buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * 2 * kBuf;
+    __nv_bfloat16* buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * 2 * kBuf;  // value-only layout
     if (g.T == 1) {
       int c0 = 16 * half, k = 0;
       if (c0 >= ti.ng) return;
@@ -359,26 +371,38 @@ struct EpiTcLayer : ContigTiles {
       return;
     }
     const int Tp = g.Tp, T = g.T;
+    // per warp: two residual/output chunk buffers, then two fp32 chunks of the
+    // broadcast terms, all refilled by cp.async one chunk ahead
+    buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * (2 * kBuf + 2 * kGbuf * 2);
+    float* gbuf0 = reinterpret_cast<float*>(buf0 + 2 * kBuf);
     for (int lg = half; lg < ti.ng; lg += 2) {
       const int gi = ti.g0 + lg;
       const size_t r0 = (size_t)gi * Tp;
       const uint32_t tcol = taddr + (uint32_t)(lg * Tp);
-      const float* gb = Gb + (size_t)(gi / n) * Tp * N + fc;
+      const float* gbw = Gb + (size_t)(gi / n) * Tp * N;  // this walker's broadcast rows
+      fetch_gb(gbw, min(16, Tp), col0, N, lane, gbuf0);
       if (RESID) fetch(resid, r0, min(16, Tp), col0, nvec, lane, buf0);
+      else ptx::cp_async_commit();
       FlState st{};
       int k = 0;
       for (int t0 = 0; t0 < Tp; t0 += 16, k ^= 1) {
         __nv_bfloat16* buf = buf0 + k * kBuf;
+        const float* gbuf = gbuf0 + k * kGbuf;
         const int cs = min(16, Tp - t0);  // a multiple of 4, uniform
         const bool more = t0 + 16 < Tp;
-        if (RESID && more) fetch(resid, r0 + t0 + 16, min(16, Tp - t0 - 16), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
+        if (more) {
+          const int nr = min(16, Tp - t0 - 16);
+          fetch_gb(gbw + (size_t)(t0 + 16) * N, nr, col0, N, lane, gbuf0 + (k ^ 1) * kGbuf);
+          if (RESID) fetch(resid, r0 + t0 + 16, nr, col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
+          else ptx::cp_async_commit();
+        }
         const bool full = cs == 16 && t0 + 16 <= T;  // every row of the chunk a real tangent
         if (t0 == 0) {
-          if (full) chunk<true, true>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
-          else chunk<true, false>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
+          if (full) chunk<true, true>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
+          else chunk<true, false>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
         } else {
-          if (full) chunk<false, true>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
-          else chunk<false, false>(st, tcol, gb, t0, cs, T, N, b, more, lane, buf);
+          if (full) chunk<false, true>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
+          else chunk<false, false>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
         }
         __syncwarp();
         store(out, r0 + t0, cs, t0 == 0 ? 1 : -1, col0, nvec, lane, buf);
@@ -403,7 +427,7 @@ struct EpiTcLayer : ContigTiles {
   // value row (t = 0) and the Laplacian row (t = 1, finished after the last
   // chunk).  FULL: all 16 rows are real tangents (no size or padding checks).
   template <bool FIRST, bool FULL>
-  __device__ __forceinline__ void chunk(FlState& st, uint32_t tcol, const float* gb, int t0, int cs, int T, int N,
+  __device__ __forceinline__ void chunk(FlState& st, uint32_t tcol, const float* gbuf, int t0, int cs, int T,
                                         float b, bool more, int lane, __nv_bfloat16* buf) const {
     uint32_t r[16];
     if (FULL || cs == 16) {
@@ -413,13 +437,13 @@ struct EpiTcLayer : ContigTiles {
       for (int kk = 0; kk < 4; ++kk)
         if (4 * kk < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * kk, r + 4 * kk);
     }
-    float gbv[16];
-#pragma unroll
-    for (int e = 0; e < 16; ++e) gbv[e] = (FULL || t0 + e < T) ? __ldg(gb + (size_t)(t0 + e) * N) : 0.f;
     ptx::tmem_wait16(r);
     if (more) ptx::cp_async_wait<1>();
     else ptx::cp_async_wait<0>();
     __syncwarp();
+    float gbv[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) gbv[e] = (FULL || t0 + e < T) ? gbuf[e * 32 + lane] : 0.f;
     if (FIRST) {  // value row and Laplacian row
       st.h = tanhf(__uint_as_float(r[0]) + gbv[0] + b);
       st.d1 = 1.f - st.h * st.h;
@@ -628,8 +652,12 @@ static int tc_stages_fitting(int n_cols, int ebuf_bytes) {
 }
 
 // Epilogue staging bytes per half of a layer tile: four warps x two chunk
-// buffers x [2 planes][16 rows][32 features] bf16.
-static int tc_layer_ebuf(int) { return 4 * 2 * 2 * 16 * 32 * 2; }
+// buffers x [2 planes][16 rows][32 features] bf16, plus (tangent passes) two
+// fp32 chunks [16][32] of the broadcast terms.
+static int tc_layer_ebuf(int Tp) {
+  const int per_warp = 2 * 2 * 16 * 32 * 2 + (Tp == 1 ? 0 : 2 * 16 * 32 * 4);
+  return 4 * per_warp;
+}
 
 int tc_groups_per_tile(int Tp) {
   if (Tp == 1) return 128;  // value-only tiles: 128 rows, so short launches spread over all SMs
