@@ -328,8 +328,16 @@ def run_request_only(args, wl):
     e1.record()
     torch.cuda.synchronize()
     assert m.check_error() == 0
-    print(json.dumps({"op": args.op, "precision": args.precision, "walkers": B, "system": wl["system"],
-                      "ms_per_step": e0.elapsed_time(e1) / args.steps}), flush=True)
+    line = {"op": args.op, "precision": args.precision, "walkers": B, "system": wl["system"],
+            "ms_per_step": e0.elapsed_time(e1) / args.steps}
+    if args.kernel_classes:
+        _native.profile_enable(True)
+        _native.profile_read()
+        one(args.warmup + args.steps)
+        prof = _native.profile_read()
+        _native.profile_enable(False)
+        line["kernel_ms"] = {k: round(v[1], 4) for k, v in prof.items() if v[0]}
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -571,6 +579,8 @@ def main():
                     help="only W warm-up + K timed requests of --precision (for profiler runs)")
     ap.add_argument("--op", default="request", choices=["request", "el", "mh"],
                     help="with --request-only: the whole request, only E_L, or only the MH steps")
+    ap.add_argument("--kernel-classes", action="store_true",
+                    help="with --request-only: add one profiled pass and its per-class kernel times")
     ap.add_argument("--serve-only", action="store_true", help="print only the serving measurement")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrival rate (jobs/s)")
     ap.add_argument("--serve-jobs", type=int, default=48)

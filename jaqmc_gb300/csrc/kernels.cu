@@ -415,8 +415,36 @@ __global__ void __launch_bounds__(256) k_pair_layer_mean(int n, int n_up, int C,
 // shared memory, and after each layer the spin means over the first electron
 // index that the next one-electron layer reads (G2 of layers 1..nl).  Pair
 // activations never leave the SM.  Widths: input 4 or 32, output 32.
+// z[0..3] += x * W[0..7] as packed pairs (8 consecutive weights of one row).
+__device__ __forceinline__ void pair_fma8(float x, const float* __restrict__ w, float2* z) {
+  const float2 xx = make_float2(x, x);
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const float4 wv = w4[q];
+    z[2 * q] = __ffma2_rn(xx, make_float2(wv.x, wv.y), z[2 * q]);
+    z[2 * q + 1] = __ffma2_rn(xx, make_float2(wv.z, wv.w), z[2 * q + 1]);
+  }
+}
+
+// tanh for the two-electron stream.  FAST (mixed form): from
+// tanh|x| = (1 - e) / (1 + e), e = 2^(-2 log2(e) |x|), with the hardware
+// base-2 exponential and a fast divide; absolute error a few 1e-7, below the
+// ~1e-5 relative error of the form's split-BF16 operands.  Otherwise tanhf.
+template <bool FAST>
+__device__ __forceinline__ float pair_tanh(float x) {
+  if constexpr (FAST) {
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(fabsf(x) * -2.8853900817779268f));
+    return copysignf(__fdividef(1.f - e, 1.f + e), x);
+  } else {
+    return tanhf(x);
+  }
+}
+
 template <class Out>
 __global__ void __launch_bounds__(256) k_pair_stream_value(PairStreamArgs a, PairStreamOut<Out> o) {
+  constexpr bool kFastTanh = std::is_same<Out, StSplit>::value;
   extern __shared__ float shs[];
   constexpr int DO = 32, RS = 36;  // row stride 36 floats: conflict-free 16-byte accesses
   float* Ws = shs;                         // [nl][32][32]
@@ -449,39 +477,36 @@ __global__ void __launch_bounds__(256) k_pair_stream_value(PairStreamArgs a, Pai
           x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
         }
       }
+      // 8 outputs per pass: each input broadcast feeds 4 packed FMAs
+      // (__ffma2_rn rounds each lane like fmaf, so the sums are unchanged)
 #pragma unroll
-      for (int f4 = 0; f4 < DO / 4; ++f4) {
-        float z[4];
+      for (int f8 = 0; f8 < DO / 8; ++f8) {
+        float2 z[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) z[e] = bl[4 * f4 + e];
+        for (int e = 0; e < 4; ++e) z[e] = make_float2(bl[8 * f8 + 2 * e], bl[8 * f8 + 2 * e + 1]);
         if (din == 4) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const float4 wv = *reinterpret_cast<const float4*>(&Wl[k * DO + 4 * f4]);
-            z[0] = fmaf(x[k], wv.x, z[0]);
-            z[1] = fmaf(x[k], wv.y, z[1]);
-            z[2] = fmaf(x[k], wv.z, z[2]);
-            z[3] = fmaf(x[k], wv.w, z[3]);
-          }
+          for (int k = 0; k < 4; ++k) pair_fma8(x[k], Wl + k * DO + 8 * f8, z);
         } else {
 #pragma unroll
-          for (int k = 0; k < DO; ++k) {
-            const float4 wv = *reinterpret_cast<const float4*>(&Wl[k * DO + 4 * f4]);
-            z[0] = fmaf(x[k], wv.x, z[0]);
-            z[1] = fmaf(x[k], wv.y, z[1]);
-            z[2] = fmaf(x[k], wv.z, z[2]);
-            z[3] = fmaf(x[k], wv.w, z[3]);
+          for (int k = 0; k < DO; ++k) pair_fma8(x[k], Wl + k * DO + 8 * f8, z);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          float4 v;
+          v.x = pair_tanh<kFastTanh>(z[2 * q].x);
+          v.y = pair_tanh<kFastTanh>(z[2 * q].y);
+          v.z = pair_tanh<kFastTanh>(z[2 * q + 1].x);
+          v.w = pair_tanh<kFastTanh>(z[2 * q + 1].y);
+          if (din == DO) {  // residual: this thread's own row, not yet overwritten
+            const float4 r = *reinterpret_cast<const float4*>(row + 8 * f8 + 4 * q);
+            v.x = (v.x + r.x) * kRsqrt2;
+            v.y = (v.y + r.y) * kRsqrt2;
+            v.z = (v.z + r.z) * kRsqrt2;
+            v.w = (v.w + r.w) * kRsqrt2;
           }
+          *reinterpret_cast<float4*>(row + 8 * f8 + 4 * q) = v;
         }
-        float4 v;
-        v.x = tanhf(z[0]); v.y = tanhf(z[1]); v.z = tanhf(z[2]); v.w = tanhf(z[3]);
-        if (din == DO) {
-          v.x = (v.x + x[4 * f4]) * kRsqrt2;
-          v.y = (v.y + x[4 * f4 + 1]) * kRsqrt2;
-          v.z = (v.z + x[4 * f4 + 2]) * kRsqrt2;
-          v.w = (v.w + x[4 * f4 + 3]) * kRsqrt2;
-        }
-        *reinterpret_cast<float4*>(row + 4 * f4) = v;
       }
     }
     __syncthreads();
@@ -1003,6 +1028,116 @@ __device__ S warp_trace_sq(const S* Ms, int n, int ldm) {
   return t2;
 }
 
+// Tangent traces of one determinant for n <= 16 (FP32):
+//   tL = tr(A^-1 L_A) as one dot product, and for every Jacobian direction d
+//   P_d = A^-1 J_d A, t1_d = tr(P_d), t2 += tr(P_d^2), q += t1_d^2.
+// Each half-warp owns one direction per pass with lane j computing column j
+// of P_d, and every lane carries two directions, so a warp pass covers four
+// directions and each broadcast row of A^-1 feeds 2 x NMAX FMAs.  P_d goes
+// to shared memory (row stride ldm, odd) for tr(P_d^2) = sum_i P_ij P_ji.
+// (Packing the two directions into f32x2 FMAs needs a duplicated A^-1 and
+// more shared-memory loads per row, which measured slower.)
+template <int NMAX>
+__device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak, int n, int T, size_t ts,
+                                 int ld, int ldm, float* Ms, float* t1s, DetOut& o) {
+  static_assert(NMAX <= 16 && NMAX % 4 == 0, "half-warp columns");
+  const int lane = threadIdx.x & 31;
+  const int h = lane >> 4, j = lane & 15;
+  const bool colv = j < n;
+  // tL = sum_{i,m} A^-1_im L_mi
+  {
+    const float* L = Ak + ts;
+    float acc = 0.f;
+    for (int e = lane; e < n * n; e += 32) {
+      const int m = e / n, i = e - m * n;
+      acc = fmaf(Ainv[i * ld + m], L[e], acc);
+    }
+    o.tL = warp_sum(acc);
+  }
+  const int D = T - 2;
+  float t2acc = 0.f, qacc = 0.f;
+  float* Ma = Ms + (size_t)h * n * ldm;        // direction 4g + h
+  float* Mb = Ms + (size_t)(2 + h) * n * ldm;  // direction 4g + 2 + h
+  float xa[NMAX], xb[NMAX];
+  auto load_cols = [&](int g) {
+    const int da = 4 * g + h, db = 4 * g + 2 + h;
+    const float* Ja = Ak + (size_t)(2 + da) * ts;
+    const float* Jb = Ak + (size_t)(2 + db) * ts;
+    const bool va = colv && da < D, vb = colv && db < D;
+#pragma unroll
+    for (int m = 0; m < NMAX; ++m) {
+      xa[m] = (va && m < n) ? __ldg(Ja + m * n + j) : 0.f;
+      xb[m] = (vb && m < n) ? __ldg(Jb + m * n + j) : 0.f;
+    }
+  };
+  const int G = (D + 3) / 4;
+  if (G > 0) load_cols(0);
+  for (int g = 0; g < G; ++g) {
+    float tra = 0.f, trb = 0.f;
+#pragma unroll
+    for (int i = 0; i < NMAX; ++i) {
+      if (i < n) {
+        const float4* a4 = reinterpret_cast<const float4*>(Ainv + i * ld);
+        float acc_a = 0.f, acc_b = 0.f;
+#pragma unroll
+        for (int m4 = 0; m4 < NMAX / 4; ++m4) {
+          if (4 * m4 < n) {
+            const float4 a = a4[m4];
+            acc_a = fmaf(a.x, xa[4 * m4], acc_a);
+            acc_a = fmaf(a.y, xa[4 * m4 + 1], acc_a);
+            acc_a = fmaf(a.z, xa[4 * m4 + 2], acc_a);
+            acc_a = fmaf(a.w, xa[4 * m4 + 3], acc_a);
+            acc_b = fmaf(a.x, xb[4 * m4], acc_b);
+            acc_b = fmaf(a.y, xb[4 * m4 + 1], acc_b);
+            acc_b = fmaf(a.z, xb[4 * m4 + 2], acc_b);
+            acc_b = fmaf(a.w, xb[4 * m4 + 3], acc_b);
+          }
+        }
+        if (colv) {
+          Ma[i * ldm + j] = acc_a;
+          Mb[i * ldm + j] = acc_b;
+        }
+        if (i == j) {
+          tra = acc_a;
+          trb = acc_b;
+        }
+      }
+    }
+    // next pass's columns are in flight while this pass is reduced
+    if (g + 1 < G) load_cols(g + 1);
+    __syncwarp();
+    float sq = 0.f;
+    if (colv) {
+      const float* ra = Ma + j * ldm;
+      const float* rb = Mb + j * ldm;
+#pragma unroll
+      for (int i = 0; i < NMAX; ++i)
+        if (i < n) sq = fmaf(Ma[i * ldm + j], ra[i], fmaf(Mb[i * ldm + j], rb[i], sq));
+    }
+    t2acc += sq;
+    // per-half sums of the diagonals (lanes j >= n contribute zero)
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) {
+      tra += __shfl_xor_sync(0xffffffffu, tra, off);
+      trb += __shfl_xor_sync(0xffffffffu, trb, off);
+    }
+    const int da = 4 * g + h, db = 4 * g + 2 + h;
+    if (j == 0) {
+      if (da < D) {
+        t1s[da] = tra;
+        qacc = fmaf(tra, tra, qacc);
+      }
+      if (db < D) {
+        t1s[db] = trb;
+        qacc = fmaf(trb, trb, qacc);
+      }
+    }
+    __syncwarp();
+  }
+  o.t2 = warp_sum(t2acc);
+  o.q = warp_sum(qacc);
+}
+
 // Factorise determinant k of a walker and, for T > 1, the slogdet traces
 //   tL = tr(A^-1 L_A),  t1_d = tr(A^-1 J_d A),  t2 = sum_d tr((A^-1 J_d A)^2),
 //   q = sum_d t1_d^2.
@@ -1026,6 +1161,11 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* sc
   o.refactor = (!fp64_pass && !o.singular && !(growth <= (double)kRefactorGrowth)) ? 1 : 0;
   if (T <= 1 || o.singular || o.refactor) return o;
   warp_inverse<S>(LU, Ainv, perm, n, ld);
+  if constexpr (sizeof(S) == 4 && NMAX <= 16) {
+    det_tangents_f32<NMAX>(reinterpret_cast<const float*>(Ainv), Ak, n, T, ts, ld, ldm,
+                           reinterpret_cast<float*>(Ms), t1s, o);
+    return o;
+  }
   float t2acc = 0.f, qacc = 0.f;
   for (int t = 1; t < T; ++t) {
     const float* At = Ak + (size_t)t * ts;
@@ -1047,7 +1187,7 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* sc
 }
 
 template <int NMAX>
-__global__ void k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
+__global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
                          const float* __restrict__ pe, float* __restrict__ logpsi,
                          float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
                          uint8_t* __restrict__ flags, int* __restrict__ n_refactor) {
@@ -1140,11 +1280,24 @@ __global__ void k_logdet(int n, int K, int Tp, int T, const float* __restrict__ 
 }
 
 // Value-only determinant stage (MH passes): LU in registers.  A segment of
-// SEG lanes factorises one matrix, lane i holding row i (rows >= n are
-// identity rows), so a warp works on 32/SEG matrices at once.  Pivot search,
-// row exchange and pivot-row broadcast are segment shuffles; the multipliers
-// are not kept (only U's diagonal is needed).  Matrices whose pivot growth
-// exceeds the threshold are re-factorised in FP64 afterwards by warp 0.
+// SEG lanes factorises one matrix, lane i holding row i, so a warp works on
+// 32/SEG matrices at once.  Rows stay in their lanes: step k picks the pivot
+// among the lanes not yet used (one packed |value|:lane key, SEG-lane max by
+// shuffles), the pivot lane writes its row to a per-segment shared-memory
+// buffer that every lane reads back, and the permutation's parity comes from
+// the used-lane mask.  |det| is a running FP32 product of the pivots kept as
+// mantissa and exponent; the multipliers are not kept.  Matrices whose pivot
+// growth exceeds the threshold are re-factorised in FP64 afterwards by warp 0.
+template <int SEG>
+__device__ __forceinline__ unsigned pivot_key(float v, int i, bool cand) {
+  constexpr unsigned IB = SEG <= 4 ? 2 : SEG <= 8 ? 3 : SEG <= 16 ? 4 : 5;  // lane index bits
+  constexpr unsigned MARK = 1u << IB;
+  constexpr unsigned KEEP = ~((MARK << 1) - 1u);
+  // |v| bit patterns order like the values; ties (to 2^-(23-IB-1) relative)
+  // go to the lower lane, and any candidate beats a non-candidate (key 0)
+  return cand ? ((__float_as_uint(fabsf(v)) & KEEP) | MARK | (unsigned)(SEG - 1 - i)) : 0u;
+}
+
 template <int SEG>
 __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int WB, float* __restrict__ A,
                                                       float* __restrict__ logpsi, float* __restrict__ sign,
@@ -1155,12 +1308,17 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
   float* sgs = reinterpret_cast<float*>(lds + nmat);       // [nmat]
   int* redo = reinterpret_cast<int*>(sgs + nmat);          // [nmat] re-factorise flags
   int* singular = redo + nmat;                             // [nmat]
-  char* scratch = reinterpret_cast<char*>(shv) + align_up((size_t)nmat * 20, 16);
+  float* rowbuf = reinterpret_cast<float*>(reinterpret_cast<char*>(shv) + align_up((size_t)nmat * 20, 16));
+  char* scratch = reinterpret_cast<char*>(rowbuf + 8 * 64);  // FP64 re-factorisation
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / SEG, i = lane % SEG;
-  const unsigned seg_mask = (SEG == 32) ? 0xffffffffu : (((1u << SEG) - 1u) << (sub * SEG));
+  // two pivot-row buffers per segment, used on alternate steps
+  float* rb0 = rowbuf + warp * 64 + sub * SEG;
+  float* rb1 = rb0 + 32;
   const int w0 = blockIdx.x * WB;
   const int mpw = 32 / SEG;
+  const unsigned all_rows = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+  int my_redo = 0;
   for (int base = warp * mpw; base < nmat; base += 8 * mpw) {
     const int mloc = base + sub;
     const int w = w0 + mloc / K;
@@ -1168,7 +1326,7 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
     float r[SEG];
     float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
 #pragma unroll
-    for (int j = 0; j < SEG; ++j) r[j] = (active && i < n && j < n) ? Am[i * n + j] : (j == i ? 1.f : 0.f);
+    for (int j = 0; j < SEG; ++j) r[j] = (active && i < n && j < n) ? Am[i * n + j] : 0.f;
     if (env.env && active && i < n) {  // envelope factors of row i
       const float* Em = env.env + ((size_t)w * K + (mloc % K)) * n * n;
 #pragma unroll
@@ -1177,86 +1335,91 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
     }
     float amax = 0.f;
 #pragma unroll
-    for (int j = 0; j < SEG; ++j) amax = fmaxf(amax, (i < n) ? fabsf(r[j]) : 0.f);
+    for (int j = 0; j < SEG; ++j) amax = fmaxf(amax, fabsf(r[j]));
 #pragma unroll
     for (int o = SEG / 2; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o, SEG));
-    float sg = 1.f;
+    bool cand = active && i < n;
+    unsigned unused = all_rows;
+    __syncwarp();  // the previous matrix's last pivot rows have been read
+    int inversions = 0, ex = 0, sing = 0;
+    float mant = 1.f, sg = 1.f, umax = 0.f;
 #pragma unroll
     for (int k = 0; k < SEG; ++k) {
       if (k < n) {
-        float v = (i >= k && i < n) ? fabsf(r[k]) : -1.f;
-        int vi = i;
+        unsigned key = pivot_key<SEG>(r[k], i, cand);
 #pragma unroll
-        for (int o = SEG / 2; o > 0; o >>= 1) {
-          float ov = __shfl_xor_sync(0xffffffffu, v, o, SEG);
-          int oi = __shfl_xor_sync(0xffffffffu, vi, o, SEG);
-          if (ov > v || (ov == v && oi < vi)) { v = ov; vi = oi; }
+        for (int o = SEG / 2; o > 0; o >>= 1) key = max(key, __shfl_xor_sync(0xffffffffu, key, o, SEG));
+        const int p = SEG - 1 - (int)(key & (unsigned)(SEG - 1));
+        inversions += __popc(unused & ((1u << p) - 1u));
+        unused &= ~(1u << p);
+        float* rb = (k & 1) ? rb1 : rb0;
+        if (i == p) {
+#pragma unroll
+          for (int q = 0; q < SEG / 4; ++q)
+            if (4 * q + 3 >= k)
+              *reinterpret_cast<float4*>(rb + 4 * q) = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+          cand = false;
         }
-        const int p = vi;
-        if (p != k) sg = -sg;
-        const int src = (i == k) ? p : ((i == p) ? k : i);
-#pragma unroll
-        for (int j = 0; j < SEG; ++j)
-          if (j >= k) r[j] = __shfl_sync(0xffffffffu, r[j], src, SEG);
+        __syncwarp();
         float u[SEG];
 #pragma unroll
+        for (int q = 0; q < SEG / 4; ++q)
+          if (4 * q + 3 >= k) {
+            const float4 v = *reinterpret_cast<const float4*>(rb + 4 * q);
+            u[4 * q] = v.x; u[4 * q + 1] = v.y; u[4 * q + 2] = v.z; u[4 * q + 3] = v.w;
+          }
+        const float ukk = u[k];
+#pragma unroll
         for (int j = 0; j < SEG; ++j)
-          if (j >= k) u[j] = __shfl_sync(0xffffffffu, r[j], k, SEG);
-        if (i > k && i < n && u[k] != 0.f) {
-          const float l = r[k] / u[k];
+          if (j >= k) umax = fmaxf(umax, fabsf(u[j]));
+        if (ukk == 0.f) sing = 1;
+        if (ukk < 0.f) sg = -sg;
+        int e2;
+        mant = frexpf(mant * fabsf(ukk), &e2);
+        ex += e2;
+        if (cand && ukk != 0.f) {
+          const float l = r[k] / ukk;
 #pragma unroll
           for (int j = 0; j < SEG; ++j)
             if (j > k) r[j] = fmaf(-l, u[j], r[j]);
         }
       }
     }
-    // diagonal of U sits in r[i] of lane i
-    float d = (i < n) ? r[i] : 1.f;
-    float umax = 0.f;
-#pragma unroll
-    for (int j = 0; j < SEG; ++j)
-      if (j >= i && i < n) umax = fmaxf(umax, fabsf(r[j]));
-    double la = (d != 0.f) ? (double)logf(fabsf(d)) : 0.0;
-    int neg = d < 0.f ? 1 : 0, zero = d == 0.f ? 1 : 0;
-#pragma unroll
-    for (int o = SEG / 2; o > 0; o >>= 1) {
-      umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o, SEG));
-      la += __shfl_xor_sync(0xffffffffu, la, o, SEG);
-      neg += __shfl_xor_sync(0xffffffffu, neg, o, SEG);
-      zero += __shfl_xor_sync(0xffffffffu, zero, o, SEG);
-    }
-    (void)seg_mask;
+    if (inversions & 1) sg = -sg;
     if (active && i == 0) {
-      const bool sing = zero > 0;
-      lds[mloc] = sing ? -INFINITY : la;
-      sgs[mloc] = sing ? 0.f : ((neg & 1) ? -sg : sg);
+      lds[mloc] = sing ? -INFINITY : (double)logf(mant) + (double)ex * 0.69314718055994530942;
+      sgs[mloc] = sing ? 0.f : sg;
       singular[mloc] = sing;
-      redo[mloc] = (!sing && !(umax <= kRefactorGrowth * amax)) ? 1 : 0;
+      const int rd = (!sing && !(umax <= kRefactorGrowth * amax)) ? 1 : 0;
+      redo[mloc] = rd;
+      my_redo |= rd;
     }
   }
-  __syncthreads();
   // rare: FP64 re-factorisation of matrices with large pivot growth
-  if (warp == 0) {
-    for (int mloc = 0; mloc < nmat; ++mloc) {
-      const int w = w0 + mloc / K;
-      if (w >= B || !redo[mloc]) continue;
-      float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
-      if (env.env) {  // the FP64 pass reads the matrix with its envelope factors
-        const float* Em = env.env + ((size_t)w * K + (mloc % K)) * n * n;
-        for (int e = lane; e < n * n; e += 32) Am[e] *= Em[e];
+  if (__syncthreads_or(my_redo)) {
+    if (warp == 0) {
+      for (int mloc = 0; mloc < nmat; ++mloc) {
+        const int w = w0 + mloc / K;
+        if (w >= B || !redo[mloc]) continue;
+        float* Am = A + ((size_t)w * K + (mloc % K)) * n * n;
+        if (env.env) {  // the FP64 pass reads the matrix with its envelope factors
+          const float* Em = env.env + ((size_t)w * K + (mloc % K)) * n * n;
+          for (int e = lane; e < n * n; e += 32) Am[e] *= Em[e];
+          __syncwarp();
+        }
+        DetOut o = det_stage<double, 16>(Am, n, 1, scratch, nullptr, true);
+        if (lane == 0) {
+          lds[mloc] = o.ld;
+          sgs[mloc] = o.singular ? 0.f : o.sgn;
+          singular[mloc] = o.singular;
+        }
         __syncwarp();
       }
-      DetOut o = det_stage<double, 16>(Am, n, 1, scratch, nullptr, true);
-      if (lane == 0) {
-        lds[mloc] = o.ld;
-        sgs[mloc] = o.singular ? 0.f : o.sgn;
-        singular[mloc] = o.singular;
-      }
-      __syncwarp();
     }
+    __syncthreads();
   }
-  __syncthreads();
-  // FP64 signed log-sum-exp per walker, one warp per walker
+  // signed log-sum-exp per walker, one warp per walker: FP64 determinant
+  // logs and sum, FP32 exponentials of the (non-positive) differences
   for (int wl = warp; wl < WB; wl += 8) {
     const int w = w0 + wl;
     if (w >= B) break;
@@ -1269,7 +1432,7 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
     double S = 0.0;
     int anyredo = 0, anysing = 0;
     for (int k = lane; k < K; k += 32) {
-      if (sgw[k] != 0.f) S += (double)sgw[k] * exp(ldw[k] - lmax);
+      if (sgw[k] != 0.f) S += (double)(sgw[k] * expf((float)(ldw[k] - lmax)));
       anyredo |= redo[wl * K + k];
       anysing |= singular[wl * K + k];
     }
@@ -1277,7 +1440,8 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
     anyredo = __any_sync(0xffffffffu, anyredo);
     anysing = __any_sync(0xffffffffu, anysing);
     if (lane == 0) {
-      double lp = log(fabs(S)) + lmax;
+      const double aS = fabs(S);
+      double lp = (aS > 1e-30 ? (double)logf((float)aS) : log(aS)) + lmax;
       if (logpsi) logpsi[w] = (float)lp;
       if (sign) sign[w] = S > 0 ? 1.f : (S < 0 ? -1.f : 0.f);
       if (flags)
@@ -1294,7 +1458,7 @@ static cudaError_t launch_logdet_value(cudaStream_t s, int B, int n, int K, floa
   const int seg = n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32;
   const int per_pass = 8 * (32 / seg);
   const int WB = std::max(1, per_pass / K);
-  const size_t sm = align_up((size_t)WB * K * 20, 16) + DetScratch(n).bytes;
+  const size_t sm = align_up((size_t)WB * K * 20, 16) + 8 * 64 * sizeof(float) + DetScratch(n).bytes;
   const unsigned grid = (unsigned)((B + WB - 1) / WB);
   switch (seg) {
     case 4: k_logdet_value<4><<<grid, 256, sm, s>>>(B, n, K, WB, A, logpsi, sign, flags, env); break;
