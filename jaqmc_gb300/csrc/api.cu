@@ -167,6 +167,7 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
   }
   for (int s = 0; s < nch; ++s) a->t_orb[s] = takeb(2 * (size_t)d.norb * d.d_last);
   a->t0_pad = takeb(2 * (size_t)d.d1[0] * a->k0w);
+  for (int l = 0; l < d.L; ++l) a->pfrag[l] = d.upd2[l] ? takeb(256 * 8) : 0;
   a->total_bf16 = b;
 }
 
@@ -281,6 +282,7 @@ static qmc_status run_pair_stream(qmc_model* m, const Plan& p, void* ws, cudaStr
   for (int l = 0; l < a.nl; ++l) {
     a.din[l] = d.d2_in[l];
     a.W[l] = ar + m->a.w2[l];
+    a.Wf[l] = reinterpret_cast<const uint4*>(m->arena_bf16 + m->a.pfrag[l]);
     a.b[l] = ar + m->a.b2[l];
     a.g2p[l] = d.g2_p[l + 1];
     char* base = static_cast<char*>(ws) + stream_g2(p, l + 1);
@@ -833,6 +835,9 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
                              sizeof(float) * k2 * d1, cudaMemcpyDeviceToDevice, s));
     QMC_CUDA(launch_transpose_split(s, ar + a.w0_pad, a.k0w, d1, d1, m->arena_bf16 + a.t0_pad, a.k0w, d1));
   }
+  for (int l = 0; l < d.L; ++l)
+    if (d.upd2[l] && d.d2[l] == 32 && d.d2_in[l] <= 32)
+      QMC_CUDA(launch_pair_frags(s, ar + a.w2[l], d.d2_in[l], reinterpret_cast<uint4*>(m->arena_bf16 + a.pfrag[l])));
   m->params_set = true;
   return QMC_OK;
 }

@@ -82,6 +82,9 @@ struct ArenaLayout {
   // bf16 planes [d1][k0w]
   size_t w0_pad, t0_pad;
   int k0w;
+  // 32-wide two-electron layers as split-BF16 m16n8k16 B fragments
+  // (bf16 offsets; 256 x 16 bytes per layer, in per-lane order)
+  size_t pfrag[QMC_MAX_LAYERS];
   size_t total_bf16;
 };
 

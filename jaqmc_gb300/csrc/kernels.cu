@@ -530,14 +530,186 @@ __global__ void __launch_bounds__(256) k_pair_stream_value(PairStreamArgs a, Pai
 
 size_t pair_stream_smem(int n, int nl) { return sizeof(float) * ((size_t)nl * (32 * 32 + 32) + (size_t)n * n * 36); }
 
+// ---------------------------------------------------------------------
+// Mixed form of the same stream on the tensor cores: every 32-wide pair
+// layer of a 16-pair tile is a 16 x 32 x K product done by warp-level
+// m16n8k16 BF16 MMAs, each operand split into hi + lo BF16 parts
+// (lo*hi + hi*lo + hi*hi, FP32 accumulation), like the split-BF16 one-electron
+// layers.  The layers are a chain of tiny products whose operands live in
+// registers: an accumulator tile maps element for element onto the next
+// layer's A operand, so no shared-memory operand staging is needed.  The
+// activations pass through shared memory only for the spin means between
+// layers.  Fragment layouts (PTX ISA, mma.m16n8k16 .bf16): g = lane / 4,
+// t = lane % 4; A regs (row g | g+8, cols 2t..2t+1 | 2t+8..2t+9), B regs
+// (k 2t..2t+1 | 2t+8..2t+9, col g), C (row g | g+8, cols 2t..2t+1).
+// ---------------------------------------------------------------------
+constexpr int kPairMmaWarps = 8;
+constexpr int kPairRS = 40;  // activation row stride (floats): conflict-free 8-byte fragment accesses
+
+__device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+__device__ __forceinline__ void mma_16816_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void k_pair_frags(const float* __restrict__ W, int din, uint4* __restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 256) return;
+  const int ks = (e >> 7) & 1, nt = (e >> 5) & 3, ln = e & 31;
+  const int col = 8 * nt + (ln >> 2), k0 = 16 * ks + 2 * (ln & 3);
+  auto wv = [&](int k) { return k < din ? W[k * 32 + col] : 0.f; };
+  uint32_t h0, l0, h1, l1;
+  split_bf16x2(wv(k0), wv(k0 + 1), h0, l0);
+  split_bf16x2(wv(k0 + 8), wv(k0 + 9), h1, l1);
+  out[e] = make_uint4(h0, h1, l0, l1);
+}
+
+cudaError_t launch_pair_frags(cudaStream_t s, const float* W, int din, uint4* out) {
+  if (din < 1 || din > 32) return cudaErrorInvalidValue;
+  k_pair_frags<<<1, 256, 0, s>>>(W, din, out);
+  return cudaGetLastError();
+}
+
+static size_t pair_stream_mma_smem(int n, int nl) {
+  const size_t mt = ((size_t)n * n + 15) / 16;
+  return sizeof(uint4) * (size_t)nl * 256 + sizeof(float) * ((size_t)nl * 32 + mt * 16 * kPairRS);
+}
+
+__global__ void __launch_bounds__(kPairMmaWarps * 32, 4) k_pair_stream_mma(PairStreamArgs a, PairStreamOut<StSplit> o) {
+  extern __shared__ uint4 shq[];
+  uint4* Wf = shq;                                          // [nl][ks 2][nt 4][lane 32] {b0 hi, b1 hi, b0 lo, b1 lo}
+  float* bs = reinterpret_cast<float*>(Wf + a.nl * 256);   // [nl][32]
+  float* Os = bs + a.nl * 32;                               // [tiles * 16][kPairRS]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int n = a.n, np = n * n, mt = (np + 15) / 16, w = blockIdx.x;
+  for (int e = threadIdx.x; e < a.nl * 256; e += blockDim.x) Wf[e] = __ldg(a.Wf[e >> 8] + (e & 255));
+  for (int e = threadIdx.x; e < a.nl * 32; e += blockDim.x) bs[e] = a.b[e >> 5][e & 31];
+  __syncthreads();
+  for (int l = 0; l < a.nl; ++l) {
+    const uint4* Wl = Wf + l * 256;
+    const float* bl = bs + l * 32;
+    const int din = a.din[l];
+    const int nks = din > 16 ? 2 : 1;
+    float2 bias[4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) bias[nt] = *reinterpret_cast<const float2*>(bl + 8 * nt + 2 * t);
+    for (int tile = warp; tile < mt; tile += kPairMmaWarps) {
+      const int r0 = tile * 16 + g, r1 = r0 + 8;
+      // x[ks] = {(r0, c), (r0, c+1), (r1, c), (r1, c+1), (r0, c+8), (r0, c+9), (r1, c+8), (r1, c+9)},
+      // c = 16 ks + 2t: the A operand and, for 32-wide inputs, the residual
+      float x[2][8];
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int r = (q & 1) ? r1 : r0;
+          const int c = 16 * ks + 2 * t + ((q & 2) ? 8 : 0);
+          float2 v = make_float2(0.f, 0.f);
+          if (ks < nks) {
+            if (l == 0) {
+              if (r < np && c < din)
+                v = __ldg(reinterpret_cast<const float2*>(a.H0 + ((size_t)w * np + r) * din + c));
+            } else {
+              v = *reinterpret_cast<const float2*>(Os + r * kPairRS + c);
+            }
+          }
+          x[ks][2 * q] = v.x;
+          x[ks][2 * q + 1] = v.y;
+        }
+      }
+      uint32_t ahi[2][4], alo[2][4];
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) split_bf16x2(x[ks][2 * q], x[ks][2 * q + 1], ahi[ks][q], alo[ks][q]);
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        float acc[4];
+        acc[0] = acc[2] = bias[nt].x;
+        acc[1] = acc[3] = bias[nt].y;
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+          if (ks < nks) {
+            const uint4 bw = Wl[(ks * 4 + nt) * 32 + lane];
+            mma_16816_bf16(acc, alo[ks], bw.x, bw.y);
+            mma_16816_bf16(acc, ahi[ks], bw.z, bw.w);
+            mma_16816_bf16(acc, ahi[ks], bw.x, bw.y);
+          }
+        }
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) v[e] = pair_tanh<true>(acc[e]);
+        if (din == 32) {
+          // the input at this output's position: k-slice nt / 2, column half nt % 2
+          const float* xr = &x[nt >> 1][(nt & 1) * 4];
+          v[0] = (v[0] + xr[0]) * kRsqrt2;
+          v[1] = (v[1] + xr[1]) * kRsqrt2;
+          v[2] = (v[2] + xr[2]) * kRsqrt2;
+          v[3] = (v[3] + xr[3]) * kRsqrt2;
+        }
+        *reinterpret_cast<float2*>(Os + r0 * kPairRS + 8 * nt + 2 * t) = make_float2(v[0], v[1]);
+        *reinterpret_cast<float2*>(Os + r1 * kPairRS + 8 * nt + 2 * t) = make_float2(v[2], v[3]);
+      }
+    }
+    __syncthreads();
+    // <h2>_s[i] = mean over a in channel s of h2[a, i]  (first index
+    // averaged): one (i, feature) per thread, both channels in one pass
+    const int g2p = a.g2p[l];
+    for (int e = threadIdx.x; e < n * 32; e += blockDim.x) {
+      const int i = e >> 5, f = e & 31;
+      const size_t row = (size_t)w * n + i;
+      if (a.C == 1) {
+        float acc = 0.f;
+        for (int aa = 0; aa < n; ++aa) acc += Os[(aa * n + i) * kPairRS + f];
+        o.G2[l].put(row, f, acc / (float)n);
+      } else {
+        float s0 = 0.f, s1 = 0.f;
+        for (int aa = 0; aa < a.n_up; ++aa) s0 += Os[(aa * n + i) * kPairRS + f];
+        for (int aa = a.n_up; aa < n; ++aa) s1 += Os[(aa * n + i) * kPairRS + f];
+        o.G2[l].put(row, f, s0 / (float)a.n_up);
+        o.G2[l].put(row, 32 + f, s1 / (float)(n - a.n_up));
+      }
+    }
+    const int padc = g2p - a.C * 32;  // zero padding columns
+    for (int e = threadIdx.x; e < n * padc; e += blockDim.x)
+      o.G2[l].put((size_t)w * n + e / padc, a.C * 32 + e % padc, 0.f);
+    __syncthreads();
+  }
+}
+
 template <class Out>
 cudaError_t launch_pair_stream_value(cudaStream_t s, int B, const PairStreamArgs& a, const PairStreamOut<Out>& o) {
-  const size_t sm = pair_stream_smem(a.n, a.nl);
-  if (sm > 200 * 1024 || a.nl < 1 || a.nl > kPairStreamMax) return cudaErrorNotSupported;
-  static int attr_dev = -1;
+  if (a.nl < 1 || a.nl > kPairStreamMax) return cudaErrorNotSupported;
   int dev;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  if constexpr (std::is_same<Out, StSplit>::value) {
+    bool ok = pair_stream_mma_smem(a.n, a.nl) <= 200 * 1024;
+    for (int l = 0; l < a.nl; ++l) ok = ok && (a.din[l] == 32 || (a.din[l] == 4 && l == 0));
+    if (ok) {
+      static int mma_dev = -1;
+      if (mma_dev != dev) {
+        e = cudaFuncSetAttribute(k_pair_stream_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        mma_dev = dev;
+      }
+      k_pair_stream_mma<<<B, kPairMmaWarps * 32, pair_stream_mma_smem(a.n, a.nl), s>>>(a, o);
+      return cudaGetLastError();
+    }
+  }
+  const size_t sm = pair_stream_smem(a.n, a.nl);
+  if (sm > 200 * 1024) return cudaErrorNotSupported;
+  static int attr_dev = -1;
   if (attr_dev != dev) {
     e = cudaFuncSetAttribute(k_pair_stream_value<Out>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;

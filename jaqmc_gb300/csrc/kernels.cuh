@@ -79,12 +79,16 @@ struct PairStreamArgs {
   const float* b[kPairStreamMax];           // [32]
   const float* H0;                          // [B][n][n][din[0]] pair features
   int g2p[kPairStreamMax];                  // padded width of the means after layer l
+  const uint4* Wf[kPairStreamMax];          // split-BF16 fragments of W (mixed form), launch_pair_frags
 };
 template <class Out>
 struct PairStreamOut {
   Out G2[kPairStreamMax];                   // means after pair layer l (input of layer l+1)
 };
 size_t pair_stream_smem(int n, int nl);
+// B fragments of one 32-wide pair layer W [din][32] (din <= 32) for the
+// mixed-form stream: out[ks][nt][lane] = {b0 hi, b1 hi, b0 lo, b1 lo}.
+cudaError_t launch_pair_frags(cudaStream_t s, const float* W, int din, uint4* out);
 template <class Out>
 cudaError_t launch_pair_stream_value(cudaStream_t s, int B, const PairStreamArgs& a, const PairStreamOut<Out>& o);
 
