@@ -36,6 +36,17 @@ __host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m *
 __host__ __device__ inline size_t align_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
 constexpr float kRsqrt2 = 0.70710678118654752440f;
+
+// Orbital matrices A (row i = electron, column j = orbital, determinant k).
+// Value passes (Tp == 1): A[w][k][i][j].  Tangent passes: A[w][t][i][k][j],
+// so the K*n columns (k, j) of one electron row and tangent are contiguous
+// (a warp's output columns store as one run); a matrix then has row stride
+// K*n and tangent stride n*K*n.
+__host__ __device__ inline size_t amat_index(int Tp, int n, int K, size_t w, int k, int t, int i, int j) {
+  return Tp == 1 ? ((w * K + k) * n + i) * (size_t)n + j : (((w * Tp + t) * n + i) * (size_t)K + k) * n + j;
+}
+__host__ __device__ inline int amat_row_stride(int Tp, int n, int K) { return Tp == 1 ? n : K * n; }
+__host__ __device__ inline size_t amat_tangent_stride(int n, int K) { return (size_t)n * K * n; }
 constexpr int kMaxAtoms = 64;
 
 // ---------------------------------------------------------------- model

@@ -89,7 +89,7 @@ struct EpiLayer {
 };
 
 // Orbitals x envelope with the product rule; writes the orbital matrices
-// A[w][k][t][i][j] (fp32).  Columns are (k, j) = k*n + j.
+// (fp32, layout of amat_index).  Columns are (k, j) = k*n + j.
 struct EpiOrbital {
   float* A;
   const float* rae;    // [walkers*n][A]
@@ -131,11 +131,11 @@ struct EpiOrbital {
         }
       }
       const float* cs = Cs + (lg * Tp) * kCsLd + c;
-      float* dst = A + (((size_t)w * K + k) * Tp) * n * n + (size_t)i * n + j;
-      const size_t ts = (size_t)n * n;
+      float* dst = A + amat_index(Tp, n, K, w, k, 0, i, j);
+      const size_t ts = amat_tangent_stride(n, K);
       float o0 = cs[0];
       dst[0] = o0 * e0;
-      if (orb) orb[(((size_t)w * K + k) * Tp) * n * n + (size_t)i * n + j] = o0;
+      if (orb) orb[amat_index(1, n, K, w, k, 0, i, j)] = o0;
       if (T > 1) {
         int ti = 2 + 3 * i;
         for (int t = 2; t < T; ++t) {

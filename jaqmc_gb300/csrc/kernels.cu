@@ -1139,13 +1139,13 @@ __device__ void warp_inverse(const S* LU, S* Ainv, const int* perm, int n, int l
 // held in registers, rows of A^-1 read as float4 broadcasts.
 template <int NMAX>
 __device__ float warp_product_f32(const float* Ainv, const float* __restrict__ At, float* Ms, int n,
-                                  int ld, int ldm) {
+                                  int ld, int ldm, int rs) {
   const int lane = threadIdx.x & 31;
   float tr = 0.f;
   for (int j = lane; j < n; j += 32) {
     float x[NMAX];
 #pragma unroll
-    for (int m = 0; m < NMAX; ++m) x[m] = m < n ? At[m * n + j] : 0.f;
+    for (int m = 0; m < NMAX; ++m) x[m] = m < n ? At[m * rs + j] : 0.f;
 #pragma unroll 4
     for (int i = 0; i < n; ++i) {
       const float4* a4 = reinterpret_cast<const float4*>(Ainv + i * ld);
@@ -1171,9 +1171,9 @@ __device__ float warp_product_f32(const float* Ainv, const float* __restrict__ A
 
 // FP64 variant (re-factorised determinants only): A_t staged in shared memory.
 __device__ double warp_product_f64(const double* Ainv, const float* __restrict__ At, double* Ms,
-                                   double* Xs, int n, int ld, int ldm) {
+                                   double* Xs, int n, int ld, int ldm, int rs) {
   const int lane = threadIdx.x & 31;
-  for (int e = lane; e < n * n; e += 32) Xs[(e / n) * ldm + (e % n)] = (double)At[e];
+  for (int e = lane; e < n * n; e += 32) Xs[(e / n) * ldm + (e % n)] = (double)At[(e / n) * rs + (e % n)];
   __syncwarp();
   double tr = 0.0;
   for (int j = lane; j < n; j += 32) {
@@ -1211,7 +1211,7 @@ __device__ S warp_trace_sq(const S* Ms, int n, int ldm) {
 // more shared-memory loads per row, which measured slower.)
 template <int NMAX>
 __device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak, int n, int T, size_t ts,
-                                 int ld, int ldm, float* Ms, float* t1s, DetOut& o) {
+                                 int rs, int ld, int ldm, float* Ms, float* t1s, DetOut& o) {
   static_assert(NMAX <= 16 && NMAX % 4 == 0, "half-warp columns");
   const int lane = threadIdx.x & 31;
   const int h = lane >> 4, j = lane & 15;
@@ -1222,7 +1222,7 @@ __device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak
     float acc = 0.f;
     for (int e = lane; e < n * n; e += 32) {
       const int m = e / n, i = e - m * n;
-      acc = fmaf(Ainv[i * ld + m], L[e], acc);
+      acc = fmaf(Ainv[i * ld + m], L[m * rs + i], acc);
     }
     o.tL = warp_sum(acc);
   }
@@ -1238,8 +1238,8 @@ __device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak
     const bool va = colv && da < D, vb = colv && db < D;
 #pragma unroll
     for (int m = 0; m < NMAX; ++m) {
-      xa[m] = (va && m < n) ? __ldg(Ja + m * n + j) : 0.f;
-      xb[m] = (vb && m < n) ? __ldg(Jb + m * n + j) : 0.f;
+      xa[m] = (va && m < n) ? __ldg(Ja + m * rs + j) : 0.f;
+      xb[m] = (vb && m < n) ? __ldg(Jb + m * rs + j) : 0.f;
     }
   };
   const int G = (D + 3) / 4;
@@ -1313,8 +1313,9 @@ __device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak
 // Factorise determinant k of a walker and, for T > 1, the slogdet traces
 //   tL = tr(A^-1 L_A),  t1_d = tr(A^-1 J_d A),  t2 = sum_d tr((A^-1 J_d A)^2),
 //   q = sum_d t1_d^2.
+// Ak: the matrix (row stride rs floats); tangent t at Ak + t * ts.
 template <typename S, int NMAX>
-__device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* scratch,
+__device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, char* scratch,
                             float* t1s, bool fp64_pass) {
   const int lane = threadIdx.x & 31;
   const DetScratch sc(n);
@@ -1324,9 +1325,8 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* sc
   S* Ms = Ainv + n * ld;
   S* Xs = Ms + n * ldm;
   int* perm = reinterpret_cast<int*>(scratch + (size_t)(2 * n * ld + 2 * n * ldm) * 8);
-  const size_t ts = (size_t)n * n;
   DetOut o{};
-  for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (S)Ak[e];
+  for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (S)Ak[(e / n) * rs + (e % n)];
   __syncwarp();
   double growth;
   warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular);
@@ -1334,7 +1334,7 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* sc
   if (T <= 1 || o.singular || o.refactor) return o;
   warp_inverse<S>(LU, Ainv, perm, n, ld);
   if constexpr (sizeof(S) == 4 && NMAX <= 16) {
-    det_tangents_f32<NMAX>(reinterpret_cast<const float*>(Ainv), Ak, n, T, ts, ld, ldm,
+    det_tangents_f32<NMAX>(reinterpret_cast<const float*>(Ainv), Ak, n, T, ts, rs, ld, ldm,
                            reinterpret_cast<float*>(Ms), t1s, o);
     return o;
   }
@@ -1342,8 +1342,8 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, char* sc
   for (int t = 1; t < T; ++t) {
     const float* At = Ak + (size_t)t * ts;
     S tr;
-    if constexpr (sizeof(S) == 4) tr = warp_product_f32<NMAX>(Ainv, At, Ms, n, ld, ldm);
-    else tr = warp_product_f64(Ainv, At, Ms, Xs, n, ld, ldm);
+    if constexpr (sizeof(S) == 4) tr = warp_product_f32<NMAX>(Ainv, At, Ms, n, ld, ldm, rs);
+    else tr = warp_product_f64(Ainv, At, Ms, Xs, n, ld, ldm, rs);
     if (t == 1) {
       o.tL = (float)tr;
     } else {
@@ -1382,11 +1382,13 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   if (threadIdx.x < 2) ints[threadIdx.x] = 0;
   __syncthreads();
   for (int k = warp; k < K; k += nw) {
-    const float* Ak = A + ((size_t)w * K + k) * Tp * n * n;
+    const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
+    const int rs = amat_row_stride(Tp, n, K);
+    const size_t ts = amat_tangent_stride(n, K);
     float* t1k = t1s + (size_t)k * D;
-    DetOut o = det_stage<float, NMAX>(Ak, n, T, scratch, t1k, false);
+    DetOut o = det_stage<float, NMAX>(Ak, n, T, rs, ts, scratch, t1k, false);
     if (o.refactor) {
-      o = det_stage<double, NMAX>(Ak, n, T, scratch, t1k, true);
+      o = det_stage<double, NMAX>(Ak, n, T, rs, ts, scratch, t1k, true);
       o.refactor = 1;
     }
     if (lane == 0) {
@@ -1579,7 +1581,7 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
           for (int e = lane; e < n * n; e += 32) Am[e] *= Em[e];
           __syncwarp();
         }
-        DetOut o = det_stage<double, 16>(Am, n, 1, scratch, nullptr, true);
+        DetOut o = det_stage<double, 16>(Am, n, 1, n, (size_t)n * n, scratch, nullptr, true);
         if (lane == 0) {
           lds[mloc] = o.ld;
           sgs[mloc] = o.singular ? 0.f : o.sgn;

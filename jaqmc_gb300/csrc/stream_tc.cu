@@ -568,7 +568,7 @@ struct EpiTcOrbital {
   __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t*) const {
     const bool fok = f < g.n_out;
     const int k = fok ? f / n : 0, j = fok ? f % n : 0;
-    const size_t ts = (size_t)n * n;
+    const size_t ts = amat_tangent_stride(n, K);
     EnvParams ep;
     load_params(ti.a_sel, k, j, ep);
     if (g.T == 1) {
@@ -581,7 +581,7 @@ struct EpiTcOrbital {
 #pragma unroll
         for (int jj = 0; jj < 16; ++jj) {
           if (c0 + jj < ti.ng && (!split || (i < n_up ? 0 : 1) == ti.a_sel)) {
-            const size_t idx = ((size_t)w * K + k) * ts + (size_t)i * n + j;
+            const size_t idx = amat_index(1, n, K, w, k, 0, i, j);
             if (raw) {
               A[idx] = v[jj];
             } else {
@@ -602,36 +602,35 @@ struct EpiTcOrbital {
       const int i = ti.i0 + lg;
       float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
       if (fok) envelope(ti.a_sel, ti.w, i, k, j, g.T, e, ep);
-      float* dst = A + (((size_t)ti.w * K + k) * g.Tp) * ts + (size_t)i * n + j;
+      float* dst = A + amat_index(g.Tp, n, K, ti.w, k, 0, i, j);
       const int ti3 = 2 + 3 * i;
-      float o0 = 0.f, oL = 0.f, cross = 0.f;
+      const uint32_t col0 = taddr + lg * g.Tp;
+      // pass 1: every tangent row as o_t e (rows >= T padded with zeros); the
+      // Laplacian row and electron i's own three gradient rows are rewritten
+      // in pass 2 with their product-rule terms
       for (int q4 = 0; q4 < g.Tp / 4; ++q4) {
         float v[4];
-        ptx::tmem_ld4(taddr + lg * g.Tp + 4 * q4, v);
+        ptx::tmem_ld4(col0 + 4 * q4, v);
         if (!fok) continue;
+        float* d4 = dst + (size_t)(4 * q4) * ts;
 #pragma unroll
-        for (int ee = 0; ee < 4; ++ee) {
-          const int t = 4 * q4 + ee;
-          const float o = v[ee];
-          if (t == 0) {
-            o0 = o;
-            dst[0] = o * e[0];
-          } else if (t == 1) {
-            oL = o;
-          } else if (t < g.T) {
-            float val = o * e[0];
-            int c = t - ti3;
-            if (c >= 0 && c < 3) {
-              val = fmaf(o0, e[1 + c], val);
-              cross = fmaf(o, e[1 + c], cross);
-            }
-            dst[(size_t)t * ts] = val;
-          } else {
-            dst[(size_t)t * ts] = 0.f;
-          }
-        }
+        for (int ee = 0; ee < 4; ++ee) d4[ee * ts] = (4 * q4 + ee < g.T) ? v[ee] * e[0] : 0.f;
       }
-      if (fok) dst[ts] = oL * e[0] + 2.0f * cross + o0 * e[4];
+      // pass 2: value o_0 and Laplacian o_L (columns 0, 1) and o_c of the
+      // gradient rows ti3 + c: grad row = o_c e + o_0 de_c,
+      // Laplacian = o_L e + 2 sum_c o_c de_c + o_0 lap e
+      float v01[4], oc[3];
+      ptx::tmem_ld4_ld1x3(col0, col0 + ti3, col0 + ti3 + 1, col0 + ti3 + 2, v01, oc);
+      if (fok) {
+        const float o0 = v01[0], oL = v01[1];
+        float cross = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          dst[(size_t)(ti3 + c) * ts] = fmaf(o0, e[1 + c], oc[c] * e[0]);
+          cross = fmaf(oc[c], e[1 + c], cross);
+        }
+        dst[ts] = oL * e[0] + 2.0f * cross + o0 * e[4];
+      }
     }
   }
 };

@@ -124,6 +124,24 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
   v[2] = __uint_as_float(r2);
   v[3] = __uint_as_float(r3);
 }
+// One 4-column load and three single-column loads (any columns), one wait.
+__device__ __forceinline__ void tmem_ld4_ld1x3(uint32_t a4, uint32_t c0, uint32_t c1, uint32_t c2, float* v4,
+                                               float* v3) {
+  uint32_t r[7];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%7];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%4}, [%8];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%5}, [%9];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%6}, [%10];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6])
+      : "r"(a4), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v4[q] = __uint_as_float(r[q]);
+#pragma unroll
+  for (int q = 0; q < 3; ++q) v3[q] = __uint_as_float(r[4 + q]);
+}
 // 16-byte global -> shared copy that bypasses the registers (and L1).
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
