@@ -754,8 +754,90 @@ template cudaError_t launch_pair_layer_mean<StF32>(cudaStream_t, int, int, int, 
 template cudaError_t launch_pair_layer_mean<StSplit>(cudaStream_t, int, int, int, int, int, int, const float*,
                                                      const float*, const float*, float*, int, StSplit);
 
+// Tangent form (P2 = 5 planes: value, Laplacian, three gradient components),
+// 32 outputs: 32 pairs per block, each thread four features of one pair, so
+// every 4 inputs cost 5 + 4 16-byte shared loads for 80 FMAs and the outputs
+// leave as 16-byte stores.  Same arithmetic order per output as k_pair_layer.
+template <int DIN>
+__global__ void __launch_bounds__(256) k_pair_layer_t5(int npairs, const float* __restrict__ Hin,
+                                                       const float* __restrict__ W, const float* __restrict__ b,
+                                                       float* __restrict__ Hout) {
+  constexpr int P2 = 5, DO = 32, PPB = 32;
+  constexpr int IS = P2 * DIN + 4;  // per-pair stride (floats): four pairs per warp on distinct banks
+  __shared__ __align__(16) float Ws[DIN * DO];
+  __shared__ __align__(16) float Is[PPB * IS];
+  for (int e = threadIdx.x; e < DIN * DO; e += blockDim.x) Ws[e] = W[e];
+  const int p0 = blockIdx.x * PPB;
+  const int np = min(PPB, npairs - p0);
+  constexpr int V4 = P2 * DIN / 4;  // float4 per pair
+  const float4* src = reinterpret_cast<const float4*>(Hin + (size_t)p0 * P2 * DIN);
+  for (int e = threadIdx.x; e < np * V4; e += blockDim.x) {
+    const int pr = e / V4, q = e - pr * V4;
+    *reinterpret_cast<float4*>(Is + pr * IS + 4 * q) = __ldg(src + e);
+  }
+  __syncthreads();
+  const int lp = threadIdx.x >> 3, f0 = 4 * (threadIdx.x & 7);
+  if (lp >= np) return;
+  const float* in = Is + lp * IS;
+  float z[P2][4];
+#pragma unroll
+  for (int p = 0; p < P2; ++p)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) z[p][c] = 0.f;
+#pragma unroll
+  for (int k0 = 0; k0 < DIN; k0 += 4) {
+    float4 x[P2];
+#pragma unroll
+    for (int p = 0; p < P2; ++p) x[p] = *reinterpret_cast<const float4*>(in + p * DIN + k0);
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const float4 w = *reinterpret_cast<const float4*>(Ws + (k0 + kk) * DO + f0);
+#pragma unroll
+      for (int p = 0; p < P2; ++p) {
+        const float xv = kk == 0 ? x[p].x : kk == 1 ? x[p].y : kk == 2 ? x[p].z : x[p].w;
+        z[p][0] = fmaf(xv, w.x, z[p][0]);
+        z[p][1] = fmaf(xv, w.y, z[p][1]);
+        z[p][2] = fmaf(xv, w.z, z[p][2]);
+        z[p][3] = fmaf(xv, w.w, z[p][3]);
+      }
+    }
+  }
+  float out[P2][4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float h = tanhf(z[0][c] + b[f0 + c]);
+    const float d1 = 1.f - h * h, d2 = -2.f * h * d1;
+    const float S = z[2][c] * z[2][c] + z[3][c] * z[3][c] + z[4][c] * z[4][c];
+    out[0][c] = h;
+    out[1][c] = d1 * z[1][c] + d2 * S;
+    out[2][c] = d1 * z[2][c];
+    out[3][c] = d1 * z[3][c];
+    out[4][c] = d1 * z[4][c];
+  }
+  float* o = Hout + (size_t)(p0 + lp) * P2 * DO + f0;
+#pragma unroll
+  for (int p = 0; p < P2; ++p) {
+    float4 v = make_float4(out[p][0], out[p][1], out[p][2], out[p][3]);
+    if (DIN == DO) {
+      const float4 r = *reinterpret_cast<const float4*>(in + p * DIN + f0);
+      v.x = (v.x + r.x) * kRsqrt2;
+      v.y = (v.y + r.y) * kRsqrt2;
+      v.z = (v.z + r.z) * kRsqrt2;
+      v.w = (v.w + r.w) * kRsqrt2;
+    }
+    *reinterpret_cast<float4*>(o + p * DO) = v;
+  }
+}
+
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout) {
+  if (P2 == 5 && d_out == 32 && (d_in == 4 || d_in == 32) && ((uintptr_t)Hin & 15) == 0 &&
+      ((uintptr_t)Hout & 15) == 0) {
+    const unsigned grid = (unsigned)((npairs + 31) / 32);
+    if (d_in == 4) k_pair_layer_t5<4><<<grid, 256, 0, s>>>(npairs, Hin, W, b, Hout);
+    else k_pair_layer_t5<32><<<grid, 256, 0, s>>>(npairs, Hin, W, b, Hout);
+    return cudaGetLastError();
+  }
   if (P2 == 1) {
     const unsigned grid = (unsigned)((npairs + 127) / 128);
     if (d_in == 4 && d_out == 32) {
@@ -850,15 +932,17 @@ static bool vec8_ok(const StSplit& X) {
 
 // Spin means of 8 features per thread: all electron rows of a batch are
 // loaded (16-byte vectors) before they are summed.
+// (32-bit index arithmetic: the launcher keeps B * Tp * g1p / 8 below 2^31)
 template <class In, class Out>
 __global__ void k_mean_h1_vec(int B, int n, int n_up, int C, int Tp, int d, In X, int g1p, Out G1) {
-  const int nv = g1p / 8;
-  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)B * Tp * nv) return;
-  const int col = 8 * (int)(e % nv);
-  const size_t wt = e / nv;
-  const int t = (int)(wt % Tp);
-  const int w = (int)(wt / Tp);
+  const unsigned nv = (unsigned)g1p / 8u;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (unsigned)B * (unsigned)Tp * nv) return;
+  const unsigned wt32 = e / nv;
+  const int col = 8 * (int)(e - wt32 * nv);
+  const size_t wt = wt32;
+  const int w = (int)(wt32 / (unsigned)Tp);
+  const int t = (int)(wt32 - (unsigned)w * (unsigned)Tp);
   float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (col < C * d) {
     const int s = col / d, f = col % d;
@@ -886,7 +970,7 @@ __global__ void k_mean_h1_vec(int B, int n, int n_up, int C, int Tp, int d, In X
 template <class In, class Out>
 cudaError_t launch_mean_h1(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int d, In X, int g1p,
                            Out G1) {
-  if (d % 8 == 0 && g1p % 8 == 0 && vec8_ok(X) && vec8_ok(G1)) {
+  if (d % 8 == 0 && g1p % 8 == 0 && vec8_ok(X) && vec8_ok(G1) && (size_t)B * Tp * (g1p / 8) < (1ull << 31)) {
     const size_t total = (size_t)B * Tp * (g1p / 8);
     k_mean_h1_vec<In, Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, d, X, g1p, G1);
     return cudaGetLastError();
@@ -946,15 +1030,17 @@ __global__ void k_mean_h2(int B, int n, int n_up, int C, int Tp, int T, int d2, 
 template <class Out>
 __global__ void k_mean_h2_vec(int B, int n, int n_up, int C, int Tp, int T, int d2, int P2,
                               const float* __restrict__ H2, int g2p, Out G2) {
-  const int nv = g2p / 8;
-  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)B * n * Tp * nv) return;
-  const int col = 8 * (int)(e % nv);
-  const size_t r = e / nv;
-  const int t = (int)(r % Tp);
-  const size_t wi = r / Tp;
-  const int i = (int)(wi % n);
-  const int w = (int)(wi / n);
+  // 32-bit index arithmetic: the launcher keeps B * n * Tp * g2p / 8 below 2^31
+  const unsigned nv = (unsigned)g2p / 8u;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (unsigned)B * (unsigned)n * (unsigned)Tp * nv) return;
+  const unsigned r32 = e / nv;
+  const int col = 8 * (int)(e - r32 * nv);
+  const size_t r = r32;
+  const unsigned wi = r32 / (unsigned)Tp;
+  const int t = (int)(r32 - wi * (unsigned)Tp);
+  const int w = (int)(wi / (unsigned)n);
+  const int i = (int)(wi - (unsigned)w * (unsigned)n);
   float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (col < C * d2 && t < T) {
     const int sc = col / d2, f = col % d2;
@@ -990,7 +1076,8 @@ __global__ void k_mean_h2_vec(int B, int n, int n_up, int C, int Tp, int T, int 
 template <class Out>
 cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d2,
                            int P2, const float* H2, int g2p, Out G2) {
-  if (d2 % 8 == 0 && g2p % 8 == 0 && ((uintptr_t)H2 & 15) == 0 && vec8_ok(G2)) {
+  if (d2 % 8 == 0 && g2p % 8 == 0 && ((uintptr_t)H2 & 15) == 0 && vec8_ok(G2) &&
+      (size_t)B * n * Tp * (g2p / 8) < (1ull << 31)) {
     const size_t total = (size_t)B * n * Tp * (g2p / 8);
     k_mean_h2_vec<Out><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, n_up, C, Tp, T, d2, P2, H2, g2p, G2);
     return cudaGetLastError();
