@@ -312,6 +312,33 @@ struct EpiTcLayer : ContigTiles {
             *reinterpret_cast<const uint4*>(buf + (pl * kCR + r) * 32 + 8 * vq);
     }
   }
+  // Value-pass staging tiles [2 planes][16 rows][4 pieces of 8 features],
+  // piece p of row r stored at p ^ ((r >> 1) & 3): the eight rows of an 8x8
+  // ldmatrix / stmatrix tile then fall on distinct bank groups.
+  static __device__ __forceinline__ int swz(int r, int p) { return p ^ ((r >> 1) & 3); }
+  __device__ __forceinline__ void fetch_sw(const StSplit& st, size_t row0, int nrows, int col0, int nvec, int lane,
+                                           __nv_bfloat16* buf) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
+      if (r < nrows && vq < nvec)
+        ptx::cp_async16(buf + (pl * kCR + r) * 32 + 8 * swz(r, vq),
+                        st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq);
+    }
+    ptx::cp_async_commit();
+  }
+  __device__ __forceinline__ void store_sw(const StSplit& st, size_t row0, int nrows, int col0, int nvec, int lane,
+                                           const __nv_bfloat16* buf) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
+      if (r < nrows && vq < nvec)
+        *reinterpret_cast<uint4*>(st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq) =
+            *reinterpret_cast<const uint4*>(buf + (pl * kCR + r) * 32 + 8 * swz(r, vq));
+    }
+  }
   __device__ __forceinline__ float get(const __nv_bfloat16* buf, int r, int lane) const {
     return __bfloat162float(buf[r * 32 + lane]) + __bfloat162float(buf[(kCR + r) * 32 + lane]);
   }
@@ -330,42 +357,89 @@ struct EpiTcLayer : ContigTiles {
     const float b = bias[fc];
     __nv_bfloat16* buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * 2 * kBuf;  // value-only layout
     if (g.T == 1) {
+      // Thread T holds features col0 + T/4 + 8 fb (fb = 0..3) of rows
+      // 8 rb + 2(T%4) + {0, 1} (rb = 0, 1) of each 16-row chunk: the 16x256b
+      // TMEM fragment, which ldmatrix / stmatrix (.trans) move to and from the
+      // [row][feature] staging tile.
+      const int T4 = lane >> 2, T2 = 2 * (lane & 3);
+      float bq[4];
+      int Fq[4];
+#pragma unroll
+      for (int fb = 0; fb < 4; ++fb) {
+        Fq[fb] = col0 + T4 + 8 * fb;
+        bq[fb] = Fq[fb] < N ? bias[Fq[fb]] : 0.f;
+      }
       int c0 = 16 * half, k = 0;
       if (c0 >= ti.ng) return;
-      if (RESID) fetch(resid, (size_t)(ti.g0 + c0), min(16, ti.ng - c0), col0, nvec, lane, buf0);
+      const uint32_t tq = taddr;  // lane field: this warp's quarter
+      if (RESID) fetch_sw(resid, (size_t)(ti.g0 + c0), min(16, ti.ng - c0), col0, nvec, lane, buf0);
       for (; c0 < ti.ng; c0 += 32, k ^= 1) {
         __nv_bfloat16* buf = buf0 + k * kBuf;
         const int nrows = min(16, ti.ng - c0);
         const size_t row0 = (size_t)(ti.g0 + c0);
         const bool more = c0 + 32 < ti.ng;
         if (RESID && more)
-          fetch(resid, row0 + 32, min(16, ti.ng - c0 - 32), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
+          fetch_sw(resid, row0 + 32, min(16, ti.ng - c0 - 32), col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
+        // r[4 (2 lh + rb) + q]: lane half lh (features + 16 lh), row block rb
         uint32_t r[16];
-        ptx::tmem_ld16_nw(taddr + c0, r);
-        float gbv[16];
-        int w = (int)(row0 / n), e = (int)(row0 % n);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          gbv[j] = __ldg(Gb + (size_t)w * N + fc);
-          if (++e == n) {
-            e = 0;
-            ++w;
+        for (int lh = 0; lh < 2; ++lh)
+#pragma unroll
+          for (int rb = 0; rb < 2; ++rb)
+            ptx::tmem_ld16x256_nw(tq + ((uint32_t)(16 * lh) << 16) + (uint32_t)(c0 + 8 * rb), r + 4 * (2 * lh + rb));
+        // broadcast terms of the rows' walkers
+        float gb[2][2][4];  // [rb][e][fb]
+#pragma unroll
+        for (int rb = 0; rb < 2; ++rb)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int rr = 8 * rb + T2 + e;
+            const size_t w = (row0 + rr) / (size_t)n;
+#pragma unroll
+            for (int fb = 0; fb < 4; ++fb)
+              gb[rb][e][fb] = (rr < nrows && Fq[fb] < N) ? __ldg(Gb + w * N + Fq[fb]) : 0.f;
           }
-        }
         ptx::tmem_wait16(r);
         if (more) ptx::cp_async_wait<1>();
         else ptx::cp_async_wait<0>();
         __syncwarp();
+        const uint32_t sb = ptx::smem_u32(buf);
+        // tile address of this lane: row 8 rb + (lane % 8) of piece (lane / 8)
+        const int lr = lane & 7, lp = lane >> 3;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          if (j < nrows) {
-            float y = tanhf(__uint_as_float(r[j]) + gbv[j] + b);
-            if (RESID) y = (y + get(buf, j, lane)) * kRsqrt2;
-            put(buf, j, lane, y);
+        for (int rb = 0; rb < 2; ++rb) {
+          const int row = 8 * rb + lr;
+          const uint32_t a_hi = sb + (uint32_t)(((0 * kCR + row) * 32 + 8 * swz(row, lp)) * 2);
+          const uint32_t a_lo = sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2);
+          uint32_t rh[4], rl[4];
+          if (RESID) {
+            ptx::ldsm_x4_trans(a_hi, rh);
+            ptx::ldsm_x4_trans(a_lo, rl);
           }
+          uint32_t oh[4], ol[4];
+#pragma unroll
+          for (int fb = 0; fb < 4; ++fb) {
+            // accumulator registers of (fb, rb): lane half fb / 2, rows even/odd at q = 2 (fb & 1) + e
+            const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
+            float y0 = tanhf(__uint_as_float(ra[0]) + gb[rb][0][fb] + bq[fb]);
+            float y1 = tanhf(__uint_as_float(ra[1]) + gb[rb][1][fb] + bq[fb]);
+            if (RESID) {
+              const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[fb]));
+              const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[fb]));
+              y0 = (y0 + (h2.x + l2.x)) * kRsqrt2;
+              y1 = (y1 + (h2.y + l2.y)) * kRsqrt2;
+            }
+            const __nv_bfloat162 hi = __floats2bfloat162_rn(y0, y1);
+            const float2 hf = __bfloat1622float2(hi);
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(y0 - hf.x, y1 - hf.y);
+            oh[fb] = *reinterpret_cast<const uint32_t*>(&hi);
+            ol[fb] = *reinterpret_cast<const uint32_t*>(&lo);
+          }
+          ptx::stsm_x4_trans(a_hi, oh);
+          ptx::stsm_x4_trans(a_lo, ol);
         }
         __syncwarp();
-        store(out, row0, nrows, -1, col0, nvec, lane, buf);
+        store_sw(out, row0, nrows, col0, nvec, lane, buf);
         __syncwarp();
       }
       return;

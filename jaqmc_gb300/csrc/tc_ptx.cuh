@@ -142,6 +142,28 @@ __device__ __forceinline__ void tmem_ld4_ld1x3(uint32_t a4, uint32_t c0, uint32_
 #pragma unroll
   for (int q = 0; q < 3; ++q) v3[q] = __uint_as_float(r[4 + q]);
 }
+// 16 lanes x 256 bits, no wait: thread T gets (lane T/4, columns 2(T%4) and
+// 2(T%4)+1) in r[0], r[1] and (lane T/4 + 8, same columns) in r[2], r[3].
+__device__ __forceinline__ void tmem_ld16x256_nw(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.16x256b.x1.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+}
+// Four transposed 8x8 b16 tiles: lanes 8m..8m+7 give the row addresses of
+// tile m; thread T receives rows 2(T%4), 2(T%4)+1 of column T/4 (low half =
+// even row).  stmatrix is the inverse.
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t addr, uint32_t* d) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3])
+               : "r"(addr)
+               : "memory");
+}
+__device__ __forceinline__ void stsm_x4_trans(uint32_t addr, const uint32_t* d) {
+  asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(d[0]),
+               "r"(d[1]), "r"(d[2]), "r"(d[3])
+               : "memory");
+}
 // 16-byte global -> shared copy that bypasses the registers (and L1).
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
