@@ -46,6 +46,7 @@ struct TcArgs {
   int n_out;
   int resid_last;  // order the K chunks so this CTA's residual features come last
   int ebuf_bytes;  // epilogue staging bytes per half (0: unused)
+  int b4d;         // activation maps are 4-D (k, electron, walker, plane), one per spin channel
   int* err;
 };
 
@@ -158,9 +159,15 @@ k_tc_gemm(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUt
           ptx::mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
           ptx::tma_load_3d(base, A, ka, m0, 0, &full[s]);
           ptx::tma_load_3d(base + kATile, A, ka, m0, 1, &full[s]);
-          const CUtensorMap* Bm = b2 ? &mapB2 : &mapB1;
-          ptx::tma_load_3d(base + 2 * kATile, Bm, kx, ti.row0, 0, &full[s]);
-          ptx::tma_load_3d(base + 2 * kATile + stage_b, Bm, kx, ti.row0, 1, &full[s]);
+          if (g.b4d) {  // one spin channel's electrons of walkers row0 ..
+            const CUtensorMap* Bm = ti.a_sel ? &mapB2 : &mapB1;
+            ptx::tma_load_4d(base + 2 * kATile, Bm, kx, 0, ti.row0, 0, &full[s]);
+            ptx::tma_load_4d(base + 2 * kATile + stage_b, Bm, kx, 0, ti.row0, 1, &full[s]);
+          } else {
+            const CUtensorMap* Bm = b2 ? &mapB2 : &mapB1;
+            ptx::tma_load_3d(base + 2 * kATile, Bm, kx, ti.row0, 0, &full[s]);
+            ptx::tma_load_3d(base + 2 * kATile + stage_b, Bm, kx, ti.row0, 1, &full[s]);
+          }
         }
       }
       // never leave with copies in flight: wait (bounded) for the last phase
@@ -566,8 +573,22 @@ struct EpiTcOrbital {
   float* A;
   int raw;           // value-only passes: store orbitals without the envelope factor
   int n_rows;  // B * n (value-only passes)
+  // value-only passes with split orbitals: tiles of W4[s] walkers x the
+  // electrons of channel s (4-D activation maps), tpc4[s] tiles per channel
+  int chan4d, B;
+  int W4[2], tpc4[2];
   __device__ TileInfo tile(int tx, const TcArgs& g) const {
     TileInfo t{};
+    if (g.T == 1 && chan4d) {
+      const int s = tx < tpc4[0] ? 0 : 1;
+      const int ns = s ? n - n_up : n_up;
+      t.a_sel = s;
+      t.w = (s ? tx - tpc4[0] : tx) * W4[s];
+      t.row0 = t.w;
+      t.i0 = s ? n_up : 0;
+      t.ng = min(W4[s], B - t.w) * ns;
+      return t;
+    }
     if (g.T == 1) {
       // value-only: contiguous 256-row tiles over all walkers, one pass per
       // spin channel; rows of the other channel are skipped in the epilogue
@@ -645,6 +666,34 @@ struct EpiTcOrbital {
     const size_t ts = amat_tangent_stride(n, K);
     EnvParams ep;
     load_params(ti.a_sel, k, j, ep);
+    if (g.T == 1 && chan4d) {
+      const int ns = ti.a_sel ? n - n_up : n_up;
+      for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
+        float v[16];
+        ptx::tmem_ld16(taddr + c0, v);
+        if (!fok || c0 >= ti.ng) continue;
+        int wq = c0 / ns, iq = c0 - wq * ns;
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+          if (c0 + jj < ti.ng) {
+            const int w = ti.w + wq, i = ti.i0 + iq;
+            const size_t idx = amat_index(1, n, K, w, k, 0, i, j);
+            if (raw) {
+              A[idx] = v[jj];
+            } else {
+              float e[5];
+              envelope(ti.a_sel, w, i, k, j, 1, e, ep);
+              A[idx] = v[jj] * e[0];
+            }
+          }
+          if (++iq == ns) {
+            iq = 0;
+            ++wq;
+          }
+        }
+      }
+      return;
+    }
     if (g.T == 1) {
       for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
         float v[16];
@@ -774,6 +823,31 @@ static qmc_status make_map(CUtensorMap* m, const void* base, int k_extent, size_
   if (r != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (%d): k=%d rows=%zu ld=%d plane=%zu box_rows=%d", (int)r,
               k_extent, rows, ld, plane, box_rows);
+    return QMC_ERR_CUDA;
+  }
+  return QMC_OK;
+}
+
+// 4-D map over two bf16 planes of rows [walker][electron][ld] whose first
+// electron row is `base`: dims (k_extent, ne, walkers, 2), box (64, ne,
+// box_w, 1); a box lands in shared memory as box_w * ne consecutive rows.
+static qmc_status make_map4(CUtensorMap* m, const void* base, int k_extent, int ne, size_t walkers, int ld, int n,
+                            size_t plane, int box_w) {
+  auto enc = encoder();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled is unavailable");
+    return QMC_ERR_UNSUPPORTED;
+  }
+  cuuint64_t dims[4] = {(cuuint64_t)k_extent, (cuuint64_t)ne, (cuuint64_t)walkers, 2};
+  cuuint64_t strides[3] = {(cuuint64_t)ld * 2, (cuuint64_t)n * ld * 2, (cuuint64_t)plane * 2};
+  cuuint32_t box[4] = {(cuuint32_t)kKChunk, (cuuint32_t)ne, (cuuint32_t)box_w, 1};
+  cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (4-D) failed (%d): k=%d ne=%d walkers=%zu box_w=%d", (int)r, k_extent, ne,
+              walkers, box_w);
     return QMC_ERR_CUDA;
   }
   return QMC_OK;
@@ -942,6 +1016,30 @@ qmc_status tc_orbitals(cudaStream_t s, const TcOrbitalArgs& a) {
   e.aevec = a.aevec;
   e.A = a.A;
   e.raw = a.T == 1 ? a.raw : 0;
+  // value-only split orbitals: tiles of one channel's electrons only, N the
+  // largest multiple of lcm(16, n_up, n_dn) up to 256
+  const int nd = a.n - a.n_up;
+  if (a.T == 1 && a.split && a.n_up > 0 && nd > 0) {
+    auto gcd = [](int x, int y) { while (y) { const int t = x % y; x = y; y = t; } return x; };
+    long L = 16;
+    L = L / gcd((int)L, a.n_up) * a.n_up;
+    L = L / gcd((int)L, nd) * nd;
+    if (L <= 256) {
+      const int N4 = (int)(256 / L * L);
+      g.n_cols = N4;
+      g.b4d = 1;
+      e.chan4d = 1;
+      e.B = a.B;
+      e.W4[0] = N4 / a.n_up;
+      e.W4[1] = N4 / nd;
+      e.tpc4[0] = (a.B + e.W4[0] - 1) / e.W4[0];
+      e.tpc4[1] = (a.B + e.W4[1] - 1) / e.W4[1];
+      CUtensorMap m4u, m4d;
+      QMC_TRY(make_map4(&m4u, a.X, a.k, a.n_up, a.B, a.k, a.n, a.x_plane, e.W4[0]));
+      QMC_TRY(make_map4(&m4d, a.X + (size_t)a.n_up * a.k, a.k, nd, a.B, a.k, a.n, a.x_plane, e.W4[1]));
+      return launch(s, mA0, mA1, m4u, m4d, g, e.tpc4[0] + e.tpc4[1], e);
+    }
+  }
   return launch(s, mA0, mA1, mB, mB, g, n_tiles, e);
 }
 
