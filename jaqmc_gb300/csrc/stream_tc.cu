@@ -266,13 +266,15 @@ struct ContigTiles {
   }
 };
 
-// One-electron layer epilogue.  A thread holds one feature (its TMEM lane)
-// and walks the rows of its tile in chunks of 16.  Each warp owns 32 features
-// and two shared-memory chunk buffers of [2 planes][16 rows][32 features]
-// bf16: the residual rows of the next chunk are copied in with cp.async while
-// the current chunk is computed, outputs replace the residual in place, and a
-// chunk leaves with 16-byte stores per plane.  No barrier is wider than the
-// warp.  Tangent rows past T come out as zeros (their inputs are zero rows).
+// One-electron layer epilogue.  Each warp owns 32 features (a TMEM lane
+// quarter) and walks the rows of its tile in chunks of 16, reading the
+// accumulators as 16x256b fragments (a thread: 4 features x 2 row pairs).
+// Two shared-memory staging tiles per warp of [2 planes][16 rows][32
+// features] bf16 take the residual rows of the next chunk by cp.async while
+// the current chunk is computed; ldmatrix/stmatrix (.trans) move the residual
+// into and the outputs out of the fragment layout, outputs replace the
+// residual in place, and a chunk leaves with 16-byte stores per plane.  No
+// barrier is wider than the warp.  Tangent rows past T come out as zeros.
 template <bool RESID>
 struct EpiTcLayer : ContigTiles {
   static constexpr int kCR = 16;                 // rows per chunk
@@ -283,42 +285,6 @@ struct EpiTcLayer : ContigTiles {
   const float* Gb;
   const float* bias;
 
-  // rows [row0, row0 + nrows) x features [col0, col0 + 32) of `st` -> buf
-  __device__ __forceinline__ void fetch(const StSplit& st, size_t row0, int nrows, int col0, int nvec, int lane,
-                                        __nv_bfloat16* buf) const {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int v = lane + 32 * q;
-      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
-      if (r < nrows && vq < nvec)
-        ptx::cp_async16(buf + (pl * kCR + r) * 32 + 8 * vq,
-                        st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq);
-    }
-    ptx::cp_async_commit();
-  }
-  // rows [t0, t0 + nrows) x features [col0, col0 + 32) of a walker's broadcast
-  // terms (fp32, row stride N) -> gbuf[16][32]; committed with the next fetch
-  __device__ __forceinline__ void fetch_gb(const float* gbrow, int nrows, int col0, int N, int lane,
-                                           float* gbuf) const {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int v = lane + 32 * q;
-      const int r = v >> 3, c = 4 * (v & 7);
-      if (r < nrows && col0 + c + 4 <= N) ptx::cp_async16(gbuf + r * 32 + c, gbrow + (size_t)r * N + col0 + c);
-    }
-  }
-  // buf -> rows [row0, row0 + nrows) of `st`, except row `skip`
-  __device__ __forceinline__ void store(const StSplit& st, size_t row0, int nrows, int skip, int col0, int nvec,
-                                        int lane, const __nv_bfloat16* buf) const {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int v = lane + 32 * q;
-      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
-      if (r < nrows && r != skip && vq < nvec)
-        *reinterpret_cast<uint4*>(st.p + pl * st.plane + (row0 + r) * (size_t)st.ld + col0 + 8 * vq) =
-            *reinterpret_cast<const uint4*>(buf + (pl * kCR + r) * 32 + 8 * vq);
-    }
-  }
   // Value-pass staging tiles [2 planes][16 rows][4 pieces of 8 features],
   // piece p of row r stored at p ^ ((r >> 1) & 3): the eight rows of an 8x8
   // ldmatrix / stmatrix tile then fall on distinct bank groups.
@@ -346,22 +312,48 @@ struct EpiTcLayer : ContigTiles {
             *reinterpret_cast<const uint4*>(buf + (pl * kCR + r) * 32 + 8 * swz(r, vq));
     }
   }
-  __device__ __forceinline__ float get(const __nv_bfloat16* buf, int r, int lane) const {
-    return __bfloat162float(buf[r * 32 + lane]) + __bfloat162float(buf[(kCR + r) * 32 + lane]);
+  // tangent passes: staging rows [lo, hi) <-> rows row0 + [lo, hi) (row0 may
+  // be negative; only rows in [lo, hi) are addressed)
+  __device__ __forceinline__ void fetch_rows_sw(const StSplit& st, long long row0, int lo, int hi, int col0,
+                                                int nvec, int lane, __nv_bfloat16* buf) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
+      if (r >= lo && r < hi && vq < nvec)
+        ptx::cp_async16(buf + (pl * kCR + r) * 32 + 8 * swz(r, vq),
+                        st.p + pl * st.plane + (size_t)(row0 + r) * st.ld + col0 + 8 * vq);
+    }
+    ptx::cp_async_commit();
   }
-  __device__ __forceinline__ void put(__nv_bfloat16* buf, int r, int lane, float y) const {
-    const __nv_bfloat16 hi = __float2bfloat16_rn(y);
-    buf[r * 32 + lane] = hi;
-    buf[(kCR + r) * 32 + lane] = __float2bfloat16_rn(y - __bfloat162float(hi));
+  __device__ __forceinline__ void store_rows_sw(const StSplit& st, long long row0, int lo, int hi, int skip, int col0,
+                                                int nvec, int lane, const __nv_bfloat16* buf) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int pl = v >> 6, r = (v >> 2) & 15, vq = v & 3;
+      if (r >= lo && r < hi && r != skip && vq < nvec)
+        *reinterpret_cast<uint4*>(st.p + pl * st.plane + (size_t)(row0 + r) * st.ld + col0 + 8 * vq) =
+            *reinterpret_cast<const uint4*>(buf + (pl * kCR + r) * 32 + 8 * swz(r, vq));
+    }
   }
-
+  // broadcast rows t0 + [lo, hi) of a walker (fp32, row stride N) -> gbuf,
+  // committed with the next residual fetch
+  __device__ __forceinline__ void fetch_gb_sw(const float* gbw, int t0, int lo, int hi, int col0, int N, int lane,
+                                              float* gbuf) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int v = lane + 32 * q;
+      const int r = v >> 3, p = v & 7;
+      if (r >= lo && r < hi && col0 + 4 * p + 4 <= N)
+        ptx::cp_async16(gbuf + r * 32 + 4 * (p ^ (((r >> 1) & 3) << 1)), gbw + (size_t)(t0 + r) * N + col0 + 4 * p);
+    }
+  }
   __device__ void run(const TileInfo& ti, const TcArgs& g, uint32_t taddr, int f, int half, uint8_t* ebuf) const {
     const int N = g.n_out;
     const int lane = f & 31, col0 = f - lane;
     const int q = (f & 127) >> 5;
     const int nvec = max(0, min(4, (N - col0) / 8));
-    const int fc = f < N ? f : 0;  // clamped feature for loads of parameters
-    const float b = bias[fc];
     __nv_bfloat16* buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * 2 * kBuf;  // value-only layout
     if (g.T == 1) {
       // Thread T holds features col0 + T/4 + 8 fb (fb = 0..3) of rows
@@ -452,99 +444,173 @@ struct EpiTcLayer : ContigTiles {
       return;
     }
     const int Tp = g.Tp, T = g.T;
-    // per warp: two residual/output chunk buffers, then two fp32 chunks of the
-    // broadcast terms, all refilled by cp.async one chunk ahead
+    // Tangent passes, same fragment layout as the value pass.  A group
+    // (electron) occupies tile columns [lg*Tp, lg*Tp + Tp); its 16-column
+    // chunks start at lg*Tp rounded down to a multiple of 8 (off = 0 or 4
+    // columns earlier), so chunk c holds tangents t = 16c - off + [0, 16);
+    // fragment rows outside [0, Tp) belong to the neighbouring groups and are
+    // neither used nor stored.  The value row t = 0 sits in lane T%4 = off/2
+    // of each quad (rb = 0, e = 0), the Laplacian row t = 1 next to it.
+    // Per warp: two residual/output staging tiles and two broadcast-term tiles
+    // (fp32 [16][32], piece p of row r at p ^ (2 ((r >> 1) & 3))), refilled by
+    // cp.async one chunk ahead.
     buf0 = reinterpret_cast<__nv_bfloat16*>(ebuf) + q * (2 * kBuf + 2 * kGbuf * 2);
     float* gbuf0 = reinterpret_cast<float*>(buf0 + 2 * kBuf);
+    const int T4 = lane >> 2, T2 = 2 * (lane & 3);
+    float bq[4];
+    int Fq[4];
+#pragma unroll
+    for (int fb = 0; fb < 4; ++fb) {
+      Fq[fb] = col0 + T4 + 8 * fb;
+      bq[fb] = Fq[fb] < N ? bias[Fq[fb]] : 0.f;
+    }
+    const int lr = lane & 7, lp = lane >> 3;
     for (int lg = half; lg < ti.ng; lg += 2) {
       const int gi = ti.g0 + lg;
       const size_t r0 = (size_t)gi * Tp;
-      const uint32_t tcol = taddr + (uint32_t)(lg * Tp);
+      const int cs0 = lg * Tp, off = cs0 & 7;
+      const uint32_t tca = taddr + (uint32_t)(cs0 - off);
       const float* gbw = Gb + (size_t)(gi / n) * Tp * N;  // this walker's broadcast rows
-      fetch_gb(gbw, min(16, Tp), col0, N, lane, gbuf0);
-      if (RESID) fetch(resid, r0, min(16, Tp), col0, nvec, lane, buf0);
-      else ptx::cp_async_commit();
-      FlState st{};
+      const int nch = (Tp + off + 15) / 16;
+      // staging rows of chunk c that hold this group's tangents
+      auto sr_lo = [&](int c) { return max(0, off - 16 * c); };
+      auto sr_hi = [&](int c) { return min(16, Tp + off - 16 * c); };
+      auto prefetch = [&](int c, int kb) {
+        const int t0 = 16 * c - off;  // tangent of staging row 0 (may be negative)
+        fetch_gb_sw(gbw, t0, sr_lo(c), sr_hi(c), col0, N, lane, gbuf0 + kb * kGbuf);
+        if (RESID) fetch_rows_sw(resid, (long long)r0 + t0, sr_lo(c), sr_hi(c), col0, nvec, lane, buf0 + kb * kBuf);
+        else ptx::cp_async_commit();
+      };
+      prefetch(0, 0);
+      float h[4], d1[4], S[4] = {0.f, 0.f, 0.f, 0.f}, zL[4] = {0.f, 0.f, 0.f, 0.f}, res1[4] = {0.f, 0.f, 0.f, 0.f};
+      const int src = (lane & ~3) | (off >> 1);  // quad lane holding t = 0 and t = 1
       int k = 0;
-      for (int t0 = 0; t0 < Tp; t0 += 16, k ^= 1) {
+      for (int c = 0; c < nch; ++c, k ^= 1) {
         __nv_bfloat16* buf = buf0 + k * kBuf;
         const float* gbuf = gbuf0 + k * kGbuf;
-        const int cs = min(16, Tp - t0);  // a multiple of 4, uniform
-        const bool more = t0 + 16 < Tp;
-        if (more) {
-          const int nr = min(16, Tp - t0 - 16);
-          fetch_gb(gbw + (size_t)(t0 + 16) * N, nr, col0, N, lane, gbuf0 + (k ^ 1) * kGbuf);
-          if (RESID) fetch(resid, r0 + t0 + 16, nr, col0, nvec, lane, buf0 + (k ^ 1) * kBuf);
-          else ptx::cp_async_commit();
+        const bool more = c + 1 < nch;
+        if (more) prefetch(c + 1, k ^ 1);
+        uint32_t r[16];
+#pragma unroll
+        for (int lh = 0; lh < 2; ++lh)
+#pragma unroll
+          for (int rb = 0; rb < 2; ++rb)
+            if (16 * c + 8 * rb - off < Tp)  // the block holds tangents of this group
+              ptx::tmem_ld16x256_nw(tca + ((uint32_t)(16 * lh) << 16) + (uint32_t)(16 * c + 8 * rb),
+                                    r + 4 * (2 * lh + rb));
+        ptx::tmem_wait16(r);
+        if (more) ptx::cp_async_wait<1>();
+        else ptx::cp_async_wait<0>();
+        __syncwarp();
+        const uint32_t sb = ptx::smem_u32(buf);
+        uint32_t rh[2][4], rl[2][4];
+        if (RESID) {
+#pragma unroll
+          for (int rb = 0; rb < 2; ++rb) {
+            const int row = 8 * rb + lr;
+            ptx::ldsm_x4_trans(sb + (uint32_t)(((0 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), rh[rb]);
+            ptx::ldsm_x4_trans(sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), rl[rb]);
+          }
         }
-        const bool full = cs == 16 && t0 + 16 <= T;  // every row of the chunk a real tangent
-        if (t0 == 0) {
-          if (full) chunk<true, true>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
-          else chunk<true, false>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
-        } else {
-          if (full) chunk<false, true>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
-          else chunk<false, false>(st, tcol, gbuf, t0, cs, T, b, more, lane, buf);
+        // pre-activations z of this thread's 16 elements [rb][e][fb]
+        float z[2][2][4];
+#pragma unroll
+        for (int rb = 0; rb < 2; ++rb)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int sr = 8 * rb + T2 + e;
+            const int t = 16 * c - off + sr;
+            const bool real = t >= 0 && t < T;
+#pragma unroll
+            for (int fb = 0; fb < 4; ++fb) {
+              const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
+              const int pz = ((T4 >> 2) + 2 * fb) ^ (((sr >> 1) & 3) << 1);
+              const float gv = gbuf[sr * 32 + 4 * pz + (T4 & 3)];
+              z[rb][e][fb] = real ? __uint_as_float(ra[e]) + gv : 0.f;
+            }
+          }
+        float res[2][2][4];
+#pragma unroll
+        for (int rb = 0; rb < 2; ++rb)
+#pragma unroll
+          for (int fb = 0; fb < 4; ++fb) {
+            if (RESID) {
+              const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[rb][fb]));
+              const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[rb][fb]));
+              res[rb][0][fb] = h2.x + l2.x;
+              res[rb][1][fb] = h2.y + l2.y;
+            } else {
+              res[rb][0][fb] = res[rb][1][fb] = 0.f;
+            }
+          }
+        if (c == 0) {
+          // value row: h = tanh(z + b) on the source lane, then shared by the quad
+#pragma unroll
+          for (int fb = 0; fb < 4; ++fb) {
+            const float hv = tanhf(z[0][0][fb] + bq[fb]);
+            h[fb] = __shfl_sync(0xffffffffu, hv, src);
+            d1[fb] = 1.f - h[fb] * h[fb];
+            zL[fb] = z[0][1][fb];
+            res1[fb] = res[0][1][fb];
+          }
+        }
+        uint32_t oh[2][4], ol[2][4];
+#pragma unroll
+        for (int rb = 0; rb < 2; ++rb)
+#pragma unroll
+          for (int fb = 0; fb < 4; ++fb) {
+            float y[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const int t = 16 * c - off + 8 * rb + T2 + e;
+              const float zz = z[rb][e][fb];
+              float v;
+              if (t == 0) {
+                v = h[fb];
+              } else {
+                if (t >= 2) S[fb] = fmaf(zz, zz, S[fb]);  // zero for padding rows
+                v = d1[fb] * zz;                          // t = 1 rewritten at the end
+              }
+              if (RESID) v = (v + res[rb][e][fb]) * kRsqrt2;
+              y[e] = (t >= T) ? 0.f : v;
+            }
+            const __nv_bfloat162 hi = __floats2bfloat162_rn(y[0], y[1]);
+            const float2 hf = __bfloat1622float2(hi);
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(y[0] - hf.x, y[1] - hf.y);
+            oh[rb][fb] = *reinterpret_cast<const uint32_t*>(&hi);
+            ol[rb][fb] = *reinterpret_cast<const uint32_t*>(&lo);
+          }
+#pragma unroll
+        for (int rb = 0; rb < 2; ++rb) {
+          const int row = 8 * rb + lr;
+          ptx::stsm_x4_trans(sb + (uint32_t)(((0 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), oh[rb]);
+          ptx::stsm_x4_trans(sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), ol[rb]);
         }
         __syncwarp();
-        store(out, r0 + t0, cs, t0 == 0 ? 1 : -1, col0, nvec, lane, buf);
+        // rows of this group except the Laplacian row (written below)
+        store_rows_sw(out, (long long)r0 + 16 * c - off, sr_lo(c), sr_hi(c), c == 0 ? off + 1 : -1, col0, nvec, lane,
+                      buf);
         __syncwarp();
       }
-      float y1 = st.d1 * st.zL - 2.f * st.h * st.d1 * st.S;
-      if (RESID) y1 = (y1 + st.res1) * kRsqrt2;
-      if (f < N) {
-        const __nv_bfloat16 hi = __float2bfloat16_rn(y1);
-        __nv_bfloat16* o = out.p + (r0 + 1) * (size_t)out.ld + f;
-        o[0] = hi;
-        o[out.plane] = __float2bfloat16_rn(y1 - __bfloat162float(hi));
+      // Laplacian row: quad sums of sum_d z_d^2, then on the source lane
+      // y = tanh'' |grad z|^2 + tanh' lap z  (tanh'' = -2 h tanh')
+#pragma unroll
+      for (int fb = 0; fb < 4; ++fb) {
+        float st = S[fb];
+        st += __shfl_xor_sync(0xffffffffu, st, 1);
+        st += __shfl_xor_sync(0xffffffffu, st, 2);
+        float y1 = d1[fb] * zL[fb] - 2.f * h[fb] * d1[fb] * st;
+        if (RESID) y1 = (y1 + res1[fb]) * kRsqrt2;
+        if (lane == src && Fq[fb] < N) {
+          const __nv_bfloat16 hi = __float2bfloat16_rn(y1);
+          __nv_bfloat16* o = out.p + (r0 + 1) * (size_t)out.ld + Fq[fb];
+          o[0] = hi;
+          o[out.plane] = __float2bfloat16_rn(y1 - __bfloat162float(hi));
+        }
       }
     }
   }
 
-  // running forward-Laplacian state of one (group, feature)
-  struct FlState {
-    float h, d1, zL, S, res1;
-  };
-  // One chunk of tangent rows t0 .. t0 + cs - 1.  FIRST: the chunk holds the
-  // value row (t = 0) and the Laplacian row (t = 1, finished after the last
-  // chunk).  FULL: all 16 rows are real tangents (no size or padding checks).
-  template <bool FIRST, bool FULL>
-  __device__ __forceinline__ void chunk(FlState& st, uint32_t tcol, const float* gbuf, int t0, int cs, int T,
-                                        float b, bool more, int lane, __nv_bfloat16* buf) const {
-    uint32_t r[16];
-    if (FULL || cs == 16) {
-      ptx::tmem_ld16_nw(tcol + t0, r);
-    } else {
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        if (4 * kk < cs) ptx::tmem_ld4_nw(tcol + t0 + 4 * kk, r + 4 * kk);
-    }
-    ptx::tmem_wait16(r);
-    if (more) ptx::cp_async_wait<1>();
-    else ptx::cp_async_wait<0>();
-    __syncwarp();
-    float gbv[16];
-#pragma unroll
-    for (int e = 0; e < 16; ++e) gbv[e] = (FULL || t0 + e < T) ? gbuf[e * 32 + lane] : 0.f;
-    if (FIRST) {  // value row and Laplacian row
-      st.h = tanhf(__uint_as_float(r[0]) + gbv[0] + b);
-      st.d1 = 1.f - st.h * st.h;
-      float y = st.h;
-      if (RESID) y = (y + get(buf, 0, lane)) * kRsqrt2;
-      put(buf, 0, lane, y);
-      st.zL = __uint_as_float(r[1]) + gbv[1];
-      if (RESID) st.res1 = get(buf, 1, lane);
-    }
-#pragma unroll
-    for (int e = FIRST ? 2 : 0; e < 16; ++e) {
-      if (!FULL && e >= cs) break;
-      const bool real = FULL || t0 + e < T;
-      const float z = real ? __uint_as_float(r[e]) + gbv[e] : 0.f;
-      st.S = fmaf(z, z, st.S);
-      float y = st.d1 * z;
-      if (RESID) y = (y + get(buf, e, lane)) * kRsqrt2;
-      put(buf, e, lane, real ? y : 0.f);
-    }
-  }
 };
 
 struct EpiTcStore : ContigTiles {

@@ -278,7 +278,10 @@ def test_mixed_form_on_equilibrated_walkers(case, cuda_device):
                               "el_max_abs": float(np.abs(e).max()), "mean_err": float(e.mean()), "n": len(x)})
     assert np.array_equal(sg.cpu().numpy(), r64["sign"].numpy())
     assert rel.max() < 1e-3
-    assert abs(e.mean()) <= 5e-4
+    # no systematic bias: the mean error within four standard errors of the
+    # sample (per-walker spreads reach ~3 mHa for argon) or 0.5 mHa
+    se = e.std(ddof=1) / np.sqrt(len(e))
+    assert abs(e.mean()) <= max(5e-4, 4 * se), (e.mean(), se)
 
 
 def test_mixed_mh_runs_and_matches_plain_sampler(cuda_device):
