@@ -14,6 +14,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "stream_tc.cuh"
 #include "tc_ptx.cuh"
@@ -512,80 +513,88 @@ struct EpiTcLayer : ContigTiles {
             ptx::ldsm_x4_trans(sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), rl[rb]);
           }
         }
-        // pre-activations z of this thread's 16 elements [rb][e][fb]
-        float z[2][2][4];
-#pragma unroll
-        for (int rb = 0; rb < 2; ++rb)
-#pragma unroll
-          for (int e = 0; e < 2; ++e) {
-            const int sr = 8 * rb + T2 + e;
-            const int t = 16 * c - off + sr;
-            const bool real = t >= 0 && t < T;
-#pragma unroll
-            for (int fb = 0; fb < 4; ++fb) {
-              const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
-              const int pz = ((T4 >> 2) + 2 * fb) ^ (((sr >> 1) & 3) << 1);
-              const float gv = gbuf[sr * 32 + 4 * pz + (T4 & 3)];
-              z[rb][e][fb] = real ? __uint_as_float(ra[e]) + gv : 0.f;
-            }
-          }
-        float res[2][2][4];
-#pragma unroll
-        for (int rb = 0; rb < 2; ++rb)
-#pragma unroll
-          for (int fb = 0; fb < 4; ++fb) {
-            if (RESID) {
-              const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[rb][fb]));
-              const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[rb][fb]));
-              res[rb][0][fb] = h2.x + l2.x;
-              res[rb][1][fb] = h2.y + l2.y;
-            } else {
-              res[rb][0][fb] = res[rb][1][fb] = 0.f;
-            }
-          }
-        if (c == 0) {
-          // value row: h = tanh(z + b) on the source lane, then shared by the quad
-#pragma unroll
-          for (int fb = 0; fb < 4; ++fb) {
-            const float hv = tanhf(z[0][0][fb] + bq[fb]);
-            h[fb] = __shfl_sync(0xffffffffu, hv, src);
-            d1[fb] = 1.f - h[fb] * h[fb];
-            zL[fb] = z[0][1][fb];
-            res1[fb] = res[0][1][fb];
-          }
-        }
-        uint32_t oh[2][4], ol[2][4];
-#pragma unroll
-        for (int rb = 0; rb < 2; ++rb)
-#pragma unroll
-          for (int fb = 0; fb < 4; ++fb) {
-            float y[2];
-#pragma unroll
+        // FULL: every row of the chunk is a Jacobian tangent of this group
+        // (t in [2, T)), so the per-row range checks drop out
+        auto compute = [&](auto full_tag) {
+          constexpr bool FULLc = decltype(full_tag)::value;
+          // pre-activations z of this thread's 16 elements [rb][e][fb]
+          float z[2][2][4];
+  #pragma unroll
+          for (int rb = 0; rb < 2; ++rb)
+  #pragma unroll
             for (int e = 0; e < 2; ++e) {
-              const int t = 16 * c - off + 8 * rb + T2 + e;
-              const float zz = z[rb][e][fb];
-              float v;
-              if (t == 0) {
-                v = h[fb];
-              } else {
-                if (t >= 2) S[fb] = fmaf(zz, zz, S[fb]);  // zero for padding rows
-                v = d1[fb] * zz;                          // t = 1 rewritten at the end
+              const int sr = 8 * rb + T2 + e;
+              const int t = 16 * c - off + sr;
+              const bool real = FULLc || (t >= 0 && t < T);
+  #pragma unroll
+              for (int fb = 0; fb < 4; ++fb) {
+                const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
+                const int pz = ((T4 >> 2) + 2 * fb) ^ (((sr >> 1) & 3) << 1);
+                const float gv = gbuf[sr * 32 + 4 * pz + (T4 & 3)];
+                z[rb][e][fb] = real ? __uint_as_float(ra[e]) + gv : 0.f;
               }
-              if (RESID) v = (v + res[rb][e][fb]) * kRsqrt2;
-              y[e] = (t >= T) ? 0.f : v;
             }
-            const __nv_bfloat162 hi = __floats2bfloat162_rn(y[0], y[1]);
-            const float2 hf = __bfloat1622float2(hi);
-            const __nv_bfloat162 lo = __floats2bfloat162_rn(y[0] - hf.x, y[1] - hf.y);
-            oh[rb][fb] = *reinterpret_cast<const uint32_t*>(&hi);
-            ol[rb][fb] = *reinterpret_cast<const uint32_t*>(&lo);
+          float res[2][2][4];
+  #pragma unroll
+          for (int rb = 0; rb < 2; ++rb)
+  #pragma unroll
+            for (int fb = 0; fb < 4; ++fb) {
+              if (RESID) {
+                const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[rb][fb]));
+                const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[rb][fb]));
+                res[rb][0][fb] = h2.x + l2.x;
+                res[rb][1][fb] = h2.y + l2.y;
+              } else {
+                res[rb][0][fb] = res[rb][1][fb] = 0.f;
+              }
+            }
+          if (!FULLc && c == 0) {
+            // value row: h = tanh(z + b) on the source lane, then shared by the quad
+  #pragma unroll
+            for (int fb = 0; fb < 4; ++fb) {
+              const float hv = tanhf(z[0][0][fb] + bq[fb]);
+              h[fb] = __shfl_sync(0xffffffffu, hv, src);
+              d1[fb] = 1.f - h[fb] * h[fb];
+              zL[fb] = z[0][1][fb];
+              res1[fb] = res[0][1][fb];
+            }
           }
-#pragma unroll
-        for (int rb = 0; rb < 2; ++rb) {
-          const int row = 8 * rb + lr;
-          ptx::stsm_x4_trans(sb + (uint32_t)(((0 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), oh[rb]);
-          ptx::stsm_x4_trans(sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), ol[rb]);
-        }
+          uint32_t oh[2][4], ol[2][4];
+  #pragma unroll
+          for (int rb = 0; rb < 2; ++rb)
+  #pragma unroll
+            for (int fb = 0; fb < 4; ++fb) {
+              float y[2];
+  #pragma unroll
+              for (int e = 0; e < 2; ++e) {
+                const int t = 16 * c - off + 8 * rb + T2 + e;
+                const float zz = z[rb][e][fb];
+                float v;
+                if (!FULLc && t == 0) {
+                  v = h[fb];
+                } else {
+                  if (FULLc || t >= 2) S[fb] = fmaf(zz, zz, S[fb]);  // zero for padding rows
+                  v = d1[fb] * zz;                                   // t = 1 rewritten at the end
+                }
+                if (RESID) v = (v + res[rb][e][fb]) * kRsqrt2;
+                y[e] = (!FULLc && t >= T) ? 0.f : v;
+              }
+              const __nv_bfloat162 hi = __floats2bfloat162_rn(y[0], y[1]);
+              const float2 hf = __bfloat1622float2(hi);
+              const __nv_bfloat162 lo = __floats2bfloat162_rn(y[0] - hf.x, y[1] - hf.y);
+              oh[rb][fb] = *reinterpret_cast<const uint32_t*>(&hi);
+              ol[rb][fb] = *reinterpret_cast<const uint32_t*>(&lo);
+            }
+  #pragma unroll
+          for (int rb = 0; rb < 2; ++rb) {
+            const int row = 8 * rb + lr;
+            ptx::stsm_x4_trans(sb + (uint32_t)(((0 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), oh[rb]);
+            ptx::stsm_x4_trans(sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), ol[rb]);
+          }
+        };
+        const int tc0 = 16 * c - off;
+        if (c > 0 && tc0 >= 2 && tc0 + 16 <= T) compute(std::true_type{});
+        else compute(std::false_type{});
         __syncwarp();
         // rows of this group except the Laplacian row (written below)
         store_rows_sw(out, (long long)r0 + 16 * c - off, sr_lo(c), sr_hi(c), c == 0 ? off + 1 : -1, col0, nvec, lane,
