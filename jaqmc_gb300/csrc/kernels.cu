@@ -133,11 +133,22 @@ cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, 
   return cudaGetLastError();
 }
 
+// 2^x by the hardware base-2 exponential (relative error ~2^-22).  Used by
+// the mixed form's envelope factors: exp(-|sigma| r) = 2^(-log2(e) |sigma| r)
+// with log2(e) |sigma| rounded to FP32 adds at most ~1e-6 relative error for
+// the arguments that matter, below the form's split-BF16 operand error.
+__device__ __forceinline__ float fast_exp2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Envelope factor of every value-only orbital matrix element (walker w,
 // determinant k, electron i, orbital j): sum_I pi[j,I,k] exp(-s r_iI) with
 // s = |sigma[j,I,k]| (abs_isotropic) or sigma (isotropic), per spin channel
 // of electron i (src/jaqmc/wavefunction/output/envelope.py:98-140).  Same
-// terms in the same order as the tangent epilogues.  One block per
+// terms in the same order as the tangent epilogues, the exponentials by
+// fast_exp2 (the kernel serves the mixed form only).  One block per
 // kEnvWalkers walkers, thread (walker, i, j); the parameters are staged once
 // per block as [channel][I][k][j] so a warp reads consecutive j.
 constexpr int kEnvWalkers = 8;
@@ -148,14 +159,14 @@ __global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A
   extern __shared__ float she[];
   const int nch = split ? 2 : 1, per = A * K * n;
   float* ps = she;               // [nch][A][K][n]
-  float* ss = she + nch * per;   // [nch][A][K][n], already |sigma| when env_abs
+  float* ss = she + nch * per;   // [nch][A][K][n]: log2(e) |sigma| (or log2(e) sigma)
   for (int e = threadIdx.x; e < nch * per; e += blockDim.x) {
     const int c = e / per, rem = e % per;
     const int I = rem / (K * n), k = (rem / n) % K, j = rem % n;
     const size_t q = ((size_t)j * A + I) * K + k;
     ps[e] = (c ? pi1 : pi0)[q];
     const float sv = (c ? sg1 : sg0)[q];
-    ss[e] = env_abs ? fabsf(sv) : sv;
+    ss[e] = (env_abs ? fabsf(sv) : sv) * 1.4426950408889634f;
   }
   __syncthreads();
   const int nn = n * n;
@@ -170,7 +181,7 @@ __global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A
       float acc = 0.f;
       for (int I = 0; I < A; ++I) {
         const int o = ((c * A + I) * K + k) * n + j;
-        acc += ps[o] * expf(-ss[o] * __ldg(ra + I));
+        acc += ps[o] * fast_exp2(-ss[o] * __ldg(ra + I));
       }
       out[(size_t)k * nn] = acc;
     }
