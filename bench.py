@@ -520,7 +520,7 @@ FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12
 # walkers, scaled to the workload's walkers (traffic grows with the rows)
 TRAFFIC_PER_WALKER: dict = {
     # ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch at 512 walkers
-    ("N2", "mixed"): (437.89184e6 + 282.870016e6) / 512,
+    ("N2", "mixed"): (434.893056e6 + 283.123712e6) / 512,
 }
 
 
