@@ -40,17 +40,18 @@ __global__ void k_features(int n, int A, int Tp, int T, int K0p, const float* __
     aevec_g[3 * gi] = dx;
     aevec_g[3 * gi + 1] = dy;
     aevec_g[3 * gi + 2] = dz;
-    vpot -= (double)charges[I] / (double)r;
+    if (pe) vpot -= (double)charges[I] / (double)r;
   }
   __syncthreads();
-  // one-electron rows
+  // one-electron rows (32-bit index arithmetic within a walker)
   const int A4 = 4 * A;
-  const size_t per_w = (size_t)n * Tp * K0p;
+  const int per_w = n * Tp * K0p;
   float* Xw = X0 + (size_t)w * per_w;
-  for (size_t e = threadIdx.x; e < per_w; e += blockDim.x) {
-    int f = (int)(e % K0p);
-    int t = (int)((e / K0p) % Tp);
-    int i = (int)(e / ((size_t)K0p * Tp));
+  for (int e = threadIdx.x; e < per_w; e += blockDim.x) {
+    const int f = e % K0p;
+    const int it = e / K0p;
+    const int t = it % Tp;
+    const int i = it / Tp;
     float v = 0.f;
     if (f < A4 && t < T) {
       int I = f >> 2, comp = f & 3;
@@ -69,13 +70,13 @@ __global__ void k_features(int n, int A, int Tp, int T, int K0p, const float* __
   }
   // two-electron rows
   const int P2 = T > 1 ? 5 : 1;
-  const size_t per_w2 = (size_t)n * n * P2 * 4;
+  const int per_w2 = n * n * P2 * 4;
   float* Hw = H2 + (size_t)w * per_w2;
-  for (size_t e = threadIdx.x; e < per_w2; e += blockDim.x) {
-    int comp = (int)(e & 3);
-    int p = (int)((e >> 2) % P2);
-    int pr = (int)(e / (4 * P2));
-    int i = pr / n, j = pr % n;
+  for (int e = threadIdx.x; e < per_w2; e += blockDim.x) {
+    const int comp = e & 3;
+    const int p = (e >> 2) % P2;
+    const int pr = e / (4 * P2);
+    const int i = pr / n, j = pr % n;
     float v = 0.f;
     if (i != j) {
       float d[3] = {xs[3 * i] - xs[3 * j], xs[3 * i + 1] - xs[3 * j + 1], xs[3 * i + 2] - xs[3 * j + 2]};

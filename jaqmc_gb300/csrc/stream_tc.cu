@@ -387,14 +387,18 @@ struct EpiTcLayer : ContigTiles {
 #pragma unroll
           for (int rb = 0; rb < 2; ++rb)
             ptx::tmem_ld16x256_nw(tq + ((uint32_t)(16 * lh) << 16) + (uint32_t)(c0 + 8 * rb), r + 4 * (2 * lh + rb));
-        // broadcast terms of the rows' walkers
+        // broadcast terms of the rows' walkers (row0 = w0 n + e0; rows past
+        // the chunk's first walker found by 32-bit division of e0 + rr)
+        const unsigned row32 = (unsigned)(ti.g0 + c0);
+        const unsigned w0 = row32 / (unsigned)n;
+        const unsigned e0 = row32 - w0 * (unsigned)n;
         float gb[2][2][4];  // [rb][e][fb]
 #pragma unroll
         for (int rb = 0; rb < 2; ++rb)
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
             const int rr = 8 * rb + T2 + e;
-            const size_t w = (row0 + rr) / (size_t)n;
+            const size_t w = w0 + (e0 + (unsigned)rr) / (unsigned)n;
 #pragma unroll
             for (int fb = 0; fb < 4; ++fb)
               gb[rb][e][fb] = (rr < nrows && Fq[fb] < N) ? __ldg(Gb + w * N + Fq[fb]) : 0.f;
