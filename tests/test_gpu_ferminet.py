@@ -30,13 +30,15 @@ from oracle import mcmc as OM
 from oracle import philox as OP
 
 pytestmark = pytest.mark.gpu
-OUT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
+# parity statistics are appended (JSON lines) to the file this variable names
+STATS = os.environ.get("QMC_PARITY_STATS")
 
 
 def _record(name, stats):
-    os.makedirs(OUT, exist_ok=True)
-    path = os.path.join(OUT, "parity_stats.jsonl")
-    with open(path, "a") as f:
+    if not STATS:
+        return
+    os.makedirs(os.path.dirname(os.path.abspath(STATS)), exist_ok=True)
+    with open(STATS, "a") as f:
         f.write(json.dumps({"case": name, **stats}) + "\n")
 
 
