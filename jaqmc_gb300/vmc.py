@@ -16,12 +16,18 @@ implementation:
   :class:`LossAndGrad`, :func:`mean_reduce` — ``src/jaqmc/estimator/kinetic/euclidean.py:29-135``,
   ``src/jaqmc/app/molecule/hamiltonian.py:9-22``, ``src/jaqmc/estimator/total_energy.py:16-70``,
   ``src/jaqmc/estimator/loss_grad.py:25-128``, ``src/jaqmc/estimator/base.py:27-53``.
+* :class:`EstimatorPipeline`, :class:`EvaluationStage` — ``src/jaqmc/estimator/base.py:287-427``,
+  ``src/jaqmc/workflow/stage/evaluation.py:150-272`` (sampling and estimation
+  without an optimiser, per-step statistics and the digest).
+* :func:`load_reference_checkpoint`, :func:`save_checkpoint` —
+  ``src/jaqmc/utils/checkpoint.py:26-274`` (the stage state's ``.npz`` key layout).
 
 Everything numerical runs on the GPU through the C ABI; there is no CPU path.
 """
 from __future__ import annotations
 
 import dataclasses
+import functools
 from dataclasses import dataclass, field
 from typing import Any, NamedTuple
 
@@ -455,3 +461,190 @@ class LossAndGrad:
         if J is not None:
             stats["grad_logpsi"] = J
         return stats
+
+
+# ------------------------------------------------------------ evaluation
+class EstimatorPipeline:
+    """Ordered estimators (``src/jaqmc/estimator/base.py:287-427``).
+
+    Each estimator sees the walker statistics of the ones before it (the
+    kinetic and potential parts feed :class:`TotalEnergy`).  An estimator is an
+    object with ``evaluate_batch_walkers`` and optionally ``init``, ``reduce``,
+    ``finalize_stats`` and ``finalize_state``, or a plain function
+    ``f(params, batched_data, prev_walker_stats, state, rngs) -> (stats, state)``
+    (reduced by :func:`mean_reduce`, averaged over steps).
+    """
+
+    def __init__(self, estimators: dict, group=None):
+        self.estimators = dict(estimators)
+        self.group = group
+        self._reduce_keys: dict[str, frozenset] = {}
+
+    def init(self, data, rngs=None) -> dict:
+        return {name: (est.init(data, rngs) if hasattr(est, "init") else None)
+                for name, est in self.estimators.items()}
+
+    def evaluate(self, params, batched_data, state: dict, rngs=None):
+        """``(step_stats, state)``: every estimator's ``reduce`` output merged."""
+        walker_stats, step_stats, state = {}, {}, dict(state)
+        for name, est in self.estimators.items():
+            f = est.evaluate_batch_walkers if hasattr(est, "evaluate_batch_walkers") else est
+            parts, state[name] = f(params, batched_data, walker_stats, state.get(name), rngs)
+            walker_stats.update(parts)
+            reduced = est.reduce(parts) if hasattr(est, "reduce") else mean_reduce(parts, group=self.group)
+            self._reduce_keys[name] = frozenset(reduced)
+            step_stats.update(reduced)
+        return step_stats, state
+
+    def finalize_stats(self, batched_stats: dict, state: dict) -> dict:
+        """Per-step statistics (leading step axis) -> final values; by default
+        the NaN-skipping mean over steps."""
+        if not self._reduce_keys:
+            raise RuntimeError("finalize_stats() called before evaluate(); key ownership is unknown.")
+        out = {}
+        for name, est in self.estimators.items():
+            own = {k: np.asarray(batched_stats[k]) for k in self._reduce_keys.get(name, ()) if k in batched_stats}
+            if hasattr(est, "finalize_stats"):
+                out.update(est.finalize_stats(own, state.get(name)))
+            else:
+                out.update({k: np.nanmean(v, axis=0) for k, v in own.items()})
+        return out
+
+    def digest(self, batched_stats: dict, state: dict, *, n_steps: int) -> dict:
+        """:meth:`finalize_stats` merged with each estimator's ``finalize_state``."""
+        result = self.finalize_stats(batched_stats, state) if batched_stats else {}
+        for name, est in self.estimators.items():
+            if hasattr(est, "finalize_state"):
+                result.update(est.finalize_state(state.get(name), n_steps=n_steps))
+        return result
+
+
+def energy_pipeline(wf, group=None) -> EstimatorPipeline:
+    """The molecule workflow's energy estimators: potential, kinetic, total."""
+    return EstimatorPipeline({
+        "potential": functools.partial(potential_energy, wf=wf),
+        "kinetic": EuclideanKinetic(f_log_psi=wf),
+        "total_energy": TotalEnergy(),
+    }, group=group)
+
+
+@dataclass
+class EvaluationStage:
+    """Evaluation work stage: sampling and estimation without parameter
+    updates (``src/jaqmc/workflow/stage/evaluation.py:150-272``).
+
+    ``burn_in`` sampler steps, then per iteration one sampler step and the
+    estimator pipeline; the per-step statistics are kept (and written to
+    ``[prefix_]stats.npz`` when ``save_dir`` is set, the reference's HDF5 file
+    in NumPy form) and the digest (:meth:`EstimatorPipeline.digest`) goes to
+    ``[prefix_]digest.npz``.  With ``digest_step_interval`` > 0 a preview of
+    the running digest is passed to ``log`` every that many steps.
+    """
+
+    wf: Any
+    sampler: MCMCSampler
+    pipeline: EstimatorPipeline
+    iterations: int = 10
+    burn_in: int = 0
+    digest_step_interval: int = 0
+    save_dir: str | None = None
+    prefix: str = ""
+    log: Any = None
+
+    def run(self, params, data, sampler_state, estimator_state=None, rngs=None):
+        """Returns ``(digest, stacked_stats, data, sampler_state, estimator_state)``."""
+        est_state = estimator_state if estimator_state is not None else self.pipeline.init(data, rngs)
+
+        def sample(data, sampler_state):
+            d, _, sampler_state = self.sampler.step(self.wf.batch_log_prob(params, data), data, sampler_state)
+            return data.merge({"electrons": d.electrons if hasattr(d, "electrons") else d["electrons"]}), sampler_state
+
+        for _ in range(self.burn_in):
+            data, sampler_state = sample(data, sampler_state)
+        history: dict[str, list] = {}
+        for step in range(self.iterations):
+            data, sampler_state = sample(data, sampler_state)
+            step_stats, est_state = self.pipeline.evaluate(params, BatchedData(data), est_state, rngs)
+            for k, v in step_stats.items():
+                history.setdefault(k, []).append(float(v))
+            last = step + 1 == self.iterations
+            if self.log and ((self.digest_step_interval and (step + 1) % self.digest_step_interval == 0) or last):
+                self.log(step, self.pipeline.finalize_stats(history, est_state))
+        stacked = {k: np.asarray(v) for k, v in history.items()}
+        digest = self.pipeline.digest(stacked, est_state, n_steps=self.iterations)
+        if self.save_dir is not None:
+            import os
+            os.makedirs(self.save_dir, exist_ok=True)
+            pre = f"{self.prefix}_" if self.prefix else ""
+            np.savez(os.path.join(self.save_dir, f"{pre}stats.npz"), **stacked)
+            if digest:
+                np.savez(os.path.join(self.save_dir, f"{pre}digest.npz"), **digest)
+        return digest, stacked, data, sampler_state, est_state
+
+
+# ------------------------------------------------------------ checkpoints
+# The reference's NumPyCheckpointManager (src/jaqmc/utils/checkpoint.py:26-274)
+# writes a work stage's state pytree as one .npz: every leaf under its
+# slash-joined key path plus ``step``.  For the sampling stages the state is
+# (params, batched_data, sampler_state, estimator_state[, opt_state]), so the
+# wavefunction parameters sit at ``params/params/<module path>`` (the Flax
+# variables dict), the walkers at ``batched_data/data/electrons`` and the MCMC
+# state at ``sampler_state/stddev`` and ``sampler_state/pmoves``.
+_CKPT_PARAMS = "params/params/"
+_CKPT_ELECTRONS = "batched_data/data/electrons"
+
+
+def _param_leaves(wf, n_atoms: int):
+    if isinstance(wf, PsiformerWavefunction):
+        return P.psiformer_leaves(wf.config, n_atoms)
+    return P.ferminet_leaves(wf.config, n_atoms)
+
+
+def load_reference_checkpoint(path, wf, n_atoms: int, device=None) -> dict:
+    """Restore a reference checkpoint into this library's objects.
+
+    Returns ``{"step", "params", "electrons", "sampler_state"}``: ``step`` is
+    the run's initial step (saved step + 1, as the reference's
+    ``restore_from_file`` returns), ``params`` a :class:`DeviceParams` in the
+    layout of ``wf`` (shapes checked leaf by leaf), ``electrons`` the saved
+    walkers (or None) and ``sampler_state`` an :class:`MCMCState` with the
+    saved proposal width and acceptance history (or None).
+    """
+    leaves = _param_leaves(wf, n_atoms)
+    with np.load(path, allow_pickle=False) as f:
+        tree: dict = {}
+        for p, shape in leaves:
+            key = _CKPT_PARAMS + "/".join(p)
+            if key not in f.files:
+                raise KeyError(f"checkpoint {path} has no parameter {key}")
+            a = np.asarray(f[key], np.float32)
+            if tuple(a.shape) != tuple(shape):
+                raise ValueError(f"{key}: checkpoint shape {a.shape}, model expects {tuple(shape)}")
+            P._set(tree, p, a)
+        electrons = np.asarray(f[_CKPT_ELECTRONS], np.float32) if _CKPT_ELECTRONS in f.files else None
+        sstate = None
+        if "sampler_state/stddev" in f.files:
+            pm = np.asarray(f["sampler_state/pmoves"], np.float64) if "sampler_state/pmoves" in f.files else None
+            sstate = MCMCState(float(np.asarray(f["sampler_state/stddev"])), pm, 0, 0, 0)
+        step = int(np.asarray(f["step"]).item()) + 1 if "step" in f.files else 0
+    dev = device if device is not None else (wf._dev() if torch.cuda.is_available() else torch.device("cpu"))
+    return {"step": step, "params": DeviceParams(tree, leaves, dev), "electrons": electrons,
+            "sampler_state": sstate}
+
+
+def save_checkpoint(path, step: int, params: DeviceParams, data=None, sampler_state: MCMCState | None = None):
+    """Write ``params`` (and optionally the walkers and the MCMC state) with
+    the reference's key layout (compressed .npz, as its ``save``).  The file
+    holds no optimiser or estimator state."""
+    tree = params.tree()
+    arrays = {"step": np.asarray(step)}
+    for p, _ in params.leaves:
+        arrays[_CKPT_PARAMS + "/".join(p)] = np.asarray(P._get(tree, p))
+    if data is not None:
+        e = data["electrons"] if isinstance(data, dict) else data.electrons
+        arrays[_CKPT_ELECTRONS] = np.asarray(torch.as_tensor(e).detach().cpu(), np.float32)
+    if sampler_state is not None:
+        arrays["sampler_state/stddev"] = np.asarray(sampler_state.stddev, np.float32)
+        arrays["sampler_state/pmoves"] = np.asarray(sampler_state.pmoves, np.float32)
+    with open(path, "wb") as f:
+        np.savez_compressed(f, allow_pickle=False, **arrays)

@@ -93,3 +93,33 @@ def test_autograd_function_and_custom_op(cuda_device):
     torch.testing.assert_close(lp2, lp.detach())
     (lp2 * w).sum().backward()
     torch.testing.assert_close(flat2.grad, flat.grad)
+
+
+def test_evaluation_stage_exact_hydrogen(cuda_device, tmp_path):
+    """Evaluation stage (sampling + energy estimators, no optimiser) on the
+    exact hydrogen ground state psi ~ exp(-r): every local energy is -1/2, so
+    the digest has E = -0.5 Ha with zero variance and the virial split
+    <T> = -<V>/2 = 0.5 Ha (to sampling noise)."""
+    import os
+
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from helpers import hydrogenic_tree
+    from jaqmc_gb300 import params as P
+
+    mol = S.hydrogen()
+    wf = vmc.FermiNetWavefunction(nspins=(1, 0), ndets=2, hidden_dims_single=[16, 16], hidden_dims_double=[4, 4])
+    data = _system(mol, 2048)
+    tree = hydrogenic_tree(wf.config, 1, sigma=1.0)
+    params = vmc.DeviceParams(tree, P.ferminet_leaves(wf.config, 1), data.electrons.device)
+    sampler = vmc.MCMCSampler(steps=10, initial_width=0.5)
+    stage = vmc.EvaluationStage(wf, sampler, vmc.energy_pipeline(wf), iterations=20, burn_in=20,
+                                save_dir=str(tmp_path), prefix="h")
+    digest, stacked, *_ = stage.run(params, data, sampler.init(data, 11))
+    assert set(stacked) >= {"total_energy", "total_energy_var", "energy:kinetic", "energy:potential"}
+    assert stacked["total_energy"].shape == (20,)
+    assert abs(float(digest["total_energy"]) + 0.5) < 1e-4
+    assert float(digest["total_energy_var"]) < 1e-6
+    assert abs(float(digest["energy:kinetic"]) - 0.5) < 0.03
+    assert abs(float(digest["energy:potential"]) + 1.0) < 0.03
+    assert os.path.exists(os.path.join(tmp_path, "h_digest.npz"))
