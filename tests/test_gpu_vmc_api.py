@@ -123,3 +123,65 @@ def test_evaluation_stage_exact_hydrogen(cuda_device, tmp_path):
     assert abs(float(digest["energy:kinetic"]) - 0.5) < 0.03
     assert abs(float(digest["energy:potential"]) + 1.0) < 0.03
     assert os.path.exists(os.path.join(tmp_path, "h_digest.npz"))
+
+
+def test_sr_on_adjoint_scores_matches_closed_form(cuda_device):
+    """Robust SR (standard form) on the adjoint's per-walker scores equals
+    (O^T O + lambda I)^-1 g solved in FP64 on the device."""
+    from jaqmc_gb300 import sr as SR
+
+    mol = S.lithium()
+    wf = vmc.FermiNetWavefunction(nspins=mol.nspins, ndets=2, hidden_dims_single=[16, 16], hidden_dims_double=[4, 4])
+    data = _system(mol, 96)
+    params = wf.init_params(data, 0)
+    bd = vmc.BatchedData(data)
+    ws = {}
+    ws.update(vmc.potential_energy(params, bd, ws, None, wf=wf)[0])
+    ws.update(vmc.EuclideanKinetic(f_log_psi=wf).evaluate_batch_walkers(params, bd, ws, None)[0])
+    ws.update(vmc.TotalEnergy().evaluate_batch_walkers(params, bd, ws, None)[0])
+    st = vmc.LossAndGrad(f_log_psi=wf, per_walker=True).gradient(params, bd, ws["total_energy"])
+    g, score = st["grads"], st["grad_logpsi"]
+    lam = 1e-2
+    opt = SR.RobustSR(learning_rate=1.0, damping=lam)
+    delta, _ = opt.precondition(g, opt.init(g.numel(), g.device), score)
+    O = score.double()
+    O = (O - O.mean(0, keepdim=True)) / O.shape[0] ** 0.5
+    ref = torch.linalg.solve(O.T @ O + lam * torch.eye(O.shape[1], dtype=O.dtype, device=O.device), g.double())
+    assert float(torch.linalg.norm(delta - ref)) <= 1e-8 * float(torch.linalg.norm(ref))
+
+
+def test_hydrogen_training_with_sr(cuda_device):
+    """VMC on the hydrogen atom with robust SR over the adjoint's scores
+    reaches -0.5 Ha."""
+    from jaqmc_gb300 import sr as SR
+
+    mol = S.hydrogen()
+    wf = vmc.FermiNetWavefunction(nspins=(1, 0), ndets=2, hidden_dims_single=[16, 16], hidden_dims_double=[4, 4])
+    data = _system(mol, 512)
+    params = wf.init_params(data, 0)
+    sampler = vmc.MCMCSampler(steps=10, initial_width=0.3)
+    state = sampler.init(data, 7)
+    kin, tot = vmc.EuclideanKinetic(f_log_psi=wf), vmc.TotalEnergy()
+    lg = vmc.LossAndGrad(f_log_psi=wf, per_walker=True)
+    opt = SR.RobustSR(learning_rate=0.1, max_norm=0.1, damping=1e-3)
+    ostate = opt.init(params.flat.numel(), params.flat.device)
+    for _ in range(5):
+        d, _, state = sampler.step(wf.batch_log_prob(params, data), data, state)
+        data = data.merge({"electrons": d.electrons})
+    energies = []
+    for it in range(300):
+        d, _, state = sampler.step(wf.batch_log_prob(params, data), data, state)
+        data = data.merge({"electrons": d.electrons})
+        bd = vmc.BatchedData(data)
+        ws = {}
+        ws.update(vmc.potential_energy(params, bd, ws, None, wf=wf)[0])
+        ws.update(kin.evaluate_batch_walkers(params, bd, ws, None)[0])
+        ws.update(tot.evaluate_batch_walkers(params, bd, ws, None)[0])
+        st = lg.gradient(params, bd, ws["total_energy"])
+        energies.append(vmc.mean_reduce({"e": ws["total_energy"]})["e"])
+        upd, ostate = opt.update(st["grads"], ostate, st["grad_logpsi"])
+        with torch.no_grad():
+            params.flat += upd.to(torch.float32)
+        params.touch()
+    e = float(np.mean(energies[-20:]))
+    assert abs(e + 0.5) < 5e-3, energies[-20:]
