@@ -139,3 +139,111 @@ def logpsi_fn(params, cfg, atoms, dtype=torch.float64):
     def f(electrons):
         return evaluate(params, cfg, electrons, atoms, dtype=dtype)["logpsi"]
     return f
+
+
+# ---------------------------------------------------------------- forward Laplacian
+# The same network carried through the forward-Laplacian tangent algebra of
+# ``oracle/lap.py`` (value, Jacobian over the 3n coordinates, Laplacian),
+# composing the reference interpreter's rules: linear maps, the elementwise
+# rule, and the product rule for the bilinear attention terms
+# (``src/jaqmc/laplacian/primitives/arithmetic.py:385``,
+# ``dot_general.py:713``, ``elementwise.py:42-72``).
+def _bilinear(a, b, eq: str):
+    """``einsum(eq, a, b)`` of two tangent carriers (walker axis first in
+    every operand): J by the product rule, L = L_a b + a L_b + 2 sum_d J_a J_b."""
+    from .lap import LT
+    lhs, out = eq.split("->")
+    ea, eb = lhs.split(",")
+    ja, jb, jo = ea[0] + "z" + ea[1:], eb[0] + "z" + eb[1:], out[0] + "z" + out[1:]
+    x = torch.einsum(eq, a.x, b.x)
+    J = torch.einsum(f"{ja},{eb}->{jo}", a.J, b.x) + torch.einsum(f"{ea},{jb}->{jo}", a.x, b.J)
+    L = (torch.einsum(eq, a.L, b.x) + torch.einsum(eq, a.x, b.L)
+         + 2.0 * torch.einsum(f"{ja},{jb}->{out}", a.J, b.J))
+    return LT(x, J, L)
+
+
+def features_lt(xl, atoms: torch.Tensor, nspins):
+    """Tangent form of :func:`features`: ``(ae (B, n, 4A+1), r_ae (B, n, A))``."""
+    B, n, _ = xl.shape
+    A = atoms.shape[0]
+    ae = xl.unsqueeze(2) - atoms.reshape(A, 3)
+    r = lap.norm_last(ae)
+    lr = lap.log1p(r)
+    vec = ae * (lr * lap.reciprocal(r)).unsqueeze(-1)
+    f = lap.concat([lr.unsqueeze(-1), vec], -1).reshape(n, 4 * A)
+    spins = torch.cat([torch.ones(nspins[0]), -torch.ones(nspins[1])]).to(xl.x.dtype)
+    return lap.concat([f, lap.const(spins.expand(B, n)[..., None].clone(), xl.D)], -1), r
+
+
+def layer_norm_lt(a, scale, bias, eps=1e-5):
+    m = a.mean(-1).unsqueeze(-1)
+    var = (a * a).mean(-1).unsqueeze(-1) - m * m
+    inv = lap.reciprocal(lap.sqrt(var + eps))
+    return ((a - m) * inv).scale(scale) + bias
+
+
+def attention_lt(p, x, cfg: PsiformerConfig, dtype):
+    H, Dh = cfg.num_heads, cfg.heads_dim
+    n = x.shape[1]
+
+    def proj(name):
+        W = _t(p[name]["kernel"], dtype)
+        b = _t(p[name]["bias"], dtype)
+        return lap.linear(x, W.reshape(W.shape[0], H * Dh), b.reshape(H * Dh)).reshape(n, H, Dh)
+    q = proj("query").scale(1.0 / Dh ** 0.5)
+    k = proj("key")
+    v = proj("value")
+    s = _bilinear(q, k, "bqhd,bkhd->bhqk")
+    e = lap.exp(s - s.x.max(-1, keepdim=True).values)
+    w = e * lap.reciprocal(e.sum(-1)).unsqueeze(-1)
+    o = _bilinear(w, v, "bhqk,bkhd->bqhd").reshape(n, H * Dh)
+    Wo = _t(p["out"]["kernel"], dtype)
+    return lap.linear(o, Wo.reshape(H * Dh, Wo.shape[-1]), _t(p["out"]["bias"], dtype))
+
+
+def backbone_lt(p, cfg: PsiformerConfig, ae, dtype):
+    x = lap.linear(ae, _t(p["Dense_0"]["kernel"], dtype), _t(p["Dense_0"]["bias"], dtype))
+    for l in range(cfg.num_layers):
+        q = p[f"PsiformerLayer_{l}"]
+        xin = layer_norm_lt(x, _t(q["LayerNorm_0"]["scale"], dtype), _t(q["LayerNorm_0"]["bias"], dtype))
+        x = x + attention_lt(q["MultiHeadDotProductAttention_0"], xin, cfg, dtype)
+        h = layer_norm_lt(x, _t(q["LayerNorm_1"]["scale"], dtype), _t(q["LayerNorm_1"]["bias"], dtype))
+        for k in range(len(cfg.mlp_hidden_dims) + 1):
+            h = lap.tanh(lap.linear(h, _t(q[f"Dense_{k}"]["kernel"], dtype), _t(q[f"Dense_{k}"]["bias"], dtype)))
+        x = x + h
+    return x
+
+
+def jastrow_lt(p, cfg: PsiformerConfig, xl, dtype):
+    nu, nd = cfg.nspins
+    n = nu + nd
+    if n < 2:
+        return lap.const(xl.x.new_zeros(xl.shape[0]), xl.D)
+    a_par = _t(p["alpha_par"], dtype)[0]
+    a_anti = _t(p["alpha_anti"], dtype)[0]
+    i, j = torch.triu_indices(n, n, 1)
+    diff = (xl.unsqueeze(2) - xl.unsqueeze(1))[(i, j)]
+    r = lap.norm_last(diff)
+    same = ((i < nu) == (j < nu)).to(dtype)
+    f_par = lap.reciprocal(r + a_par).scale(-0.25 * a_par ** 2)
+    f_anti = lap.reciprocal(r + a_anti).scale(-0.5 * a_anti ** 2)
+    return (f_par.scale(same) + f_anti.scale(1.0 - same)).sum(-1)
+
+
+def evaluate_fl(params, cfg: PsiformerConfig, electrons, atoms, *, dtype=torch.float64):
+    """Forward-Laplacian ``log|psi|``: ``{"logpsi", "grad" (B, 3n), "lap" (B,),
+    "sign"}`` of the Psiformer + SimpleEE Jastrow."""
+    p = params["params"]
+    e = _t(electrons, dtype)
+    R = _t(atoms, dtype)
+    xl = lap.seed(e)
+    ae, r_ae = features_lt(xl, R, cfg.nspins)
+    h = backbone_lt(p["backbone_layer"], cfg, ae, dtype)
+    orb = OF.orbital_projection(p["orbital_layer"], cfg, h, dtype)
+    env = OF.envelope(p["envelope_layer"], cfg, r_ae, dtype)
+    sign, ld = lap.slogdet(orb * env)
+    s, lp = lap.signed_logsumexp(sign, ld, -1)
+    if cfg.jastrow == "simple_ee":
+        lp = lp + jastrow_lt(p["jastrow_layer"], cfg, xl, dtype)
+    B = e.shape[0]
+    return {"logpsi": lp.x, "grad": lp.J.reshape(B, -1), "lap": lp.L, "sign": s}
