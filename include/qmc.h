@@ -69,8 +69,9 @@ typedef struct {
 /* Psiformer with the SimpleEE Jastrow (PsiformerWavefunction,
  * src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94): Pre-LN layers,
  * biased attention projections and input layer, log-rescaled input features,
- * no orbital bias.  Value path only: qmc_forward, qmc_mh_steps(_resident) and
- * qmc_mh_draws; qmc_local_energy and qmc_grad return QMC_ERR_UNSUPPORTED. */
+ * no orbital bias.  qmc_forward, qmc_mh_steps(_resident), qmc_mh_draws and the
+ * forward-Laplacian qmc_local_energy (at most 42 electrons); qmc_grad returns
+ * QMC_ERR_UNSUPPORTED. */
 typedef struct {
   int n_up, n_down, n_atoms;
   int ndets;                            /* K                                    */
@@ -205,6 +206,11 @@ qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const doubl
 
 /* Byte budget of the adjoint's workspace (default 8 GiB); sets the chunk size. */
 qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes);
+
+/* Byte budget of the Psiformer local-energy workspace (default 32 GiB): walkers
+ * run in balanced chunks whose forward-Laplacian activations fit it.  FermiNet
+ * models ignore it. */
+qmc_status qmc_model_set_energy_budget(qmc_model* m, size_t bytes);
 
 /* FP64 walker-batch mean and variance <x^2> - <x>^2 of a float32 vector,
  * NaNs skipped (src/jaqmc/estimator/base.py:27-53).  mean_var: 2 doubles. */

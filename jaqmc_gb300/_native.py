@@ -81,6 +81,7 @@ _SIGS = {
     "qmc_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p, C.c_size_t, C.c_void_p]),
     "qmc_model_set_grad_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "qmc_model_set_energy_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
     "qmc_model_check_error": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qmc_profile_enable": (C.c_int, [C.c_int]),
     "qmc_profile_read": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p]),
@@ -297,6 +298,10 @@ class NativeFermiNet:
     def set_grad_budget(self, nbytes: int):
         check(self.lib.qmc_model_set_grad_budget(self.h, int(nbytes)))
 
+    def set_energy_budget(self, nbytes: int):
+        """Workspace budget of the chunked Psiformer local energy."""
+        check(self.lib.qmc_model_set_energy_budget(self.h, int(nbytes)))
+
     def grad(self, electrons, weights=None, per_walker=False, stream=None):
         """Adjoint of log|psi|: returns ``(per_walker (B,P) or None, grad (P,) float64 or
         None, logpsi (B,))``; ``grad = sum_w weights[w] d log|psi_w|/d theta``."""
@@ -325,8 +330,8 @@ class NativeFermiNet:
 
 class NativePsiformer(NativeFermiNet):
     """A ``qmc_model`` handle for a Psiformer (+ SimpleEE Jastrow): the value
-    path (``forward``, ``mh_steps``, ``mh_steps_resident``, ``mh_draws``);
-    ``local_energy`` and ``grad`` raise QMC_ERR_UNSUPPORTED."""
+    path (``forward``, ``mh_steps``, ``mh_steps_resident``, ``mh_draws``) and
+    the forward-Laplacian ``local_energy``; ``grad`` raises QMC_ERR_UNSUPPORTED."""
 
     def __init__(self, cfg, atoms, charges, precision="mixed", device=None):
         self._open(device)

@@ -181,6 +181,17 @@ static int padded_tangents(const Dims& d, int T, bool mixed) {
   return mixed ? tc_padded_tangents(T) : T;
 }
 
+double nuclear_repulsion(const float* atoms, const float* charges, int A) {
+  double nuc = 0.0;
+  for (int I = 0; I < A; ++I)
+    for (int J = I + 1; J < A; ++J) {
+      double dx = atoms[3 * I] - atoms[3 * J], dy = atoms[3 * I + 1] - atoms[3 * J + 1],
+             dz = atoms[3 * I + 2] - atoms[3 * J + 2];
+      nuc += (double)charges[I] * charges[J] / std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  return nuc;
+}
+
 Plan make_plan(const qmc_model* m, int op, int B) {
   const Dims& d = m->d;
   Plan p{};
@@ -578,11 +589,13 @@ qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, 
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1) { set_error("batch must be >= 1"); return QMC_ERR_SHAPE; }
   if (m->kind == QMC_KIND_PSIFORMER) {
-    if (op != QMC_OP_FORWARD && op != QMC_OP_MH) {
-      set_error("Psiformer models support the value path only (forward, MH steps)");
+    if (op != QMC_OP_FORWARD && op != QMC_OP_MH && op != QMC_OP_LOCAL_ENERGY) {
+      set_error("Psiformer models support forward, MH steps and the local energy (no parameter adjoint)");
       return QMC_ERR_UNSUPPORTED;
     }
-    const size_t need = psi_make_plan(m, batch).base.total;
+    if (op == QMC_OP_LOCAL_ENERGY) QMC_TRY(psi_fl_check(m));
+    const size_t need = op == QMC_OP_LOCAL_ENERGY ? psi_fl_plan(m, psi_fl_chunk(m, batch)).base.total
+                                                  : psi_make_plan(m, batch).base.total;
     if (!ws || ws_bytes < need) {
       set_error("workspace too small: %zu bytes given, %zu needed", ws_bytes, need);
       return QMC_ERR_WORKSPACE;
@@ -709,14 +722,7 @@ qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atom
   const int A = m->d.A;
   memcpy(m->atoms_host, atoms_host, sizeof(float) * 3 * A);
   memcpy(m->charges_host, charges_host, sizeof(float) * A);
-  double nuc = 0.0;
-  for (int I = 0; I < A; ++I)
-    for (int J = I + 1; J < A; ++J) {
-      double dx = atoms_host[3 * I] - atoms_host[3 * J], dy = atoms_host[3 * I + 1] - atoms_host[3 * J + 1],
-             dz = atoms_host[3 * I + 2] - atoms_host[3 * J + 2];
-      nuc += (double)charges_host[I] * charges_host[J] / std::sqrt(dx * dx + dy * dy + dz * dz);
-    }
-  m->nuclear_repulsion = nuc;
+  m->nuclear_repulsion = nuclear_repulsion(atoms_host, charges_host, A);
   if (e == cudaSuccess)
     e = cudaMemcpy(m->arena + m->a.atoms, atoms_host, sizeof(float) * 3 * A, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -844,10 +850,18 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
 
 size_t qmc_workspace_size(const qmc_model* m, int op, int batch) {
   if (!m || batch < 1) return 0;
-  if (m->kind == QMC_KIND_PSIFORMER)
+  if (m->kind == QMC_KIND_PSIFORMER) {
+    if (op == QMC_OP_LOCAL_ENERGY) return psi_fl_check(m) == QMC_OK ? psi_fl_plan(m, psi_fl_chunk(m, batch)).base.total : 0;
     return op == QMC_OP_FORWARD || op == QMC_OP_MH ? psi_make_plan(m, batch).base.total : 0;
+  }
   if (op == QMC_OP_GRAD) return grad_workspace(m, batch);
   return make_plan(m, op, batch).total;
+}
+
+qmc_status qmc_model_set_energy_budget(qmc_model* m, size_t bytes) {
+  if (!m || bytes == 0) { set_error("null model or zero budget"); return QMC_ERR_ARG; }
+  m->energy_budget = bytes;
+  return QMC_OK;
 }
 
 qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes) {
@@ -885,6 +899,7 @@ qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, flo
                             cudaStream_t s) {
   QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_LOCAL_ENERGY));
   if (!electrons || !e_local) { set_error("null electrons/e_local"); return QMC_ERR_ARG; }
+  if (m->kind == QMC_KIND_PSIFORMER) return psi_local_energy(m, batch, electrons, e_local, ke, pe, logpsi, flags, ws, s);
   Plan p = make_plan(m, QMC_OP_LOCAL_ENERGY, batch);
   QMC_TRY(evaluate(m, p, ws, electrons, true, logpsi ? logpsi : at<float>(ws, p.lpsi),
                    at<float>(ws, p.sgn), ke, e_local, flags, s));
@@ -894,7 +909,10 @@ qmc_status qmc_local_energy(qmc_model* m, int batch, const float* electrons, flo
 
 int qmc_tangent_rows(const qmc_model* m, int op) {
   if (!m || op < QMC_OP_FORWARD || op > QMC_OP_GRAD) return -1;
-  if (m->kind == QMC_KIND_PSIFORMER) return op == QMC_OP_FORWARD || op == QMC_OP_MH ? 1 : -1;
+  if (m->kind == QMC_KIND_PSIFORMER) {
+    if (op == QMC_OP_LOCAL_ENERGY) return psi_fl_plan(m, 1).base.Tp;
+    return op == QMC_OP_FORWARD || op == QMC_OP_MH ? 1 : -1;
+  }
   return make_plan(m, op, 1).Tp;
 }
 

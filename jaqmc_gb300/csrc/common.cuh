@@ -130,6 +130,7 @@ struct qmc_model {
   int* dev_err = nullptr;          // device error word of bounded waits
   bool params_set = false;
   size_t grad_budget = (size_t)8 << 30;  // bytes for the adjoint's chunked workspace
+  size_t energy_budget = (size_t)32 << 30;  // bytes for the chunked Psiformer local-energy workspace
   int n_sms = 0;
 };
 

@@ -1456,7 +1456,8 @@ template <int NMAX>
 __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
                          const float* __restrict__ pe, float* __restrict__ logpsi,
                          float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
-                         uint8_t* __restrict__ flags, int* __restrict__ n_refactor) {
+                         uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
+                         const float* __restrict__ gl_add) {
   extern __shared__ double shd[];
   const int w = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1520,17 +1521,24 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
     }
     __syncwarp();
     // grad_d = sum_k w_k t1_kd ; lap = sum_k w_k (tL - t2 + q) - |grad|^2
-    double g2 = 0.0;
+    // an additive log term (gl_add: its gradient, then its Laplacian) joins
+    // the gradient before it is squared
+    const float* ga = gl_add ? gl_add + (size_t)w * (D + 1) : nullptr;
+    double g2 = 0.0, gt2 = 0.0;
     for (int d = lane; d < D; d += 32) {
       double g = 0.0;
       for (int k = 0; k < K; ++k) g += (double)wk[k] * (double)t1s[(size_t)k * D + d];
       g2 += g * g;
+      const double gt = ga ? g + (double)ga[d] : g;
+      gt2 += gt * gt;
     }
     g2 = warp_sum(g2);
+    gt2 = warp_sum(gt2);
     double lap = 0.0;
     for (int k = 0; k < K; ++k) lap += lds[k];
     lap -= g2;
-    double kin = -0.5 * (lap + g2);
+    if (ga) lap += (double)ga[D];
+    double kin = -0.5 * (lap + gt2);
     if (lane == 0) {
       if (ke) ke[w] = (float)kin;
       if (el) el[w] = (float)(kin + (pe ? (double)pe[w] : 0.0));
@@ -1841,7 +1849,7 @@ static cudaError_t launch_logdet_value_smem(cudaStream_t s, int B, int n, int K,
 
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
-                          uint8_t* flags, int* n_refactor, const EnvArgs* env) {
+                          uint8_t* flags, int* n_refactor, const EnvArgs* env, const float* gl_add) {
   if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, const_cast<float*>(A), logpsi, sign, flags, env);
   if (T == 1 && n <= 64 && !env) return launch_logdet_value_smem(s, B, n, K, A, logpsi, sign, flags);
   if (env) return cudaErrorInvalidValue;  // tangent passes take enveloped matrices
@@ -1867,7 +1875,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
       set_dev = dev;                                                                        \
     }                                                                                       \
     k_logdet<NM><<<B, 32 * nw, sm, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags,    \
-                                        n_refactor);                                        \
+                                        n_refactor, gl_add);                                \
   }
   if (n <= 8) QMC_LD(8)
   else if (n <= 16) QMC_LD(16)

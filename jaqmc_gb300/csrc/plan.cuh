@@ -18,6 +18,9 @@ struct Plan {
 
 Plan make_plan(const qmc_model* m, int op, int B);
 
+// sum_{I<J} Z_I Z_J / |R_I - R_J| in FP64
+double nuclear_repulsion(const float* atoms, const float* charges, int A);
+
 // Validates a call: parameters set, batch >= 1, workspace large enough,
 // supported shapes, model on the current device.
 qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, int op);

@@ -326,7 +326,7 @@ PsiPlan psi_make_plan(const qmc_model* m, int B) {
 // z[rows][n_out] = X[rows][k] W[k][n_out] (X: GEMM-input buffer at `xoff`)
 static qmc_status psi_gemm(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s, size_t xoff, int k,
                            size_t w_f32, size_t t_bf16, int n_out) {
-  const int rows = pp.base.B * m->psi->d.n;
+  const int rows = pp.base.B * m->psi->d.n * pp.base.Tp;
   float* z = at<float>(ws, pp.z);
   if (pp.base.mixed) {
     TcStoreArgs a{rows, at<__nv_bfloat16>(ws, xoff), k, pp.in_plane, m->arena_bf16 + t_bf16, n_out, z, m->dev_err};
@@ -433,6 +433,147 @@ qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* 
   QMC_TRY(run_logdet(m, p, ws, nullptr, logpsi, sign, nullptr, nullptr, flags, s));
   QMC_PROF(QMC_KC_OTHER, (k_psi_add<<<(p.B + 255) / 256, 256, 0, s>>>(p.B, logpsi, at<float>(ws, pp.jas)),
                           cudaGetLastError()));
+  return QMC_OK;
+}
+
+// ------------------------------------------------------------ forward Laplacian
+PsiPlan psi_fl_plan(const qmc_model* m, int B) {
+  const PsiDims& d = m->psi->d;
+  PsiPlan pp{};
+  Plan& p = pp.base;
+  p.B = B;
+  p.mixed = m->precision == QMC_PRECISION_MIXED_BF16;
+  p.T = 3 * d.n + 2;
+  p.Tp = p.mixed ? tc_padded_tangents(p.T) : p.T;
+  p.P2 = 1;
+  p.K0p = d.K0p;
+  p.act_bytes = 4;
+  const size_t rows = (size_t)B * d.n * p.Tp;
+  int W = d.D;
+  for (int k = 0; k < d.n_dense; ++k) W = std::max(W, d.mlp[k]);
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes, 256); return r; };
+  p.x0 = take(rows * d.K0p * 4);
+  pp.x = take(rows * d.D * 4);
+  pp.in_plane = rows * W;
+  pp.xn = take(rows * W * 4);
+  pp.att = take(rows * W * 4);
+  // the backbone output (orbital GEMM operand) reuses the attention buffer,
+  // free once the last layer's MLP has read it
+  p.h1[0] = p.h1[1] = pp.att;
+  p.h1_plane = pp.in_plane;
+  pp.z = take(rows * std::max(3 * d.D, W) * 4);
+  p.rae = take((size_t)B * d.n * d.A * 4);
+  p.aevec = take((size_t)B * d.n * d.A * 12);
+  p.amat = take((size_t)B * d.K * p.Tp * d.n * d.n * 4);
+  p.pe = take((size_t)B * 4);
+  p.lpsi = take((size_t)B * 4);
+  p.sgn = take((size_t)B * 4);
+  p.refac = take(16);
+  pp.jas = take((size_t)B * 4);
+  pp.jgl = take((size_t)B * (3 * d.n + 1) * 4);
+  p.h2[0] = p.h2[1] = p.g1 = p.gb = p.g2 = p.xp = p.lp = o;  // unused by these passes
+  p.dmax = d.D;
+  p.total = o;
+  return pp;
+}
+
+// Walkers per chunk: at most the model's energy budget of workspace, chunks balanced.
+int psi_fl_chunk(const qmc_model* m, int batch) {
+  const size_t per = psi_fl_plan(m, 1).base.total;
+  const int cap = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, m->energy_budget / per));
+  const int nch = (batch + cap - 1) / cap;
+  return (batch + nch - 1) / nch;
+}
+
+qmc_status psi_fl_check(const qmc_model* m) {
+  const PsiDims& d = m->psi->d;
+  const PsiPlan pp = psi_fl_plan(m, 1);
+  if (pp.base.Tp <= 0 || pp.base.Tp > 128) {
+    set_error("local energy supports at most 42 electrons (3n+2 <= 128 tangents per tile)");
+    return QMC_ERR_SHAPE;
+  }
+  if (!psi_attention_fl_supported(d.n, d.Dh)) {
+    set_error("psiformer local energy: %d electrons x head width %d exceed the attention kernel", d.n, d.Dh);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  return QMC_OK;
+}
+
+template <class Out>
+static qmc_status psi_backbone_fl(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s,
+                                  Out (*fmt)(void*, const PsiPlan&, size_t, int)) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const float* ar = m->arena;
+  const Plan& p = pp.base;
+  const int groups = p.B * d.n, rows = groups * p.Tp, Tp = p.Tp, D = d.D;
+  float* x = at<float>(ws, pp.x);
+  float* z = at<float>(ws, pp.z);
+  {
+    const RowMap map{1, 0, 1, 1};
+    QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, rows, map, at<float>(ws, p.x0), d.K0p, d.K0p, nullptr, 0, 0,
+                                             ar + a.w_in, D, D, EpiStore{z, D, nullptr}));
+  }
+  QMC_PROF(QMC_KC_LAYER0, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + P.in_b, 0, x, 1, ar + P.ln0_s[0],
+                                              ar + P.ln0_b[0], fmt(ws, pp, pp.xn, D)));
+  for (int l = 0; l < d.L; ++l) {
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, a.w_qkv[l], a.t_qkv[l], 3 * D));
+    QMC_PROF(QMC_KC_PAIR, launch_psi_attention_fl(s, p.B, d.n, Tp, p.T, d.H, d.Dh, z, ar + a.b_qkv[l],
+                                                  fmt(ws, pp, pp.att, D)));
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.att, D, P.o_k[l], a.t_o[l], D));
+    QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + P.o_b[l], 0, x, 2, ar + P.ln1_s[l],
+                                               ar + P.ln1_b[l], fmt(ws, pp, pp.xn, D)));
+    size_t in = pp.xn, other = pp.att;
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      const int dout = d.mlp[k];
+      QMC_TRY(psi_gemm(m, pp, ws, s, in, din, P.mlp_k[l][k], a.t_mlp[l][k], dout));
+      if (k + 1 < d.n_dense) {
+        QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, dout, z, dout, ar + P.mlp_b[l][k], 1, x, 0,
+                                                   nullptr, nullptr, fmt(ws, pp, other, dout)));
+        std::swap(in, other);
+        din = dout;
+      } else if (l + 1 < d.L) {
+        QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + P.mlp_b[l][k], 1, x, 2,
+                                                   ar + P.ln0_s[l + 1], ar + P.ln0_b[l + 1], fmt(ws, pp, pp.xn, D)));
+      } else {
+        QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + P.mlp_b[l][k], 1, x, 2, nullptr,
+                                                   nullptr, fmt(ws, pp, p.h1[0], D)));
+      }
+    }
+  }
+  return QMC_OK;
+}
+
+qmc_status psi_local_energy(qmc_model* m, int batch, const float* electrons, float* e_local, float* ke,
+                            float* pe, float* logpsi, uint8_t* flags, void* ws, cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const float* ar = m->arena;
+  const int chunk = psi_fl_chunk(m, batch);
+  for (int b0 = 0; b0 < batch; b0 += chunk) {
+    const int Bc = std::min(chunk, batch - b0);
+    const PsiPlan pp = psi_fl_plan(m, Bc);
+    const Plan& p = pp.base;
+    float* pe_ws = at<float>(ws, p.pe);
+    QMC_PROF(QMC_KC_FEATURES,
+             launch_psi_features_fl(s, Bc, d.n, d.n_up, d.A, p.Tp, p.T, d.K0p, electrons + (size_t)b0 * 3 * d.n,
+                                    ar + m->a.atoms, ar + m->a.charges, m->nuclear_repulsion,
+                                    d.jastrow ? ar + P.alpha_par : nullptr, at<float>(ws, p.x0), at<float>(ws, p.rae),
+                                    at<float>(ws, p.aevec), pe_ws, at<float>(ws, pp.jas), at<float>(ws, pp.jgl)));
+    if (p.mixed) QMC_TRY(psi_backbone_fl<StSplit>(m, pp, ws, s, fmt_split));
+    else QMC_TRY(psi_backbone_fl<StF32>(m, pp, ws, s, fmt_f32));
+    QMC_TRY(run_orbitals(m, p, ws, 0, s));
+    float* lp = logpsi ? logpsi + b0 : at<float>(ws, p.lpsi);
+    QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, Bc, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe_ws, lp,
+                                          at<float>(ws, p.sgn), ke ? ke + b0 : nullptr, e_local + b0,
+                                          flags ? flags + b0 : nullptr, nullptr, nullptr, at<float>(ws, pp.jgl)));
+    QMC_PROF(QMC_KC_OTHER, (k_psi_add<<<(Bc + 255) / 256, 256, 0, s>>>(Bc, lp, at<float>(ws, pp.jas)),
+                            cudaGetLastError()));
+    if (pe) QMC_CUDA(cudaMemcpyAsync(pe + b0, pe_ws, sizeof(float) * Bc, cudaMemcpyDeviceToDevice, s));
+  }
   return QMC_OK;
 }
 
@@ -642,6 +783,7 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   if (e == cudaSuccess) e = cudaMemset(m->arena_bf16, 0, fa.total_bf16 * sizeof(__nv_bfloat16));
   memcpy(m->atoms_host, atoms_host, sizeof(float) * 3 * A);
   memcpy(m->charges_host, charges_host, sizeof(float) * A);
+  m->nuclear_repulsion = nuclear_repulsion(atoms_host, charges_host, A);
   if (e == cudaSuccess) e = cudaMemcpy(m->arena + fa.atoms, atoms_host, sizeof(float) * 3 * A, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(m->arena + fa.charges, charges_host, sizeof(float) * A, cudaMemcpyHostToDevice);

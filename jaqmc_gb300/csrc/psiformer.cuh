@@ -61,10 +61,33 @@ struct PsiPlan {
   size_t z;     // [rows][max(3D, mlp)] f32 GEMM output
   size_t att;   // [rows][D] attention output, GEMM input
   size_t jas;   // [B] Jastrow
+  size_t jgl;   // [B][3n+1] Jastrow gradient and Laplacian (forward-Laplacian passes)
   size_t in_plane;  // bf16 elements between planes of xn / att / h1[0]
 };
 
 PsiPlan psi_make_plan(const qmc_model* m, int B);
+
+// Forward-Laplacian local energy (psiformer.cu driver, psiformer_fl.cu kernels).
+// Rows carry T = 3n+2 tangents (padded to the tensor-core tile in the mixed
+// form); walkers run in chunks of psi_fl_chunk so the workspace stays bounded.
+PsiPlan psi_fl_plan(const qmc_model* m, int B);
+int psi_fl_chunk(const qmc_model* m, int batch);
+qmc_status psi_fl_check(const qmc_model* m);
+qmc_status psi_local_energy(qmc_model* m, int batch, const float* electrons, float* e_local, float* ke,
+                            float* pe, float* logpsi, uint8_t* flags, void* ws, cudaStream_t s);
+
+cudaError_t launch_psi_features_fl(cudaStream_t s, int B, int n, int n_up, int A, int Tp, int T, int K0p,
+                                   const float* x, const float* atoms, const float* charges, double nuc,
+                                   const float* alpha, float* X0, float* rae, float* aevec, float* pe,
+                                   float* jas, float* jgl);
+template <class Out>
+cudaError_t launch_psi_group_fl(cudaStream_t s, int groups, int Tp, int D, const float* z, int ldz,
+                                const float* bias, int act, float* x, int xmode, const float* ln_s,
+                                const float* ln_b, Out out);
+template <class Out>
+cudaError_t launch_psi_attention_fl(cudaStream_t s, int B, int n, int Tp, int T, int H, int Dh, const float* qkv,
+                                    const float* bqkv, Out out);
+bool psi_attention_fl_supported(int n, int Dh);
 qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* electrons, float* logpsi,
                         float* sign, uint8_t* flags, cudaStream_t s);
 qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s);
