@@ -220,9 +220,13 @@ def psiformer_forward_flops(cfg, n, A):
     return 2 * (n * per_row + attn)
 
 
-def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10):
+def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=8, burn_in=50):
     """Benzene Psiformer (4 layers, 4 x 64 heads, MLP 256, K = 16, SimpleEE
-    Jastrow), split-BF16 GEMMs: walker-steps/s of ``mh_steps`` MH updates."""
+    Jastrow): walker-steps/s of requests of ``mh_steps`` MH updates + the
+    forward-Laplacian E_L and its FP64 mean/variance, in the split-BF16 and the
+    FP32 form, on walkers burnt in from |psi|^2; the two forms' batch-mean
+    energies on identical walkers, and both against the FP64 oracle on the
+    first ``oracle_walkers`` walkers."""
     import torch
 
     from jaqmc_gb300 import _native
@@ -230,39 +234,74 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10):
     from jaqmc_gb300 import systems as S
     mol = S.benzene()
     cfg = P.PsiformerConfig(nspins=mol.nspins)
-    flat = torch.as_tensor(P.flatten(P.init_psiformer(cfg, mol.n_atoms, seed=0),
-                                     P.psiformer_leaves(cfg, mol.n_atoms)), device=dev)
-    m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision="mixed", device=dev)
-    m.set_params(flat)
-    x = torch.as_tensor(S.init_walkers(mol, walkers, seed=1), device=dev)
-    for k in range(warmup):
-        m.mh_steps(x, mh_steps, 0.02, 2, k * mh_steps)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for k in range(steps):
-        m.mh_steps(x, mh_steps, 0.02, 2, (warmup + k) * mh_steps)
-    e1.record()
-    torch.cuda.synchronize()
-    assert m.check_error() == 0
-    ms = e0.elapsed_time(e1) / steps
-    _native.profile_enable(True)
-    _native.profile_read()
-    m.mh_steps(x, mh_steps, 0.02, 2, (warmup + steps) * mh_steps)
-    prof = _native.profile_read()
-    _native.profile_enable(False)
+    tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
+    flat = torch.as_tensor(P.flatten(tree, P.psiformer_leaves(cfg, mol.n_atoms)), device=dev)
+    models = {}
+    for prec in ("mixed", "fp32"):
+        m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision=prec, device=dev)
+        m.set_params(flat)
+        models[prec] = m
+    x0 = torch.as_tensor(S.init_walkers(mol, walkers, seed=1), device=dev)
+    models["mixed"].mh_steps(x0, burn_in, 0.15, 1000, 0)
+
+    def request(m, x, counter):
+        m.mh_steps(x, mh_steps, 0.02, 2, counter)
+        return _native.reduce_mean_var(m.local_energy(x)["e_local"])
+
     names = {"stream_layer": "gemm", "pair": "attention", "means": "bias_act_residual_layernorm",
              "layer0": "input_layer", "orbital": "orbital", "logdet": "logdet", "features": "features_jastrow",
              "mh": "mh", "other": "other", "broadcast": "broadcast"}
-    flops = psiformer_forward_flops(cfg, mol.n_electrons, mol.n_atoms) * walkers * (mh_steps + 1)
-    pk, kind = peaks()
+    forms = {}
+    counter = 0
+    for prec, m in models.items():
+        x = x0.clone()
+        for _ in range(warmup):
+            request(m, x, counter)
+            counter += mh_steps
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            mv = request(m, x, counter)
+            counter += mh_steps
+        e1.record()
+        torch.cuda.synchronize()
+        assert m.check_error() == 0
+        ms = e0.elapsed_time(e1) / steps
+        _native.profile_enable(True)
+        _native.profile_read()
+        request(m, x, counter)
+        counter += mh_steps
+        prof = _native.profile_read()
+        _native.profile_enable(False)
+        forms[prec] = {"ms_per_request": ms, "walker_steps_per_s": walkers * mh_steps / (ms / 1e3),
+                       "E_mean_var": mv.cpu().numpy().tolist(),
+                       "gpu_launches_per_request": sum(v[0] for v in prof.values()),
+                       "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]}}
+    el = {p: m.local_energy(x0)["e_local"].double() for p, m in models.items()}
+    d_mean = float((el["mixed"].mean() - el["fp32"].mean()).abs())
+    d_oracle = None
+    if oracle_walkers:
+        from oracle import hamiltonian as OH
+        from oracle import psiformer as OP
+        sub = x0[:oracle_walkers].double().cpu()
+        oc = OP.PsiformerConfig(nspins=cfg.nspins, ndets=cfg.ndets, num_layers=cfg.num_layers,
+                                num_heads=cfg.num_heads, heads_dim=cfg.heads_dim,
+                                mlp_hidden_dims=list(cfg.mlp_hidden_dims), envelope=cfg.envelope,
+                                orbitals_spin_split=cfg.orbitals_spin_split, jastrow=cfg.jastrow)
+        r = OP.evaluate_fl(tree, oc, sub, mol.atoms)
+        el64 = (OH.kinetic_from_tangents(r["grad"], r["lap"]) + OH.potential_energy(sub, mol.atoms, mol.charges))
+        d_oracle = {"walkers": int(sub.shape[0])}
+        for p in models:
+            e = el[p][:oracle_walkers].cpu()
+            d_oracle[p] = {"dE_mean": float(e.mean() - el64.mean()), "max_abs": float((e - el64).abs().max())}
     return {"workload": f"C6H6 Psiformer 4x(4x64), MLP 256, K=16, SimpleEE Jastrow, {walkers} walkers, "
-                        f"{mh_steps} MH steps, split-BF16",
-            "walker_steps_per_s": walkers * mh_steps / (ms / 1e3), "ms_per_call": ms,
-            "tflops": flops / (ms / 1e3) / 1e12,
-            "frac_of_bf16_sustained": flops / (ms / 1e3) / 1e12 / pk["bf16_tflops_sustained"],
-            "kernel_ms_per_call": {names.get(k, k): v[1] for k, v in prof.items() if v[0]},
-            "local_energy": "not built (value path only)"}
+                        f"{mh_steps} MH steps + forward-Laplacian E_L",
+            "walker_steps_per_s": forms["mixed"]["walker_steps_per_s"],
+            "forms": forms,
+            "mixed_over_plain": forms["fp32"]["ms_per_request"] / forms["mixed"]["ms_per_request"],
+            "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
+            "dE_vs_fp64_oracle_Ha": d_oracle}
 
 
 # ----------------------------------------------------------------- serving
@@ -598,18 +637,15 @@ def main():
     wl = dict(WORKLOADS[args.workload])
     if args.walkers:
         wl["walkers"] = args.walkers
-    if args.request_only and wl.get("model") == "psiformer":
+    if wl.get("model") == "psiformer" and args.impl != "reference":
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(run_psiformer(torch.device("cuda", 0), args.steps, args.warmup, walkers=wl["walkers"],
-                                       mh_steps=wl["mh_steps"])), flush=True)
+                                       mh_steps=wl["mh_steps"], oracle_walkers=0 if args.no_cpu else 8)),
+              flush=True)
         return 0
     if args.request_only:
         return run_request_only(args, wl)
-    if wl.get("model") == "psiformer":
-        print("the Psiformer workload runs with --request-only (MH only: its local energy is not built)",
-              file=sys.stderr)
-        return 2
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

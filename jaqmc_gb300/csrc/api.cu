@@ -239,6 +239,7 @@ Plan make_plan(const qmc_model* m, int op, int B) {
   p.xp = take((size_t)B * d.n * 12);
   p.lp = take((size_t)B * 4);
   p.refac = take(16);
+  p.redo = take((size_t)B);
   p.total = o;
   return p;
 }
@@ -557,7 +558,8 @@ qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, fl
                                                    at<float>(ws, p.rae), at<float>(ws, p.amat)));
   }
   QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
-                                        flags, nullptr, mode == 1 ? &env : nullptr));
+                                        flags, nullptr, mode == 1 ? &env : nullptr, nullptr,
+                                        at<uint8_t>(ws, p.redo)));
   return QMC_OK;
 }
 

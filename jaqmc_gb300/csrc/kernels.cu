@@ -1107,6 +1107,12 @@ template cudaError_t launch_mean_h2<StSplit>(cudaStream_t, int, int, int, int, i
 // =====================================================================
 // FP64 re-factorisation threshold on the pivot growth factor max|U| / max|A|.
 constexpr float kRefactorGrowth = 1e6f;
+// Tangent passes with n > 16 also re-factorise in FP64 when the smallest
+// pivot is below kRefactorPivot x max|A| (condition number >~ 1e4): the traces
+// tr(P_d^2) of such a determinant lose to FP32 inversion error what the
+// kinetic energy needs (measured on 42-electron walkers: FP32 errors of up to
+// 20 Ha fall to 0.03 Ha).
+constexpr float kRefactorPivot = 1e-4f;
 
 __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -1130,7 +1136,7 @@ struct DetOut {
 // Returns the pivot growth factor max|U| / max|A| in *growth.
 template <typename S>
 __device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* sgn, double* growth,
-                        int* singular) {
+                        int* singular, double* pivmin = nullptr) {
   const int lane = threadIdx.x & 31;
   for (int i = lane; i < n; i += 32) perm[i] = i;
   S amax = (S)0;
@@ -1141,6 +1147,7 @@ __device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* 
   int ex = 0;
   float sg = 1.f;
   int sing = 0;
+  S pmn = (S)INFINITY;
   for (int k = 0; k < n; ++k) {
     S best = (S)-1;
     int bi = k;
@@ -1169,6 +1176,7 @@ __device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* 
     __syncwarp();
     S piv = LU[k * ld + k];
     if (!(fabs(piv) > (S)0)) { sing = 1; break; }
+    pmn = fmin(pmn, (S)fabs(piv));
     if (piv < (S)0) sg = -sg;
     int e2;
     mant = frexp(mant * (S)fabs(piv), &e2);
@@ -1191,6 +1199,7 @@ __device__ void warp_lu(S* LU, int n, int ld, int* perm, double* logabs, float* 
   *sgn = sg;
   *growth = sing ? INFINITY : (double)umax / (double)amax;
   *singular = sing;
+  if (pivmin) *pivmin = sing ? 0.0 : (double)pmn / (double)amax;
 }
 
 // Per-warp scratch for one determinant: LU and A^-1 (row stride ld), the
@@ -1410,7 +1419,7 @@ __device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak
 // Ak: the matrix (row stride rs floats); tangent t at Ak + t * ts.
 template <typename S, int NMAX>
 __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, char* scratch,
-                            float* t1s, bool fp64_pass) {
+                            float* t1s, bool fp64_pass, float piv_thresh) {
   const int lane = threadIdx.x & 31;
   const DetScratch sc(n);
   const int ld = sc.ld, ldm = sc.ldm;
@@ -1422,9 +1431,11 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, 
   DetOut o{};
   for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (S)Ak[(e / n) * rs + (e % n)];
   __syncwarp();
-  double growth;
-  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular);
-  o.refactor = (!fp64_pass && !o.singular && !(growth <= (double)kRefactorGrowth)) ? 1 : 0;
+  double growth, pivmin;
+  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular, &pivmin);
+  o.refactor = (!fp64_pass && !o.singular &&
+                (!(growth <= (double)kRefactorGrowth) || (T > 1 && pivmin < (double)piv_thresh)))
+                   ? 1 : 0;
   if (T <= 1 || o.singular || o.refactor) return o;
   warp_inverse<S>(LU, Ainv, perm, n, ld);
   if constexpr (sizeof(S) == 4 && NMAX <= 16) {
@@ -1452,53 +1463,17 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, 
   return o;
 }
 
-template <int NMAX>
-__global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
-                         const float* __restrict__ pe, float* __restrict__ logpsi,
-                         float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
-                         uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
-                         const float* __restrict__ gl_add) {
-  extern __shared__ double shd[];
-  const int w = blockIdx.x;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nw = blockDim.x >> 5;
+// Warp 0 of a walker's block: FP64 signed log-sum-exp over the K
+// determinants and, for T > 1, the gradient, Laplacian and kinetic energy
+// from the per-determinant traces (lds / sgs / tLs / t2s / qs / t1s in shared
+// memory; ints = {any refactored, any singular}).
+__device__ void logdet_finish(int w, int K, int T, double* lds, float* sgs, float* tLs, const float* t2s,
+                              const float* qs, const float* t1s, const int* ints, const float* __restrict__ pe,
+                              float* __restrict__ logpsi, float* __restrict__ sign, float* __restrict__ ke,
+                              float* __restrict__ el, uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
+                              const float* __restrict__ gl_add) {
+  const int lane = threadIdx.x & 31;
   const int D = T > 1 ? T - 2 : 0;
-  // shared layout: per-det results, then per-warp scratch
-  double* lds = shd;                                    // [K]
-  float* sgs = reinterpret_cast<float*>(lds + K);       // [K]
-  float* tLs = sgs + K;                                 // [K]
-  float* t2s = tLs + K;                                 // [K]
-  float* qs = t2s + K;                                  // [K]
-  float* t1s = qs + K;                                  // [K][D]
-  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);  // flags [2]
-  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
-  const DetScratch sc(n);
-  char* scratch = reinterpret_cast<char*>(shd) + head + sc.bytes * warp;
-  if (threadIdx.x < 2) ints[threadIdx.x] = 0;
-  __syncthreads();
-  for (int k = warp; k < K; k += nw) {
-    const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
-    const int rs = amat_row_stride(Tp, n, K);
-    const size_t ts = amat_tangent_stride(n, K);
-    float* t1k = t1s + (size_t)k * D;
-    DetOut o = det_stage<float, NMAX>(Ak, n, T, rs, ts, scratch, t1k, false);
-    if (o.refactor) {
-      o = det_stage<double, NMAX>(Ak, n, T, rs, ts, scratch, t1k, true);
-      o.refactor = 1;
-    }
-    if (lane == 0) {
-      lds[k] = o.ld;
-      sgs[k] = o.singular ? 0.f : o.sgn;
-      tLs[k] = o.tL;
-      t2s[k] = o.t2;
-      qs[k] = o.q;
-      if (o.refactor) atomicOr(&ints[0], 1);
-      if (o.singular) atomicOr(&ints[1], 1);
-    }
-    __syncwarp();
-  }
-  __syncthreads();
-  if (warp != 0) return;
   // FP64 signed log-sum-exp over determinants, one determinant per lane
   double lmax = -INFINITY;
   for (int k = lane; k < K; k += 32)
@@ -1515,9 +1490,9 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
     // w_k = s_k exp(ld_k - max) / S, once per determinant (FP64)
     float* wk = tLs;  // reuse: tL_k is folded into the per-det term below
     for (int k = lane; k < K; k += 32) {
-      double w = sgs[k] != 0.f ? (double)sgs[k] * exp(lds[k] - lmax) / Ssum : 0.0;
-      lds[k] = w * ((double)tLs[k] - (double)t2s[k] + (double)qs[k]);
-      wk[k] = (float)w;
+      const double wt = sgs[k] != 0.f ? (double)sgs[k] * exp(lds[k] - lmax) / Ssum : 0.0;
+      lds[k] = wt * ((double)tLs[k] - (double)t2s[k] + (double)qs[k]);
+      wk[k] = (float)wt;
     }
     __syncwarp();
     // grad_d = sum_k w_k t1_kd ; lap = sum_k w_k (tL - t2 + q) - |grad|^2
@@ -1553,6 +1528,173 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
     if (flags) flags[w] = f;
     if (ints[0] && n_refactor) atomicAdd(n_refactor, 1);
   }
+}
+
+template <int NMAX>
+__global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
+                         const float* __restrict__ pe, float* __restrict__ logpsi,
+                         float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
+                         uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
+                         const float* __restrict__ gl_add, const uint8_t* __restrict__ only) {
+  extern __shared__ double shd[];
+  const int w = blockIdx.x;
+  if (only && !only[w]) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  const int D = T > 1 ? T - 2 : 0;
+  // shared layout: per-det results, then per-warp scratch
+  double* lds = shd;                                    // [K]
+  float* sgs = reinterpret_cast<float*>(lds + K);       // [K]
+  float* tLs = sgs + K;                                 // [K]
+  float* t2s = tLs + K;                                 // [K]
+  float* qs = t2s + K;                                  // [K]
+  float* t1s = qs + K;                                  // [K][D]
+  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);  // flags [2]
+  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
+  const DetScratch sc(n);
+  char* scratch = reinterpret_cast<char*>(shd) + head + sc.bytes * warp;
+  if (threadIdx.x < 2) ints[threadIdx.x] = 0;
+  __syncthreads();
+  for (int k = warp; k < K; k += nw) {
+    const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
+    const int rs = amat_row_stride(Tp, n, K);
+    const size_t ts = amat_tangent_stride(n, K);
+    float* t1k = t1s + (size_t)k * D;
+    DetOut o = det_stage<float, NMAX>(Ak, n, T, rs, ts, scratch, t1k, false, only ? kRefactorPivot : 0.f);
+    if (o.refactor) {
+      o = det_stage<double, NMAX>(Ak, n, T, rs, ts, scratch, t1k, true, 0.f);
+      o.refactor = 1;
+    }
+    if (lane == 0) {
+      lds[k] = o.ld;
+      sgs[k] = o.singular ? 0.f : o.sgn;
+      tLs[k] = o.tL;
+      t2s[k] = o.t2;
+      qs[k] = o.q;
+      if (o.refactor) atomicOr(&ints[0], 1);
+      if (o.singular) atomicOr(&ints[1], 1);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, n_refactor, gl_add);
+}
+
+// Tangent determinant stage for 16 < n <= 64 in FP32: one block per walker,
+// the K determinants in turn.  Warp 0 factorises and inverts A_k; then every
+// warp takes a share of the Jacobian directions d, computing
+// P_d = A_k^-1 J_d A_k column by column into its own shared-memory tile for
+// t1_d = tr P_d and tr(P_d^2), while all threads share tL = tr(A_k^-1 L A_k).
+// A walker with a determinant whose pivot growth exceeds kRefactorGrowth, or
+// whose smallest pivot is below kRefactorPivot x max|A|, is left whole to the
+// FP64 pass: redo[w] = 1, and k_logdet recomputes it.
+struct WideShape {
+  int ld, ldm;
+  size_t head, bytes;
+  __host__ __device__ WideShape(int n, int K, int D, int nw) {
+    ld = (n + 3) / 4 * 4;
+    ldm = (n % 2 == 0) ? n + 1 : n + 2;
+    head = align_up((size_t)K * 8 + (size_t)4 * K * 4 + (size_t)K * D * 4 + 16 + (size_t)nw * 12, 16);
+    bytes = head + (size_t)2 * n * ld * 4 + align_up((size_t)n * 4, 16) + (size_t)nw * n * ldm * 4;
+  }
+};
+
+template <int NMAX>
+__global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp, int T, const float* __restrict__ A,
+                                                            const float* __restrict__ pe, float* __restrict__ logpsi,
+                                                            float* __restrict__ sign, float* __restrict__ ke,
+                                                            float* __restrict__ el, uint8_t* __restrict__ flags,
+                                                            uint8_t* __restrict__ redo,
+                                                            const float* __restrict__ gl_add) {
+  extern __shared__ double shd[];
+  const int w = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int D = T - 2;
+  const WideShape sh(n, K, D, nw);
+  const int ld = sh.ld, ldm = sh.ldm;
+  double* lds = shd;                                         // [K]
+  float* sgs = reinterpret_cast<float*>(lds + K);            // [K]
+  float* tLs = sgs + K;                                      // [K]
+  float* t2s = tLs + K;                                      // [K]
+  float* qs = t2s + K;                                       // [K]
+  float* t1s = qs + K;                                       // [K][D]
+  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);   // refactor, singular, skip this det
+  float* red = reinterpret_cast<float*>(ints + 4);           // [nw][3]
+  float* LU = reinterpret_cast<float*>(reinterpret_cast<char*>(shd) + sh.head);
+  float* Ainv = LU + (size_t)n * ld;
+  int* perm = reinterpret_cast<int*>(Ainv + (size_t)n * ld);
+  float* Ms = reinterpret_cast<float*>(reinterpret_cast<char*>(perm) + align_up((size_t)n * 4, 16)) +
+              (size_t)warp * n * ldm;
+  if (threadIdx.x < 3) ints[threadIdx.x] = 0;
+  const int rs = amat_row_stride(Tp, n, K);
+  const size_t ts = amat_tangent_stride(n, K);
+  for (int k = 0; k < K; ++k) {
+    const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
+    __syncthreads();  // the previous determinant is done with LU / Ainv / red
+    if (warp == 0) {
+      for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = Ak[(e / n) * rs + (e % n)];
+      __syncwarp();
+      double ldv, growth, pivmin;
+      float sg;
+      int sing;
+      warp_lu<float>(LU, n, ld, perm, &ldv, &sg, &growth, &sing, &pivmin);
+      const bool refac = !sing && (!(growth <= (double)kRefactorGrowth) || pivmin < (double)kRefactorPivot);
+      if (!sing && !refac) warp_inverse<float>(LU, Ainv, perm, n, ld);
+      if (lane == 0) {
+        lds[k] = ldv;
+        sgs[k] = sing ? 0.f : sg;
+        ints[2] = sing || refac;
+        if (refac) ints[0] = 1;
+        if (sing) ints[1] = 1;
+      }
+    }
+    __syncthreads();
+    if (ints[0]) break;
+    if (ints[2]) {  // singular: no tangents (its weight in the sum is zero)
+      for (int d = threadIdx.x; d < D; d += blockDim.x) t1s[(size_t)k * D + d] = 0.f;
+      if (threadIdx.x == 0) tLs[k] = t2s[k] = qs[k] = 0.f;
+      continue;
+    }
+    float tl = 0.f;
+    {
+      const float* L = Ak + ts;
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int m = e / n, i = e - m * n;
+        tl = fmaf(Ainv[i * ld + m], L[m * rs + i], tl);
+      }
+    }
+    tl = warp_sum(tl);
+    float t2acc = 0.f, qacc = 0.f;
+    for (int d = warp; d < D; d += nw) {
+      const float tr = warp_product_f32<NMAX>(Ainv, Ak + (size_t)(2 + d) * ts, Ms, n, ld, ldm, rs);
+      const float t2 = warp_trace_sq<float>(Ms, n, ldm);
+      if (lane == 0) t1s[(size_t)k * D + d] = tr;
+      t2acc += t2;
+      qacc = fmaf(tr, tr, qacc);
+    }
+    if (lane == 0) {
+      red[3 * warp] = tl;
+      red[3 * warp + 1] = t2acc;
+      red[3 * warp + 2] = qacc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float a = 0.f, b = 0.f, c = 0.f;
+      for (int v = 0; v < nw; ++v) {
+        a += red[3 * v];
+        b += red[3 * v + 1];
+        c += red[3 * v + 2];
+      }
+      tLs[k] = a;
+      t2s[k] = b;
+      qs[k] = c;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) redo[w] = ints[0] ? 1 : 0;
+  if (ints[0] || warp != 0) return;
+  logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
 }
 
 // Value-only determinant stage (MH passes): LU in registers.  A segment of
@@ -1683,7 +1825,7 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
           for (int e = lane; e < n * n; e += 32) Am[e] *= Em[e];
           __syncwarp();
         }
-        DetOut o = det_stage<double, 16>(Am, n, 1, n, (size_t)n * n, scratch, nullptr, true);
+        DetOut o = det_stage<double, 16>(Am, n, 1, n, (size_t)n * n, scratch, nullptr, true, 0.f);
         if (lane == 0) {
           lds[mloc] = o.ld;
           sgs[mloc] = o.singular ? 0.f : o.sgn;
@@ -1849,7 +1991,36 @@ static cudaError_t launch_logdet_value_smem(cudaStream_t s, int B, int n, int K,
 
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
-                          uint8_t* flags, int* n_refactor, const EnvArgs* env, const float* gl_add) {
+                          uint8_t* flags, int* n_refactor, const EnvArgs* env, const float* gl_add,
+                          uint8_t* redo) {
+  const uint8_t* only = nullptr;
+  if (T > 1 && n > 16 && n <= 64 && redo && !env) {
+    const int nw = 8;
+    const WideShape sh(n, K, T - 2, nw);
+    if (sh.bytes <= 110 * 1024) {
+      int dev;
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e != cudaSuccess) return e;
+#define QMC_LDW(NM)                                                                               \
+  {                                                                                               \
+    static int set_dev = -1;                                                                      \
+    if (set_dev != dev) {                                                                         \
+      e = cudaFuncSetAttribute(k_logdet_fl_wide<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                               110 * 1024);                                                       \
+      if (e != cudaSuccess) return e;                                                             \
+      set_dev = dev;                                                                              \
+    }                                                                                             \
+    k_logdet_fl_wide<NM><<<B, 32 * nw, sh.bytes, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el,   \
+                                                      flags, redo, gl_add);                       \
+  }
+      if (n <= 32) QMC_LDW(32)
+      else QMC_LDW(64)
+#undef QMC_LDW
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      only = redo;  // the FP64 pass below visits the walkers marked in redo only
+    }
+  }
   if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, const_cast<float*>(A), logpsi, sign, flags, env);
   if (T == 1 && n <= 64 && !env) return launch_logdet_value_smem(s, B, n, K, A, logpsi, sign, flags);
   if (env) return cudaErrorInvalidValue;  // tangent passes take enveloped matrices
@@ -1875,7 +2046,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
       set_dev = dev;                                                                        \
     }                                                                                       \
     k_logdet<NM><<<B, 32 * nw, sm, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags,    \
-                                        n_refactor, gl_add);                                \
+                                        n_refactor, gl_add, only);                          \
   }
   if (n <= 8) QMC_LD(8)
   else if (n <= 16) QMC_LD(16)
