@@ -220,13 +220,15 @@ def psiformer_forward_flops(cfg, n, A):
     return 2 * (n * per_row + attn)
 
 
-def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=8, burn_in=50):
+def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=8, burn_in=50,
+                  forms=("mixed", "fp32")):
     """Benzene Psiformer (4 layers, 4 x 64 heads, MLP 256, K = 16, SimpleEE
     Jastrow): walker-steps/s of requests of ``mh_steps`` MH updates + the
     forward-Laplacian E_L and its FP64 mean/variance, in the split-BF16 and the
     FP32 form, on walkers burnt in from |psi|^2; the two forms' batch-mean
     energies on identical walkers, and both against the FP64 oracle on the
-    first ``oracle_walkers`` walkers."""
+    first ``oracle_walkers`` walkers.  ``forms`` may name one form only (a
+    profiler run); the cross-form figures are then left out."""
     import torch
 
     from jaqmc_gb300 import _native
@@ -237,12 +239,12 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
     tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
     flat = torch.as_tensor(P.flatten(tree, P.psiformer_leaves(cfg, mol.n_atoms)), device=dev)
     models = {}
-    for prec in ("mixed", "fp32"):
+    for prec in forms:
         m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision=prec, device=dev)
         m.set_params(flat)
         models[prec] = m
     x0 = torch.as_tensor(S.init_walkers(mol, walkers, seed=1), device=dev)
-    models["mixed"].mh_steps(x0, burn_in, 0.15, 1000, 0)
+    models[forms[0]].mh_steps(x0, burn_in, 0.15, 1000, 0)
 
     def request(m, x, counter):
         m.mh_steps(x, mh_steps, 0.02, 2, counter)
@@ -279,7 +281,7 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
                        "gpu_launches_per_request": sum(v[0] for v in prof.values()),
                        "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]}}
     el = {p: m.local_energy(x0)["e_local"].double() for p, m in models.items()}
-    d_mean = float((el["mixed"].mean() - el["fp32"].mean()).abs())
+    d_mean = float((el["mixed"].mean() - el["fp32"].mean()).abs()) if len(el) == 2 else None
     d_oracle = None
     if oracle_walkers:
         from oracle import hamiltonian as OH
@@ -297,9 +299,10 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
             d_oracle[p] = {"dE_mean": float(e.mean() - el64.mean()), "max_abs": float((e - el64).abs().max())}
     return {"workload": f"C6H6 Psiformer 4x(4x64), MLP 256, K=16, SimpleEE Jastrow, {walkers} walkers, "
                         f"{mh_steps} MH steps + forward-Laplacian E_L",
-            "walker_steps_per_s": forms["mixed"]["walker_steps_per_s"],
+            "walker_steps_per_s": forms[next(iter(forms))]["walker_steps_per_s"],
             "forms": forms,
-            "mixed_over_plain": forms["fp32"]["ms_per_request"] / forms["mixed"]["ms_per_request"],
+            "mixed_over_plain": (forms["fp32"]["ms_per_request"] / forms["mixed"]["ms_per_request"]
+                                 if len(forms) == 2 else None),
             "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
             "dE_vs_fp64_oracle_Ha": d_oracle}
 
@@ -640,9 +643,10 @@ def main():
     if wl.get("model") == "psiformer" and args.impl != "reference":
         import torch
         torch.cuda.set_device(0)
+        forms = (args.precision,) if args.request_only else ("mixed", "fp32")
         print(json.dumps(run_psiformer(torch.device("cuda", 0), args.steps, args.warmup, walkers=wl["walkers"],
-                                       mh_steps=wl["mh_steps"], oracle_walkers=0 if args.no_cpu else 8)),
-              flush=True)
+                                       mh_steps=wl["mh_steps"], oracle_walkers=0 if args.no_cpu else 8,
+                                       forms=forms)), flush=True)
         return 0
     if args.request_only:
         return run_request_only(args, wl)

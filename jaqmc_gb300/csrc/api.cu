@@ -239,7 +239,7 @@ Plan make_plan(const qmc_model* m, int op, int B) {
   p.xp = take((size_t)B * d.n * 12);
   p.lp = take((size_t)B * 4);
   p.refac = take(16);
-  p.redo = take((size_t)B);
+  p.redo = take(logdet_fl_scratch_bytes(B, d.K, p.T));
   p.total = o;
   return p;
 }
@@ -559,7 +559,7 @@ qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, fl
   }
   QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
                                         flags, nullptr, mode == 1 ? &env : nullptr, nullptr,
-                                        at<uint8_t>(ws, p.redo)));
+                                        at<void>(ws, p.redo)));
   return QMC_OK;
 }
 

@@ -1419,7 +1419,7 @@ __device__ void det_tangents_f32(const float* Ainv, const float* __restrict__ Ak
 // Ak: the matrix (row stride rs floats); tangent t at Ak + t * ts.
 template <typename S, int NMAX>
 __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, char* scratch,
-                            float* t1s, bool fp64_pass, float piv_thresh) {
+                            float* t1s, bool fp64_pass) {
   const int lane = threadIdx.x & 31;
   const DetScratch sc(n);
   const int ld = sc.ld, ldm = sc.ldm;
@@ -1431,11 +1431,9 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, 
   DetOut o{};
   for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (S)Ak[(e / n) * rs + (e % n)];
   __syncwarp();
-  double growth, pivmin;
-  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular, &pivmin);
-  o.refactor = (!fp64_pass && !o.singular &&
-                (!(growth <= (double)kRefactorGrowth) || (T > 1 && pivmin < (double)piv_thresh)))
-                   ? 1 : 0;
+  double growth;
+  warp_lu<S>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular);
+  o.refactor = (!fp64_pass && !o.singular && !(growth <= (double)kRefactorGrowth)) ? 1 : 0;
   if (T <= 1 || o.singular || o.refactor) return o;
   warp_inverse<S>(LU, Ainv, perm, n, ld);
   if constexpr (sizeof(S) == 4 && NMAX <= 16) {
@@ -1535,10 +1533,9 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
                          const float* __restrict__ pe, float* __restrict__ logpsi,
                          float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
                          uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
-                         const float* __restrict__ gl_add, const uint8_t* __restrict__ only) {
+                         const float* __restrict__ gl_add) {
   extern __shared__ double shd[];
   const int w = blockIdx.x;
-  if (only && !only[w]) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
   const int D = T > 1 ? T - 2 : 0;
@@ -1560,9 +1557,9 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
     const int rs = amat_row_stride(Tp, n, K);
     const size_t ts = amat_tangent_stride(n, K);
     float* t1k = t1s + (size_t)k * D;
-    DetOut o = det_stage<float, NMAX>(Ak, n, T, rs, ts, scratch, t1k, false, only ? kRefactorPivot : 0.f);
+    DetOut o = det_stage<float, NMAX>(Ak, n, T, rs, ts, scratch, t1k, false);
     if (o.refactor) {
-      o = det_stage<double, NMAX>(Ak, n, T, rs, ts, scratch, t1k, true, 0.f);
+      o = det_stage<double, NMAX>(Ak, n, T, rs, ts, scratch, t1k, true);
       o.refactor = 1;
     }
     if (lane == 0) {
@@ -1581,14 +1578,23 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, n_refactor, gl_add);
 }
 
-// Tangent determinant stage for 16 < n <= 64 in FP32: one block per walker,
-// the K determinants in turn.  Warp 0 factorises and inverts A_k; then every
-// warp takes a share of the Jacobian directions d, computing
+// Tangent determinant stage for 16 < n <= 64: three launches.
+//
+// k_logdet_fl_wide (FP32, one block of 8 warps per walker, the K
+// determinants in turn): warp 0 factorises and inverts A_k; then every warp
+// takes a share of the Jacobian directions d, computing
 // P_d = A_k^-1 J_d A_k column by column into its own shared-memory tile for
 // t1_d = tr P_d and tr(P_d^2), while all threads share tL = tr(A_k^-1 L A_k).
-// A walker with a determinant whose pivot growth exceeds kRefactorGrowth, or
-// whose smallest pivot is below kRefactorPivot x max|A|, is left whole to the
-// FP64 pass: redo[w] = 1, and k_logdet recomputes it.
+// A determinant whose pivot growth exceeds kRefactorGrowth, or whose smallest
+// pivot is below kRefactorPivot x max|A|, is marked instead: inverting it in
+// FP64 and forming its products in FP32 is not enough (the products cancel),
+// so it goes whole to FP64.  A walker without marked determinants finishes in
+// this kernel; one with marks leaves its per-determinant results in a record
+// in global memory.
+//
+// k_logdet_fl_det64 (one warp per marked (walker, determinant)) recomputes
+// the marked determinants in FP64 into the records, spread over the GPU, and
+// k_logdet_fl_finish completes the marked walkers from their records.
 struct WideShape {
   int ld, ldm;
   size_t head, bytes;
@@ -1600,18 +1606,42 @@ struct WideShape {
   }
 };
 
+// Per-walker record of the determinant results (global scratch):
+// ld[K] (double), sg[K], tL[K], t2[K], q[K], t1[K][D] (float), mark[K] (byte),
+// any-singular (int).
+struct DetRecord {
+  size_t sg, tL, t2, q, t1, mark, sing, bytes;
+  __host__ __device__ DetRecord(int K, int D) {
+    sg = (size_t)K * 8;
+    tL = sg + (size_t)K * 4;
+    t2 = tL + (size_t)K * 4;
+    q = t2 + (size_t)K * 4;
+    t1 = q + (size_t)K * 4;
+    mark = t1 + (size_t)K * D * 4;
+    sing = align_up(mark + (size_t)K, 4);
+    bytes = align_up(sing + 4, 16);
+  }
+};
+
+size_t logdet_fl_scratch_bytes(int B, int K, int T) {
+  const int D = T > 1 ? T - 2 : 0;
+  return align_up((size_t)B, 16) + (size_t)B * DetRecord(K, D).bytes;
+}
+
 template <int NMAX>
 __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp, int T, const float* __restrict__ A,
                                                             const float* __restrict__ pe, float* __restrict__ logpsi,
                                                             float* __restrict__ sign, float* __restrict__ ke,
                                                             float* __restrict__ el, uint8_t* __restrict__ flags,
-                                                            uint8_t* __restrict__ redo,
+                                                            uint8_t* __restrict__ redo, char* __restrict__ records,
                                                             const float* __restrict__ gl_add) {
   extern __shared__ double shd[];
   const int w = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int D = T - 2;
   const WideShape sh(n, K, D, nw);
+  const DetRecord rec(K, D);
+  char* rw = records + (size_t)w * rec.bytes;
   const int ld = sh.ld, ldm = sh.ldm;
   double* lds = shd;                                         // [K]
   float* sgs = reinterpret_cast<float*>(lds + K);            // [K]
@@ -1619,7 +1649,7 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
   float* t2s = tLs + K;                                      // [K]
   float* qs = t2s + K;                                       // [K]
   float* t1s = qs + K;                                       // [K][D]
-  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);   // refactor, singular, skip this det
+  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);   // any marked, any singular, skip this det
   float* red = reinterpret_cast<float*>(ints + 4);           // [nw][3]
   float* LU = reinterpret_cast<float*>(reinterpret_cast<char*>(shd) + sh.head);
   float* Ainv = LU + (size_t)n * ld;
@@ -1639,19 +1669,19 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
       float sg;
       int sing;
       warp_lu<float>(LU, n, ld, perm, &ldv, &sg, &growth, &sing, &pivmin);
-      const bool refac = !sing && (!(growth <= (double)kRefactorGrowth) || pivmin < (double)kRefactorPivot);
-      if (!sing && !refac) warp_inverse<float>(LU, Ainv, perm, n, ld);
+      const bool mark = !sing && (!(growth <= (double)kRefactorGrowth) || pivmin < (double)kRefactorPivot);
+      if (!sing && !mark) warp_inverse<float>(LU, Ainv, perm, n, ld);
       if (lane == 0) {
         lds[k] = ldv;
         sgs[k] = sing ? 0.f : sg;
-        ints[2] = sing || refac;
-        if (refac) ints[0] = 1;
+        ints[2] = sing || mark;
+        if (mark) ints[0] = 1;
         if (sing) ints[1] = 1;
+        reinterpret_cast<uint8_t*>(rw + rec.mark)[k] = mark ? 1 : 0;
       }
     }
     __syncthreads();
-    if (ints[0]) break;
-    if (ints[2]) {  // singular: no tangents (its weight in the sum is zero)
+    if (ints[2]) {  // singular (zero weight) or marked (recomputed in FP64)
       for (int d = threadIdx.x; d < D; d += blockDim.x) t1s[(size_t)k * D + d] = 0.f;
       if (threadIdx.x == 0) tLs[k] = t2s[k] = qs[k] = 0.f;
       continue;
@@ -1693,7 +1723,87 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
   }
   __syncthreads();
   if (threadIdx.x == 0) redo[w] = ints[0] ? 1 : 0;
-  if (ints[0] || warp != 0) return;
+  if (ints[0]) {  // leave the record for the FP64 pass
+    double* rld = reinterpret_cast<double*>(rw);
+    float* rsg = reinterpret_cast<float*>(rw + rec.sg);
+    float* rtL = reinterpret_cast<float*>(rw + rec.tL);
+    float* rt2 = reinterpret_cast<float*>(rw + rec.t2);
+    float* rq = reinterpret_cast<float*>(rw + rec.q);
+    float* rt1 = reinterpret_cast<float*>(rw + rec.t1);
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      rld[k] = lds[k];
+      rsg[k] = sgs[k];
+      rtL[k] = tLs[k];
+      rt2[k] = t2s[k];
+      rq[k] = qs[k];
+    }
+    for (int e = threadIdx.x; e < K * D; e += blockDim.x) rt1[e] = t1s[e];
+    if (threadIdx.x == 0) *reinterpret_cast<int*>(rw + rec.sing) = ints[1];
+    return;
+  }
+  if (warp != 0) return;
+  logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
+}
+
+template <int NMAX>
+__global__ void __launch_bounds__(32) k_logdet_fl_det64(int n, int K, int Tp, int T, const float* __restrict__ A,
+                                                         const uint8_t* __restrict__ redo, char* __restrict__ records) {
+  extern __shared__ double shd[];
+  const int w = blockIdx.x / K, k = blockIdx.x % K;
+  if (!redo[w]) return;
+  const int D = T - 2;
+  const DetRecord rec(K, D);
+  char* rw = records + (size_t)w * rec.bytes;
+  if (!reinterpret_cast<const uint8_t*>(rw + rec.mark)[k]) return;
+  const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
+  float* t1k = reinterpret_cast<float*>(rw + rec.t1) + (size_t)k * D;
+  const DetOut o = det_stage<double, NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K),
+                                           reinterpret_cast<char*>(shd), t1k, true);
+  if ((threadIdx.x & 31) == 0) {
+    reinterpret_cast<double*>(rw)[k] = o.ld;
+    reinterpret_cast<float*>(rw + rec.sg)[k] = o.singular ? 0.f : o.sgn;
+    reinterpret_cast<float*>(rw + rec.tL)[k] = o.singular ? 0.f : o.tL;
+    reinterpret_cast<float*>(rw + rec.t2)[k] = o.singular ? 0.f : o.t2;
+    reinterpret_cast<float*>(rw + rec.q)[k] = o.singular ? 0.f : o.q;
+    if (o.singular) {
+      for (int d = 0; d < D; ++d) t1k[d] = 0.f;
+      atomicOr(reinterpret_cast<int*>(rw + rec.sing), 1);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32) k_logdet_fl_finish(int K, int T, const uint8_t* __restrict__ redo,
+                                                          const char* __restrict__ records,
+                                                          const float* __restrict__ pe, float* __restrict__ logpsi,
+                                                          float* __restrict__ sign, float* __restrict__ ke,
+                                                          float* __restrict__ el, uint8_t* __restrict__ flags,
+                                                          const float* __restrict__ gl_add) {
+  extern __shared__ double shd[];
+  const int w = blockIdx.x;
+  if (!redo[w]) return;
+  const int D = T - 2;
+  const DetRecord rec(K, D);
+  const char* rw = records + (size_t)w * rec.bytes;
+  double* lds = shd;
+  float* sgs = reinterpret_cast<float*>(lds + K);
+  float* tLs = sgs + K;
+  float* t2s = tLs + K;
+  float* qs = t2s + K;
+  float* t1s = qs + K;
+  int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    lds[k] = reinterpret_cast<const double*>(rw)[k];
+    sgs[k] = reinterpret_cast<const float*>(rw + rec.sg)[k];
+    tLs[k] = reinterpret_cast<const float*>(rw + rec.tL)[k];
+    t2s[k] = reinterpret_cast<const float*>(rw + rec.t2)[k];
+    qs[k] = reinterpret_cast<const float*>(rw + rec.q)[k];
+  }
+  for (int e = threadIdx.x; e < K * D; e += blockDim.x) t1s[e] = reinterpret_cast<const float*>(rw + rec.t1)[e];
+  if (threadIdx.x == 0) {
+    ints[0] = 1;
+    ints[1] = *reinterpret_cast<const int*>(rw + rec.sing);
+  }
+  __syncwarp();
   logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
 }
 
@@ -1825,7 +1935,7 @@ __global__ void __launch_bounds__(256) k_logdet_value(int B, int n, int K, int W
           for (int e = lane; e < n * n; e += 32) Am[e] *= Em[e];
           __syncwarp();
         }
-        DetOut o = det_stage<double, 16>(Am, n, 1, n, (size_t)n * n, scratch, nullptr, true, 0.f);
+        DetOut o = det_stage<double, 16>(Am, n, 1, n, (size_t)n * n, scratch, nullptr, true);
         if (lane == 0) {
           lds[mloc] = o.ld;
           sgs[mloc] = o.singular ? 0.f : o.sgn;
@@ -1992,33 +2102,40 @@ static cudaError_t launch_logdet_value_smem(cudaStream_t s, int B, int n, int K,
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor, const EnvArgs* env, const float* gl_add,
-                          uint8_t* redo) {
-  const uint8_t* only = nullptr;
-  if (T > 1 && n > 16 && n <= 64 && redo && !env) {
+                          void* fl_scratch) {
+  if (T > 1 && n > 16 && n <= 64 && fl_scratch && !env) {
     const int nw = 8;
     const WideShape sh(n, K, T - 2, nw);
-    if (sh.bytes <= 110 * 1024) {
+    const DetScratch sc(n);
+    const size_t fin = (size_t)K * 8 + (size_t)4 * K * 4 + (size_t)K * (T - 2) * 4 + 16;
+    if (sh.bytes <= 110 * 1024 && sc.bytes <= 110 * 1024 && fin <= 110 * 1024) {
+      uint8_t* redo = static_cast<uint8_t*>(fl_scratch);
+      char* records = static_cast<char*>(fl_scratch) + align_up((size_t)B, 16);
       int dev;
       cudaError_t e = cudaGetDevice(&dev);
       if (e != cudaSuccess) return e;
-#define QMC_LDW(NM)                                                                               \
-  {                                                                                               \
-    static int set_dev = -1;                                                                      \
-    if (set_dev != dev) {                                                                         \
-      e = cudaFuncSetAttribute(k_logdet_fl_wide<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                               110 * 1024);                                                       \
-      if (e != cudaSuccess) return e;                                                             \
-      set_dev = dev;                                                                              \
-    }                                                                                             \
-    k_logdet_fl_wide<NM><<<B, 32 * nw, sh.bytes, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el,   \
-                                                      flags, redo, gl_add);                       \
+#define QMC_LDW(NM)                                                                                         \
+  {                                                                                                         \
+    static int set_dev = -1;                                                                                \
+    if (set_dev != dev) {                                                                                   \
+      e = cudaFuncSetAttribute(k_logdet_fl_wide<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024); \
+      if (e == cudaSuccess)                                                                                 \
+        e = cudaFuncSetAttribute(k_logdet_fl_det64<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                                 110 * 1024);                                                               \
+      if (e == cudaSuccess)                                                                                 \
+        e = cudaFuncSetAttribute(k_logdet_fl_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024); \
+      if (e != cudaSuccess) return e;                                                                       \
+      set_dev = dev;                                                                                        \
+    }                                                                                                       \
+    k_logdet_fl_wide<NM><<<B, 32 * nw, sh.bytes, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags, redo, \
+                                                      records, gl_add);                                     \
+    k_logdet_fl_det64<NM><<<B * K, 32, sc.bytes, s>>>(n, K, Tp, T, A, redo, records);                       \
   }
       if (n <= 32) QMC_LDW(32)
       else QMC_LDW(64)
 #undef QMC_LDW
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-      only = redo;  // the FP64 pass below visits the walkers marked in redo only
+      k_logdet_fl_finish<<<B, 32, fin, s>>>(K, T, redo, records, pe, logpsi, sign, ke, el, flags, gl_add);
+      return cudaGetLastError();
     }
   }
   if (T == 1 && n <= 32) return launch_logdet_value(s, B, n, K, const_cast<float*>(A), logpsi, sign, flags, env);
@@ -2046,7 +2163,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
       set_dev = dev;                                                                        \
     }                                                                                       \
     k_logdet<NM><<<B, 32 * nw, sm, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags,    \
-                                        n_refactor, gl_add, only);                          \
+                                        n_refactor, gl_add);                                \
   }
   if (n <= 8) QMC_LD(8)
   else if (n <= 16) QMC_LD(16)

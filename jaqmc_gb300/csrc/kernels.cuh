@@ -63,13 +63,15 @@ cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp
 // signed log-sum-exp and, when T > 1, the slogdet forward-Laplacian traces
 // combined into the kinetic energy.  A: [w][k][Tp][n][n].  gl_add [B][T-1]
 // (optional, tangent passes): gradient (T-2) and Laplacian of a log term added
-// to log|det| before the kinetic energy (the Psiformer's Jastrow).  redo [B]
-// (optional scratch): with it, tangent passes with 16 < n <= 64 run the FP32
-// block-per-walker kernel and send only the walkers it marks to the FP64 pass.
+// to log|det| before the kinetic energy (the Psiformer's Jastrow).
+// fl_scratch (optional, logdet_fl_scratch_bytes): with it, tangent passes with
+// 16 < n <= 64 run the FP32 block-per-walker kernel and recompute only the
+// determinants it marks in FP64.
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor, const EnvArgs* env = nullptr,
-                          const float* gl_add = nullptr, uint8_t* redo = nullptr);
+                          const float* gl_add = nullptr, void* fl_scratch = nullptr);
+size_t logdet_fl_scratch_bytes(int B, int K, int T);
 
 // Cotangent of log|psi| with respect to the value orbital matrices:
 // Abar[w][k] = w_k A_k^{-T}; also writes log|psi| (may be null).

@@ -9,7 +9,7 @@ struct Plan {
   int B, T, Tp, P2, K0p;
   bool mixed;
   size_t x0, h1[2], h2[2], g1, gb, g2, rae, aevec, amat, pe, lpsi, sgn, xp, lp, refac, total;
-  size_t redo;  // [B] bytes: walkers sent to the FP64 determinant pass
+  size_t redo;  // determinant-stage scratch of tangent passes (logdet_fl_scratch_bytes)
   size_t x0s, g2s0;  // mixed form: the first layer's features / pair means as bf16 planes
   size_t act_bytes;  // bytes per one-electron activation (fp32, or two bf16 planes)
   size_t h1_plane, g1_plane, g2_plane;  // bf16 elements between split planes

@@ -471,7 +471,7 @@ PsiPlan psi_fl_plan(const qmc_model* m, int B) {
   p.lpsi = take((size_t)B * 4);
   p.sgn = take((size_t)B * 4);
   p.refac = take(16);
-  p.redo = take((size_t)B);
+  p.redo = take(logdet_fl_scratch_bytes(B, d.K, p.T));
   pp.jas = take((size_t)B * 4);
   pp.jgl = take((size_t)B * (3 * d.n + 1) * 4);
   p.h2[0] = p.h2[1] = p.g1 = p.gb = p.g2 = p.xp = p.lp = o;  // unused by these passes
@@ -572,7 +572,7 @@ qmc_status psi_local_energy(qmc_model* m, int batch, const float* electrons, flo
     QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, Bc, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe_ws, lp,
                                           at<float>(ws, p.sgn), ke ? ke + b0 : nullptr, e_local + b0,
                                           flags ? flags + b0 : nullptr, nullptr, nullptr, at<float>(ws, pp.jgl),
-                                          at<uint8_t>(ws, p.redo)));
+                                          at<void>(ws, p.redo)));
     QMC_PROF(QMC_KC_OTHER, (k_psi_add<<<(Bc + 255) / 256, 256, 0, s>>>(Bc, lp, at<float>(ws, pp.jas)),
                             cudaGetLastError()));
     if (pe) QMC_CUDA(cudaMemcpyAsync(pe + b0, pe_ws, sizeof(float) * Bc, cudaMemcpyDeviceToDevice, s));
