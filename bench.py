@@ -220,6 +220,21 @@ def psiformer_forward_flops(cfg, n, A):
     return 2 * (n * per_row + attn)
 
 
+def psiformer_attention_fl_roofline(cfg, n, walkers, attention_ms):
+    """FP32-SIMT roofline of the forward-Laplacian attention kernel
+    (k_psi_attention_fl) over one E_L of ``walkers`` walkers: per (walker,
+    head, layer) and per direction, the score tangents (2 n^2 Dh FMA), the
+    cross term (n^2 Dh) and the mixing tangents with their cross term
+    (3 n^2 Dh), over 3n directions: 18 n^3 Dh FMA."""
+    if not attention_ms:
+        return None
+    flop = 2.0 * 18 * n ** 3 * cfg.heads_dim * cfg.num_heads * cfg.num_layers * walkers
+    achieved = flop / (attention_ms / 1e3) / 1e12
+    return {"kernel": "k_psi_attention_fl", "bound": "fp32 simt", "achieved": achieved, "peak": FP32_SIMT_PEAK,
+            "unit": "TFLOP/s", "frac": achieved / FP32_SIMT_PEAK, "traffic": None,
+            "algorithmic_flop_per_request": flop}
+
+
 def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=8, burn_in=50,
                   forms=("mixed", "fp32")):
     """Benzene Psiformer (4 layers, 4 x 64 heads, MLP 256, K = 16, SimpleEE
@@ -279,7 +294,9 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         forms[prec] = {"ms_per_request": ms, "walker_steps_per_s": walkers * mh_steps / (ms / 1e3),
                        "E_mean_var": mv.cpu().numpy().tolist(),
                        "gpu_launches_per_request": sum(v[0] for v in prof.values()),
-                       "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]}}
+                       "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]},
+                       "roofline_attention": psiformer_attention_fl_roofline(
+                           cfg, mol.n_electrons, walkers, prof.get("pair", (0, 0.0))[1])}
     el = {p: m.local_energy(x0)["e_local"].double() for p, m in models.items()}
     d_mean = float((el["mixed"].mean() - el["fp32"].mean()).abs()) if len(el) == 2 else None
     d_oracle = None
