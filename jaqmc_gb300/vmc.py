@@ -170,8 +170,9 @@ class FermiNetWavefunction:
 class PsiformerWavefunction(FermiNetWavefunction):
     """Psiformer ansatz with the SimpleEE Jastrow (hyper-parameters and
     defaults of ``src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94``),
-    evaluated by the GB300 library: log|psi| and the MH sampler.  Its local
-    energy is not provided by the library (value path only)."""
+    evaluated by the GB300 library: log|psi|, the MH sampler and the
+    forward-Laplacian local energy (the same estimators as FermiNet).  There is
+    no parameter adjoint for it."""
 
     num_layers: int = 4
     num_heads: int = 4

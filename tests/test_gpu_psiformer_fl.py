@@ -135,3 +135,28 @@ def test_benzene_full_config(cuda_device):
         assert np.isfinite(got).all()
         assert (err / np.maximum(1.0, np.abs(r64["e_local"]))).max() < tol, (got, r64["e_local"])
         np.testing.assert_allclose(out["logpsi"].cpu().numpy(), r64["logpsi"], rtol=1e-3)
+
+
+def test_host_mirror_evaluation_stage(cuda_device, tmp_path):
+    """PsiformerWavefunction through the host mirror's evaluation stage
+    (sampling + kinetic / potential / total energy estimators): finite
+    per-step energies, E = <T> + <V>, and the kinetic estimator equal to the
+    library's local energy on the stage's final walkers."""
+    from jaqmc_gb300 import vmc
+    mol = S.lithium()
+    wf = vmc.PsiformerWavefunction(nspins=mol.nspins, **SMALL)
+    x = torch.as_tensor(S.init_walkers(mol, 256, seed=1), device=cuda_device)
+    data = vmc.MoleculeData(x, mol.atoms, mol.charges)
+    params = wf.init_params(data, 0)
+    sampler = vmc.MCMCSampler(steps=5, initial_width=0.1)
+    stage = vmc.EvaluationStage(wf, sampler, vmc.energy_pipeline(wf), iterations=4, burn_in=5,
+                                save_dir=str(tmp_path), prefix="psi")
+    digest, stacked, data_out, *_ = stage.run(params, data, sampler.init(data, 5))
+    for k in ("total_energy", "energy:kinetic", "energy:potential"):
+        assert np.isfinite(np.asarray(stacked[k])).all(), k
+    assert abs(float(digest["total_energy"]) - float(digest["energy:kinetic"])
+               - float(digest["energy:potential"])) < 1e-3 * max(1.0, abs(float(digest["total_energy"])))
+    m = wf.model(data_out, params)
+    out = m.local_energy(data_out.electrons.contiguous())
+    ke = vmc.EuclideanKinetic(f_log_psi=wf).evaluate_batch_walkers(params, vmc.BatchedData(data_out), {}, None)[0]
+    assert torch.equal(ke["energy:kinetic"], out["kinetic"])
