@@ -175,6 +175,50 @@ def cpu_request_rate(wl, seconds=12.0, sample_walkers=64, threads=None):
     return rate, threads, desc
 
 
+def cpu_psiformer_request_rate(seconds=12.0, sample_walkers=4, mh_steps=10, threads=None):
+    """The oracle (torch FP32 on the host cores) running benzene Psiformer
+    requests (``mh_steps`` MH updates + forward-Laplacian E_L) on a bounded
+    sample of walkers; returns (walker-steps/s, cores, description)."""
+    import torch
+
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+    from oracle import hamiltonian as OH
+    from oracle import psiformer as OP
+    threads = threads or os.cpu_count()
+    torch.set_num_threads(threads)
+    mol = S.benzene()
+    cfg = P.PsiformerConfig(nspins=mol.nspins)
+    tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
+    oc = OP.PsiformerConfig(nspins=cfg.nspins, ndets=cfg.ndets, num_layers=cfg.num_layers, num_heads=cfg.num_heads,
+                            heads_dim=cfg.heads_dim, mlp_hidden_dims=list(cfg.mlp_hidden_dims),
+                            envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split, jastrow=cfg.jastrow)
+    f = OP.logpsi_fn(tree, oc, mol.atoms, dtype=torch.float32)
+    x = torch.as_tensor(S.init_walkers(mol, sample_walkers, seed=1))
+    g = torch.Generator().manual_seed(2)
+    reqs, t0 = 0, time.perf_counter()
+    with torch.no_grad():
+        while True:
+            lp = 2 * f(x)
+            for _ in range(mh_steps):
+                x2 = x + 0.02 * torch.randn(x.shape, generator=g)
+                lp2 = 2 * f(x2)
+                acc = (lp2 - lp) > torch.log(torch.rand(lp.shape, generator=g))
+                x = torch.where(acc[:, None, None], x2, x)
+                lp = torch.where(acc, lp2, lp)
+            r = OP.evaluate_fl(tree, oc, x, mol.atoms, dtype=torch.float32)
+            el = OH.kinetic_from_tangents(r["grad"], r["lap"]) + OH.potential_energy(x, mol.atoms, mol.charges)
+            float(el.double().mean())
+            reqs += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
+    dt = time.perf_counter() - t0
+    rate = reqs * sample_walkers * mh_steps / dt
+    desc = (f"oracle (torch fp32, {threads} threads) on {sample_walkers} walkers, "
+            f"{reqs} requests of {mh_steps} MH steps + forward-Laplacian E_L in {dt:.1f} s")
+    return rate, threads, desc
+
+
 def run_reference(args, wl):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -314,6 +358,10 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         for p in models:
             e = el[p][:oracle_walkers].cpu()
             d_oracle[p] = {"dE_mean": float(e.mean() - el64.mean()), "max_abs": float((e - el64).abs().max())}
+    cpu = None
+    if oracle_walkers:
+        r_, cores, desc = cpu_psiformer_request_rate(mh_steps=mh_steps)
+        cpu = {"value": r_, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
     return {"workload": f"C6H6 Psiformer 4x(4x64), MLP 256, K=16, SimpleEE Jastrow, {walkers} walkers, "
                         f"{mh_steps} MH steps + forward-Laplacian E_L",
             "walker_steps_per_s": forms[next(iter(forms))]["walker_steps_per_s"],
@@ -321,7 +369,8 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
             "mixed_over_plain": (forms["fp32"]["ms_per_request"] / forms["mixed"]["ms_per_request"]
                                  if len(forms) == 2 else None),
             "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
-            "dE_vs_fp64_oracle_Ha": d_oracle}
+            "dE_vs_fp64_oracle_Ha": d_oracle,
+            "cpu_baseline": cpu}
 
 
 # ----------------------------------------------------------------- serving
