@@ -358,6 +358,8 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         for p in models:
             e = el[p][:oracle_walkers].cpu()
             d_oracle[p] = {"dE_mean": float(e.mean() - el64.mean()), "max_abs": float((e - el64).abs().max())}
+    del models, el, x0, m, x, mv
+    torch.cuda.empty_cache()  # the E_L workspaces (tens of GB) go back before the next leg
     cpu = None
     if oracle_walkers:
         r_, cores, desc = cpu_psiformer_request_rate(mh_steps=mh_steps)
