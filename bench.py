@@ -279,6 +279,20 @@ def psiformer_attention_fl_roofline(cfg, n, walkers, attention_ms):
             "algorithmic_flop_per_request": flop}
 
 
+def psiformer_request_roofline(cfg, n, A, walkers, mh_steps, ms, prec, pk, pk_kind):
+    """Dense-tangent roofline of a whole request: (mh_steps + 3n + 2) forwards
+    of psiformer_forward_flops per walker over the request's time, against the
+    bf16 sustained peak (mixed form) or the FP32 SIMT peak (plain form)."""
+    flop = psiformer_forward_flops(cfg, n, A) * (mh_steps + 3 * n + 2) * walkers
+    achieved = flop / (ms / 1e3) / 1e12
+    if prec == "mixed":
+        peak, kind = pk["bf16_tflops_sustained"], f"bf16 sustained, {pk_kind}"
+    else:
+        peak, kind = FP32_SIMT_PEAK, "fp32 simt nominal at 2070 MHz"
+    return {"bound": "tensor" if prec == "mixed" else "fp32 simt", "achieved": achieved, "peak": peak,
+            "peak_kind": kind, "unit": "TFLOP/s", "frac": achieved / peak, "algorithmic_tflop_per_request": flop / 1e12}
+
+
 def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=8, burn_in=50,
                   forms=("mixed", "fp32")):
     """Benzene Psiformer (4 layers, 4 x 64 heads, MLP 256, K = 16, SimpleEE
@@ -309,6 +323,7 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         m.mh_steps(x, mh_steps, 0.02, 2, counter)
         return _native.reduce_mean_var(m.local_energy(x)["e_local"])
 
+    pk, pk_kind = peaks()
     names = {"stream_layer": "gemm", "pair": "attention", "means": "bias_act_residual_layernorm",
              "layer0": "input_layer", "orbital": "orbital", "logdet": "logdet", "features": "features_jastrow",
              "mh": "mh", "other": "other", "broadcast": "broadcast"}
@@ -340,7 +355,9 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
                        "gpu_launches_per_request": sum(v[0] for v in prof.values()),
                        "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]},
                        "roofline_attention": psiformer_attention_fl_roofline(
-                           cfg, mol.n_electrons, walkers, prof.get("pair", (0, 0.0))[1])}
+                           cfg, mol.n_electrons, walkers, prof.get("pair", (0, 0.0))[1]),
+                       "roofline_request": psiformer_request_roofline(
+                           cfg, mol.n_electrons, mol.n_atoms, walkers, mh_steps, ms, prec, pk, pk_kind)}
     el = {p: m.local_energy(x0)["e_local"].double() for p, m in models.items()}
     d_mean = float((el["mixed"].mean() - el["fp32"].mean()).abs()) if len(el) == 2 else None
     d_oracle = None
