@@ -327,7 +327,7 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
     names = {"stream_layer": "gemm", "pair": "attention", "means": "bias_act_residual_layernorm",
              "layer0": "input_layer", "orbital": "orbital", "logdet": "logdet", "features": "features_jastrow",
              "mh": "mh", "other": "other", "broadcast": "broadcast"}
-    forms = {}
+    results = {}
     counter = 0
     for prec, m in models.items():
         x = x0.clone()
@@ -350,7 +350,7 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         counter += mh_steps
         prof = _native.profile_read()
         _native.profile_enable(False)
-        forms[prec] = {"ms_per_request": ms, "walker_steps_per_s": walkers * mh_steps / (ms / 1e3),
+        results[prec] = {"ms_per_request": ms, "walker_steps_per_s": walkers * mh_steps / (ms / 1e3),
                        "E_mean_var": mv.cpu().numpy().tolist(),
                        "gpu_launches_per_request": sum(v[0] for v in prof.values()),
                        "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]},
@@ -383,10 +383,10 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         cpu = {"value": r_, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
     return {"workload": f"C6H6 Psiformer 4x(4x64), MLP 256, K=16, SimpleEE Jastrow, {walkers} walkers, "
                         f"{mh_steps} MH steps + forward-Laplacian E_L",
-            "walker_steps_per_s": forms[next(iter(forms))]["walker_steps_per_s"],
-            "forms": forms,
-            "mixed_over_plain": (forms["fp32"]["ms_per_request"] / forms["mixed"]["ms_per_request"]
-                                 if len(forms) == 2 else None),
+            "walker_steps_per_s": results[forms[0]]["walker_steps_per_s"],
+            "forms": results,
+            "mixed_over_plain": (results["fp32"]["ms_per_request"] / results["mixed"]["ms_per_request"]
+                                 if len(results) == 2 else None),
             "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
             "dE_vs_fp64_oracle_Ha": d_oracle,
             "cpu_baseline": cpu}
