@@ -359,7 +359,11 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
                        "roofline_request": psiformer_request_roofline(
                            cfg, mol.n_electrons, mol.n_atoms, walkers, mh_steps, ms, prec, pk, pk_kind)}
     el = {p: m.local_energy(x0)["e_local"].double() for p, m in models.items()}
-    d_mean = float((el["mixed"].mean() - el["fp32"].mean()).abs()) if len(el) == 2 else None
+    d_mean = d_se = None
+    if len(el) == 2:
+        d = el["mixed"] - el["fp32"]
+        d_mean = float(d.mean().abs())
+        d_se = float(d.std() / d.numel() ** 0.5)
     d_oracle = None
     if oracle_walkers:
         from oracle import hamiltonian as OH
@@ -388,6 +392,7 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
             "mixed_over_plain": (results["fp32"]["ms_per_request"] / results["mixed"]["ms_per_request"]
                                  if len(results) == 2 else None),
             "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
+            "dE_mean_paired_se_Ha": d_se,
             "dE_vs_fp64_oracle_Ha": d_oracle,
             "cpu_baseline": cpu}
 
@@ -540,6 +545,7 @@ def run_ours(args, wl):
     e_plain = models["fp32"].local_energy(xe)["e_local"].double()
     e_mixed = models["mixed"].local_energy(xe)["e_local"].double()
     d_mean = float((e_mixed.mean() - e_plain.mean()).abs())
+    d_se = float((e_mixed - e_plain).std() / e_plain.numel() ** 0.5)
     d_oracle = None
     if rank == 0 and not args.no_cpu:
         import torch as _t
@@ -623,6 +629,7 @@ def run_ours(args, wl):
                           "E_mean_var": r_["mean_var"]} for p, r_ in results.items()},
             "mixed_over_plain": results["fp32"]["ms_per_step"] / results["mixed"]["ms_per_step"],
             "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
+            "dE_mean_paired_se_Ha": d_se,
             "dE_mean_vs_fp64_oracle_Ha": d_oracle,
             "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": int(B * mol.n_electrons * 3 * 4),
                     "d2h_bytes_per_step": 16},
