@@ -134,6 +134,41 @@ class FermiNetWavefunction:
         return logpsi(self.model(data), params, data.electrons)[0]
 
 
+class PsiformerWavefunction(FermiNetWavefunction):
+    """``PsiformerWavefunction``-shaped front end (``src/jaqmc/app/molecule/
+    wavefunction/psiformer.py:38-146``) over the same three custom calls: the
+    library's Psiformer handle serves log|psi|, MH steps and the
+    forward-Laplacian local energy (no parameter adjoint).  UNTESTED."""
+
+    def __init__(self, nspins=(1, 1), ndets=16, num_layers=4, num_heads=4, heads_dim=64, mlp_hidden_dims=(256,),
+                 envelope="abs_isotropic", orbitals_spin_split=True, jastrow="simple_ee", precision="mixed"):
+        from . import params as P
+        self.cfg = P.PsiformerConfig(nspins=tuple(nspins), ndets=ndets, num_layers=num_layers, num_heads=num_heads,
+                                     heads_dim=heads_dim, mlp_hidden_dims=list(mlp_hidden_dims), envelope=envelope,
+                                     orbitals_spin_split=orbitals_spin_split, jastrow=jastrow)
+        self.precision = precision
+        self._models = {}
+
+    def model(self, data):
+        import numpy as np
+
+        from . import _native
+        key = (np.asarray(data.atoms).tobytes(), np.asarray(data.charges).tobytes())
+        if key not in self._models:
+            self._models[key] = _native.NativePsiformer(self.cfg, np.asarray(data.atoms), np.asarray(data.charges),
+                                                        precision=self.precision)
+        return self._models[key]
+
+    def init_params(self, data, rngs):
+        import jax.numpy as jnp
+        import numpy as np
+
+        from . import params as P
+        A = np.asarray(data.atoms).reshape(-1, 3).shape[0]
+        seed = int(np.asarray(rngs).ravel()[-1]) if rngs is not None else 0
+        return jnp.asarray(P.flatten(P.init_psiformer(self.cfg, A, seed=seed), P.psiformer_leaves(self.cfg, A)))
+
+
 class EuclideanKinetic:
     """``estimators.energy.kinetic`` replacement: kinetic energy from the
     library's fused forward Laplacian (``evaluate_batch_walkers`` protocol of
