@@ -224,10 +224,17 @@ def run_reference(args, wl):
     if rank != 0:
         return 0
     rates = []
+    psi = wl.get("model") == "psiformer"
     for _ in range(args.warmup):
-        cpu_request_rate(wl, seconds=1.0, sample_walkers=16)
+        if psi:
+            cpu_psiformer_request_rate(seconds=1.0, sample_walkers=2, mh_steps=wl["mh_steps"])
+        else:
+            cpu_request_rate(wl, seconds=1.0, sample_walkers=16)
     for _ in range(args.steps):
-        r, cores, desc = cpu_request_rate(wl, seconds=4.0, sample_walkers=32)
+        if psi:
+            r, cores, desc = cpu_psiformer_request_rate(seconds=4.0, sample_walkers=4, mh_steps=wl["mh_steps"])
+        else:
+            r, cores, desc = cpu_request_rate(wl, seconds=4.0, sample_walkers=32)
         rates.append(r)
     v = float(np.mean(rates))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
@@ -243,6 +250,9 @@ def run_reference(args, wl):
 
 
 def workload_name(wl, prec):
+    if wl.get("model") == "psiformer":
+        return (f"{wl['system']} Psiformer 4x(4x64), MLP 256, K=16, SimpleEE Jastrow, {wl['walkers']} walkers, "
+                f"{wl['mh_steps']} MH steps + forward-Laplacian E_L, {prec}")
     return (f"{wl['system']} FermiNet 4x(256,32) K=16, {wl['walkers']} walkers, "
             f"{wl['mh_steps']} MH steps + forward-Laplacian E_L, {prec}")
 
