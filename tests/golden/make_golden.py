@@ -1,0 +1,103 @@
+"""Generate the golden fixtures of the parity tests: seeded walkers and the
+FP64 oracle's log|psi|, sign and local energy (with its kinetic and potential
+parts), plus the oracle's own FP32 results, which set the per-walker FP32
+conditioning bars.  Parameters are not stored: they are regenerated from
+their seed by ``jaqmc_gb300.params`` and checked against the stored SHA-256 of
+the flat float32 vector.
+
+    python tests/golden/make_golden.py          # writes tests/golden/*.npz
+
+The reference (JAX/Flax) cannot run in this environment and its own tests hold
+no numeric vectors for these paths, so the values come from the oracle under
+``oracle/``, which is pinned by the property tests in ``tests/test_oracle*.py``.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from jaqmc_gb300 import params as P  # noqa: E402
+from jaqmc_gb300 import systems as S  # noqa: E402
+from oracle import ferminet as OF  # noqa: E402
+from oracle import hamiltonian as OH  # noqa: E402
+from oracle import psiformer as OP  # noqa: E402
+
+PSI_SMALL = dict(ndets=3, num_layers=2, num_heads=4, heads_dim=16, mlp_hidden_dims=[64])
+
+# name: (model, system, config keyword arguments, walkers); params seed 0, walkers seed 1
+CASES = {
+    "ferminet_li_full": ("ferminet", "Li", {}, 48),
+    "ferminet_n2_full": ("ferminet", "N2", {}, 32),
+    "psiformer_li_small": ("psiformer", "Li", PSI_SMALL, 32),
+    "psiformer_ch4_small": ("psiformer", "CH4", PSI_SMALL, 32),
+    "psiformer_c6h6_full": ("psiformer", "C6H6", {}, 2),
+}
+
+
+def build(case):
+    """(mol, cfg, tree, flat, walkers) of a case, from its seeds."""
+    model, system, kw, B = CASES[case]
+    mol = S.SYSTEMS[system]()
+    if model == "ferminet":
+        cfg = P.FermiNetConfig(nspins=mol.nspins, **kw)
+        tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+        flat = P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms))
+    else:
+        cfg = P.PsiformerConfig(nspins=mol.nspins, **kw)
+        tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
+        flat = P.flatten(tree, P.psiformer_leaves(cfg, mol.n_atoms))
+    x = S.init_walkers(mol, B, seed=1)
+    return mol, cfg, tree, np.asarray(flat, np.float32), x
+
+
+def params_sha(flat) -> str:
+    return hashlib.sha256(np.ascontiguousarray(flat, np.float32).tobytes()).hexdigest()
+
+
+def oracle_values(case, mol, cfg, tree, x, dtype):
+    """log|psi|, sign, E_L, kinetic and potential energy from the oracle."""
+    model = CASES[case][0]
+    xt = torch.as_tensor(x, dtype=dtype)
+    if model == "ferminet":
+        oc = OF.FermiNetConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets,
+                               hidden_dims_single=list(cfg.hidden_dims_single),
+                               hidden_dims_double=list(cfg.hidden_dims_double), use_last_layer=cfg.use_last_layer,
+                               envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split)
+        r = OF.evaluate(tree, oc, xt, mol.atoms, dtype=dtype, tangents=True)
+        sign = r["sign_logpsi"]
+    else:
+        oc = OP.PsiformerConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets, num_layers=cfg.num_layers,
+                                num_heads=cfg.num_heads, heads_dim=cfg.heads_dim,
+                                mlp_hidden_dims=list(cfg.mlp_hidden_dims), envelope=cfg.envelope,
+                                orbitals_spin_split=cfg.orbitals_spin_split, jastrow=cfg.jastrow)
+        r = OP.evaluate_fl(tree, oc, xt, mol.atoms, dtype=dtype)
+        sign = r["sign"]
+    ke = OH.kinetic_from_tangents(r["grad"], r["lap"])
+    pe = OH.potential_energy(xt, mol.atoms, mol.charges)
+    f = lambda t: t.detach().double().numpy()  # noqa: E731
+    return {"logpsi": f(r["logpsi"]), "sign": f(sign), "e_local": f(ke + pe), "kinetic": f(ke), "potential": f(pe)}
+
+
+def main():
+    torch.set_num_threads(os.cpu_count() or 1)
+    for case in CASES:
+        mol, cfg, tree, flat, x = build(case)
+        v64 = oracle_values(case, mol, cfg, tree, x, torch.float64)
+        v32 = oracle_values(case, mol, cfg, tree, x, torch.float32)
+        meta = {"case": case, "model": CASES[case][0], "system": CASES[case][1], "config": CASES[case][2],
+                "walkers": CASES[case][3], "params_seed": 0, "walkers_seed": 1, "params_sha256": params_sha(flat)}
+        np.savez_compressed(os.path.join(HERE, f"{case}.npz"), meta=json.dumps(meta), walkers=x.astype(np.float32),
+                            **v64, **{f"{k}_fp32": v for k, v in v32.items()})
+        print(case, "E_L mean", float(v64["e_local"].mean()))
+
+
+if __name__ == "__main__":
+    main()

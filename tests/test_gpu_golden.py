@@ -1,0 +1,59 @@
+"""The FP32 CUDA path against the committed golden fixtures
+(tests/golden/*.npz: seeded walkers, FP64 oracle values and the oracle's own
+FP32 values), through the C ABI.  Bars as in the live-oracle tests: sign
+exact; log|psi| and E_L per walker within 1e-5 relative / 1e-4 Ha at the
+median, tails within a small multiple of the FP32 oracle's own error; the
+potential within 1e-5 relative; the benzene configuration within 2e-3
+relative (E_L) and 1e-3 (log|psi|)."""
+import glob
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+from jaqmc_gb300 import _native
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden as G  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+def test_fp32_path_matches_fixture(path, cuda_device):
+    z = np.load(path)
+    meta = json.loads(str(z["meta"]))
+    mol, cfg, _, flat, _ = G.build(meta["case"])
+    assert G.params_sha(flat) == meta["params_sha256"]
+    cls = _native.NativeFermiNet if meta["model"] == "ferminet" else _native.NativePsiformer
+    m = cls(cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
+    m.set_params(torch.as_tensor(flat, device=cuda_device))
+    x = torch.as_tensor(z["walkers"], device=cuda_device)
+    lp, sg, _ = m.forward(x)
+    out = m.local_energy(x)
+    assert m.check_error() == 0
+    assert np.array_equal(sg.cpu().numpy(), z["sign"])
+    ref = z["logpsi"]
+    err = np.abs(lp.cpu().double().numpy() - ref)
+    e32 = np.abs(z["logpsi_fp32"] - ref)
+    el = out["e_local"].cpu().double().numpy()
+    eerr = np.abs(el - z["e_local"])
+    ee32 = np.abs(z["e_local_fp32"] - z["e_local"])
+    np.testing.assert_allclose(out["potential"].cpu().numpy(), z["potential"], rtol=1e-5, atol=1e-5)
+    if meta["system"] == "C6H6":
+        assert (eerr / np.abs(z["e_local"])).max() < 2e-3
+        np.testing.assert_allclose(lp.cpu().numpy(), ref, rtol=1e-3)
+        return
+    tol = 1e-5 * np.maximum(1.0, np.abs(ref)).max()
+    assert np.median(err) <= 3 * np.median(e32) + tol
+    assert err.max() <= 20 * e32.max() + 10 * tol
+    assert np.median(eerr) <= 3 * np.median(ee32) + 1e-4
+    assert np.quantile(eerr, 0.9) <= 3 * np.quantile(ee32, 0.9) + 1e-4
+    assert eerr.max() <= 20 * ee32.max() + 1e-3
+    assert abs(el.mean() - z["e_local"].mean()) <= 3 * ee32.mean() + 5e-4
