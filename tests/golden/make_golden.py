@@ -1,9 +1,12 @@
 """Generate the golden fixtures of the parity tests: seeded walkers and the
 FP64 oracle's log|psi|, sign and local energy (with its kinetic and potential
 parts), plus the oracle's own FP32 results, which set the per-walker FP32
-conditioning bars.  Parameters are not stored: they are regenerated from
-their seed by ``jaqmc_gb300.params`` and checked against the stored SHA-256 of
-the flat float32 vector.
+conditioning bars; and MH fixtures: walkers, Philox4x32-10 draws (the
+oracle's restatement, injected on both sides) and the FP64 oracle's accept
+counts, final walkers, log-probabilities and acceptance ratios.  Parameters
+are not stored: they are regenerated from their seed by
+``jaqmc_gb300.params`` and checked against the stored SHA-256 of the flat
+float32 vector.
 
     python tests/golden/make_golden.py          # writes tests/golden/*.npz
 
@@ -28,6 +31,8 @@ from jaqmc_gb300 import params as P  # noqa: E402
 from jaqmc_gb300 import systems as S  # noqa: E402
 from oracle import ferminet as OF  # noqa: E402
 from oracle import hamiltonian as OH  # noqa: E402
+from oracle import mcmc as OM  # noqa: E402
+from oracle import philox as OX  # noqa: E402
 from oracle import psiformer as OP  # noqa: E402
 
 PSI_SMALL = dict(ndets=3, num_layers=2, num_heads=4, heads_dim=16, mlp_hidden_dims=[64])
@@ -39,6 +44,14 @@ CASES = {
     "psiformer_li_small": ("psiformer", "Li", PSI_SMALL, 32),
     "psiformer_ch4_small": ("psiformer", "CH4", PSI_SMALL, 32),
     "psiformer_c6h6_full": ("psiformer", "C6H6", {}, 2),
+}
+
+
+# MH fixtures: name -> (case whose model and system they use, walkers, steps, stddev, seed)
+MH_CASES = {
+    "mh_ferminet_li_full": ("ferminet_li_full", 64, 3, 0.02, 2),
+    "mh_ferminet_n2_full": ("ferminet_n2_full", 64, 3, 0.02, 2),
+    "mh_psiformer_li_small": ("psiformer_li_small", 64, 3, 0.05, 4),
 }
 
 
@@ -86,8 +99,51 @@ def oracle_values(case, mol, cfg, tree, x, dtype):
     return {"logpsi": f(r["logpsi"]), "sign": f(sign), "e_local": f(ke + pe), "kinetic": f(ke), "potential": f(pe)}
 
 
+def logpsi_fn(case, mol, cfg, tree):
+    """FP64 oracle log|psi| of a case's model, as a function of the walkers."""
+    if CASES[case][0] == "ferminet":
+        oc = OF.FermiNetConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets,
+                               hidden_dims_single=list(cfg.hidden_dims_single),
+                               hidden_dims_double=list(cfg.hidden_dims_double), use_last_layer=cfg.use_last_layer,
+                               envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split)
+        return OF.logpsi_fn(tree, oc, mol.atoms)
+    oc = OP.PsiformerConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets, num_layers=cfg.num_layers,
+                            num_heads=cfg.num_heads, heads_dim=cfg.heads_dim, mlp_hidden_dims=list(cfg.mlp_hidden_dims),
+                            envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split, jastrow=cfg.jastrow)
+    return OP.logpsi_fn(tree, oc, torch.as_tensor(mol.atoms, dtype=torch.float64))
+
+
+def build_mh(name):
+    """(mol, cfg, tree, flat, walkers, normals, uniforms) of an MH fixture."""
+    case, B, steps, _, seed = MH_CASES[name]
+    mol, cfg, tree, flat, _ = build(case)
+    x = S.init_walkers(mol, B, seed=1)
+    draws = [OX.mh_draws(seed, s, B, mol.n_electrons) for s in range(steps)]
+    normals = np.stack([d[0] for d in draws]).astype(np.float32)
+    uniforms = np.stack([d[1] for d in draws]).astype(np.float32)
+    return mol, cfg, tree, flat, x, normals, uniforms
+
+
+def oracle_mh(name, mol, cfg, tree, x, normals, uniforms):
+    case, _, _, stddev, _ = MH_CASES[name]
+    f = logpsi_fn(case, mol, cfg, tree)
+    xo, lpo, acc, ratios = OM.mh_steps(f, torch.as_tensor(x, dtype=torch.float64),
+                                       torch.as_tensor(normals, dtype=torch.float64),
+                                       torch.as_tensor(uniforms, dtype=torch.float64), stddev)
+    return {"x_final": xo.numpy(), "log_prob": lpo.numpy(), "accepts": acc.numpy(), "ratios": ratios.numpy()}
+
+
 def main():
     torch.set_num_threads(os.cpu_count() or 1)
+    for name in MH_CASES:
+        mol, cfg, tree, flat, x, normals, uniforms = build_mh(name)
+        v = oracle_mh(name, mol, cfg, tree, x, normals, uniforms)
+        case, B, steps, stddev, seed = MH_CASES[name]
+        meta = {"case": name, "model_case": case, "model": CASES[case][0], "walkers": B, "steps": steps,
+                "stddev": stddev, "seed": seed, "params_sha256": params_sha(flat)}
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), meta=json.dumps(meta), walkers=x.astype(np.float32),
+                            normals=normals, uniforms=uniforms, **v)
+        print(name, "accepts", int(v["accepts"].sum()))
     for case in CASES:
         mol, cfg, tree, flat, x = build(case)
         v64 = oracle_values(case, mol, cfg, tree, x, torch.float64)

@@ -1,6 +1,7 @@
 """The golden fixtures (tests/golden/*.npz, written by tests/golden/make_golden.py)
-on the CPU: the seeded parameters and walkers regenerate bit for bit, and the
-FP64 oracle reproduces the stored log|psi|, sign and local energies."""
+on the CPU: the seeded parameters, walkers and Philox draws regenerate bit for
+bit, and the FP64 oracle reproduces the stored log|psi|, sign, local energies
+and MH updates."""
 import glob
 import json
 import os
@@ -15,13 +16,29 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden as G  # noqa: E402
 
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+VALUE = [f for f in FIXTURES if not os.path.basename(f).startswith("mh_")]
+MH = [f for f in FIXTURES if os.path.basename(f).startswith("mh_")]
 
 
 def test_every_case_has_a_fixture():
-    assert sorted(os.path.basename(f)[:-4] for f in FIXTURES) == sorted(G.CASES)
+    assert sorted(os.path.basename(f)[:-4] for f in FIXTURES) == sorted(list(G.CASES) + list(G.MH_CASES))
 
 
-@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+@pytest.mark.parametrize("path", MH, ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_reproduces_mh_fixture(path):
+    z = np.load(path)
+    meta = json.loads(str(z["meta"]))
+    mol, cfg, tree, flat, x, normals, uniforms = G.build_mh(meta["case"])
+    assert G.params_sha(flat) == meta["params_sha256"]
+    assert np.array_equal(x.astype(np.float32), z["walkers"])
+    assert np.array_equal(normals, z["normals"]) and np.array_equal(uniforms, z["uniforms"])
+    v = G.oracle_mh(meta["case"], mol, cfg, tree, x, normals, uniforms)
+    assert np.array_equal(v["accepts"], z["accepts"])
+    np.testing.assert_allclose(v["x_final"], z["x_final"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(v["log_prob"], z["log_prob"], rtol=1e-11, atol=1e-10)
+
+
+@pytest.mark.parametrize("path", VALUE, ids=lambda p: os.path.basename(p)[:-4])
 def test_oracle_reproduces_fixture(path):
     z = np.load(path)
     meta = json.loads(str(z["meta"]))

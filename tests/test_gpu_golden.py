@@ -23,9 +23,36 @@ import make_golden as G  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+VALUE = [f for f in FIXTURES if not os.path.basename(f).startswith("mh_")]
+MH = [f for f in FIXTURES if os.path.basename(f).startswith("mh_")]
 
 
-@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+@pytest.mark.parametrize("path", MH, ids=lambda p: os.path.basename(p)[:-4])
+def test_mh_matches_fixture(path, cuda_device):
+    """The fixture's Philox draws injected into qmc_mh_steps: accept counts
+    bit-exact on the walkers with no near tie (|ratio - log u| < 1e-4 at any
+    step, excluded and counted), positions within 1e-5, 2 log|psi| within 1e-4."""
+    z = np.load(path)
+    meta = json.loads(str(z["meta"]))
+    mol, cfg, _, flat, _ = G.build(meta["model_case"])
+    assert G.params_sha(flat) == meta["params_sha256"]
+    cls = _native.NativeFermiNet if meta["model"] == "ferminet" else _native.NativePsiformer
+    m = cls(cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
+    m.set_params(torch.as_tensor(flat, device=cuda_device))
+    xg = torch.as_tensor(z["walkers"], device=cuda_device).clone()
+    nz = torch.as_tensor(z["normals"], device=cuda_device)
+    uz = torch.as_tensor(z["uniforms"], device=cuda_device)
+    _, lpg, accg, _ = m.mh_steps(xg, meta["steps"], meta["stddev"], meta["seed"], 0, normals=nz, uniforms=uz)
+    assert m.check_error() == 0
+    near = (np.abs(z["ratios"] - np.log(z["uniforms"].astype(np.float64))) < 1e-4).any(0)
+    keep = ~near
+    assert keep.sum() >= meta["walkers"] - 2
+    assert np.array_equal(accg.cpu().numpy()[keep], z["accepts"][keep])
+    np.testing.assert_allclose(xg.cpu().numpy()[keep], z["x_final"][keep], atol=1e-5)
+    np.testing.assert_allclose(lpg.cpu().numpy()[keep], z["log_prob"][keep], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.parametrize("path", VALUE, ids=lambda p: os.path.basename(p)[:-4])
 def test_fp32_path_matches_fixture(path, cuda_device):
     z = np.load(path)
     meta = json.loads(str(z["meta"]))
