@@ -3,7 +3,10 @@ FP64 oracle's log|psi|, sign and local energy (with its kinetic and potential
 parts), plus the oracle's own FP32 results, which set the per-walker FP32
 conditioning bars; and MH fixtures: walkers, Philox4x32-10 draws (the
 oracle's restatement, injected on both sides) and the FP64 oracle's accept
-counts, final walkers, log-probabilities and acceptance ratios.  Parameters
+counts, final walkers, log-probabilities and acceptance ratios; and a
+gradient fixture: the FP64 oracle's per-walker d log|psi| / d theta (torch
+autograd, the role of the reference's jax.grad) on 64 seeded parameter
+entries and projected on 8 seeded random unit vectors.  Parameters
 are not stored: they are regenerated from their seed by
 ``jaqmc_gb300.params`` and checked against the stored SHA-256 of the flat
 float32 vector.
@@ -53,6 +56,21 @@ MH_CASES = {
     "mh_ferminet_n2_full": ("ferminet_n2_full", 64, 3, 0.02, 2),
     "mh_psiformer_li_small": ("psiformer_li_small", 64, 3, 0.05, 4),
 }
+
+
+# gradient fixtures: name -> (case, walkers, seed of the entries and projections, entries, projections)
+GRAD_CASES = {
+    "grad_ferminet_ch4_full": ("ferminet_ch4_full", 4, 64, 64, 8),
+}
+CASES["ferminet_ch4_full"] = ("ferminet", "CH4", {}, 4)
+
+
+def grad_probes(P_, seed, entries, projections):
+    """Seeded parameter entries and unit projection vectors (P, projections)."""
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(P_, entries, replace=False))
+    R = rng.standard_normal((P_, projections))
+    return idx, R / np.linalg.norm(R, axis=0)
 
 
 def build(case):
@@ -133,8 +151,28 @@ def oracle_mh(name, mol, cfg, tree, x, normals, uniforms):
     return {"x_final": xo.numpy(), "log_prob": lpo.numpy(), "accepts": acc.numpy(), "ratios": ratios.numpy()}
 
 
+def oracle_grad(name):
+    """(flat, walkers, meta-free values) of a gradient fixture."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from helpers import oracle_param_jacobian
+    case, B, seed, entries, projections = GRAD_CASES[name]
+    mol, cfg, _, flat, _ = build(case)
+    x = S.init_walkers(mol, B, seed=1)
+    J, lp = oracle_param_jacobian(flat, cfg, mol, x)
+    idx, R = grad_probes(flat.size, seed, entries, projections)
+    return flat, x, {"entries": idx, "jacobian_entries": J[:, idx], "projections": J @ R,
+                     "jacobian_norm": np.linalg.norm(J, axis=1), "logpsi": lp}
+
+
 def main():
     torch.set_num_threads(os.cpu_count() or 1)
+    for name in GRAD_CASES:
+        flat, x, v = oracle_grad(name)
+        case, B, seed, entries, projections = GRAD_CASES[name]
+        meta = {"case": name, "model_case": case, "walkers": B, "seed": seed, "params_sha256": params_sha(flat)}
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), meta=json.dumps(meta), walkers=x.astype(np.float32),
+                            **v)
+        print(name, "|J| per walker", v["jacobian_norm"])
     for name in MH_CASES:
         mol, cfg, tree, flat, x, normals, uniforms = build_mh(name)
         v = oracle_mh(name, mol, cfg, tree, x, normals, uniforms)
@@ -145,6 +183,8 @@ def main():
                             normals=normals, uniforms=uniforms, **v)
         print(name, "accepts", int(v["accepts"].sum()))
     for case in CASES:
+        if case in (c[0] for c in GRAD_CASES.values()):
+            continue  # a model for the gradient fixture only
         mol, cfg, tree, flat, x = build(case)
         v64 = oracle_values(case, mol, cfg, tree, x, torch.float64)
         v32 = oracle_values(case, mol, cfg, tree, x, torch.float32)

@@ -23,8 +23,34 @@ import make_golden as G  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
-VALUE = [f for f in FIXTURES if not os.path.basename(f).startswith("mh_")]
 MH = [f for f in FIXTURES if os.path.basename(f).startswith("mh_")]
+GRAD = [f for f in FIXTURES if os.path.basename(f).startswith("grad_")]
+VALUE = [f for f in FIXTURES if f not in MH and f not in GRAD]
+
+
+@pytest.mark.parametrize("path", GRAD, ids=lambda p: os.path.basename(p)[:-4])
+def test_grad_matches_fixture(path, cuda_device):
+    """The adjoint's per-walker d log|psi| / d theta against the FP64 oracle's
+    on the fixture's 64 entries (error <= 1e-3 of each walker's largest
+    component) and along its 8 seeded unit directions (RMS error <= 1e-2 of
+    the oracle's |J| / sqrt(P), i.e. the live test's per-walker bar)."""
+    z = np.load(path)
+    meta = json.loads(str(z["meta"]))
+    case, B, seed, entries, projections = G.GRAD_CASES[meta["case"]]
+    mol, cfg, _, flat, _ = G.build(case)
+    assert G.params_sha(flat) == meta["params_sha256"]
+    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, device=cuda_device)
+    m.set_params(torch.as_tensor(flat, device=cuda_device))
+    J, _, lp = m.grad(torch.as_tensor(z["walkers"], device=cuda_device), per_walker=True)
+    assert m.check_error() == 0
+    J = J.double().cpu().numpy()
+    idx, R = G.grad_probes(flat.size, seed, entries, projections)
+    assert np.array_equal(idx, z["entries"])
+    scale = np.abs(J).max(axis=1, keepdims=True)
+    assert (np.abs(J[:, idx] - z["jacobian_entries"]) / scale).max() <= 1e-3
+    rms = np.sqrt(((J @ R - z["projections"]) ** 2).mean(axis=1))
+    assert (rms / (z["jacobian_norm"] / np.sqrt(flat.size))).max() <= 1e-2
+    np.testing.assert_allclose(lp.cpu().numpy(), z["logpsi"], rtol=1e-4, atol=1e-4)
 
 
 @pytest.mark.parametrize("path", MH, ids=lambda p: os.path.basename(p)[:-4])
