@@ -32,8 +32,9 @@ VALUE = [f for f in FIXTURES if f not in MH and f not in GRAD]
 def test_grad_matches_fixture(path, cuda_device):
     """The adjoint's per-walker d log|psi| / d theta against the FP64 oracle's
     on the fixture's 64 entries (error <= 1e-3 of each walker's largest
-    component) and along its 8 seeded unit directions (RMS error <= 1e-2 of
-    the oracle's |J| / sqrt(P), i.e. the live test's per-walker bar)."""
+    component) and along its 8 seeded unit directions (RMS error <= 2e-2 of
+    the oracle's |J| / sqrt(P): the live test's worst-walker bar of 1e-2 on
+    the whole vector, with room for the scatter of an 8-direction estimate)."""
     z = np.load(path)
     meta = json.loads(str(z["meta"]))
     case, B, seed, entries, projections = G.GRAD_CASES[meta["case"]]
@@ -49,7 +50,7 @@ def test_grad_matches_fixture(path, cuda_device):
     scale = np.abs(J).max(axis=1, keepdims=True)
     assert (np.abs(J[:, idx] - z["jacobian_entries"]) / scale).max() <= 1e-3
     rms = np.sqrt(((J @ R - z["projections"]) ** 2).mean(axis=1))
-    assert (rms / (z["jacobian_norm"] / np.sqrt(flat.size))).max() <= 1e-2
+    assert (rms / (z["jacobian_norm"] / np.sqrt(flat.size))).max() <= 2e-2
     np.testing.assert_allclose(lp.cpu().numpy(), z["logpsi"], rtol=1e-4, atol=1e-4)
 
 
