@@ -122,7 +122,11 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
 /* Switch between QMC_PRECISION_FP32 and QMC_PRECISION_MIXED_BF16. */
 qmc_status qmc_model_set_precision(qmc_model* m, int precision);
 
-/* Bytes of workspace needed by `op` (QMC_OP_*) for `batch` walkers. */
+/* Bytes of workspace needed by `op` (QMC_OP_*) for `batch` walkers.  For
+ * QMC_OP_GRAD, and QMC_OP_LOCAL_ENERGY on a Psiformer model, the call runs in
+ * chunks under the model's byte budget (qmc_model_set_grad_budget /
+ * qmc_model_set_energy_budget) and this is one chunk's workspace.  0 for an
+ * op the model does not support. */
 size_t qmc_workspace_size(const qmc_model* m, int op, int batch);
 
 /* log|psi| and sign for a batch: the vmapped FermiNetWavefunction.evaluate /
