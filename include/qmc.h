@@ -1,7 +1,8 @@
 /*
- * qmc.h — C ABI of the GB300 (sm_103a) VMC inner loop: FermiNet log|psi|,
- * forward-Laplacian local energy and the all-electron Metropolis-Hastings
- * walker step, plus the walker-batch reductions and the parameter adjoint.
+ * qmc.h — C ABI of the GB300 (sm_103a) VMC inner loop: FermiNet and
+ * Psiformer log|psi|, forward-Laplacian local energy and the all-electron
+ * Metropolis-Hastings walker step, plus the walker-batch reductions and the
+ * FermiNet parameter adjoint.
  *
  * Conventions
  *  - Every array argument is caller-owned DEVICE memory unless the name ends
