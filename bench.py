@@ -284,8 +284,9 @@ def psiformer_attention_fl_roofline(cfg, n, walkers, attention_ms):
         return None
     flop = 2.0 * 18 * n ** 3 * cfg.heads_dim * cfg.num_heads * cfg.num_layers * walkers
     achieved = flop / (attention_ms / 1e3) / 1e12
-    return {"kernel": "k_psi_attention_fl", "bound": "fp32 simt", "achieved": achieved, "peak": FP32_SIMT_PEAK,
-            "unit": "TFLOP/s", "frac": achieved / FP32_SIMT_PEAK, "traffic": None,
+    peak = SIMT_PEAK["value"]
+    return {"kernel": "k_psi_attention_fl", "bound": "fp32 simt", "achieved": achieved, "peak": peak,
+            "peak_kind": SIMT_PEAK["source"], "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
             "algorithmic_flop_per_request": flop}
 
 
@@ -298,7 +299,7 @@ def psiformer_request_roofline(cfg, n, A, walkers, mh_steps, ms, prec, pk, pk_ki
     if prec == "mixed":
         peak, kind = pk["bf16_tflops_sustained"], f"bf16 sustained, {pk_kind}"
     else:
-        peak, kind = FP32_SIMT_PEAK, "fp32 simt nominal at 2070 MHz"
+        peak, kind = SIMT_PEAK["value"], SIMT_PEAK["source"]
     return {"bound": "tensor" if prec == "mixed" else "fp32 simt", "achieved": achieved, "peak": peak,
             "peak_kind": kind, "unit": "TFLOP/s", "frac": achieved / peak, "algorithmic_tflop_per_request": flop / 1e12}
 
@@ -497,6 +498,7 @@ def run_ours(args, wl):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    measure_simt_peak(dev)
     mol = S.SYSTEMS[wl["system"]]()
     cfg = P.FermiNetConfig(nspins=mol.nspins)
     tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
@@ -558,18 +560,7 @@ def run_ours(args, wl):
     d_se = float((e_mixed - e_plain).std() / e_plain.numel() ** 0.5)
     d_oracle = None
     if rank == 0 and not args.no_cpu:
-        import torch as _t
-
-        from oracle import ferminet as OF
-        from oracle import hamiltonian as OH
-        sub = xe[:args.oracle_walkers].double().cpu()
-        oc = OF.FermiNetConfig(nspins=cfg.nspins, ndets=cfg.ndets)
-        ref = OF.evaluate(tree, oc, sub, mol.atoms, dtype=_t.float64, tangents=True)
-        el64 = OH.kinetic_from_tangents(ref["grad"], ref["lap"]) + OH.potential_energy(sub, mol.atoms, mol.charges)
-        nsub = sub.shape[0]
-        d_oracle = {p: float(models[p].local_energy(xe[:nsub].contiguous())["e_local"].double().mean().cpu()
-                             - el64.mean()) for p in models}
-        d_oracle["walkers"] = nsub
+        d_oracle = oracle_energy_gap(models, tree, cfg, mol, xe[:args.oracle_walkers].contiguous())
 
     # live per-kernel timing of the same request (second pass, profiler on)
     _native.profile_enable(True)
@@ -626,6 +617,8 @@ def run_ours(args, wl):
         r, cores, desc = cpu_request_rate(wl)
         cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
     if rank == 0:
+        # large nested blocks first, so that the end of the line (what a log
+        # tail shows) carries the N2 figures
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_main, "higher_is_better": True, "scaling": "weak",
@@ -634,23 +627,26 @@ def run_ours(args, wl):
             "config": {"workload": workload_name(wl, prec_main), **wl, "precision": prec_main,
                        "parallelism": f"replicas x{world}",
                        "l2": "working set larger than L2 (local-energy workspace several GB)"},
-            "forms": {p: {"ms_per_step": r_["ms_per_step"],
-                          "walker_steps_per_s": world * B * S_ / (r_["ms_per_step"] / 1e3),
-                          "E_mean_var": r_["mean_var"]} for p, r_ in results.items()},
-            "mixed_over_plain": results["fp32"]["ms_per_step"] / results["mixed"]["ms_per_step"],
-            "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
-            "dE_mean_paired_se_Ha": d_se,
-            "dE_mean_vs_fp64_oracle_Ha": d_oracle,
+            "psiformer": psi,
+            "serving": serve,
+            "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items()},
+            "gpu_launches": launches,
             "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": int(B * mol.n_electrons * 3 * 4),
                     "d2h_bytes_per_step": 16},
-            "gpu_launches": launches,
-            "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items()},
-            "roofline": rl,
-            "roofline_tensor": rl_t,
-            "serving": serve,
-            "psiformer": psi,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "fp32_simt_peak_tflops": SIMT_PEAK,
+            "roofline": rl,
+            "roofline_tensor": rl_t,
+            "roofline_request": {p_: ferminet_request_roofline(cfg, mol.n_atoms, world * B, S_, r_["ms_per_step"],
+                                                               p_, pk, pk_kind) for p_, r_ in results.items()},
+            "forms": {p_: {"ms_per_step": r_["ms_per_step"],
+                           "walker_steps_per_s": world * B * S_ / (r_["ms_per_step"] / 1e3),
+                           "E_mean_var": r_["mean_var"]} for p_, r_ in results.items()},
+            "abs_dE_mean_mixed_vs_plain_Ha": d_mean,
+            "dE_mean_paired_se_Ha": d_se,
+            "dE_vs_fp64_oracle": d_oracle,
+            "mixed_over_plain": results["fp32"]["ms_per_step"] / results["mixed"]["ms_per_step"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -658,7 +654,17 @@ def run_ours(args, wl):
     return 0
 
 
-FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12
+# FP32 SIMT peak (TFLOP/s): measured on the device by the library's FMA probe
+# (qmc_ffma_throughput) before the timed regions; the nominal figure
+# (152 SMs x 128 FMA/clk x 2 FLOP x 2.07 GHz) stands only until then
+SIMT_PEAK = {"value": 152 * 128 * 2 * 2.07e9 / 1e12, "source": "FP32 SIMT nominal (152 SM x 128 FMA x 2 x 2.07 GHz)"}
+
+
+def measure_simt_peak(dev):
+    from jaqmc_gb300 import _native
+    v = _native.fp32_simt_peak(dev)
+    SIMT_PEAK.update(value=v, source="FP32 SIMT measured (FMA probe, CUDA events, best of 5)")
+    return v
 # dram__bytes_read.sum + dram__bytes_write.sum of one forward-Laplacian launch
 # of the one-electron layer kernel, from the committed ncu capture at 512
 # walkers, scaled to the workload's walkers (traffic grows with the rows)
@@ -666,6 +672,65 @@ TRAFFIC_PER_WALKER: dict = {
     # ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch at 512 walkers
     ("N2", "mixed"): (434.893056e6 + 283.123712e6) / 512,
 }
+
+
+def oracle_energy_gap(models, tree, cfg, mol, x, chunk=32):
+    """Per form: the batch-mean E_L on ``x`` minus the FP64 oracle's, with the
+    paired standard error of that difference (walker by walker), the median
+    and maximum per-walker |dE_L| and the fraction within 1e-4 Ha."""
+    import torch
+
+    from oracle import ferminet as OF
+    from oracle import hamiltonian as OH
+    oc = OF.FermiNetConfig(nspins=cfg.nspins, ndets=cfg.ndets)
+    el64 = []
+    xc = x.double().cpu()
+    for c0 in range(0, xc.shape[0], chunk):
+        sub = xc[c0:c0 + chunk]
+        ref = OF.evaluate(tree, oc, sub, mol.atoms, dtype=torch.float64, tangents=True)
+        el64.append(OH.kinetic_from_tangents(ref["grad"], ref["lap"]) + OH.potential_energy(sub, mol.atoms,
+                                                                                         mol.charges))
+    el64 = torch.cat(el64).numpy()
+    out = {"walkers": int(xc.shape[0])}
+    for p_, m in models.items():
+        d = m.local_energy(x)["e_local"].double().cpu().numpy() - el64
+        ad = np.abs(d)
+        out[p_] = {"dE_mean_Ha": float(d.mean()), "paired_se_Ha": float(d.std(ddof=1) / np.sqrt(d.size)),
+                   "median_abs_Ha": float(np.median(ad)), "max_abs_Ha": float(ad.max()),
+                   "frac_within_1e-4": float((ad <= 1e-4).mean())}
+    return out
+
+
+def ferminet_forward_flops(cfg, n_atoms):
+    """Dense FLOPs of one FermiNet log|psi| forward per walker (2 per
+    multiply-add): one-electron layers over [h1, spin means of h1 and h2]
+    (src/jaqmc/wavefunction/backbone/ferminet.py:51-63), two-electron layers
+    (:37-48) and the orbital projection to K x n orbitals per electron
+    (src/jaqmc/wavefunction/output/orbital.py:60-78).  N2 at widths
+    4 x (256, 32), K = 16: 20.58 MFLOP."""
+    n, C = cfg.n, cfg.channels
+    tot = 0
+    for (d1, d2, s_, dd, upd) in cfg.layer_dims(n_atoms):
+        tot += 2 * n * ((1 + C) * d1 + C * d2) * s_
+        if upd:
+            tot += 2 * n * n * d2 * dd
+    tot += 2 * n * cfg.hidden_dims_single[-1] * cfg.ndets * n
+    return tot
+
+
+def ferminet_request_roofline(cfg, n_atoms, walkers, mh_steps, ms, prec, pk, pk_kind):
+    """Dense-tangent roofline of a whole request: (mh_steps + 3n + 2) forwards
+    of ferminet_forward_flops per walker over the request's time, against the
+    bf16 sustained peak (mixed form) or the measured FP32 SIMT peak (plain)."""
+    flop = ferminet_forward_flops(cfg, n_atoms) * (mh_steps + 3 * cfg.n + 2) * walkers
+    achieved = flop / (ms / 1e3) / 1e12
+    if prec == "mixed":
+        peak, kind = pk["bf16_tflops_sustained"], f"bf16 sustained, {pk_kind}"
+    else:
+        peak, kind = SIMT_PEAK["value"], SIMT_PEAK["source"]
+    return {"bound": "tensor" if prec == "mixed" else "fp32 simt", "achieved": achieved, "peak": peak,
+            "peak_kind": kind, "unit": "TFLOP/s", "frac": achieved / peak,
+            "algorithmic_tflop_per_request": flop / 1e12}
 
 
 def fl_layer_bytes_flops(cfg, mol, B, Tp):
@@ -699,7 +764,7 @@ def fl_layer_roofline(cfg, mol, B, Tp, prec, prof_el, pk, pk_kind):
     if prec == "mixed":
         peak, src = pk["bf16_tflops_sustained"], f"bf16 dense sustained ({pk_kind})"
     else:
-        peak, src = FP32_SIMT_PEAK, "FP32 SIMT nominal (152 SM x 128 FMA x 2 x 2.07 GHz)"
+        peak, src = SIMT_PEAK["value"], SIMT_PEAK["source"]
     rl_t = {"bound": "tensor" if prec == "mixed" else "fp32-simt", "achieved": flops / t / 1e12, "peak": peak,
             "peak_source": src, "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak, "algorithmic_flops": flops}
     return rl, rl_t
@@ -714,7 +779,7 @@ def main():
     ap.add_argument("--workload", default="N2", choices=list(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"])
     ap.add_argument("--burn-in", type=int, default=200)
-    ap.add_argument("--oracle-walkers", type=int, default=64)
+    ap.add_argument("--oracle-walkers", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-psiformer", action="store_true")
@@ -745,6 +810,7 @@ def main():
     if wl.get("model") == "psiformer" and args.impl != "reference":
         import torch
         torch.cuda.set_device(0)
+        measure_simt_peak(torch.device("cuda", 0))
         forms = (args.precision,) if args.request_only else ("mixed", "fp32")
         print(json.dumps(run_psiformer(torch.device("cuda", 0), args.steps, args.warmup, walkers=wl["walkers"],
                                        mh_steps=wl["mh_steps"], oracle_walkers=0 if args.no_cpu else 8,

@@ -145,8 +145,11 @@ qmc_status qmc_forward(qmc_model* m, int batch, const float* electrons, float* l
  * batches whose forward pass needs more are rejected with QMC_ERR_WORKSPACE.
  * The array is shared by all calls on a device: calls whose GPU work overlaps
  * race, so serialise them.  The first call on a device resolves the array's
- * address; make it before any stream capture.  This entry point has no
- * counterpart in the reference. */
+ * address; make it before any stream capture.  That address stays valid only
+ * while the CUDA context that resolved it lives: after cudaDeviceReset do not
+ * call this entry point again in the same process.  Both model families
+ * (FermiNet and Psiformer) are served.  This entry point has no counterpart
+ * in the reference. */
 qmc_status qmc_forward_noalloc(qmc_model* m, int batch, const float* electrons, float* logpsi,
                                float* sign, uint8_t* flags, cudaStream_t stream);
 
@@ -246,6 +249,14 @@ enum {
 };
 qmc_status qmc_profile_enable(int on);
 qmc_status qmc_profile_read(int n_classes, int64_t* launches, double* ms);
+
+/* FP32 FMA throughput probe: one launch of `blocks` blocks of 256 threads,
+ * each thread running 8 independent chains of 16 x iters FMAs; `out` receives
+ * blocks x 256 floats (a sink).  *fma_per_launch = the FMAs issued.  Timed
+ * with CUDA events by the caller, it measures the FP32 SIMT peak that the
+ * plain-form rooflines divide by.  No counterpart in the reference. */
+qmc_status qmc_ffma_throughput(int blocks, int iters, float* out, double* fma_per_launch,
+                               cudaStream_t stream);
 
 #ifdef __cplusplus
 }

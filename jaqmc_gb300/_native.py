@@ -85,6 +85,7 @@ _SIGS = {
     "qmc_model_check_error": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qmc_profile_enable": (C.c_int, [C.c_int]),
     "qmc_profile_read": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p]),
+    "qmc_ffma_throughput": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
 }
 
 
@@ -378,3 +379,27 @@ def reduce_mean_var(x: torch.Tensor, stream=None):
     x = x.to(torch.float32).contiguous()
     check(load().qmc_reduce_mean_var(x.numel(), ptr(x), ptr(out), stream_handle(stream)))
     return out
+
+
+def fp32_simt_peak(device=None, iters=4096, repeats=5):
+    """Measured FP32 SIMT throughput in TFLOP/s (2 FLOPs per FMA): the best of
+    ``repeats`` launches of the library's FMA probe, timed with CUDA events on
+    the launching stream after one warm-up launch."""
+    dev = torch.device(device or "cuda")
+    props = torch.cuda.get_device_properties(dev)
+    blocks = props.multi_processor_count * 8
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
+    fma = C.c_double()
+    lib = load()
+    s = torch.cuda.current_stream(dev)
+    check(lib.qmc_ffma_throughput(blocks, iters, ptr(out), C.byref(fma), stream_handle(s)))
+    best = float("inf")
+    for _ in range(repeats):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(s)
+        check(lib.qmc_ffma_throughput(blocks, iters, ptr(out), C.byref(fma), stream_handle(s)))
+        e1.record(s)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * fma.value / best / 1e12

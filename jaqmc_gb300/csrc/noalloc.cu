@@ -23,10 +23,17 @@
 //    race on the array; serialise them.
 //  * The first call on each device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture begins.
+//    before any stream capture begins.  The address is kept for the life of
+//    the process, so it is only valid while the CUDA context that first
+//    resolved it lives: after cudaDeviceReset (or anything else that destroys
+//    the device's primary context) do not call this entry point again in the
+//    same process.
+//  * FermiNet and Psiformer models are both served (the same forward pass as
+//    qmc_forward for each); the batch limit depends on the model.
 #include <mutex>
 
 #include "plan.cuh"
+#include "psiformer.cuh"
 
 namespace qmc {
 
@@ -63,15 +70,33 @@ static qmc_status noalloc_scratch(void** out) {
 extern "C" qmc_status qmc_forward_noalloc(qmc_model* m, int batch, const float* electrons, float* logpsi,
                                           float* sign, uint8_t* flags, cudaStream_t stream) {
   using namespace qmc;
+  // argument errors first, so that the size message below is only given when
+  // the size is the cause
   if (!m) {
     set_error("null model");
+    return QMC_ERR_ARG;
+  }
+  if (!m->params_set) {
+    set_error("parameters not set (qmc_model_set_params)");
     return QMC_ERR_ARG;
   }
   if (batch < 1) {
     set_error("batch must be >= 1");
     return QMC_ERR_SHAPE;
   }
-  const Plan p = make_plan(m, QMC_OP_FORWARD, batch);
+  if (!electrons || !logpsi) {
+    set_error("null electrons/logpsi");
+    return QMC_ERR_ARG;
+  }
+  int dev;
+  QMC_CUDA(cudaGetDevice(&dev));
+  if (dev != m->device) {
+    set_error("model lives on device %d but device %d is current", m->device, dev);
+    return QMC_ERR_ARG;
+  }
+  const bool psi = m->kind == QMC_KIND_PSIFORMER;
+  const PsiPlan pp = psi ? psi_make_plan(m, batch) : PsiPlan{};
+  const Plan p = psi ? pp.base : make_plan(m, QMC_OP_FORWARD, batch);
   if (p.total > kNoAllocBytes) {
     set_error("qmc_forward_noalloc: %d walkers need %zu bytes of scratch but the built-in array holds %zu; "
               "use a smaller batch or qmc_forward with a workspace",
@@ -80,10 +105,8 @@ extern "C" qmc_status qmc_forward_noalloc(qmc_model* m, int batch, const float* 
   }
   void* ws = nullptr;
   QMC_TRY(noalloc_scratch(&ws));
+  // the remaining shape checks of qmc_forward (mixed-form widths and the like)
   QMC_TRY(check_call(m, batch, ws, kNoAllocBytes, QMC_OP_FORWARD));
-  if (!electrons || !logpsi) {
-    set_error("null electrons/logpsi");
-    return QMC_ERR_ARG;
-  }
+  if (psi) return psi_evaluate(m, pp, ws, electrons, logpsi, sign, flags, stream);
   return evaluate(m, p, ws, electrons, false, logpsi, sign, nullptr, nullptr, flags, stream);
 }

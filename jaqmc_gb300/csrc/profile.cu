@@ -48,9 +48,41 @@ ProfScope::~ProfScope() {
   cudaEventRecord(p.pool[slot + 1], s);
 }
 
+// FP32 FMA throughput probe: every thread runs kFmaChains independent
+// dependent chains of `iters` FMAs (enough independent work to hide the FMA
+// latency on each SM sub-partition), and writes one value so that nothing is
+// eliminated.  Work per launch: blocks x 256 x kFmaChains x iters FMAs.
+constexpr int kFmaChains = 8;
+__global__ void __launch_bounds__(256) k_ffma_throughput(int iters, float b, float c, float* __restrict__ out) {
+  float a[kFmaChains];
+#pragma unroll
+  for (int k = 0; k < kFmaChains; ++k) a[k] = (float)(threadIdx.x + k) * 1e-3f;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+#pragma unroll
+      for (int k = 0; k < kFmaChains; ++k) a[k] = fmaf(a[k], b, c);
+    }
+  }
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < kFmaChains; ++k) acc += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
 }  // namespace qmc
 
 extern "C" {
+
+qmc_status qmc_ffma_throughput(int blocks, int iters, float* out, double* fma_per_launch, cudaStream_t stream) {
+  if (blocks < 1 || iters < 1 || !out) {
+    qmc::set_error("qmc_ffma_throughput: blocks, iters >= 1 and an output of blocks x 256 floats");
+    return QMC_ERR_ARG;
+  }
+  qmc::k_ffma_throughput<<<blocks, 256, 0, stream>>>(iters, 0.999999f, 1e-7f, out);
+  if (fma_per_launch) *fma_per_launch = (double)blocks * 256.0 * qmc::kFmaChains * 16.0 * (double)iters;
+  return qmc::cuda_status(cudaGetLastError(), "k_ffma_throughput");
+}
 
 qmc_status qmc_profile_enable(int on) {
   qmc::ProfState& p = qmc::st();

@@ -226,7 +226,7 @@ class BoundLogProb:
 # ----------------------------------------------------------------- sampler
 class MCMCState(NamedTuple):
     stddev: float
-    pmoves: np.ndarray
+    pmoves: np.ndarray  # or a float64 device tensor once the sampler has stepped
     counter: int
     rng_counter: int
     seed: int
@@ -257,22 +257,45 @@ class MCMCSampler:
         m = wf.model(system, params)
         accepts = torch.zeros(x.shape[0], dtype=torch.int32, device=x.device)
         m.mh_steps(x, self.steps, state.stddev, state.seed, state.rng_counter, accepts=accepts)
-        pmove = float(accepts.sum().item()) / (self.steps * x.shape[0])
+        # pmove over all ranks' walkers (pmean, src/jaqmc/sampler/mcmc.py:180),
+        # kept on the device: no host synchronisation between adaptations
+        pmove = global_pmove(accepts.sum(), self.steps * x.shape[0])
         # width adaptation (src/jaqmc/sampler/mcmc.py:182-197)
         counter = state.counter + 1
         t = counter % self.adapt_frequency
-        pmoves = state.pmoves.copy()
+        pmoves = torch.as_tensor(state.pmoves, dtype=torch.float64).to(x.device).clone()
         pmoves[t] = pmove
         stddev = state.stddev
         if t == 0:
-            mean = float(np.mean(pmoves))
-            if mean > self.pmove_range[1]:
-                stddev = stddev * 1.1
-            elif mean < self.pmove_range[0]:
-                stddev = stddev / 1.1
+            stddev = adapt_width(stddev, float(pmoves.mean()), self.pmove_range)
         new_state = MCMCState(stddev, pmoves, counter, state.rng_counter + self.steps, state.seed)
         new_data = {"electrons": x} if isinstance(data, dict) else data.merge({"electrons": x})
         return new_data, {"pmove": pmove}, new_state
+
+
+def adapt_width(stddev: float, mean_pmove: float, pmove_range=(0.5, 0.55)) -> float:
+    """Widen the proposal by 1.1 when the mean acceptance over the last
+    adaptation window is above the range, narrow it by 1.1 when below
+    (src/jaqmc/sampler/mcmc.py:184-197)."""
+    if mean_pmove > pmove_range[1]:
+        return stddev * 1.1
+    if mean_pmove < pmove_range[0]:
+        return stddev / 1.1
+    return stddev
+
+
+def global_pmove(accepted: torch.Tensor, proposals: int, group=None) -> torch.Tensor:
+    """Fraction of accepted proposals over every rank's walkers, the pmean of
+    pmove (src/jaqmc/sampler/mcmc.py:180).  ``accepted`` is this rank's count
+    as a 0-d tensor and ``proposals`` this rank's number of proposals; the
+    result is a float64 0-d tensor on ``accepted``'s device.  On one rank it
+    is computed on the device without a host synchronisation; with several
+    ranks the counts are summed (ranks weighted by their proposals)."""
+    acc = accepted.to(torch.float64)
+    if _ranks(group) == 1:
+        return acc / float(proposals)
+    t = allreduce_sum(torch.stack([acc, torch.zeros_like(acc) + float(proposals)]), group)
+    return t[0] / t[1]
 
 
 # ------------------------------------------------------- data-parallel ranks
@@ -646,6 +669,8 @@ def save_checkpoint(path, step: int, params: DeviceParams, data=None, sampler_st
         arrays[_CKPT_ELECTRONS] = np.asarray(torch.as_tensor(e).detach().cpu(), np.float32)
     if sampler_state is not None:
         arrays["sampler_state/stddev"] = np.asarray(sampler_state.stddev, np.float32)
-        arrays["sampler_state/pmoves"] = np.asarray(sampler_state.pmoves, np.float32)
+        pm = sampler_state.pmoves
+        pm = pm.detach().cpu().numpy() if isinstance(pm, torch.Tensor) else np.asarray(pm)
+        arrays["sampler_state/pmoves"] = pm.astype(np.float32)
     with open(path, "wb") as f:
         np.savez_compressed(f, allow_pickle=False, **arrays)

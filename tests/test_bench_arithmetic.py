@@ -31,3 +31,22 @@ def test_psiformer_benzene_counts():
     att = bench.psiformer_attention_fl_roofline(cfg, n, 4096, 1000.0)
     assert att["algorithmic_flop_per_request"] == 2 * 18 * n ** 3 * 64 * 4 * 4 * 4096
     assert bench.psiformer_attention_fl_roofline(cfg, n, 4096, 0.0) is None
+
+
+def test_ferminet_counts():
+    """Dense FLOPs per FermiNet forward at widths 4 x (256, 32), K = 16 (Li,
+    CH4, N2), and the N2 request count (20 MH steps + 3n + 2 tangents)."""
+    want = {"Li": 3.977472e6, "CH4": 14.38208e6, "N2": 20.579328e6}
+    for name, v in want.items():
+        mol = S.SYSTEMS[name]()
+        cfg = P.FermiNetConfig(nspins=mol.nspins)
+        assert bench.ferminet_forward_flops(cfg, mol.n_atoms) == pytest.approx(v, rel=1e-9)
+    mol = S.nitrogen_dimer()
+    cfg = P.FermiNetConfig(nspins=mol.nspins)
+    # N2 by hand: layer 0 input 3*8 + 2*4, layers 1-3 input 3*256 + 2*32,
+    # pair layers 4->32->32->32, orbitals 256 -> 16 x 14
+    n = 14
+    hand = 2 * (n * 32 * 256 + 3 * n * 832 * 256 + n * n * (4 * 32 + 32 * 32 + 32 * 32) + n * 256 * 16 * n)
+    assert bench.ferminet_forward_flops(cfg, 2) == hand
+    rl = bench.ferminet_request_roofline(cfg, 2, 4096, 20, 1000.0, "mixed", {"bf16_tflops_sustained": 1.0}, "x")
+    assert rl["algorithmic_tflop_per_request"] == pytest.approx(hand * 64 * 4096 / 1e12, rel=1e-12)

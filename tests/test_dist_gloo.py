@@ -1,6 +1,7 @@
 """Data-parallel host logic on two CPU ranks (gloo): the cross-rank energy
-statistics, the all-gather clip window, the gradient weights and the bench's
-max-over-ranks timing equal what one process computes on all walkers."""
+statistics, the all-gather clip window, the gradient weights, the sampler's
+pmove (pmean over ranks) and the bench's max-over-ranks timing equal what one
+process computes on all walkers."""
 import os
 import socket
 import sys
@@ -43,8 +44,11 @@ def _worker(rank, world, port, out):
         gathered = vmc.gather_walkers(e)
         g = vmc.allreduce_sum(torch.full((3,), float(rank + 1), dtype=torch.float64))
         slowest = bench.max_over_ranks(10.0 + rank, torch.device("cpu"))
+        # rank r accepted 10 (r + 1) of 40 (r + 1) proposals: pmove over all = 30 / 120
+        pm = vmc.global_pmove(torch.tensor(10 * (rank + 1)), 40 * (rank + 1))
         out[rank] = {"m": m, "v": v, "c": c, "clipped": clipped.numpy(), "clipped_iqr": clipped_iqr.numpy(),
-                     "w": w.numpy(), "gathered": gathered.numpy(), "g": g.numpy(), "slowest": slowest}
+                     "w": w.numpy(), "gathered": gathered.numpy(), "g": g.numpy(), "slowest": slowest,
+                     "pmove": float(pm)}
     finally:
         dist.destroy_process_group()
 
@@ -79,5 +83,16 @@ def test_two_rank_reductions():
         np.testing.assert_array_equal(o["gathered"], all_e)
         np.testing.assert_array_equal(o["g"], np.full(3, 3.0))
         assert o["slowest"] == 11.0
+        assert o["pmove"] == pytest.approx(0.25, rel=1e-15)
     # the outliers were clipped
     assert ref_mad.max() < 0.0
+
+
+def test_width_adaptation_rule():
+    """x1.1 above the pmove range, /1.1 below, unchanged inside
+    (src/jaqmc/sampler/mcmc.py:184-197), and the one-rank pmove."""
+    from jaqmc_gb300 import vmc
+    assert vmc.adapt_width(0.2, 0.6) == pytest.approx(0.22)
+    assert vmc.adapt_width(0.2, 0.4) == pytest.approx(0.2 / 1.1)
+    assert vmc.adapt_width(0.2, 0.52) == 0.2
+    assert float(vmc.global_pmove(torch.tensor(7), 28)) == 0.25

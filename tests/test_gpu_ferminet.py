@@ -11,7 +11,8 @@ Tolerances (plain FP32 form vs the FP64 oracle):
 Mixed (split-BF16) form, on walkers equilibrated by MH: signs bit-exact,
 log|psi| within 1e-3 relative, batch-mean E_L within 0.5 mHa of FP64.
 MH: draws injected into both sides; the accept mask is bit-exact except
-near-ties |ratio - log u| < 1e-4, which are excluded and counted.
+near-ties |ratio - log u| < 1e-6, which are excluded and counted (plain and
+mixed forms against the FP64 oracle).
 """
 import json
 import os
@@ -223,27 +224,50 @@ def test_philox_draws_match_oracle(cuda_device):
         np.testing.assert_allclose(nz[s].cpu().numpy(), zo, atol=2e-5)
 
 
-@pytest.mark.parametrize("case", ["Li-full", "N2-full"])
-def test_mh_matches_oracle(case, cuda_device):
+NEAR_TIE = 1e-6  # |ratio - log u| below this: excluded from the bit-exact mask and counted
+
+
+def _mh_against_oracle(case, precision, cuda_device, B=64, steps=3):
     molf, cfgf, _ = CASES[case]
     mol, cfg = molf(), cfgf()
-    B, steps = 64, 3
     tree, flat, x = setup(mol, cfg, B)
-    m = _model(mol, cfg, flat, cuda_device)
+    m = _model(mol, cfg, flat, cuda_device, precision=precision)
     nz, uz = m.mh_draws(B, steps, seed=2, counter=0)
     xg = torch.as_tensor(x, device=cuda_device).clone()
-    _, lpg, accg, _ = m.mh_steps(xg, steps, 0.02, 2, 0)
+    _, lpg, accg, _ = m.mh_steps(xg, steps, 0.02, 2, 0, normals=nz, uniforms=uz)
+    assert m.check_error() == 0
     f = OF.logpsi_fn(tree, oracle_cfg(cfg), mol.atoms)
     xo, lpo, acco, ratios = OM.mh_steps(f, torch.as_tensor(x, dtype=torch.float64), nz.cpu().double(),
                                         uz.cpu().double(), 0.02)
-    near = ((ratios - torch.log(uz.cpu().double())).abs() < 1e-4).any(0).numpy()
+    near = ((ratios - torch.log(uz.cpu().double())).abs() < NEAR_TIE).any(0).numpy()
     keep = ~near
-    _record(f"mh/{case}", {"excluded_near_ties": int(near.sum()), "n": B,
-                           "accepts_gpu": int(accg.sum()), "accepts_oracle": int(acco.sum())})
-    assert keep.sum() >= B - 2
+    mism = int((accg.cpu().numpy()[keep] != acco.numpy()[keep]).sum())
+    _record(f"mh/{case}/{precision}", {"excluded_near_ties": int(near.sum()), "band": NEAR_TIE, "n": B,
+                                       "steps": steps, "mismatches_outside_band": mism,
+                                       "accepts_gpu": int(accg.sum()), "accepts_oracle": int(acco.sum())})
+    return m, keep, xg, lpg, accg, xo, lpo, acco
+
+
+@pytest.mark.parametrize("case", ["Li-full", "N2-full"])
+def test_mh_matches_oracle(case, cuda_device):
+    _, keep, xg, lpg, accg, xo, lpo, acco = _mh_against_oracle(case, "fp32", cuda_device)
+    assert keep.sum() >= len(keep) - 2
     assert np.array_equal(accg.cpu().numpy()[keep], acco.numpy()[keep])
     np.testing.assert_allclose(xg.cpu().numpy()[keep], xo.numpy()[keep], atol=1e-5)
     np.testing.assert_allclose(lpg.cpu().numpy()[keep], lpo.numpy()[keep], rtol=1e-4, atol=1e-4)
+
+
+def test_mixed_mh_accept_mask_matches_oracle(cuda_device):
+    """Split-BF16 form on N2 with the same injected draws as the FP64 oracle:
+    the accept mask bit-exact outside the 1e-6 near-tie band (exclusions
+    counted), positions of kept walkers within 1e-5, 2 log|psi| within 1e-3
+    relative."""
+    _, keep, xg, lpg, accg, xo, lpo, acco = _mh_against_oracle("N2-full", "mixed", cuda_device, B=128)
+    assert keep.sum() >= len(keep) - 2
+    assert np.array_equal(accg.cpu().numpy()[keep], acco.numpy()[keep])
+    np.testing.assert_allclose(xg.cpu().numpy()[keep], xo.numpy()[keep], atol=1e-5)
+    lo = lpo.numpy()[keep]
+    assert (np.abs(lpg.cpu().numpy()[keep] - lo) / np.maximum(1.0, np.abs(lo))).max() < 1e-3
 
 
 def test_reduce_mean_var(cuda_device):
@@ -280,6 +304,42 @@ def _equilibrated(mol, cfg, flat, dev, B, steps=300, stddev=0.15, seed=3):
     x = torch.as_tensor(S.init_walkers(mol, B, seed=1), device=dev)
     m.mh_steps(x, steps, stddev, seed, 0)
     return x.cpu().numpy()
+
+
+# floors of the fraction of equilibrated walkers whose FP32 E_L is within
+# 1e-4 Ha of the FP64 oracle (the oracle's own FP32 evaluation reaches about
+# 0.998 / 0.95 / 0.85 on these cases: the FP32 determinant tangents of
+# moderately conditioned orbital matrices set the rest)
+EQ_FLOOR = {"Li-full": 0.98, "CH4-full": 0.90, "N2-full": 0.75}
+
+
+@pytest.mark.parametrize("case", list(EQ_FLOOR))
+def test_local_energy_on_equilibrated_walkers(case, cuda_device):
+    """Plain FP32 form on 256 walkers burnt in from |psi|^2 by 300 MH steps
+    (the walkers a VMC run evaluates), per walker against the FP64 oracle:
+    median |dE_L| <= 1e-4 Ha; max <= 3x the oracle's own FP32 max; the
+    fraction within 1e-4 Ha at least EQ_FLOOR and at most 0.05 below the FP32
+    oracle's fraction on the same walkers (both recorded)."""
+    molf, cfgf, _ = CASES[case]
+    mol, cfg = molf(), cfgf()
+    tree, flat, _ = setup(mol, cfg, 1)
+    x = _equilibrated(mol, cfg, flat, cuda_device, 256)
+    m = _model(mol, cfg, flat, cuda_device)
+    got = m.local_energy(torch.as_tensor(x, device=cuda_device))["e_local"].cpu().numpy()
+    ref = np.concatenate([oracle_local_energy(tree, cfg, mol, x[i:i + 64])["e_local"].numpy()
+                          for i in range(0, len(x), 64)])
+    r32 = np.concatenate([oracle_local_energy(tree, cfg, mol, x[i:i + 64], dtype=torch.float32)["e_local"]
+                          .double().numpy() for i in range(0, len(x), 64)])
+    err, e32 = np.abs(got - ref), np.abs(r32 - ref)
+    frac, frac32 = float((err <= 1e-4).mean()), float((e32 <= 1e-4).mean())
+    _record(f"local_energy_equilibrated/{case}", {
+        "n": len(x), "median_abs": float(np.median(err)), "max_abs": float(err.max()),
+        "frac_within_1e-4": frac, "oracle32_frac_within_1e-4": frac32,
+        "oracle32_median_abs": float(np.median(e32)), "oracle32_max_abs": float(e32.max()),
+        "mean_err": float(got.mean() - ref.mean()), "se": float((got - ref).std(ddof=1) / np.sqrt(len(x)))})
+    assert np.median(err) <= 1e-4, np.median(err)
+    assert err.max() <= 3 * e32.max(), (err.max(), e32.max())
+    assert frac >= EQ_FLOOR[case] and frac >= frac32 - 0.05, (frac, frac32)
 
 
 # atoms whose tangent tiles take fewer groups per tensor-core tile (P: 48

@@ -81,7 +81,7 @@ def test_mh_matches_oracle(cuda_device):
     f = OP.logpsi_fn(tree, _ocfg(cfg), torch.as_tensor(mol.atoms, dtype=torch.float64))
     xo, lpo, acco, ratios = OM.mh_steps(f, torch.as_tensor(x, dtype=torch.float64), nz.cpu().double(),
                                         uz.cpu().double(), 0.05)
-    near = ((ratios - torch.log(uz.cpu().double())).abs() < 1e-4).any(0).numpy()
+    near = ((ratios - torch.log(uz.cpu().double())).abs() < 1e-6).any(0).numpy()
     keep = ~near
     assert keep.sum() >= B - 2
     assert np.array_equal(accg.cpu().numpy()[keep], acco.numpy()[keep])

@@ -118,3 +118,16 @@ def test_null_space_lift_and_gram():
     lifted = SR.lift_null_space(gram)
     ev = np.linalg.eigvalsh(lifted.numpy())
     assert ev.min() > 0.5 / 10  # the constant direction now has eigenvalue 1
+
+
+def test_required_damping_bounds_the_condition_number():
+    """lam = eig_max / (kappa - 1) against the exact largest eigenvalue, and the
+    argument check on kappa."""
+    S, _ = _problem(B=12, P=50, seed=9)
+    O = _O(S)
+    gram = _t(O @ O.T)
+    eig_max = np.linalg.eigvalsh(O @ O.T).max()
+    lam = float(SR.estimate_required_damping(gram, 1e3, num_iters=200))
+    np.testing.assert_allclose(lam, eig_max / (1e3 - 1.0), rtol=1e-4)
+    with pytest.raises(ValueError):
+        SR.estimate_required_damping(gram, 1.0)
