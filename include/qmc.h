@@ -48,7 +48,13 @@ enum {
 };
 
 enum { QMC_PRECISION_FP32 = 0, QMC_PRECISION_MIXED_BF16 = 1 };
-enum { QMC_ENVELOPE_ISOTROPIC = 0, QMC_ENVELOPE_ABS_ISOTROPIC = 1 };
+/* Envelope types (src/jaqmc/wavefunction/output/envelope.py:16-35):
+ * isotropic exp(-sigma r), abs_isotropic exp(-|sigma| r), diagonal
+ * exp(-||sigma (.) (r - R)||) with a decay rate per dimension (sigma has shape
+ * (n_orb, A, 3, K) per channel), null (no envelope and no envelope
+ * parameters). */
+enum { QMC_ENVELOPE_ISOTROPIC = 0, QMC_ENVELOPE_ABS_ISOTROPIC = 1, QMC_ENVELOPE_DIAGONAL = 2,
+       QMC_ENVELOPE_NULL = 3 };
 enum { QMC_OP_FORWARD = 0, QMC_OP_LOCAL_ENERGY = 1, QMC_OP_MH = 2, QMC_OP_GRAD = 3 };
 
 #define QMC_MAX_LAYERS 8
@@ -122,6 +128,15 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
 
 /* Switch between QMC_PRECISION_FP32 and QMC_PRECISION_MIXED_BF16. */
 qmc_status qmc_model_set_precision(qmc_model* m, int precision);
+
+/* Determinant accuracy guard of qmc_local_energy: determinants whose FP32
+ * kinetic term w_k (tr(A^-1 L) - sum_d tr((A^-1 J_d)^2) + sum_d tr(A^-1 J_d)^2)
+ * loses too many digits to cancellation are evaluated again in FP64 (and the
+ * walker flagged QMC_FLAG_REFACTOR).  mode 1 = on, 0 = off, -1 = the default:
+ * on for QMC_PRECISION_FP32, off for QMC_PRECISION_MIXED_BF16.  No
+ * counterpart in the reference (it evaluates slogdet's rule,
+ * src/jaqmc/laplacian/primitives/slogdet.py:25-72, in the working precision). */
+qmc_status qmc_model_set_det_guard(qmc_model* m, int mode);
 
 /* Bytes of workspace needed by `op` (QMC_OP_*) for `batch` walkers.  For
  * QMC_OP_GRAD, and QMC_OP_LOCAL_ENERGY on a Psiformer model, the call runs in

@@ -19,7 +19,7 @@ QMC_OK = 0
 STATUS = {0: "OK", 1: "ARG", 2: "SHAPE", 3: "NUMERIC", 4: "TIMEOUT", 5: "CUDA", 6: "WORKSPACE",
           7: "UNSUPPORTED"}
 PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 1}
-ENVELOPE = {"isotropic": 0, "abs_isotropic": 1}
+ENVELOPE = {"isotropic": 0, "abs_isotropic": 1, "diagonal": 2, "null": 3}
 OP_FORWARD, OP_LOCAL_ENERGY, OP_MH, OP_GRAD = 0, 1, 2, 3
 FLAG_NONFINITE, FLAG_REFACTOR, FLAG_SINGULAR = 1, 2, 4
 MAX_LAYERS = 8
@@ -60,6 +60,7 @@ _SIGS = {
     "qmc_param_count": (C.c_size_t, [C.c_void_p]),
     "qmc_model_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "qmc_model_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
+    "qmc_model_set_det_guard": (C.c_int, [C.c_void_p, C.c_int]),
     "qmc_workspace_size": (C.c_size_t, [C.c_void_p, C.c_int, C.c_int]),
     "qmc_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_void_p, C.c_size_t, C.c_void_p]),
@@ -211,6 +212,11 @@ class NativeFermiNet:
     @property
     def param_count(self) -> int:
         return int(self.lib.qmc_param_count(self.h))
+
+    def set_det_guard(self, mode: int):
+        """FP64 re-evaluation of cancelling determinants in the local energy:
+        1 on, 0 off, -1 by precision (on for FP32, off for mixed)."""
+        check(self.lib.qmc_model_set_det_guard(self.h, int(mode)))
 
     def set_precision(self, precision: str):
         check(self.lib.qmc_model_set_precision(self.h, PRECISION[precision]))

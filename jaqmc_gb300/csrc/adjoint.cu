@@ -58,9 +58,33 @@ __global__ void k_pair_fwd_save(int npairs, int d_in, int d_out, const float* __
 }
 
 // orbital / envelope cotangents from Abar (value-only pass)
-__global__ void k_orb_bwd(int B, int n, int n_up, int split, int K, int natom, int env_abs, int norb_p,
+// Envelope value of column (k, j) at electron (w, i) for every envelope kind
+// (src/jaqmc/wavefunction/output/envelope.py:123-163); 1 for the null envelope.
+__device__ float env_value(int kind, int env_abs, int natom, int K, int k, int j, size_t wi, const float* pi,
+                           const float* sg, const float* rae, const float* aevec) {
+  if (kind == QMC_ENVELOPE_NULL) return 1.f;
+  float env = 0.f;
+  for (int I = 0; I < natom; ++I) {
+    const size_t q = (size_t)j * natom + I;
+    if (kind == QMC_ENVELOPE_DIAGONAL) {
+      float s2 = 0.f;
+      for (int c = 0; c < 3; ++c) {
+        const float t = sg[(q * 3 + c) * K + k] * aevec[(wi * natom + I) * 3 + c];
+        s2 = fmaf(t, t, s2);
+      }
+      env += pi[q * K + k] * expf(-sqrtf(s2));
+    } else {
+      const float sv = sg[q * K + k];
+      const float se = env_abs ? fabsf(sv) : sv;
+      env += pi[q * K + k] * expf(-se * rae[wi * natom + I]);
+    }
+  }
+  return env;
+}
+
+__global__ void k_orb_bwd(int B, int n, int n_up, int split, int K, int natom, int env_abs, int env_kind, int norb_p,
                           const float* __restrict__ Abar, const float* __restrict__ orb,
-                          const float* __restrict__ rae, const float* __restrict__ pi0,
+                          const float* __restrict__ rae, const float* __restrict__ aevec, const float* __restrict__ pi0,
                           const float* __restrict__ sg0, const float* __restrict__ pi1,
                           const float* __restrict__ sg1, float* __restrict__ orbbar, float* __restrict__ envbar) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,12 +100,7 @@ __global__ void k_orb_bwd(int B, int n, int n_up, int split, int K, int natom, i
   const bool c1 = split && i >= n_up;
   const float* pi = c1 ? pi1 : pi0;
   const float* sg = c1 ? sg1 : sg0;
-  float env = 0.f;
-  for (int I = 0; I < natom; ++I) {
-    float sv = sg[((size_t)j * natom + I) * K + k];
-    float se = env_abs ? fabsf(sv) : sv;
-    env += pi[((size_t)j * natom + I) * K + k] * expf(-se * rae[wi * natom + I]);
-  }
+  const float env = env_value(env_kind, env_abs, natom, K, k, j, wi, pi, sg, rae, aevec);
   const size_t ai = (((size_t)w * K + k) * n + i) * n + j;
   const float ab = Abar[ai];
   orbbar[e] = ab * env;
@@ -111,6 +130,39 @@ __global__ void k_env_jac(int B, int n, int i0, int ns, int K, int natom, int en
   }
   J[(size_t)w * P + off_pi + q] = dpi;
   J[(size_t)w * P + off_sg + q] = dsg;
+}
+
+// Diagonal envelope parameter rows: d/dpi[j,I,k] = sum_i Ebar e^{-s},
+// d/dsigma[j,I,c,k] = sum_i Ebar (-pi e^{-s} sigma_c v_c^2 / s), v = r_i - R_I,
+// s = ||sigma (.) v|| (src/jaqmc/wavefunction/output/envelope.py:143-163).
+__global__ void k_env_jac_diag(int B, int n, int i0, int ns, int K, int natom, const float* __restrict__ envbar,
+                               const float* __restrict__ aevec, const float* __restrict__ pi,
+                               const float* __restrict__ sg, float* __restrict__ J, size_t P, size_t off_pi,
+                               size_t off_sg) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t per_w = (size_t)n * natom * K;
+  if (e >= (size_t)B * per_w) return;
+  const int w = (int)(e / per_w);
+  const size_t q = e % per_w;  // (j, I, k)
+  const int k = (int)(q % K), I = (int)((q / K) % natom), j = (int)(q / ((size_t)K * natom));
+  const size_t jI = (size_t)j * natom + I;
+  const float pv = pi[q];
+  float sc[3];
+  for (int c = 0; c < 3; ++c) sc[c] = sg[(jI * 3 + c) * K + k];
+  float dpi = 0.f, ds[3] = {0.f, 0.f, 0.f};
+  for (int i = i0; i < i0 + ns; ++i) {
+    const float* v = aevec + (((size_t)w * n + i) * natom + I) * 3;
+    float s2 = 0.f;
+    for (int c = 0; c < 3; ++c) s2 = fmaf(sc[c] * v[c], sc[c] * v[c], s2);
+    const float s = sqrtf(s2);
+    const float ex = expf(-s);
+    const float eb = envbar[(((size_t)w * K + k) * n + i) * n + j];
+    dpi = fmaf(eb, ex, dpi);
+    const float f = s > 0.f ? -eb * pv * ex / s : 0.f;
+    for (int c = 0; c < 3; ++c) ds[c] = fmaf(f * sc[c] * v[c], v[c], ds[c]);
+  }
+  J[(size_t)w * P + off_pi + q] = dpi;
+  for (int c = 0; c < 3; ++c) J[(size_t)w * P + off_sg + (jI * 3 + c) * K + k] = ds[c];
 }
 
 // Jacobian block of a dense layer: J[w][off + kx*N + c] =
@@ -321,8 +373,15 @@ static qmc_status forward_save(qmc_model* m, const GradPlan& p, void* ws, const 
     EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + a.env_pi[c],
                    ar + a.env_sigma[c], n, d.A, d.K, 1, d.env_abs};
     epi.orb = at<float>(ws, p.orb);
+    epi.unit_env = !env_in_epilogue(d.env_kind);
     QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, at<float>(ws, p.h1[d.L - 1]), d.d_last, d.d_last, nullptr,
                                               0, 0, ar + a.w_orb[c], d.norb_p, d.norb, epi));
+  }
+  if (d.env_kind == QMC_ENVELOPE_DIAGONAL) {
+    const int c1 = nch - 1;
+    QMC_PROF(QMC_KC_ORBITAL, launch_envelope_diag(s, B, n, d.n_up, d.split, d.K, d.A, 1, 1, ar + a.env_pi[0],
+                                                  ar + a.env_sigma[0], ar + a.env_pi[c1], ar + a.env_sigma[c1],
+                                                  at<float>(ws, p.aevec), at<float>(ws, p.amat)));
   }
   return QMC_OK;
 }
@@ -342,8 +401,8 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
   {
     ::qmc::ProfScope ps_(QMC_KC_ORBITAL, s);
     k_orb_bwd<<<blocks(rows * d.norb_p), 256, 0, s>>>(
-        B, n, d.n_up, d.split, d.K, d.A, d.env_abs, d.norb_p, at<float>(ws, p.abar), at<float>(ws, p.orb),
-        at<float>(ws, p.rae), ar + a.env_pi[0], ar + a.env_sigma[0], ar + a.env_pi[nch - 1],
+        B, n, d.n_up, d.split, d.K, d.A, d.env_abs, d.env_kind, d.norb_p, at<float>(ws, p.abar), at<float>(ws, p.orb),
+        at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + a.env_pi[0], ar + a.env_sigma[0], ar + a.env_pi[nch - 1],
         ar + a.env_sigma[nch - 1], at<float>(ws, p.orbbar), at<float>(ws, p.envbar));
     QMC_CUDA(cudaGetLastError());
   }
@@ -353,10 +412,15 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
     const int i0 = (d.split && c == 1) ? d.n_up : 0;
     {
       ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
-      k_env_jac<<<blocks((size_t)B * n * d.A * d.K), 256, 0, s>>>(B, n, i0, ns, d.K, d.A, d.env_abs,
-                                                                 at<float>(ws, p.envbar), at<float>(ws, p.rae),
-                                                                 ar + a.env_pi[c], ar + a.env_sigma[c], J, P,
-                                                                 pl.env_pi[c], pl.env_sigma[c]);
+      if (d.env_kind == QMC_ENVELOPE_DIAGONAL)
+        k_env_jac_diag<<<blocks((size_t)B * n * d.A * d.K), 256, 0, s>>>(
+            B, n, i0, ns, d.K, d.A, at<float>(ws, p.envbar), at<float>(ws, p.aevec), ar + a.env_pi[c],
+            ar + a.env_sigma[c], J, P, pl.env_pi[c], pl.env_sigma[c]);
+      else if (d.env_kind != QMC_ENVELOPE_NULL)
+        k_env_jac<<<blocks((size_t)B * n * d.A * d.K), 256, 0, s>>>(B, n, i0, ns, d.K, d.A, d.env_abs,
+                                                                   at<float>(ws, p.envbar), at<float>(ws, p.rae),
+                                                                   ar + a.env_pi[c], ar + a.env_sigma[c], J, P,
+                                                                   pl.env_pi[c], pl.env_sigma[c]);
       QMC_CUDA(cudaGetLastError());
       k_jac_outer<<<blocks((size_t)B * d.d_last * d.norb), 256, 0, s>>>(
           B, ns, n, i0, at<float>(ws, p.h1[d.L - 1]), d.d_last, d.d_last, at<float>(ws, p.orbbar), d.norb_p, d.norb, J,

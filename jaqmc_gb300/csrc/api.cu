@@ -77,7 +77,8 @@ static qmc_status build_dims(const qmc_ferminet_config* c, Dims* d) {
   d->C = (d->n_up > 0) + (d->n_dn > 0);
   d->split = c->orbitals_spin_split && d->n_up > 0 && d->n_dn > 0;
   d->env_abs = c->envelope == QMC_ENVELOPE_ABS_ISOTROPIC;
-  if (c->envelope != QMC_ENVELOPE_ABS_ISOTROPIC && c->envelope != QMC_ENVELOPE_ISOTROPIC) {
+  d->env_kind = c->envelope;
+  if (c->envelope < QMC_ENVELOPE_ISOTROPIC || c->envelope > QMC_ENVELOPE_NULL) {
     set_error("unsupported envelope %d", c->envelope);
     return QMC_ERR_UNSUPPORTED;
   }
@@ -124,8 +125,8 @@ static void build_param_layout(const Dims& d, ParamLayout* p) {
   int nch = d.split ? 2 : 1;
   for (int s = 0; s < nch; ++s) { p->orb_k[s] = o; o += (size_t)d.d_last * d.norb; }
   for (int s = 0; s < nch; ++s) {
-    p->env_pi[s] = o; o += (size_t)d.n * d.A * d.K;
-    p->env_sigma[s] = o; o += (size_t)d.n * d.A * d.K;
+    p->env_pi[s] = o; o += env_pi_floats(d.env_kind, d.n, d.A, d.K);
+    p->env_sigma[s] = o; o += env_sigma_floats(d.env_kind, d.n, d.A, d.K);
   }
   p->total = o;
 }
@@ -145,8 +146,8 @@ static void build_arena(const Dims& d, ArenaLayout* a) {
   int nch = d.split ? 2 : 1;
   for (int s = 0; s < nch; ++s) a->w_orb[s] = take((size_t)d.d_last * d.norb_p);
   for (int s = 0; s < nch; ++s) {
-    a->env_pi[s] = take((size_t)d.n * d.A * d.K);
-    a->env_sigma[s] = take((size_t)d.n * d.A * d.K);
+    a->env_pi[s] = take(env_pi_floats(d.env_kind, d.n, d.A, d.K));
+    a->env_sigma[s] = take(env_sigma_floats(d.env_kind, d.n, d.A, d.K));
   }
   a->atoms = take(3 * d.A);
   a->charges = take(d.A);
@@ -482,10 +483,24 @@ static bool env_in_lu(const Dims& d, const Plan& p) {
 // orbitals multiplied in place by launch_envelope_apply before the LU;
 // 0 = inside the orbital epilogue (FP32 form and tangent passes).
 static int env_mode(const Dims& d, const Plan& p) {
-  if (!p.mixed || p.T != 1) return 0;
+  if (!p.mixed || p.T != 1 || !env_in_epilogue(d.env_kind)) return 0;
   if (env_in_lu(d, p)) return 1;
   const bool fits = (size_t)4 * (2 * (d.split ? 2 : 1) * d.A * d.n + d.n * d.A) <= 48 * 1024;
   return d.n <= 64 && fits ? 2 : 0;
+}
+
+// The diagonal envelope, after an orbital stage that stored the orbitals
+// without one (nothing to do for the other envelopes).
+static qmc_status apply_late_envelope(qmc_model* m, const Plan& p, void* ws, cudaStream_t s) {
+  const Dims& d = m->d;
+  if (d.env_kind != QMC_ENVELOPE_DIAGONAL) return QMC_OK;
+  const float* ar = m->arena;
+  const int c1 = d.split ? 1 : 0;
+  QMC_PROF(QMC_KC_ORBITAL, launch_envelope_diag(s, p.B, d.n, d.n_up, d.split, d.K, d.A, p.Tp, p.T,
+                                                ar + m->a.env_pi[0], ar + m->a.env_sigma[0], ar + m->a.env_pi[c1],
+                                                ar + m->a.env_sigma[c1], at<float>(ws, p.aevec),
+                                                at<float>(ws, p.amat)));
+  return QMC_OK;
 }
 
 qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStream_t s) {
@@ -517,10 +532,12 @@ qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStrea
     oa.rae = at<float>(ws, p.rae);
     oa.aevec = at<float>(ws, p.aevec);
     oa.A = at<float>(ws, p.amat);
-    oa.raw = env_mode(d, p) != 0;
+    const bool epi_env = env_in_epilogue(d.env_kind);
+    oa.raw = epi_env ? env_mode(d, p) != 0 : 1;
+    oa.unit_env = !epi_env;
     oa.err = m->dev_err;
     QMC_PROF_TRY(QMC_KC_ORBITAL, tc_orbitals(s, oa));
-    return QMC_OK;
+    return apply_late_envelope(m, p, ws, s);
   }
   const float* h = at<float>(ws, p.h1[hb]);
   for (int c = 0; c < nch; ++c) {
@@ -529,10 +546,11 @@ qmc_status run_orbitals(qmc_model* m, const Plan& p, void* ws, int hb, cudaStrea
     RowMap map{ns, i0, d.n, p.Tp};
     EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec),
                    ar + a.env_pi[c], ar + a.env_sigma[c], d.n, d.A, d.K, p.T, d.env_abs};
+    epi.unit_env = !env_in_epilogue(d.env_kind);
     QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, p.B * ns, map, h, d.d_last, d.d_last, nullptr, 0, 0,
                                               ar + a.w_orb[c], d.norb_p, d.norb, epi));
   }
-  return QMC_OK;
+  return apply_late_envelope(m, p, ws, s);
 }
 
 // Determinant stage: LU (with the value-only envelope factors when the
@@ -559,7 +577,7 @@ qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, fl
   }
   QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, p.B, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe, logpsi, sign, ke, el,
                                         flags, nullptr, mode == 1 ? &env : nullptr, nullptr,
-                                        at<void>(ws, p.redo)));
+                                        at<void>(ws, p.redo), m->det_guard_on()));
   return QMC_OK;
 }
 
@@ -808,8 +826,10 @@ qmc_status qmc_model_set_params(qmc_model* m, const float* params, cudaStream_t 
     QMC_CUDA(cudaMemcpy2DAsync(ar + a.w_orb[c], sizeof(float) * d.norb_p, params + p.orb_k[c],
                                sizeof(float) * d.norb, sizeof(float) * d.norb, d.d_last,
                                cudaMemcpyDeviceToDevice, s));
-    QMC_CUDA(cp(a.env_pi[c], p.env_pi[c], (size_t)d.n * d.A * d.K));
-    QMC_CUDA(cp(a.env_sigma[c], p.env_sigma[c], (size_t)d.n * d.A * d.K));
+    if (d.env_kind != QMC_ENVELOPE_NULL) {
+      QMC_CUDA(cp(a.env_pi[c], p.env_pi[c], env_pi_floats(d.env_kind, d.n, d.A, d.K)));
+      QMC_CUDA(cp(a.env_sigma[c], p.env_sigma[c], env_sigma_floats(d.env_kind, d.n, d.A, d.K)));
+    }
   }
   // FP32 transposes for the adjoint
   for (int l = 0; l < d.L; ++l) {
@@ -863,6 +883,12 @@ size_t qmc_workspace_size(const qmc_model* m, int op, int batch) {
 qmc_status qmc_model_set_energy_budget(qmc_model* m, size_t bytes) {
   if (!m || bytes == 0) { set_error("null model or zero budget"); return QMC_ERR_ARG; }
   m->energy_budget = bytes;
+  return QMC_OK;
+}
+
+qmc_status qmc_model_set_det_guard(qmc_model* m, int mode) {
+  if (!m || mode < -1 || mode > 1) { set_error("null model or mode outside -1..1"); return QMC_ERR_ARG; }
+  m->det_guard = mode;
   return QMC_OK;
 }
 

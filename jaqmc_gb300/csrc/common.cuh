@@ -49,6 +49,22 @@ __host__ __device__ inline int amat_row_stride(int Tp, int n, int K) { return Tp
 __host__ __device__ inline size_t amat_tangent_stride(int n, int K) { return (size_t)n * K * n; }
 constexpr int kMaxAtoms = 64;
 
+// Floats of one envelope channel's pi and sigma (the reference's shapes:
+// pi (n_orb, A, K); sigma (n_orb, A, K), or (n_orb, A, 3, K) for the diagonal
+// envelope; the null envelope has neither).
+__host__ __device__ inline size_t env_pi_floats(int kind, int n, int A, int K) {
+  return kind == QMC_ENVELOPE_NULL ? 0 : (size_t)n * A * K;
+}
+__host__ __device__ inline size_t env_sigma_floats(int kind, int n, int A, int K) {
+  return kind == QMC_ENVELOPE_NULL ? 0 : (size_t)n * A * K * (kind == QMC_ENVELOPE_DIAGONAL ? 3 : 1);
+}
+// The orbital GEMM epilogues apply the isotropic envelopes themselves; the
+// diagonal envelope is applied afterwards by launch_envelope_diag and the
+// null envelope not at all.
+__host__ __device__ inline bool env_in_epilogue(int kind) {
+  return kind == QMC_ENVELOPE_ISOTROPIC || kind == QMC_ENVELOPE_ABS_ISOTROPIC;
+}
+
 // ---------------------------------------------------------------- model
 // Dimensions derived from qmc_ferminet_config.  Widths with a trailing `p`
 // are padded to a multiple of 8 (the K step of the SIMT GEMM); padded
@@ -56,7 +72,8 @@ constexpr int kMaxAtoms = 64;
 struct Dims {
   int n_up, n_dn, n, A, K, L, C;  // C: non-empty spin channels
   int split;                      // per-spin orbitals/envelopes
-  int env_abs;
+  int env_abs;                    // isotropic envelopes: |sigma| (abs_isotropic)
+  int env_kind;                   // QMC_ENVELOPE_*
   int d1_in[QMC_MAX_LAYERS], d2_in[QMC_MAX_LAYERS];
   int d1[QMC_MAX_LAYERS], d2[QMC_MAX_LAYERS];
   int upd2[QMC_MAX_LAYERS];
@@ -132,6 +149,10 @@ struct qmc_model {
   size_t grad_budget = (size_t)8 << 30;  // bytes for the adjoint's chunked workspace
   size_t energy_budget = (size_t)32 << 30;  // bytes for the chunked Psiformer local-energy workspace
   int n_sms = 0;
+  // FP64 re-evaluation of determinants whose FP32 kinetic term cancels
+  // (qmc_model_set_det_guard): -1 = by precision (on for FP32, off for mixed)
+  int det_guard = -1;
+  bool det_guard_on() const { return det_guard < 0 ? precision == QMC_PRECISION_FP32 : det_guard != 0; }
 };
 
 namespace qmc {

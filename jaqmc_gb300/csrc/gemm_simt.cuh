@@ -98,6 +98,7 @@ struct EpiOrbital {
   const float* sigma;  // [n][A][K]
   int n, natom, K, T, env_abs;
   float* orb = nullptr;  // value-only passes: also store the orbitals before the envelope
+  int unit_env = 0;      // store the orbitals without an envelope (diagonal / null envelopes)
   __device__ void operator()(const float* Cs, int ng, int g0, int n0, int N, const RowMap& m) const {
     const int Tp = m.Tp;
     for (int p = threadIdx.x; p < ng * kBN; p += blockDim.x) {
@@ -112,10 +113,11 @@ struct EpiOrbital {
       float pvs[8], svs[8];
 #pragma unroll
       for (int I = 0; I < 8; ++I) {
-        pvs[I] = I < natom ? pi[((size_t)j * natom + I) * K + k] : 0.f;
-        svs[I] = I < natom ? sigma[((size_t)j * natom + I) * K + k] : 0.f;
+        pvs[I] = I < natom && !unit_env ? pi[((size_t)j * natom + I) * K + k] : 0.f;
+        svs[I] = I < natom && !unit_env ? sigma[((size_t)j * natom + I) * K + k] : 0.f;
       }
-      for (int I = 0; I < natom; ++I) {
+      if (unit_env) e0 = 1.f;
+      for (int I = 0; I < (unit_env ? 0 : natom); ++I) {
         float pv = I < 8 ? pvs[I] : pi[((size_t)j * natom + I) * K + k];
         float sv = I < 8 ? svs[I] : sigma[((size_t)j * natom + I) * K + k];
         float r = ra[I];

@@ -244,6 +244,86 @@ cudaError_t launch_envelope_apply(cudaStream_t s, int B, int n, int n_up, int sp
   return cudaGetLastError();
 }
 
+// Diagonal envelope (src/jaqmc/wavefunction/output/envelope.py:143-163),
+// applied in place to orbital matrices that the orbital GEMM stored without
+// an envelope.  For column (k, j) at electron i, with v = r_i - R_I,
+//   s_I = ||sigma_I (.) v||,  E = sum_I pi_I e^{-s_I},
+//   dE/dv_c = -sum_I pi_I e^{-s_I} sigma_Ic^2 v_c / s_I,
+//   lap E = sum_I pi_I e^{-s_I} (|grad s_I|^2 - lap s_I),
+//   lap s = sum_c (sigma_c^2 / s - sigma_c^4 v_c^2 / s^3).
+// Value rows become O E; tangent rows O_t E, plus O_0 dE/dv_c on electron i's
+// own three gradient rows; the Laplacian row O_L E + 2 sum_c O_c dE_c + O_0 lap E
+// (the product rule of the tangent epilogues).  One block per (walker,
+// electron); thread (k, j) over the K n columns of the electron's row, so a
+// warp reads and writes consecutive columns of each tangent row.
+__global__ void __launch_bounds__(256) k_envelope_diag(int n, int n_up, int split, int K, int A, int Tp, int T,
+                                                       const float* __restrict__ pi0, const float* __restrict__ sg0,
+                                                       const float* __restrict__ pi1, const float* __restrict__ sg1,
+                                                       const float* __restrict__ aevec, float* __restrict__ Amat) {
+  __shared__ float av[3 * kMaxAtoms];
+  const int w = blockIdx.x / n, i = blockIdx.x % n;
+  const int ch = split && i >= n_up ? 1 : 0;
+  const float* pi = ch ? pi1 : pi0;
+  const float* sg = ch ? sg1 : sg0;
+  for (int e = threadIdx.x; e < 3 * A; e += blockDim.x) av[e] = aevec[((size_t)w * n + i) * A * 3 + e];
+  __syncthreads();
+  const size_t ts = amat_tangent_stride(n, K);
+  for (int col = threadIdx.x; col < K * n; col += blockDim.x) {
+    const int k = col / n, j = col - k * n;
+    float e0 = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, el = 0.f;
+    for (int I = 0; I < A; ++I) {
+      const size_t q = (size_t)j * A + I;
+      const float pv = pi[q * K + k];
+      float s2[3], sq = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float sc = sg[(q * 3 + c) * K + k];
+        s2[c] = sc * sc;
+        sq = fmaf(s2[c] * av[3 * I + c], av[3 * I + c], sq);
+      }
+      const float s = sqrtf(sq);
+      const float ev = pv * expf(-s);
+      e0 += ev;
+      if (T > 1) {
+        const float inv = 1.f / s;
+        float d[3], gsq = 0.f, lap_s = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          d[c] = s2[c] * av[3 * I + c] * inv;
+          gsq = fmaf(d[c], d[c], gsq);
+          lap_s += s2[c] * inv - d[c] * d[c] * inv;
+        }
+        g0 = fmaf(-ev, d[0], g0);
+        g1 = fmaf(-ev, d[1], g1);
+        g2 = fmaf(-ev, d[2], g2);
+        el = fmaf(ev, gsq - lap_s, el);
+      }
+    }
+    float* dst = Amat + amat_index(Tp, n, K, w, k, 0, i, j);
+    if (T == 1) {
+      dst[0] *= e0;
+      continue;
+    }
+    const int t3 = 2 + 3 * i;
+    const float o0 = dst[0], oL = dst[ts];
+    const float oc0 = dst[(size_t)t3 * ts], oc1 = dst[(size_t)(t3 + 1) * ts], oc2 = dst[(size_t)(t3 + 2) * ts];
+    for (int t = 0; t < T; ++t) dst[(size_t)t * ts] *= e0;  // rows T..Tp-1 are zero and stay so
+    dst[(size_t)t3 * ts] = fmaf(o0, g0, oc0 * e0);
+    dst[(size_t)(t3 + 1) * ts] = fmaf(o0, g1, oc1 * e0);
+    dst[(size_t)(t3 + 2) * ts] = fmaf(o0, g2, oc2 * e0);
+    dst[ts] = oL * e0 + 2.f * (oc0 * g0 + oc1 * g1 + oc2 * g2) + o0 * el;
+  }
+}
+
+cudaError_t launch_envelope_diag(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int Tp, int T,
+                                 const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                 const float* aevec, float* Amat) {
+  if (A > kMaxAtoms) return cudaErrorNotSupported;
+  k_envelope_diag<<<(unsigned)((size_t)B * n), 256, 0, s>>>(n, n_up, split, K, A, Tp, T, pi0, sg0, pi1, sg1, aevec,
+                                                            Amat);
+  return cudaGetLastError();
+}
+
 // hi = bf16(v), lo = bf16(v - hi) for n contiguous values (planes `plane` apart).
 __global__ void k_to_split(size_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, size_t plane) {
   const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1114,6 +1194,40 @@ constexpr float kRefactorGrowth = 1e6f;
 // 20 Ha fall to 0.03 Ha).
 constexpr float kRefactorPivot = 1e-4f;
 
+// Cancellation trigger of the tangent passes.  Determinant k enters the
+// kinetic energy as w_k (tL_k - t2_k + q_k) (w_k = s_k e^{l_k} / psi), and
+// the FP32 rounding errors of its traces are about eps32 times their
+// magnitudes, so its error in Ha is about eps32 times
+//   |w_k| (|tL| + |t2| + |q|)^2 / |tL - t2 + q|
+// (the weight, the magnitude and the cancellation between the traces).  A
+// determinant whose score exceeds kCancelScore is evaluated again in FP64.
+// On burnt-in N2 walkers (FermiNet 4 x (256, 32), K = 16) this re-evaluates
+// about one determinant in eight and takes the share of walkers whose FP32
+// E_L is within 1e-4 Ha of an FP64 evaluation from ~0.84 to ~0.98.
+constexpr float kCancelScore = 1e3f;
+__device__ __forceinline__ bool cancel_marks(float wk, float tL, float t2, float q) {
+  const float mag = fabsf(tL) + fabsf(t2) + fabsf(q);
+  const float net = fabsf(tL - t2 + q);
+  return fabsf(wk) * mag * mag > kCancelScore * net;  // also true for net == 0 with mag > 0
+}
+
+// w_k = s_k exp(l_k - lmax) / sum_k s_k exp(l_k - lmax) for the K
+// determinants (warp-cooperative; singular determinants have s_k = 0).
+__device__ void det_weights(int K, const double* lds, const float* sgs, float* wts) {
+  const int lane = threadIdx.x & 31;
+  double lmax = -INFINITY;
+  for (int k = lane; k < K; k += 32)
+    if (sgs[k] != 0.f) lmax = fmax(lmax, lds[k]);
+  for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  double S = 0.0;
+  for (int k = lane; k < K; k += 32)
+    if (sgs[k] != 0.f) S += (double)sgs[k] * exp(lds[k] - lmax);
+  for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+  for (int k = lane; k < K; k += 32)
+    wts[k] = (sgs[k] != 0.f && S != 0.0) ? (float)((double)sgs[k] * exp(lds[k] - lmax) / S) : 0.f;
+  __syncwarp();
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -1533,7 +1647,7 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
                          const float* __restrict__ pe, float* __restrict__ logpsi,
                          float* __restrict__ sign, float* __restrict__ ke, float* __restrict__ el,
                          uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
-                         const float* __restrict__ gl_add) {
+                         const float* __restrict__ gl_add, int cancel) {
   extern __shared__ double shd[];
   const int w = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1547,7 +1661,9 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   float* qs = t2s + K;                                  // [K]
   float* t1s = qs + K;                                  // [K][D]
   int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);  // flags [2]
-  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
+  float* wts = reinterpret_cast<float*>(ints + 2);          // [K] determinant weights
+  int* done64 = reinterpret_cast<int*>(wts + K);            // [K] already evaluated in FP64
+  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8), 16);
   const DetScratch sc(n);
   char* scratch = reinterpret_cast<char*>(shd) + head + sc.bytes * warp;
   if (threadIdx.x < 2) ints[threadIdx.x] = 0;
@@ -1568,12 +1684,37 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
       tLs[k] = o.tL;
       t2s[k] = o.t2;
       qs[k] = o.q;
+      done64[k] = o.refactor;
       if (o.refactor) atomicOr(&ints[0], 1);
       if (o.singular) atomicOr(&ints[1], 1);
     }
     __syncwarp();
   }
   __syncthreads();
+  if (cancel && T > 1) {
+    // determinants whose FP32 kinetic term cancels too much: FP64 again
+    if (warp == 0) det_weights(K, lds, sgs, wts);
+    __syncthreads();
+    for (int k = warp; k < K; k += nw) {
+      if (sgs[k] == 0.f || done64[k] || !cancel_marks(wts[k], tLs[k], t2s[k], qs[k])) continue;
+      const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
+      DetOut o = det_stage<double, NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K), scratch,
+                                         t1s + (size_t)k * D, true);
+      if (lane == 0) {
+        lds[k] = o.ld;
+        sgs[k] = o.singular ? 0.f : o.sgn;
+        tLs[k] = o.singular ? 0.f : o.tL;
+        t2s[k] = o.singular ? 0.f : o.t2;
+        qs[k] = o.singular ? 0.f : o.q;
+        atomicOr(&ints[0], 1);
+        if (o.singular) atomicOr(&ints[1], 1);
+      }
+      if (o.singular)
+        for (int d = lane; d < D; d += 32) t1s[(size_t)k * D + d] = 0.f;
+      __syncwarp();
+    }
+    __syncthreads();
+  }
   if (warp != 0) return;
   logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, n_refactor, gl_add);
 }
@@ -1601,7 +1742,9 @@ struct WideShape {
   __host__ __device__ WideShape(int n, int K, int D, int nw) {
     ld = (n + 3) / 4 * 4;
     ldm = (n % 2 == 0) ? n + 1 : n + 2;
-    head = align_up((size_t)K * 8 + (size_t)4 * K * 4 + (size_t)K * D * 4 + 16 + (size_t)nw * 12, 16);
+    // ... ints[4], then red: [nw][3] partial traces, later [K] weights
+    head = align_up((size_t)K * 8 + (size_t)4 * K * 4 + (size_t)K * D * 4 + 16 + (size_t)(3 * nw > K ? 3 * nw : K) * 4,
+                    16);
     bytes = head + (size_t)2 * n * ld * 4 + align_up((size_t)n * 4, 16) + (size_t)nw * n * ldm * 4;
   }
 };
@@ -1634,7 +1777,7 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
                                                             float* __restrict__ sign, float* __restrict__ ke,
                                                             float* __restrict__ el, uint8_t* __restrict__ flags,
                                                             uint8_t* __restrict__ redo, char* __restrict__ records,
-                                                            const float* __restrict__ gl_add) {
+                                                            const float* __restrict__ gl_add, int cancel) {
   extern __shared__ double shd[];
   const int w = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -1722,6 +1865,22 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
     }
   }
   __syncthreads();
+  if (cancel) {
+    // determinants whose FP32 kinetic term cancels too much join the FP64 pass
+    float* wts = red;  // [K] (red is sized for 3 nw >= K floats: see WideShape)
+    if (warp == 0) {
+      det_weights(K, lds, sgs, wts);
+      uint8_t* mk = reinterpret_cast<uint8_t*>(rw + rec.mark);
+      bool any = false;
+      for (int k = lane; k < K; k += 32)
+        if (sgs[k] != 0.f && !mk[k] && cancel_marks(wts[k], tLs[k], t2s[k], qs[k])) {
+          mk[k] = 1;
+          any = true;
+        }
+      if (__any_sync(0xffffffffu, any) && lane == 0) ints[0] = 1;
+    }
+    __syncthreads();
+  }
   if (threadIdx.x == 0) redo[w] = ints[0] ? 1 : 0;
   if (ints[0]) {  // leave the record for the FP64 pass
     double* rld = reinterpret_cast<double*>(rw);
@@ -2102,7 +2261,7 @@ static cudaError_t launch_logdet_value_smem(cudaStream_t s, int B, int n, int K,
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor, const EnvArgs* env, const float* gl_add,
-                          void* fl_scratch) {
+                          void* fl_scratch, bool cancel64) {
   if (T > 1 && n > 16 && n <= 64 && fl_scratch && !env) {
     const int nw = 8;
     const WideShape sh(n, K, T - 2, nw);
@@ -2128,7 +2287,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
       set_dev = dev;                                                                                        \
     }                                                                                                       \
     k_logdet_fl_wide<NM><<<B, 32 * nw, sh.bytes, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags, redo, \
-                                                      records, gl_add);                                     \
+                                                      records, gl_add, cancel64 ? 1 : 0);                   \
     k_logdet_fl_det64<NM><<<B * K, 32, sc.bytes, s>>>(n, K, Tp, T, A, redo, records);                       \
   }
       if (n <= 32) QMC_LDW(32)
@@ -2142,7 +2301,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
   if (T == 1 && n <= 64 && !env) return launch_logdet_value_smem(s, B, n, K, A, logpsi, sign, flags);
   if (env) return cudaErrorInvalidValue;  // tangent passes take enveloped matrices
   const int D = T > 1 ? T - 2 : 0;
-  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8), 16);
+  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8), 16);
   const DetScratch sc(n);
   int nw = (int)((200 * 1024 - head) / sc.bytes);
   nw = nw < 1 ? 1 : nw;
@@ -2163,7 +2322,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
       set_dev = dev;                                                                        \
     }                                                                                       \
     k_logdet<NM><<<B, 32 * nw, sm, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags,    \
-                                        n_refactor, gl_add);                                \
+                                        n_refactor, gl_add, cancel64 ? 1 : 0);              \
   }
   if (n <= 8) QMC_LD(8)
   else if (n <= 16) QMC_LD(16)

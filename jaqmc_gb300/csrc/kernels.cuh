@@ -18,6 +18,11 @@ cudaError_t launch_to_split(cudaStream_t s, size_t n, const float* src, __nv_bfl
 cudaError_t launch_envelope_apply(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,
                                   const float* rae, float* Amat);
+// Diagonal envelope with the product rule, in place on orbital matrices stored
+// without an envelope (value layout for Tp == 1, tangent layout otherwise).
+cudaError_t launch_envelope_diag(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int Tp, int T,
+                                 const float* pi0, const float* sg0, const float* pi1, const float* sg1,
+                                 const float* aevec, float* Amat);
 // Envelopes [w][k][i][j] of the value-only orbital matrices.
 cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,
@@ -67,10 +72,13 @@ cudaError_t launch_mean_h2(cudaStream_t s, int B, int n, int n_up, int C, int Tp
 // fl_scratch (optional, logdet_fl_scratch_bytes): with it, tangent passes with
 // 16 < n <= 64 run the FP32 block-per-walker kernel and recompute only the
 // determinants it marks in FP64.
+// cancel64 (tangent passes): also evaluate in FP64 every determinant whose
+// FP32 kinetic term cancels beyond kCancelScore (the FP32 form's accuracy
+// guard; see kernels.cu).
 cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, const float* A,
                           const float* pe, float* logpsi, float* sign, float* ke, float* el,
                           uint8_t* flags, int* n_refactor, const EnvArgs* env = nullptr,
-                          const float* gl_add = nullptr, void* fl_scratch = nullptr);
+                          const float* gl_add = nullptr, void* fl_scratch = nullptr, bool cancel64 = false);
 size_t logdet_fl_scratch_bytes(int B, int K, int T);
 
 // Cotangent of log|psi| with respect to the value orbital matrices:

@@ -81,7 +81,8 @@ qmc_status qmc_ffma_throughput(int blocks, int iters, float* out, double* fma_pe
   }
   qmc::k_ffma_throughput<<<blocks, 256, 0, stream>>>(iters, 0.999999f, 1e-7f, out);
   if (fma_per_launch) *fma_per_launch = (double)blocks * 256.0 * qmc::kFmaChains * 16.0 * (double)iters;
-  return qmc::cuda_status(cudaGetLastError(), "k_ffma_throughput");
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? QMC_OK : qmc::cuda_status(e, "k_ffma_throughput");
 }
 
 qmc_status qmc_profile_enable(int on) {

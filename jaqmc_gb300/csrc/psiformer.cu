@@ -572,7 +572,7 @@ qmc_status psi_local_energy(qmc_model* m, int batch, const float* electrons, flo
     QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, Bc, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe_ws, lp,
                                           at<float>(ws, p.sgn), ke ? ke + b0 : nullptr, e_local + b0,
                                           flags ? flags + b0 : nullptr, nullptr, nullptr, at<float>(ws, pp.jgl),
-                                          at<void>(ws, p.redo)));
+                                          at<void>(ws, p.redo), m->det_guard_on()));
     QMC_PROF(QMC_KC_OTHER, (k_psi_add<<<(Bc + 255) / 256, 256, 0, s>>>(Bc, lp, at<float>(ws, pp.jas)),
                             cudaGetLastError()));
     if (pe) QMC_CUDA(cudaMemcpyAsync(pe + b0, pe_ws, sizeof(float) * Bc, cudaMemcpyDeviceToDevice, s));
@@ -615,10 +615,14 @@ qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
     QMC_CUDA(cudaMemcpy2DAsync(ar + oa.w_orb[c], sizeof(float) * m->d.norb_p, params + P.orb_k[c],
                                sizeof(float) * m->d.norb, sizeof(float) * m->d.norb, D, cudaMemcpyDeviceToDevice,
                                s));
-    QMC_CUDA(cudaMemcpyAsync(ar + oa.env_pi[c], params + P.env_pi[c], sizeof(float) * d.n * d.A * d.K,
-                             cudaMemcpyDeviceToDevice, s));
-    QMC_CUDA(cudaMemcpyAsync(ar + oa.env_sigma[c], params + P.env_sigma[c], sizeof(float) * d.n * d.A * d.K,
-                             cudaMemcpyDeviceToDevice, s));
+    if (m->d.env_kind != QMC_ENVELOPE_NULL) {
+      QMC_CUDA(cudaMemcpyAsync(ar + oa.env_pi[c], params + P.env_pi[c],
+                               sizeof(float) * env_pi_floats(m->d.env_kind, d.n, d.A, d.K), cudaMemcpyDeviceToDevice,
+                               s));
+      QMC_CUDA(cudaMemcpyAsync(ar + oa.env_sigma[c], params + P.env_sigma[c],
+                               sizeof(float) * env_sigma_floats(m->d.env_kind, d.n, d.A, d.K),
+                               cudaMemcpyDeviceToDevice, s));
+    }
     QMC_CUDA(launch_transpose_split(s, ar + oa.w_orb[c], D, m->d.norb, m->d.norb_p, ab + oa.t_orb[c], D,
                                     m->d.norb));
   }
@@ -660,6 +664,10 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
     set_error("unknown precision %d", cfg->precision);
     return QMC_ERR_ARG;
   }
+  if (cfg->envelope < QMC_ENVELOPE_ISOTROPIC || cfg->envelope > QMC_ENVELOPE_NULL) {
+    set_error("unsupported envelope %d", cfg->envelope);
+    return QMC_ERR_UNSUPPORTED;
+  }
   qmc_model* m = new qmc_model();
   m->kind = QMC_KIND_PSIFORMER;
   m->psi = new PsiModel();
@@ -678,6 +686,7 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   d.mlp[cfg->n_mlp] = D;
   d.split = cfg->orbitals_spin_split && cfg->n_up > 0 && cfg->n_down > 0;
   d.env_abs = cfg->envelope == QMC_ENVELOPE_ABS_ISOTROPIC;
+  const int env_kind = cfg->envelope;
   d.jastrow = cfg->jastrow != 0;
   d.K0 = 4 * A + 1;
   d.K0p = (d.K0 + 7) / 8 * 8;  // the SIMT GEMM walks K in steps of 8
@@ -710,8 +719,8 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   const int nch = d.split ? 2 : 1;
   for (int c = 0; c < nch; ++c) P.orb_k[c] = take((size_t)D * d.K * n);
   for (int c = 0; c < nch; ++c) {
-    P.env_pi[c] = take((size_t)n * A * d.K);
-    P.env_sigma[c] = take((size_t)n * A * d.K);
+    P.env_pi[c] = take(env_pi_floats(env_kind, n, A, d.K));
+    P.env_sigma[c] = take(env_sigma_floats(env_kind, n, A, d.K));
   }
   if (nch == 1) {
     P.orb_k[1] = P.orb_k[0];
@@ -744,6 +753,7 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   fd.C = (d.n_up > 0) + (d.n_dn > 0);
   fd.split = d.split;
   fd.env_abs = d.env_abs;
+  fd.env_kind = env_kind;
   fd.d_last = D;
   fd.norb = d.K * n;
   fd.norb_p = align_up(fd.norb, 8);
@@ -751,8 +761,8 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   for (int c = 0; c < 2; ++c) {
     if (c < nch) {
       fa.w_orb[c] = takea((size_t)D * fd.norb_p);
-      fa.env_pi[c] = takea((size_t)n * A * d.K);
-      fa.env_sigma[c] = takea((size_t)n * A * d.K);
+      fa.env_pi[c] = takea(env_pi_floats(env_kind, n, A, d.K));
+      fa.env_sigma[c] = takea(env_sigma_floats(env_kind, n, A, d.K));
     } else {
       fa.w_orb[1] = fa.w_orb[0];
       fa.env_pi[1] = fa.env_pi[0];

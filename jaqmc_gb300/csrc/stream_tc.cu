@@ -651,6 +651,7 @@ struct EpiTcOrbital {
   const float* aevec;
   float* A;
   int raw;           // value-only passes: store orbitals without the envelope factor
+  int unit_env;      // tangent passes: envelope 1 (the diagonal / null envelopes come later)
   int n_rows;  // B * n (value-only passes)
   // value-only passes with split orbitals: tiles of W4[s] walkers x the
   // electrons of channel s (4-D activation maps), tpc4[s] tiles per channel
@@ -702,7 +703,7 @@ struct EpiTcOrbital {
 #pragma unroll
     for (int I = 0; I < kEnvRegs; ++I) {
       float pv = 0.f, se = 0.f;
-      if (I < natom) {
+      if (I < natom && !unit_env) {
         pv = pi[s][((size_t)j * natom + I) * K + k];
         float sv = sigma[s][((size_t)j * natom + I) * K + k];
         se = env_abs ? fabsf(sv) : sv;
@@ -713,6 +714,10 @@ struct EpiTcOrbital {
   }
   // envelope value, gradient (wrt the electron) and Laplacian for column (k, j)
   __device__ void envelope(int s, int w, int i, int k, int j, int T, float* e, const EnvParams& ep) const {
+    if (unit_env) {
+      e[0] = 1.f; e[1] = 0.f; e[2] = 0.f; e[3] = 0.f; e[4] = 0.f;
+      return;
+    }
     const float* ra = rae + ((size_t)w * n + i) * natom;
     const float* av = aevec + ((size_t)w * n + i) * natom * 3;
     float e0 = 0.f, ex = 0.f, ey = 0.f, ez = 0.f, el = 0.f;
@@ -1095,6 +1100,7 @@ qmc_status tc_orbitals(cudaStream_t s, const TcOrbitalArgs& a) {
   e.aevec = a.aevec;
   e.A = a.A;
   e.raw = a.T == 1 ? a.raw : 0;
+  e.unit_env = a.T == 1 ? 0 : a.unit_env;
   // value-only split orbitals: tiles of one channel's electrons only, N the
   // largest multiple of lcm(16, n_up, n_dn) up to 256
   const int nd = a.n - a.n_up;

@@ -54,6 +54,7 @@ struct TcOrbitalArgs {
   const float* rae; const float* aevec;
   float* A;                                         // [w][k][Tp][n][n]
   int raw;           // T == 1: store orbitals without the envelope (applied by the LU pass)
+  int unit_env;      // T > 1: orbitals without an envelope (diagonal / null envelopes)
   int* err;
 };
 // orbital projection x envelope with the product rule.

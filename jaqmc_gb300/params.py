@@ -9,7 +9,9 @@ checkpoint's ``params`` can be loaded leaf by leaf:
   ``orbital_layer/SplitChannelDense_0/DenseGeneral_s`` or
   ``orbital_layer/DenseGeneral_0`` (``src/jaqmc/wavefunction/output/orbital.py:60-78``),
   ``envelope_layer/_env_up|_env_down|_env`` with ``pi`` and ``sigma``
-  (``src/jaqmc/wavefunction/output/envelope.py:65-95,123-140``).
+  (``src/jaqmc/wavefunction/output/envelope.py:65-95,123-163``; ``sigma`` has a
+  per-dimension axis for the diagonal envelope, and the null envelope has no
+  parameters).
 
 Initialisation is fan-in scaled ``N(0, 1/fan_in)`` for kernels, zero biases,
 and ones for the envelope ``pi`` / ``sigma`` (their reference initialisers).
@@ -98,10 +100,37 @@ def init_ferminet(cfg: FermiNetConfig, n_atoms: int, seed: int = 0):
         orb = {"DenseGeneral_0": dg()}
 
     def env():
-        return {"pi": np.ones((n, n_atoms, K), np.float32), "sigma": np.ones((n, n_atoms, K), np.float32)}
+        return {"pi": np.ones((n, n_atoms, K), np.float32),
+                "sigma": np.ones(envelope_sigma_shape(cfg.envelope, n, n_atoms, K), np.float32)}
 
-    envl = {"_env_up": env(), "_env_down": env()} if cfg.split else {"_env": env()}
-    return {"params": {"backbone_layer": bb, "orbital_layer": orb, "envelope_layer": envl}}
+    tree = {"backbone_layer": bb, "orbital_layer": orb}
+    if cfg.envelope != "null":
+        tree["envelope_layer"] = {"_env_up": env(), "_env_down": env()} if cfg.split else {"_env": env()}
+    return {"params": tree}
+
+
+ENVELOPES = ("isotropic", "abs_isotropic", "diagonal", "null")
+
+
+def envelope_sigma_shape(envelope: str, n: int, n_atoms: int, K: int):
+    """Shape of an envelope channel's ``sigma``: ``(n_orb, A, K)`` for the
+    isotropic envelopes, ``(n_orb, A, 3, K)`` for the diagonal one
+    (src/jaqmc/wavefunction/output/envelope.py:131-134,153-156)."""
+    if envelope not in ENVELOPES:
+        raise ValueError(f"unknown envelope {envelope!r}: one of {ENVELOPES}")
+    return (n, n_atoms, 3, K) if envelope == "diagonal" else (n, n_atoms, K)
+
+
+def envelope_leaves(envelope: str, split: bool, n: int, n_atoms: int, K: int):
+    """``pi`` and ``sigma`` per envelope channel; none for the null envelope
+    (src/jaqmc/wavefunction/output/envelope.py:58-96)."""
+    if envelope == "null":
+        return []
+    out = []
+    for nm in (["_env_up", "_env_down"] if split else ["_env"]):
+        out.append((("envelope_layer", nm, "pi"), (n, n_atoms, K)))
+        out.append((("envelope_layer", nm, "sigma"), envelope_sigma_shape(envelope, n, n_atoms, K)))
+    return out
 
 
 def ferminet_leaves(cfg: FermiNetConfig, n_atoms: int):
@@ -124,10 +153,7 @@ def ferminet_leaves(cfg: FermiNetConfig, n_atoms: int):
             out.append((("orbital_layer", "SplitChannelDense_0", f"DenseGeneral_{s}", "kernel"), (d_last, K, n)))
     else:
         out.append((("orbital_layer", "DenseGeneral_0", "kernel"), (d_last, K, n)))
-    names = ["_env_up", "_env_down"] if cfg.split else ["_env"]
-    for nm in names:
-        out.append((("envelope_layer", nm, "pi"), (n, n_atoms, K)))
-        out.append((("envelope_layer", nm, "sigma"), (n, n_atoms, K)))
+    out += envelope_leaves(cfg.envelope, cfg.split, n, n_atoms, K)
     return out
 
 
@@ -233,9 +259,7 @@ def psiformer_leaves(cfg: PsiformerConfig, n_atoms: int):
             out.append((("orbital_layer", "SplitChannelDense_0", f"DenseGeneral_{s}", "kernel"), (D, K, n)))
     else:
         out.append((("orbital_layer", "DenseGeneral_0", "kernel"), (D, K, n)))
-    for nm in (["_env_up", "_env_down"] if cfg.split else ["_env"]):
-        out.append((("envelope_layer", nm, "pi"), (n, n_atoms, K)))
-        out.append((("envelope_layer", nm, "sigma"), (n, n_atoms, K)))
+    out += envelope_leaves(cfg.envelope, cfg.split, n, n_atoms, K)
     if cfg.jastrow == "simple_ee":
         out.append((("jastrow_layer", "alpha_par"), (1,)))
         out.append((("jastrow_layer", "alpha_anti"), (1,)))

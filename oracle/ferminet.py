@@ -10,7 +10,8 @@ Test infrastructure only.  Restates, for a batch of walkers:
   residual ``(x+y)/sqrt(2)`` ``:60-63``, last layer skips the two-electron
   update ``:41-48``);
 * ``OrbitalProjection`` — ``src/jaqmc/wavefunction/output/orbital.py:24-31,60-78``;
-* ``Envelope`` (isotropic / abs_isotropic) — ``src/jaqmc/wavefunction/output/envelope.py:98-140``;
+* ``Envelope`` (isotropic / abs_isotropic / diagonal / null) —
+  ``src/jaqmc/wavefunction/output/envelope.py:98-163``;
 * ``LogDet`` — ``src/jaqmc/wavefunction/output/logdet.py:53-80``;
 * composition — ``src/jaqmc/app/molecule/wavefunction/ferminet.py:76-96``.
 
@@ -35,7 +36,7 @@ class FermiNetConfig:
     hidden_dims_single: list = field(default_factory=lambda: [256] * 4)
     hidden_dims_double: list = field(default_factory=lambda: [32] * 4)
     use_last_layer: bool = False
-    envelope: str = "abs_isotropic"  # or "isotropic"
+    envelope: str = "abs_isotropic"  # or "isotropic", "diagonal", "null"
     orbitals_spin_split: bool = True
 
 
@@ -138,25 +139,49 @@ def isotropic_envelope(pe, r_ae: LT, is_abs: bool, dtype) -> LT:
     return env.permute(3, 1, 2)
 
 
-def envelope(p, cfg: FermiNetConfig, r_ae: LT, dtype) -> LT:
-    if cfg.envelope not in ("isotropic", "abs_isotropic"):
+def diagonal_envelope(pe, ae_vec: LT, dtype) -> LT:
+    """``_DiagonalEnvelope`` (``envelope.py:143-163``): per-dimension decay
+    rates, ``sum_I pi exp(-|| sigma_I (.) (r_i - R_I) ||)`` ->
+    ``(B, K, n_s, n_orb)``.  ``sigma`` has shape ``(n_orb, A, 3, K)``."""
+    pi = _t(pe["pi"], dtype)        # (n_orb, A, K)
+    sigma = _t(pe["sigma"], dtype)  # (n_orb, A, 3, K)
+    B, ns, A, _ = ae_vec.shape
+    n_orb, _, _, K = sigma.shape
+    v = ae_vec.reshape(ns, 1, A, 3, 1).expand_as_value((ns, n_orb, A, 3, K))
+    sv = v.scale(sigma)
+    dist = lap.sqrt((sv * sv).sum(4))            # (B, ns, n_orb, A, K)
+    env = lap.exp(-dist).scale(pi).sum(3)        # (B, ns, n_orb, K)
+    return env.permute(3, 1, 2)
+
+
+def _one_envelope(pe, cfg, r_ae: LT, ae_vec: LT, dtype) -> LT:
+    if cfg.envelope == "diagonal":
+        return diagonal_envelope(pe, ae_vec, dtype)
+    return isotropic_envelope(pe, r_ae, cfg.envelope == "abs_isotropic", dtype)
+
+
+def envelope(p, cfg: FermiNetConfig, r_ae: LT, dtype, ae_vec: LT | None = None) -> LT | None:
+    """``Envelope.__call__`` (``envelope.py:98-120``); ``None`` for the null
+    envelope (the orbitals are used as they are)."""
+    if cfg.envelope == "null":
+        return None
+    if cfg.envelope not in ("isotropic", "abs_isotropic", "diagonal"):
         raise NotImplementedError(cfg.envelope)
-    is_abs = cfg.envelope == "abs_isotropic"
     nu, nd = cfg.nspins
     if cfg.orbitals_spin_split and nu > 0 and nd > 0:
-        e_u = isotropic_envelope(p["_env_up"], r_ae[:nu], is_abs, dtype)
-        e_d = isotropic_envelope(p["_env_down"], r_ae[nu:], is_abs, dtype)
+        e_u = _one_envelope(p["_env_up"], cfg, r_ae[:nu], None if ae_vec is None else ae_vec[:nu], dtype)
+        e_d = _one_envelope(p["_env_down"], cfg, r_ae[nu:], None if ae_vec is None else ae_vec[nu:], dtype)
         return lap.concat([e_u, e_d], 2)
-    return isotropic_envelope(p["_env"], r_ae, is_abs, dtype)
+    return _one_envelope(p["_env"], cfg, r_ae, ae_vec, dtype)
 
 
 def orbitals(params, cfg: FermiNetConfig, x: LT, atoms, dtype) -> LT:
     p = params["params"]
-    ae, ee, r_ae, _ = features(x, atoms)
+    ae, ee, r_ae, ae_vec = features(x, atoms)
     h1 = backbone(p["backbone_layer"], cfg, ae, ee, dtype)
     orb = orbital_projection(p["orbital_layer"], cfg, h1, dtype)
-    env = envelope(p["envelope_layer"], cfg, r_ae, dtype)
-    return orb * env
+    env = envelope(p.get("envelope_layer", {}), cfg, r_ae, dtype, ae_vec)
+    return orb if env is None else orb * env
 
 
 def evaluate(params, cfg: FermiNetConfig, electrons, atoms, *, dtype=torch.float64,

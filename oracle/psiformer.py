@@ -121,12 +121,12 @@ def evaluate(params, cfg: PsiformerConfig, electrons, atoms, *, dtype=torch.floa
     p = params["params"]
     electrons = _t(electrons, dtype)
     atoms = _t(atoms, dtype)
-    ae, r_ae, _, r_ee = features(electrons, atoms, cfg.nspins)
+    ae, r_ae, ae_vec, r_ee = features(electrons, atoms, cfg.nspins)
     h = backbone(p["backbone_layer"], cfg, ae, dtype)
     h_lt = lap.const(h, 0)
     orb = OF.orbital_projection(p["orbital_layer"], cfg, h_lt, dtype)
-    env = OF.envelope(p["envelope_layer"], cfg, lap.const(r_ae, 0), dtype)
-    A = orb * env
+    env = OF.envelope(p.get("envelope_layer", {}), cfg, lap.const(r_ae, 0), dtype, lap.const(ae_vec, 0))
+    A = orb if env is None else orb * env
     sign, ld = lap.slogdet(A)
     s, lp = lap.signed_logsumexp(sign, ld, -1)
     J = jastrow(p["jastrow_layer"], cfg, r_ee, dtype) if cfg.jastrow == "simple_ee" else torch.zeros_like(lp.x)
@@ -240,8 +240,8 @@ def evaluate_fl(params, cfg: PsiformerConfig, electrons, atoms, *, dtype=torch.f
     ae, r_ae = features_lt(xl, R, cfg.nspins)
     h = backbone_lt(p["backbone_layer"], cfg, ae, dtype)
     orb = OF.orbital_projection(p["orbital_layer"], cfg, h, dtype)
-    env = OF.envelope(p["envelope_layer"], cfg, r_ae, dtype)
-    sign, ld = lap.slogdet(orb * env)
+    env = OF.envelope(p.get("envelope_layer", {}), cfg, r_ae, dtype, xl.unsqueeze(2) - R.reshape(-1, 3))
+    sign, ld = lap.slogdet(orb if env is None else orb * env)
     s, lp = lap.signed_logsumexp(sign, ld, -1)
     if cfg.jastrow == "simple_ee":
         lp = lp + jastrow_lt(p["jastrow_layer"], cfg, xl, dtype)

@@ -183,3 +183,51 @@ def test_mh_draws_statistics():
     z, u = OP.mh_draws(seed=2, step=0, batch=4096, n=5)
     assert abs(z.mean()) < 0.02 and abs(z.std() - 1) < 0.02
     assert 0 < u.min() and u.max() < 1 and abs(u.mean() - 0.5) < 0.02
+
+
+def _random_envelopes(tree, rng):
+    for ch in tree["params"].get("envelope_layer", {}).values():
+        ch["pi"][:] = rng.uniform(0.5, 1.5, ch["pi"].shape)
+        ch["sigma"][:] = rng.uniform(0.4, 1.6, ch["sigma"].shape)
+
+
+@pytest.mark.parametrize("envelope", ["diagonal", "null"])
+@pytest.mark.parametrize("nspins,A", [((2, 1), 1), ((3, 2), 2)])
+def test_fl_matches_bruteforce_other_envelopes(envelope, nspins, A):
+    """The diagonal (per-dimension decay, src/jaqmc/wavefunction/output/
+    envelope.py:143-163) and null (:79-80,110-112) envelopes through the
+    forward Laplacian: gradient and kinetic energy equal the brute-force
+    Hessian trace."""
+    cfg = small_cfg(nspins, ndets=3, envelope=envelope)
+    tree = P.init_ferminet(cfg, A, seed=7)
+    _random_envelopes(tree, np.random.default_rng(5))
+    oc = oracle_cfg(cfg)
+    atoms = np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 1.4]])[:A]
+    x = torch.randn(4, cfg.n, 3, dtype=torch.float64, generator=torch.Generator().manual_seed(3))
+    out = OF.evaluate(tree, oc, x, atoms, tangents=True)
+    ke = OH.kinetic_from_tangents(out["grad"], out["lap"])
+    ke_ref, g_ref, _ = OH.kinetic_bruteforce(OF.logpsi_fn(tree, oc, atoms), x)
+    np.testing.assert_allclose(out["grad"].numpy(), g_ref.numpy(), rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(ke.numpy(), ke_ref.numpy(), rtol=1e-9, atol=1e-9)
+
+
+def test_diagonal_envelope_with_equal_rates_is_abs_isotropic():
+    """sigma_c = s for the three dimensions gives ||s (r - R)|| = |s| r: the
+    diagonal envelope equals the abs_isotropic one with sigma = s."""
+    mol = S.methane()
+    cd = small_cfg(mol.nspins, ndets=2, envelope="diagonal")
+    ci = small_cfg(mol.nspins, ndets=2, envelope="abs_isotropic")
+    td = P.init_ferminet(cd, mol.n_atoms, seed=1)
+    ti = P.init_ferminet(ci, mol.n_atoms, seed=1)
+    rng = np.random.default_rng(2)
+    for nm, ch in ti["params"]["envelope_layer"].items():
+        ch["pi"][:] = rng.uniform(0.5, 1.5, ch["pi"].shape)
+        ch["sigma"][:] = rng.uniform(-1.5, 1.5, ch["sigma"].shape)
+        td["params"]["envelope_layer"][nm]["pi"][:] = ch["pi"]
+        td["params"]["envelope_layer"][nm]["sigma"][:] = ch["sigma"][:, :, None, :]
+    x = torch.as_tensor(S.init_walkers(mol, 6, seed=3), dtype=torch.float64)
+    a = OF.evaluate(td, oracle_cfg(cd), x, mol.atoms, tangents=True)
+    b = OF.evaluate(ti, oracle_cfg(ci), x, mol.atoms, tangents=True)
+    for k in ("logpsi", "grad", "lap"):
+        np.testing.assert_allclose(a[k].numpy(), b[k].numpy(), rtol=1e-12, atol=1e-12)
+    assert [s for _, s in P.ferminet_leaves(cd, mol.n_atoms)][-1] == (mol.n_electrons, mol.n_atoms, 3, 2)
