@@ -408,6 +408,108 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
             "cpu_baseline": cpu}
 
 
+# ---------------------------------------------------------------- gradient
+def run_gradient(dev, steps, warmup, walkers=4096, budget_gb=8, burn_in=200, fd_walkers=2, fd_entries=64,
+                 fd_step=1e-4):
+    """The gradient path on CH4 (FermiNet 4 x (256, 32), K = 16, FP32): on
+    ``walkers`` walkers burnt in from |psi|^2, with the adjoint's workspace
+    budget set to ``budget_gb`` GiB (activations recomputed per chunk),
+    (a) the per-walker Jacobian d log|psi_w| / d theta (B x P floats, caller
+    buffer) and (b) the VMC energy gradient 2 <(E_L - E) d log|psi|>: E_L,
+    its FP64 mean and one weighted adjoint pass.  Times per call by CUDA
+    events; a check of the Jacobian against FP64 central differences of the
+    oracle (step ``fd_step``) on ``fd_entries`` seeded entries for
+    ``fd_walkers`` walkers of the same run."""
+    import torch
+
+    from jaqmc_gb300 import _native
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+    mol = S.methane()
+    cfg = P.FermiNetConfig(nspins=mol.nspins)
+    tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+    leaves = P.ferminet_leaves(cfg, mol.n_atoms)
+    flat_np = P.flatten(tree, leaves)
+    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision="fp32", device=dev)
+    m.set_params(torch.as_tensor(flat_np, device=dev))
+    m.set_grad_budget(budget_gb << 30)
+    x = torch.as_tensor(S.init_walkers(mol, walkers, seed=1), device=dev)
+    m.mh_steps(x, burn_in, 0.15, 1000, 0)
+    Pn = m.param_count
+    ws_bytes = m.lib.qmc_workspace_size(m.h, _native.OP_GRAD, walkers)
+    # the adjoint runs in chunks of the largest batch whose workspace fits the
+    # budget: the workspace stops growing at that batch
+    lo, hi = 1, walkers
+    while lo < hi:
+        mid = (lo + hi) // 2
+        if m.lib.qmc_workspace_size(m.h, _native.OP_GRAD, mid) >= ws_bytes:
+            hi = mid
+        else:
+            lo = mid + 1
+    chunk = lo
+    J = torch.empty((walkers, Pn), dtype=torch.float32, device=dev)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    lp = torch.empty(walkers, dtype=torch.float32, device=dev)
+    g = torch.empty(Pn, dtype=torch.float64, device=dev)
+    stream = _native.stream_handle()
+
+    def jac():
+        _native.check(m.lib.qmc_grad(m.h, walkers, x.data_ptr(), None, J.data_ptr(), None, lp.data_ptr(),
+                                     ws.data_ptr(), ws_bytes, stream))
+
+    def vmc_grad():
+        e = m.local_energy(x)["e_local"]
+        mv = _native.reduce_mean_var(e)
+        wts = (2.0 / walkers) * (e.double() - mv[0])
+        _native.check(m.lib.qmc_grad(m.h, walkers, x.data_ptr(), wts.data_ptr(), None, g.data_ptr(),
+                                     lp.data_ptr(), ws.data_ptr(), ws_bytes, stream))
+
+    out = {}
+    for name, fn in (("per_walker_jacobian", jac), ("vmc_energy_gradient", vmc_grad)):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = {"ms_per_call": e0.elapsed_time(e1) / steps}
+    assert m.check_error() == 0
+    jb = walkers * Pn * 4
+    out["per_walker_jacobian"].update({
+        "jacobian_bytes": jb, "achieved_write_GBs": jb / (out["per_walker_jacobian"]["ms_per_call"] / 1e3) / 1e9})
+    fd = None
+    if fd_walkers:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from oracle import ferminet as OF
+        xs = x[:fd_walkers].double().cpu()
+        Jw = J[:fd_walkers].double().cpu().numpy()
+        rng = np.random.default_rng(64)
+        idx = rng.choice(Pn, fd_entries, replace=False)
+        oc = OF.FermiNetConfig(nspins=cfg.nspins, ndets=cfg.ndets)
+        base = flat_np.astype(np.float64)
+        fdv = np.zeros((fd_walkers, fd_entries))
+        for c, p in enumerate(idx):
+            vals = []
+            for sgn in (1.0, -1.0):
+                v = base.copy()
+                v[p] += sgn * fd_step
+                tr = P.unflatten(v, leaves)
+                vals.append(OF.evaluate(tr, oc, xs, mol.atoms, dtype=torch.float64)["logpsi"].numpy())
+            fdv[:, c] = (vals[0] - vals[1]) / (2 * fd_step)
+        scale = np.abs(Jw).max(axis=1, keepdims=True)
+        fd = {"walkers": fd_walkers, "entries": fd_entries, "step": fd_step,
+              "max_err_over_walker_scale": float((np.abs(Jw[:, idx] - fdv) / scale).max())}
+    res = {"workload": f"CH4 FermiNet 4x(256,32) K=16 FP32, {walkers} walkers, adjoint budget {budget_gb} GiB",
+           "params": Pn, "walkers": walkers, "workspace_bytes": int(ws_bytes),
+           "walkers_per_chunk": chunk, "chunks": -(-walkers // chunk), **out, "fd_check": fd}
+    del J, ws, m
+    torch.cuda.empty_cache()
+    return res
+
+
 # ----------------------------------------------------------------- serving
 def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
     """Poisson(rate) arrivals of neutral-atom jobs (Z ~ U{2..18}, Hund spins,
@@ -609,6 +711,9 @@ def run_ours(args, wl):
     psi = None
     if not args.no_psiformer:
         psi = run_psiformer(dev, max(1, args.steps // 2), 1)
+    grad = None
+    if not args.no_grad:
+        grad = run_gradient(dev, max(1, args.steps // 2), 1, fd_walkers=0 if args.no_cpu else 2)
     serve = None
     if not args.no_serve:
         serve = run_serving(dev, args.serve_rate, args.serve_jobs, args.serve_requests, slots=args.serve_slots)
@@ -628,6 +733,7 @@ def run_ours(args, wl):
                        "parallelism": f"replicas x{world}",
                        "l2": "working set larger than L2 (local-energy workspace several GB)"},
             "psiformer": psi,
+            "gradient": grad,
             "serving": serve,
             "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items()},
             "gpu_launches": launches,
@@ -783,6 +889,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-psiformer", action="store_true")
+    ap.add_argument("--no-grad", action="store_true", help="skip the CH4 gradient leg")
     ap.add_argument("--walkers", type=int, default=None, help="override the workload's walker count")
     ap.add_argument("--request-only", action="store_true",
                     help="only W warm-up + K timed requests of --precision (for profiler runs)")

@@ -616,6 +616,10 @@ class EvaluationStage:
 # state at ``sampler_state/stddev`` and ``sampler_state/pmoves``.
 _CKPT_PARAMS = "params/params/"
 _CKPT_ELECTRONS = "batched_data/data/electrons"
+# this library's sampler counters (the Philox stream position and seed, the
+# adaptation counter), kept apart from the reference's keys, which a
+# reference restore reads by its own state's paths and so ignores these
+_CKPT_OWN = "qmc_gb300/"
 
 
 def _param_leaves(wf, n_atoms: int):
@@ -632,7 +636,10 @@ def load_reference_checkpoint(path, wf, n_atoms: int, device=None) -> dict:
     ``restore_from_file`` returns), ``params`` a :class:`DeviceParams` in the
     layout of ``wf`` (shapes checked leaf by leaf), ``electrons`` the saved
     walkers (or None) and ``sampler_state`` an :class:`MCMCState` with the
-    saved proposal width and acceptance history (or None).
+    saved proposal width and acceptance history (or None); a file written by
+    :func:`save_checkpoint` also restores the Philox stream position, seed and
+    adaptation counter, so that a resumed run draws what the uninterrupted run
+    would have drawn.
     """
     leaves = _param_leaves(wf, n_atoms)
     with np.load(path, allow_pickle=False) as f:
@@ -649,7 +656,12 @@ def load_reference_checkpoint(path, wf, n_atoms: int, device=None) -> dict:
         sstate = None
         if "sampler_state/stddev" in f.files:
             pm = np.asarray(f["sampler_state/pmoves"], np.float64) if "sampler_state/pmoves" in f.files else None
-            sstate = MCMCState(float(np.asarray(f["sampler_state/stddev"])), pm, 0, 0, 0)
+
+            def own(name):
+                k = _CKPT_OWN + name
+                return int(np.asarray(f[k]).item()) if k in f.files else 0
+            sstate = MCMCState(float(np.asarray(f["sampler_state/stddev"])), pm, own("sampler_counter"),
+                               own("sampler_rng_counter"), own("sampler_seed"))
         step = int(np.asarray(f["step"]).item()) + 1 if "step" in f.files else 0
     dev = device if device is not None else (wf._dev() if torch.cuda.is_available() else torch.device("cpu"))
     return {"step": step, "params": DeviceParams(tree, leaves, dev), "electrons": electrons,
@@ -672,5 +684,8 @@ def save_checkpoint(path, step: int, params: DeviceParams, data=None, sampler_st
         pm = sampler_state.pmoves
         pm = pm.detach().cpu().numpy() if isinstance(pm, torch.Tensor) else np.asarray(pm)
         arrays["sampler_state/pmoves"] = pm.astype(np.float32)
+        arrays[_CKPT_OWN + "sampler_counter"] = np.asarray(sampler_state.counter, np.int64)
+        arrays[_CKPT_OWN + "sampler_rng_counter"] = np.asarray(sampler_state.rng_counter, np.uint64)
+        arrays[_CKPT_OWN + "sampler_seed"] = np.asarray(sampler_state.seed, np.uint64)
     with open(path, "wb") as f:
         np.savez_compressed(f, allow_pickle=False, **arrays)

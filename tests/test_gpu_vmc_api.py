@@ -185,3 +185,42 @@ def test_hydrogen_training_with_sr(cuda_device):
         params.touch()
     e = float(np.mean(energies[-20:]))
     assert abs(e + 0.5) < 5e-3, energies[-20:]
+
+
+def test_resume_from_checkpoint_continues_the_run(cuda_device, tmp_path):
+    """A run checkpointed after 3 of 6 sampler + energy steps and resumed from
+    the file (parameters, walkers, sampler state through
+    load_reference_checkpoint) reproduces the uninterrupted run's walkers and
+    energies bit for bit (src/jaqmc/utils/checkpoint.py:26-274 is the layout;
+    src/jaqmc/workflow/stage/base.py:122-190 resumes at saved step + 1)."""
+    mol = S.lithium()
+    wf = vmc.FermiNetWavefunction(nspins=mol.nspins)
+    data = _system(mol, 256)
+    params = wf.init_params(data, 0)
+    sampler = vmc.MCMCSampler(steps=10, initial_width=0.2, adapt_frequency=1000)
+    kin = vmc.EuclideanKinetic(f_log_psi=wf)
+
+    def step(params, data, state):
+        d, _, state = sampler.step(wf.batch_log_prob(params, data), data, state)
+        data = data.merge({"electrons": d.electrons})
+        bd = vmc.BatchedData(data)
+        ws = vmc.potential_energy(params, bd, {}, None, wf=wf)[0]
+        ws.update(kin.evaluate_batch_walkers(params, bd, ws, None)[0])
+        return data, state, (ws["energy:kinetic"] + ws["energy:potential"]).cpu().numpy()
+
+    state = sampler.init(data, 5)
+    ref = []
+    for it in range(6):
+        data, state, e = step(params, data, state)
+        ref.append((data.electrons.cpu().numpy().copy(), e))
+        if it == 2:
+            path = tmp_path / "ckpt_000002.npz"
+            vmc.save_checkpoint(path, 2, params, data, state)
+    r = vmc.load_reference_checkpoint(path, wf, mol.n_atoms)
+    assert r["step"] == 3
+    data2 = vmc.MoleculeData(torch.as_tensor(r["electrons"], device="cuda"), mol.atoms, mol.charges)
+    state2 = r["sampler_state"]
+    for it in range(3, 6):
+        data2, state2, e = step(r["params"], data2, state2)
+        np.testing.assert_array_equal(data2.electrons.cpu().numpy(), ref[it][0])
+        np.testing.assert_array_equal(e, ref[it][1])
