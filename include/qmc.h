@@ -230,6 +230,45 @@ qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const doubl
 /* Byte budget of the adjoint's workspace (default 8 GiB); sets the chunk size. */
 qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes);
 
+/* Layer taps of the parameter adjoint, the statistics a Kronecker-factored
+ * curvature (KFAC) needs: for every dense layer the inputs x and the output
+ * cotangents dy = d log|psi_w| / d(layer output) of each of its applications,
+ * and for the remaining parameters (the envelope's) the per-walker gradients.
+ * Replaces the layer-tag registration and the curvature statistics that
+ * kfac_jax collects from the jaxpr of vmap(log|psi|)
+ * (src/jaqmc/optimizer/kfac/kfac.py:162-186,
+ *  src/jaqmc/optimizer/kfac/curvature_blocks.py:94-137,
+ *  src/jaqmc/optimizer/kfac/tag_registration.py:22-259).  FermiNet models only.
+ * Tap order: per layer l the one-electron Dense (input [h1 | spin means of h1
+ * | spin means of h2], n applications per walker, bias) then, when layer l
+ * updates the two-electron stream, the two-electron Dense (n^2 applications,
+ * bias); the orbital projection of each spin channel (n_s applications, no
+ * bias); last the envelope parameters as one diagonal tap (rows_per_walker 1,
+ * in_cols 0, out_cols = their count).  A tap's inputs are a row-major
+ * [batch * rows_per_walker][in_cols] block at float offset in_offset of the
+ * taps buffer and its cotangents (or per-walker gradients) a
+ * [batch * rows_per_walker][out_cols] block at out_offset; walker w's rows are
+ * w * rows_per_walker ... (w + 1) * rows_per_walker - 1. */
+enum { QMC_TAP_DENSE = 0, QMC_TAP_DIAGONAL = 1 };
+typedef struct {
+  int kind;              /* QMC_TAP_*                                          */
+  int rows_per_walker;   /* applications per walker                            */
+  int in_cols, out_cols; /* input width (no bias column) and output width       */
+  int has_bias;
+  size_t kernel_offset;  /* flat parameter offset of the kernel [in_cols][out] (or of the diagonal block) */
+  size_t bias_offset;    /* flat parameter offset of the bias (has_bias)        */
+  size_t in_offset, out_offset;  /* float offsets in the taps buffer            */
+} qmc_layer_tap;
+/* Fills up to max_taps descriptors for `batch` walkers; returns the number of
+ * taps (or -1 for a model without taps) and the taps buffer size in floats. */
+int qmc_layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total_floats);
+/* Runs the adjoint (forward with saved activations + backward, chunked under
+ * the gradient budget; workspace = qmc_workspace_size(QMC_OP_GRAD)) and writes
+ * the taps of every walker into `taps` (total_floats floats); logpsi
+ * (batch,) may be NULL. */
+qmc_status qmc_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,
+                         float* logpsi, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
 /* Byte budget of the Psiformer local-energy workspace (default 32 GiB): walkers
  * run in balanced chunks whose forward-Laplacian activations fit it.  FermiNet
  * models ignore it. */

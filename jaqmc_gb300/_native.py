@@ -45,6 +45,14 @@ class PsiformerConfigC(C.Structure):
                 ("jastrow", C.c_int), ("precision", C.c_int)]
 
 
+class LayerTapC(C.Structure):
+    _fields_ = [("kind", C.c_int), ("rows_per_walker", C.c_int), ("in_cols", C.c_int), ("out_cols", C.c_int),
+                ("has_bias", C.c_int), ("kernel_offset", C.c_size_t), ("bias_offset", C.c_size_t),
+                ("in_offset", C.c_size_t), ("out_offset", C.c_size_t)]
+
+
+TAP_DENSE, TAP_DIAGONAL = 0, 1
+
 _lib = None
 _lock = threading.Lock()
 
@@ -82,6 +90,9 @@ _SIGS = {
     "qmc_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p, C.c_size_t, C.c_void_p]),
     "qmc_model_set_grad_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "qmc_layer_taps": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LayerTapC), C.c_int, C.POINTER(C.c_size_t)]),
+    "qmc_grad_taps": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+                                C.c_size_t, C.c_void_p]),
     "qmc_model_set_energy_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
     "qmc_model_check_error": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qmc_profile_enable": (C.c_int, [C.c_int]),
@@ -326,6 +337,37 @@ class NativeFermiNet:
         check(self.lib.qmc_grad(self.h, B, ptr(e), ptr(w), ptr(J), ptr(g), ptr(lp), ptr(ws), ws.numel(),
                                 stream_handle(stream)))
         return J, g, lp
+
+    def layer_taps(self, electrons, stream=None):
+        """Per-layer KFAC statistics of the adjoint (``qmc_grad_taps``): a list
+        of dicts with ``kind`` ("dense" or "diagonal"), ``rows_per_walker``,
+        ``has_bias``, ``kernel_offset`` / ``bias_offset`` (flat parameter
+        offsets), ``x`` (B*rows, in_cols) inputs and ``dy`` (B*rows, out_cols)
+        output cotangents of log|psi_w| (for the diagonal tap: per-walker
+        gradients of its parameters); plus log|psi| (B,)."""
+        e = self._elec(electrons)
+        B = e.shape[0]
+        n = int(self.lib.qmc_layer_taps(self.h, B, None, 0, None))
+        if n < 0:
+            raise QmcError(7, "layer taps are built for FermiNet models only")
+        descs = (LayerTapC * n)()
+        total = C.c_size_t()
+        self.lib.qmc_layer_taps(self.h, B, descs, n, C.byref(total))
+        buf = torch.empty(int(total.value), dtype=torch.float32, device=self.device)
+        lp = torch.empty(B, dtype=torch.float32, device=self.device)
+        ws, nb = self.workspace(OP_GRAD, B)
+        check(self.lib.qmc_grad_taps(self.h, B, ptr(e), ptr(buf), buf.numel(), ptr(lp), ptr(ws), ws.numel(),
+                                     stream_handle(stream)))
+        out = []
+        for t in descs:
+            rows = B * t.rows_per_walker
+            x = buf[t.in_offset:t.in_offset + rows * t.in_cols].view(rows, t.in_cols)
+            dy = buf[t.out_offset:t.out_offset + rows * t.out_cols].view(rows, t.out_cols)
+            out.append({"kind": "dense" if t.kind == TAP_DENSE else "diagonal",
+                        "rows_per_walker": t.rows_per_walker, "has_bias": bool(t.has_bias),
+                        "kernel_offset": int(t.kernel_offset), "bias_offset": int(t.bias_offset),
+                        "in_cols": t.in_cols, "out_cols": t.out_cols, "x": x, "dy": dy})
+        return out, lp
 
     def mh_draws(self, batch, steps, seed, counter, stream=None):
         nz = torch.empty((steps, batch, self.n, 3), dtype=torch.float32, device=self.device)

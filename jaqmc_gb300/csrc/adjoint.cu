@@ -259,6 +259,90 @@ __global__ void k_weighted_sum(int B, size_t P, const float* __restrict__ J, con
 
 static inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
+// ------------------------------------------------------------ layer taps
+// Input rows of one-electron layer l for a chunk: [h1 (din) | spin means of
+// h1 (C din, the walker's) | spin means of h2 (C d2in, the row's)], the order
+// of the reference's Dense kernel rows (backbone/ferminet.py:82-90).
+__global__ void k_tap_x1(int B, int n, int din, int dinp, int c_din, int g1p, int c_d2, int g2p,
+                         const float* __restrict__ in, const float* __restrict__ g1m, const float* __restrict__ G2,
+                         float* __restrict__ dst) {
+  const int cols = din + c_din + c_d2;
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * n * cols) return;
+  const int c = (int)(e % cols);
+  const size_t r = e / cols;
+  float v;
+  if (c < din) v = in[r * dinp + c];
+  else if (c < din + c_din) v = g1m[(r / n) * g1p + (c - din)];
+  else v = G2[r * g2p + (c - din - c_din)];
+  dst[e] = v;
+}
+
+// dst[(w ns + ii) cols + c] = scale * src[(w n + i0 + ii) ld + c]
+__global__ void k_tap_gather(int B, int n, int i0, int ns, const float* __restrict__ src, int ld, int cols,
+                             float* __restrict__ dst) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * ns * cols) return;
+  const int c = (int)(e % cols);
+  const size_t r = e / cols;
+  const size_t w = r / ns;
+  const int ii = (int)(r % ns);
+  dst[e] = src[(w * n + i0 + ii) * (size_t)ld + c];
+}
+
+struct TapPlan {
+  int count = 0;
+  qmc_layer_tap t[2 * QMC_MAX_LAYERS + 3];
+  size_t total = 0;
+};
+
+static TapPlan make_taps(const qmc_model* m, int B) {
+  const Dims& d = m->d;
+  const ParamLayout& pl = m->p;
+  TapPlan tp;
+  size_t o = 0;
+  auto add = [&](int kind, int rpw, int in_cols, int out_cols, int bias, size_t k_off, size_t b_off) {
+    qmc_layer_tap& t = tp.t[tp.count++];
+    t.kind = kind;
+    t.rows_per_walker = rpw;
+    t.in_cols = in_cols;
+    t.out_cols = out_cols;
+    t.has_bias = bias;
+    t.kernel_offset = k_off;
+    t.bias_offset = b_off;
+    t.in_offset = o;
+    o += (size_t)B * rpw * in_cols;
+    t.out_offset = o;
+    o += (size_t)B * rpw * out_cols;
+  };
+  for (int l = 0; l < d.L; ++l) {
+    add(QMC_TAP_DENSE, d.n, d.d1_in[l] + d.C * d.d1_in[l] + d.C * d.d2_in[l], d.d1[l], 1, pl.dense1_k[l],
+        pl.dense1_b[l]);
+    if (d.upd2[l]) add(QMC_TAP_DENSE, d.n * d.n, d.d2_in[l], d.d2[l], 1, pl.dense2_k[l], pl.dense2_b[l]);
+  }
+  const int nch = d.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    const int ns = d.split ? (c == 0 ? d.n_up : d.n_dn) : d.n;
+    add(QMC_TAP_DENSE, ns, d.d_last, d.norb, 0, pl.orb_k[c], 0);
+  }
+  const size_t env0 = pl.env_pi[0];
+  if (pl.total > env0) add(QMC_TAP_DIAGONAL, 1, 0, (int)(pl.total - env0), 0, env0, 0);
+  tp.total = o;
+  return tp;
+}
+
+// Where backward() writes the taps of a chunk: the call's plan and the
+// chunk's first walker.
+struct TapOut {
+  float* base = nullptr;
+  const TapPlan* plan = nullptr;
+  int w0 = 0;
+  float* in(int k) const { return base + plan->t[k].in_offset + (size_t)w0 * plan->t[k].rows_per_walker * plan->t[k].in_cols; }
+  float* out(int k) const {
+    return base + plan->t[k].out_offset + (size_t)w0 * plan->t[k].rows_per_walker * plan->t[k].out_cols;
+  }
+};
+
 // ------------------------------------------------------------ plan
 struct GradPlan {
   int B;
@@ -387,7 +471,8 @@ static qmc_status forward_save(qmc_model* m, const GradPlan& p, void* ws, const 
 }
 
 // Backward pass of one chunk: per-walker Jacobian rows into J (row stride P).
-static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, float* logpsi, cudaStream_t s) {
+static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, float* logpsi, cudaStream_t s,
+                           const TapOut* taps = nullptr) {
   const Dims& d = m->d;
   const ArenaLayout& a = m->a;
   const ParamLayout& pl = m->p;
@@ -427,6 +512,17 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
           P, pl.orb_k[c]);
       QMC_CUDA(cudaGetLastError());
     }
+    if (taps) {  // orbital projection of channel c: inputs h1[L-1] and cotangents orbbar, its rows only
+      int k = 0;
+      for (int l = 0; l < d.L; ++l) k += d.upd2[l] ? 2 : 1;
+      k += c;
+      k_tap_gather<<<blocks((size_t)B * ns * d.d_last), 256, 0, s>>>(B, n, i0, ns, at<float>(ws, p.h1[d.L - 1]),
+                                                                    d.d_last, d.d_last, taps->in(k));
+      QMC_CUDA(cudaGetLastError());
+      k_tap_gather<<<blocks((size_t)B * ns * d.norb), 256, 0, s>>>(B, n, i0, ns, at<float>(ws, p.orbbar), d.norb_p,
+                                                                  d.norb, taps->out(k));
+      QMC_CUDA(cudaGetLastError());
+    }
     // hbar of the last layer's rows of this channel = orbbar W_orb^T
     RowMap map{ns, i0, n, 1};
     QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, at<float>(ws, p.orbbar), d.norb_p, d.norb_p, nullptr, 0, 0,
@@ -445,6 +541,15 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
       k_tanh_bwd<<<blocks(rows * dout), 256, 0, s>>>(rows * dout, res ? kRsqrt2 : 1.f, hb_out, at<float>(ws, p.y1[l]),
                                                      zbar);
       QMC_CUDA(cudaGetLastError());
+      if (taps) {  // one-electron Dense l: inputs [h1 | means] and output cotangents zbar
+        int k = 0;
+        for (int q = 0; q < l; ++q) k += d.upd2[q] ? 2 : 1;
+        const int cols = din + d.C * din + d.C * d.d2_in[l];
+        k_tap_x1<<<blocks(rows * cols), 256, 0, s>>>(B, n, din, dinp, d.C * din, d.g1_p[l], d.C * d.d2_in[l], d.g2_p[l],
+                                                     in, at<float>(ws, p.g1m[l]), at<float>(ws, p.G2[l]), taps->in(k));
+        QMC_CUDA(cudaGetLastError());
+        QMC_CUDA(cudaMemcpyAsync(taps->out(k), zbar, sizeof(float) * rows * dout, cudaMemcpyDeviceToDevice, s));
+      }
       const size_t k0 = pl.dense1_k[l];
       k_jac_outer<<<blocks((size_t)B * din * dout), 256, 0, s>>>(B, n, n, 0, in, dinp, din, zbar, dout, dout, J, P, k0);
       QMC_CUDA(cudaGetLastError());
@@ -484,6 +589,13 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
         k_tanh_bwd<<<blocks(pairs * d.d2[l]), 256, 0, s>>>(pairs * d.d2[l], d.d2_in[l] == d.d2[l] ? kRsqrt2 : 1.f,
                                                           h2b_next, at<float>(ws, p.y2[l]), z2);
         QMC_CUDA(cudaGetLastError());
+        if (taps) {  // two-electron Dense l: inputs h2[l] and output cotangents z2 (contiguous pair rows)
+          int k = 1;
+          for (int q = 0; q < l; ++q) k += d.upd2[q] ? 2 : 1;
+          QMC_CUDA(cudaMemcpyAsync(taps->in(k), at<float>(ws, p.h2[l]), sizeof(float) * pairs * d.d2_in[l],
+                                   cudaMemcpyDeviceToDevice, s));
+          QMC_CUDA(cudaMemcpyAsync(taps->out(k), z2, sizeof(float) * pairs * d.d2[l], cudaMemcpyDeviceToDevice, s));
+        }
         k_jac_outer<<<blocks((size_t)B * d.d2_in[l] * d.d2[l]), 256, 0, s>>>(
             B, n * n, n * n, 0, at<float>(ws, p.h2[l]), d.d2_in[l], d.d2_in[l], z2, d.d2[l], d.d2[l], J, P,
             pl.dense2_k[l]);
@@ -508,6 +620,47 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
     hb ^= 1;
   }
   return QMC_OK;
+}
+
+// qmc_grad_taps: the adjoint's chunks with the layer taps written out; the
+// envelope tap is the envelope columns of each chunk's per-walker Jacobian.
+qmc_status run_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,
+                         float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
+  const int chunk = grad_chunk(m, batch);
+  const GradPlan p = make_grad_plan(m, chunk);
+  if (ws_bytes < p.total) {
+    set_error("workspace too small for the adjoint: %zu bytes given, %zu needed", ws_bytes, p.total);
+    return QMC_ERR_WORKSPACE;
+  }
+  const TapPlan tp = make_taps(m, batch);
+  if (taps_floats < tp.total) {
+    set_error("taps buffer too small: %zu floats given, %zu needed", taps_floats, tp.total);
+    return QMC_ERR_WORKSPACE;
+  }
+  const size_t P = m->p.total;
+  for (int w0 = 0; w0 < batch; w0 += chunk) {
+    const int B = std::min(chunk, batch - w0);
+    GradPlan q = make_grad_plan(m, B);
+    float* J = at<float>(ws, q.J);
+    TapOut to;
+    to.base = taps;
+    to.plan = &tp;
+    to.w0 = w0;
+    QMC_TRY(forward_save(m, q, ws, electrons + (size_t)w0 * m->d.n * 3, s));
+    QMC_TRY(backward(m, q, ws, J, logpsi ? logpsi + w0 : nullptr, s, &to));
+    const qmc_layer_tap& et = tp.t[tp.count - 1];
+    if (et.kind == QMC_TAP_DIAGONAL)
+      QMC_CUDA(cudaMemcpy2DAsync(to.out(tp.count - 1), sizeof(float) * et.out_cols, J + et.kernel_offset,
+                                 sizeof(float) * P, sizeof(float) * et.out_cols, B, cudaMemcpyDeviceToDevice, s));
+  }
+  return QMC_OK;
+}
+
+int layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total) {
+  const TapPlan tp = make_taps(m, batch);
+  for (int k = 0; k < tp.count && k < max_taps; ++k) taps[k] = tp.t[k];
+  if (total) *total = tp.total;
+  return tp.count;
 }
 
 qmc_status run_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
