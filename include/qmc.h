@@ -278,6 +278,28 @@ qmc_status qmc_model_set_energy_budget(qmc_model* m, size_t bytes);
  * NaNs skipped (src/jaqmc/estimator/base.py:27-53).  mean_var: 2 doubles. */
 qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t stream);
 
+/* Effective-core-potential energy per walker: the reference's ECPEnergy
+ * estimator (src/jaqmc/estimator/ecp/estimator.py:33-155, nonlocal integral
+ * src/jaqmc/estimator/ecp/nonlocal_integral.py:17-130).  e_local (batch,) =
+ * sum_{i,I} V_0(r_iI); e_nonlocal (batch,) = sum_i sum over the max_core
+ * nearest ECP atoms of sum_l V_{l+1}(r) (2l+1) sum_q w_q P_l(cos theta_q)
+ * psi(r_i -> R + r Rot_i x_q) / psi, each displaced configuration one forward
+ * pass of the model (run in chunks inside the workspace).  Device tables:
+ * ecp_atoms [n_ecp_atoms] indices into the model's atoms; radial
+ * [n_ecp_atoms][n_channels][max_terms][3] = (alpha, coeff, power) with
+ * V_c(r) = sum_t coeff r^power exp(-alpha r^2), channel 0 local and channel
+ * l + 1 the semi-local l (zero coefficients pad); quad [n_quad][4] = (x, y,
+ * z, weight), weights summing to 1; rotations [batch][n][9] row-major or NULL
+ * (then drawn from Philox4x32-10 with seed / counter: phi = 2 pi u1,
+ * cos theta = 1 - 2 u2 per walker and electron).  n_channels <= 5, max_core
+ * <= 8, n_quad <= 256. */
+size_t qmc_ecp_workspace_size(const qmc_model* m, int batch, int n_channels, int max_core, int n_quad);
+qmc_status qmc_ecp_energy(qmc_model* m, int batch, const float* electrons, int n_ecp_atoms, const int* ecp_atoms,
+                          int n_channels, int max_terms, const float* radial, int max_core, int n_quad,
+                          const float* quad, const float* rotations, uint64_t seed, uint64_t counter,
+                          float* e_local, float* e_nonlocal, void* workspace, size_t workspace_bytes,
+                          cudaStream_t stream);
+
 /* Reads and clears the model's device error word (synchronises the device).
  * Returns QMC_ERR_TIMEOUT with *code != 0 when a bounded wait inside a
  * tensor-core kernel expired since the last check. */

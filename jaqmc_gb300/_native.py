@@ -97,6 +97,10 @@ _SIGS = {
     "qmc_model_check_error": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qmc_profile_enable": (C.c_int, [C.c_int]),
     "qmc_profile_read": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p]),
+    "qmc_ecp_workspace_size": (C.c_size_t, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "qmc_ecp_energy": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                 C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "qmc_ffma_throughput": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
 }
 
@@ -368,6 +372,26 @@ class NativeFermiNet:
                         "kernel_offset": int(t.kernel_offset), "bias_offset": int(t.bias_offset),
                         "in_cols": t.in_cols, "out_cols": t.out_cols, "x": x, "dy": dy})
         return out, lp
+
+    def ecp_energy(self, electrons, tables, rotations=None, seed=0, counter=0, stream=None):
+        """ECP energy per walker (``qmc_ecp_energy``): ``(local, nonlocal)``.
+        ``tables`` is the dict ECPTables.device() returns (device arrays and
+        sizes); ``rotations`` (B, n, 3, 3) or None for Philox draws."""
+        e = self._elec(electrons)
+        B = e.shape[0]
+        t = tables
+        loc = torch.empty(B, dtype=torch.float32, device=self.device)
+        nl = torch.empty(B, dtype=torch.float32, device=self.device)
+        nb = int(self.lib.qmc_ecp_workspace_size(self.h, B, t["n_channels"], t["max_core"], t["n_quad"]))
+        ws = self.ws.get(nb)
+        rot = None
+        if rotations is not None:
+            rot = rotations.to(device=self.device, dtype=torch.float32).contiguous()
+        check(self.lib.qmc_ecp_energy(self.h, B, ptr(e), t["n_ecp_atoms"], ptr(t["ecp_atoms"]), t["n_channels"],
+                                      t["max_terms"], ptr(t["radial"]), t["max_core"], t["n_quad"], ptr(t["quad"]),
+                                      ptr(rot), int(seed), int(counter), ptr(loc), ptr(nl), ptr(ws), ws.numel(),
+                                      stream_handle(stream)))
+        return loc, nl
 
     def mh_draws(self, batch, steps, seed, counter, stream=None):
         nz = torch.empty((steps, batch, self.n, 3), dtype=torch.float32, device=self.device)

@@ -412,6 +412,43 @@ def potential_energy(params, batched_data: BatchedData, prev_walker_stats, state
 
 
 @dataclass
+class ECPEnergy:
+    """Effective-core-potential energy ``energy:ecp`` (the reference's
+    ECPEnergy, src/jaqmc/estimator/ecp/estimator.py:33-155): the local channel
+    plus the nonlocal channels integrated on a randomly rotated spherical rule
+    around the ``max_core`` nearest ECP atoms of each electron, every
+    displaced configuration evaluated by the GPU forward pass
+    (``qmc_ecp_energy``).  ``ecp_coefficients`` are PySCF ECP dictionaries,
+    ``atom_symbols`` the molecule's element symbols; the rotations come from
+    Philox draws keyed by ``rngs`` and the call count (state)."""
+
+    max_core: int = 2
+    quadrature_id: str | None = None
+    phase_logpsi: Any = None  # the wavefunction
+    ecp_coefficients: dict = field(default_factory=dict)
+    atom_symbols: list = field(default_factory=list)
+
+    def init(self, data, rngs=None):
+        from . import ecp as _ecp
+        self._tables = _ecp.ECPTables(self.ecp_coefficients, self.atom_symbols, self.max_core, self.quadrature_id)
+        seed = 0 if rngs is None else (int(rngs) if np.isscalar(rngs) else int(np.asarray(rngs).ravel()[0]))
+        return {"seed": seed, "calls": 0}
+
+    def evaluate_batch_walkers(self, params, batched_data: BatchedData, prev_walker_stats, state, rngs=None):
+        if state is None:
+            state = self.init(batched_data.data, rngs)
+        wf = self.phase_logpsi
+        m = wf.model(batched_data.data, params)
+        x = _device_electrons(batched_data.data.electrons, wf._dev())
+        loc, nl = m.ecp_energy(x, self._tables.device_tables(m.device), seed=state["seed"],
+                               counter=state["calls"])
+        return {"energy:ecp": loc + nl}, {**state, "calls": state["calls"] + 1}
+
+    def reduce(self, walker_stats):
+        return mean_reduce(walker_stats)
+
+
+@dataclass
 class TotalEnergy:
     output_name: str = "total_energy"
     components: list | None = None

@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("nspins,split", [((2, 1), True), ((2, 1), False), ((2, 0), True)])
 def test_taps_rebuild_the_per_walker_jacobian(nspins, split, cuda_device):
-    mol = S.make_molecule("Li", [3], [[0, 0, 0]], nspins) if nspins != (2, 1) else S.lithium()
+    mol = S.make_molecule("He", [2], [[0, 0, 0]], nspins) if nspins == (2, 0) else S.lithium()
     cfg = small_cfg(nspins, ndets=3, orbitals_spin_split=split)
     _, flat, x = setup(mol, cfg, 5)
     m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, device=cuda_device)
