@@ -38,7 +38,7 @@ def _case(name):
 @pytest.mark.parametrize("name,quad", [("Li", "icosahedron_12"), ("LiH", "octahedron_18")])
 def test_ecp_energy_matches_oracle(name, quad, cuda_device):
     mol, symbols, max_core = _case(name)
-    cfg = small_cfg(mol.nspins, ndets=2)
+    cfg = small_cfg(mol.nspins, ndets=2, hidden_dims_single=[16, 16])
     tree, flat, x = setup(mol, cfg, 12)
     m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, device=cuda_device)
     m.set_params(torch.as_tensor(flat, device=cuda_device))
