@@ -13,6 +13,7 @@
 #include "kernels.cuh"
 #include "plan.cuh"
 #include "profile.cuh"
+#include "psiformer.cuh"
 
 namespace qmc {
 
@@ -680,6 +681,566 @@ qmc_status run_grad(qmc_model* m, int batch, const float* electrons, const doubl
     float* J = per_walker ? per_walker + (size_t)w0 * P : at<float>(ws, q.J);
     QMC_TRY(forward_save(m, q, ws, electrons + (size_t)w0 * m->d.n * 3, s));
     QMC_TRY(backward(m, q, ws, J, logpsi ? logpsi + w0 : nullptr, s));
+    if (grad && weights) {
+      ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
+      k_weighted_sum<<<blocks(P), 256, 0, s>>>(B, P, J, weights + w0, grad);
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  return QMC_OK;
+}
+
+
+// =====================================================================
+// Psiformer parameter adjoint (FP32 SIMT): per-walker d log|psi| / d theta of
+// PsiformerWavefunction (src/jaqmc/app/molecule/wavefunction/psiformer.py:
+// 38-146, backbone src/jaqmc/wavefunction/backbone/psiformer.py:29-187,
+// Jastrow src/jaqmc/wavefunction/jastrow.py:48-122), the reverse of the value
+// forward: input Dense, per layer LayerNorm -> multi-head attention (QKV
+// Dense, softmax(q k^T / sqrt(Dh)) v, output Dense) -> residual -> LayerNorm
+// -> tanh MLP -> residual, orbitals x envelope, log-sum-exp of determinants,
+// plus the Jastrow.  The forward keeps every layer's activations (the
+// backward needs them all); walkers run in chunks under the gradient budget.
+// =====================================================================
+
+// LayerNorm of one row per warp (D <= 512, a multiple of 32): y = (x - mu) rs s + b,
+// rs = 1 / sqrt(var + 1e-5) with the biased two-pass variance; mu and rs kept.
+__global__ void k_psi_ln_fwd(int rows, int D, const float* __restrict__ x, const float* __restrict__ sc,
+                             const float* __restrict__ bi, float* __restrict__ y, float* __restrict__ mu,
+                             float* __restrict__ rs) {
+  const int lane = threadIdx.x & 31;
+  const size_t r = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= (size_t)rows) return;
+  const float* xr = x + r * D;
+  float s = 0.f;
+  for (int f = lane; f < D; f += 32) s += xr[f];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const float m = s / (float)D;
+  float q = 0.f;
+  for (int f = lane; f < D; f += 32) q += (xr[f] - m) * (xr[f] - m);
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+  const float inv = rsqrtf(q / (float)D + 1e-5f);
+  for (int f = lane; f < D; f += 32) y[r * D + f] = (xr[f] - m) * inv * sc[f] + bi[f];
+  if (lane == 0) {
+    mu[r] = m;
+    rs[r] = inv;
+  }
+}
+
+// dx += rs (g - mean(g) - xhat mean(g xhat)), g = dy s, xhat = (x - mu) rs (one warp per row).
+__global__ void k_psi_ln_bwd(int rows, int D, const float* __restrict__ x, const float* __restrict__ mu,
+                             const float* __restrict__ rs, const float* __restrict__ sc, const float* __restrict__ dy,
+                             float* __restrict__ dx) {
+  const int lane = threadIdx.x & 31;
+  const size_t r = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= (size_t)rows) return;
+  const float m = mu[r], inv = rs[r];
+  float sg = 0.f, sgx = 0.f;
+  for (int f = lane; f < D; f += 32) {
+    const float g = dy[r * D + f] * sc[f];
+    sg += g;
+    sgx += g * (x[r * D + f] - m) * inv;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sg += __shfl_xor_sync(0xffffffffu, sg, o);
+    sgx += __shfl_xor_sync(0xffffffffu, sgx, o);
+  }
+  sg /= (float)D;
+  sgx /= (float)D;
+  for (int f = lane; f < D; f += 32) {
+    const float xh = (x[r * D + f] - m) * inv;
+    dx[r * D + f] += inv * (dy[r * D + f] * sc[f] - sg - xh * sgx);
+  }
+}
+
+// Per-walker LayerNorm parameter rows: J[scale_f] = sum_i xhat_if dy_if, J[bias_f] = sum_i dy_if.
+__global__ void k_psi_ln_jac(int B, int n, int D, const float* __restrict__ x, const float* __restrict__ mu,
+                             const float* __restrict__ rs, const float* __restrict__ dy, float* __restrict__ J,
+                             size_t P, size_t off_s, size_t off_b) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)B * D) return;
+  const int w = (int)(e / D), f = (int)(e % D);
+  float js = 0.f, jb = 0.f;
+  for (int i = 0; i < n; ++i) {
+    const size_t r = (size_t)w * n + i;
+    const float g = dy[r * D + f];
+    js = fmaf((x[r * D + f] - mu[r]) * rs[r], g, js);
+    jb += g;
+  }
+  J[(size_t)w * P + off_s + f] = js;
+  J[(size_t)w * P + off_b + f] = jb;
+}
+
+__global__ void k_psi_add_jas(int B, float* __restrict__ lp, const float* __restrict__ jas) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < B) lp[w] += jas[w];
+}
+
+__global__ void k_psi_tanh_add(size_t count, float* __restrict__ z, const float* __restrict__ res,
+                               float* __restrict__ out, int act) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  float v = z[e];
+  if (act) v = tanhf(v);
+  z[e] = v;
+  if (out) out[e] = v + res[e];
+}
+
+// Attention of one (walker, head) per block, keeping the probabilities:
+// qkv rows [q | k | v] with biases (q unscaled); P[w][h][i][j] = softmax_j(q_i . k_j / sqrt(Dh));
+// o[w n + i][h Dh + d] = sum_j P_ij v_jd.  n <= 64, Dh <= 64.
+__global__ void __launch_bounds__(128) k_psi_attn_save(int n, int H, int Dh, const float* __restrict__ qkv,
+                                                       float* __restrict__ Pr, float* __restrict__ o) {
+  extern __shared__ float sm[];
+  const int w = blockIdx.x / H, h = blockIdx.x % H, D = H * Dh;
+  float* q = sm;              // [n][Dh]
+  float* k = q + n * Dh;      // [n][Dh]
+  float* v = k + n * Dh;      // [n][Dh]
+  float* S = v + n * Dh;      // [n][n]
+  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
+    const int i = e / Dh, d = e % Dh;
+    const float* r = qkv + ((size_t)w * n + i) * 3 * D + h * Dh + d;
+    q[e] = r[0];
+    k[e] = r[D];
+    v[e] = r[2 * D];
+  }
+  __syncthreads();
+  const float sc = 1.0f / sqrtf((float)Dh);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    float a = 0.f;
+    for (int d = 0; d < Dh; ++d) a = fmaf(q[i * Dh + d], k[j * Dh + d], a);
+    S[e] = a * sc;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int i = threadIdx.x >> 5; i < n; i += nw) {
+    float mx = -INFINITY;
+    for (int j = lane; j < n; j += 32) mx = fmaxf(mx, S[i * n + j]);
+    for (int of = 16; of > 0; of >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, of));
+    float sum = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      const float e = expf(S[i * n + j] - mx);
+      S[i * n + j] = e;
+      sum += e;
+    }
+    for (int of = 16; of > 0; of >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, of);
+    for (int j = lane; j < n; j += 32) S[i * n + j] /= sum;
+  }
+  __syncthreads();
+  float* Pw = Pr + ((size_t)w * H + h) * n * n;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Pw[e] = S[e];
+  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
+    const int i = e / Dh, d = e % Dh;
+    float a = 0.f;
+    for (int j = 0; j < n; ++j) a = fmaf(S[i * n + j], v[j * Dh + d], a);
+    o[((size_t)w * n + i) * D + h * Dh + d] = a;
+  }
+}
+
+// Attention backward of one (walker, head): from do (the cotangent of o),
+//   dv = P^T do, dP = do v^T, dS = P (dP - rowsum(dP P)),
+//   dq = dS k / sqrt(Dh), dk = dS^T q / sqrt(Dh), written into qkvbar rows [dq | dk | dv].
+__global__ void __launch_bounds__(128) k_psi_attn_bwd(int n, int H, int Dh, const float* __restrict__ qkv,
+                                                      const float* __restrict__ Pr, const float* __restrict__ dout,
+                                                      float* __restrict__ qkvbar) {
+  extern __shared__ float sm[];
+  const int w = blockIdx.x / H, h = blockIdx.x % H, D = H * Dh;
+  float* q = sm;
+  float* k = q + n * Dh;
+  float* v = k + n * Dh;
+  float* g = v + n * Dh;      // do [n][Dh]
+  float* P = g + n * Dh;      // [n][n]
+  float* dS = P + n * n;      // [n][n]
+  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
+    const int i = e / Dh, d = e % Dh;
+    const float* r = qkv + ((size_t)w * n + i) * 3 * D + h * Dh + d;
+    q[e] = r[0];
+    k[e] = r[D];
+    v[e] = r[2 * D];
+    g[e] = dout[((size_t)w * n + i) * D + h * Dh + d];
+  }
+  const float* Pw = Pr + ((size_t)w * H + h) * n * n;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) P[e] = Pw[e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {  // dP_ij = do_i . v_j
+    const int i = e / n, j = e % n;
+    float a = 0.f;
+    for (int d = 0; d < Dh; ++d) a = fmaf(g[i * Dh + d], v[j * Dh + d], a);
+    dS[e] = a;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int i = threadIdx.x >> 5; i < n; i += nw) {
+    float t = 0.f;
+    for (int j = lane; j < n; j += 32) t += dS[i * n + j] * P[i * n + j];
+    for (int of = 16; of > 0; of >>= 1) t += __shfl_xor_sync(0xffffffffu, t, of);
+    for (int j = lane; j < n; j += 32) dS[i * n + j] = P[i * n + j] * (dS[i * n + j] - t);
+  }
+  __syncthreads();
+  const float sc = 1.0f / sqrtf((float)Dh);
+  for (int e = threadIdx.x; e < n * Dh; e += blockDim.x) {
+    const int i = e / Dh, d = e % Dh;
+    float dq = 0.f, dk = 0.f, dv = 0.f;
+    for (int j = 0; j < n; ++j) {
+      dq = fmaf(dS[i * n + j], k[j * Dh + d], dq);
+      dk = fmaf(dS[j * n + i], q[j * Dh + d], dk);
+      dv = fmaf(P[j * n + i], g[j * Dh + d], dv);
+    }
+    float* out = qkvbar + ((size_t)w * n + i) * 3 * D + h * Dh + d;
+    out[0] = dq * sc;
+    out[D] = dk * sc;
+    out[2 * D] = dv;
+  }
+}
+
+// SimpleEE Jastrow parameter rows: d/d alpha of -c alpha^2 / (alpha + r) is
+// -c alpha (alpha + 2 r) / (alpha + r)^2 (c = 1/4 same spin, 1/2 opposite).
+__global__ void k_psi_jas_jac(int B, int n, int n_up, const float* __restrict__ x, const float* __restrict__ alpha,
+                              float* __restrict__ J, size_t P, size_t off_par, size_t off_anti) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= B) return;
+  const float ap = alpha[0], aa = alpha[1];
+  float jp = 0.f, ja = 0.f;
+  const float* xw = x + (size_t)w * n * 3;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      const float dx = xw[3 * i] - xw[3 * j], dy = xw[3 * i + 1] - xw[3 * j + 1], dz = xw[3 * i + 2] - xw[3 * j + 2];
+      const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+      if ((i < n_up) == (j < n_up)) jp += -0.25f * ap * (ap + 2.f * r) / ((ap + r) * (ap + r));
+      else ja += -0.5f * aa * (aa + 2.f * r) / ((aa + r) * (aa + r));
+    }
+  J[(size_t)w * P + off_par] = jp;
+  J[(size_t)w * P + off_anti] = ja;
+}
+
+struct PsiGradPlan {
+  int B;
+  size_t x0, rae, aevec, jas, h[kPsiMaxLayers + 1], mu0[kPsiMaxLayers], rs0[kPsiMaxLayers], xn0[kPsiMaxLayers],
+      qkv[kPsiMaxLayers], pr[kPsiMaxLayers], o[kPsiMaxLayers], hm[kPsiMaxLayers], mu1[kPsiMaxLayers],
+      rs1[kPsiMaxLayers], xn1[kPsiMaxLayers], y[kPsiMaxLayers][kPsiMaxMlp + 1];
+  size_t amat, orb, abar, envbar, hbar, hmbar, zbar, tmp, obar, qkvbar, orbbar, J, total;
+};
+
+static PsiGradPlan make_psi_grad_plan(const qmc_model* m, int B) {
+  const PsiDims& d = m->psi->d;
+  PsiGradPlan p{};
+  p.B = B;
+  size_t o = 0;
+  auto take = [&](size_t floats) { size_t r = o; o += align_up(floats * 4, 256); return r; };
+  const size_t rows = (size_t)B * d.n, D = d.D;
+  int wmax = d.D;
+  for (int k = 0; k < d.n_dense; ++k) wmax = std::max(wmax, d.mlp[k]);
+  p.x0 = take(rows * d.K0p);
+  p.rae = take(rows * d.A);
+  p.aevec = take(rows * d.A * 3);
+  p.jas = take(B);
+  for (int l = 0; l <= d.L; ++l) p.h[l] = take(rows * D);
+  for (int l = 0; l < d.L; ++l) {
+    p.mu0[l] = take(rows);
+    p.rs0[l] = take(rows);
+    p.xn0[l] = take(rows * D);
+    p.qkv[l] = take(rows * 3 * D);
+    p.pr[l] = take((size_t)B * d.H * d.n * d.n);
+    p.o[l] = take(rows * D);
+    p.hm[l] = take(rows * D);
+    p.mu1[l] = take(rows);
+    p.rs1[l] = take(rows);
+    p.xn1[l] = take(rows * D);
+    for (int k = 0; k < d.n_dense; ++k) p.y[l][k] = take(rows * d.mlp[k]);
+  }
+  const size_t am = (size_t)B * d.K * d.n * d.n;
+  p.amat = take(am);
+  p.orb = take(am);
+  p.abar = take(am);
+  p.envbar = take(am);
+  p.hbar = take(rows * D);
+  p.hmbar = take(rows * D);
+  p.zbar = take(rows * wmax);
+  p.tmp = take(rows * std::max<size_t>(3 * D, std::max<size_t>(wmax, m->d.norb_p)));
+  p.obar = take(rows * D);
+  p.qkvbar = take(rows * 3 * D);
+  p.orbbar = take(rows * m->d.norb_p);
+  p.J = take((size_t)B * m->psi->p.total);
+  p.total = o;
+  return p;
+}
+
+static int psi_grad_chunk(const qmc_model* m, int B) {
+  const size_t one = make_psi_grad_plan(m, 1).total;
+  const size_t two = make_psi_grad_plan(m, 2).total;
+  const size_t per = two > one ? two - one : one;
+  const size_t c = m->grad_budget > one ? 1 + (m->grad_budget - one) / per : 1;
+  return (int)std::max<size_t>(1, std::min<size_t>(c, (size_t)B));
+}
+
+size_t psi_grad_workspace(const qmc_model* m, int B) { return make_psi_grad_plan(m, psi_grad_chunk(m, B)).total; }
+
+static qmc_status psi_forward_save(qmc_model* m, const PsiGradPlan& p, void* ws, const float* electrons,
+                                   cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const Dims& fd = m->d;
+  const ArenaLayout& fa = m->a;
+  const float* ar = m->arena;
+  const int B = p.B, n = d.n, D = d.D;
+  const size_t rows = (size_t)B * n;
+  const RowMap rmap{n, 0, n, 1};
+  const unsigned wb = (unsigned)((rows + 7) / 8);  // warp-per-row kernels, 8 rows per block
+  QMC_PROF(QMC_KC_FEATURES, launch_psi_features(s, B, n, d.n_up, d.A, d.K0p, electrons, ar + fa.atoms,
+                                                d.jastrow ? ar + P.alpha_par : nullptr, at<float>(ws, p.x0),
+                                                at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, p.jas)));
+  QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.x0), d.K0p, d.K0p, nullptr, 0, 0,
+                                           ar + a.w_in, D, D, EpiStore{at<float>(ws, p.h[0]), D, ar + P.in_b}));
+  float* tmp = at<float>(ws, p.tmp);
+  for (int l = 0; l < d.L; ++l) {
+    float* h = at<float>(ws, p.h[l]);
+    {
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_psi_ln_fwd<<<wb, 256, 0, s>>>((int)rows, D, h, ar + P.ln0_s[l], ar + P.ln0_b[l], at<float>(ws, p.xn0[l]),
+                                     at<float>(ws, p.mu0[l]), at<float>(ws, p.rs0[l]));
+      QMC_CUDA(cudaGetLastError());
+    }
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.xn0[l]), D, D, nullptr, 0, 0,
+                                                   ar + a.w_qkv[l], 3 * D, 3 * D,
+                                                   EpiStore{at<float>(ws, p.qkv[l]), 3 * D, ar + a.b_qkv[l]}));
+    {
+      ::qmc::ProfScope ps_(QMC_KC_PAIR, s);
+      const size_t sm = sizeof(float) * (3 * (size_t)n * d.Dh + (size_t)n * n);
+      k_psi_attn_save<<<B * d.H, 128, sm, s>>>(n, d.H, d.Dh, at<float>(ws, p.qkv[l]), at<float>(ws, p.pr[l]),
+                                               at<float>(ws, p.o[l]));
+      QMC_CUDA(cudaGetLastError());
+    }
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.o[l]), D, D, nullptr, 0, 0,
+                                                   ar + P.o_k[l], D, D, EpiStore{tmp, D, ar + P.o_b[l]}));
+    {
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_psi_tanh_add<<<blocks(rows * D), 256, 0, s>>>(rows * D, tmp, h, at<float>(ws, p.hm[l]), 0);
+      QMC_CUDA(cudaGetLastError());
+      k_psi_ln_fwd<<<wb, 256, 0, s>>>((int)rows, D, at<float>(ws, p.hm[l]), ar + P.ln1_s[l], ar + P.ln1_b[l],
+                                     at<float>(ws, p.xn1[l]), at<float>(ws, p.mu1[l]), at<float>(ws, p.rs1[l]));
+      QMC_CUDA(cudaGetLastError());
+    }
+    const float* in = at<float>(ws, p.xn1[l]);
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      float* y = at<float>(ws, p.y[l][k]);
+      QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, in, din, din, nullptr, 0, 0,
+                                                     ar + P.mlp_k[l][k], d.mlp[k], d.mlp[k],
+                                                     EpiStore{y, d.mlp[k], ar + P.mlp_b[l][k]}));
+      const bool last = k == d.n_dense - 1;
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_psi_tanh_add<<<blocks(rows * d.mlp[k]), 256, 0, s>>>(rows * d.mlp[k], y, at<float>(ws, p.hm[l]),
+                                                            last ? at<float>(ws, p.h[l + 1]) : nullptr, 1);
+      QMC_CUDA(cudaGetLastError());
+      in = y;
+      din = d.mlp[k];
+    }
+  }
+  // orbitals x envelope (the raw orbitals kept for the envelope cotangent)
+  const int nch = fd.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
+    const int i0 = (fd.split && c == 1) ? fd.n_up : 0;
+    RowMap map{ns, i0, n, 1};
+    EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + fa.env_pi[c],
+                   ar + fa.env_sigma[c], n, fd.A, fd.K, 1, fd.env_abs};
+    epi.orb = at<float>(ws, p.orb);
+    epi.unit_env = !env_in_epilogue(fd.env_kind);
+    QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, at<float>(ws, p.h[d.L]), D, D, nullptr, 0, 0,
+                                              ar + fa.w_orb[c], fd.norb_p, fd.norb, epi));
+  }
+  if (fd.env_kind == QMC_ENVELOPE_DIAGONAL) {
+    const int c1 = nch - 1;
+    QMC_PROF(QMC_KC_ORBITAL, launch_envelope_diag(s, B, n, fd.n_up, fd.split, fd.K, fd.A, 1, 1, ar + fa.env_pi[0],
+                                                  ar + fa.env_sigma[0], ar + fa.env_pi[c1], ar + fa.env_sigma[c1],
+                                                  at<float>(ws, p.aevec), at<float>(ws, p.amat)));
+  }
+  return QMC_OK;
+}
+
+static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, const float* electrons, float* J,
+                               float* logpsi, cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const Dims& fd = m->d;
+  const ArenaLayout& fa = m->a;
+  const float* ar = m->arena;
+  const int B = p.B, n = d.n, D = d.D;
+  const size_t rows = (size_t)B * n, Pn = P.total;
+  const RowMap rmap{n, 0, n, 1};
+  const unsigned wb = (unsigned)((rows + 7) / 8);
+  float* lp = logpsi;
+  QMC_PROF(QMC_KC_LOGDET, launch_logdet_bwd(s, B, n, fd.K, at<float>(ws, p.amat), at<float>(ws, p.abar), lp));
+  const int nch = fd.split ? 2 : 1;
+  {
+    ::qmc::ProfScope ps_(QMC_KC_ORBITAL, s);
+    if (lp) {
+      k_psi_add_jas<<<blocks(B), 256, 0, s>>>(B, lp, at<float>(ws, p.jas));
+      QMC_CUDA(cudaGetLastError());
+    }
+    k_orb_bwd<<<blocks(rows * fd.norb_p), 256, 0, s>>>(
+        B, n, fd.n_up, fd.split, fd.K, fd.A, fd.env_abs, fd.env_kind, fd.norb_p, at<float>(ws, p.abar),
+        at<float>(ws, p.orb), at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + fa.env_pi[0], ar + fa.env_sigma[0],
+        ar + fa.env_pi[nch - 1], ar + fa.env_sigma[nch - 1], at<float>(ws, p.orbbar), at<float>(ws, p.envbar));
+    QMC_CUDA(cudaGetLastError());
+  }
+  float* hbar = at<float>(ws, p.hbar);
+  for (int c = 0; c < nch; ++c) {
+    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
+    const int i0 = (fd.split && c == 1) ? fd.n_up : 0;
+    ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
+    if (fd.env_kind == QMC_ENVELOPE_DIAGONAL)
+      k_env_jac_diag<<<blocks((size_t)B * n * fd.A * fd.K), 256, 0, s>>>(
+          B, n, i0, ns, fd.K, fd.A, at<float>(ws, p.envbar), at<float>(ws, p.aevec), ar + fa.env_pi[c],
+          ar + fa.env_sigma[c], J, Pn, P.env_pi[c], P.env_sigma[c]);
+    else if (fd.env_kind != QMC_ENVELOPE_NULL)
+      k_env_jac<<<blocks((size_t)B * n * fd.A * fd.K), 256, 0, s>>>(B, n, i0, ns, fd.K, fd.A, fd.env_abs,
+                                                                   at<float>(ws, p.envbar), at<float>(ws, p.rae),
+                                                                   ar + fa.env_pi[c], ar + fa.env_sigma[c], J, Pn,
+                                                                   P.env_pi[c], P.env_sigma[c]);
+    QMC_CUDA(cudaGetLastError());
+    k_jac_outer<<<blocks((size_t)B * D * fd.norb), 256, 0, s>>>(B, ns, n, i0, at<float>(ws, p.h[d.L]), D, D,
+                                                              at<float>(ws, p.orbbar), fd.norb_p, fd.norb, J, Pn,
+                                                              P.orb_k[c]);
+    QMC_CUDA(cudaGetLastError());
+    RowMap map{ns, i0, n, 1};
+    QMC_CUDA(launch_gemm_simt(s, B * ns, map, at<float>(ws, p.orbbar), fd.norb_p, fd.norb_p, nullptr, 0, 0,
+                              ar + fa.wt_orb[c], D, D, EpiStore{hbar, D, nullptr}));
+  }
+  float* hmbar = at<float>(ws, p.hmbar);
+  float* zbar = at<float>(ws, p.zbar);
+  float* tmp = at<float>(ws, p.tmp);
+  float* obar = at<float>(ws, p.obar);
+  float* qkvbar = at<float>(ws, p.qkvbar);
+  for (int l = d.L - 1; l >= 0; --l) {
+    // h[l+1] = hm + y_last: both branches take hbar
+    QMC_CUDA(cudaMemcpyAsync(hmbar, hbar, sizeof(float) * rows * D, cudaMemcpyDeviceToDevice, s));
+    const float* ybar = hbar;
+    for (int k = d.n_dense - 1; k >= 0; --k) {
+      const int dout = d.mlp[k], din = k == 0 ? D : d.mlp[k - 1];
+      const float* x = k == 0 ? at<float>(ws, p.xn1[l]) : at<float>(ws, p.y[l][k - 1]);
+      ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
+      k_tanh_bwd<<<blocks(rows * dout), 256, 0, s>>>(rows * dout, 1.f, ybar, at<float>(ws, p.y[l][k]), zbar);
+      QMC_CUDA(cudaGetLastError());
+      k_jac_outer<<<blocks((size_t)B * din * dout), 256, 0, s>>>(B, n, n, 0, x, din, din, zbar, dout, dout, J, Pn,
+                                                                P.mlp_k[l][k]);
+      QMC_CUDA(cudaGetLastError());
+      k_colsum<<<blocks((size_t)B * dout), 256, 0, s>>>(B, n, zbar, dout, dout, nullptr, J, Pn, P.mlp_b[l][k]);
+      QMC_CUDA(cudaGetLastError());
+      // input cotangent zbar W^T into tmp (the next k's ybar, or the LayerNorm output's)
+      QMC_CUDA(launch_gemm_simt(s, B * n, rmap, zbar, dout, dout, nullptr, 0, 0, ar + a.t32_mlp[l][k], din, din,
+                                EpiStore{tmp, din, nullptr}));
+      ybar = tmp;
+    }
+    {
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      // LayerNorm 1: parameters and the cotangent of hm (tmp holds the cotangent of xn1)
+      k_psi_ln_jac<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, D, at<float>(ws, p.hm[l]), at<float>(ws, p.mu1[l]),
+                                                        at<float>(ws, p.rs1[l]), tmp, J, Pn, P.ln1_s[l], P.ln1_b[l]);
+      QMC_CUDA(cudaGetLastError());
+      k_psi_ln_bwd<<<wb, 256, 0, s>>>((int)rows, D, at<float>(ws, p.hm[l]), at<float>(ws, p.mu1[l]),
+                                     at<float>(ws, p.rs1[l]), ar + P.ln1_s[l], tmp, hmbar);
+      QMC_CUDA(cudaGetLastError());
+    }
+    {
+      // att = o Wo + bo; hm = h + att
+      ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
+      k_jac_outer<<<blocks((size_t)B * D * D), 256, 0, s>>>(B, n, n, 0, at<float>(ws, p.o[l]), D, D, hmbar, D, D, J,
+                                                            Pn, P.o_k[l]);
+      QMC_CUDA(cudaGetLastError());
+      k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hmbar, D, D, nullptr, J, Pn, P.o_b[l]);
+      QMC_CUDA(cudaGetLastError());
+      QMC_CUDA(launch_gemm_simt(s, B * n, rmap, hmbar, D, D, nullptr, 0, 0, ar + a.t32_o[l], D, D,
+                                EpiStore{obar, D, nullptr}));
+    }
+    {
+      ::qmc::ProfScope ps_(QMC_KC_PAIR, s);
+      const size_t sm = sizeof(float) * (4 * (size_t)n * d.Dh + 2 * (size_t)n * n);
+      k_psi_attn_bwd<<<B * d.H, 128, sm, s>>>(n, d.H, d.Dh, at<float>(ws, p.qkv[l]), at<float>(ws, p.pr[l]), obar,
+                                              qkvbar);
+      QMC_CUDA(cudaGetLastError());
+    }
+    {
+      ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
+      const float* xn0 = at<float>(ws, p.xn0[l]);
+      const size_t kofs[3] = {P.q_k[l], P.k_k[l], P.v_k[l]}, bofs[3] = {P.q_b[l], P.k_b[l], P.v_b[l]};
+      for (int c = 0; c < 3; ++c) {
+        k_jac_outer<<<blocks((size_t)B * D * D), 256, 0, s>>>(B, n, n, 0, xn0, D, D, qkvbar + (size_t)c * D, 3 * D, D,
+                                                              J, Pn, kofs[c]);
+        QMC_CUDA(cudaGetLastError());
+        k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, qkvbar + (size_t)c * D, 3 * D, D, nullptr, J, Pn,
+                                                       bofs[c]);
+        QMC_CUDA(cudaGetLastError());
+      }
+      QMC_CUDA(launch_gemm_simt(s, B * n, rmap, qkvbar, 3 * D, 3 * D, nullptr, 0, 0, ar + a.t32_qkv[l], D, D,
+                                EpiStore{tmp, D, nullptr}));
+    }
+    {
+      // LayerNorm 0 on h[l]; hbar(h[l]) = hmbar (residual) + its input cotangent
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_psi_ln_jac<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, D, at<float>(ws, p.h[l]), at<float>(ws, p.mu0[l]),
+                                                        at<float>(ws, p.rs0[l]), tmp, J, Pn, P.ln0_s[l], P.ln0_b[l]);
+      QMC_CUDA(cudaGetLastError());
+      QMC_CUDA(cudaMemcpyAsync(hbar, hmbar, sizeof(float) * rows * D, cudaMemcpyDeviceToDevice, s));
+      k_psi_ln_bwd<<<wb, 256, 0, s>>>((int)rows, D, at<float>(ws, p.h[l]), at<float>(ws, p.mu0[l]),
+                                     at<float>(ws, p.rs0[l]), ar + P.ln0_s[l], tmp, hbar);
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  {
+    ::qmc::ProfScope ps_(QMC_KC_LAYER0, s);
+    k_jac_outer<<<blocks((size_t)B * d.K0 * D), 256, 0, s>>>(B, n, n, 0, at<float>(ws, p.x0), d.K0p, d.K0, hbar, D, D,
+                                                             J, Pn, P.in_k);
+    QMC_CUDA(cudaGetLastError());
+    k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hbar, D, D, nullptr, J, Pn, P.in_b);
+    QMC_CUDA(cudaGetLastError());
+    if (d.jastrow) {
+      k_psi_jas_jac<<<blocks(B), 256, 0, s>>>(B, n, d.n_up, electrons, ar + P.alpha_par, J, Pn, P.alpha_par,
+                                              P.alpha_anti);
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  return QMC_OK;
+}
+
+qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
+                        double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
+  const PsiDims& pd = m->psi->d;
+  if (pd.n > 64 || pd.Dh > 64) {
+    set_error("the Psiformer adjoint supports at most 64 electrons and head width 64");
+    return QMC_ERR_SHAPE;
+  }
+  {
+    int dev;
+    QMC_CUDA(cudaGetDevice(&dev));
+    static int set_dev = -1;
+    if (set_dev != dev) {
+      QMC_CUDA(cudaFuncSetAttribute(k_psi_attn_save, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      QMC_CUDA(cudaFuncSetAttribute(k_psi_attn_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      set_dev = dev;
+    }
+  }
+  const int chunk = psi_grad_chunk(m, batch);
+  const PsiGradPlan p = make_psi_grad_plan(m, chunk);
+  if (ws_bytes < p.total) {
+    set_error("workspace too small for the adjoint: %zu bytes given, %zu needed", ws_bytes, p.total);
+    return QMC_ERR_WORKSPACE;
+  }
+  const size_t P = m->psi->p.total;
+  const int n = m->psi->d.n;
+  if (grad) QMC_CUDA(cudaMemsetAsync(grad, 0, P * sizeof(double), s));
+  for (int w0 = 0; w0 < batch; w0 += chunk) {
+    const int B = std::min(chunk, batch - w0);
+    const PsiGradPlan q = make_psi_grad_plan(m, B);
+    float* J = per_walker ? per_walker + (size_t)w0 * P : at<float>(ws, q.J);
+    // parameters without a term (the Jastrow when it is off) stay zero
+    QMC_CUDA(cudaMemsetAsync(J, 0, sizeof(float) * B * P, s));
+    const float* x = electrons + (size_t)w0 * n * 3;
+    QMC_TRY(psi_forward_save(m, q, ws, x, s));
+    QMC_TRY(psi_backward(m, q, ws, x, J, logpsi ? logpsi + w0 : nullptr, s));
     if (grad && weights) {
       ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
       k_weighted_sum<<<blocks(P), 256, 0, s>>>(B, P, J, weights + w0, grad);

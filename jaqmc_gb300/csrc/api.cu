@@ -874,6 +874,7 @@ size_t qmc_workspace_size(const qmc_model* m, int op, int batch) {
   if (!m || batch < 1) return 0;
   if (m->kind == QMC_KIND_PSIFORMER) {
     if (op == QMC_OP_LOCAL_ENERGY) return psi_fl_check(m) == QMC_OK ? psi_fl_plan(m, psi_fl_chunk(m, batch)).base.total : 0;
+    if (op == QMC_OP_GRAD) return psi_grad_workspace(m, batch);
     return op == QMC_OP_FORWARD || op == QMC_OP_MH ? psi_make_plan(m, batch).base.total : 0;
   }
   if (op == QMC_OP_GRAD) return grad_workspace(m, batch);
@@ -901,15 +902,19 @@ qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes) {
 qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                     double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
-  if (m->kind != QMC_KIND_FERMINET) {
-    set_error("the parameter adjoint is built for FermiNet models only");
-    return QMC_ERR_UNSUPPORTED;
-  }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1 || !electrons) { set_error("bad batch/electrons"); return QMC_ERR_ARG; }
   if (!per_walker && !grad) { set_error("nothing to compute: per_walker and grad are both null"); return QMC_ERR_ARG; }
   if (grad && !weights) { set_error("grad needs per-walker weights"); return QMC_ERR_ARG; }
   if (!ws) { set_error("null workspace"); return QMC_ERR_WORKSPACE; }
+  int dev;
+  QMC_CUDA(cudaGetDevice(&dev));
+  if (dev != m->device) {
+    set_error("model lives on device %d but device %d is current", m->device, dev);
+    return QMC_ERR_ARG;
+  }
+  if (m->kind == QMC_KIND_PSIFORMER)
+    return run_psi_grad(m, batch, electrons, weights, per_walker, grad, logpsi, ws, ws_bytes, s);
   return run_grad(m, batch, electrons, weights, per_walker, grad, logpsi, ws, ws_bytes, s);
 }
 

@@ -42,6 +42,10 @@ qmc_status run_logdet(qmc_model* m, const Plan& p, void* ws, const float* pe, fl
 size_t grad_workspace(const qmc_model* m, int batch);
 qmc_status run_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                     double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s);
+// Psiformer adjoint: workspace under the gradient budget and the chunked driver.
+size_t psi_grad_workspace(const qmc_model* m, int batch);
+qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
+                        double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s);
 // Layer taps of the adjoint (KFAC statistics): descriptors and the chunked run.
 int layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total);
 qmc_status run_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,

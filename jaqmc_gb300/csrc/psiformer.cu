@@ -280,6 +280,13 @@ __global__ void k_psi_add(int B, float* __restrict__ lp, const float* __restrict
 
 static size_t attention_smem(int n, int Dh) { return sizeof(float) * AttnShape(n, Dh).floats(); }
 
+cudaError_t launch_psi_features(cudaStream_t s, int B, int n, int n_up, int A, int K0p, const float* x,
+                                const float* atoms, const float* alpha, float* X0, float* rae, float* aevec,
+                                float* jas) {
+  k_psi_features<<<B, 256, sizeof(float) * 3 * n, s>>>(n, n_up, A, K0p, x, atoms, alpha, X0, rae, aevec, jas);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ host side
 PsiPlan psi_make_plan(const qmc_model* m, int B) {
   const PsiDims& d = m->psi->d;
@@ -602,10 +609,13 @@ qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
     }
     QMC_CUDA(launch_transpose_split(s, ar + a.w_qkv[l], D, 3 * D, 3 * D, ab + a.t_qkv[l], D, 3 * D));
     QMC_CUDA(launch_transpose_split(s, ar + P.o_k[l], D, D, D, ab + a.t_o[l], D, D));
+    QMC_CUDA(launch_transpose_f32(s, ar + a.w_qkv[l], D, 3 * D, 3 * D, ar + a.t32_qkv[l]));
+    QMC_CUDA(launch_transpose_f32(s, ar + P.o_k[l], D, D, D, ar + a.t32_o[l]));
     int din = D;
     for (int k = 0; k < d.n_dense; ++k) {
       QMC_CUDA(launch_transpose_split(s, ar + P.mlp_k[l][k], din, d.mlp[k], d.mlp[k], ab + a.t_mlp[l][k], din,
                                       d.mlp[k]));
+      QMC_CUDA(launch_transpose_f32(s, ar + P.mlp_k[l][k], din, d.mlp[k], d.mlp[k], ar + a.t32_mlp[l][k]));
       din = d.mlp[k];
     }
   }
@@ -625,6 +635,8 @@ qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
     }
     QMC_CUDA(launch_transpose_split(s, ar + oa.w_orb[c], D, m->d.norb, m->d.norb_p, ab + oa.t_orb[c], D,
                                     m->d.norb));
+    QMC_CUDA(cudaMemsetAsync(ar + oa.wt_orb[c], 0, sizeof(float) * m->d.norb_p * D, s));
+    QMC_CUDA(launch_transpose_f32(s, ar + oa.w_orb[c], D, m->d.norb, m->d.norb_p, ar + oa.wt_orb[c]));
   }
   m->params_set = true;
   return QMC_OK;
@@ -741,6 +753,13 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   for (int l = 0; l < d.L; ++l) {
     a.w_qkv[l] = takea((size_t)D * 3 * D);
     a.b_qkv[l] = takea((size_t)3 * D);
+    a.t32_qkv[l] = takea((size_t)3 * D * D);
+    a.t32_o[l] = takea((size_t)D * D);
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      a.t32_mlp[l][k] = takea((size_t)d.mlp[k] * din);
+      din = d.mlp[k];
+    }
   }
   // FermiNet-shared orbital / envelope fields of the model
   Dims& fd = m->d;
@@ -761,10 +780,12 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   for (int c = 0; c < 2; ++c) {
     if (c < nch) {
       fa.w_orb[c] = takea((size_t)D * fd.norb_p);
+      fa.wt_orb[c] = takea((size_t)fd.norb_p * D);
       fa.env_pi[c] = takea(env_pi_floats(env_kind, n, A, d.K));
       fa.env_sigma[c] = takea(env_sigma_floats(env_kind, n, A, d.K));
     } else {
       fa.w_orb[1] = fa.w_orb[0];
+      fa.wt_orb[1] = fa.wt_orb[0];
       fa.env_pi[1] = fa.env_pi[0];
       fa.env_sigma[1] = fa.env_sigma[0];
     }

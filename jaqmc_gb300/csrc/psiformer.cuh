@@ -38,6 +38,10 @@ struct PsiArena {
   size_t w_in;                    // [K0p][D] input kernel, zero rows past K0
   size_t w_qkv[kPsiMaxLayers];    // [D][3D]: query | key | value kernels side by side
   size_t b_qkv[kPsiMaxLayers];    // [3D]
+  // FP32 transposes for the adjoint's input-cotangent GEMMs
+  size_t t32_qkv[kPsiMaxLayers];  // [3D][D]
+  size_t t32_o[kPsiMaxLayers];    // [D][D]
+  size_t t32_mlp[kPsiMaxLayers][kPsiMaxMlp + 1];  // [dout][din]
   size_t total;
   size_t t_qkv[kPsiMaxLayers];    // [3D][D]
   size_t t_o[kPsiMaxLayers];      // [D][D]
@@ -91,5 +95,10 @@ bool psi_attention_fl_supported(int n, int Dh);
 qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* electrons, float* logpsi,
                         float* sign, uint8_t* flags, cudaStream_t s);
 qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s);
+// Value-pass features (log-rescaled ae features + spin column, rae, aevec) and
+// the SimpleEE Jastrow per walker (alpha == nullptr: no Jastrow).
+cudaError_t launch_psi_features(cudaStream_t s, int B, int n, int n_up, int A, int K0p, const float* x,
+                                const float* atoms, const float* alpha, float* X0, float* rae, float* aevec,
+                                float* jas);
 
 }  // namespace qmc
