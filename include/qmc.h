@@ -76,9 +76,9 @@ typedef struct {
 /* Psiformer with the SimpleEE Jastrow (PsiformerWavefunction,
  * src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94): Pre-LN layers,
  * biased attention projections and input layer, log-rescaled input features,
- * no orbital bias.  qmc_forward, qmc_mh_steps(_resident), qmc_mh_draws and the
- * forward-Laplacian qmc_local_energy (at most 42 electrons); qmc_grad returns
- * QMC_ERR_UNSUPPORTED. */
+ * no orbital bias.  qmc_forward, qmc_mh_steps(_resident), qmc_mh_draws, the
+ * forward-Laplacian qmc_local_energy (at most 42 electrons) and the FP32
+ * parameter adjoint qmc_grad (at most 64 electrons, head width <= 64). */
 typedef struct {
   int n_up, n_down, n_atoms;
   int ndets;                            /* K                                    */
@@ -223,7 +223,10 @@ qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
  *     e.g. weights = 2 (E_c,w - <E_c>) / batch for the VMC energy gradient;
  *   logpsi (batch, may be NULL).
  * Walkers are processed in chunks sized by the gradient budget; every chunk
- * recomputes its forward activations.  Workspace: qmc_workspace_size(m, QMC_OP_GRAD, batch). */
+ * recomputes its forward activations.  Workspace: qmc_workspace_size(m, QMC_OP_GRAD, batch).
+ * FermiNet and Psiformer models (for a Psiformer: the backward of the input
+ * Dense, LayerNorms, attention, tanh MLP, orbitals, envelope and Jastrow,
+ * src/jaqmc/app/molecule/wavefunction/psiformer.py:38-146). */
 qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                     double* grad, float* logpsi, void* workspace, size_t workspace_bytes, cudaStream_t stream);
 

@@ -404,7 +404,7 @@ class NativeFermiNet:
 class NativePsiformer(NativeFermiNet):
     """A ``qmc_model`` handle for a Psiformer (+ SimpleEE Jastrow): the value
     path (``forward``, ``mh_steps``, ``mh_steps_resident``, ``mh_draws``) and
-    the forward-Laplacian ``local_energy``; ``grad`` raises QMC_ERR_UNSUPPORTED."""
+    the forward-Laplacian ``local_energy`` and the FP32 parameter adjoint ``grad``."""
 
     def __init__(self, cfg, atoms, charges, precision="mixed", device=None):
         self._open(device)
