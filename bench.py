@@ -716,7 +716,8 @@ def run_ours(args, wl):
         grad = run_gradient(dev, max(1, args.steps // 2), 1, fd_walkers=0 if args.no_cpu else 2)
     serve = None
     if not args.no_serve:
-        serve = run_serving(dev, args.serve_rate, args.serve_jobs, args.serve_requests, slots=args.serve_slots)
+        serve = {"by_arrival_rate": [run_serving(dev, float(r), args.serve_jobs, args.serve_requests,
+                                                 slots=args.serve_slots) for r in args.serve_rates.split(",")]}
     cpu = None
     if rank == 0 and not args.no_cpu:
         r, cores, desc = cpu_request_rate(wl)
@@ -898,7 +899,8 @@ def main():
     ap.add_argument("--kernel-classes", action="store_true",
                     help="with --request-only: add one profiled pass and its per-class kernel times")
     ap.add_argument("--serve-only", action="store_true", help="print only the serving measurement")
-    ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrival rate (jobs/s)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrival rate (jobs/s) of --serve-only")
+    ap.add_argument("--serve-rates", default="10,40", help="arrival rates (jobs/s) of the serving leg")
     ap.add_argument("--serve-jobs", type=int, default=48)
     ap.add_argument("--serve-requests", type=int, default=2)
     ap.add_argument("--serve-slots", type=int, default=8)

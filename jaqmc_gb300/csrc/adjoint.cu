@@ -182,6 +182,76 @@ __global__ void k_jac_outer(int B, int R, int Rs, int row0, const float* __restr
   J[(size_t)w * P + off + (size_t)kx * N + c] = acc;
 }
 
+// The same Jacobian block with the walker's rows staged in shared memory:
+// one block per (walker, 32 columns of X); Z [R][N] and X [R][32] are read
+// from global memory once per block, and a thread forms 4 consecutive kx of
+// one output column c per pass (consecutive threads take consecutive c, so the
+// X float4 reads are broadcasts and the J stores are coalesced).
+constexpr int kJacKT = 32;
+__global__ void __launch_bounds__(256) k_jac_outer_tiled(int R, int Rs, int row0, const float* __restrict__ X, int ldx,
+                                                         int Kx, const float* __restrict__ Z, int ldz, int N,
+                                                         float* __restrict__ J, size_t P, size_t off) {
+  extern __shared__ __align__(16) float sj[];
+  const int w = blockIdx.x, kx0 = blockIdx.y * kJacKT;
+  const int kt = min(kJacKT, Kx - kx0);
+  float* Xs = sj;                   // [R][kJacKT]
+  float* Zs = sj + R * kJacKT;      // [R][N]
+  const size_t base = (size_t)w * Rs + row0;
+  for (int e = threadIdx.x; e < R * N; e += blockDim.x) {
+    const int r = e / N, c = e - r * N;
+    Zs[e] = Z[(base + r) * ldz + c];
+  }
+  for (int e = threadIdx.x; e < R * kJacKT; e += blockDim.x) {
+    const int r = e / kJacKT, k = e - r * kJacKT;
+    Xs[e] = k < kt ? X[(base + r) * ldx + kx0 + k] : 0.f;
+  }
+  __syncthreads();
+  float* Jw = J + (size_t)w * P + off;
+  const int pairs = (kJacKT / 4) * N;
+  for (int p = threadIdx.x; p < pairs; p += blockDim.x) {
+    const int kq = p / N, c = p - kq * N;
+    if (4 * kq >= kt) continue;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    for (int r = 0; r < R; ++r) {
+      const float z = Zs[r * N + c];
+      const float4 x = *reinterpret_cast<const float4*>(Xs + r * kJacKT + 4 * kq);
+      a0 = fmaf(x.x, z, a0);
+      a1 = fmaf(x.y, z, a1);
+      a2 = fmaf(x.z, z, a2);
+      a3 = fmaf(x.w, z, a3);
+    }
+    const int k = kx0 + 4 * kq;
+    Jw[(size_t)k * N + c] = a0;
+    if (4 * kq + 1 < kt) Jw[(size_t)(k + 1) * N + c] = a1;
+    if (4 * kq + 2 < kt) Jw[(size_t)(k + 2) * N + c] = a2;
+    if (4 * kq + 3 < kt) Jw[(size_t)(k + 3) * N + c] = a3;
+  }
+}
+
+// J[w][off + kx N + c] = sum_r X[..][kx] Z[..][c]: the staged kernel when a
+// walker's rows fit in shared memory, else the plain one.
+static cudaError_t jac_outer(cudaStream_t s, int B, int R, int Rs, int row0, const float* X, int ldx, int Kx,
+                             const float* Z, int ldz, int N, float* J, size_t P, size_t off) {
+  const size_t sm = sizeof(float) * (size_t)R * (kJacKT + N);
+  if (sm <= 160 * 1024) {
+    int dev;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    static int set_dev = -1;
+    if (set_dev != dev) {
+      e = cudaFuncSetAttribute(k_jac_outer_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+      if (e != cudaSuccess) return e;
+      set_dev = dev;
+    }
+    k_jac_outer_tiled<<<dim3((unsigned)B, (unsigned)((Kx + kJacKT - 1) / kJacKT)), 256, sm, s>>>(
+        R, Rs, row0, X, ldx, Kx, Z, ldz, N, J, P, off);
+    return cudaGetLastError();
+  }
+  const size_t total = (size_t)B * Kx * N;
+  k_jac_outer<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, R, Rs, row0, X, ldx, Kx, Z, ldz, N, J, P, off);
+  return cudaGetLastError();
+}
+
 // per-walker column sums Zs[w][c] = sum_{r<R} Z[w*R + r][c]; optionally also
 // written as Jacobian rows (bias gradients)
 __global__ void k_colsum(int B, int R, const float* __restrict__ Z, int ldz, int N, float* __restrict__ Zs,
@@ -508,10 +578,9 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
                                                                    ar + a.env_pi[c], ar + a.env_sigma[c], J, P,
                                                                    pl.env_pi[c], pl.env_sigma[c]);
       QMC_CUDA(cudaGetLastError());
-      k_jac_outer<<<blocks((size_t)B * d.d_last * d.norb), 256, 0, s>>>(
+      QMC_CUDA(jac_outer(s,
           B, ns, n, i0, at<float>(ws, p.h1[d.L - 1]), d.d_last, d.d_last, at<float>(ws, p.orbbar), d.norb_p, d.norb, J,
-          P, pl.orb_k[c]);
-      QMC_CUDA(cudaGetLastError());
+          P, pl.orb_k[c]));
     }
     if (taps) {  // orbital projection of channel c: inputs h1[L-1] and cotangents orbbar, its rows only
       int k = 0;
@@ -552,18 +621,15 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
         QMC_CUDA(cudaMemcpyAsync(taps->out(k), zbar, sizeof(float) * rows * dout, cudaMemcpyDeviceToDevice, s));
       }
       const size_t k0 = pl.dense1_k[l];
-      k_jac_outer<<<blocks((size_t)B * din * dout), 256, 0, s>>>(B, n, n, 0, in, dinp, din, zbar, dout, dout, J, P, k0);
-      QMC_CUDA(cudaGetLastError());
-      k_jac_outer<<<blocks((size_t)B * d.C * d.d2_in[l] * dout), 256, 0, s>>>(
+      QMC_CUDA(jac_outer(s, B, n, n, 0, in, dinp, din, zbar, dout, dout, J, P, k0));
+      QMC_CUDA(jac_outer(s,
           B, n, n, 0, at<float>(ws, p.G2[l]), d.g2_p[l], d.C * d.d2_in[l], zbar, dout, dout, J, P,
-          k0 + (size_t)(din + d.C * din) * dout);
-      QMC_CUDA(cudaGetLastError());
+          k0 + (size_t)(din + d.C * din) * dout));
       k_colsum<<<blocks((size_t)B * dout), 256, 0, s>>>(B, n, zbar, dout, dout, zsum, J, P, pl.dense1_b[l]);
       QMC_CUDA(cudaGetLastError());
-      k_jac_outer<<<blocks((size_t)B * d.C * din * dout), 256, 0, s>>>(B, 1, 1, 0, at<float>(ws, p.g1m[l]), d.g1_p[l],
+      QMC_CUDA(jac_outer(s, B, 1, 1, 0, at<float>(ws, p.g1m[l]), d.g1_p[l],
                                                                       d.C * din, zsum, dout, dout, J, P,
-                                                                      k0 + (size_t)din * dout);
-      QMC_CUDA(cudaGetLastError());
+                                                                      k0 + (size_t)din * dout));
     }
     float* tmp = at<float>(ws, p.tmp);
     const int kmain = dinp + d.g2_p[l];
@@ -597,10 +663,9 @@ static qmc_status backward(qmc_model* m, const GradPlan& p, void* ws, float* J, 
                                    cudaMemcpyDeviceToDevice, s));
           QMC_CUDA(cudaMemcpyAsync(taps->out(k), z2, sizeof(float) * pairs * d.d2[l], cudaMemcpyDeviceToDevice, s));
         }
-        k_jac_outer<<<blocks((size_t)B * d.d2_in[l] * d.d2[l]), 256, 0, s>>>(
+        QMC_CUDA(jac_outer(s,
             B, n * n, n * n, 0, at<float>(ws, p.h2[l]), d.d2_in[l], d.d2_in[l], z2, d.d2[l], d.d2[l], J, P,
-            pl.dense2_k[l]);
-        QMC_CUDA(cudaGetLastError());
+            pl.dense2_k[l]));
         k_colsum<<<blocks((size_t)B * d.d2[l]), 256, 0, s>>>(B, n * n, z2, d.d2[l], d.d2[l], nullptr, J, P,
                                                              pl.dense2_b[l]);
         QMC_CUDA(cudaGetLastError());
@@ -1102,10 +1167,9 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
                                                                    ar + fa.env_pi[c], ar + fa.env_sigma[c], J, Pn,
                                                                    P.env_pi[c], P.env_sigma[c]);
     QMC_CUDA(cudaGetLastError());
-    k_jac_outer<<<blocks((size_t)B * D * fd.norb), 256, 0, s>>>(B, ns, n, i0, at<float>(ws, p.h[d.L]), D, D,
+    QMC_CUDA(jac_outer(s, B, ns, n, i0, at<float>(ws, p.h[d.L]), D, D,
                                                               at<float>(ws, p.orbbar), fd.norb_p, fd.norb, J, Pn,
-                                                              P.orb_k[c]);
-    QMC_CUDA(cudaGetLastError());
+                                                              P.orb_k[c]));
     RowMap map{ns, i0, n, 1};
     QMC_CUDA(launch_gemm_simt(s, B * ns, map, at<float>(ws, p.orbbar), fd.norb_p, fd.norb_p, nullptr, 0, 0,
                               ar + fa.wt_orb[c], D, D, EpiStore{hbar, D, nullptr}));
@@ -1125,9 +1189,8 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
       ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
       k_tanh_bwd<<<blocks(rows * dout), 256, 0, s>>>(rows * dout, 1.f, ybar, at<float>(ws, p.y[l][k]), zbar);
       QMC_CUDA(cudaGetLastError());
-      k_jac_outer<<<blocks((size_t)B * din * dout), 256, 0, s>>>(B, n, n, 0, x, din, din, zbar, dout, dout, J, Pn,
-                                                                P.mlp_k[l][k]);
-      QMC_CUDA(cudaGetLastError());
+      QMC_CUDA(jac_outer(s, B, n, n, 0, x, din, din, zbar, dout, dout, J, Pn,
+                                                                P.mlp_k[l][k]));
       k_colsum<<<blocks((size_t)B * dout), 256, 0, s>>>(B, n, zbar, dout, dout, nullptr, J, Pn, P.mlp_b[l][k]);
       QMC_CUDA(cudaGetLastError());
       // input cotangent zbar W^T into tmp (the next k's ybar, or the LayerNorm output's)
@@ -1148,9 +1211,8 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
     {
       // att = o Wo + bo; hm = h + att
       ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
-      k_jac_outer<<<blocks((size_t)B * D * D), 256, 0, s>>>(B, n, n, 0, at<float>(ws, p.o[l]), D, D, hmbar, D, D, J,
-                                                            Pn, P.o_k[l]);
-      QMC_CUDA(cudaGetLastError());
+      QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.o[l]), D, D, hmbar, D, D, J,
+                                                            Pn, P.o_k[l]));
       k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hmbar, D, D, nullptr, J, Pn, P.o_b[l]);
       QMC_CUDA(cudaGetLastError());
       QMC_CUDA(launch_gemm_simt(s, B * n, rmap, hmbar, D, D, nullptr, 0, 0, ar + a.t32_o[l], D, D,
@@ -1168,9 +1230,8 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
       const float* xn0 = at<float>(ws, p.xn0[l]);
       const size_t kofs[3] = {P.q_k[l], P.k_k[l], P.v_k[l]}, bofs[3] = {P.q_b[l], P.k_b[l], P.v_b[l]};
       for (int c = 0; c < 3; ++c) {
-        k_jac_outer<<<blocks((size_t)B * D * D), 256, 0, s>>>(B, n, n, 0, xn0, D, D, qkvbar + (size_t)c * D, 3 * D, D,
-                                                              J, Pn, kofs[c]);
-        QMC_CUDA(cudaGetLastError());
+        QMC_CUDA(jac_outer(s, B, n, n, 0, xn0, D, D, qkvbar + (size_t)c * D, 3 * D, D,
+                                                              J, Pn, kofs[c]));
         k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, qkvbar + (size_t)c * D, 3 * D, D, nullptr, J, Pn,
                                                        bofs[c]);
         QMC_CUDA(cudaGetLastError());
@@ -1192,9 +1253,8 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
   }
   {
     ::qmc::ProfScope ps_(QMC_KC_LAYER0, s);
-    k_jac_outer<<<blocks((size_t)B * d.K0 * D), 256, 0, s>>>(B, n, n, 0, at<float>(ws, p.x0), d.K0p, d.K0, hbar, D, D,
-                                                             J, Pn, P.in_k);
-    QMC_CUDA(cudaGetLastError());
+    QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.x0), d.K0p, d.K0, hbar, D, D,
+                                                             J, Pn, P.in_k));
     k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hbar, D, D, nullptr, J, Pn, P.in_b);
     QMC_CUDA(cudaGetLastError());
     if (d.jastrow) {

@@ -1241,6 +1241,7 @@ struct DetOut {
   double ld;
   float sgn;
   float tL, t2, q;
+  double kin;  // tL - t2 + q, formed in the precision the traces were computed in
   int refactor, singular;
 };
 
@@ -1553,25 +1554,129 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, 
   if constexpr (sizeof(S) == 4 && NMAX <= 16) {
     det_tangents_f32<NMAX>(reinterpret_cast<const float*>(Ainv), Ak, n, T, ts, rs, ld, ldm,
                            reinterpret_cast<float*>(Ms), t1s, o);
+    o.kin = (double)o.tL - (double)o.t2 + (double)o.q;
     return o;
   }
-  float t2acc = 0.f, qacc = 0.f;
+  S tl = (S)0, t2acc = (S)0, qacc = (S)0;
   for (int t = 1; t < T; ++t) {
     const float* At = Ak + (size_t)t * ts;
     S tr;
     if constexpr (sizeof(S) == 4) tr = warp_product_f32<NMAX>(Ainv, At, Ms, n, ld, ldm, rs);
     else tr = warp_product_f64(Ainv, At, Ms, Xs, n, ld, ldm, rs);
     if (t == 1) {
-      o.tL = (float)tr;
+      tl = tr;
     } else {
       S t2 = warp_trace_sq<S>(Ms, n, ldm);
       if (lane == 0) t1s[t - 2] = (float)tr;
-      t2acc += (float)t2;
-      qacc += (float)(tr * tr);
+      t2acc += t2;
+      qacc += tr * tr;
     }
   }
-  o.t2 = t2acc;
-  o.q = qacc;
+  o.tL = (float)tl;
+  o.t2 = (float)t2acc;
+  o.q = (float)qacc;
+  o.kin = (double)tl - (double)t2acc + (double)qacc;
+  return o;
+}
+
+// The tangent traces of one determinant with the products in double-float
+// arithmetic (the determinant guard's re-evaluation; FP64 runs at about 1/64
+// of the FP32 rate on this part).  LU and inverse in FP64; A^-1 split into
+// hi + lo floats; each entry of M_d = A^-1 J_d (J_d exact in FP32) summed as
+// s + c with TwoProduct (p = a x, e = fma(a, x, -p)) and TwoSum error-free
+// transformations (Ogita, Rump & Oishi, "Accurate sum and dot product", SIAM
+// J. Sci. Comput. 26, 2005), so an entry errs by ~n eps32^2 relative to
+// sum |A^-1| |J| instead of n eps32; the traces tr M, tr M^2, tr(A^-1 L) and
+// their combination tL - t2 + q are then accumulated in FP64.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+template <int NMAX>
+__device__ DetOut det_stage_df(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, char* scratch,
+                               float* t1s) {
+  const int lane = threadIdx.x & 31;
+  const DetScratch sc(n);
+  const int ld = sc.ld, ldm = sc.ldm;
+  double* LU = reinterpret_cast<double*>(scratch);
+  double* Ai = LU + n * ld;
+  float* Mh = reinterpret_cast<float*>(Ai + n * ld);  // [n][ldm]
+  float* Ml = Mh + n * ldm;                            // [n][ldm] (both inside the 2 n ldm doubles)
+  int* perm = reinterpret_cast<int*>(scratch + (size_t)(2 * n * ld + 2 * n * ldm) * 8);
+  DetOut o{};
+  for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (double)Ak[(e / n) * rs + (e % n)];
+  __syncwarp();
+  double growth;
+  warp_lu<double>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular);
+  o.refactor = 1;
+  if (o.singular || T <= 1) return o;
+  warp_inverse<double>(LU, Ai, perm, n, ld);
+  float* Ah = reinterpret_cast<float*>(LU);  // the factors are no longer needed
+  float* Al = Ah + n * ld;
+  for (int e = lane; e < n * ld; e += 32) {
+    const double v = Ai[e];
+    const float hv = (float)v;
+    Ah[e] = hv;
+    Al[e] = (float)(v - (double)hv);
+  }
+  __syncwarp();
+  double tl = 0.0;
+  {
+    const float* L = Ak + ts;
+    for (int e = lane; e < n * n; e += 32) {
+      const int m = e / n, i = e - m * n;
+      tl = fma(Ai[i * ld + m], (double)L[m * rs + i], tl);
+    }
+    tl = warp_sum(tl);
+  }
+  double t2acc = 0.0, qacc = 0.0;
+  for (int t = 2; t < T; ++t) {
+    const float* J = Ak + (size_t)t * ts;
+    double tr = 0.0;
+    for (int j = lane; j < n; j += 32) {
+      float x[NMAX];
+#pragma unroll
+      for (int m = 0; m < NMAX; ++m) x[m] = m < n ? J[m * rs + j] : 0.f;
+      for (int i = 0; i < n; ++i) {
+        float sh = 0.f, sl = 0.f;
+#pragma unroll
+        for (int m = 0; m < NMAX; ++m) {
+          if (m < n) {
+            const float a = Ah[i * ld + m];
+            const float p = a * x[m];
+            const float pe = fmaf(a, x[m], -p);
+            float s2, se;
+            two_sum(sh, p, s2, se);
+            sh = s2;
+            sl += se + fmaf(Al[i * ld + m], x[m], pe);
+          }
+        }
+        const float hv = sh + sl;
+        const float lv = sl - (hv - sh);
+        Mh[i * ldm + j] = hv;
+        Ml[i * ldm + j] = lv;
+        if (i == j) tr += (double)hv + (double)lv;
+      }
+    }
+    tr = warp_sum(tr);
+    __syncwarp();
+    double t2 = 0.0;
+    for (int j = lane; j < n; j += 32)
+      for (int i = 0; i < n; ++i)
+        t2 = fma((double)Mh[i * ldm + j] + (double)Ml[i * ldm + j], (double)Mh[j * ldm + i] + (double)Ml[j * ldm + i],
+                 t2);
+    t2 = warp_sum(t2);
+    __syncwarp();
+    if (lane == 0) t1s[t - 2] = (float)tr;
+    t2acc += t2;
+    qacc = fma(tr, tr, qacc);
+  }
+  o.tL = (float)tl;
+  o.t2 = (float)t2acc;
+  o.q = (float)qacc;
+  o.kin = tl - t2acc + qacc;
   return o;
 }
 
@@ -1579,8 +1684,9 @@ __device__ DetOut det_stage(const float* __restrict__ Ak, int n, int T, int rs, 
 // determinants and, for T > 1, the gradient, Laplacian and kinetic energy
 // from the per-determinant traces (lds / sgs / tLs / t2s / qs / t1s in shared
 // memory; ints = {any refactored, any singular}).
-__device__ void logdet_finish(int w, int K, int T, double* lds, float* sgs, float* tLs, const float* t2s,
-                              const float* qs, const float* t1s, const int* ints, const float* __restrict__ pe,
+__device__ void logdet_finish(int w, int K, int T, double* lds, const double* kins, float* sgs, float* tLs,
+                              const float* t2s, const float* qs, const float* t1s, const int* ints,
+                              const float* __restrict__ pe,
                               float* __restrict__ logpsi, float* __restrict__ sign, float* __restrict__ ke,
                               float* __restrict__ el, uint8_t* __restrict__ flags, int* __restrict__ n_refactor,
                               const float* __restrict__ gl_add) {
@@ -1603,7 +1709,7 @@ __device__ void logdet_finish(int w, int K, int T, double* lds, float* sgs, floa
     float* wk = tLs;  // reuse: tL_k is folded into the per-det term below
     for (int k = lane; k < K; k += 32) {
       const double wt = sgs[k] != 0.f ? (double)sgs[k] * exp(lds[k] - lmax) / Ssum : 0.0;
-      lds[k] = wt * ((double)tLs[k] - (double)t2s[k] + (double)qs[k]);
+      lds[k] = wt * kins[k];
       wk[k] = (float)wt;
     }
     __syncwarp();
@@ -1655,7 +1761,8 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   const int D = T > 1 ? T - 2 : 0;
   // shared layout: per-det results, then per-warp scratch
   double* lds = shd;                                    // [K]
-  float* sgs = reinterpret_cast<float*>(lds + K);       // [K]
+  double* kins = lds + K;                               // [K] tL - t2 + q
+  float* sgs = reinterpret_cast<float*>(kins + K);      // [K]
   float* tLs = sgs + K;                                 // [K]
   float* t2s = tLs + K;                                 // [K]
   float* qs = t2s + K;                                  // [K]
@@ -1663,7 +1770,7 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);  // flags [2]
   float* wts = reinterpret_cast<float*>(ints + 2);          // [K] determinant weights
   int* done64 = reinterpret_cast<int*>(wts + K);            // [K] already evaluated in FP64
-  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8), 16);
+  const size_t head = align_up((size_t)(2 * K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8), 16);
   const DetScratch sc(n);
   char* scratch = reinterpret_cast<char*>(shd) + head + sc.bytes * warp;
   if (threadIdx.x < 2) ints[threadIdx.x] = 0;
@@ -1680,6 +1787,7 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
     }
     if (lane == 0) {
       lds[k] = o.ld;
+      kins[k] = o.singular ? 0.0 : o.kin;
       sgs[k] = o.singular ? 0.f : o.sgn;
       tLs[k] = o.tL;
       t2s[k] = o.t2;
@@ -1692,16 +1800,18 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   }
   __syncthreads();
   if (cancel && T > 1) {
-    // determinants whose FP32 kinetic term cancels too much: FP64 again
+    // determinants whose FP32 kinetic term cancels too much: again, with the
+    // products in double-float and the traces in FP64
     if (warp == 0) det_weights(K, lds, sgs, wts);
     __syncthreads();
     for (int k = warp; k < K; k += nw) {
       if (sgs[k] == 0.f || done64[k] || !cancel_marks(wts[k], tLs[k], t2s[k], qs[k])) continue;
       const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
-      DetOut o = det_stage<double, NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K), scratch,
-                                         t1s + (size_t)k * D, true);
+      DetOut o = det_stage_df<NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K), scratch,
+                                    t1s + (size_t)k * D);
       if (lane == 0) {
         lds[k] = o.ld;
+        kins[k] = o.singular ? 0.0 : o.kin;
         sgs[k] = o.singular ? 0.f : o.sgn;
         tLs[k] = o.singular ? 0.f : o.tL;
         t2s[k] = o.singular ? 0.f : o.t2;
@@ -1716,7 +1826,8 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
     __syncthreads();
   }
   if (warp != 0) return;
-  logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, n_refactor, gl_add);
+  logdet_finish(w, K, T, lds, kins, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, n_refactor,
+                gl_add);
 }
 
 // Tangent determinant stage for 16 < n <= 64: three launches.
@@ -1742,20 +1853,23 @@ struct WideShape {
   __host__ __device__ WideShape(int n, int K, int D, int nw) {
     ld = (n + 3) / 4 * 4;
     ldm = (n % 2 == 0) ? n + 1 : n + 2;
-    // ... ints[4], then red: [nw][3] partial traces, later [K] weights
-    head = align_up((size_t)K * 8 + (size_t)4 * K * 4 + (size_t)K * D * 4 + 16 + (size_t)(3 * nw > K ? 3 * nw : K) * 4,
+    // lds[K], kins[K] (double), sgs, tLs, t2s, qs [K], t1s [K][D], ints[4], then
+    // red: [nw][3] partial traces, later [K] weights
+    head = align_up((size_t)2 * K * 8 + (size_t)4 * K * 4 + (size_t)K * D * 4 + 16 +
+                        (size_t)(3 * nw > K ? 3 * nw : K) * 4,
                     16);
     bytes = head + (size_t)2 * n * ld * 4 + align_up((size_t)n * 4, 16) + (size_t)nw * n * ldm * 4;
   }
 };
 
 // Per-walker record of the determinant results (global scratch):
-// ld[K] (double), sg[K], tL[K], t2[K], q[K], t1[K][D] (float), mark[K] (byte),
-// any-singular (int).
+// ld[K], kin[K] (double), sg[K], tL[K], t2[K], q[K], t1[K][D] (float),
+// mark[K] (byte), any-singular (int).
 struct DetRecord {
-  size_t sg, tL, t2, q, t1, mark, sing, bytes;
+  size_t kin, sg, tL, t2, q, t1, mark, sing, bytes;
   __host__ __device__ DetRecord(int K, int D) {
-    sg = (size_t)K * 8;
+    kin = (size_t)K * 8;
+    sg = kin + (size_t)K * 8;
     tL = sg + (size_t)K * 4;
     t2 = tL + (size_t)K * 4;
     q = t2 + (size_t)K * 4;
@@ -1787,7 +1901,8 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
   char* rw = records + (size_t)w * rec.bytes;
   const int ld = sh.ld, ldm = sh.ldm;
   double* lds = shd;                                         // [K]
-  float* sgs = reinterpret_cast<float*>(lds + K);            // [K]
+  double* kins = lds + K;                                    // [K] tL - t2 + q
+  float* sgs = reinterpret_cast<float*>(kins + K);           // [K]
   float* tLs = sgs + K;                                      // [K]
   float* t2s = tLs + K;                                      // [K]
   float* qs = t2s + K;                                       // [K]
@@ -1826,7 +1941,10 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
     __syncthreads();
     if (ints[2]) {  // singular (zero weight) or marked (recomputed in FP64)
       for (int d = threadIdx.x; d < D; d += blockDim.x) t1s[(size_t)k * D + d] = 0.f;
-      if (threadIdx.x == 0) tLs[k] = t2s[k] = qs[k] = 0.f;
+      if (threadIdx.x == 0) {
+        tLs[k] = t2s[k] = qs[k] = 0.f;
+        kins[k] = 0.0;
+      }
       continue;
     }
     float tl = 0.f;
@@ -1862,6 +1980,7 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
       tLs[k] = a;
       t2s[k] = b;
       qs[k] = c;
+      kins[k] = (double)a - (double)b + (double)c;
     }
   }
   __syncthreads();
@@ -1884,6 +2003,7 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
   if (threadIdx.x == 0) redo[w] = ints[0] ? 1 : 0;
   if (ints[0]) {  // leave the record for the FP64 pass
     double* rld = reinterpret_cast<double*>(rw);
+    double* rkin = reinterpret_cast<double*>(rw + rec.kin);
     float* rsg = reinterpret_cast<float*>(rw + rec.sg);
     float* rtL = reinterpret_cast<float*>(rw + rec.tL);
     float* rt2 = reinterpret_cast<float*>(rw + rec.t2);
@@ -1891,6 +2011,7 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
     float* rt1 = reinterpret_cast<float*>(rw + rec.t1);
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
       rld[k] = lds[k];
+      rkin[k] = kins[k];
       rsg[k] = sgs[k];
       rtL[k] = tLs[k];
       rt2[k] = t2s[k];
@@ -1901,7 +2022,7 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
     return;
   }
   if (warp != 0) return;
-  logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
+  logdet_finish(w, K, T, lds, kins, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
 }
 
 template <int NMAX>
@@ -1916,10 +2037,11 @@ __global__ void __launch_bounds__(32) k_logdet_fl_det64(int n, int K, int Tp, in
   if (!reinterpret_cast<const uint8_t*>(rw + rec.mark)[k]) return;
   const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
   float* t1k = reinterpret_cast<float*>(rw + rec.t1) + (size_t)k * D;
-  const DetOut o = det_stage<double, NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K),
-                                           reinterpret_cast<char*>(shd), t1k, true);
+  const DetOut o = det_stage_df<NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K),
+                                      reinterpret_cast<char*>(shd), t1k);
   if ((threadIdx.x & 31) == 0) {
     reinterpret_cast<double*>(rw)[k] = o.ld;
+    reinterpret_cast<double*>(rw + rec.kin)[k] = o.singular ? 0.0 : o.kin;
     reinterpret_cast<float*>(rw + rec.sg)[k] = o.singular ? 0.f : o.sgn;
     reinterpret_cast<float*>(rw + rec.tL)[k] = o.singular ? 0.f : o.tL;
     reinterpret_cast<float*>(rw + rec.t2)[k] = o.singular ? 0.f : o.t2;
@@ -1944,7 +2066,8 @@ __global__ void __launch_bounds__(32) k_logdet_fl_finish(int K, int T, const uin
   const DetRecord rec(K, D);
   const char* rw = records + (size_t)w * rec.bytes;
   double* lds = shd;
-  float* sgs = reinterpret_cast<float*>(lds + K);
+  double* kins = lds + K;
+  float* sgs = reinterpret_cast<float*>(kins + K);
   float* tLs = sgs + K;
   float* t2s = tLs + K;
   float* qs = t2s + K;
@@ -1952,6 +2075,7 @@ __global__ void __launch_bounds__(32) k_logdet_fl_finish(int K, int T, const uin
   int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     lds[k] = reinterpret_cast<const double*>(rw)[k];
+    kins[k] = reinterpret_cast<const double*>(rw + rec.kin)[k];
     sgs[k] = reinterpret_cast<const float*>(rw + rec.sg)[k];
     tLs[k] = reinterpret_cast<const float*>(rw + rec.tL)[k];
     t2s[k] = reinterpret_cast<const float*>(rw + rec.t2)[k];
@@ -1963,7 +2087,7 @@ __global__ void __launch_bounds__(32) k_logdet_fl_finish(int K, int T, const uin
     ints[1] = *reinterpret_cast<const int*>(rw + rec.sing);
   }
   __syncwarp();
-  logdet_finish(w, K, T, lds, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
+  logdet_finish(w, K, T, lds, kins, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
 }
 
 // Value-only determinant stage (MH passes): LU in registers.  A segment of
@@ -2266,7 +2390,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
     const int nw = 8;
     const WideShape sh(n, K, T - 2, nw);
     const DetScratch sc(n);
-    const size_t fin = (size_t)K * 8 + (size_t)4 * K * 4 + (size_t)K * (T - 2) * 4 + 16;
+    const size_t fin = (size_t)2 * K * 8 + (size_t)4 * K * 4 + (size_t)K * (T - 2) * 4 + 16;
     if (sh.bytes <= 110 * 1024 && sc.bytes <= 110 * 1024 && fin <= 110 * 1024) {
       uint8_t* redo = static_cast<uint8_t*>(fl_scratch);
       char* records = static_cast<char*>(fl_scratch) + align_up((size_t)B, 16);

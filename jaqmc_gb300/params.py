@@ -288,3 +288,99 @@ def init_psiformer(cfg: PsiformerConfig, n_atoms: int, seed: int = 0):
             v = np.zeros(shape, np.float32)
         _set(tree, path, v)
     return tree
+
+
+# ------------------------------------------------------------------ LapNet
+@dataclass
+class LapNetConfig:
+    """Hyper-parameters of ``LapNetWavefunction``
+    (src/jaqmc/app/molecule/wavefunction/lapnet.py:27-75): same names and
+    defaults (no LayerNorm, biases on, two local updates of the individual
+    stream, abs_isotropic envelope, spin-split orbitals, SimpleEE Jastrow,
+    log-rescaled input features)."""
+
+    nspins: tuple = (1, 1)
+    ndets: int = 16
+    num_layers: int = 4
+    num_heads: int = 4
+    heads_dim: int = 64
+    use_layernorm: bool = False
+    jastrow: str = "simple_ee"
+    use_input_bias: bool = True
+    use_backbone_bias: bool = True
+    num_local_updates: int = 2
+    envelope: str = "abs_isotropic"
+    use_orbital_bias: bool = False
+    rescale: bool = True
+    jastrow_alpha_init: float = 1.0
+    full_det: bool = True
+    orbitals_spin_split: bool = True
+
+    @property
+    def n(self) -> int:
+        return int(sum(self.nspins))
+
+    @property
+    def dim(self) -> int:
+        return self.num_heads * self.heads_dim
+
+    @property
+    def split(self) -> bool:
+        return bool(self.nspins[0] > 0 and self.nspins[1] > 0)
+
+
+def lapnet_leaves(cfg: LapNetConfig, n_atoms: int):
+    """``[(path, shape)]`` in C-ABI order: the input projection, per layer the
+    query/key, value, output and value-update projections and the local
+    updates of the individual stream (``src/jaqmc/wavefunction/backbone/
+    lapnet/_backbone.py:39-66``), orbitals, envelope, Jastrow."""
+    if cfg.use_layernorm:
+        raise NotImplementedError("LapNet with use_layernorm=True is not supported")
+    n, K, D = cfg.n, cfg.ndets, cfg.dim
+    bb = ("backbone_layer",)
+    out = [(bb + ("input_projection", "kernel"), (4 * n_atoms + 1, D))]
+    if cfg.use_input_bias:
+        out.append((bb + ("input_projection", "bias"), (D,)))
+
+    def dense(base, name, din, dout):
+        out.append((base + (name, "kernel"), (din, dout)))
+        if cfg.use_backbone_bias:
+            out.append((base + (name, "bias"), (dout,)))
+    for l in range(cfg.num_layers):
+        base = bb + (f"layers_{l}",)
+        dense(base, "qk_projection", D, 2 * D)
+        dense(base, "value_projection", D, D)
+        dense(base, "output_projection", D, D)
+        dense(base, "value_update", D, D)
+        for j in range(cfg.num_local_updates if l < cfg.num_layers - 1 else 0):
+            dense(base, f"qk_update_layers_{j}", D, D)
+    if cfg.split:
+        for s in range(2):
+            out.append((("orbital_layer", "SplitChannelDense_0", f"DenseGeneral_{s}", "kernel"), (D, K, n)))
+    else:
+        out.append((("orbital_layer", "DenseGeneral_0", "kernel"), (D, K, n)))
+    out += envelope_leaves(cfg.envelope, cfg.split, n, n_atoms, K)
+    if cfg.jastrow == "simple_ee":
+        out.append((("jastrow_layer", "alpha_par"), (1,)))
+        out.append((("jastrow_layer", "alpha_anti"), (1,)))
+    return out
+
+
+def init_lapnet(cfg: LapNetConfig, n_atoms: int, seed: int = 0):
+    """A Flax-shaped parameter tree: fan-in-scaled N(0, 1/fan_in) kernels,
+    backbone biases N(0, 1) (the reference's bias initialiser,
+    _backbone.py:42-66), envelope ones, Jastrow alphas at jastrow_alpha_init."""
+    rng = np.random.default_rng(seed)
+    tree = {}
+    for path, shape in lapnet_leaves(cfg, n_atoms):
+        name = path[-1]
+        if name == "kernel":
+            v = (rng.standard_normal(shape) / np.sqrt(shape[0])).astype(np.float32)
+        elif name == "bias":
+            v = rng.standard_normal(shape).astype(np.float32)
+        elif name in ("pi", "sigma"):
+            v = np.ones(shape, np.float32)
+        else:
+            v = np.full(shape, cfg.jastrow_alpha_init, np.float32)
+        _set(tree, path, v)
+    return tree
