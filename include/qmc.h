@@ -92,6 +92,30 @@ typedef struct {
   int precision;                        /* QMC_PRECISION_*                      */
 } qmc_psiformer_config;
 
+/* LapNet with the SimpleEE Jastrow (LapNetWavefunction,
+ * src/jaqmc/app/molecule/wavefunction/lapnet.py:27-140; backbone
+ * src/jaqmc/wavefunction/backbone/lapnet/_backbone.py:15-250): an individual
+ * stream giving queries and keys and taking num_local_updates tanh updates
+ * per layer (none in the last), a dense stream giving values and taking the
+ * attention and value-update residuals, log-rescaled input features, spin-
+ * split orbitals.  use_layernorm is not supported.  qmc_forward,
+ * qmc_mh_steps(_resident), qmc_mh_draws, qmc_ecp_energy and the forward-
+ * Laplacian qmc_local_energy (at most 42 electrons); no parameter adjoint. */
+typedef struct {
+  int n_up, n_down, n_atoms;
+  int ndets;                            /* K                                    */
+  int n_layers;                         /* num_layers, <= 8                     */
+  int n_heads, head_dim;                /* num_heads, heads_dim                 */
+  int num_local_updates;                /* <= 4                                 */
+  int use_input_bias;                   /* 0/1                                  */
+  int use_backbone_bias;                /* 0/1                                  */
+  int envelope;                         /* QMC_ENVELOPE_*                       */
+  int orbitals_spin_split;              /* 0/1                                  */
+  int jastrow;                          /* 0 none, 1 SimpleEE                   */
+  int precision;                        /* QMC_PRECISION_*                      */
+} qmc_lapnet_config;
+
+/* Model kinds: FermiNet, and the attention backbones (Psiformer, LapNet). */
 enum { QMC_KIND_FERMINET = 0, QMC_KIND_PSIFORMER = 1 };
 
 typedef struct qmc_model qmc_model;
@@ -113,6 +137,16 @@ qmc_status qmc_ferminet_create(const qmc_ferminet_config* cfg, const float* atom
  * (src/jaqmc/app/molecule/workflow.py:119-136). */
 qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, const float* atoms_host,
                                 const float* charges_host, qmc_model** out);
+/* Create a LapNet model on the current device (see qmc_lapnet_config).
+ * Replaces the construction of LapNetWavefunction + its wiring
+ * (src/jaqmc/app/molecule/workflow.py:119-136).  The flat parameter vector
+ * holds, in order: the input projection kernel (4A+1, D) [and bias], per
+ * layer qk_projection (D, 2D) [bias], value_projection, output_projection,
+ * value_update (D, D) [bias] and qk_update_layers_j (D, D) [bias] for
+ * j < num_local_updates except in the last layer, then the orbitals,
+ * envelope and Jastrow leaves as for the Psiformer. */
+qmc_status qmc_lapnet_create(const qmc_lapnet_config* cfg, const float* atoms_host, const float* charges_host,
+                             qmc_model** out);
 qmc_status qmc_model_destroy(qmc_model* m);
 
 /* Number of float32 entries of the flat parameter vector (leaf order:

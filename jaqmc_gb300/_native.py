@@ -45,6 +45,14 @@ class PsiformerConfigC(C.Structure):
                 ("jastrow", C.c_int), ("precision", C.c_int)]
 
 
+class LapNetConfigC(C.Structure):
+    _fields_ = [("n_up", C.c_int), ("n_down", C.c_int), ("n_atoms", C.c_int), ("ndets", C.c_int),
+                ("n_layers", C.c_int), ("n_heads", C.c_int), ("head_dim", C.c_int),
+                ("num_local_updates", C.c_int), ("use_input_bias", C.c_int), ("use_backbone_bias", C.c_int),
+                ("envelope", C.c_int), ("orbitals_spin_split", C.c_int), ("jastrow", C.c_int),
+                ("precision", C.c_int)]
+
+
 class LayerTapC(C.Structure):
     _fields_ = [("kind", C.c_int), ("rows_per_walker", C.c_int), ("in_cols", C.c_int), ("out_cols", C.c_int),
                 ("has_bias", C.c_int), ("kernel_offset", C.c_size_t), ("bias_offset", C.c_size_t),
@@ -64,6 +72,7 @@ _SIGS = {
                                       C.POINTER(C.c_void_p)]),
     "qmc_psiformer_create": (C.c_int, [C.POINTER(PsiformerConfigC), C.c_void_p, C.c_void_p,
                                        C.POINTER(C.c_void_p)]),
+    "qmc_lapnet_create": (C.c_int, [C.POINTER(LapNetConfigC), C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "qmc_model_destroy": (C.c_int, [C.c_void_p]),
     "qmc_param_count": (C.c_size_t, [C.c_void_p]),
     "qmc_model_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -426,6 +435,36 @@ class NativePsiformer(NativeFermiNet):
         c.precision = PRECISION[precision]
         h = C.c_void_p()
         check(self.lib.qmc_psiformer_create(C.byref(c), atoms.ctypes.data, charges.ctypes.data, C.byref(h)))
+        self._finish(h, c.n_up + c.n_down, precision)
+
+
+class NativeLapNet(NativeFermiNet):
+    """A ``qmc_model`` handle for LapNet (+ SimpleEE Jastrow): the value path
+    (``forward``, ``mh_steps``, ``mh_steps_resident``, ``mh_draws``), the
+    forward-Laplacian ``local_energy`` and ``ecp_energy``; no parameter adjoint."""
+
+    def __init__(self, cfg, atoms, charges, precision="mixed", device=None):
+        if getattr(cfg, "use_layernorm", False):
+            raise NotImplementedError("LapNet with use_layernorm=True is not supported")
+        self._open(device)
+        c = LapNetConfigC()
+        c.n_up, c.n_down = int(cfg.nspins[0]), int(cfg.nspins[1])
+        atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 3))
+        charges = np.ascontiguousarray(np.asarray(charges, np.float32).reshape(-1))
+        c.n_atoms = atoms.shape[0]
+        c.ndets = int(cfg.ndets)
+        c.n_layers = int(cfg.num_layers)
+        c.n_heads = int(cfg.num_heads)
+        c.head_dim = int(cfg.heads_dim)
+        c.num_local_updates = int(cfg.num_local_updates)
+        c.use_input_bias = int(bool(cfg.use_input_bias))
+        c.use_backbone_bias = int(bool(cfg.use_backbone_bias))
+        c.envelope = ENVELOPE[str(cfg.envelope)]
+        c.orbitals_spin_split = int(bool(getattr(cfg, "orbitals_spin_split", True)))
+        c.jastrow = 1 if cfg.jastrow == "simple_ee" else 0
+        c.precision = PRECISION[precision]
+        h = C.c_void_p()
+        check(self.lib.qmc_lapnet_create(C.byref(c), atoms.ctypes.data, charges.ctypes.data, C.byref(h)))
         self._finish(h, c.n_up + c.n_down, precision)
 
 

@@ -1039,7 +1039,10 @@ static int psi_grad_chunk(const qmc_model* m, int B) {
   return (int)std::max<size_t>(1, std::min<size_t>(c, (size_t)B));
 }
 
-size_t psi_grad_workspace(const qmc_model* m, int B) { return make_psi_grad_plan(m, psi_grad_chunk(m, B)).total; }
+size_t psi_grad_workspace(const qmc_model* m, int B) {
+  if (m->psi->d.arch != kArchPsiformer) return 0;
+  return make_psi_grad_plan(m, psi_grad_chunk(m, B)).total;
+}
 
 static qmc_status psi_forward_save(qmc_model* m, const PsiGradPlan& p, void* ws, const float* electrons,
                                    cudaStream_t s) {
@@ -1269,6 +1272,10 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
 qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                         double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
   const PsiDims& pd = m->psi->d;
+  if (pd.arch != kArchPsiformer) {
+    set_error("the parameter adjoint is built for FermiNet and Psiformer models (not LapNet)");
+    return QMC_ERR_UNSUPPORTED;
+  }
   if (pd.n > 64 || pd.Dh > 64) {
     set_error("the Psiformer adjoint supports at most 64 electrons and head width 64");
     return QMC_ERR_SHAPE;

@@ -1748,6 +1748,13 @@ __device__ void logdet_finish(int w, int K, int T, double* lds, const double* ki
   }
 }
 
+// Shared-memory bytes of k_logdet's per-walker head (the launcher and the
+// kernel both size it here): lds, kins [K] (double); sgs, tLs, t2s, qs [K];
+// t1s [K][D]; ints [2]; wts [K]; done64 [K].
+__host__ __device__ inline size_t logdet_head_bytes(int K, int D) {
+  return align_up((size_t)2 * K * 8 + (size_t)4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8, 16);
+}
+
 template <int NMAX>
 __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K, int Tp, int T, const float* __restrict__ A,
                          const float* __restrict__ pe, float* __restrict__ logpsi,
@@ -1770,7 +1777,7 @@ __global__ void __launch_bounds__(256, NMAX <= 16 ? 3 : 2) k_logdet(int n, int K
   int* ints = reinterpret_cast<int*>(t1s + (size_t)K * D);  // flags [2]
   float* wts = reinterpret_cast<float*>(ints + 2);          // [K] determinant weights
   int* done64 = reinterpret_cast<int*>(wts + K);            // [K] already evaluated in FP64
-  const size_t head = align_up((size_t)(2 * K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8), 16);
+  const size_t head = logdet_head_bytes(K, D);
   const DetScratch sc(n);
   char* scratch = reinterpret_cast<char*>(shd) + head + sc.bytes * warp;
   if (threadIdx.x < 2) ints[threadIdx.x] = 0;
@@ -2425,7 +2432,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
   if (T == 1 && n <= 64 && !env) return launch_logdet_value_smem(s, B, n, K, A, logpsi, sign, flags);
   if (env) return cudaErrorInvalidValue;  // tangent passes take enveloped matrices
   const int D = T > 1 ? T - 2 : 0;
-  const size_t head = align_up((size_t)(K * 8 + 4 * K * 4 + (size_t)K * D * 4 + 8 + (size_t)K * 8), 16);
+  const size_t head = logdet_head_bytes(K, D);
   const DetScratch sc(n);
   int nw = (int)((200 * 1024 - head) / sc.bytes);
   nw = nw < 1 ? 1 : nw;

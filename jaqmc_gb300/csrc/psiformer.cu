@@ -326,23 +326,31 @@ PsiPlan psi_make_plan(const qmc_model* m, int B) {
   pp.att = take(rows * W * 4);
   pp.z = take(rows * std::max(3 * d.D, W) * 4);
   pp.jas = take((size_t)B * 4);
+  if (d.arch == kArchLapNet) {
+    pp.x2 = take(rows * d.D * 4);
+    pp.xn2 = take(rows * W * 4);
+    pp.z2 = take(rows * d.D * 4);
+  }
   p.dmax = d.D;
   p.total = o;
   return pp;
 }
 
-// z[rows][n_out] = X[rows][k] W[k][n_out] (X: GEMM-input buffer at `xoff`)
+// out[rows][n_out] (row stride ldo; default the z buffer, ldo = n_out) =
+// X[rows][k] W[k][n_out] (X: GEMM-input buffer at `xoff`)
 static qmc_status psi_gemm(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s, size_t xoff, int k,
-                           size_t w_f32, size_t t_bf16, int n_out) {
+                           size_t w_f32, size_t t_bf16, int n_out, float* out = nullptr, int ldo = 0) {
   const int rows = pp.base.B * m->psi->d.n * pp.base.Tp;
-  float* z = at<float>(ws, pp.z);
+  float* z = out ? out : at<float>(ws, pp.z);
+  const int ld = ldo > 0 ? ldo : n_out;
   if (pp.base.mixed) {
     TcStoreArgs a{rows, at<__nv_bfloat16>(ws, xoff), k, pp.in_plane, m->arena_bf16 + t_bf16, n_out, z, m->dev_err};
+    a.ld_out = ld;
     QMC_PROF_TRY(QMC_KC_STREAM_LAYER, tc_store_gemm(s, a));
   } else {
     const RowMap map{1, 0, 1, 1};
     QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, rows, map, at<float>(ws, xoff), k, k, nullptr, 0, 0,
-                                                   m->arena + w_f32, n_out, n_out, EpiStore{z, n_out, nullptr}));
+                                                   m->arena + w_f32, n_out, n_out, EpiStore{z, ld, nullptr}));
   }
   return QMC_OK;
 }
@@ -419,6 +427,56 @@ static qmc_status psi_backbone(qmc_model* m, const PsiPlan& pp, void* ws, cudaSt
   return QMC_OK;
 }
 
+// LapNet backbone, value pass (src/jaqmc/wavefunction/backbone/lapnet/
+// _backbone.py:68-150, no LayerNorm).  Two residual streams: hs (x2, GEMM
+// operand xn2) gives queries and keys and takes the local updates; hd (x,
+// operand xn) gives values and takes the attention and value-update
+// residuals.  Per layer:
+//   z[:, 0:2D]  = hs Wqk                      (before the local updates)
+//   hs += tanh(hs Wu_j + bu_j), j < n_local   (not in the last layer)
+//   z[:, 2D:3D] = hd Wv
+//   att = MHA(z + [bqk | bv])                 the Psiformer attention kernel
+//   r = hd + att Wo + bo;  hd = r + tanh(r Wvu + bvu)
+template <class Out>
+static qmc_status lapnet_backbone(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s,
+                                  Out (*fmt)(void*, const PsiPlan&, size_t, int)) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const float* ar = m->arena;
+  const int B = pp.base.B, rows = B * d.n, D = d.D;
+  float* x = at<float>(ws, pp.x);
+  float* x2 = at<float>(ws, pp.x2);
+  float* z = at<float>(ws, pp.z);
+  float* z2 = at<float>(ws, pp.z2);
+  {
+    const RowMap map{1, 0, 1, 1};
+    QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, rows, map, at<float>(ws, pp.base.x0), d.K0p, d.K0p, nullptr, 0, 0,
+                                             ar + a.w_in, D, D, EpiStore{z, D, nullptr}));
+  }
+  QMC_PROF(QMC_KC_LAYER0, launch_row(s, rows, D, z, D, ar + a.lb_in, 0, x, 0, 1, nullptr, nullptr,
+                                     fmt(ws, pp, pp.xn, D)));
+  QMC_PROF(QMC_KC_LAYER0, launch_row(s, rows, D, z, D, ar + a.lb_in, 0, x2, 0, 1, nullptr, nullptr,
+                                     fmt(ws, pp, pp.xn2, D)));
+  for (int l = 0; l < d.L; ++l) {
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn2, D, P.qk_k[l], a.t_qkv[l], 2 * D, z, 3 * D));
+    for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) {
+      QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn2, D, P.ul_k[l][j], a.t_ul[l][j], D, z2, D));
+      QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, D, z2, D, ar + a.lb_ul[l][j], 1, x2, 1, 1, nullptr, nullptr,
+                                        fmt(ws, pp, pp.xn2, D)));
+    }
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, P.lv_k[l], a.t_v[l], D, z + 2 * D, 3 * D));
+    QMC_PROF(QMC_KC_PAIR, launch_attention(s, B, d.n, d.H, d.Dh, z, ar + a.b_qkv[l], fmt(ws, pp, pp.att, D)));
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.att, D, P.lo_k[l], a.t_o[l], D));
+    QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, D, z, D, ar + a.lb_o[l], 0, x, 1, 1, nullptr, nullptr,
+                                      fmt(ws, pp, pp.xn, D)));
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, P.vu_k[l], a.t_vu[l], D));
+    QMC_PROF(QMC_KC_MEANS, launch_row(s, rows, D, z, D, ar + a.lb_vu[l], 1, x, 1, 1, nullptr, nullptr,
+                                      fmt(ws, pp, l + 1 < d.L ? pp.xn : pp.base.h1[0], D)));
+  }
+  return QMC_OK;
+}
+
 static StSplit fmt_split(void* ws, const PsiPlan& pp, size_t off, int ld) {
   return StSplit{at<__nv_bfloat16>(ws, off), ld, off == pp.base.h1[0] ? pp.base.h1_plane : pp.in_plane};
 }
@@ -435,8 +493,13 @@ qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* 
                                                 d.jastrow ? m->arena + P.alpha_par : nullptr, at<float>(ws, p.x0),
                                                 at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, pp.jas)),
             cudaGetLastError()));
-  if (p.mixed) QMC_TRY(psi_backbone<StSplit>(m, pp, ws, s, fmt_split));
-  else QMC_TRY(psi_backbone<StF32>(m, pp, ws, s, fmt_f32));
+  if (d.arch == kArchLapNet) {
+    if (p.mixed) QMC_TRY(lapnet_backbone<StSplit>(m, pp, ws, s, fmt_split));
+    else QMC_TRY(lapnet_backbone<StF32>(m, pp, ws, s, fmt_f32));
+  } else {
+    if (p.mixed) QMC_TRY(psi_backbone<StSplit>(m, pp, ws, s, fmt_split));
+    else QMC_TRY(psi_backbone<StF32>(m, pp, ws, s, fmt_f32));
+  }
   QMC_TRY(run_orbitals(m, p, ws, 0, s));
   QMC_TRY(run_logdet(m, p, ws, nullptr, logpsi, sign, nullptr, nullptr, flags, s));
   QMC_PROF(QMC_KC_OTHER, (k_psi_add<<<(p.B + 255) / 256, 256, 0, s>>>(p.B, logpsi, at<float>(ws, pp.jas)),
@@ -481,6 +544,11 @@ PsiPlan psi_fl_plan(const qmc_model* m, int B) {
   p.redo = take(logdet_fl_scratch_bytes(B, d.K, p.T));
   pp.jas = take((size_t)B * 4);
   pp.jgl = take((size_t)B * (3 * d.n + 1) * 4);
+  if (d.arch == kArchLapNet) {
+    pp.x2 = take(rows * d.D * 4);
+    pp.xn2 = take(rows * W * 4);
+    pp.z2 = take(rows * d.D * 4);
+  }
   p.h2[0] = p.h2[1] = p.g1 = p.gb = p.g2 = p.xp = p.lp = o;  // unused by these passes
   p.dmax = d.D;
   p.total = o;
@@ -556,6 +624,52 @@ static qmc_status psi_backbone_fl(qmc_model* m, const PsiPlan& pp, void* ws, cud
   return QMC_OK;
 }
 
+// LapNet backbone with forward-Laplacian tangents: lapnet_backbone's steps on
+// groups of Tp tangent rows (the group kernel carries value, Laplacian and
+// Jacobian rows through bias, tanh and the residuals; the tangent attention
+// kernel propagates through softmax and the bilinear products).
+template <class Out>
+static qmc_status lapnet_backbone_fl(qmc_model* m, const PsiPlan& pp, void* ws, cudaStream_t s,
+                                     Out (*fmt)(void*, const PsiPlan&, size_t, int)) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const float* ar = m->arena;
+  const Plan& p = pp.base;
+  const int groups = p.B * d.n, rows = groups * p.Tp, Tp = p.Tp, D = d.D;
+  float* x = at<float>(ws, pp.x);
+  float* x2 = at<float>(ws, pp.x2);
+  float* z = at<float>(ws, pp.z);
+  float* z2 = at<float>(ws, pp.z2);
+  {
+    const RowMap map{1, 0, 1, 1};
+    QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, rows, map, at<float>(ws, p.x0), d.K0p, d.K0p, nullptr, 0, 0,
+                                             ar + a.w_in, D, D, EpiStore{z, D, nullptr}));
+  }
+  QMC_PROF(QMC_KC_LAYER0, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + a.lb_in, 0, x, 1, nullptr, nullptr,
+                                              fmt(ws, pp, pp.xn, D)));
+  QMC_PROF(QMC_KC_LAYER0, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + a.lb_in, 0, x2, 1, nullptr, nullptr,
+                                              fmt(ws, pp, pp.xn2, D)));
+  for (int l = 0; l < d.L; ++l) {
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn2, D, P.qk_k[l], a.t_qkv[l], 2 * D, z, 3 * D));
+    for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) {
+      QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn2, D, P.ul_k[l][j], a.t_ul[l][j], D, z2, D));
+      QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, D, z2, D, ar + a.lb_ul[l][j], 1, x2, 2, nullptr,
+                                                 nullptr, fmt(ws, pp, pp.xn2, D)));
+    }
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, P.lv_k[l], a.t_v[l], D, z + 2 * D, 3 * D));
+    QMC_PROF(QMC_KC_PAIR, launch_psi_attention_fl(s, p.B, d.n, Tp, p.T, d.H, d.Dh, z, ar + a.b_qkv[l],
+                                                  fmt(ws, pp, pp.att, D)));
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.att, D, P.lo_k[l], a.t_o[l], D));
+    QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + a.lb_o[l], 0, x, 2, nullptr, nullptr,
+                                               fmt(ws, pp, pp.xn, D)));
+    QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, P.vu_k[l], a.t_vu[l], D));
+    QMC_PROF(QMC_KC_MEANS, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + a.lb_vu[l], 1, x, 2, nullptr, nullptr,
+                                               fmt(ws, pp, l + 1 < d.L ? pp.xn : p.h1[0], D)));
+  }
+  return QMC_OK;
+}
+
 qmc_status psi_local_energy(qmc_model* m, int batch, const float* electrons, float* e_local, float* ke,
                             float* pe, float* logpsi, uint8_t* flags, void* ws, cudaStream_t s) {
   const PsiDims& d = m->psi->d;
@@ -572,8 +686,13 @@ qmc_status psi_local_energy(qmc_model* m, int batch, const float* electrons, flo
                                     ar + m->a.atoms, ar + m->a.charges, m->nuclear_repulsion,
                                     d.jastrow ? ar + P.alpha_par : nullptr, at<float>(ws, p.x0), at<float>(ws, p.rae),
                                     at<float>(ws, p.aevec), pe_ws, at<float>(ws, pp.jas), at<float>(ws, pp.jgl)));
-    if (p.mixed) QMC_TRY(psi_backbone_fl<StSplit>(m, pp, ws, s, fmt_split));
-    else QMC_TRY(psi_backbone_fl<StF32>(m, pp, ws, s, fmt_f32));
+    if (d.arch == kArchLapNet) {
+      if (p.mixed) QMC_TRY(lapnet_backbone_fl<StSplit>(m, pp, ws, s, fmt_split));
+      else QMC_TRY(lapnet_backbone_fl<StF32>(m, pp, ws, s, fmt_f32));
+    } else {
+      if (p.mixed) QMC_TRY(psi_backbone_fl<StSplit>(m, pp, ws, s, fmt_split));
+      else QMC_TRY(psi_backbone_fl<StF32>(m, pp, ws, s, fmt_f32));
+    }
     QMC_TRY(run_orbitals(m, p, ws, 0, s));
     float* lp = logpsi ? logpsi + b0 : at<float>(ws, p.lpsi);
     QMC_PROF(QMC_KC_LOGDET, launch_logdet(s, Bc, d.n, d.K, p.Tp, p.T, at<float>(ws, p.amat), pe_ws, lp,
@@ -599,7 +718,28 @@ qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
   // input kernel [K0][D] zero-padded to [K0p][D]
   QMC_CUDA(cudaMemsetAsync(ar + a.w_in, 0, sizeof(float) * d.K0p * D, s));
   QMC_CUDA(cudaMemcpyAsync(ar + a.w_in, params + P.in_k, sizeof(float) * d.K0 * D, cudaMemcpyDeviceToDevice, s));
-  for (int l = 0; l < d.L; ++l) {
+  auto copy = [&](size_t dst, size_t src, size_t count) {
+    return cudaMemcpyAsync(ar + dst, params + src, sizeof(float) * count, cudaMemcpyDeviceToDevice, s);
+  };
+  for (int l = 0; d.arch == kArchLapNet && l < d.L; ++l) {
+    // biases stay zero (arena initialisation) when the model has none
+    if (d.bb_bias) {
+      QMC_CUDA(copy(a.b_qkv[l], P.qk_b[l], 2 * (size_t)D));
+      QMC_CUDA(copy(a.b_qkv[l] + 2 * (size_t)D, P.lv_b[l], D));
+      QMC_CUDA(copy(a.lb_o[l], P.lo_b[l], D));
+      QMC_CUDA(copy(a.lb_vu[l], P.vu_b[l], D));
+    }
+    QMC_CUDA(launch_transpose_split(s, ar + P.qk_k[l], D, 2 * D, 2 * D, ab + a.t_qkv[l], D, 2 * D));
+    QMC_CUDA(launch_transpose_split(s, ar + P.lv_k[l], D, D, D, ab + a.t_v[l], D, D));
+    QMC_CUDA(launch_transpose_split(s, ar + P.lo_k[l], D, D, D, ab + a.t_o[l], D, D));
+    QMC_CUDA(launch_transpose_split(s, ar + P.vu_k[l], D, D, D, ab + a.t_vu[l], D, D));
+    for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) {
+      if (d.bb_bias) QMC_CUDA(copy(a.lb_ul[l][j], P.ul_b[l][j], D));
+      QMC_CUDA(launch_transpose_split(s, ar + P.ul_k[l][j], D, D, D, ab + a.t_ul[l][j], D, D));
+    }
+  }
+  if (d.arch == kArchLapNet && d.in_bias) QMC_CUDA(copy(a.lb_in, P.in_b, D));
+  for (int l = 0; d.arch == kArchPsiformer && l < d.L; ++l) {
     const size_t src[3] = {P.q_k[l], P.k_k[l], P.v_k[l]}, bsrc[3] = {P.q_b[l], P.k_b[l], P.v_b[l]};
     for (int c = 0; c < 3; ++c) {
       QMC_CUDA(cudaMemcpy2DAsync(ar + a.w_qkv[l] + (size_t)c * D, sizeof(float) * 3 * D, params + src[c],
@@ -644,71 +784,32 @@ qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
 
 }  // namespace qmc
 
-using namespace qmc;
+namespace qmc {
 
-extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, const float* atoms_host,
-                                           const float* charges_host, qmc_model** out) {
-  if (!cfg || !atoms_host || !charges_host || !out) {
-    set_error("null argument");
-    return QMC_ERR_ARG;
-  }
-  *out = nullptr;
-  const int n = cfg->n_up + cfg->n_down, A = cfg->n_atoms;
-  if (cfg->n_up < 0 || cfg->n_down < 0 || n < 1 || n > 64 || A < 1 || A > kMaxAtoms || cfg->ndets < 1 ||
-      cfg->n_layers < 1 || cfg->n_layers > kPsiMaxLayers || cfg->n_heads < 1 || cfg->head_dim < 1 ||
-      cfg->n_mlp < 0 || cfg->n_mlp > kPsiMaxMlp) {
-    set_error("psiformer: bad sizes (n=%d atoms=%d layers=%d mlp=%d)", n, A, cfg->n_layers, cfg->n_mlp);
-    return QMC_ERR_SHAPE;
-  }
-  const int D = cfg->n_heads * cfg->head_dim;
-  bool widths_ok = D % 64 == 0 && D <= 512 && cfg->head_dim % 4 == 0;
-  for (int k = 0; k < cfg->n_mlp; ++k) widths_ok = widths_ok && cfg->mlp_dims[k] % 64 == 0 && cfg->mlp_dims[k] <= 512;
-  if (!widths_ok) {
-    set_error("psiformer: attention and MLP widths must be multiples of 64 (at most 512), head width a multiple of 4");
-    return QMC_ERR_UNSUPPORTED;
-  }
-  if (attention_smem(n, cfg->head_dim) > 200 * 1024) {
-    set_error("psiformer: %d electrons x head width %d exceed the attention kernel's shared memory", n,
-              cfg->head_dim);
-    return QMC_ERR_UNSUPPORTED;
-  }
-  if (cfg->precision != QMC_PRECISION_FP32 && cfg->precision != QMC_PRECISION_MIXED_BF16) {
-    set_error("unknown precision %d", cfg->precision);
-    return QMC_ERR_ARG;
-  }
-  if (cfg->envelope < QMC_ENVELOPE_ISOTROPIC || cfg->envelope > QMC_ENVELOPE_NULL) {
-    set_error("unsupported envelope %d", cfg->envelope);
-    return QMC_ERR_UNSUPPORTED;
-  }
-  qmc_model* m = new qmc_model();
-  m->kind = QMC_KIND_PSIFORMER;
-  m->psi = new PsiModel();
+// Flat parameter offsets (C-ABI leaf order), derived arena fields and the
+// bf16 K-major weight copies of an attention-backbone model whose dims are
+// filled in; allocates and initialises the device arenas.
+static qmc_status psi_layout_alloc(qmc_model* m, int env_kind, const float* atoms_host, const float* charges_host) {
   PsiDims& d = m->psi->d;
-  d.n = n;
-  d.n_up = cfg->n_up;
-  d.n_dn = cfg->n_down;
-  d.A = A;
-  d.K = cfg->ndets;
-  d.L = cfg->n_layers;
-  d.H = cfg->n_heads;
-  d.Dh = cfg->head_dim;
-  d.D = D;
-  d.n_dense = cfg->n_mlp + 1;
-  for (int k = 0; k < cfg->n_mlp; ++k) d.mlp[k] = cfg->mlp_dims[k];
-  d.mlp[cfg->n_mlp] = D;
-  d.split = cfg->orbitals_spin_split && cfg->n_up > 0 && cfg->n_down > 0;
-  d.env_abs = cfg->envelope == QMC_ENVELOPE_ABS_ISOTROPIC;
-  const int env_kind = cfg->envelope;
-  d.jastrow = cfg->jastrow != 0;
-  d.K0 = 4 * A + 1;
-  d.K0p = (d.K0 + 7) / 8 * 8;  // the SIMT GEMM walks K in steps of 8
-  // flat parameter offsets (reference leaf order)
+  const int n = d.n, A = d.A, D = d.D;
   PsiParams& P = m->psi->p;
   size_t o = 0;
   auto take = [&](size_t count) { size_t r = o; o += count; return r; };
   P.in_k = take((size_t)d.K0 * D);
-  P.in_b = take(D);
+  if (d.arch == kArchPsiformer || d.in_bias) P.in_b = take(D);
   for (int l = 0; l < d.L; ++l) {
+    if (d.arch == kArchLapNet) {
+      auto dense = [&](size_t* k, size_t* b, int dout) {
+        *k = take((size_t)D * dout);
+        if (d.bb_bias) *b = take(dout);
+      };
+      dense(&P.qk_k[l], &P.qk_b[l], 2 * D);
+      dense(&P.lv_k[l], &P.lv_b[l], D);
+      dense(&P.lo_k[l], &P.lo_b[l], D);
+      dense(&P.vu_k[l], &P.vu_b[l], D);
+      for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) dense(&P.ul_k[l][j], &P.ul_b[l][j], D);
+      continue;
+    }
     P.ln0_s[l] = take(D);
     P.ln0_b[l] = take(D);
     P.q_k[l] = take((size_t)D * D);
@@ -750,7 +851,16 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   o = align_up(P.total, 64);
   auto takea = [&](size_t count) { size_t r = o; o += align_up(count, 16); return r; };
   a.w_in = takea((size_t)d.K0p * D);
-  for (int l = 0; l < d.L; ++l) {
+  if (d.arch == kArchLapNet) {
+    a.lb_in = takea(D);
+    for (int l = 0; l < d.L; ++l) {
+      a.b_qkv[l] = takea((size_t)3 * D);
+      a.lb_o[l] = takea(D);
+      a.lb_vu[l] = takea(D);
+      for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) a.lb_ul[l][j] = takea(D);
+    }
+  }
+  for (int l = 0; d.arch == kArchPsiformer && l < d.L; ++l) {
     a.w_qkv[l] = takea((size_t)D * 3 * D);
     a.b_qkv[l] = takea((size_t)3 * D);
     a.t32_qkv[l] = takea((size_t)3 * D * D);
@@ -796,6 +906,14 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   size_t ob = 0;
   auto takeb = [&](size_t count) { size_t r = ob; ob += align_up(count, 64); return r; };
   for (int l = 0; l < d.L; ++l) {
+    if (d.arch == kArchLapNet) {
+      a.t_qkv[l] = takeb((size_t)2 * D * 2 * D);
+      a.t_v[l] = takeb((size_t)2 * D * D);
+      a.t_o[l] = takeb((size_t)2 * D * D);
+      a.t_vu[l] = takeb((size_t)2 * D * D);
+      for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) a.t_ul[l][j] = takeb((size_t)2 * D * D);
+      continue;
+    }
     a.t_qkv[l] = takeb((size_t)2 * D * 3 * D);
     a.t_o[l] = takeb((size_t)2 * D * D);
     int din = D;
@@ -806,7 +924,6 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
   }
   for (int c = 0; c < 2; ++c) fa.t_orb[c] = c < nch ? takeb((size_t)2 * fd.norb_p * D) : fa.t_orb[0];
   a.total_bf16 = fa.total_bf16 = ob;
-  m->precision = cfg->precision;
   cudaError_t e = cudaGetDevice(&m->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->n_sms, cudaDevAttrMultiProcessorCount, m->device);
   if (e == cudaSuccess) e = cudaMalloc(&m->arena, fa.total * sizeof(float));
@@ -825,10 +942,133 @@ extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, cons
     cudaFree(m->arena);
     cudaFree(m->arena_bf16);
     cudaFree(m->dev_err);
+    m->arena = nullptr;
+    m->arena_bf16 = nullptr;
+    m->dev_err = nullptr;
+    return cuda_status(e, "attention-backbone model create");
+  }
+  return QMC_OK;
+}
+
+// Shared validation of the attention sizes, precision and envelope.
+static qmc_status psi_check_common(const char* who, int n, int A, int ndets, int n_layers, int n_heads,
+                                   int head_dim, int precision, int envelope) {
+  if (n < 1 || n > 64 || A < 1 || A > kMaxAtoms || ndets < 1 || n_layers < 1 || n_layers > kPsiMaxLayers ||
+      n_heads < 1 || head_dim < 1) {
+    set_error("%s: bad sizes (n=%d atoms=%d layers=%d heads=%d)", who, n, A, n_layers, n_heads);
+    return QMC_ERR_SHAPE;
+  }
+  const int D = n_heads * head_dim;
+  if (!(D % 64 == 0 && D <= 512 && head_dim % 4 == 0)) {
+    set_error("%s: attention width must be a multiple of 64 (at most 512), head width a multiple of 4", who);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  if (attention_smem(n, head_dim) > 200 * 1024) {
+    set_error("%s: %d electrons x head width %d exceed the attention kernel's shared memory", who, n, head_dim);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  if (precision != QMC_PRECISION_FP32 && precision != QMC_PRECISION_MIXED_BF16) {
+    set_error("unknown precision %d", precision);
+    return QMC_ERR_ARG;
+  }
+  if (envelope < QMC_ENVELOPE_ISOTROPIC || envelope > QMC_ENVELOPE_NULL) {
+    set_error("unsupported envelope %d", envelope);
+    return QMC_ERR_UNSUPPORTED;
+  }
+  return QMC_OK;
+}
+
+static void psi_common_dims(PsiDims& d, int n_up, int n_down, int A, int K, int L, int H, int Dh, int split,
+                            int envelope, int jastrow) {
+  d.n = n_up + n_down;
+  d.n_up = n_up;
+  d.n_dn = n_down;
+  d.A = A;
+  d.K = K;
+  d.L = L;
+  d.H = H;
+  d.Dh = Dh;
+  d.D = H * Dh;
+  d.split = split && n_up > 0 && n_down > 0;
+  d.env_abs = envelope == QMC_ENVELOPE_ABS_ISOTROPIC;
+  d.jastrow = jastrow != 0;
+  d.K0 = 4 * A + 1;
+  d.K0p = (d.K0 + 7) / 8 * 8;  // the SIMT GEMM walks K in steps of 8
+}
+
+static qmc_status psi_finish(qmc_model* m, int precision, int envelope, const float* atoms_host,
+                             const float* charges_host, qmc_model** out) {
+  m->precision = precision;
+  const qmc_status st = psi_layout_alloc(m, envelope, atoms_host, charges_host);
+  if (st != QMC_OK) {
     delete m->psi;
     delete m;
-    return cuda_status(e, "qmc_psiformer_create");
+    return st;
   }
   *out = m;
   return QMC_OK;
+}
+
+}  // namespace qmc
+
+using namespace qmc;
+
+extern "C" qmc_status qmc_psiformer_create(const qmc_psiformer_config* cfg, const float* atoms_host,
+                                           const float* charges_host, qmc_model** out) {
+  if (!cfg || !atoms_host || !charges_host || !out) {
+    set_error("null argument");
+    return QMC_ERR_ARG;
+  }
+  *out = nullptr;
+  if (cfg->n_up < 0 || cfg->n_down < 0 || cfg->n_mlp < 0 || cfg->n_mlp > kPsiMaxMlp) {
+    set_error("psiformer: bad sizes (n_up=%d n_down=%d mlp=%d)", cfg->n_up, cfg->n_down, cfg->n_mlp);
+    return QMC_ERR_SHAPE;
+  }
+  QMC_TRY(psi_check_common("psiformer", cfg->n_up + cfg->n_down, cfg->n_atoms, cfg->ndets, cfg->n_layers,
+                           cfg->n_heads, cfg->head_dim, cfg->precision, cfg->envelope));
+  for (int k = 0; k < cfg->n_mlp; ++k) {
+    if (cfg->mlp_dims[k] % 64 || cfg->mlp_dims[k] < 64 || cfg->mlp_dims[k] > 512) {
+      set_error("psiformer: MLP widths must be multiples of 64 (at most 512)");
+      return QMC_ERR_UNSUPPORTED;
+    }
+  }
+  qmc_model* m = new qmc_model();
+  m->kind = QMC_KIND_PSIFORMER;
+  m->psi = new PsiModel();
+  PsiDims& d = m->psi->d;
+  d.arch = kArchPsiformer;
+  psi_common_dims(d, cfg->n_up, cfg->n_down, cfg->n_atoms, cfg->ndets, cfg->n_layers, cfg->n_heads, cfg->head_dim,
+                  cfg->orbitals_spin_split, cfg->envelope, cfg->jastrow);
+  d.n_dense = cfg->n_mlp + 1;
+  for (int k = 0; k < cfg->n_mlp; ++k) d.mlp[k] = cfg->mlp_dims[k];
+  d.mlp[cfg->n_mlp] = d.D;
+  return psi_finish(m, cfg->precision, cfg->envelope, atoms_host, charges_host, out);
+}
+
+extern "C" qmc_status qmc_lapnet_create(const qmc_lapnet_config* cfg, const float* atoms_host,
+                                        const float* charges_host, qmc_model** out) {
+  if (!cfg || !atoms_host || !charges_host || !out) {
+    set_error("null argument");
+    return QMC_ERR_ARG;
+  }
+  *out = nullptr;
+  if (cfg->n_up < 0 || cfg->n_down < 0 || cfg->num_local_updates < 0 || cfg->num_local_updates > kLapMaxLocal) {
+    set_error("lapnet: bad sizes (n_up=%d n_down=%d local updates=%d, at most %d)", cfg->n_up, cfg->n_down,
+              cfg->num_local_updates, kLapMaxLocal);
+    return QMC_ERR_SHAPE;
+  }
+  QMC_TRY(psi_check_common("lapnet", cfg->n_up + cfg->n_down, cfg->n_atoms, cfg->ndets, cfg->n_layers,
+                           cfg->n_heads, cfg->head_dim, cfg->precision, cfg->envelope));
+  qmc_model* m = new qmc_model();
+  m->kind = QMC_KIND_PSIFORMER;
+  m->psi = new PsiModel();
+  PsiDims& d = m->psi->d;
+  d.arch = kArchLapNet;
+  psi_common_dims(d, cfg->n_up, cfg->n_down, cfg->n_atoms, cfg->ndets, cfg->n_layers, cfg->n_heads, cfg->head_dim,
+                  cfg->orbitals_spin_split, cfg->envelope, cfg->jastrow);
+  d.n_dense = 0;
+  d.n_local = cfg->num_local_updates;
+  d.in_bias = cfg->use_input_bias != 0;
+  d.bb_bias = cfg->use_backbone_bias != 0;
+  return psi_finish(m, cfg->precision, cfg->envelope, atoms_host, charges_host, out);
 }

@@ -8,14 +8,24 @@ namespace qmc {
 
 constexpr int kPsiMaxLayers = 8;
 constexpr int kPsiMaxMlp = 4;  // hidden MLP widths per layer (plus the final one back to D)
+constexpr int kLapMaxLocal = 4;  // LapNet: local updates of the individual stream per layer
+
+// The attention-backbone models share this description: the Psiformer
+// (arch 0) and LapNet (arch 1, src/jaqmc/wavefunction/backbone/lapnet/
+// _backbone.py: an individual stream hs giving queries and keys, a dense
+// stream hd giving values and carrying the attention and update residuals).
+enum { kArchPsiformer = 0, kArchLapNet = 1 };
 
 struct PsiDims {
+  int arch;
   int n, n_up, n_dn, A, K;
   int L, H, Dh, D;                // layers, heads, head width, attention width H*Dh
   int n_dense;                    // MLP dense layers per block (hidden widths + 1)
   int mlp[kPsiMaxMlp + 1];        // output widths of the MLP dense layers (last = D)
   int split, env_abs, jastrow;
   int K0, K0p;                    // 4A + 1 input features, padded to a multiple of 8
+  int n_local;                    // LapNet: local updates per layer (not in the last layer)
+  int in_bias, bb_bias;           // LapNet: input / backbone projections have biases
 };
 
 // Offsets (floats) of each leaf in the flat parameter vector (reference leaf
@@ -29,6 +39,11 @@ struct PsiParams {
   size_t mlp_k[kPsiMaxLayers][kPsiMaxMlp + 1], mlp_b[kPsiMaxLayers][kPsiMaxMlp + 1];
   size_t orb_k[2], env_pi[2], env_sigma[2];
   size_t alpha_par, alpha_anti;
+  // LapNet (arch 1): query|key, value, output, value-update and local-update
+  // projections per layer (bias offsets only when the model has biases)
+  size_t qk_k[kPsiMaxLayers], qk_b[kPsiMaxLayers], lv_k[kPsiMaxLayers], lv_b[kPsiMaxLayers];
+  size_t lo_k[kPsiMaxLayers], lo_b[kPsiMaxLayers], vu_k[kPsiMaxLayers], vu_b[kPsiMaxLayers];
+  size_t ul_k[kPsiMaxLayers][kLapMaxLocal], ul_b[kPsiMaxLayers][kLapMaxLocal];
   size_t total;
 };
 
@@ -42,10 +57,14 @@ struct PsiArena {
   size_t t32_qkv[kPsiMaxLayers];  // [3D][D]
   size_t t32_o[kPsiMaxLayers];    // [D][D]
   size_t t32_mlp[kPsiMaxLayers][kPsiMaxMlp + 1];  // [dout][din]
+  // LapNet: biases (zero when the model has none): input, output,
+  // value-update and local-update projections; b_qkv holds query|key|value
+  size_t lb_in, lb_o[kPsiMaxLayers], lb_vu[kPsiMaxLayers], lb_ul[kPsiMaxLayers][kLapMaxLocal];
   size_t total;
-  size_t t_qkv[kPsiMaxLayers];    // [3D][D]
+  size_t t_qkv[kPsiMaxLayers];    // [3D][D] (LapNet: query|key [2D][D])
   size_t t_o[kPsiMaxLayers];      // [D][D]
   size_t t_mlp[kPsiMaxLayers][kPsiMaxMlp + 1];
+  size_t t_v[kPsiMaxLayers], t_vu[kPsiMaxLayers], t_ul[kPsiMaxLayers][kLapMaxLocal];  // LapNet [D][D]
   size_t total_bf16;
 };
 
@@ -67,6 +86,7 @@ struct PsiPlan {
   size_t jas;   // [B] Jastrow
   size_t jgl;   // [B][3n+1] Jastrow gradient and Laplacian (forward-Laplacian passes)
   size_t in_plane;  // bf16 elements between planes of xn / att / h1[0]
+  size_t x2, xn2, z2;  // LapNet: individual stream (f32), its GEMM operand, projection outputs [rows][D]
 };
 
 PsiPlan psi_make_plan(const qmc_model* m, int B);

@@ -1052,7 +1052,7 @@ qmc_status tc_store_gemm(cudaStream_t s, const TcStoreArgs& a) {
   EpiTcStore e{};
   e.n_groups = a.n_rows;
   e.out = a.out;
-  e.ld = a.n_out;
+  e.ld = a.ld_out > 0 ? a.ld_out : a.n_out;
   return launch(s, mA, mA, mB, mB, g, (a.n_rows + kRows - 1) / kRows, e);
 }
 

@@ -40,8 +40,9 @@ struct TcStoreArgs {
   int n_rows;
   const __nv_bfloat16* X; int k; size_t x_plane;    // [n_rows][k] split planes
   const __nv_bfloat16* Wt; int n_out;               // [n_out][k] split planes
-  float* out;                                       // [n_rows][n_out] fp32
+  float* out;                                       // [n_rows][ld_out] fp32
   int* err;
+  int ld_out = 0;                                   // row stride of out (0: n_out)
 };
 // out = X W (the spin-mean broadcast term of a layer).
 qmc_status tc_store_gemm(cudaStream_t s, const TcStoreArgs& a);

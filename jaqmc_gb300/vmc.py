@@ -170,9 +170,9 @@ class FermiNetWavefunction:
 class PsiformerWavefunction(FermiNetWavefunction):
     """Psiformer ansatz with the SimpleEE Jastrow (hyper-parameters and
     defaults of ``src/jaqmc/app/molecule/wavefunction/psiformer.py:38-94``),
-    evaluated by the GB300 library: log|psi|, the MH sampler and the
-    forward-Laplacian local energy (the same estimators as FermiNet).  There is
-    no parameter adjoint for it."""
+    evaluated by the GB300 library: log|psi|, the MH sampler, the
+    forward-Laplacian local energy (the same estimators as FermiNet) and the
+    FP32 parameter adjoint (at most 64 electrons, head width <= 64)."""
 
     num_layers: int = 4
     num_heads: int = 4
@@ -203,6 +203,55 @@ class PsiformerWavefunction(FermiNetWavefunction):
         m = self._models.get(key)
         if m is None:
             m = _native.NativePsiformer(self.config, atoms, charges, precision=self.precision, device=self._dev())
+            self._models[key] = m
+        stamp = (id(params), params.version)
+        if self._loaded.get(key) != stamp:
+            m.set_params(params.flat)
+            self._loaded[key] = stamp
+        return m
+
+
+@dataclass
+class LapNetWavefunction(FermiNetWavefunction):
+    """LapNet ansatz with the SimpleEE Jastrow (hyper-parameters and defaults
+    of ``src/jaqmc/app/molecule/wavefunction/lapnet.py:27-75``), evaluated by
+    the GB300 library: log|psi|, the MH sampler, the forward-Laplacian local
+    energy and the ECP estimator.  ``use_layernorm`` and the parameter adjoint
+    are not built (``LossAndGrad`` raises)."""
+
+    num_layers: int = 4
+    num_heads: int = 4
+    heads_dim: int = 64
+    use_layernorm: bool = False
+    jastrow: str = "simple_ee"
+    use_input_bias: bool = True
+    use_backbone_bias: bool = True
+    num_local_updates: int = 2
+    jastrow_alpha_init: float = 1.0
+    precision: str = "mixed"
+
+    @property
+    def config(self) -> P.LapNetConfig:
+        return P.LapNetConfig(nspins=tuple(self.nspins), ndets=self.ndets, num_layers=self.num_layers,
+                              num_heads=self.num_heads, heads_dim=self.heads_dim, use_layernorm=self.use_layernorm,
+                              jastrow=self.jastrow, use_input_bias=self.use_input_bias,
+                              use_backbone_bias=self.use_backbone_bias, num_local_updates=self.num_local_updates,
+                              envelope=self.envelope, jastrow_alpha_init=self.jastrow_alpha_init,
+                              orbitals_spin_split=self.orbitals_spin_split)
+
+    def init_params(self, data: MoleculeData, rngs=0) -> DeviceParams:
+        seed = int(rngs) if np.isscalar(rngs) else int(np.asarray(rngs).ravel()[0])
+        A = np.asarray(data.atoms, np.float64).reshape(-1, 3).shape[0]
+        tree = P.init_lapnet(self.config, A, seed=seed)
+        return DeviceParams(tree, P.lapnet_leaves(self.config, A), self._dev())
+
+    def model(self, data: MoleculeData, params: DeviceParams) -> _native.NativeLapNet:
+        atoms = np.asarray(torch.as_tensor(data.atoms).cpu(), np.float32).reshape(-1, 3)
+        charges = np.asarray(torch.as_tensor(data.charges).cpu(), np.float32).reshape(-1)
+        key = (atoms.tobytes(), charges.tobytes(), self.precision)
+        m = self._models.get(key)
+        if m is None:
+            m = _native.NativeLapNet(self.config, atoms, charges, precision=self.precision, device=self._dev())
             self._models[key] = m
         stamp = (id(params), params.version)
         if self._loaded.get(key) != stamp:
