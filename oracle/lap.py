@@ -23,8 +23,14 @@ forward-Laplacian interpreter:
 
 With ``D == 0`` the same code is a plain forward pass (the tangent tensors are
 empty), which lets the model code in this package serve both purposes.
+
+:func:`split_bf16_gemms` makes ``linear`` round its operands the way the
+library's split-BF16 tensor-core GEMMs do, so that the oracle can state what
+that precision form should give (its operand rounding, nothing else).
 """
 from __future__ import annotations
+
+from contextlib import contextmanager
 
 import torch
 
@@ -166,8 +172,48 @@ def stack(parts, axis: int) -> LT:
               torch.stack([p.L for p in parts], axis))
 
 
+_SPLIT_SELECT = None  # predicate on W: emulate the split-BF16 product for this GEMM
+
+
+def _split_bf16(a: torch.Tensor):
+    """FP32 value of ``a`` as hi + lo bf16 (both round-to-nearest-even)."""
+    a = a.to(torch.float32).to(torch.float64)
+    hi = a.to(torch.bfloat16).to(torch.float64)
+    lo = (a - hi).to(torch.bfloat16).to(torch.float64)
+    return hi, lo
+
+
+def _split_matmul(a: torch.Tensor, W: torch.Tensor) -> torch.Tensor:
+    ah, al = _split_bf16(a)
+    wh, wl = _split_bf16(W)
+    return (ah @ wh + ah @ wl + al @ wh).to(a.dtype)
+
+
+@contextmanager
+def split_bf16_gemms(select=lambda W: True):
+    """Within the block, ``linear`` with a weight ``W`` for which
+    ``select(W)`` holds rounds both operands to FP32, splits each into a high
+    and a low bf16 part and forms ``hi_a hi_W + hi_a lo_W + lo_a hi_W`` (the
+    low x low product dropped) in the oracle's dtype: the product of the
+    library's split-BF16 tensor-core GEMMs up to their FP32 accumulation.
+    The value, Jacobian and Laplacian rows are rounded alike, as they are on
+    the GPU."""
+    global _SPLIT_SELECT
+    prev = _SPLIT_SELECT
+    _SPLIT_SELECT = select
+    try:
+        yield
+    finally:
+        _SPLIT_SELECT = prev
+
+
 def linear(a: LT, W: torch.Tensor, b: torch.Tensor | None = None) -> LT:
     """``a @ W + b`` over the last axis (dot_general rule)."""
+    if _SPLIT_SELECT is not None and _SPLIT_SELECT(W):
+        x = _split_matmul(a.x, W)
+        if b is not None:
+            x = x + b
+        return LT(x, _split_matmul(a.J, W), _split_matmul(a.L, W))
     x = a.x @ W
     if b is not None:
         x = x + b
