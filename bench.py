@@ -304,7 +304,7 @@ def psiformer_request_roofline(cfg, n, A, walkers, mh_steps, ms, prec, pk, pk_ki
             "peak_kind": kind, "unit": "TFLOP/s", "frac": achieved / peak, "algorithmic_tflop_per_request": flop / 1e12}
 
 
-def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=8, burn_in=50,
+def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=32, burn_in=50,
                   forms=("mixed", "fp32")):
     """Benzene Psiformer (4 layers, 4 x 64 heads, MLP 256, K = 16, SimpleEE
     Jastrow): walker-steps/s of requests of ``mh_steps`` MH updates + the
@@ -388,8 +388,10 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
         el64 = (OH.kinetic_from_tangents(r["grad"], r["lap"]) + OH.potential_energy(sub, mol.atoms, mol.charges))
         d_oracle = {"walkers": int(sub.shape[0])}
         for p in models:
-            e = el[p][:oracle_walkers].cpu()
-            d_oracle[p] = {"dE_mean": float(e.mean() - el64.mean()), "max_abs": float((e - el64).abs().max())}
+            d = (el[p][:oracle_walkers].cpu() - el64).numpy()
+            ad = np.abs(d)
+            d_oracle[p] = {"dE_mean_Ha": float(d.mean()), "paired_se_Ha": float(d.std(ddof=1) / np.sqrt(d.size)),
+                           "median_abs_Ha": float(np.median(ad)), "max_abs_Ha": float(ad.max())}
     del models, el, x0, m, x, mv
     torch.cuda.empty_cache()  # the E_L workspaces (tens of GB) go back before the next leg
     cpu = None

@@ -99,8 +99,9 @@ typedef struct {
  * per layer (none in the last), a dense stream giving values and taking the
  * attention and value-update residuals, log-rescaled input features, spin-
  * split orbitals.  use_layernorm is not supported.  qmc_forward,
- * qmc_mh_steps(_resident), qmc_mh_draws, qmc_ecp_energy and the forward-
- * Laplacian qmc_local_energy (at most 42 electrons); no parameter adjoint. */
+ * qmc_mh_steps(_resident), qmc_mh_draws, qmc_ecp_energy, the forward-
+ * Laplacian qmc_local_energy (at most 42 electrons) and the FP32 parameter
+ * adjoint qmc_grad (at most 64 electrons, head width <= 64). */
 typedef struct {
   int n_up, n_down, n_atoms;
   int ndets;                            /* K                                    */
@@ -258,9 +259,11 @@ qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
  *   logpsi (batch, may be NULL).
  * Walkers are processed in chunks sized by the gradient budget; every chunk
  * recomputes its forward activations.  Workspace: qmc_workspace_size(m, QMC_OP_GRAD, batch).
- * FermiNet and Psiformer models (for a Psiformer: the backward of the input
- * Dense, LayerNorms, attention, tanh MLP, orbitals, envelope and Jastrow,
- * src/jaqmc/app/molecule/wavefunction/psiformer.py:38-146). */
+ * FermiNet, Psiformer and LapNet models (for a Psiformer: the backward of
+ * the input Dense, LayerNorms, attention, tanh MLP, orbitals, envelope and
+ * Jastrow, src/jaqmc/app/molecule/wavefunction/psiformer.py:38-146; for
+ * LapNet: of both streams, the local updates, attention, value updates,
+ * orbitals, envelope and Jastrow, .../wavefunction/lapnet.py:27-140). */
 qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                     double* grad, float* logpsi, void* workspace, size_t workspace_bytes, cudaStream_t stream);
 

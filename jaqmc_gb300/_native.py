@@ -441,7 +441,8 @@ class NativePsiformer(NativeFermiNet):
 class NativeLapNet(NativeFermiNet):
     """A ``qmc_model`` handle for LapNet (+ SimpleEE Jastrow): the value path
     (``forward``, ``mh_steps``, ``mh_steps_resident``, ``mh_draws``), the
-    forward-Laplacian ``local_energy`` and ``ecp_energy``; no parameter adjoint."""
+    forward-Laplacian ``local_energy``, ``ecp_energy`` and the FP32 parameter
+    adjoint ``grad``."""
 
     def __init__(self, cfg, atoms, charges, precision="mixed", device=None):
         if getattr(cfg, "use_layernorm", False):

@@ -1031,17 +1031,93 @@ static PsiGradPlan make_psi_grad_plan(const qmc_model* m, int B) {
   return p;
 }
 
+static size_t attn_grad_total(const qmc_model* m, int B);
+
 static int psi_grad_chunk(const qmc_model* m, int B) {
-  const size_t one = make_psi_grad_plan(m, 1).total;
-  const size_t two = make_psi_grad_plan(m, 2).total;
+  const size_t one = attn_grad_total(m, 1);
+  const size_t two = attn_grad_total(m, 2);
   const size_t per = two > one ? two - one : one;
   const size_t c = m->grad_budget > one ? 1 + (m->grad_budget - one) / per : 1;
   return (int)std::max<size_t>(1, std::min<size_t>(c, (size_t)B));
 }
 
-size_t psi_grad_workspace(const qmc_model* m, int B) {
-  if (m->psi->d.arch != kArchPsiformer) return 0;
-  return make_psi_grad_plan(m, psi_grad_chunk(m, B)).total;
+size_t psi_grad_workspace(const qmc_model* m, int B) { return attn_grad_total(m, psi_grad_chunk(m, B)); }
+
+// Orbitals x envelope of an attention backbone's output hL [B n][D] into
+// amat (the raw orbitals kept in orb for the envelope cotangent).
+static qmc_status attn_orbitals_fwd(qmc_model* m, int B, void* ws, const float* hL, size_t amat, size_t orb,
+                                    size_t rae, size_t aevec, cudaStream_t s) {
+  const Dims& fd = m->d;
+  const ArenaLayout& fa = m->a;
+  const float* ar = m->arena;
+  const int n = fd.n, D = fd.d_last;
+  const int nch = fd.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
+    const int i0 = (fd.split && c == 1) ? fd.n_up : 0;
+    RowMap map{ns, i0, n, 1};
+    EpiOrbital epi{at<float>(ws, amat), at<float>(ws, rae), at<float>(ws, aevec), ar + fa.env_pi[c],
+                   ar + fa.env_sigma[c], n, fd.A, fd.K, 1, fd.env_abs};
+    epi.orb = at<float>(ws, orb);
+    epi.unit_env = !env_in_epilogue(fd.env_kind);
+    QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, hL, D, D, nullptr, 0, 0, ar + fa.w_orb[c], fd.norb_p,
+                                              fd.norb, epi));
+  }
+  if (fd.env_kind == QMC_ENVELOPE_DIAGONAL) {
+    const int c1 = nch - 1;
+    QMC_PROF(QMC_KC_ORBITAL, launch_envelope_diag(s, B, n, fd.n_up, fd.split, fd.K, fd.A, 1, 1, ar + fa.env_pi[0],
+                                                  ar + fa.env_sigma[0], ar + fa.env_pi[c1], ar + fa.env_sigma[c1],
+                                                  at<float>(ws, aevec), at<float>(ws, amat)));
+  }
+  return QMC_OK;
+}
+
+// Determinant, orbital and envelope backward of an attention backbone:
+// log|psi| (+ Jastrow) into lp, the orbital and envelope Jacobian rows, and
+// the cotangent hbar [B n][D] of the backbone output hL.
+static qmc_status attn_orbitals_bwd(qmc_model* m, int B, void* ws, const float* hL, size_t amat, size_t orb,
+                                    size_t abar, size_t envbar, size_t rae, size_t aevec, size_t orbbar, size_t jas,
+                                    float* hbar, float* J, float* lp, cudaStream_t s) {
+  const PsiParams& P = m->psi->p;
+  const Dims& fd = m->d;
+  const ArenaLayout& fa = m->a;
+  const float* ar = m->arena;
+  const int n = fd.n, D = fd.d_last;
+  const size_t rows = (size_t)B * n, Pn = P.total;
+  QMC_PROF(QMC_KC_LOGDET, launch_logdet_bwd(s, B, n, fd.K, at<float>(ws, amat), at<float>(ws, abar), lp));
+  const int nch = fd.split ? 2 : 1;
+  {
+    ::qmc::ProfScope ps_(QMC_KC_ORBITAL, s);
+    if (lp) {
+      k_psi_add_jas<<<blocks(B), 256, 0, s>>>(B, lp, at<float>(ws, jas));
+      QMC_CUDA(cudaGetLastError());
+    }
+    k_orb_bwd<<<blocks(rows * fd.norb_p), 256, 0, s>>>(
+        B, n, fd.n_up, fd.split, fd.K, fd.A, fd.env_abs, fd.env_kind, fd.norb_p, at<float>(ws, abar),
+        at<float>(ws, orb), at<float>(ws, rae), at<float>(ws, aevec), ar + fa.env_pi[0], ar + fa.env_sigma[0],
+        ar + fa.env_pi[nch - 1], ar + fa.env_sigma[nch - 1], at<float>(ws, orbbar), at<float>(ws, envbar));
+    QMC_CUDA(cudaGetLastError());
+  }
+  for (int c = 0; c < nch; ++c) {
+    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
+    const int i0 = (fd.split && c == 1) ? fd.n_up : 0;
+    ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
+    if (fd.env_kind == QMC_ENVELOPE_DIAGONAL)
+      k_env_jac_diag<<<blocks((size_t)B * n * fd.A * fd.K), 256, 0, s>>>(
+          B, n, i0, ns, fd.K, fd.A, at<float>(ws, envbar), at<float>(ws, aevec), ar + fa.env_pi[c],
+          ar + fa.env_sigma[c], J, Pn, P.env_pi[c], P.env_sigma[c]);
+    else if (fd.env_kind != QMC_ENVELOPE_NULL)
+      k_env_jac<<<blocks((size_t)B * n * fd.A * fd.K), 256, 0, s>>>(B, n, i0, ns, fd.K, fd.A, fd.env_abs,
+                                                                   at<float>(ws, envbar), at<float>(ws, rae),
+                                                                   ar + fa.env_pi[c], ar + fa.env_sigma[c], J, Pn,
+                                                                   P.env_pi[c], P.env_sigma[c]);
+    QMC_CUDA(cudaGetLastError());
+    QMC_CUDA(jac_outer(s, B, ns, n, i0, hL, D, D, at<float>(ws, orbbar), fd.norb_p, fd.norb, J, Pn, P.orb_k[c]));
+    RowMap map{ns, i0, n, 1};
+    QMC_CUDA(launch_gemm_simt(s, B * ns, map, at<float>(ws, orbbar), fd.norb_p, fd.norb_p, nullptr, 0, 0,
+                              ar + fa.wt_orb[c], D, D, EpiStore{hbar, D, nullptr}));
+  }
+  return QMC_OK;
 }
 
 static qmc_status psi_forward_save(qmc_model* m, const PsiGradPlan& p, void* ws, const float* electrons,
@@ -1106,26 +1182,7 @@ static qmc_status psi_forward_save(qmc_model* m, const PsiGradPlan& p, void* ws,
       din = d.mlp[k];
     }
   }
-  // orbitals x envelope (the raw orbitals kept for the envelope cotangent)
-  const int nch = fd.split ? 2 : 1;
-  for (int c = 0; c < nch; ++c) {
-    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
-    const int i0 = (fd.split && c == 1) ? fd.n_up : 0;
-    RowMap map{ns, i0, n, 1};
-    EpiOrbital epi{at<float>(ws, p.amat), at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + fa.env_pi[c],
-                   ar + fa.env_sigma[c], n, fd.A, fd.K, 1, fd.env_abs};
-    epi.orb = at<float>(ws, p.orb);
-    epi.unit_env = !env_in_epilogue(fd.env_kind);
-    QMC_PROF(QMC_KC_ORBITAL, launch_gemm_simt(s, B * ns, map, at<float>(ws, p.h[d.L]), D, D, nullptr, 0, 0,
-                                              ar + fa.w_orb[c], fd.norb_p, fd.norb, epi));
-  }
-  if (fd.env_kind == QMC_ENVELOPE_DIAGONAL) {
-    const int c1 = nch - 1;
-    QMC_PROF(QMC_KC_ORBITAL, launch_envelope_diag(s, B, n, fd.n_up, fd.split, fd.K, fd.A, 1, 1, ar + fa.env_pi[0],
-                                                  ar + fa.env_sigma[0], ar + fa.env_pi[c1], ar + fa.env_sigma[c1],
-                                                  at<float>(ws, p.aevec), at<float>(ws, p.amat)));
-  }
-  return QMC_OK;
+  return attn_orbitals_fwd(m, B, ws, at<float>(ws, p.h[d.L]), p.amat, p.orb, p.rae, p.aevec, s);
 }
 
 static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, const float* electrons, float* J,
@@ -1140,43 +1197,9 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
   const size_t rows = (size_t)B * n, Pn = P.total;
   const RowMap rmap{n, 0, n, 1};
   const unsigned wb = (unsigned)((rows + 7) / 8);
-  float* lp = logpsi;
-  QMC_PROF(QMC_KC_LOGDET, launch_logdet_bwd(s, B, n, fd.K, at<float>(ws, p.amat), at<float>(ws, p.abar), lp));
-  const int nch = fd.split ? 2 : 1;
-  {
-    ::qmc::ProfScope ps_(QMC_KC_ORBITAL, s);
-    if (lp) {
-      k_psi_add_jas<<<blocks(B), 256, 0, s>>>(B, lp, at<float>(ws, p.jas));
-      QMC_CUDA(cudaGetLastError());
-    }
-    k_orb_bwd<<<blocks(rows * fd.norb_p), 256, 0, s>>>(
-        B, n, fd.n_up, fd.split, fd.K, fd.A, fd.env_abs, fd.env_kind, fd.norb_p, at<float>(ws, p.abar),
-        at<float>(ws, p.orb), at<float>(ws, p.rae), at<float>(ws, p.aevec), ar + fa.env_pi[0], ar + fa.env_sigma[0],
-        ar + fa.env_pi[nch - 1], ar + fa.env_sigma[nch - 1], at<float>(ws, p.orbbar), at<float>(ws, p.envbar));
-    QMC_CUDA(cudaGetLastError());
-  }
   float* hbar = at<float>(ws, p.hbar);
-  for (int c = 0; c < nch; ++c) {
-    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
-    const int i0 = (fd.split && c == 1) ? fd.n_up : 0;
-    ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
-    if (fd.env_kind == QMC_ENVELOPE_DIAGONAL)
-      k_env_jac_diag<<<blocks((size_t)B * n * fd.A * fd.K), 256, 0, s>>>(
-          B, n, i0, ns, fd.K, fd.A, at<float>(ws, p.envbar), at<float>(ws, p.aevec), ar + fa.env_pi[c],
-          ar + fa.env_sigma[c], J, Pn, P.env_pi[c], P.env_sigma[c]);
-    else if (fd.env_kind != QMC_ENVELOPE_NULL)
-      k_env_jac<<<blocks((size_t)B * n * fd.A * fd.K), 256, 0, s>>>(B, n, i0, ns, fd.K, fd.A, fd.env_abs,
-                                                                   at<float>(ws, p.envbar), at<float>(ws, p.rae),
-                                                                   ar + fa.env_pi[c], ar + fa.env_sigma[c], J, Pn,
-                                                                   P.env_pi[c], P.env_sigma[c]);
-    QMC_CUDA(cudaGetLastError());
-    QMC_CUDA(jac_outer(s, B, ns, n, i0, at<float>(ws, p.h[d.L]), D, D,
-                                                              at<float>(ws, p.orbbar), fd.norb_p, fd.norb, J, Pn,
-                                                              P.orb_k[c]));
-    RowMap map{ns, i0, n, 1};
-    QMC_CUDA(launch_gemm_simt(s, B * ns, map, at<float>(ws, p.orbbar), fd.norb_p, fd.norb_p, nullptr, 0, 0,
-                              ar + fa.wt_orb[c], D, D, EpiStore{hbar, D, nullptr}));
-  }
+  QMC_TRY(attn_orbitals_bwd(m, B, ws, at<float>(ws, p.h[d.L]), p.amat, p.orb, p.abar, p.envbar, p.rae, p.aevec,
+                            p.orbbar, p.jas, hbar, J, logpsi, s));
   float* hmbar = at<float>(ws, p.hmbar);
   float* zbar = at<float>(ws, p.zbar);
   float* tmp = at<float>(ws, p.tmp);
@@ -1269,15 +1292,221 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
   return QMC_OK;
 }
 
+// ------------------------------------------------------------ LapNet adjoint
+// Saved activations of a chunk of B walkers: the individual stream hs before
+// each local update (hs[l][0] = the layer's query/key input), the update
+// outputs u = tanh(hs Wu + bu), the dense stream hd[l] (hd[L] = the backbone
+// output), q|k|v with biases, the attention probabilities and output, the
+// post-attention residual r and the value update y = tanh(r Wvu + bvu).
+struct LapGradPlan {
+  int B;
+  size_t x0, rae, aevec, jas;
+  size_t hs[kPsiMaxLayers][kLapMaxLocal + 1], u[kPsiMaxLayers][kLapMaxLocal], hd[kPsiMaxLayers + 1];
+  size_t qkv[kPsiMaxLayers], pr[kPsiMaxLayers], o[kPsiMaxLayers], r[kPsiMaxLayers], y[kPsiMaxLayers];
+  size_t amat, orb, abar, envbar, hbar, hsbar, zbar, obar, qkvbar, orbbar, J, total;
+};
+
+// y += x
+__global__ void k_add_to(size_t count, const float* __restrict__ x, float* __restrict__ y) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < count) y[e] += x[e];
+}
+
+static int lap_local(const PsiDims& d, int l) { return l + 1 < d.L ? d.n_local : 0; }
+
+static LapGradPlan make_lap_grad_plan(const qmc_model* m, int B) {
+  const PsiDims& d = m->psi->d;
+  LapGradPlan p{};
+  p.B = B;
+  size_t o = 0;
+  auto take = [&](size_t floats) { size_t r = o; o += align_up(floats * 4, 256); return r; };
+  const size_t rows = (size_t)B * d.n, D = d.D;
+  p.x0 = take(rows * d.K0p);
+  p.rae = take(rows * d.A);
+  p.aevec = take(rows * d.A * 3);
+  p.jas = take(B);
+  for (int l = 0; l <= d.L; ++l) p.hd[l] = take(rows * D);
+  for (int l = 0; l < d.L; ++l) {
+    for (int j = 0; j <= lap_local(d, l); ++j) p.hs[l][j] = take(rows * D);
+    for (int j = 0; j < lap_local(d, l); ++j) p.u[l][j] = take(rows * D);
+    p.qkv[l] = take(rows * 3 * D);
+    p.pr[l] = take((size_t)B * d.H * d.n * d.n);
+    p.o[l] = take(rows * D);
+    p.r[l] = take(rows * D);
+    p.y[l] = take(rows * D);
+  }
+  const size_t am = (size_t)B * d.K * d.n * d.n;
+  p.amat = take(am);
+  p.orb = take(am);
+  p.abar = take(am);
+  p.envbar = take(am);
+  p.hbar = take(rows * D);
+  p.hsbar = take(rows * D);
+  p.zbar = take(rows * D);
+  p.obar = take(rows * D);
+  p.qkvbar = take(rows * 3 * D);
+  p.orbbar = take(rows * m->d.norb_p);
+  p.J = take((size_t)B * m->psi->p.total);
+  p.total = o;
+  return p;
+}
+
+static qmc_status lap_forward_save(qmc_model* m, const LapGradPlan& p, void* ws, const float* electrons,
+                                   cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const ArenaLayout& fa = m->a;
+  const float* ar = m->arena;
+  const int B = p.B, n = d.n, D = d.D;
+  const size_t rows = (size_t)B * n;
+  const RowMap rmap{n, 0, n, 1};
+  QMC_PROF(QMC_KC_FEATURES, launch_psi_features(s, B, n, d.n_up, d.A, d.K0p, electrons, ar + fa.atoms,
+                                                d.jastrow ? ar + P.alpha_par : nullptr, at<float>(ws, p.x0),
+                                                at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, p.jas)));
+  QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.x0), d.K0p, d.K0p, nullptr, 0, 0,
+                                           ar + a.w_in, D, D, EpiStore{at<float>(ws, p.hd[0]), D, ar + a.lb_in}));
+  QMC_CUDA(cudaMemcpyAsync(at<float>(ws, p.hs[0][0]), at<float>(ws, p.hd[0]), sizeof(float) * rows * D,
+                           cudaMemcpyDeviceToDevice, s));
+  for (int l = 0; l < d.L; ++l) {
+    float* qkv = at<float>(ws, p.qkv[l]);
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.hs[l][0]), D, D, nullptr, 0, 0,
+                                                   ar + P.qk_k[l], 2 * D, 2 * D,
+                                                   EpiStore{qkv, 3 * D, ar + a.b_qkv[l]}));
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.hd[l]), D, D, nullptr, 0, 0,
+                                                   ar + P.lv_k[l], D, D,
+                                                   EpiStore{qkv + 2 * D, 3 * D, ar + a.b_qkv[l] + 2 * D}));
+    const int nl = lap_local(d, l);
+    for (int j = 0; j < nl; ++j) {
+      float* u = at<float>(ws, p.u[l][j]);
+      QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.hs[l][j]), D, D, nullptr, 0,
+                                                     0, ar + P.ul_k[l][j], D, D, EpiStore{u, D, ar + a.lb_ul[l][j]}));
+      // u = tanh(u); next hs = hs + u (into the next layer's first state after the last update)
+      float* next = j + 1 < nl ? at<float>(ws, p.hs[l][j + 1]) : at<float>(ws, p.hs[l + 1][0]);
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_psi_tanh_add<<<blocks(rows * D), 256, 0, s>>>(rows * D, u, at<float>(ws, p.hs[l][j]), next, 1);
+      QMC_CUDA(cudaGetLastError());
+    }
+    if (nl == 0 && l + 1 < d.L)
+      QMC_CUDA(cudaMemcpyAsync(at<float>(ws, p.hs[l + 1][0]), at<float>(ws, p.hs[l][0]), sizeof(float) * rows * D,
+                               cudaMemcpyDeviceToDevice, s));
+    {
+      ::qmc::ProfScope ps_(QMC_KC_PAIR, s);
+      const size_t sm = sizeof(float) * (3 * (size_t)n * d.Dh + (size_t)n * n);
+      k_psi_attn_save<<<B * d.H, 128, sm, s>>>(n, d.H, d.Dh, qkv, at<float>(ws, p.pr[l]), at<float>(ws, p.o[l]));
+      QMC_CUDA(cudaGetLastError());
+    }
+    float* r = at<float>(ws, p.r[l]);
+    float* y = at<float>(ws, p.y[l]);
+    // r = hd + o Wo + bo
+    QMC_CUDA(cudaMemcpyAsync(r, at<float>(ws, p.hd[l]), sizeof(float) * rows * D, cudaMemcpyDeviceToDevice, s));
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, at<float>(ws, p.o[l]), D, D, nullptr, 0, 0,
+                                                   ar + P.lo_k[l], D, D, EpiStore{r, D, ar + a.lb_o[l], 1}));
+    QMC_PROF(QMC_KC_STREAM_LAYER, launch_gemm_simt(s, B * n, rmap, r, D, D, nullptr, 0, 0, ar + P.vu_k[l], D, D,
+                                                   EpiStore{y, D, ar + a.lb_vu[l]}));
+    {
+      ::qmc::ProfScope ps_(QMC_KC_MEANS, s);
+      k_psi_tanh_add<<<blocks(rows * D), 256, 0, s>>>(rows * D, y, r, at<float>(ws, p.hd[l + 1]), 1);
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  return attn_orbitals_fwd(m, B, ws, at<float>(ws, p.hd[d.L]), p.amat, p.orb, p.rae, p.aevec, s);
+}
+
+static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, const float* electrons, float* J,
+                               float* logpsi, cudaStream_t s) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const PsiArena& a = m->psi->a;
+  const float* ar = m->arena;
+  const int B = p.B, n = d.n, D = d.D;
+  const size_t rows = (size_t)B * n, Pn = P.total;
+  const RowMap rmap{n, 0, n, 1};
+  float* hbar = at<float>(ws, p.hbar);    // cotangent of the dense stream
+  float* hsbar = at<float>(ws, p.hsbar);  // cotangent of the individual stream
+  float* zbar = at<float>(ws, p.zbar);
+  float* obar = at<float>(ws, p.obar);
+  float* qkvbar = at<float>(ws, p.qkvbar);
+  QMC_TRY(attn_orbitals_bwd(m, B, ws, at<float>(ws, p.hd[d.L]), p.amat, p.orb, p.abar, p.envbar, p.rae, p.aevec,
+                            p.orbbar, p.jas, hbar, J, logpsi, s));
+  QMC_CUDA(cudaMemsetAsync(hsbar, 0, sizeof(float) * rows * D, s));
+  auto bias_rows = [&](const float* z, int ldz, int N, size_t off) -> qmc_status {
+    if (!d.bb_bias) return QMC_OK;
+    k_colsum<<<blocks((size_t)B * N), 256, 0, s>>>(B, n, z, ldz, N, nullptr, J, Pn, off);
+    QMC_CUDA(cudaGetLastError());
+    return QMC_OK;
+  };
+  for (int l = d.L - 1; l >= 0; --l) {
+    ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
+    // hd[l+1] = r + y, y = tanh(r Wvu + bvu): rbar = hbar + zbar Wvu^T, zbar = hbar (1 - y^2)
+    const float* r = at<float>(ws, p.r[l]);
+    k_tanh_bwd<<<blocks(rows * D), 256, 0, s>>>(rows * D, 1.f, hbar, at<float>(ws, p.y[l]), zbar);
+    QMC_CUDA(cudaGetLastError());
+    QMC_CUDA(jac_outer(s, B, n, n, 0, r, D, D, zbar, D, D, J, Pn, P.vu_k[l]));
+    QMC_TRY(bias_rows(zbar, D, D, P.vu_b[l]));
+    QMC_CUDA(launch_gemm_simt(s, B * n, rmap, zbar, D, D, nullptr, 0, 0, ar + a.t32_vu[l], D, D,
+                              EpiStore{hbar, D, nullptr, 1}));  // hbar now holds rbar
+    // r = hd[l] + o Wo + bo
+    QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.o[l]), D, D, hbar, D, D, J, Pn, P.lo_k[l]));
+    QMC_TRY(bias_rows(hbar, D, D, P.lo_b[l]));
+    QMC_CUDA(launch_gemm_simt(s, B * n, rmap, hbar, D, D, nullptr, 0, 0, ar + a.t32_o[l], D, D,
+                              EpiStore{obar, D, nullptr}));
+    {
+      ::qmc::ProfScope ps2_(QMC_KC_PAIR, s);
+      const size_t sm = sizeof(float) * (4 * (size_t)n * d.Dh + 2 * (size_t)n * n);
+      k_psi_attn_bwd<<<B * d.H, 128, sm, s>>>(n, d.H, d.Dh, at<float>(ws, p.qkv[l]), at<float>(ws, p.pr[l]), obar,
+                                              qkvbar);
+      QMC_CUDA(cudaGetLastError());
+    }
+    // v = hd[l] Wv + bv: hd[l]'s cotangent = rbar (residual) + vbar Wv^T
+    const float* hd = at<float>(ws, p.hd[l]);
+    QMC_CUDA(jac_outer(s, B, n, n, 0, hd, D, D, qkvbar + 2 * D, 3 * D, D, J, Pn, P.lv_k[l]));
+    QMC_TRY(bias_rows(qkvbar + 2 * D, 3 * D, D, P.lv_b[l]));
+    QMC_CUDA(launch_gemm_simt(s, B * n, rmap, qkvbar + 2 * D, 3 * D, D, nullptr, 0, 0, ar + a.t32_v[l], D, D,
+                              EpiStore{hbar, D, nullptr, 1}));
+    // local updates, last first: hs_{j+1} = hs_j + u_j, u_j = tanh(hs_j Wu_j + bu_j)
+    for (int j = lap_local(d, l) - 1; j >= 0; --j) {
+      k_tanh_bwd<<<blocks(rows * D), 256, 0, s>>>(rows * D, 1.f, hsbar, at<float>(ws, p.u[l][j]), zbar);
+      QMC_CUDA(cudaGetLastError());
+      QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.hs[l][j]), D, D, zbar, D, D, J, Pn, P.ul_k[l][j]));
+      QMC_TRY(bias_rows(zbar, D, D, P.ul_b[l][j]));
+      QMC_CUDA(launch_gemm_simt(s, B * n, rmap, zbar, D, D, nullptr, 0, 0, ar + a.t32_ul[l][j], D, D,
+                                EpiStore{hsbar, D, nullptr, 1}));
+    }
+    // q|k = hs[l][0] Wqk + bqk
+    QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.hs[l][0]), D, D, qkvbar, 3 * D, 2 * D, J, Pn, P.qk_k[l]));
+    QMC_TRY(bias_rows(qkvbar, 3 * D, 2 * D, P.qk_b[l]));
+    QMC_CUDA(launch_gemm_simt(s, B * n, rmap, qkvbar, 3 * D, 2 * D, nullptr, 0, 0, ar + a.t32_qkv[l], D, D,
+                              EpiStore{hsbar, D, nullptr, 1}));
+  }
+  {
+    // both streams start as the input projection
+    ::qmc::ProfScope ps_(QMC_KC_LAYER0, s);
+    k_add_to<<<blocks(rows * D), 256, 0, s>>>(rows * D, hsbar, hbar);
+    QMC_CUDA(cudaGetLastError());
+    QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.x0), d.K0p, d.K0, hbar, D, D, J, Pn, P.in_k));
+    if (d.in_bias) {
+      k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hbar, D, D, nullptr, J, Pn, P.in_b);
+      QMC_CUDA(cudaGetLastError());
+    }
+    if (d.jastrow) {
+      k_psi_jas_jac<<<blocks(B), 256, 0, s>>>(B, n, d.n_up, electrons, ar + P.alpha_par, J, Pn, P.alpha_par,
+                                              P.alpha_anti);
+      QMC_CUDA(cudaGetLastError());
+    }
+  }
+  return QMC_OK;
+}
+
+static size_t attn_grad_total(const qmc_model* m, int B) {
+  return m->psi->d.arch == kArchLapNet ? make_lap_grad_plan(m, B).total : make_psi_grad_plan(m, B).total;
+}
+
 qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                         double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
   const PsiDims& pd = m->psi->d;
-  if (pd.arch != kArchPsiformer) {
-    set_error("the parameter adjoint is built for FermiNet and Psiformer models (not LapNet)");
-    return QMC_ERR_UNSUPPORTED;
-  }
   if (pd.n > 64 || pd.Dh > 64) {
-    set_error("the Psiformer adjoint supports at most 64 electrons and head width 64");
+    set_error("the attention-backbone adjoint supports at most 64 electrons and head width 64");
     return QMC_ERR_SHAPE;
   }
   {
@@ -1291,9 +1520,9 @@ qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const d
     }
   }
   const int chunk = psi_grad_chunk(m, batch);
-  const PsiGradPlan p = make_psi_grad_plan(m, chunk);
-  if (ws_bytes < p.total) {
-    set_error("workspace too small for the adjoint: %zu bytes given, %zu needed", ws_bytes, p.total);
+  const size_t need = attn_grad_total(m, chunk);
+  if (ws_bytes < need) {
+    set_error("workspace too small for the adjoint: %zu bytes given, %zu needed", ws_bytes, need);
     return QMC_ERR_WORKSPACE;
   }
   const size_t P = m->psi->p.total;
@@ -1301,13 +1530,20 @@ qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const d
   if (grad) QMC_CUDA(cudaMemsetAsync(grad, 0, P * sizeof(double), s));
   for (int w0 = 0; w0 < batch; w0 += chunk) {
     const int B = std::min(chunk, batch - w0);
-    const PsiGradPlan q = make_psi_grad_plan(m, B);
-    float* J = per_walker ? per_walker + (size_t)w0 * P : at<float>(ws, q.J);
+    const bool lapnet = pd.arch == kArchLapNet;
+    const PsiGradPlan q = lapnet ? PsiGradPlan{} : make_psi_grad_plan(m, B);
+    const LapGradPlan ql = lapnet ? make_lap_grad_plan(m, B) : LapGradPlan{};
+    float* J = per_walker ? per_walker + (size_t)w0 * P : at<float>(ws, lapnet ? ql.J : q.J);
     // parameters without a term (the Jastrow when it is off) stay zero
     QMC_CUDA(cudaMemsetAsync(J, 0, sizeof(float) * B * P, s));
     const float* x = electrons + (size_t)w0 * n * 3;
-    QMC_TRY(psi_forward_save(m, q, ws, x, s));
-    QMC_TRY(psi_backward(m, q, ws, x, J, logpsi ? logpsi + w0 : nullptr, s));
+    if (lapnet) {
+      QMC_TRY(lap_forward_save(m, ql, ws, x, s));
+      QMC_TRY(lap_backward(m, ql, ws, x, J, logpsi ? logpsi + w0 : nullptr, s));
+    } else {
+      QMC_TRY(psi_forward_save(m, q, ws, x, s));
+      QMC_TRY(psi_backward(m, q, ws, x, J, logpsi ? logpsi + w0 : nullptr, s));
+    }
     if (grad && weights) {
       ::qmc::ProfScope ps_(QMC_KC_OTHER, s);
       k_weighted_sum<<<blocks(P), 256, 0, s>>>(B, P, J, weights + w0, grad);

@@ -904,10 +904,6 @@ qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const doubl
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1 || !electrons) { set_error("bad batch/electrons"); return QMC_ERR_ARG; }
-  if (m->kind == QMC_KIND_PSIFORMER && m->psi->d.arch != kArchPsiformer) {
-    set_error("the parameter adjoint is built for FermiNet and Psiformer models (not LapNet)");
-    return QMC_ERR_UNSUPPORTED;
-  }
   if (!per_walker && !grad) { set_error("nothing to compute: per_walker and grad are both null"); return QMC_ERR_ARG; }
   if (grad && !weights) { set_error("grad needs per-walker weights"); return QMC_ERR_ARG; }
   if (!ws) { set_error("null workspace"); return QMC_ERR_WORKSPACE; }

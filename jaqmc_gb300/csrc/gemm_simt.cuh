@@ -35,6 +35,7 @@ struct EpiStore {
   float* out;
   int ld;
   const float* bias;
+  int accumulate = 0;  // out += result instead of out = result
   __device__ void operator()(const float* Cs, int ng, int g0, int n0, int N, const RowMap& m) const {
     const int Tp = m.Tp;
     for (int p = threadIdx.x; p < ng * Tp * kBN; p += blockDim.x) {
@@ -43,7 +44,8 @@ struct EpiStore {
       int lg = r / Tp, t = r % Tp;
       float v = Cs[r * kCsLd + c];
       if (bias) v += bias[col];
-      out[m.row(g0 + lg, t) * ld + col] = v;
+      float* o = out + m.row(g0 + lg, t) * ld + col;
+      *o = accumulate ? *o + v : v;
     }
   }
 };

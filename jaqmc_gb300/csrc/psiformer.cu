@@ -733,9 +733,14 @@ qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s) {
     QMC_CUDA(launch_transpose_split(s, ar + P.lv_k[l], D, D, D, ab + a.t_v[l], D, D));
     QMC_CUDA(launch_transpose_split(s, ar + P.lo_k[l], D, D, D, ab + a.t_o[l], D, D));
     QMC_CUDA(launch_transpose_split(s, ar + P.vu_k[l], D, D, D, ab + a.t_vu[l], D, D));
+    QMC_CUDA(launch_transpose_f32(s, ar + P.qk_k[l], D, 2 * D, 2 * D, ar + a.t32_qkv[l]));
+    QMC_CUDA(launch_transpose_f32(s, ar + P.lv_k[l], D, D, D, ar + a.t32_v[l]));
+    QMC_CUDA(launch_transpose_f32(s, ar + P.lo_k[l], D, D, D, ar + a.t32_o[l]));
+    QMC_CUDA(launch_transpose_f32(s, ar + P.vu_k[l], D, D, D, ar + a.t32_vu[l]));
     for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) {
       if (d.bb_bias) QMC_CUDA(copy(a.lb_ul[l][j], P.ul_b[l][j], D));
       QMC_CUDA(launch_transpose_split(s, ar + P.ul_k[l][j], D, D, D, ab + a.t_ul[l][j], D, D));
+      QMC_CUDA(launch_transpose_f32(s, ar + P.ul_k[l][j], D, D, D, ar + a.t32_ul[l][j]));
     }
   }
   if (d.arch == kArchLapNet && d.in_bias) QMC_CUDA(copy(a.lb_in, P.in_b, D));
@@ -857,7 +862,14 @@ static qmc_status psi_layout_alloc(qmc_model* m, int env_kind, const float* atom
       a.b_qkv[l] = takea((size_t)3 * D);
       a.lb_o[l] = takea(D);
       a.lb_vu[l] = takea(D);
-      for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) a.lb_ul[l][j] = takea(D);
+      a.t32_qkv[l] = takea((size_t)2 * D * D);
+      a.t32_o[l] = takea((size_t)D * D);
+      a.t32_v[l] = takea((size_t)D * D);
+      a.t32_vu[l] = takea((size_t)D * D);
+      for (int j = 0; l + 1 < d.L && j < d.n_local; ++j) {
+        a.lb_ul[l][j] = takea(D);
+        a.t32_ul[l][j] = takea((size_t)D * D);
+      }
     }
   }
   for (int l = 0; d.arch == kArchPsiformer && l < d.L; ++l) {

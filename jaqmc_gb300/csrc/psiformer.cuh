@@ -60,6 +60,8 @@ struct PsiArena {
   // LapNet: biases (zero when the model has none): input, output,
   // value-update and local-update projections; b_qkv holds query|key|value
   size_t lb_in, lb_o[kPsiMaxLayers], lb_vu[kPsiMaxLayers], lb_ul[kPsiMaxLayers][kLapMaxLocal];
+  // LapNet FP32 transposes for the adjoint ([dout][din]; t32_qkv holds query|key, t32_o the output)
+  size_t t32_v[kPsiMaxLayers], t32_vu[kPsiMaxLayers], t32_ul[kPsiMaxLayers][kLapMaxLocal];
   size_t total;
   size_t t_qkv[kPsiMaxLayers];    // [3D][D] (LapNet: query|key [2D][D])
   size_t t_o[kPsiMaxLayers];      // [D][D]

@@ -138,7 +138,7 @@ class PsiformerWavefunction(FermiNetWavefunction):
     """``PsiformerWavefunction``-shaped front end (``src/jaqmc/app/molecule/
     wavefunction/psiformer.py:38-146``) over the same three custom calls: the
     library's Psiformer handle serves log|psi|, MH steps and the
-    forward-Laplacian local energy (no parameter adjoint).  UNTESTED."""
+    forward-Laplacian local energy.  UNTESTED."""
 
     def __init__(self, nspins=(1, 1), ndets=16, num_layers=4, num_heads=4, heads_dim=64, mlp_hidden_dims=(256,),
                  envelope="abs_isotropic", orbitals_spin_split=True, jastrow="simple_ee", precision="mixed"):
@@ -167,6 +167,42 @@ class PsiformerWavefunction(FermiNetWavefunction):
         A = np.asarray(data.atoms).reshape(-1, 3).shape[0]
         seed = int(np.asarray(rngs).ravel()[-1]) if rngs is not None else 0
         return jnp.asarray(P.flatten(P.init_psiformer(self.cfg, A, seed=seed), P.psiformer_leaves(self.cfg, A)))
+
+
+class LapNetWavefunction(FermiNetWavefunction):
+    """``LapNetWavefunction``-shaped front end (``src/jaqmc/app/molecule/
+    wavefunction/lapnet.py:27-140``) over the same custom calls on the
+    library's LapNet handle.  UNTESTED."""
+
+    def __init__(self, nspins=(1, 1), ndets=16, num_layers=4, num_heads=4, heads_dim=64, use_layernorm=False,
+                 jastrow="simple_ee", use_input_bias=True, use_backbone_bias=True, num_local_updates=2,
+                 envelope="abs_isotropic", precision="mixed"):
+        from . import params as P
+        self.cfg = P.LapNetConfig(nspins=tuple(nspins), ndets=ndets, num_layers=num_layers, num_heads=num_heads,
+                                  heads_dim=heads_dim, use_layernorm=use_layernorm, jastrow=jastrow,
+                                  use_input_bias=use_input_bias, use_backbone_bias=use_backbone_bias,
+                                  num_local_updates=num_local_updates, envelope=envelope)
+        self.precision = precision
+        self._models = {}
+
+    def model(self, data):
+        import numpy as np
+
+        from . import _native
+        key = (np.asarray(data.atoms).tobytes(), np.asarray(data.charges).tobytes())
+        if key not in self._models:
+            self._models[key] = _native.NativeLapNet(self.cfg, np.asarray(data.atoms), np.asarray(data.charges),
+                                                     precision=self.precision)
+        return self._models[key]
+
+    def init_params(self, data, rngs):
+        import jax.numpy as jnp
+        import numpy as np
+
+        from . import params as P
+        A = np.asarray(data.atoms).reshape(-1, 3).shape[0]
+        seed = int(np.asarray(rngs).ravel()[-1]) if rngs is not None else 0
+        return jnp.asarray(P.flatten(P.init_lapnet(self.cfg, A, seed=seed), P.lapnet_leaves(self.cfg, A)))
 
 
 class EuclideanKinetic:

@@ -216,8 +216,9 @@ class LapNetWavefunction(FermiNetWavefunction):
     """LapNet ansatz with the SimpleEE Jastrow (hyper-parameters and defaults
     of ``src/jaqmc/app/molecule/wavefunction/lapnet.py:27-75``), evaluated by
     the GB300 library: log|psi|, the MH sampler, the forward-Laplacian local
-    energy and the ECP estimator.  ``use_layernorm`` and the parameter adjoint
-    are not built (``LossAndGrad`` raises)."""
+    energy, the ECP estimator and the FP32 parameter adjoint (``LossAndGrad``;
+    at most 64 electrons, head width <= 64).  ``use_layernorm`` is not
+    built."""
 
     num_layers: int = 4
     num_heads: int = 4

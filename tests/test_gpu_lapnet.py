@@ -7,7 +7,9 @@ form) / 1e-3 (split-BF16 form) with tails held to a small multiple of the
 oracle's own FP32 error; per-walker E_L within 1e-4 Ha for the bulk of the
 walkers (FP32 form), batch mean without bias beyond four standard errors
 (split-BF16 form); potential within 1e-5 relative; MH accept masks
-bit-exact away from near ties (|log ratio - log u| < 1e-6)."""
+bit-exact away from near ties (|log ratio - log u| < 1e-6); the FP32
+parameter adjoint against autograd of the FP64 oracle and central
+differences."""
 import json
 import os
 
@@ -182,13 +184,96 @@ def test_mh_matches_oracle(cuda_device):
     np.testing.assert_allclose(lpg.cpu().numpy()[keep], lpo.numpy()[keep], rtol=1e-4, atol=1e-4)
 
 
-def test_adjoint_is_reported_unsupported(cuda_device):
-    mol = S.lithium()
+def _oracle_jacobian(tree, cfg, mol, x):
+    """(B, P) FP64 d log|psi_w| / d theta by torch autograd of the oracle (the
+    role of the reference's jax.grad), in the flat leaf order."""
+    leaves = P.lapnet_leaves(cfg, mol.n_atoms)
+    ts, tr = [], {}
+    for path, shape in leaves:
+        t = torch.tensor(np.asarray(P._get(tree, path), np.float64), requires_grad=True)
+        ts.append(t)
+        node = tr.setdefault("params", {})
+        for k in path[:-1]:
+            node = node.setdefault(k, {})
+        node[path[-1]] = t
+    lp = OL.evaluate(tr, _ocfg(cfg), torch.as_tensor(x, dtype=torch.float64), mol.atoms)["logpsi"]
+    rows = []
+    for w in range(lp.shape[0]):
+        g = torch.autograd.grad(lp[w], ts, retain_graph=True, allow_unused=True)
+        rows.append(torch.cat([(gi if gi is not None else torch.zeros_like(t)).reshape(-1) for gi, t in zip(g, ts)]))
+    return torch.stack(rows).numpy(), lp.detach().numpy()
+
+
+@pytest.mark.parametrize("case", ["Li", "CH4", "CH4-nobias-1update", "Li-diagonal-3layers"])
+def test_parameter_adjoint_matches_autograd(case, cuda_device):
+    """Per-walker d log|psi| / d theta of LapNet (input projection, query/key,
+    value, output and value-update projections, local updates of the
+    individual stream, orbitals, envelope, Jastrow) against autograd of the
+    FP64 oracle: norm-wise relative error per walker <= 1e-4 (median), every
+    parameter leaf covered, and the weighted sum equal to J^T c."""
+    system = case.split("-")[0]
+    mol = S.SYSTEMS[system]()
+    kw = dict(SMALL)
+    if "nobias" in case:
+        kw.update(use_input_bias=False, use_backbone_bias=False, num_local_updates=1, jastrow="none")
+    if "diagonal" in case:
+        kw.update(envelope="diagonal", num_layers=3)
+    cfg = P.LapNetConfig(nspins=mol.nspins, **kw)
+    m, tree, x = _setup(mol, cfg, 5, cuda_device, "fp32")
+    xd = torch.as_tensor(x, device=cuda_device)
+    J, _, lp = m.grad(xd, per_walker=True)
+    Jr, lpr = _oracle_jacobian(tree, cfg, mol, x)
+    Jg = J.double().cpu().numpy()
+    rel = np.linalg.norm(Jg - Jr, axis=1) / np.linalg.norm(Jr, axis=1)
+    _record(f"lapnet_adjoint/{case}", {"rel_median": float(np.median(rel)), "rel_max": float(rel.max())})
+    # log|psi| to the forward parity bar: 1e-5 relative, or the FP32
+    # oracle's own error on a badly conditioned walker
+    r32 = _oracle(tree, cfg, mol, x, torch.float32, tangents=False)["logpsi"]
+    _check_logpsi(lp.cpu().double().numpy(), lpr, r32, 1e-5)
+    assert np.median(rel) <= 1e-4 and rel.max() <= 2e-3, rel
+    off = 0
+    scale = np.abs(Jr).max()
+    for path, shape in P.lapnet_leaves(cfg, mol.n_atoms):
+        size = int(np.prod(shape))
+        blk, ref = Jg[:, off:off + size], Jr[:, off:off + size]
+        assert np.abs(blk - ref).max() <= 1e-3 * scale + 1e-3 * np.abs(ref).max(), path
+        off += size
+    c = torch.linspace(-1.0, 1.0, 5, dtype=torch.float64)
+    _, g, _ = m.grad(xd, weights=c)
+    ref = (J.double().cpu() * c[:, None]).sum(0).numpy()
+    np.testing.assert_allclose(g.cpu().numpy(), ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())
+
+
+def test_parameter_adjoint_finite_differences_and_chunks(cuda_device):
+    """CH4 LapNet: 32 seeded entries of the per-walker Jacobian against FP64
+    central differences of the oracle (step 1e-4), and the same Jacobian when
+    a small gradient budget splits the batch into recomputed chunks."""
+    mol = S.methane()
     cfg = P.LapNetConfig(nspins=mol.nspins, **SMALL)
-    m, _, x = _setup(mol, cfg, 4, cuda_device, "fp32")
-    assert m.workspace(_native.OP_GRAD, 4)[1] == 0
-    with pytest.raises(_native.QmcError, match="LapNet"):
-        m.grad(torch.as_tensor(x, device=cuda_device), weights=torch.ones(4, dtype=torch.float64, device=cuda_device))
+    m, tree, x = _setup(mol, cfg, 3, cuda_device, "fp32")
+    xd = torch.as_tensor(x, device=cuda_device)
+    J, _, _ = m.grad(xd, per_walker=True)
+    leaves = P.lapnet_leaves(cfg, mol.n_atoms)
+    base = P.flatten(tree, leaves).astype(np.float64)
+    rng = np.random.default_rng(32)
+    idx = rng.choice(base.size, 32, replace=False)
+    h = 1e-4
+    fd = np.zeros((3, idx.size))
+    for k, p_ in enumerate(idx):
+        vals = []
+        for sgn in (1.0, -1.0):
+            v = base.copy()
+            v[p_] += sgn * h
+            vals.append(OL.evaluate(P.unflatten(v, leaves), _ocfg(cfg), torch.as_tensor(x, dtype=torch.float64),
+                                    mol.atoms)["logpsi"].numpy())
+        fd[:, k] = (vals[0] - vals[1]) / (2 * h)
+    Jn = J.double().cpu().numpy()
+    scale = np.abs(Jn).max(axis=1, keepdims=True)
+    assert (np.abs(Jn[:, idx] - fd) / scale).max() <= 1e-3
+    one = m.lib.qmc_workspace_size(m.h, _native.OP_GRAD, 1)
+    m.set_grad_budget(one + one // 2)  # one walker per chunk
+    J2, _, _ = m.grad(xd, per_walker=True)
+    torch.testing.assert_close(J2, J, rtol=0, atol=0)
 
 
 def test_host_mirror_evaluation_stage(cuda_device, tmp_path):

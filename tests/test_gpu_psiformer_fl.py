@@ -117,24 +117,65 @@ def test_chunked_equals_whole(precision, cuda_device):
 
 def test_benzene_full_config(cuda_device):
     """The benzene configuration (21+21 electrons, 12 atoms, 4 layers of 4 x 64
-    heads, MLP 256, K = 16; T = 128 tangents per electron), both forms."""
+    heads, MLP 256, K = 16; T = 128 tangents per electron) on 16 walkers
+    burnt in from |psi|^2, both forms against the FP64 oracle.
+
+    FP32 form: per-walker |dE_L| median within 3x the FP32 oracle's own
+    median (+ 0.1 mHa) and maximum within 3x its maximum (+ 1 mHa); batch mean
+    within four paired standard errors (+ 0.1 mHa).
+    Split-BF16 form: its error is the rounding of the GEMM operands to hi + lo
+    bf16 (about 2^-17 relative), which the kinetic energy amplifies to mHa
+    per walker on this system.  The oracle with that operand rounding
+    emulated (oracle/lap.py split_bf16_gemms) states the size to expect: the
+    per-walker median within 3x the emulation's (+ 1 mHa), the maximum within
+    5x (+ 10 mHa), and the batch mean unbiased: within max(0.5 mHa, 4 paired
+    standard errors) of FP64."""
+    from oracle import lap
     mol = S.benzene()
     cfg = P.PsiformerConfig(nspins=mol.nspins)
-    B = 2
-    r64 = None
-    for precision, tol in (("fp32", 2e-3), ("mixed", 2e-2)):
-        m, tree, x = _setup(mol, cfg, B, cuda_device, precision)
-        out = m.local_energy(torch.as_tensor(x, device=cuda_device))
+    B = 16
+    tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
+    flat = torch.as_tensor(P.flatten(tree, P.psiformer_leaves(cfg, mol.n_atoms)), device=cuda_device)
+    models = {}
+    for precision in ("mixed", "fp32"):
+        m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision=precision, device=cuda_device)
+        m.set_params(flat)
+        models[precision] = m
+    xd = torch.as_tensor(S.init_walkers(mol, 256, seed=1), device=cuda_device)
+    models["mixed"].mh_steps(xd, 200, 0.15, 1000, 0)
+    xd = xd[:B].contiguous()
+    x = xd.cpu().numpy()
+    r64 = _oracle(tree, cfg, mol, x, torch.float64)
+    r32 = _oracle(tree, cfg, mol, x, torch.float32)
+    K0 = 4 * mol.n_atoms + 1
+    with lap.split_bf16_gemms(lambda W: W.shape[0] != K0):
+        remu = _oracle(tree, cfg, mol, x, torch.float64)
+    ref = r64["e_local"]
+    e32 = np.abs(r32["e_local"] - ref)
+    eemu = np.abs(remu["e_local"] - ref)
+    for precision, m in models.items():
+        out = m.local_energy(xd)
         assert m.check_error() == 0
-        if r64 is None:
-            r64 = _oracle(tree, cfg, mol, x, torch.float64)
         got = out["e_local"].cpu().double().numpy()
-        err = np.abs(got - r64["e_local"])
+        d = got - ref
+        err = np.abs(d)
+        se = d.std(ddof=1) / np.sqrt(B)
         _record(f"psiformer_local_energy/C6H6/{precision}",
-                {"max_abs": float(err.max()), "rel": float((err / np.abs(r64["e_local"])).max()), "n": B})
+                {"max_abs": float(err.max()), "median_abs": float(np.median(err)), "mean_err": float(d.mean()),
+                 "paired_se": float(se), "oracle32_median_abs": float(np.median(e32)),
+                 "oracle32_max_abs": float(e32.max()), "emulated_median_abs": float(np.median(eemu)),
+                 "emulated_max_abs": float(eemu.max()), "n": B})
         assert np.isfinite(got).all()
-        assert (err / np.maximum(1.0, np.abs(r64["e_local"]))).max() < tol, (got, r64["e_local"])
-        np.testing.assert_allclose(out["logpsi"].cpu().numpy(), r64["logpsi"], rtol=1e-3)
+        np.testing.assert_allclose(out["logpsi"].cpu().numpy(), r64["logpsi"], rtol=1e-4 if precision == "fp32"
+                                   else 1e-3)
+        if precision == "fp32":
+            assert np.median(err) <= 3 * np.median(e32) + 1e-4, (np.median(err), np.median(e32))
+            assert err.max() <= 3 * e32.max() + 1e-3, (err.max(), e32.max())
+            assert abs(d.mean()) <= 4 * se + 1e-4, (d.mean(), se)
+        else:
+            assert np.median(err) <= 3 * np.median(eemu) + 1e-3, (np.median(err), np.median(eemu))
+            assert err.max() <= 5 * eemu.max() + 1e-2, (err.max(), eemu.max())
+            assert abs(d.mean()) <= max(5e-4, 4 * se), (d.mean(), se)
 
 
 def test_host_mirror_evaluation_stage(cuda_device, tmp_path):
