@@ -114,6 +114,12 @@ template <class Out>
 cudaError_t launch_psi_attention_fl(cudaStream_t s, int B, int n, int Tp, int T, int H, int Dh, const float* qkv,
                                     const float* bqkv, Out out);
 bool psi_attention_fl_supported(int n, int Dh);
+// The split-BF16 warp-MMA variant of the forward-Laplacian attention
+// (attention_mma.cu), used by the mixed form when the shape allows it.
+bool psi_attention_fl_mma_supported(int n, int Dh);
+template <class Out>
+cudaError_t launch_psi_attention_fl_mma(cudaStream_t s, int B, int n, int Tp, int T, int H, int Dh, const float* qkv,
+                                        const float* bqkv, Out out);
 qmc_status psi_evaluate(qmc_model* m, const PsiPlan& pp, void* ws, const float* electrons, float* logpsi,
                         float* sign, uint8_t* flags, cudaStream_t s);
 qmc_status psi_set_params(qmc_model* m, const float* params, cudaStream_t s);

@@ -20,6 +20,7 @@
 //   k_psi_attention_fl  one (walker, head): scores, softmax and mixing with
 //                       their tangent rules, directions streamed one by one
 #include <cmath>
+#include <type_traits>
 
 #include "act.cuh"
 #include "psiformer.cuh"
@@ -682,6 +683,10 @@ __global__ void __launch_bounds__(kAttnFlThreads, 2) k_psi_attention_fl(int n, i
 template <class Out>
 cudaError_t launch_psi_attention_fl(cudaStream_t s, int B, int n, int Tp, int T, int H, int Dh, const float* qkv,
                                     const float* bqkv, Out out) {
+  // split-BF16 operands (the mixed form): the warp-MMA kernel
+  if constexpr (std::is_same<Out, StSplit>::value) {
+    if (psi_attention_fl_mma_supported(n, Dh)) return launch_psi_attention_fl_mma(s, B, n, Tp, T, H, Dh, qkv, bqkv, out);
+  }
   if (!psi_attention_fl_supported(n, Dh) || T < 2 || Tp < T) return cudaErrorInvalidValue;
   const size_t sm = psi_attention_fl_smem(n, Dh);
   const int rt = attention_fl_rows(n, Dh);

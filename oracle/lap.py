@@ -173,6 +173,11 @@ def stack(parts, axis: int) -> LT:
 
 
 _SPLIT_SELECT = None  # predicate on W: emulate the split-BF16 product for this GEMM
+_SPLIT_ATTENTION = False  # emulate the split-BF16 attention products too
+
+
+def split_attention() -> bool:
+    return _SPLIT_ATTENTION
 
 
 def _split_bf16(a: torch.Tensor):
@@ -190,21 +195,24 @@ def _split_matmul(a: torch.Tensor, W: torch.Tensor) -> torch.Tensor:
 
 
 @contextmanager
-def split_bf16_gemms(select=lambda W: True):
+def split_bf16_gemms(select=lambda W: True, attention: bool = False):
     """Within the block, ``linear`` with a weight ``W`` for which
     ``select(W)`` holds rounds both operands to FP32, splits each into a high
     and a low bf16 part and forms ``hi_a hi_W + hi_a lo_W + lo_a hi_W`` (the
     low x low product dropped) in the oracle's dtype: the product of the
     library's split-BF16 tensor-core GEMMs up to their FP32 accumulation.
     The value, Jacobian and Laplacian rows are rounded alike, as they are on
-    the GPU."""
-    global _SPLIT_SELECT
-    prev = _SPLIT_SELECT
+    the GPU.  With ``attention`` the forward-Laplacian attention products of
+    the Psiformer / LapNet oracles are split the same way (all but the value
+    scores, which the library forms in FP32)."""
+    global _SPLIT_SELECT, _SPLIT_ATTENTION
+    prev, prev_att = _SPLIT_SELECT, _SPLIT_ATTENTION
     _SPLIT_SELECT = select
+    _SPLIT_ATTENTION = bool(attention)
     try:
         yield
     finally:
-        _SPLIT_SELECT = prev
+        _SPLIT_SELECT, _SPLIT_ATTENTION = prev, prev_att
 
 
 def linear(a: LT, W: torch.Tensor, b: torch.Tensor | None = None) -> LT:

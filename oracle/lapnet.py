@@ -75,7 +75,7 @@ def backbone(p, cfg: LapNetConfig, ae, dtype):
         s = _bilinear(Q, K, "bqhd,bkhd->bhqk")
         e = lap.exp(s - s.x.max(-1, keepdim=True).values)
         w = e * lap.reciprocal(e.sum(-1)).unsqueeze(-1)
-        o = _bilinear(w, V, "bhqk,bkhd->bqhd").reshape(n, D)
+        o = _bilinear(w, V, "bhqk,bkhd->bqhd", split_value=True).reshape(n, D)
         r = hd + _dense(q["output_projection"], o, dtype)
         hd = r + lap.tanh(_dense(q["value_update"], r, dtype))
     return hd

@@ -148,17 +148,30 @@ def logpsi_fn(params, cfg, atoms, dtype=torch.float64):
 # rule, and the product rule for the bilinear attention terms
 # (``src/jaqmc/laplacian/primitives/arithmetic.py:385``,
 # ``dot_general.py:713``, ``elementwise.py:42-72``).
-def _bilinear(a, b, eq: str):
+def _bilinear(a, b, eq: str, split_value: bool = False):
     """``einsum(eq, a, b)`` of two tangent carriers (walker axis first in
-    every operand): J by the product rule, L = L_a b + a L_b + 2 sum_d J_a J_b."""
+    every operand): J by the product rule, L = L_a b + a L_b + 2 sum_d J_a J_b.
+
+    Inside ``lap.split_bf16_gemms(..., attention=True)`` every product of
+    the tangent terms (and of the values too with ``split_value``) takes its
+    operands split into hi + lo bf16 with the lo x lo product dropped, as the
+    library's warp-MMA forward-Laplacian attention forms them."""
     from .lap import LT
     lhs, out = eq.split("->")
     ea, eb = lhs.split(",")
     ja, jb, jo = ea[0] + "z" + ea[1:], eb[0] + "z" + eb[1:], out[0] + "z" + out[1:]
-    x = torch.einsum(eq, a.x, b.x)
-    J = torch.einsum(f"{ja},{eb}->{jo}", a.J, b.x) + torch.einsum(f"{ea},{jb}->{jo}", a.x, b.J)
-    L = (torch.einsum(eq, a.L, b.x) + torch.einsum(eq, a.x, b.L)
-         + 2.0 * torch.einsum(f"{ja},{jb}->{out}", a.J, b.J))
+    if lap.split_attention():
+        def mul(e, u, v):
+            uh, ul = lap._split_bf16(u)
+            vh, vl = lap._split_bf16(v)
+            return (torch.einsum(e, uh, vh) + torch.einsum(e, uh, vl) + torch.einsum(e, ul, vh)).to(u.dtype)
+        x = mul(eq, a.x, b.x) if split_value else torch.einsum(eq, a.x, b.x)
+    else:
+        def mul(e, u, v):
+            return torch.einsum(e, u, v)
+        x = torch.einsum(eq, a.x, b.x)
+    J = mul(f"{ja},{eb}->{jo}", a.J, b.x) + mul(f"{ea},{jb}->{jo}", a.x, b.J)
+    L = mul(eq, a.L, b.x) + mul(eq, a.x, b.L) + 2.0 * mul(f"{ja},{jb}->{out}", a.J, b.J)
     return LT(x, J, L)
 
 
@@ -196,7 +209,7 @@ def attention_lt(p, x, cfg: PsiformerConfig, dtype):
     s = _bilinear(q, k, "bqhd,bkhd->bhqk")
     e = lap.exp(s - s.x.max(-1, keepdim=True).values)
     w = e * lap.reciprocal(e.sum(-1)).unsqueeze(-1)
-    o = _bilinear(w, v, "bhqk,bkhd->bqhd").reshape(n, H * Dh)
+    o = _bilinear(w, v, "bhqk,bkhd->bqhd", split_value=True).reshape(n, H * Dh)
     Wo = _t(p["out"]["kernel"], dtype)
     return lap.linear(o, Wo.reshape(H * Dh, Wo.shape[-1]), _t(p["out"]["bias"], dtype))
 

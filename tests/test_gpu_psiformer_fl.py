@@ -123,10 +123,11 @@ def test_benzene_full_config(cuda_device):
     FP32 form: per-walker |dE_L| median within 3x the FP32 oracle's own
     median (+ 0.1 mHa) and maximum within 3x its maximum (+ 1 mHa); batch mean
     within four paired standard errors (+ 0.1 mHa).
-    Split-BF16 form: its error is the rounding of the GEMM operands to hi + lo
-    bf16 (about 2^-17 relative), which the kinetic energy amplifies to mHa
-    per walker on this system.  The oracle with that operand rounding
-    emulated (oracle/lap.py split_bf16_gemms) states the size to expect: the
+    Split-BF16 form: its error is the rounding of the GEMM and attention
+    operands to hi + lo bf16 (about 2^-17 relative), which the kinetic energy
+    amplifies to mHa per walker on this system.  The oracle with that operand
+    rounding emulated (oracle/lap.py split_bf16_gemms) states the size to
+    expect: the
     per-walker median within 3x the emulation's (+ 1 mHa), the maximum within
     5x (+ 10 mHa), and the batch mean unbiased: within max(0.5 mHa, 4 paired
     standard errors) of FP64."""
@@ -148,7 +149,7 @@ def test_benzene_full_config(cuda_device):
     r64 = _oracle(tree, cfg, mol, x, torch.float64)
     r32 = _oracle(tree, cfg, mol, x, torch.float32)
     K0 = 4 * mol.n_atoms + 1
-    with lap.split_bf16_gemms(lambda W: W.shape[0] != K0):
+    with lap.split_bf16_gemms(lambda W: W.shape[0] != K0, attention=True):
         remu = _oracle(tree, cfg, mol, x, torch.float64)
     ref = r64["e_local"]
     e32 = np.abs(r32["e_local"] - ref)
