@@ -36,9 +36,11 @@ from oracle import ferminet as OF  # noqa: E402
 from oracle import hamiltonian as OH  # noqa: E402
 from oracle import mcmc as OM  # noqa: E402
 from oracle import philox as OX  # noqa: E402
+from oracle import lapnet as OL  # noqa: E402
 from oracle import psiformer as OP  # noqa: E402
 
 PSI_SMALL = dict(ndets=3, num_layers=2, num_heads=4, heads_dim=16, mlp_hidden_dims=[64])
+LAP_SMALL = dict(ndets=3, num_layers=2, num_heads=4, heads_dim=16)
 
 # name: (model, system, config keyword arguments, walkers); params seed 0, walkers seed 1
 CASES = {
@@ -47,6 +49,8 @@ CASES = {
     "psiformer_li_small": ("psiformer", "Li", PSI_SMALL, 32),
     "psiformer_ch4_small": ("psiformer", "CH4", PSI_SMALL, 32),
     "psiformer_c6h6_full": ("psiformer", "C6H6", {}, 2),
+    "lapnet_li_small": ("lapnet", "Li", LAP_SMALL, 32),
+    "lapnet_ch4_small": ("lapnet", "CH4", LAP_SMALL, 32),
 }
 
 
@@ -55,6 +59,7 @@ MH_CASES = {
     "mh_ferminet_li_full": ("ferminet_li_full", 64, 3, 0.02, 2),
     "mh_ferminet_n2_full": ("ferminet_n2_full", 64, 3, 0.02, 2),
     "mh_psiformer_li_small": ("psiformer_li_small", 64, 3, 0.05, 4),
+    "mh_lapnet_li_small": ("lapnet_li_small", 64, 3, 0.05, 4),
 }
 
 
@@ -81,6 +86,10 @@ def build(case):
         cfg = P.FermiNetConfig(nspins=mol.nspins, **kw)
         tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
         flat = P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms))
+    elif model == "lapnet":
+        cfg = P.LapNetConfig(nspins=mol.nspins, **kw)
+        tree = P.init_lapnet(cfg, mol.n_atoms, seed=0)
+        flat = P.flatten(tree, P.lapnet_leaves(cfg, mol.n_atoms))
     else:
         cfg = P.PsiformerConfig(nspins=mol.nspins, **kw)
         tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
@@ -104,6 +113,9 @@ def oracle_values(case, mol, cfg, tree, x, dtype):
                                envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split)
         r = OF.evaluate(tree, oc, xt, mol.atoms, dtype=dtype, tangents=True)
         sign = r["sign_logpsi"]
+    elif model == "lapnet":
+        r = OL.evaluate(tree, lapnet_config(cfg), xt, mol.atoms, dtype=dtype, tangents=True)
+        sign = r["sign_logpsi"]
     else:
         oc = OP.PsiformerConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets, num_layers=cfg.num_layers,
                                 num_heads=cfg.num_heads, heads_dim=cfg.heads_dim,
@@ -117,6 +129,13 @@ def oracle_values(case, mol, cfg, tree, x, dtype):
     return {"logpsi": f(r["logpsi"]), "sign": f(sign), "e_local": f(ke + pe), "kinetic": f(ke), "potential": f(pe)}
 
 
+def lapnet_config(cfg):
+    return OL.LapNetConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets, num_layers=cfg.num_layers,
+                           num_heads=cfg.num_heads, heads_dim=cfg.heads_dim, num_local_updates=cfg.num_local_updates,
+                           envelope=cfg.envelope, jastrow=cfg.jastrow, use_input_bias=cfg.use_input_bias,
+                           use_backbone_bias=cfg.use_backbone_bias)
+
+
 def logpsi_fn(case, mol, cfg, tree):
     """FP64 oracle log|psi| of a case's model, as a function of the walkers."""
     if CASES[case][0] == "ferminet":
@@ -125,6 +144,8 @@ def logpsi_fn(case, mol, cfg, tree):
                                hidden_dims_double=list(cfg.hidden_dims_double), use_last_layer=cfg.use_last_layer,
                                envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split)
         return OF.logpsi_fn(tree, oc, mol.atoms)
+    if CASES[case][0] == "lapnet":
+        return OL.logpsi_fn(tree, lapnet_config(cfg), torch.as_tensor(mol.atoms, dtype=torch.float64))
     oc = OP.PsiformerConfig(nspins=tuple(cfg.nspins), ndets=cfg.ndets, num_layers=cfg.num_layers,
                             num_heads=cfg.num_heads, heads_dim=cfg.heads_dim, mlp_hidden_dims=list(cfg.mlp_hidden_dims),
                             envelope=cfg.envelope, orbitals_spin_split=cfg.orbitals_spin_split, jastrow=cfg.jastrow)

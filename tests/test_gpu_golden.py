@@ -26,6 +26,7 @@ FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
 MH = [f for f in FIXTURES if os.path.basename(f).startswith("mh_")]
 GRAD = [f for f in FIXTURES if os.path.basename(f).startswith("grad_")]
 VALUE = [f for f in FIXTURES if f not in MH and f not in GRAD]
+MODELS = {"ferminet": _native.NativeFermiNet, "psiformer": _native.NativePsiformer, "lapnet": _native.NativeLapNet}
 
 
 @pytest.mark.parametrize("path", GRAD, ids=lambda p: os.path.basename(p)[:-4])
@@ -63,8 +64,7 @@ def test_mh_matches_fixture(path, cuda_device):
     meta = json.loads(str(z["meta"]))
     mol, cfg, _, flat, _ = G.build(meta["model_case"])
     assert G.params_sha(flat) == meta["params_sha256"]
-    cls = _native.NativeFermiNet if meta["model"] == "ferminet" else _native.NativePsiformer
-    m = cls(cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
+    m = MODELS[meta["model"]](cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
     m.set_params(torch.as_tensor(flat, device=cuda_device))
     xg = torch.as_tensor(z["walkers"], device=cuda_device).clone()
     nz = torch.as_tensor(z["normals"], device=cuda_device)
@@ -85,8 +85,7 @@ def test_fp32_path_matches_fixture(path, cuda_device):
     meta = json.loads(str(z["meta"]))
     mol, cfg, _, flat, _ = G.build(meta["case"])
     assert G.params_sha(flat) == meta["params_sha256"]
-    cls = _native.NativeFermiNet if meta["model"] == "ferminet" else _native.NativePsiformer
-    m = cls(cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
+    m = MODELS[meta["model"]](cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
     m.set_params(torch.as_tensor(flat, device=cuda_device))
     x = torch.as_tensor(z["walkers"], device=cuda_device)
     lp, sg, _ = m.forward(x)
