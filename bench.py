@@ -274,16 +274,27 @@ def psiformer_forward_flops(cfg, n, A):
     return 2 * (n * per_row + attn)
 
 
-def psiformer_attention_fl_roofline(cfg, n, walkers, attention_ms):
-    """FP32-SIMT roofline of the forward-Laplacian attention kernel
-    (k_psi_attention_fl) over one E_L of ``walkers`` walkers: per (walker,
-    head, layer) and per direction, the score tangents (2 n^2 Dh FMA), the
-    cross term (n^2 Dh) and the mixing tangents with their cross term
-    (3 n^2 Dh), over 3n directions: 18 n^3 Dh FMA."""
+def psiformer_attention_fl_roofline(cfg, n, walkers, attention_ms, prec="fp32"):
+    """Roofline of the forward-Laplacian attention over one E_L of ``walkers``
+    walkers: per (walker, head, layer) and per direction, the score tangents
+    (2 n^2 Dh FMA), the cross term (n^2 Dh) and the mixing tangents with their
+    cross term (3 n^2 Dh), over 3n directions: 18 n^3 Dh FMA.  FP32 form:
+    k_psi_attention_fl against the measured FP32 SIMT peak.  Mixed form:
+    k_attention_fl_mma issues three split-BF16 warp MMAs per product, so its
+    achieved rate counts 3x the algorithmic FLOPs against the measured
+    warp-MMA peak."""
     if not attention_ms:
         return None
     flop = 2.0 * 18 * n ** 3 * cfg.heads_dim * cfg.num_heads * cfg.num_layers * walkers
-    achieved = flop / (attention_ms / 1e3) / 1e12
+    t = attention_ms / 1e3
+    if prec == "mixed" and MMA_PEAK["value"]:
+        achieved = 3.0 * flop / t / 1e12
+        peak = MMA_PEAK["value"]
+        return {"kernel": "k_attention_fl_mma", "bound": "tensor (warp mma.sync, split BF16: 3 products)",
+                "achieved": achieved, "peak": peak, "peak_kind": MMA_PEAK["source"], "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "algorithmic_flop_per_request": flop,
+                "algorithmic_tflops": flop / t / 1e12}
+    achieved = flop / t / 1e12
     peak = SIMT_PEAK["value"]
     return {"kernel": "k_psi_attention_fl", "bound": "fp32 simt", "achieved": achieved, "peak": peak,
             "peak_kind": SIMT_PEAK["source"], "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
@@ -366,7 +377,7 @@ def run_psiformer(dev, steps, warmup, walkers=4096, mh_steps=10, oracle_walkers=
                        "gpu_launches_per_request": sum(v[0] for v in prof.values()),
                        "kernel_ms_per_request": {names.get(k, k): v[1] for k, v in prof.items() if v[0]},
                        "roofline_attention": psiformer_attention_fl_roofline(
-                           cfg, mol.n_electrons, walkers, prof.get("pair", (0, 0.0))[1]),
+                           cfg, mol.n_electrons, walkers, prof.get("pair", (0, 0.0))[1], prec),
                        "roofline_request": psiformer_request_roofline(
                            cfg, mol.n_electrons, mol.n_atoms, walkers, mh_steps, ms, prec, pk, pk_kind)}
     el = {p: m.local_energy(x0)["e_local"].double() for p, m in models.items()}
@@ -549,12 +560,18 @@ def run_request_only(args, wl):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     mol = S.SYSTEMS[wl["system"]]()
-    cfg = P.FermiNetConfig(nspins=mol.nspins)
-    tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
-    flat = torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms)), device=dev)
+    if wl.get("model") == "psiformer":
+        cfg = P.PsiformerConfig(nspins=mol.nspins)
+        tree = P.init_psiformer(cfg, mol.n_atoms, seed=0)
+        flat = torch.as_tensor(P.flatten(tree, P.psiformer_leaves(cfg, mol.n_atoms)), device=dev)
+        m = _native.NativePsiformer(cfg, mol.atoms, mol.charges, precision=args.precision, device=dev)
+    else:
+        cfg = P.FermiNetConfig(nspins=mol.nspins)
+        tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+        flat = torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms)), device=dev)
+        m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision=args.precision, device=dev)
     B, S_ = wl["walkers"], wl["mh_steps"]
     x = torch.as_tensor(S.init_walkers(mol, B, seed=1), device=dev)
-    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision=args.precision, device=dev)
     m.set_params(flat)
     if args.burn_in:
         m.mh_steps(x, args.burn_in, 0.15, 1000, 0)
@@ -576,6 +593,7 @@ def run_request_only(args, wl):
     torch.cuda.synchronize()
     assert m.check_error() == 0
     line = {"op": args.op, "precision": args.precision, "walkers": B, "system": wl["system"],
+            "model": wl.get("model", "ferminet"),
             "ms_per_step": e0.elapsed_time(e1) / args.steps}
     if args.kernel_classes:
         _native.profile_enable(True)
@@ -626,12 +644,13 @@ def run_ours(args, wl):
             dist.barrier()
         torch.cuda.synchronize()
 
-    def timed(m, x, K, counter0):
+    def timed(rg, K):
+        # requests replayed from their CUDA graph on the timing stream
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for k in range(K):
-            mv = request(m, x, counter0 + k * S_)
+        for _ in range(K):
+            mv = rg.run(stream)
         e1.record(stream)
         barrier()
         return max_over_ranks(e0.elapsed_time(e1), dev), mv
@@ -644,15 +663,15 @@ def run_ours(args, wl):
     results = {}
     xs = {p: x0.clone() for p in models}
     counter = 0
-    for p, m in models.items():
+    # each form's request captured once (after one eager run) and replayed
+    graphs = {p: _native.RequestGraph(m, xs[p], S_, 0.02, 2 + rank, counter=1 << 20) for p, m in models.items()}
+    for rg in graphs.values():
         for _ in range(args.warmup):
-            request(m, xs[p], counter)
-            counter += S_
+            rg.run()
     clocks = ClockSampler(local)
     clocks.start()
     for p in (prec_main,) + tuple(q for q in models if q != prec_main):
-        ms, mv = timed(models[p], xs[p], args.steps, counter)
-        counter += args.steps * S_
+        ms, mv = timed(graphs[p], args.steps)
         results[p] = {"ms_per_step": ms / args.steps, "mean_var": mv.cpu().numpy().tolist()}
     clk = clocks.stop()
 
@@ -680,15 +699,13 @@ def run_ours(args, wl):
     # end to end through the public API with host buffers
     host_x = x0.cpu().pin_memory()
     host_out = torch.empty(2, dtype=torch.float64).pin_memory()
-    m = models[prec_main]
-    xd = torch.empty_like(x0)
+    rg = graphs[prec_main]
     barrier()
-    t0 = time.perf_counter()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for k in range(args.steps):
-        xd.copy_(host_x, non_blocking=True)
-        mv = request(m, xd, counter + k * S_)
+        rg.electrons.copy_(host_x, non_blocking=True)
+        mv = rg.run(stream)
         host_out.copy_(mv, non_blocking=True)
     e1.record(stream)
     barrier()
@@ -734,6 +751,7 @@ def run_ours(args, wl):
             "data": "synthetic (seeded walkers N(0,1) around nuclei; fan-in-scaled N(0,1/fan_in) params)",
             "config": {"workload": workload_name(wl, prec_main), **wl, "precision": prec_main,
                        "parallelism": f"replicas x{world}",
+                       "launch": "each request replayed from one CUDA graph (RequestGraph)",
                        "l2": "working set larger than L2 (local-energy workspace several GB)"},
             "psiformer": psi,
             "gradient": grad,
@@ -745,6 +763,7 @@ def run_ours(args, wl):
             "cpu_baseline": cpu,
             "clocks": clk,
             "fp32_simt_peak_tflops": SIMT_PEAK,
+            "warp_mma_bf16_peak_tflops": MMA_PEAK,
             "roofline": rl,
             "roofline_tensor": rl_t,
             "roofline_request": {p_: ferminet_request_roofline(cfg, mol.n_atoms, world * B, S_, r_["ms_per_step"],
@@ -769,10 +788,15 @@ def run_ours(args, wl):
 SIMT_PEAK = {"value": 152 * 128 * 2 * 2.07e9 / 1e12, "source": "FP32 SIMT nominal (152 SM x 128 FMA x 2 x 2.07 GHz)"}
 
 
+MMA_PEAK = {"value": None, "source": None}
+
+
 def measure_simt_peak(dev):
     from jaqmc_gb300 import _native
     v = _native.fp32_simt_peak(dev)
     SIMT_PEAK.update(value=v, source="FP32 SIMT measured (FMA probe, CUDA events, best of 5)")
+    MMA_PEAK.update(value=_native.warp_mma_peak(dev),
+                    source="warp mma.sync BF16 measured (MMA probe, CUDA events, best of 5)")
     return v
 # dram__bytes_read.sum + dram__bytes_write.sum of one forward-Laplacian launch
 # of the one-electron layer kernel, from the committed ncu capture at 512
@@ -918,17 +942,16 @@ def main():
     wl = dict(WORKLOADS[args.workload])
     if args.walkers:
         wl["walkers"] = args.walkers
+    if args.request_only:
+        return run_request_only(args, wl)
     if wl.get("model") == "psiformer" and args.impl != "reference":
         import torch
         torch.cuda.set_device(0)
         measure_simt_peak(torch.device("cuda", 0))
-        forms = (args.precision,) if args.request_only else ("mixed", "fp32")
         print(json.dumps(run_psiformer(torch.device("cuda", 0), args.steps, args.warmup, walkers=wl["walkers"],
-                                       mh_steps=wl["mh_steps"], oracle_walkers=0 if args.no_cpu else 8,
-                                       forms=forms)), flush=True)
+                                       mh_steps=wl["mh_steps"], oracle_walkers=0 if args.no_cpu else 32)),
+              flush=True)
         return 0
-    if args.request_only:
-        return run_request_only(args, wl)
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -374,6 +374,15 @@ qmc_status qmc_profile_read(int n_classes, int64_t* launches, double* ms);
 qmc_status qmc_ffma_throughput(int blocks, int iters, float* out, double* fma_per_launch,
                                cudaStream_t stream);
 
+/* Warp-level BF16 MMA throughput probe (mma.m16n8k16, FP32 accumulate, the
+ * legacy warp tensor path that the mixed form's forward-Laplacian attention
+ * uses): `blocks` blocks of 256 threads, `iters` rounds of 8 independent
+ * MMAs per warp into blocks x 256 floats (a sink); *flop_per_launch = the
+ * FLOPs issued.  Timed with CUDA events by the caller, it is the roofline
+ * denominator of that kernel.  No counterpart in the reference. */
+qmc_status qmc_mma_throughput(int blocks, int iters, float* out, double* flop_per_launch,
+                              cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,6 +111,7 @@ _SIGS = {
                                  C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "qmc_ffma_throughput": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
+    "qmc_mma_throughput": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
 }
 
 
@@ -486,11 +487,103 @@ def profile_read():
     return {k: (int(launches[i]), float(ms[i])) for i, k in enumerate(KERNEL_CLASSES)}
 
 
+class RequestGraph:
+    """One VMC request on a resident walker batch -- ``steps`` all-electron MH
+    updates with the Philox counter in device memory, the forward-Laplacian
+    local energy and its FP64 batch mean and variance (``qmc_mh_steps_resident``
+    + ``qmc_local_energy`` + ``qmc_reduce_mean_var``, the reference's
+    ``MCMCSampler.step`` + energy estimators + ``mean_reduce``) -- captured
+    into a CUDA graph and replayed by :meth:`run`, so the hundreds of launches
+    of a request leave the host as one.
+
+    ``electrons`` (B, n, 3) is updated in place by every run; ``counter``
+    advances by ``steps`` per run, so runs draw the same Philox stream as
+    successive ``mh_steps`` calls from that counter.  Construction runs one
+    request eagerly (the library sets per-kernel attributes on first use),
+    which advances the walkers and the counter, and then captures, without
+    running, the request that :meth:`run` replays."""
+
+    def __init__(self, model, electrons, steps, stddev, seed, counter=0):
+        e = model._elec(electrons)
+        B = e.shape[0]
+        dev = e.device
+        self.model, self.electrons, self.steps = model, e, int(steps)
+        self.stddev, self.seed = float(stddev), int(seed)
+        lib = model.lib
+        self.ws_bytes = max(int(lib.qmc_workspace_size(model.h, OP_MH, B)),
+                            int(lib.qmc_workspace_size(model.h, OP_LOCAL_ENERGY, B)))
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        self.log_prob = torch.empty(B, dtype=torch.float32, device=dev)
+        self.accepts = torch.zeros(B, dtype=torch.int32, device=dev)
+        self.e_local = torch.empty(B, dtype=torch.float32, device=dev)
+        self.mean_var = torch.empty(2, dtype=torch.float64, device=dev)
+        self.counter = torch.tensor([int(counter)], dtype=torch.int64, device=dev)
+        self.device = dev
+        # eager run and capture on a side stream (capture cannot use the
+        # legacy default stream), ordered after the caller's pending work
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        self._st = side
+        with torch.cuda.stream(side):
+            self._enqueue()
+        side.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(side):
+            self.graph.capture_begin(capture_error_mode="thread_local")
+            try:
+                self._enqueue()
+            finally:
+                self.graph.capture_end()
+
+    def _enqueue(self):
+        m, lib, st = self.model, self.model.lib, int(self._st.cuda_stream)
+        B = self.electrons.shape[0]
+        check(lib.qmc_mh_steps_resident(m.h, B, self.steps, self.stddev, self.seed, ptr(self.counter),
+                                        ptr(self.electrons), ptr(self.log_prob), ptr(self.accepts), None,
+                                        ptr(self.ws), self.ws_bytes, st))
+        check(lib.qmc_local_energy(m.h, B, ptr(self.electrons), ptr(self.e_local), None, None, None, None,
+                                   ptr(self.ws), self.ws_bytes, st))
+        check(lib.qmc_reduce_mean_var(B, ptr(self.e_local), ptr(self.mean_var), st))
+
+    def run(self, stream=None):
+        """Replay the request on ``stream`` (default: the current stream), in
+        order with the caller's other work there; returns the device tensor
+        (E_L mean, variance)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s):
+            self.graph.replay()
+        return self.mean_var
+
+
 def reduce_mean_var(x: torch.Tensor, stream=None):
     out = torch.empty(2, dtype=torch.float64, device=x.device)
     x = x.to(torch.float32).contiguous()
     check(load().qmc_reduce_mean_var(x.numel(), ptr(x), ptr(out), stream_handle(stream)))
     return out
+
+
+def warp_mma_peak(device=None, iters=4096, repeats=5):
+    """Measured warp-level BF16 MMA (mma.m16n8k16) throughput in TFLOP/s: the
+    best of ``repeats`` launches of the library's MMA probe (4 blocks of 8
+    warps per SM), timed with CUDA events on the launching stream."""
+    dev = torch.device(device or "cuda")
+    props = torch.cuda.get_device_properties(dev)
+    blocks = props.multi_processor_count * 4
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
+    flop = C.c_double()
+    lib = load()
+    s = torch.cuda.current_stream(dev)
+    check(lib.qmc_mma_throughput(blocks, iters, ptr(out), C.byref(flop), stream_handle(s)))
+    best = float("inf")
+    for _ in range(repeats):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(s)
+        check(lib.qmc_mma_throughput(blocks, iters, ptr(out), C.byref(flop), stream_handle(s)))
+        e1.record(s)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return flop.value / best / 1e12
 
 
 def fp32_simt_peak(device=None, iters=4096, repeats=5):

@@ -70,9 +70,45 @@ __global__ void __launch_bounds__(256) k_ffma_throughput(int iters, float b, flo
   out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
+// Warp-level BF16 MMA throughput probe (mma.m16n8k16, FP32 accumulate):
+// every warp runs kMmaChains independent accumulators; the operands are
+// register constants, so only the tensor pipe is measured.  Work per launch:
+// blocks x 8 warps x kMmaChains x iters MMAs of 2 x 16 x 8 x 16 FLOPs.
+constexpr int kMmaChains = 8;
+__global__ void __launch_bounds__(256) k_mma_throughput(int iters, float* __restrict__ out) {
+  const uint32_t a0 = threadIdx.x * 0x00010001u, a1 = a0 ^ 0x3f803f80u, a2 = a0 + 1u, a3 = a1 + 1u;
+  const uint32_t b0 = a0 ^ 0x40004000u, b1 = a1 ^ 0x3c003c00u;
+  float d[kMmaChains][4] = {};
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < kMmaChains; ++k)
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+          "{%0, %1, %2, %3};\n"
+          : "+f"(d[k][0]), "+f"(d[k][1]), "+f"(d[k][2]), "+f"(d[k][3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < kMmaChains; ++k) acc += d[k][0] + d[k][1] + d[k][2] + d[k][3];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
 }  // namespace qmc
 
 extern "C" {
+
+qmc_status qmc_mma_throughput(int blocks, int iters, float* out, double* flop_per_launch, cudaStream_t stream) {
+  if (blocks < 1 || iters < 1 || !out) {
+    qmc::set_error("qmc_mma_throughput: blocks, iters >= 1 and an output of blocks x 256 floats");
+    return QMC_ERR_ARG;
+  }
+  qmc::k_mma_throughput<<<blocks, 256, 0, stream>>>(iters, out);
+  if (flop_per_launch)
+    *flop_per_launch = (double)blocks * 8.0 * qmc::kMmaChains * (double)iters * (2.0 * 16 * 8 * 16);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? QMC_OK : qmc::cuda_status(e, "k_mma_throughput");
+}
 
 qmc_status qmc_ffma_throughput(int blocks, int iters, float* out, double* fma_per_launch, cudaStream_t stream) {
   if (blocks < 1 || iters < 1 || !out) {

@@ -210,111 +210,150 @@ constexpr int kGrpMaxD = 512;
 constexpr int kGrpMaxTp = 256;
 constexpr int kGrpWarps = 8;
 
+__device__ __forceinline__ void put4(const StF32& o, size_t r, int c, float4 v) {
+  *reinterpret_cast<float4*>(o.p + r * o.ld + c) = v;
+}
+__device__ __forceinline__ void put4(const StSplit& o, size_t r, int c, float4 v) {
+  const __nv_bfloat162 h0 = __floats2bfloat162_rn(v.x, v.y), h1 = __floats2bfloat162_rn(v.z, v.w);
+  const float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1);
+  const __nv_bfloat162 l0 = __floats2bfloat162_rn(v.x - f0.x, v.y - f0.y),
+                       l1 = __floats2bfloat162_rn(v.z - f1.x, v.w - f1.y);
+  const size_t i = r * o.ld + c;
+  uint2 hi, lo;
+  hi.x = *reinterpret_cast<const uint32_t*>(&h0);
+  hi.y = *reinterpret_cast<const uint32_t*>(&h1);
+  lo.x = *reinterpret_cast<const uint32_t*>(&l0);
+  lo.y = *reinterpret_cast<const uint32_t*>(&l1);
+  *reinterpret_cast<uint2*>(o.p + i) = hi;
+  *reinterpret_cast<uint2*>(o.p + i + o.plane) = lo;
+}
+
+// The pass reads each z row once: the value row first (h, h'), then the
+// Jacobian rows t >= 2 (J h = h' J z, accumulating sum_d (J_d z)^2 per
+// feature), then the Laplacian row, which needs that sum.  A warp takes
+// whole rows, a lane four consecutive features per 128 (16-byte accesses).
 template <class Out>
 __global__ void __launch_bounds__(kGrpWarps * 32) k_psi_group_fl(int Tp, int D, const float* __restrict__ z,
                                                                   int ldz, const float* __restrict__ bias, int act,
                                                                   float* __restrict__ x, int xmode,
                                                                   const float* __restrict__ ln_s,
                                                                   const float* __restrict__ ln_b, Out out) {
-  constexpr int kPer = kGrpMaxD / 32;
-  __shared__ float colacc[kGrpWarps][kGrpMaxD];
-  __shared__ float hv[3][kGrpMaxD];
-  __shared__ float v0[kGrpMaxD];
+  constexpr int kV = kGrpMaxD / 128;
+  __shared__ __align__(16) float colacc[kGrpWarps][kGrpMaxD];
+  __shared__ __align__(16) float hv[2][kGrpMaxD];  // h, h' of the value row
+  __shared__ __align__(16) float v0[kGrpMaxD];
   __shared__ float S1[kGrpMaxTp], S2[kGrpMaxTp];
   __shared__ float redf[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t r0 = (size_t)blockIdx.x * Tp;
-  const int per = D >> 5;
-  if (act) {
-    float acc[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) acc[k] = 0.f;
-    for (int t = 2 + warp; t < Tp; t += kGrpWarps) {
-      const float* zr = z + (r0 + t) * ldz;
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        if (k < per) {
-          const float v = zr[lane + 32 * k];
-          acc[k] = fmaf(v, v, acc[k]);
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kPer; ++k)
-      if (k < per) colacc[warp][lane + 32 * k] = acc[k];
-    __syncthreads();
-    for (int c = threadIdx.x; c < D; c += blockDim.x) {
-      float q = 0.f;
-#pragma unroll
-      for (int wv = 0; wv < kGrpWarps; ++wv) q += colacc[wv][c];
-      const float h = tanhf(z[r0 * ldz + c] + bias[c]);
-      const float h1 = 1.f - h * h;
-      hv[0][c] = h;
-      hv[1][c] = h1;
-      hv[2][c] = -2.f * h * h1 * q;
-    }
-    __syncthreads();
-  }
-  auto hval = [&](int t, int c, const float* zr) -> float {
-    if (t == 0) return act ? hv[0][c] : zr[c] + bias[c];
-    const float zv = zr[c];
-    if (!act) return zv;
-    return t == 1 ? fmaf(hv[1][c], zv, hv[2][c]) : hv[1][c] * zv;
-  };
-  if (!ln_s) {
-    for (int t = warp; t < Tp; t += kGrpWarps) {
-      const float* zr = z + (r0 + t) * ldz;
-      float* xr = x + (r0 + t) * D;
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        if (k < per) {
-          const int c = lane + 32 * k;
-          float v = hval(t, c, zr);
-          if (xmode == 2) v += xr[c];
-          if (xmode) xr[c] = v;
-          out.put(r0 + t, c, v);
-        }
-    }
-    return;
-  }
-  // value row, its mean and centred variance
+  const float invD = 1.f / (float)D;
+  // value row
   float s = 0.f;
   for (int c = threadIdx.x; c < D; c += blockDim.x) {
-    float v = hval(0, c, z + r0 * ldz);
+    float v = z[r0 * ldz + c] + bias[c];
+    if (act) {
+      v = tanhf(v);
+      hv[0][c] = v;
+      hv[1][c] = 1.f - v * v;
+    }
     if (xmode == 2) v += x[r0 * D + c];
-    x[r0 * D + c] = v;
+    if (xmode) x[r0 * D + c] = v;
     v0[c] = v;
     s += v;
   }
-  const float invD = 1.f / (float)D;
-  const float mu0 = block_sum(s, redf) * invD;
-  float q = 0.f;
-  for (int c = threadIdx.x; c < D; c += blockDim.x) q += (v0[c] - mu0) * (v0[c] - mu0);
-  const float var = block_sum(q, redf) * invD;
-  // tangent rows: residual update, row sums of v and of u v, sum of (J v)^2
-  float qq = 0.f;
-  for (int t = 1 + warp; t < Tp; t += kGrpWarps) {
+  float mu0 = 0.f, var = 0.f;
+  if (ln_s) {
+    mu0 = block_sum(s, redf) * invD;
+    float q = 0.f;
+    for (int c = threadIdx.x; c < D; c += blockDim.x) q += (v0[c] - mu0) * (v0[c] - mu0);
+    var = block_sum(q, redf) * invD;
+  } else {
+    __syncthreads();
+  }
+  // Jacobian rows
+  float4 qa[kV];
+#pragma unroll
+  for (int k = 0; k < kV; ++k) qa[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  float Qs = 0.f;
+  for (int t = 2 + warp; t < Tp; t += kGrpWarps) {
     const float* zr = z + (r0 + t) * ldz;
     float* xr = x + (r0 + t) * D;
     float s1 = 0.f, s2 = 0.f;
 #pragma unroll
-    for (int k = 0; k < kPer; ++k)
-      if (k < per) {
-        const int c = lane + 32 * k;
-        float v = hval(t, c, zr);
-        if (xmode == 2) v += xr[c];
-        xr[c] = v;
-        s1 += v;
-        s2 = fmaf(v0[c] - mu0, v, s2);
-        if (t >= 2) qq = fmaf(v, v, qq);
+    for (int k = 0; k < kV; ++k) {
+      const int c = 4 * lane + 128 * k;
+      if (c < D) {
+        const float4 zz = *reinterpret_cast<const float4*>(zr + c);
+        float4 v = zz;
+        if (act) {
+          const float4 h1 = *reinterpret_cast<const float4*>(&hv[1][c]);
+          v = make_float4(h1.x * zz.x, h1.y * zz.y, h1.z * zz.z, h1.w * zz.w);
+          qa[k].x = fmaf(zz.x, zz.x, qa[k].x);
+          qa[k].y = fmaf(zz.y, zz.y, qa[k].y);
+          qa[k].z = fmaf(zz.z, zz.z, qa[k].z);
+          qa[k].w = fmaf(zz.w, zz.w, qa[k].w);
+        }
+        if (xmode == 2) {
+          const float4 xx = *reinterpret_cast<const float4*>(xr + c);
+          v = make_float4(v.x + xx.x, v.y + xx.y, v.z + xx.z, v.w + xx.w);
+        }
+        if (xmode) *reinterpret_cast<float4*>(xr + c) = v;
+        if (!ln_s) {
+          put4(out, r0 + t, c, v);
+        } else {
+          const float4 u = *reinterpret_cast<const float4*>(&v0[c]);
+          s1 += (v.x + v.y) + (v.z + v.w);
+          s2 = fmaf(u.x - mu0, v.x, fmaf(u.y - mu0, v.y, fmaf(u.z - mu0, v.z, fmaf(u.w - mu0, v.w, s2))));
+          Qs = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, Qs))));
+        }
       }
-    s1 = wsum(s1);
-    s2 = wsum(s2);
-    if (lane == 0) {
-      S1[t] = s1;
-      S2[t] = s2;
+    }
+    if (ln_s) {
+      s1 = wsum(s1);
+      s2 = wsum(s2);
+      if (lane == 0) {
+        S1[t] = s1;
+        S2[t] = s2;
+      }
     }
   }
-  const float Q = block_sum(qq, redf);  // also publishes S1 / S2
+  // Laplacian row: L h = h' L z + h'' sum_d (J_d z)^2, h'' = -2 h h'
+  if (act) {
+#pragma unroll
+    for (int k = 0; k < kV; ++k) {
+      const int c = 4 * lane + 128 * k;
+      if (c < D) *reinterpret_cast<float4*>(&colacc[warp][c]) = qa[k];
+    }
+  }
+  __syncthreads();
+  float s1 = 0.f, s2 = 0.f;
+  for (int c = threadIdx.x; c < D; c += blockDim.x) {
+    float v = z[(r0 + 1) * ldz + c];
+    if (act) {
+      float q = 0.f;
+#pragma unroll
+      for (int wv = 0; wv < kGrpWarps; ++wv) q += colacc[wv][c];
+      const float h = hv[0][c], h1 = hv[1][c];
+      v = fmaf(h1, v, -2.f * h * h1 * q);
+    }
+    if (xmode == 2) v += x[(r0 + 1) * D + c];
+    if (xmode) x[(r0 + 1) * D + c] = v;
+    if (!ln_s) {
+      out.put(r0 + 1, c, v);
+      out.put(r0, c, v0[c]);
+    } else {
+      s1 += v;
+      s2 = fmaf(v0[c] - mu0, v, s2);
+    }
+  }
+  if (!ln_s) return;
+  s1 = block_sum(s1, redf);
+  s2 = block_sum(s2, redf);
+  if (threadIdx.x == 0) {
+    S1[1] = s1;
+    S2[1] = s2;
+  }
+  const float Q = block_sum(Qs, redf);  // also publishes S1 / S2
   const float r = rsqrtf(var + 1e-5f);
   const float r3 = r * r * r;
   float a1 = 0.f, a2 = 0.f, a3 = 0.f;  // sum_d (J mu)^2, (J var)^2, J mu J r
@@ -330,24 +369,37 @@ __global__ void __launch_bounds__(kGrpWarps * 32) k_psi_group_fl(int Tp, int D, 
   const float Lmu = S1[1] * invD;
   const float Lv = 2.f * S2[1] * invD + 2.f * (Q * invD - Sdmu2);
   const float Lr = -0.5f * r3 * Lv + 0.75f * r3 * r * r * Sdv2;
-  float cacc[kPer];
+  float4 cacc[kV];
 #pragma unroll
-  for (int k = 0; k < kPer; ++k) cacc[k] = 0.f;
+  for (int k = 0; k < kV; ++k) cacc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int t = 2 + warp; t < Tp; t += kGrpWarps) {
     const float dmu = S1[t] * invD, dr = -r3 * S2[t] * invD;
     const float* xr = x + (r0 + t) * D;
 #pragma unroll
-    for (int k = 0; k < kPer; ++k)
-      if (k < per) {
-        const int c = lane + 32 * k;
-        const float J = xr[c];
-        out.put(r0 + t, c, ln_s[c] * fmaf(J - dmu, r, (v0[c] - mu0) * dr));
-        cacc[k] = fmaf(J, dr, cacc[k]);
+    for (int k = 0; k < kV; ++k) {
+      const int c = 4 * lane + 128 * k;
+      if (c < D) {
+        const float4 J = *reinterpret_cast<const float4*>(xr + c);
+        const float4 u = *reinterpret_cast<const float4*>(&v0[c]);
+        const float4 sc = *reinterpret_cast<const float4*>(ln_s + c);
+        const float4 y = make_float4(sc.x * fmaf(J.x - dmu, r, (u.x - mu0) * dr),
+                                     sc.y * fmaf(J.y - dmu, r, (u.y - mu0) * dr),
+                                     sc.z * fmaf(J.z - dmu, r, (u.z - mu0) * dr),
+                                     sc.w * fmaf(J.w - dmu, r, (u.w - mu0) * dr));
+        put4(out, r0 + t, c, y);
+        cacc[k].x = fmaf(J.x, dr, cacc[k].x);
+        cacc[k].y = fmaf(J.y, dr, cacc[k].y);
+        cacc[k].z = fmaf(J.z, dr, cacc[k].z);
+        cacc[k].w = fmaf(J.w, dr, cacc[k].w);
       }
+    }
   }
+  __syncthreads();  // every warp is done with colacc's sums of squares
 #pragma unroll
-  for (int k = 0; k < kPer; ++k)
-    if (k < per) colacc[warp][lane + 32 * k] = cacc[k];
+  for (int k = 0; k < kV; ++k) {
+    const int c = 4 * lane + 128 * k;
+    if (c < D) *reinterpret_cast<float4*>(&colacc[warp][c]) = cacc[k];
+  }
   __syncthreads();
   for (int c = threadIdx.x; c < D; c += blockDim.x) {
     float C = -Smd;
@@ -364,7 +416,7 @@ template <class Out>
 cudaError_t launch_psi_group_fl(cudaStream_t s, int groups, int Tp, int D, const float* z, int ldz,
                                 const float* bias, int act, float* x, int xmode, const float* ln_s,
                                 const float* ln_b, Out out) {
-  if (D % 32 || D > kGrpMaxD || Tp > kGrpMaxTp || Tp < 2 || (ln_s && !xmode)) return cudaErrorInvalidValue;
+  if (D % 64 || D > kGrpMaxD || Tp > kGrpMaxTp || Tp < 2 || ldz % 4 || (ln_s && !xmode)) return cudaErrorInvalidValue;
   k_psi_group_fl<Out><<<groups, kGrpWarps * 32, 0, s>>>(Tp, D, z, ldz, bias, act, x, xmode, ln_s, ln_b, out);
   return cudaGetLastError();
 }

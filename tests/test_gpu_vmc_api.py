@@ -224,3 +224,31 @@ def test_resume_from_checkpoint_continues_the_run(cuda_device, tmp_path):
         data2, state2, e = step(r["params"], data2, state2)
         np.testing.assert_array_equal(data2.electrons.cpu().numpy(), ref[it][0])
         np.testing.assert_array_equal(e, ref[it][1])
+
+
+def test_request_graph_matches_eager_calls(cuda_device):
+    """RequestGraph (MH with a device counter + local energy + mean/variance,
+    captured once and replayed) gives bitwise the results of the same eager
+    calls from the same walkers and counter."""
+    from jaqmc_gb300 import _native
+    from jaqmc_gb300 import params as P
+    from jaqmc_gb300 import systems as S
+    mol = S.lithium()
+    cfg = P.FermiNetConfig(nspins=mol.nspins, ndets=4, hidden_dims_single=[32, 32], hidden_dims_double=[8, 8])
+    tree = P.init_ferminet(cfg, mol.n_atoms, seed=0)
+    flat = torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, mol.n_atoms)), device=cuda_device)
+    m = _native.NativeFermiNet(cfg, mol.atoms, mol.charges, precision="fp32", device=cuda_device)
+    m.set_params(flat)
+    x0 = torch.as_tensor(S.init_walkers(mol, 64, seed=1), device=cuda_device)
+    xg = x0.clone()
+    rg = _native.RequestGraph(m, xg, 5, 0.05, 3, counter=7)  # one eager request, then capture
+    outs = [rg.run().clone() for _ in range(3)]
+    torch.cuda.synchronize()
+    xe = x0.clone()
+    for k in range(4):
+        m.mh_steps(xe, 5, 0.05, 3, 7 + 5 * k)
+        mv = _native.reduce_mean_var(m.local_energy(xe)["e_local"])
+        if k:
+            assert torch.equal(mv, outs[k - 1]), k
+    assert torch.equal(xe, xg)
+    assert int(rg.counter.item()) == 7 + 20
