@@ -526,8 +526,10 @@ def run_gradient(dev, steps, warmup, walkers=4096, budget_gb=8, burn_in=200, fd_
 # ----------------------------------------------------------------- serving
 def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
     """Poisson(rate) arrivals of neutral-atom jobs (Z ~ U{2..18}, Hund spins,
-    walkers ~ U{256..4096}), each ``requests`` requests of 20 MH steps + E_L
-    mean/variance in the mixed form, served with ``slots`` concurrent slots."""
+    walkers ~ U{256..4096}, parameters seed 0 so that jobs of one element
+    share a model), each ``requests`` requests of 20 MH steps + E_L
+    mean/variance in the mixed form, served with ``slots`` concurrent slots;
+    queued requests of jobs sharing a model are packed into one launch set."""
     from jaqmc_gb300 import serving as SV
     be = SV.CudaBackend(precision="mixed", mh_steps=20, stddev=0.02, device=dev)
     warm = SV.Server(be, n_slots=2, hbm_budget=budget_gb << 30)
@@ -546,7 +548,7 @@ def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
             "request_p99_ms": float(np.percentile(lat, 99)), "job_p50_ms": float(np.percentile(jl, 50)),
             "job_p99_ms": float(np.percentile(jl, 99)), "peak_hbm_gb": srv.peak_used / 1e9,
             "graph_replays": int(sum(r.graph for r in srv.finished)), "nonfinite_jobs": bad,
-            "span_s": span}
+            "span_s": span, "packing": srv.packing()}
 
 
 def run_request_only(args, wl):

@@ -244,6 +244,22 @@ qmc_status qmc_mh_steps_resident(qmc_model* m, int batch, int steps, float stdde
                                  uint8_t* flags, void* workspace, size_t workspace_bytes,
                                  cudaStream_t stream);
 
+/* Several jobs of one model in one MH batch: their walkers concatenated in
+ * `electrons` (batch = offsets[n_jobs] walkers; offsets, seeds and counters
+ * are device arrays of n_jobs + 1, n_jobs and n_jobs entries).  Job j's
+ * walkers [offsets[j], offsets[j + 1]) take exactly the proposals and
+ * acceptances of qmc_mh_steps_resident on that job alone with seed seeds[j]
+ * and counter counters[j]; every counter advances by `steps`.  This is the
+ * grouped launch of the serving loop, which packs queued requests of jobs
+ * that share a model into one launch set.  Each walker's log|psi| depends
+ * only on its own electrons, so the batch's composition does not change any
+ * job's results.  No counterpart in the reference (one process runs one
+ * job there). */
+qmc_status qmc_mh_steps_grouped(qmc_model* m, int n_jobs, const int* offsets, const uint64_t* seeds,
+                                uint64_t* counters, int batch, int steps, float stddev, float* electrons,
+                                float* log_prob, uint32_t* accepts, uint8_t* flags, void* workspace,
+                                size_t workspace_bytes, cudaStream_t stream);
+
 /* The draws qmc_mh_steps would use for (seed, counter, steps): normals
  * (steps,batch,n,3) and uniforms (steps,batch), either may be NULL. */
 qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
@@ -317,6 +333,12 @@ qmc_status qmc_model_set_energy_budget(qmc_model* m, size_t bytes);
 /* FP64 walker-batch mean and variance <x^2> - <x>^2 of a float32 vector,
  * NaNs skipped (src/jaqmc/estimator/base.py:27-53).  mean_var: 2 doubles. */
 qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t stream);
+/* The same per segment [offsets[s], offsets[s + 1]) of x (device offsets,
+ * n_segments + 1 entries) into mean_var[2 s], mean_var[2 s + 1]: each
+ * segment's result is bitwise that of qmc_reduce_mean_var on the segment
+ * alone (the per-job statistics of a grouped request). */
+qmc_status qmc_reduce_mean_var_segments(int n_segments, const int* offsets, const float* x, double* mean_var,
+                                        cudaStream_t stream);
 
 /* Effective-core-potential energy per walker: the reference's ECPEnergy
  * estimator (src/jaqmc/estimator/ecp/estimator.py:33-155, nonlocal integral

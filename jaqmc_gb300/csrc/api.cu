@@ -663,7 +663,7 @@ qmc_status check_call(qmc_model* m, int batch, const void* ws, size_t ws_bytes, 
 qmc_status mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t seed, uint64_t counter,
                     const uint64_t* ctr_dev, float* electrons, float* log_prob, uint32_t* accepts,
                     const float* inj_normals, const float* inj_uniforms, uint8_t* flags, void* ws,
-                    size_t ws_bytes, cudaStream_t s) {
+                    size_t ws_bytes, cudaStream_t s, const MhGroup& grp = MhGroup{}) {
   QMC_TRY(check_call(m, batch, ws, ws_bytes, QMC_OP_MH));
   if (!electrons || !log_prob || steps < 0) { set_error("bad electrons/log_prob/steps"); return QMC_ERR_ARG; }
   const bool psi = m->kind == QMC_KIND_PSIFORMER;
@@ -682,10 +682,11 @@ qmc_status mh_steps(qmc_model* m, int batch, int steps, float stddev, uint64_t s
   for (int st = 0; st < steps; ++st) {
     const float* nz = inj_normals ? inj_normals + (size_t)st * batch * n * 3 : nullptr;
     const float* uz = inj_uniforms ? inj_uniforms + (size_t)st * batch : nullptr;
-    QMC_PROF(QMC_KC_MH, launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, ctr_dev, nz));
+    QMC_PROF(QMC_KC_MH,
+             launch_mh_propose(s, batch, n, electrons, xp, stddev, seed, counter + st, ctr_dev, nz, grp));
     QMC_TRY(forward(xp, lpsi, nullptr));
     QMC_PROF(QMC_KC_MH, launch_mh_accept(s, batch, n, electrons, xp, log_prob, lpsi, seed, counter + st, ctr_dev,
-                                         uz, accepts));
+                                         uz, accepts, grp));
   }
   return QMC_OK;
 }
@@ -991,6 +992,25 @@ qmc_status qmc_mh_steps_resident(qmc_model* m, int batch, int steps, float stdde
   return QMC_OK;
 }
 
+qmc_status qmc_mh_steps_grouped(qmc_model* m, int n_jobs, const int* offsets, const uint64_t* seeds,
+                                uint64_t* counters, int batch, int steps, float stddev, float* electrons,
+                                float* log_prob, uint32_t* accepts, uint8_t* flags, void* ws, size_t ws_bytes,
+                                cudaStream_t s) {
+  if (n_jobs < 1 || n_jobs > 4096 || !offsets || !seeds || !counters) {
+    set_error("grouped MH: 1..4096 jobs and device offsets / seeds / counters");
+    return QMC_ERR_ARG;
+  }
+  MhGroup g;
+  g.n_jobs = n_jobs;
+  g.offsets = offsets;
+  g.seeds = seeds;
+  g.counters = counters;
+  QMC_TRY(qmc::mh_steps(m, batch, steps, stddev, 0, 0, nullptr, electrons, log_prob, accepts, nullptr, nullptr,
+                        flags, ws, ws_bytes, s, g));
+  QMC_PROF(QMC_KC_OTHER, launch_counter_add(s, counters, (uint64_t)steps, n_jobs));
+  return QMC_OK;
+}
+
 qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed, uint64_t counter,
                         float* normals, float* uniforms, cudaStream_t s) {
   if (!m || batch < 1 || steps < 1) { set_error("bad arguments"); return QMC_ERR_ARG; }
@@ -1001,6 +1021,16 @@ qmc_status qmc_mh_draws(const qmc_model* m, int batch, int steps, uint64_t seed,
 qmc_status qmc_reduce_mean_var(int batch, const float* x, double* mean_var, cudaStream_t s) {
   if (batch < 1 || !x || !mean_var) { set_error("bad arguments"); return QMC_ERR_ARG; }
   QMC_PROF(QMC_KC_OTHER, launch_reduce_mean_var(s, batch, x, mean_var));
+  return QMC_OK;
+}
+
+qmc_status qmc_reduce_mean_var_segments(int n_segments, const int* offsets, const float* x, double* mean_var,
+                                        cudaStream_t s) {
+  if (n_segments < 1 || n_segments > 65535 || !offsets || !x || !mean_var) {
+    set_error("bad arguments");
+    return QMC_ERR_ARG;
+  }
+  QMC_PROF(QMC_KC_OTHER, launch_reduce_mean_var(s, 0, x, mean_var, offsets, n_segments));
   return QMC_OK;
 }
 

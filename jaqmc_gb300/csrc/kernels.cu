@@ -2584,9 +2584,25 @@ __device__ __forceinline__ U4 draw_block(uint64_t seed, uint64_t step, int w, in
   return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 
+// Grouped MH (several jobs of one model in one batch): walker w belongs to the
+// job j with offsets[j] <= w < offsets[j + 1] and draws from that job's seed,
+// counter and its index within the job -- the draws of the job run alone.
+__device__ __forceinline__ int mh_stream(const MhGroup& g, int w, uint64_t* seed, uint64_t* step) {
+  if (g.n_jobs <= 0) return w;
+  int lo = 0, hi = g.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.offsets[mid] <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  *seed = g.seeds[lo];
+  *step += g.counters[lo];
+  return w - g.offsets[lo];
+}
+
 __global__ void k_mh_propose(int B, int n, const float* __restrict__ x, float* __restrict__ xp,
                              float stddev, uint64_t seed, uint64_t step,
-                             const uint64_t* __restrict__ ctr_dev, const float* __restrict__ inj) {
+                             const uint64_t* __restrict__ ctr_dev, const float* __restrict__ inj, MhGroup grp) {
   const int nb = normal_blocks(n);
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (size_t)B * nb) return;
@@ -2600,7 +2616,8 @@ __global__ void k_mh_propose(int B, int n, const float* __restrict__ x, float* _
       z[q] = c < 3 * n ? inj[(size_t)w * 3 * n + c] : 0.f;
     }
   } else {
-    U4 r = draw_block(seed, step, w, b);
+    const int wl = mh_stream(grp, w, &seed, &step);
+    U4 r = draw_block(seed, step, wl, b);
     box_muller(r.x, r.y, &z[0], &z[1]);
     box_muller(r.z, r.w, &z[2], &z[3]);
   }
@@ -2616,20 +2633,26 @@ __global__ void k_mh_propose(int B, int n, const float* __restrict__ x, float* _
 
 cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
                               float stddev, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
-                              const float* inj) {
+                              const float* inj, const MhGroup& grp) {
   size_t total = (size_t)B * normal_blocks(n);
-  k_mh_propose<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, x, xp, stddev, seed, ctr, ctr_dev, inj);
+  k_mh_propose<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(B, n, x, xp, stddev, seed, ctr, ctr_dev, inj, grp);
   return cudaGetLastError();
 }
 
 __global__ void k_mh_accept(int B, int n, float* __restrict__ x, const float* __restrict__ xp,
                             float* __restrict__ lp, const float* __restrict__ logpsi_p,
                             uint64_t seed, uint64_t step, const uint64_t* __restrict__ ctr_dev,
-                            const float* __restrict__ inj, uint32_t* __restrict__ accepts) {
+                            const float* __restrict__ inj, uint32_t* __restrict__ accepts, MhGroup grp) {
   int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= B) return;
   if (ctr_dev) step += *ctr_dev;
-  float u = inj ? inj[w] : u01(draw_block(seed, step, w, normal_blocks(n)).x);
+  float u;
+  if (inj) {
+    u = inj[w];
+  } else {
+    const int wl = mh_stream(grp, w, &seed, &step);
+    u = u01(draw_block(seed, step, wl, normal_blocks(n)).x);
+  }
   float lp2 = 2.0f * logpsi_p[w];
   float ratio = lp2 - lp[w];
   bool cond = ratio > logf(u);
@@ -2642,18 +2665,19 @@ __global__ void k_mh_accept(int B, int n, float* __restrict__ x, const float* __
 
 cudaError_t launch_mh_accept(cudaStream_t s, int B, int n, float* x, const float* xp, float* lp,
                              const float* logpsi_p, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
-                             const float* inj_uniforms, uint32_t* accepts) {
+                             const float* inj_uniforms, uint32_t* accepts, const MhGroup& grp) {
   k_mh_accept<<<(B + 127) / 128, 128, 0, s>>>(B, n, x, xp, lp, logpsi_p, seed, ctr, ctr_dev, inj_uniforms,
-                                              accepts);
+                                              accepts, grp);
   return cudaGetLastError();
 }
 
-__global__ void k_counter_add(uint64_t* ctr, uint64_t inc) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *ctr += inc;
+__global__ void k_counter_add(int count, uint64_t* ctr, uint64_t inc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) ctr[i] += inc;
 }
 
-cudaError_t launch_counter_add(cudaStream_t s, uint64_t* ctr, uint64_t inc) {
-  k_counter_add<<<1, 32, 0, s>>>(ctr, inc);
+cudaError_t launch_counter_add(cudaStream_t s, uint64_t* ctr, uint64_t inc, int count) {
+  k_counter_add<<<(count + 255) / 256, 256, 0, s>>>(count, ctr, inc);
   return cudaGetLastError();
 }
 
@@ -2699,9 +2723,19 @@ cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float*
 // =====================================================================
 // FP64 batch mean / variance (src/jaqmc/estimator/base.py:27-53)
 // =====================================================================
-__global__ void k_reduce_mean_var(int B, const float* __restrict__ x, double* __restrict__ out) {
+// FP64 mean and variance of x[0, B) (offsets null), or one block per segment
+// [offsets[s], offsets[s + 1]) into out[2 s], out[2 s + 1] in the same order
+// of summation, so a segment's result equals the call on that segment alone.
+__global__ void k_reduce_mean_var(int B, const float* __restrict__ x, double* __restrict__ out,
+                                  const int* __restrict__ offsets) {
   __shared__ double s1[32], s2[32];
   __shared__ int sc[32];
+  if (offsets) {
+    const int o0 = offsets[blockIdx.x];
+    B = offsets[blockIdx.x + 1] - o0;
+    x += o0;
+    out += 2 * blockIdx.x;
+  }
   double a = 0.0, b = 0.0;
   int c = 0;
   for (int i = threadIdx.x; i < B; i += blockDim.x) {
@@ -2734,8 +2768,9 @@ __global__ void k_reduce_mean_var(int B, const float* __restrict__ x, double* __
   }
 }
 
-cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out) {
-  k_reduce_mean_var<<<1, 1024, 0, s>>>(B, x, out);
+cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out, const int* offsets,
+                                   int segments) {
+  k_reduce_mean_var<<<offsets ? segments : 1, 1024, 0, s>>>(B, x, out, offsets);
   return cudaGetLastError();
 }
 

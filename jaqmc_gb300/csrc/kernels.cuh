@@ -108,22 +108,35 @@ template <class Out>
 cudaError_t launch_pair_stream_value(cudaStream_t s, int B, const PairStreamArgs& a, const PairStreamOut<Out>& o);
 
 
+// Several jobs of one model in one MH batch (device tables): job j owns
+// walkers [offsets[j], offsets[j + 1]) and draws from seeds[j] with update
+// index counters[j] + step, indexed by the walker's position in its job.
+struct MhGroup {
+  int n_jobs = 0;
+  const int* offsets = nullptr;
+  const uint64_t* seeds = nullptr;
+  const uint64_t* counters = nullptr;
+};
+
 // MH proposal x' = x + stddev * N(0,1) for update `step` of a call.
 // The update index is ctr (+ *ctr_dev when ctr_dev is not null).
 cudaError_t launch_mh_propose(cudaStream_t s, int B, int n, const float* x, float* xp,
                               float stddev, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
-                              const float* inj_normals);
+                              const float* inj_normals, const MhGroup& grp = MhGroup{});
 // Accept/reject with 2 log|psi| and the draw for update `ctr` (+ *ctr_dev).
 cudaError_t launch_mh_accept(cudaStream_t s, int B, int n, float* x, const float* xp, float* lp,
                              const float* logpsi_p, uint64_t seed, uint64_t ctr, const uint64_t* ctr_dev,
-                             const float* inj_uniforms, uint32_t* accepts);
-// *ctr += inc on the stream.
-cudaError_t launch_counter_add(cudaStream_t s, uint64_t* ctr, uint64_t inc);
+                             const float* inj_uniforms, uint32_t* accepts, const MhGroup& grp = MhGroup{});
+// ctr[0 .. count) += inc on the stream.
+cudaError_t launch_counter_add(cudaStream_t s, uint64_t* ctr, uint64_t inc, int count = 1);
 cudaError_t launch_mh_draws(cudaStream_t s, int B, int n, int steps, uint64_t seed, uint64_t ctr,
                             float* normals, float* uniforms);
 cudaError_t launch_scale(cudaStream_t s, int B, const float* in, float c, float* out);
 
-cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out);
+// FP64 mean/variance of x[0, B), or per segment [offsets[s], offsets[s + 1])
+// (device offsets, `segments` of them) into out[2 s], out[2 s + 1].
+cudaError_t launch_reduce_mean_var(cudaStream_t s, int B, const float* x, double* out,
+                                   const int* offsets = nullptr, int segments = 1);
 
 // fp32 [rows][cols] (row stride ld_in) -> fp32 transposed [cols][rows]
 cudaError_t launch_transpose_f32(cudaStream_t s, const float* in, int rows, int cols, int ld_in, float* out);

@@ -21,15 +21,23 @@ Scheduling:
   that of the slot's previous request (its workspace is sized for it, and a
   captured graph may exist), else the oldest request that fits; a workspace
   grows only while the budget allows it;
-* with ``use_graphs`` each (job, slot) pair's request is captured once into a
-  CUDA graph (the Philox counter lives in device memory and advances inside
-  the graph) and replayed; the first request of a pair runs eagerly;
+* requests are packed: a slot that takes a request also takes up to
+  ``group_max - 1`` more queued requests of other jobs that share its model
+  (same atom, configuration and parameters, hence the same electron count),
+  and runs them as one launch set over their concatenated walkers
+  (``qmc_mh_steps_grouped``, where each job keeps its own Philox seed and
+  device counter, then one ``qmc_local_energy`` and a per-job
+  ``qmc_reduce_mean_var_segments``);
+* with ``use_graphs`` each (job, slot) pair's single-job request is captured
+  once into a CUDA graph (the Philox counter lives in device memory and
+  advances inside the graph) and replayed; the first request of a pair runs
+  eagerly, and so do packed groups (their membership changes);
 * completion is tracked with CUDA events and results come back through pinned
   host memory; a request's latency is completion minus submission.
 
 A job's results depend only on its own state and counters: they are bitwise
-the same whether the job runs alone or among others, on any slot, eagerly or
-from a graph.
+the same whether the job runs alone or among others, packed or not, on any
+slot, eagerly or from a graph.
 """
 from __future__ import annotations
 
@@ -49,8 +57,13 @@ class JobSpec:
     mol: S.Molecule
     walkers: int
     requests: int = 1
-    seed: int = 0
+    seed: int = 0              # walkers and Philox stream (and parameters when param_seed is None)
     arrival: float = 0.0
+    param_seed: int | None = None  # parameters; jobs with equal seeds and systems share a model
+
+    @property
+    def params_seed(self) -> int:
+        return self.seed if self.param_seed is None else self.param_seed
 
 
 @dataclass
@@ -62,6 +75,7 @@ class Request:
     done: float | None = None
     slot: int | None = None
     graph: bool = False
+    group: int = 1           # requests in the launch set (packed jobs)
     result: np.ndarray | None = None
 
 
@@ -89,7 +103,8 @@ class Slot:
     ws: object = None
     ws_bytes: int = 0
     last_n: int = -1
-    request: Request | None = None
+    request: Request | None = None               # the first request of the launch set
+    group: list = field(default_factory=list)    # every request of the launch set
     event: object = None
     graphs: dict = field(default_factory=dict)
 
@@ -99,10 +114,14 @@ class Server:
     GPU, or a simulated backend for testing the scheduling logic)."""
 
     def __init__(self, backend, n_slots: int = 8, hbm_budget: int = 150 << 30, use_graphs: bool = True,
-                 clock=time.perf_counter):
+                 clock=time.perf_counter, group_max: int = 8, group_walkers: int = 8192):
         self.backend = backend
         self.budget = int(hbm_budget)
         self.use_graphs = bool(use_graphs)
+        self.group_max = int(group_max) if hasattr(backend, "run_group") else 1
+        self.group_walkers = int(group_walkers)
+        self.launches = 0
+        self.packed_launches = 0
         self.clock = clock
         self.t0 = clock()
         self.slots = [Slot(i, backend.new_stream()) for i in range(n_slots)]
@@ -185,8 +204,11 @@ class Server:
                 self.used -= s.ws_bytes
                 s.ws_bytes = 0
 
+    def _busy_jobs(self) -> set:
+        return {r.job_id for s in self.slots for r in s.group}
+
     def _pick(self, slot: Slot):
-        busy = {s.request.job_id for s in self.slots if s.request is not None}
+        busy = self._busy_jobs()
         cands = [r for r in self.queue if r.job_id not in busy]
         if not cands:
             return None
@@ -202,20 +224,55 @@ class Server:
             return oldest
         return None
 
-    def _launch(self, slot: Slot, r: Request):
+    def _pack(self, slot: Slot, r: Request) -> list:
+        """``r`` and up to group_max - 1 queued requests of other idle jobs with
+        r's model, oldest first, within the walker cap; the group only if the
+        slot's workspace can hold it."""
+        if self.group_max <= 1:
+            return [r]
+        spec = self.jobs[r.job_id].spec
+        key = self.backend.model_key(spec)
+        busy = self._busy_jobs() | {r.job_id}
+        group, specs, total = [r], [spec], spec.walkers
+        for q in self.queue:
+            if len(group) >= self.group_max:
+                break
+            st = self.jobs[q.job_id]
+            if q.job_id in busy or self.backend.model_key(st.spec) != key:
+                continue
+            if total + st.spec.walkers > self.group_walkers:
+                continue
+            group.append(q)
+            specs.append(st.spec)
+            busy.add(q.job_id)
+            total += st.spec.walkers
+        if len(group) > 1 and not self._fit(slot, self.backend.group_request_bytes(specs)):
+            return [r]
+        return group
+
+    def _launch(self, slot: Slot, group: list):
+        r = group[0]
         st = self.jobs[r.job_id]
         jid = st.spec.job_id
-        g = slot.graphs.get(jid) if self.use_graphs else None
-        if g is not None:
-            self.backend.replay(g, slot.stream)
-            r.graph = True
+        if len(group) > 1:
+            self.backend.run_group([self.jobs[q.job_id].handle for q in group], slot.ws, slot.ws_bytes,
+                                   slot.stream)
+            self.packed_launches += 1
         else:
-            self.backend.run_request(st.handle, slot.ws, slot.ws_bytes, slot.stream)
-            if self.use_graphs:
-                slot.graphs[jid] = self.backend.capture(st.handle, slot.ws, slot.ws_bytes, slot.stream)
+            g = slot.graphs.get(jid) if self.use_graphs else None
+            if g is not None:
+                self.backend.replay(g, slot.stream)
+                r.graph = True
+            else:
+                self.backend.run_request(st.handle, slot.ws, slot.ws_bytes, slot.stream)
+                if self.use_graphs:
+                    slot.graphs[jid] = self.backend.capture(st.handle, slot.ws, slot.ws_bytes, slot.stream)
+        self.launches += 1
         slot.event = self.backend.record(slot.stream)
-        slot.request, slot.last_n = r, st.n_electrons
-        r.start, r.slot = self.now(), slot.index
+        slot.request, slot.group, slot.last_n = r, list(group), st.n_electrons
+        now = self.now()
+        for q in group:
+            q.start, q.slot, q.group = now, slot.index, len(group)
 
     def _dispatch(self):
         for slot in self.slots:
@@ -225,24 +282,28 @@ class Server:
             if r is None:
                 continue
             self.queue.remove(r)
-            self._launch(slot, r)
+            group = self._pack(slot, r)
+            for q in group[1:]:
+                self.queue.remove(q)
+            self._launch(slot, group)
 
     def _reap(self):
         for slot in self.slots:
-            r = slot.request
-            if r is None or not self.backend.query(slot.event):
+            if slot.request is None or not self.backend.query(slot.event):
                 continue
-            st = self.jobs[r.job_id]
-            r.result = self.backend.result(st.handle)
-            r.done = self.now()
-            slot.request = slot.event = None
-            self.finished.append(r)
-            st.results.append(r.result)
-            st.completed += 1
-            if st.completed == st.spec.requests:
-                self._release(st)
-            else:
-                self._submit_next(st)
+            done = self.now()
+            group, slot.request, slot.group, slot.event = slot.group, None, [], None
+            for r in group:
+                st = self.jobs[r.job_id]
+                r.result = self.backend.result(st.handle)
+                r.done = done
+                self.finished.append(r)
+                st.results.append(r.result)
+                st.completed += 1
+                if st.completed == st.spec.requests:
+                    self._release(st)
+                else:
+                    self._submit_next(st)
 
     def step(self):
         self._reap()
@@ -251,6 +312,12 @@ class Server:
 
     def busy(self) -> bool:
         return bool(self.pending_jobs or self.queue or any(s.request is not None for s in self.slots))
+
+    def packing(self) -> dict:
+        """Launch sets issued, how many were packed, and requests per launch."""
+        n = len(self.finished)
+        return {"launches": self.launches, "packed_launches": self.packed_launches,
+                "requests_per_launch": n / self.launches if self.launches else 0.0}
 
     def drain(self, timeout: float = 600.0, poll: float = 1e-4):
         t = self.clock()
@@ -290,24 +357,29 @@ class Server:
 
 
 def atom_job_specs(n_jobs: int, rate: float, seed: int = 0, requests: int = 1,
-                   walker_choices=(256, 512, 1024, 2048, 4096), z_range=(2, 18)) -> list[JobSpec]:
+                   walker_choices=(256, 512, 1024, 2048, 4096), z_range=(2, 18),
+                   param_seed: int | None = 0) -> list[JobSpec]:
     """Poisson arrivals (rate jobs/s) of neutral atoms with Z ~ U{z_range}
     (Hund's-rule spins) and walker counts ~ U(walker_choices); job j uses
-    seed j for its parameters, walkers and Philox stream."""
+    seed j for its walkers and Philox stream and ``param_seed`` for its
+    parameters (None: seed j), so jobs of one element share a model."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_jobs)) if rate > 0 else np.zeros(n_jobs)
     specs = []
     for j in range(n_jobs):
         z = int(rng.integers(z_range[0], z_range[1] + 1))
         B = int(rng.choice(walker_choices))
-        specs.append(JobSpec(j, S.atom(z), B, requests, seed=j, arrival=float(arrivals[j])))
+        specs.append(JobSpec(j, S.atom(z), B, requests, seed=j, arrival=float(arrivals[j]), param_seed=param_seed))
     return specs
 
 
 class CudaBackend:
-    """Device side of the server: one qmc model per job, a request is
+    """Device side of the server: one qmc model per (system, configuration,
+    parameter seed), shared by the jobs that use it; a request is
     qmc_mh_steps_resident + qmc_local_energy + qmc_reduce_mean_var on the
-    slot's stream, results come back through pinned host memory."""
+    slot's stream, a packed group qmc_mh_steps_grouped + qmc_local_energy +
+    qmc_reduce_mean_var_segments over the jobs' concatenated walkers; results
+    come back through pinned host memory."""
 
     def __init__(self, precision: str = "mixed", mh_steps: int = 20, stddev: float = 0.02, device=None,
                  config=None):
@@ -325,6 +397,7 @@ class CudaBackend:
         self.stddev = float(stddev)
         self.config = dict(config or {})
         self._ws_sizes: dict = {}
+        self._models: dict = {}  # model key -> (model, reference count)
 
     def cfg(self, spec: JobSpec):
         return P.FermiNetConfig(nspins=spec.mol.nspins, **self.config)
@@ -339,26 +412,44 @@ class CudaBackend:
         # FP32 arena with transposed copies, two BF16 planes, the walker buffers
         return int(12 * npar + 4 * npar + spec.walkers * (12 * n + 16) + 4096)
 
-    def request_bytes(self, spec: JobSpec) -> int:
-        key = (spec.mol.nspins, spec.mol.n_atoms, spec.walkers)
+    def _ws_bytes(self, spec: JobSpec, walkers: int) -> int:
+        key = (spec.mol.nspins, spec.mol.n_atoms, walkers)
         if key not in self._ws_sizes:
-            m = self._model(spec)
-            self._ws_sizes[key] = max(int(self.lib.qmc_workspace_size(m.h, self.native.OP_MH, spec.walkers)),
-                                      int(self.lib.qmc_workspace_size(m.h, self.native.OP_LOCAL_ENERGY,
-                                                                      spec.walkers)))
+            m = self.native.NativeFermiNet(self.cfg(spec), spec.mol.atoms, spec.mol.charges,
+                                           precision=self.precision, device=self.device)
+            self._ws_sizes[key] = max(int(self.lib.qmc_workspace_size(m.h, self.native.OP_MH, walkers)),
+                                      int(self.lib.qmc_workspace_size(m.h, self.native.OP_LOCAL_ENERGY, walkers)))
         return self._ws_sizes[key]
 
+    def request_bytes(self, spec: JobSpec) -> int:
+        return self._ws_bytes(spec, spec.walkers)
+
+    def group_request_bytes(self, specs) -> int:
+        return self._ws_bytes(specs[0], sum(sp.walkers for sp in specs))
+
+    def model_key(self, spec: JobSpec):
+        mol = spec.mol
+        return (tuple(mol.nspins), np.asarray(mol.atoms, np.float32).tobytes(),
+                np.asarray(mol.charges, np.float32).tobytes(), tuple(sorted(self.config.items())), spec.params_seed)
+
     def _model(self, spec: JobSpec):
-        return self.native.NativeFermiNet(self.cfg(spec), spec.mol.atoms, spec.mol.charges,
-                                          precision=self.precision, device=self.device)
+        key = self.model_key(spec)
+        if key in self._models:
+            m, refs = self._models[key]
+            self._models[key] = (m, refs + 1)
+            return m
+        cfg = self.cfg(spec)
+        m = self.native.NativeFermiNet(cfg, spec.mol.atoms, spec.mol.charges, precision=self.precision,
+                                       device=self.device)
+        tree = P.init_ferminet(cfg, spec.mol.n_atoms, seed=spec.params_seed)
+        flat = self.torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, spec.mol.n_atoms)))
+        m.set_params(flat.to(self.device))
+        self._models[key] = (m, 1)
+        return m
 
     def create_job(self, spec: JobSpec):
         torch = self.torch
-        cfg = self.cfg(spec)
         m = self._model(spec)
-        tree = P.init_ferminet(cfg, spec.mol.n_atoms, seed=spec.seed)
-        flat = torch.as_tensor(P.flatten(tree, P.ferminet_leaves(cfg, spec.mol.n_atoms)))
-        m.set_params(flat.to(self.device))
         B = spec.walkers
         x = torch.as_tensor(S.init_walkers(spec.mol, B, seed=spec.seed + 1)).to(self.device).contiguous()
         h = {
@@ -376,6 +467,12 @@ class CudaBackend:
         return h
 
     def release_job(self, h):
+        key = self.model_key(h["spec"])
+        m, refs = self._models[key]
+        if refs <= 1:
+            del self._models[key]
+        else:
+            self._models[key] = (m, refs - 1)
         h.clear()
 
     def new_workspace(self, nbytes: int, stream):
@@ -404,6 +501,46 @@ class CudaBackend:
     def run_request(self, h, ws, ws_bytes, stream):
         with self.torch.cuda.stream(stream):
             self._enqueue(h, ws, ws_bytes, stream)
+
+    def run_group(self, hs, ws, ws_bytes, stream):
+        """One launch set for the requests of jobs sharing a model: their
+        walkers, counters and seeds gathered, grouped MH + local energy over
+        the concatenation, per-job statistics, then everything scattered back."""
+        torch, lib, check = self.torch, self.lib, self.native.check
+        m = hs[0]["model"]
+        Bs = [h["spec"].walkers for h in hs]
+        offs = np.concatenate([[0], np.cumsum(Bs)]).astype(np.int32)
+        total = int(offs[-1])
+        st = stream.cuda_stream
+        with torch.cuda.stream(stream):
+            host = torch.empty(len(hs) * 3 + 1, dtype=torch.int64).pin_memory()
+            host[:len(hs) + 1] = torch.as_tensor(offs.astype(np.int64))
+            host[len(hs) + 1:2 * len(hs) + 1] = torch.as_tensor([h["spec"].seed for h in hs], dtype=torch.int64)
+            tables = host.to(self.device, non_blocking=True)
+            off_d = tables[:len(hs) + 1].to(torch.int32)
+            seeds = tables[len(hs) + 1:2 * len(hs) + 1].contiguous()
+            ctr = torch.cat([h["counter"] for h in hs])
+            x = torch.cat([h["electrons"] for h in hs])
+            lp = torch.empty(total, dtype=torch.float32, device=self.device)
+            acc = torch.zeros(total, dtype=torch.int32, device=self.device)
+            el = torch.empty(total, dtype=torch.float32, device=self.device)
+            mv = torch.empty((len(hs), 2), dtype=torch.float64, device=self.device)
+            check(lib.qmc_mh_steps_grouped(m.h, len(hs), off_d.data_ptr(), seeds.data_ptr(), ctr.data_ptr(), total,
+                                           self.mh_steps, self.stddev, x.data_ptr(), lp.data_ptr(), acc.data_ptr(),
+                                           None, ws.data_ptr(), ws_bytes, st))
+            check(lib.qmc_local_energy(m.h, total, x.data_ptr(), el.data_ptr(), None, None, None, None,
+                                       ws.data_ptr(), ws_bytes, st))
+            check(lib.qmc_reduce_mean_var_segments(len(hs), off_d.data_ptr(), el.data_ptr(), mv.data_ptr(), st))
+            for j, h in enumerate(hs):
+                o, B = int(offs[j]), Bs[j]
+                h["electrons"].copy_(x[o:o + B])
+                h["counter"].copy_(ctr[j:j + 1])
+                h["mean_var"].copy_(mv[j])
+                torch.sum(acc[o:o + B], dim=0, keepdim=True, dtype=torch.float64, out=h["acc_sum"])
+                h["host"][:2].copy_(h["mean_var"], non_blocking=True)
+                h["host"][2:].copy_(h["acc_sum"], non_blocking=True)
+            # the pinned tables stay alive until the copies that read them ran
+            hs[0]["_group_tables"] = host
 
     def capture(self, h, ws, ws_bytes, stream):
         torch = self.torch

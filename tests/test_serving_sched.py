@@ -179,3 +179,57 @@ def test_workspace_shrinks_for_starved_request():
              SV.JobSpec(2, S.atom(18), 256, requests=1, arrival=0.01)]
     _serve(srv, clock, specs)
     assert len(srv.finished_jobs) == 3
+
+
+class PackingBackend(FakeBackend):
+    """FakeBackend that also runs packed groups (one launch set for requests
+    of jobs sharing a model)."""
+
+    def __init__(self, clock, **kw):
+        super().__init__(clock, **kw)
+        self.groups = []
+
+    def model_key(self, spec):
+        return (spec.mol.n_electrons, spec.params_seed)
+
+    def group_request_bytes(self, specs):
+        return sum(self.req_bytes(sp) for sp in specs)
+
+    def run_group(self, hs, ws, ws_bytes, stream):
+        assert ws_bytes >= self.group_request_bytes([h["spec"] for h in hs])
+        assert len({self.model_key(h["spec"]) for h in hs}) == 1
+        self.groups.append([h["spec"].job_id for h in hs])
+        end = self.clock() + 1e-6 * sum(h["spec"].walkers for h in hs) * hs[0]["spec"].mol.n_electrons
+        self.inflight[id(stream)] = end
+        for h in hs:
+            h["count"] += 1
+            self.log.append((self.clock(), h["spec"].job_id, h["count"]))
+
+
+def test_requests_of_a_shared_model_are_packed():
+    clock = Clock()
+    be = PackingBackend(clock)
+    srv = SV.Server(be, n_slots=1, hbm_budget=1 << 30, clock=clock, group_max=4)
+    # six jobs of one model (carbon, parameters seed 0), two of another
+    specs = [SV.JobSpec(j, S.atom(6), 256, requests=2, seed=j, param_seed=0) for j in range(6)]
+    specs += [SV.JobSpec(6 + j, S.atom(8), 256, requests=2, seed=6 + j, param_seed=0) for j in range(2)]
+    _serve(srv, clock, specs)
+    assert len(srv.finished_jobs) == 8
+    for st in srv.finished_jobs:
+        assert [int(r[1]) for r in st.results] == [1, 2]
+    assert be.groups and max(len(g) for g in be.groups) == 4
+    for g in be.groups:
+        assert len(set(g)) == len(g)
+        assert len({6 if j < 6 else 8 for j in g}) == 1  # never across models
+    pk = srv.packing()
+    assert pk["packed_launches"] == len(be.groups)
+    assert pk["requests_per_launch"] > 1.5
+
+
+def test_packing_off_for_one_job_per_launch():
+    clock = Clock()
+    be = PackingBackend(clock)
+    srv = SV.Server(be, n_slots=2, hbm_budget=1 << 30, clock=clock, group_max=1)
+    specs = [SV.JobSpec(j, S.atom(6), 256, requests=2, seed=j, param_seed=0) for j in range(4)]
+    _serve(srv, clock, specs)
+    assert not be.groups and srv.packing()["requests_per_launch"] == 1.0
