@@ -1594,23 +1594,68 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// One tangent direction of the double-float stage: M = A^-1 J (A^-1 as the
+// FP32 pair Ah + Al, J in FP32) with error-free products and sums into the
+// hi/lo tiles Mh / Ml; returns tr M and tr M^2 in FP64 (every lane).
 template <int NMAX>
-__device__ DetOut det_stage_df(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, char* scratch,
-                               float* t1s) {
+__device__ void df_direction(const float* Ah, const float* Al, const float* __restrict__ J, float* Mh, float* Ml,
+                             int n, int ld, int ldm, int rs, double* tr_out, double* t2_out) {
+  const int lane = threadIdx.x & 31;
+  double tr = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    float x[NMAX];
+#pragma unroll
+    for (int m = 0; m < NMAX; ++m) x[m] = m < n ? J[m * rs + j] : 0.f;
+    for (int i = 0; i < n; ++i) {
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int m = 0; m < NMAX; ++m) {
+        if (m < n) {
+          const float a = Ah[i * ld + m];
+          const float p = a * x[m];
+          const float pe = fmaf(a, x[m], -p);
+          float s2, se;
+          two_sum(sh, p, s2, se);
+          sh = s2;
+          sl += se + fmaf(Al[i * ld + m], x[m], pe);
+        }
+      }
+      const float hv = sh + sl;
+      const float lv = sl - (hv - sh);
+      Mh[i * ldm + j] = hv;
+      Ml[i * ldm + j] = lv;
+      if (i == j) tr += (double)hv + (double)lv;
+    }
+  }
+  tr = warp_sum(tr);
+  __syncwarp();
+  double t2 = 0.0;
+  for (int j = lane; j < n; j += 32)
+    for (int i = 0; i < n; ++i)
+      t2 = fma((double)Mh[i * ldm + j] + (double)Ml[i * ldm + j], (double)Mh[j * ldm + i] + (double)Ml[j * ldm + i],
+               t2);
+  t2 = warp_sum(t2);
+  __syncwarp();
+  *tr_out = tr;
+  *t2_out = t2;
+}
+
+// FP64 LU and inverse of A_k by one warp into the scratch (LU, A^-1 as
+// doubles), then A^-1 split into the FP32 pair Ah + Al over the LU space and
+// tr(A^-1 L) in FP64.  Returns the determinant's log, sign and singularity.
+__device__ DetOut df_factor(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, double* LU, int* perm,
+                            float** Ah_out, float** Al_out, double* tl_out) {
   const int lane = threadIdx.x & 31;
   const DetScratch sc(n);
-  const int ld = sc.ld, ldm = sc.ldm;
-  double* LU = reinterpret_cast<double*>(scratch);
+  const int ld = sc.ld;
   double* Ai = LU + n * ld;
-  float* Mh = reinterpret_cast<float*>(Ai + n * ld);  // [n][ldm]
-  float* Ml = Mh + n * ldm;                            // [n][ldm] (both inside the 2 n ldm doubles)
-  int* perm = reinterpret_cast<int*>(scratch + (size_t)(2 * n * ld + 2 * n * ldm) * 8);
   DetOut o{};
   for (int e = lane; e < n * n; e += 32) LU[(e / n) * ld + (e % n)] = (double)Ak[(e / n) * rs + (e % n)];
   __syncwarp();
   double growth;
   warp_lu<double>(LU, n, ld, perm, &o.ld, &o.sgn, &growth, &o.singular);
   o.refactor = 1;
+  *tl_out = 0.0;
   if (o.singular || T <= 1) return o;
   warp_inverse<double>(LU, Ai, perm, n, ld);
   float* Ah = reinterpret_cast<float*>(LU);  // the factors are no longer needed
@@ -1623,52 +1668,35 @@ __device__ DetOut det_stage_df(const float* __restrict__ Ak, int n, int T, int r
   }
   __syncwarp();
   double tl = 0.0;
-  {
-    const float* L = Ak + ts;
-    for (int e = lane; e < n * n; e += 32) {
-      const int m = e / n, i = e - m * n;
-      tl = fma(Ai[i * ld + m], (double)L[m * rs + i], tl);
-    }
-    tl = warp_sum(tl);
+  const float* L = Ak + ts;
+  for (int e = lane; e < n * n; e += 32) {
+    const int m = e / n, i = e - m * n;
+    tl = fma(Ai[i * ld + m], (double)L[m * rs + i], tl);
   }
+  *tl_out = warp_sum(tl);
+  *Ah_out = Ah;
+  *Al_out = Al;
+  return o;
+}
+
+template <int NMAX>
+__device__ DetOut det_stage_df(const float* __restrict__ Ak, int n, int T, int rs, size_t ts, char* scratch,
+                               float* t1s) {
+  const int lane = threadIdx.x & 31;
+  const DetScratch sc(n);
+  const int ld = sc.ld, ldm = sc.ldm;
+  double* LU = reinterpret_cast<double*>(scratch);
+  float* Mh = reinterpret_cast<float*>(LU + 2 * n * ld);  // [n][ldm]
+  float* Ml = Mh + n * ldm;                               // [n][ldm] (both inside the 2 n ldm doubles)
+  int* perm = reinterpret_cast<int*>(scratch + (size_t)(2 * n * ld + 2 * n * ldm) * 8);
+  float *Ah = nullptr, *Al = nullptr;
+  double tl;
+  DetOut o = df_factor(Ak, n, T, rs, ts, LU, perm, &Ah, &Al, &tl);
+  if (o.singular || T <= 1) return o;
   double t2acc = 0.0, qacc = 0.0;
   for (int t = 2; t < T; ++t) {
-    const float* J = Ak + (size_t)t * ts;
-    double tr = 0.0;
-    for (int j = lane; j < n; j += 32) {
-      float x[NMAX];
-#pragma unroll
-      for (int m = 0; m < NMAX; ++m) x[m] = m < n ? J[m * rs + j] : 0.f;
-      for (int i = 0; i < n; ++i) {
-        float sh = 0.f, sl = 0.f;
-#pragma unroll
-        for (int m = 0; m < NMAX; ++m) {
-          if (m < n) {
-            const float a = Ah[i * ld + m];
-            const float p = a * x[m];
-            const float pe = fmaf(a, x[m], -p);
-            float s2, se;
-            two_sum(sh, p, s2, se);
-            sh = s2;
-            sl += se + fmaf(Al[i * ld + m], x[m], pe);
-          }
-        }
-        const float hv = sh + sl;
-        const float lv = sl - (hv - sh);
-        Mh[i * ldm + j] = hv;
-        Ml[i * ldm + j] = lv;
-        if (i == j) tr += (double)hv + (double)lv;
-      }
-    }
-    tr = warp_sum(tr);
-    __syncwarp();
-    double t2 = 0.0;
-    for (int j = lane; j < n; j += 32)
-      for (int i = 0; i < n; ++i)
-        t2 = fma((double)Mh[i * ldm + j] + (double)Ml[i * ldm + j], (double)Mh[j * ldm + i] + (double)Ml[j * ldm + i],
-                 t2);
-    t2 = warp_sum(t2);
-    __syncwarp();
+    double tr, t2;
+    df_direction<NMAX>(Ah, Al, Ak + (size_t)t * ts, Mh, Ml, n, ld, ldm, rs, &tr, &t2);
     if (lane == 0) t1s[t - 2] = (float)tr;
     t2acc += t2;
     qacc = fma(tr, tr, qacc);
@@ -2032,9 +2060,28 @@ __global__ void __launch_bounds__(256, 2) k_logdet_fl_wide(int n, int K, int Tp,
   logdet_finish(w, K, T, lds, kins, sgs, tLs, t2s, qs, t1s, ints, pe, logpsi, sign, ke, el, flags, nullptr, gl_add);
 }
 
+// Double-float re-evaluation of a marked (walker, determinant): a block of
+// kDet64Warps warps; warp 0 factorises and inverts A_k in FP64 and forms
+// tr(A^-1 L), then every warp takes a share of the Jacobian directions with
+// its own product tiles; the FP64 sums over directions are combined in warp
+// order.  Shared memory: LU and A^-1 (doubles), the permutation, then the
+// per-warp hi/lo product tiles.
+constexpr int kDet64Warps = 4;
+struct Det64Shape {
+  size_t head, per_warp, bytes;
+  __host__ __device__ Det64Shape(int n) {
+    const DetScratch sc(n);
+    head = align_up((size_t)2 * n * sc.ld * 8 + (size_t)n * 4, 16) + 64;
+    per_warp = align_up((size_t)2 * n * sc.ldm * 4, 16);
+    bytes = head + kDet64Warps * per_warp + (size_t)kDet64Warps * 2 * 8;
+  }
+};
+
 template <int NMAX>
-__global__ void __launch_bounds__(32) k_logdet_fl_det64(int n, int K, int Tp, int T, const float* __restrict__ A,
-                                                         const uint8_t* __restrict__ redo, char* __restrict__ records) {
+__global__ void __launch_bounds__(kDet64Warps * 32) k_logdet_fl_det64(int n, int K, int Tp, int T,
+                                                                       const float* __restrict__ A,
+                                                                       const uint8_t* __restrict__ redo,
+                                                                       char* __restrict__ records) {
   extern __shared__ double shd[];
   const int w = blockIdx.x / K, k = blockIdx.x % K;
   if (!redo[w]) return;
@@ -2042,21 +2089,68 @@ __global__ void __launch_bounds__(32) k_logdet_fl_det64(int n, int K, int Tp, in
   const DetRecord rec(K, D);
   char* rw = records + (size_t)w * rec.bytes;
   if (!reinterpret_cast<const uint8_t*>(rw + rec.mark)[k]) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const DetScratch sc(n);
+  const Det64Shape sh(n);
+  char* base = reinterpret_cast<char*>(shd);
+  double* LU = reinterpret_cast<double*>(base);
+  int* perm = reinterpret_cast<int*>(base + (size_t)2 * n * sc.ld * 8);
+  int* flag = reinterpret_cast<int*>(base + sh.head - 64);  // singular
+  double* red = reinterpret_cast<double*>(base + sh.head + kDet64Warps * sh.per_warp);  // [warps][2]
+  float* Mh = reinterpret_cast<float*>(base + sh.head + warp * sh.per_warp);
+  float* Ml = Mh + n * sc.ldm;
   const float* Ak = A + amat_index(Tp, n, K, w, k, 0, 0, 0);
+  const int rs = amat_row_stride(Tp, n, K);
+  const size_t ts = amat_tangent_stride(n, K);
   float* t1k = reinterpret_cast<float*>(rw + rec.t1) + (size_t)k * D;
-  const DetOut o = det_stage_df<NMAX>(Ak, n, T, amat_row_stride(Tp, n, K), amat_tangent_stride(n, K),
-                                      reinterpret_cast<char*>(shd), t1k);
-  if ((threadIdx.x & 31) == 0) {
-    reinterpret_cast<double*>(rw)[k] = o.ld;
-    reinterpret_cast<double*>(rw + rec.kin)[k] = o.singular ? 0.0 : o.kin;
-    reinterpret_cast<float*>(rw + rec.sg)[k] = o.singular ? 0.f : o.sgn;
-    reinterpret_cast<float*>(rw + rec.tL)[k] = o.singular ? 0.f : o.tL;
-    reinterpret_cast<float*>(rw + rec.t2)[k] = o.singular ? 0.f : o.t2;
-    reinterpret_cast<float*>(rw + rec.q)[k] = o.singular ? 0.f : o.q;
-    if (o.singular) {
-      for (int d = 0; d < D; ++d) t1k[d] = 0.f;
+  DetOut o{};
+  double tl = 0.0;
+  if (warp == 0) {
+    float *Ah = nullptr, *Al = nullptr;
+    o = df_factor(Ak, n, T, rs, ts, LU, perm, &Ah, &Al, &tl);
+    if (lane == 0) *flag = o.singular;
+  }
+  __syncthreads();
+  if (*flag) {
+    if (threadIdx.x == 0) {
+      reinterpret_cast<double*>(rw)[k] = o.ld;
+      reinterpret_cast<double*>(rw + rec.kin)[k] = 0.0;
+      reinterpret_cast<float*>(rw + rec.sg)[k] = 0.f;
+      reinterpret_cast<float*>(rw + rec.tL)[k] = 0.f;
+      reinterpret_cast<float*>(rw + rec.t2)[k] = 0.f;
+      reinterpret_cast<float*>(rw + rec.q)[k] = 0.f;
       atomicOr(reinterpret_cast<int*>(rw + rec.sing), 1);
     }
+    for (int d = threadIdx.x; d < D; d += blockDim.x) t1k[d] = 0.f;
+    return;
+  }
+  const float* Ah = reinterpret_cast<const float*>(LU);
+  const float* Al = Ah + n * sc.ld;
+  double t2acc = 0.0, qacc = 0.0;
+  for (int d = warp; d < D; d += kDet64Warps) {
+    double tr, t2;
+    df_direction<NMAX>(Ah, Al, Ak + (size_t)(2 + d) * ts, Mh, Ml, n, sc.ld, sc.ldm, rs, &tr, &t2);
+    if (lane == 0) t1k[d] = (float)tr;
+    t2acc += t2;
+    qacc = fma(tr, tr, qacc);
+  }
+  if (lane == 0) {
+    red[2 * warp] = t2acc;
+    red[2 * warp + 1] = qacc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t2s = 0.0, qs = 0.0;
+    for (int v = 0; v < kDet64Warps; ++v) {
+      t2s += red[2 * v];
+      qs += red[2 * v + 1];
+    }
+    reinterpret_cast<double*>(rw)[k] = o.ld;
+    reinterpret_cast<double*>(rw + rec.kin)[k] = tl - t2s + qs;
+    reinterpret_cast<float*>(rw + rec.sg)[k] = o.sgn;
+    reinterpret_cast<float*>(rw + rec.tL)[k] = (float)tl;
+    reinterpret_cast<float*>(rw + rec.t2)[k] = (float)t2s;
+    reinterpret_cast<float*>(rw + rec.q)[k] = (float)qs;
   }
 }
 
@@ -2396,9 +2490,8 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
   if (T > 1 && n > 16 && n <= 64 && fl_scratch && !env) {
     const int nw = 8;
     const WideShape sh(n, K, T - 2, nw);
-    const DetScratch sc(n);
     const size_t fin = (size_t)2 * K * 8 + (size_t)4 * K * 4 + (size_t)K * (T - 2) * 4 + 16;
-    if (sh.bytes <= 110 * 1024 && sc.bytes <= 110 * 1024 && fin <= 110 * 1024) {
+    if (sh.bytes <= 110 * 1024 && Det64Shape(n).bytes <= 220 * 1024 && fin <= 110 * 1024) {
       uint8_t* redo = static_cast<uint8_t*>(fl_scratch);
       char* records = static_cast<char*>(fl_scratch) + align_up((size_t)B, 16);
       int dev;
@@ -2411,7 +2504,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
       e = cudaFuncSetAttribute(k_logdet_fl_wide<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024); \
       if (e == cudaSuccess)                                                                                 \
         e = cudaFuncSetAttribute(k_logdet_fl_det64<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
-                                 110 * 1024);                                                               \
+                                 220 * 1024);                                                               \
       if (e == cudaSuccess)                                                                                 \
         e = cudaFuncSetAttribute(k_logdet_fl_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024); \
       if (e != cudaSuccess) return e;                                                                       \
@@ -2419,7 +2512,7 @@ cudaError_t launch_logdet(cudaStream_t s, int B, int n, int K, int Tp, int T, co
     }                                                                                                       \
     k_logdet_fl_wide<NM><<<B, 32 * nw, sh.bytes, s>>>(n, K, Tp, T, A, pe, logpsi, sign, ke, el, flags, redo, \
                                                       records, gl_add, cancel64 ? 1 : 0);                   \
-    k_logdet_fl_det64<NM><<<B * K, 32, sc.bytes, s>>>(n, K, Tp, T, A, redo, records);                       \
+    k_logdet_fl_det64<NM><<<B * K, kDet64Warps * 32, Det64Shape(n).bytes, s>>>(n, K, Tp, T, A, redo, records); \
   }
       if (n <= 32) QMC_LDW(32)
       else QMC_LDW(64)
