@@ -120,6 +120,18 @@ def rotation_matrices(u_phi, u_cos):
     return m.reshape(*np.shape(phi), 3, 3)
 
 
+def select_nearest_cores(values, vectors, distances, max_core: int):
+    """The ``max_core`` nearest ECP atoms of every electron, nearest first
+    (estimator.py:278-320): ``(values (..., max_core, C), vectors, distances)``;
+    unchanged when there are no more than ``max_core`` atoms."""
+    values, vectors, distances = np.asarray(values), np.asarray(vectors), np.asarray(distances)
+    if distances.shape[-1] <= max_core:
+        return values, vectors, distances
+    order = np.argsort(distances, axis=-1, kind="stable")[..., :max_core]
+    take = lambda a: np.take_along_axis(a, order[..., None], axis=-2)  # noqa: E731
+    return take(values), take(vectors), np.take_along_axis(distances, order, axis=-1)
+
+
 def ecp_energy(phase_logpsi, electrons, atoms, ecp_atoms, al, co, pw, rotations, quad, max_core: int = 2):
     """Per-walker ``(local, nonlocal)`` ECP energies.
 
