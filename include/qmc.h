@@ -294,13 +294,23 @@ qmc_status qmc_model_set_grad_budget(qmc_model* m, size_t bytes);
  * kfac_jax collects from the jaxpr of vmap(log|psi|)
  * (src/jaqmc/optimizer/kfac/kfac.py:162-186,
  *  src/jaqmc/optimizer/kfac/curvature_blocks.py:94-137,
- *  src/jaqmc/optimizer/kfac/tag_registration.py:22-259).  FermiNet models only.
- * Tap order: per layer l the one-electron Dense (input [h1 | spin means of h1
+ *  src/jaqmc/optimizer/kfac/tag_registration.py:22-259).
+ * FermiNet tap order: per layer l the one-electron Dense (input [h1 | spin means of h1
  * | spin means of h2], n applications per walker, bias) then, when layer l
  * updates the two-electron stream, the two-electron Dense (n^2 applications,
  * bias); the orbital projection of each spin channel (n_s applications, no
  * bias); last the envelope parameters as one diagonal tap (rows_per_walker 1,
- * in_cols 0, out_cols = their count).  A tap's inputs are a row-major
+ * in_cols 0, out_cols = their count).
+ * Psiformer tap order: the input Dense (n applications, bias); per layer the
+ * first LayerNorm (diagonal: scale then shift, 2 D), the q, k, v and output
+ * projections (n applications each, bias), the second LayerNorm (diagonal)
+ * and the MLP Dense layers (n applications, bias); the orbital projection
+ * of each spin channel; the envelope and Jastrow parameters as one diagonal
+ * tap.  LapNet: the input Dense (bias when use_input_bias); per layer the
+ * fused query/key projection [D][2D], the value, attention-output and
+ * update projections and each local update (n applications, bias when
+ * use_backbone_bias); then orbitals and the diagonal tail as above.
+ * A tap's inputs are a row-major
  * [batch * rows_per_walker][in_cols] block at float offset in_offset of the
  * taps buffer and its cotangents (or per-walker gradients) a
  * [batch * rows_per_walker][out_cols] block at out_offset; walker w's rows are

@@ -367,7 +367,7 @@ class NativeFermiNet:
         B = e.shape[0]
         n = int(self.lib.qmc_layer_taps(self.h, B, None, 0, None))
         if n < 0:
-            raise QmcError(7, "layer taps are built for FermiNet models only")
+            raise QmcError(7, "qmc_layer_taps rejected this model")
         descs = (LayerTapC * n)()
         total = C.c_size_t()
         self.lib.qmc_layer_taps(self.h, B, descs, n, C.byref(total))

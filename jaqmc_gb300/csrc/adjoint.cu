@@ -361,9 +361,10 @@ __global__ void k_tap_gather(int B, int n, int i0, int ns, const float* __restri
   dst[e] = src[(w * n + i0 + ii) * (size_t)ld + c];
 }
 
+constexpr int kMaxTaps = 128;
 struct TapPlan {
   int count = 0;
-  qmc_layer_tap t[2 * QMC_MAX_LAYERS + 3];
+  qmc_layer_tap t[kMaxTaps];
   size_t total = 0;
 };
 
@@ -1043,6 +1044,87 @@ static int psi_grad_chunk(const qmc_model* m, int B) {
 
 size_t psi_grad_workspace(const qmc_model* m, int B) { return attn_grad_total(m, psi_grad_chunk(m, B)); }
 
+// Layer taps of the attention backbones (KFAC statistics): the dense layers'
+// inputs and output cotangents per application (n rows per walker; the
+// orbital projection per spin channel), the LayerNorm scales / shifts and the
+// trailing envelope / Jastrow parameters as diagonal taps (per-walker rows of
+// the Jacobian).  The indices say where each layer's tap sits in the plan.
+struct AttnTaps {
+  TapPlan plan;
+  int in = -1, orb[2] = {-1, -1}, tail = -1;
+  int ln0[kPsiMaxLayers], ln1[kPsiMaxLayers], q[kPsiMaxLayers], k[kPsiMaxLayers], v[kPsiMaxLayers];
+  int o[kPsiMaxLayers], mlp[kPsiMaxLayers][kPsiMaxMlp + 1];
+  int qk[kPsiMaxLayers], lv[kPsiMaxLayers], lo[kPsiMaxLayers], vu[kPsiMaxLayers], ul[kPsiMaxLayers][kLapMaxLocal];
+};
+
+static int lap_local(const PsiDims& d, int l);
+
+static AttnTaps make_attn_taps(const qmc_model* m, int B) {
+  const PsiDims& d = m->psi->d;
+  const PsiParams& P = m->psi->p;
+  const Dims& fd = m->d;
+  AttnTaps a{};
+  TapPlan& tp = a.plan;
+  size_t o = 0;
+  auto add = [&](int kind, int rpw, int in_cols, int out_cols, int bias, size_t k_off, size_t b_off) {
+    qmc_layer_tap& t = tp.t[tp.count];
+    t.kind = kind;
+    t.rows_per_walker = rpw;
+    t.in_cols = in_cols;
+    t.out_cols = out_cols;
+    t.has_bias = bias;
+    t.kernel_offset = k_off;
+    t.bias_offset = b_off;
+    t.in_offset = o;
+    o += (size_t)B * rpw * in_cols;
+    t.out_offset = o;
+    o += (size_t)B * rpw * out_cols;
+    return tp.count++;
+  };
+  const int n = d.n, D = d.D;
+  const bool lap = d.arch == kArchLapNet;
+  const int in_bias = lap ? d.in_bias : 1;
+  a.in = add(QMC_TAP_DENSE, n, d.K0, D, in_bias, P.in_k, in_bias ? P.in_b : 0);
+  for (int l = 0; l < d.L; ++l) {
+    if (lap) {
+      const int bb = d.bb_bias;
+      a.qk[l] = add(QMC_TAP_DENSE, n, D, 2 * D, bb, P.qk_k[l], bb ? P.qk_b[l] : 0);
+      a.lv[l] = add(QMC_TAP_DENSE, n, D, D, bb, P.lv_k[l], bb ? P.lv_b[l] : 0);
+      a.lo[l] = add(QMC_TAP_DENSE, n, D, D, bb, P.lo_k[l], bb ? P.lo_b[l] : 0);
+      a.vu[l] = add(QMC_TAP_DENSE, n, D, D, bb, P.vu_k[l], bb ? P.vu_b[l] : 0);
+      for (int j = 0; j < lap_local(d, l); ++j)
+        a.ul[l][j] = add(QMC_TAP_DENSE, n, D, D, bb, P.ul_k[l][j], bb ? P.ul_b[l][j] : 0);
+      continue;
+    }
+    a.ln0[l] = add(QMC_TAP_DIAGONAL, 1, 0, 2 * D, 0, P.ln0_s[l], 0);  // scale then shift
+    a.q[l] = add(QMC_TAP_DENSE, n, D, D, 1, P.q_k[l], P.q_b[l]);
+    a.k[l] = add(QMC_TAP_DENSE, n, D, D, 1, P.k_k[l], P.k_b[l]);
+    a.v[l] = add(QMC_TAP_DENSE, n, D, D, 1, P.v_k[l], P.v_b[l]);
+    a.o[l] = add(QMC_TAP_DENSE, n, D, D, 1, P.o_k[l], P.o_b[l]);
+    a.ln1[l] = add(QMC_TAP_DIAGONAL, 1, 0, 2 * D, 0, P.ln1_s[l], 0);
+    int din = D;
+    for (int k = 0; k < d.n_dense; ++k) {
+      a.mlp[l][k] = add(QMC_TAP_DENSE, n, din, d.mlp[k], 1, P.mlp_k[l][k], P.mlp_b[l][k]);
+      din = d.mlp[k];
+    }
+  }
+  const int nch = fd.split ? 2 : 1;
+  for (int c = 0; c < nch; ++c) {
+    const int ns = fd.split ? (c == 0 ? fd.n_up : fd.n_dn) : n;
+    a.orb[c] = add(QMC_TAP_DENSE, ns, D, fd.norb, 0, P.orb_k[c], 0);
+  }
+  const size_t env0 = P.env_pi[0];
+  if (P.total > env0) a.tail = add(QMC_TAP_DIAGONAL, 1, 0, (int)(P.total - env0), 0, env0, 0);
+  tp.total = o;
+  return a;
+}
+
+// dst [rows][cols] (contiguous) = src [rows][cols] with row stride ld
+static cudaError_t tap_copy(cudaStream_t s, float* dst, int cols, const float* src, int ld, size_t rows) {
+  return cudaMemcpy2DAsync(dst, sizeof(float) * cols, src, sizeof(float) * ld, sizeof(float) * cols, rows,
+                           cudaMemcpyDeviceToDevice, s);
+}
+
 // Orbitals x envelope of an attention backbone's output hL [B n][D] into
 // amat (the raw orbitals kept in orb for the envelope cotangent).
 static qmc_status attn_orbitals_fwd(qmc_model* m, int B, void* ws, const float* hL, size_t amat, size_t orb,
@@ -1077,7 +1159,8 @@ static qmc_status attn_orbitals_fwd(qmc_model* m, int B, void* ws, const float* 
 // the cotangent hbar [B n][D] of the backbone output hL.
 static qmc_status attn_orbitals_bwd(qmc_model* m, int B, void* ws, const float* hL, size_t amat, size_t orb,
                                     size_t abar, size_t envbar, size_t rae, size_t aevec, size_t orbbar, size_t jas,
-                                    float* hbar, float* J, float* lp, cudaStream_t s) {
+                                    float* hbar, float* J, float* lp, cudaStream_t s, const TapOut* taps = nullptr,
+                                    const int* orb_tap = nullptr) {
   const PsiParams& P = m->psi->p;
   const Dims& fd = m->d;
   const ArenaLayout& fa = m->a;
@@ -1113,6 +1196,12 @@ static qmc_status attn_orbitals_bwd(qmc_model* m, int B, void* ws, const float* 
                                                                    P.env_pi[c], P.env_sigma[c]);
     QMC_CUDA(cudaGetLastError());
     QMC_CUDA(jac_outer(s, B, ns, n, i0, hL, D, D, at<float>(ws, orbbar), fd.norb_p, fd.norb, J, Pn, P.orb_k[c]));
+    if (taps) {
+      k_tap_gather<<<blocks((size_t)B * ns * D), 256, 0, s>>>(B, n, i0, ns, hL, D, D, taps->in(orb_tap[c]));
+      k_tap_gather<<<blocks((size_t)B * ns * fd.norb), 256, 0, s>>>(B, n, i0, ns, at<float>(ws, orbbar), fd.norb_p,
+                                                                    fd.norb, taps->out(orb_tap[c]));
+      QMC_CUDA(cudaGetLastError());
+    }
     RowMap map{ns, i0, n, 1};
     QMC_CUDA(launch_gemm_simt(s, B * ns, map, at<float>(ws, orbbar), fd.norb_p, fd.norb_p, nullptr, 0, 0,
                               ar + fa.wt_orb[c], D, D, EpiStore{hbar, D, nullptr}));
@@ -1186,7 +1275,8 @@ static qmc_status psi_forward_save(qmc_model* m, const PsiGradPlan& p, void* ws,
 }
 
 static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, const float* electrons, float* J,
-                               float* logpsi, cudaStream_t s) {
+                               float* logpsi, cudaStream_t s, const TapOut* taps = nullptr,
+                               const AttnTaps* ti = nullptr) {
   const PsiDims& d = m->psi->d;
   const PsiParams& P = m->psi->p;
   const PsiArena& a = m->psi->a;
@@ -1199,7 +1289,7 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
   const unsigned wb = (unsigned)((rows + 7) / 8);
   float* hbar = at<float>(ws, p.hbar);
   QMC_TRY(attn_orbitals_bwd(m, B, ws, at<float>(ws, p.h[d.L]), p.amat, p.orb, p.abar, p.envbar, p.rae, p.aevec,
-                            p.orbbar, p.jas, hbar, J, logpsi, s));
+                            p.orbbar, p.jas, hbar, J, logpsi, s, taps, ti ? ti->orb : nullptr));
   float* hmbar = at<float>(ws, p.hmbar);
   float* zbar = at<float>(ws, p.zbar);
   float* tmp = at<float>(ws, p.tmp);
@@ -1217,6 +1307,10 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
       QMC_CUDA(cudaGetLastError());
       QMC_CUDA(jac_outer(s, B, n, n, 0, x, din, din, zbar, dout, dout, J, Pn,
                                                                 P.mlp_k[l][k]));
+      if (taps) {
+        QMC_CUDA(tap_copy(s, taps->in(ti->mlp[l][k]), din, x, din, rows));
+        QMC_CUDA(tap_copy(s, taps->out(ti->mlp[l][k]), dout, zbar, dout, rows));
+      }
       k_colsum<<<blocks((size_t)B * dout), 256, 0, s>>>(B, n, zbar, dout, dout, nullptr, J, Pn, P.mlp_b[l][k]);
       QMC_CUDA(cudaGetLastError());
       // input cotangent zbar W^T into tmp (the next k's ybar, or the LayerNorm output's)
@@ -1239,6 +1333,10 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
       ::qmc::ProfScope ps_(QMC_KC_STREAM_LAYER, s);
       QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.o[l]), D, D, hmbar, D, D, J,
                                                             Pn, P.o_k[l]));
+      if (taps) {
+        QMC_CUDA(tap_copy(s, taps->in(ti->o[l]), D, at<float>(ws, p.o[l]), D, rows));
+        QMC_CUDA(tap_copy(s, taps->out(ti->o[l]), D, hmbar, D, rows));
+      }
       k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hmbar, D, D, nullptr, J, Pn, P.o_b[l]);
       QMC_CUDA(cudaGetLastError());
       QMC_CUDA(launch_gemm_simt(s, B * n, rmap, hmbar, D, D, nullptr, 0, 0, ar + a.t32_o[l], D, D,
@@ -1258,6 +1356,11 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
       for (int c = 0; c < 3; ++c) {
         QMC_CUDA(jac_outer(s, B, n, n, 0, xn0, D, D, qkvbar + (size_t)c * D, 3 * D, D,
                                                               J, Pn, kofs[c]));
+        if (taps) {
+          const int tk = c == 0 ? ti->q[l] : (c == 1 ? ti->k[l] : ti->v[l]);
+          QMC_CUDA(tap_copy(s, taps->in(tk), D, xn0, D, rows));
+          QMC_CUDA(tap_copy(s, taps->out(tk), D, qkvbar + (size_t)c * D, 3 * D, rows));
+        }
         k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, qkvbar + (size_t)c * D, 3 * D, D, nullptr, J, Pn,
                                                        bofs[c]);
         QMC_CUDA(cudaGetLastError());
@@ -1283,6 +1386,10 @@ static qmc_status psi_backward(qmc_model* m, const PsiGradPlan& p, void* ws, con
                                                              J, Pn, P.in_k));
     k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hbar, D, D, nullptr, J, Pn, P.in_b);
     QMC_CUDA(cudaGetLastError());
+    if (taps) {
+      QMC_CUDA(tap_copy(s, taps->in(ti->in), d.K0, at<float>(ws, p.x0), d.K0p, rows));
+      QMC_CUDA(tap_copy(s, taps->out(ti->in), D, hbar, D, rows));
+    }
     if (d.jastrow) {
       k_psi_jas_jac<<<blocks(B), 256, 0, s>>>(B, n, d.n_up, electrons, ar + P.alpha_par, J, Pn, P.alpha_par,
                                               P.alpha_anti);
@@ -1414,7 +1521,8 @@ static qmc_status lap_forward_save(qmc_model* m, const LapGradPlan& p, void* ws,
 }
 
 static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, const float* electrons, float* J,
-                               float* logpsi, cudaStream_t s) {
+                               float* logpsi, cudaStream_t s, const TapOut* taps = nullptr,
+                               const AttnTaps* ti = nullptr) {
   const PsiDims& d = m->psi->d;
   const PsiParams& P = m->psi->p;
   const PsiArena& a = m->psi->a;
@@ -1428,8 +1536,14 @@ static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, con
   float* obar = at<float>(ws, p.obar);
   float* qkvbar = at<float>(ws, p.qkvbar);
   QMC_TRY(attn_orbitals_bwd(m, B, ws, at<float>(ws, p.hd[d.L]), p.amat, p.orb, p.abar, p.envbar, p.rae, p.aevec,
-                            p.orbbar, p.jas, hbar, J, logpsi, s));
+                            p.orbbar, p.jas, hbar, J, logpsi, s, taps, ti ? ti->orb : nullptr));
   QMC_CUDA(cudaMemsetAsync(hsbar, 0, sizeof(float) * rows * D, s));
+  auto tap = [&](int k, const float* x, int in_cols, int ldx, const float* dy, int out_cols, int ldy) -> qmc_status {
+    if (!taps) return QMC_OK;
+    QMC_CUDA(tap_copy(s, taps->in(k), in_cols, x, ldx, rows));
+    QMC_CUDA(tap_copy(s, taps->out(k), out_cols, dy, ldy, rows));
+    return QMC_OK;
+  };
   auto bias_rows = [&](const float* z, int ldz, int N, size_t off) -> qmc_status {
     if (!d.bb_bias) return QMC_OK;
     k_colsum<<<blocks((size_t)B * N), 256, 0, s>>>(B, n, z, ldz, N, nullptr, J, Pn, off);
@@ -1444,11 +1558,13 @@ static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, con
     QMC_CUDA(cudaGetLastError());
     QMC_CUDA(jac_outer(s, B, n, n, 0, r, D, D, zbar, D, D, J, Pn, P.vu_k[l]));
     QMC_TRY(bias_rows(zbar, D, D, P.vu_b[l]));
+    if (taps) QMC_TRY(tap(ti->vu[l], r, D, D, zbar, D, D));
     QMC_CUDA(launch_gemm_simt(s, B * n, rmap, zbar, D, D, nullptr, 0, 0, ar + a.t32_vu[l], D, D,
                               EpiStore{hbar, D, nullptr, 1}));  // hbar now holds rbar
     // r = hd[l] + o Wo + bo
     QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.o[l]), D, D, hbar, D, D, J, Pn, P.lo_k[l]));
     QMC_TRY(bias_rows(hbar, D, D, P.lo_b[l]));
+    if (taps) QMC_TRY(tap(ti->lo[l], at<float>(ws, p.o[l]), D, D, hbar, D, D));
     QMC_CUDA(launch_gemm_simt(s, B * n, rmap, hbar, D, D, nullptr, 0, 0, ar + a.t32_o[l], D, D,
                               EpiStore{obar, D, nullptr}));
     {
@@ -1462,6 +1578,7 @@ static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, con
     const float* hd = at<float>(ws, p.hd[l]);
     QMC_CUDA(jac_outer(s, B, n, n, 0, hd, D, D, qkvbar + 2 * D, 3 * D, D, J, Pn, P.lv_k[l]));
     QMC_TRY(bias_rows(qkvbar + 2 * D, 3 * D, D, P.lv_b[l]));
+    if (taps) QMC_TRY(tap(ti->lv[l], hd, D, D, qkvbar + 2 * D, D, 3 * D));
     QMC_CUDA(launch_gemm_simt(s, B * n, rmap, qkvbar + 2 * D, 3 * D, D, nullptr, 0, 0, ar + a.t32_v[l], D, D,
                               EpiStore{hbar, D, nullptr, 1}));
     // local updates, last first: hs_{j+1} = hs_j + u_j, u_j = tanh(hs_j Wu_j + bu_j)
@@ -1470,12 +1587,14 @@ static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, con
       QMC_CUDA(cudaGetLastError());
       QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.hs[l][j]), D, D, zbar, D, D, J, Pn, P.ul_k[l][j]));
       QMC_TRY(bias_rows(zbar, D, D, P.ul_b[l][j]));
+      if (taps) QMC_TRY(tap(ti->ul[l][j], at<float>(ws, p.hs[l][j]), D, D, zbar, D, D));
       QMC_CUDA(launch_gemm_simt(s, B * n, rmap, zbar, D, D, nullptr, 0, 0, ar + a.t32_ul[l][j], D, D,
                                 EpiStore{hsbar, D, nullptr, 1}));
     }
     // q|k = hs[l][0] Wqk + bqk
     QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.hs[l][0]), D, D, qkvbar, 3 * D, 2 * D, J, Pn, P.qk_k[l]));
     QMC_TRY(bias_rows(qkvbar, 3 * D, 2 * D, P.qk_b[l]));
+    if (taps) QMC_TRY(tap(ti->qk[l], at<float>(ws, p.hs[l][0]), D, D, qkvbar, 2 * D, 3 * D));
     QMC_CUDA(launch_gemm_simt(s, B * n, rmap, qkvbar, 3 * D, 2 * D, nullptr, 0, 0, ar + a.t32_qkv[l], D, D,
                               EpiStore{hsbar, D, nullptr, 1}));
   }
@@ -1485,6 +1604,7 @@ static qmc_status lap_backward(qmc_model* m, const LapGradPlan& p, void* ws, con
     k_add_to<<<blocks(rows * D), 256, 0, s>>>(rows * D, hsbar, hbar);
     QMC_CUDA(cudaGetLastError());
     QMC_CUDA(jac_outer(s, B, n, n, 0, at<float>(ws, p.x0), d.K0p, d.K0, hbar, D, D, J, Pn, P.in_k));
+    if (taps) QMC_TRY(tap(ti->in, at<float>(ws, p.x0), d.K0, d.K0p, hbar, D, D));
     if (d.in_bias) {
       k_colsum<<<blocks((size_t)B * D), 256, 0, s>>>(B, n, hbar, D, D, nullptr, J, Pn, P.in_b);
       QMC_CUDA(cudaGetLastError());
@@ -1551,6 +1671,77 @@ qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const d
     }
   }
   return QMC_OK;
+}
+
+// Layer taps of a Psiformer / LapNet model: the adjoint chunk by chunk with
+// each dense layer's inputs and output cotangents copied out as they are
+// formed, then the diagonal taps from the chunk's Jacobian rows.
+qmc_status run_attn_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,
+                              float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
+  const PsiDims& pd = m->psi->d;
+  if (pd.n > 64 || pd.Dh > 64) {
+    set_error("the attention-backbone adjoint supports at most 64 electrons and head width 64");
+    return QMC_ERR_SHAPE;
+  }
+  {
+    int dev;
+    QMC_CUDA(cudaGetDevice(&dev));
+    static int set_dev = -1;
+    if (set_dev != dev) {
+      QMC_CUDA(cudaFuncSetAttribute(k_psi_attn_save, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      QMC_CUDA(cudaFuncSetAttribute(k_psi_attn_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      set_dev = dev;
+    }
+  }
+  const int chunk = psi_grad_chunk(m, batch);
+  const size_t need = attn_grad_total(m, chunk);
+  if (ws_bytes < need) {
+    set_error("workspace too small for the adjoint: %zu bytes given, %zu needed", ws_bytes, need);
+    return QMC_ERR_WORKSPACE;
+  }
+  const AttnTaps ti = make_attn_taps(m, batch);
+  const TapPlan& tp = ti.plan;
+  if (taps_floats < tp.total) {
+    set_error("taps buffer too small: %zu floats given, %zu needed", taps_floats, tp.total);
+    return QMC_ERR_WORKSPACE;
+  }
+  const size_t P = m->psi->p.total;
+  const int n = pd.n;
+  const bool lapnet = pd.arch == kArchLapNet;
+  for (int w0 = 0; w0 < batch; w0 += chunk) {
+    const int B = std::min(chunk, batch - w0);
+    const PsiGradPlan q = lapnet ? PsiGradPlan{} : make_psi_grad_plan(m, B);
+    const LapGradPlan ql = lapnet ? make_lap_grad_plan(m, B) : LapGradPlan{};
+    float* J = at<float>(ws, lapnet ? ql.J : q.J);
+    QMC_CUDA(cudaMemsetAsync(J, 0, sizeof(float) * B * P, s));
+    TapOut to;
+    to.base = taps;
+    to.plan = &tp;
+    to.w0 = w0;
+    const float* x = electrons + (size_t)w0 * n * 3;
+    float* lp = logpsi ? logpsi + w0 : nullptr;
+    if (lapnet) {
+      QMC_TRY(lap_forward_save(m, ql, ws, x, s));
+      QMC_TRY(lap_backward(m, ql, ws, x, J, lp, s, &to, &ti));
+    } else {
+      QMC_TRY(psi_forward_save(m, q, ws, x, s));
+      QMC_TRY(psi_backward(m, q, ws, x, J, lp, s, &to, &ti));
+    }
+    for (int k = 0; k < tp.count; ++k) {
+      const qmc_layer_tap& t = tp.t[k];
+      if (t.kind != QMC_TAP_DIAGONAL) continue;
+      QMC_CUDA(cudaMemcpy2DAsync(to.out(k), sizeof(float) * t.out_cols, J + t.kernel_offset, sizeof(float) * P,
+                                 sizeof(float) * t.out_cols, B, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  return QMC_OK;
+}
+
+int attn_layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total) {
+  const AttnTaps ti = make_attn_taps(m, batch);
+  for (int k = 0; k < ti.plan.count && k < max_taps; ++k) taps[k] = ti.plan.t[k];
+  if (total) *total = ti.plan.total;
+  return ti.plan.count;
 }
 
 }  // namespace qmc

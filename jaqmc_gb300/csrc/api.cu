@@ -920,17 +920,14 @@ qmc_status qmc_grad(qmc_model* m, int batch, const float* electrons, const doubl
 }
 
 int qmc_layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total_floats) {
-  if (!m || m->kind != QMC_KIND_FERMINET || batch < 1 || (max_taps > 0 && !taps)) return -1;
+  if (!m || batch < 1 || (max_taps > 0 && !taps)) return -1;
+  if (m->kind == QMC_KIND_PSIFORMER) return attn_layer_taps(m, batch, taps, max_taps, total_floats);
   return layer_taps(m, batch, taps, max_taps, total_floats);
 }
 
 qmc_status qmc_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,
                          float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s) {
   if (!m) { set_error("null model"); return QMC_ERR_ARG; }
-  if (m->kind != QMC_KIND_FERMINET) {
-    set_error("layer taps are built for FermiNet models only");
-    return QMC_ERR_UNSUPPORTED;
-  }
   if (!m->params_set) { set_error("parameters not set (qmc_model_set_params)"); return QMC_ERR_ARG; }
   if (batch < 1 || !electrons || !taps) { set_error("bad batch/electrons/taps"); return QMC_ERR_ARG; }
   if (!ws) { set_error("null workspace"); return QMC_ERR_WORKSPACE; }
@@ -940,6 +937,8 @@ qmc_status qmc_grad_taps(qmc_model* m, int batch, const float* electrons, float*
     set_error("model lives on device %d but device %d is current", m->device, dev);
     return QMC_ERR_ARG;
   }
+  if (m->kind == QMC_KIND_PSIFORMER)
+    return run_attn_grad_taps(m, batch, electrons, taps, taps_floats, logpsi, ws, ws_bytes, s);
   return run_grad_taps(m, batch, electrons, taps, taps_floats, logpsi, ws, ws_bytes, s);
 }
 

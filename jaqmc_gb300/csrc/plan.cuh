@@ -47,6 +47,9 @@ size_t psi_grad_workspace(const qmc_model* m, int batch);
 qmc_status run_psi_grad(qmc_model* m, int batch, const float* electrons, const double* weights, float* per_walker,
                         double* grad, float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s);
 // Layer taps of the adjoint (KFAC statistics): descriptors and the chunked run.
+int attn_layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total);
+qmc_status run_attn_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,
+                              float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s);
 int layer_taps(const qmc_model* m, int batch, qmc_layer_tap* taps, int max_taps, size_t* total);
 qmc_status run_grad_taps(qmc_model* m, int batch, const float* electrons, float* taps, size_t taps_floats,
                          float* logpsi, void* ws, size_t ws_bytes, cudaStream_t s);
