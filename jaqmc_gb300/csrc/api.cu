@@ -277,6 +277,13 @@ static bool pair_stream(const Dims& d, const Plan& p) {
   return (size_t)(d.L - 1) * p.g2_plane * 4 <= p.g1 - p.h2[1];
 }
 
+// Value-only mixed passes on the fused two-electron path take every input of
+// the first layer (split features, pair-mean rows, broadcast term) from one
+// launch_inputs_value call.
+static bool inputs_fused(const Dims& d, const Plan& p) {
+  return p.mixed && p.T == 1 && pair_fused(d, p.T) && inputs_value_smem(d.n, d.A, d.g1_p[0]) <= 48 * 1024;
+}
+
 // The means after pair layer l - 1 (input of one-electron layer l >= 1) on
 // the fused two-electron path: f32 [B*n][g2_p[l]], or two bf16 planes.
 static size_t stream_g2(const Plan& p, int l) { return p.h2[1] + (size_t)(l - 1) * p.g2_plane * 4; }
@@ -386,16 +393,19 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
       const size_t rows = (size_t)B * n * Tp;
       bf* X0s = at<bf>(ws, p.x0s);
       bf* G2s = at<bf>(ws, p.g2s0);
-      QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StF32{X0, dinp}, d.g1_p[l],
-                                            StF32{G1, d.g1_p[l]}));
-      QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
-                                                  ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
-      if (!fused)
-        QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
-                                              StSplit{G2s, d.g2_p[l], rows * d.g2_p[l]}));
-      else
-        QMC_PROF(QMC_KC_LAYER0, launch_to_split(s, rows * d.g2_p[l], at<float>(ws, p.g2), G2s, rows * d.g2_p[l]));
-      QMC_PROF(QMC_KC_LAYER0, launch_to_split(s, rows * dinp, X0, X0s, rows * dinp));
+      if (!inputs_fused(d, p)) {  // else evaluate() wrote X0s, G2s and Gb
+        QMC_PROF(QMC_KC_MEANS, launch_mean_h1(s, B, n, d.n_up, d.C, Tp, din, StF32{X0, dinp}, d.g1_p[l],
+                                              StF32{G1, d.g1_p[l]}));
+        QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
+                                                    ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
+        if (!fused)
+          QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
+                                                StSplit{G2s, d.g2_p[l], rows * d.g2_p[l]}));
+        else
+          QMC_PROF(QMC_KC_LAYER0,
+                   launch_to_split(s, rows * d.g2_p[l], at<float>(ws, p.g2), G2s, rows * d.g2_p[l]));
+        QMC_PROF(QMC_KC_LAYER0, launch_to_split(s, rows * dinp, X0, X0s, rows * dinp));
+      }
       TcLayerArgs la{};
       la.n_groups = B * n;
       la.n = n;
@@ -593,10 +603,21 @@ qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electron
   const float* ar = m->arena;
   float* pe = want_pe ? at<float>(ws, p.pe) : nullptr;
   const bool fused = pair_fused(d, p.T);
-  QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
-                           ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
-                           at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec), pe,
-                           d.n_up, d.C, d.g2_p[0], fused ? at<float>(ws, p.g2) : nullptr));
+  if (inputs_fused(d, p)) {
+    typedef __nv_bfloat16 bf;
+    const size_t rows = (size_t)p.B * d.n;
+    QMC_PROF(QMC_KC_FEATURES,
+             launch_inputs_value(s, p.B, d.n, d.A, d.n_up, d.C, p.K0p, d.g1_p[0], d.g2_p[0], d.d1[0], electrons,
+                                 ar + m->a.atoms, ar + m->a.charges, m->nuclear_repulsion, ar + m->a.w_g1[0],
+                                 at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, p.h2[0]),
+                                 StSplit{at<bf>(ws, p.x0s), p.K0p, rows * p.K0p},
+                                 StSplit{at<bf>(ws, p.g2s0), d.g2_p[0], rows * d.g2_p[0]}, at<float>(ws, p.gb), pe));
+  } else {
+    QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
+                                              ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),
+                                              at<float>(ws, p.h2[0]), at<float>(ws, p.rae), at<float>(ws, p.aevec),
+                                              pe, d.n_up, d.C, d.g2_p[0], fused ? at<float>(ws, p.g2) : nullptr));
+  }
   int hb = 0;
   if (p.mixed) QMC_TRY(run_backbone_mixed(m, p, ws, s, &hb));
   else QMC_TRY(run_backbone_plain(m, p, ws, s, &hb));

@@ -150,41 +150,60 @@ __device__ __forceinline__ float fast_exp2(float x) {
 // of electron i (src/jaqmc/wavefunction/output/envelope.py:98-140).  Same
 // terms in the same order as the tangent epilogues, the exponentials by
 // fast_exp2 (the kernel serves the mixed form only).  One block per
-// kEnvWalkers walkers, thread (walker, i, j); the parameters are staged once
-// per block as [channel][I][k][j] so a warp reads consecutive j.
+// kEnvWalkers walkers, thread (walker, i, j) looping over k with its electron's
+// distances in registers (NA atoms at compile time; NA = 0: any count); the
+// parameters are staged once per block as (pi, log2(e) s) pairs
+// [channel][k][I][j], so a warp reads consecutive j.
 constexpr int kEnvWalkers = 8;
+template <int NA>
 __global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A, int env_abs,
                                  const float* __restrict__ pi0, const float* __restrict__ sg0,
                                  const float* __restrict__ pi1, const float* __restrict__ sg1,
                                  const float* __restrict__ rae, float* __restrict__ env) {
-  extern __shared__ float she[];
-  const int nch = split ? 2 : 1, per = A * K * n;
-  float* ps = she;               // [nch][A][K][n]
-  float* ss = she + nch * per;   // [nch][A][K][n]: log2(e) |sigma| (or log2(e) sigma)
+  extern __shared__ float2 she2[];
+  const int nch = split ? 2 : 1, per = K * A * n, kan = A * n;
   for (int e = threadIdx.x; e < nch * per; e += blockDim.x) {
-    const int c = e / per, rem = e % per;
-    const int I = rem / (K * n), k = (rem / n) % K, j = rem % n;
+    const int c = e / per, rem = e - c * per;
+    const int k = rem / kan, rem2 = rem - k * kan;
+    const int I = rem2 / n, j = rem2 - I * n;
     const size_t q = ((size_t)j * A + I) * K + k;
-    ps[e] = (c ? pi1 : pi0)[q];
     const float sv = (c ? sg1 : sg0)[q];
-    ss[e] = (env_abs ? fabsf(sv) : sv) * 1.4426950408889634f;
+    she2[e] = make_float2((c ? pi1 : pi0)[q], (env_abs ? fabsf(sv) : sv) * 1.4426950408889634f);
   }
   __syncthreads();
   const int nn = n * n;
+  const int na = NA > 0 ? NA : A;
   for (int e = threadIdx.x; e < kEnvWalkers * nn; e += blockDim.x) {
-    const int w = blockIdx.x * kEnvWalkers + e / nn;
+    const int wl = e / nn, ij = e - wl * nn;
+    const int w = blockIdx.x * kEnvWalkers + wl;
     if (w >= B) break;
-    const int i = (e % nn) / n, j = e % n;
+    const int i = ij / n, j = ij - i * n;
     const int c = split && i >= n_up ? 1 : 0;
     const float* ra = rae + ((size_t)w * n + i) * A;
-    float* out = env + (size_t)w * K * nn + i * n + j;
-    for (int k = 0; k < K; ++k) {
-      float acc = 0.f;
-      for (int I = 0; I < A; ++I) {
-        const int o = ((c * A + I) * K + k) * n + j;
-        acc += ps[o] * fast_exp2(-ss[o] * __ldg(ra + I));
+    float* out = env + (size_t)w * K * nn + ij;
+    const float2* q = she2 + (size_t)c * per + j;
+    if constexpr (NA > 0) {
+      float r[NA];
+#pragma unroll
+      for (int I = 0; I < NA; ++I) r[I] = __ldg(ra + I);
+      for (int k = 0; k < K; ++k, q += kan) {
+        float acc = 0.f;
+#pragma unroll
+        for (int I = 0; I < NA; ++I) {
+          const float2 v = q[I * n];
+          acc += v.x * fast_exp2(-v.y * r[I]);
+        }
+        out[(size_t)k * nn] = acc;
       }
-      out[(size_t)k * nn] = acc;
+    } else {
+      for (int k = 0; k < K; ++k, q += kan) {
+        float acc = 0.f;
+        for (int I = 0; I < na; ++I) {
+          const float2 v = q[I * n];
+          acc += v.x * fast_exp2(-v.y * __ldg(ra + I));
+        }
+        out[(size_t)k * nn] = acc;
+      }
     }
   }
 }
@@ -192,10 +211,24 @@ __global__ void k_envelope_value(int B, int n, int n_up, int split, int K, int A
 cudaError_t launch_envelope_value(cudaStream_t s, int B, int n, int n_up, int split, int K, int A, int env_abs,
                                   const float* pi0, const float* sg0, const float* pi1, const float* sg1,
                                   const float* rae, float* env) {
-  const size_t sm = sizeof(float) * 2 * (split ? 2 : 1) * (size_t)A * K * n;
+  const size_t sm = sizeof(float2) * (split ? 2 : 1) * (size_t)A * K * n;
   if (sm > 48 * 1024) return cudaErrorNotSupported;
-  k_envelope_value<<<(unsigned)((B + kEnvWalkers - 1) / kEnvWalkers), 256, sm, s>>>(B, n, n_up, split, K, A, env_abs,
-                                                                                 pi0, sg0, pi1, sg1, rae, env);
+  const unsigned grid = (unsigned)((B + kEnvWalkers - 1) / kEnvWalkers);
+#define QMC_ENV_CASE(NA_)                                                                                       \
+  case NA_:                                                                                                     \
+    k_envelope_value<NA_><<<grid, 256, sm, s>>>(B, n, n_up, split, K, A, env_abs, pi0, sg0, pi1, sg1, rae, env); \
+    break;
+  switch (A) {
+    QMC_ENV_CASE(1)
+    QMC_ENV_CASE(2)
+    QMC_ENV_CASE(3)
+    QMC_ENV_CASE(4)
+    QMC_ENV_CASE(6)
+    QMC_ENV_CASE(12)
+    default:
+      k_envelope_value<0><<<grid, 256, sm, s>>>(B, n, n_up, split, K, A, env_abs, pi0, sg0, pi1, sg1, rae, env);
+  }
+#undef QMC_ENV_CASE
   return cudaGetLastError();
 }
 
@@ -1070,6 +1103,126 @@ template cudaError_t launch_mean_h1<StF32, StF32>(cudaStream_t, int, int, int, i
                                                   StF32);
 template cudaError_t launch_mean_h1<StSplit, StSplit>(cudaStream_t, int, int, int, int, int, int, StSplit,
                                                       int, StSplit);
+
+// Value-only passes of the mixed form: everything the first layer reads, from
+// the electron positions, in one block per walker.  The electron-atom and
+// electron-electron vectors (input/atomic.py:46-79) go to shared memory once;
+// from there the block writes the one-electron rows X0 as split bf16, the
+// pair rows H2 (fp32, read by the two-electron stream), the spin means of the
+// pair rows over their first electron (split bf16, the first layer's second
+// GEMM source) and the first layer's broadcast term Gb[w] = g1[w] W_g1, where
+// g1 holds the spin means of X0 (backbone/ferminet.py:65-90).  The means sum
+// electrons in index order, as k_mean_h1_vec and k_features do.
+__device__ __forceinline__ float f4_comp(const float4& v, int c) {
+  return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+}
+
+__global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, int g2p, int dout,
+                               const float* __restrict__ elec, const float* __restrict__ atoms,
+                               const float* __restrict__ charges, double nuc, const float* __restrict__ Wg1,
+                               float* __restrict__ rae_g, float* __restrict__ aevec_g, float* __restrict__ H2,
+                               StSplit X0s, StSplit G2s, float* __restrict__ Gb, float* __restrict__ pe) {
+  extern __shared__ float4 shin[];
+  float4* ea = shin;                                  // [n][A]: |r_i - R_I|, r_i - R_I
+  float4* pr = ea + n * A;                            // [n][n]: |r_i - r_j|, r_i - r_j (zero for i == j)
+  float* g1 = reinterpret_cast<float*>(pr + n * n);   // [g1p]
+  float* xs = g1 + g1p;                               // [n][3]
+  __shared__ double red[32];
+  const int w = blockIdx.x;
+  const float* ew = elec + (size_t)w * n * 3;
+  for (int e = threadIdx.x; e < 3 * n; e += blockDim.x) xs[e] = ew[e];
+  __syncthreads();
+  double vpot = 0.0;
+  for (int e = threadIdx.x; e < n * A; e += blockDim.x) {
+    const int i = e / A, I = e - i * A;
+    const float dx = xs[3 * i] - atoms[3 * I], dy = xs[3 * i + 1] - atoms[3 * I + 1],
+                dz = xs[3 * i + 2] - atoms[3 * I + 2];
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    ea[e] = make_float4(r, dx, dy, dz);
+    const size_t gi = (size_t)w * n * A + e;
+    rae_g[gi] = r;
+    aevec_g[3 * gi] = dx;
+    aevec_g[3 * gi + 1] = dy;
+    aevec_g[3 * gi + 2] = dz;
+    if (pe) vpot -= (double)charges[I] / (double)r;
+  }
+  float4* h2w = reinterpret_cast<float4*>(H2) + (size_t)w * n * n;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i != j) {
+      const float d0 = xs[3 * i] - xs[3 * j], d1 = xs[3 * i + 1] - xs[3 * j + 1], d2 = xs[3 * i + 2] - xs[3 * j + 2];
+      const float r = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+      v = make_float4(r, d0, d1, d2);
+      if (pe && i < j) vpot += 1.0 / (double)r;
+    }
+    pr[e] = v;
+    h2w[e] = v;
+  }
+  __syncthreads();
+  const size_t row0 = (size_t)w * n;
+  const int A4 = 4 * A;
+  for (int e = threadIdx.x; e < n * K0p; e += blockDim.x) {
+    const int i = e / K0p, f = e - i * K0p;
+    X0s.put(row0 + i, f, f < A4 ? f4_comp(ea[i * A + (f >> 2)], f & 3) : 0.f);
+  }
+  for (int col = threadIdx.x; col < g1p; col += blockDim.x) {
+    float acc = 0.f;
+    if (col < C * A4) {
+      const int sc = col / A4, f = col - sc * A4;
+      int a0, a1;
+      channel_range(sc, C, n, n_up, &a0, &a1);
+      for (int a = a0; a < a1; ++a) acc += f4_comp(ea[a * A + (f >> 2)], f & 3);
+      acc *= 1.0f / (float)(a1 - a0);
+    }
+    g1[col] = acc;
+  }
+  for (int e = threadIdx.x; e < n * g2p; e += blockDim.x) {
+    const int i = e / g2p, col = e - i * g2p;
+    float v = 0.f;
+    if (col < 4 * C) {
+      const int sc = col >> 2, c4 = col & 3;
+      int a0, a1;
+      channel_range(sc, C, n, n_up, &a0, &a1);
+      float acc = 0.f;
+      for (int a = a0; a < a1; ++a)
+        if (a != i) acc += f4_comp(pr[a * n + i], c4);  // pair (a, i): r_a - r_i
+      v = acc / (float)(a1 - a0);
+    }
+    G2s.put(row0 + i, col, v);
+  }
+  __syncthreads();
+  for (int f = threadIdx.x; f < dout; f += blockDim.x) {
+    float acc = 0.f;
+    for (int k = 0; k < g1p; ++k) acc = fmaf(g1[k], __ldg(Wg1 + (size_t)k * dout + f), acc);
+    Gb[(size_t)w * dout + f] = acc;
+  }
+  if (pe) {
+    for (int o = 16; o > 0; o >>= 1) vpot += __shfl_xor_sync(0xffffffffu, vpot, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vpot;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) pe[w] = (float)(v + nuc);
+    }
+  }
+}
+
+size_t inputs_value_smem(int n, int A, int g1p) {
+  return sizeof(float4) * ((size_t)n * A + (size_t)n * n) + sizeof(float) * ((size_t)g1p + 3 * n);
+}
+
+cudaError_t launch_inputs_value(cudaStream_t s, int B, int n, int A, int n_up, int C, int K0p, int g1p, int g2p,
+                                int dout, const float* electrons, const float* atoms, const float* charges,
+                                double nuc, const float* Wg1, float* rae, float* aevec, float* H2, StSplit X0s,
+                                StSplit G2s, float* Gb, float* pe) {
+  const size_t sm = inputs_value_smem(n, A, g1p);
+  if (sm > 48 * 1024) return cudaErrorNotSupported;
+  k_inputs_value<<<B, 128, sm, s>>>(n, A, n_up, C, K0p, g1p, g2p, dout, electrons, atoms, charges, nuc, Wg1, rae,
+                                    aevec, H2, X0s, G2s, Gb, pe);
+  return cudaGetLastError();
+}
 
 // d/dr_e of h2[a, i] = (delta_{ae} - delta_{ie}) d/dDelta (pair (a,i), a != i);
 // the full Laplacian of a pair feature is twice its Laplacian in Delta.

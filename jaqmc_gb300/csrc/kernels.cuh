@@ -40,6 +40,16 @@ cudaError_t launch_features(cudaStream_t s, int B, int n, int A, int Tp, int T, 
                             double nuc, float* X0, float* H2, float* rae, float* aevec, float* pe,
                             int n_up = 0, int C = 0, int g2p = 0, float* G2 = nullptr);
 
+// Value-only inputs of the mixed form's first layer, one block per walker:
+// rae / aevec / pe and H2 as launch_features (P2 = 1); X0 as split bf16
+// [w*n+i][K0p]; the pair rows' spin means G2 as split bf16 [w*n+i][g2p]; and
+// the broadcast term Gb [w][dout] = (spin means of X0) W_g1 [g1p][dout].
+size_t inputs_value_smem(int n, int A, int g1p);
+cudaError_t launch_inputs_value(cudaStream_t s, int B, int n, int A, int n_up, int C, int K0p, int g1p, int g2p,
+                                int dout, const float* electrons, const float* atoms, const float* charges,
+                                double nuc, const float* Wg1, float* rae, float* aevec, float* H2, StSplit X0s,
+                                StSplit G2s, float* Gb, float* pe);
+
 // Two-electron layer h2' = residual(tanh(h2 W + b)) on compact tangent rows.
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout);
