@@ -517,10 +517,17 @@ struct EpiTcLayer : ContigTiles {
             ptx::ldsm_x4_trans(sb + (uint32_t)(((1 * kCR + row) * 32 + 8 * swz(row, lp)) * 2), rl[rb]);
           }
         }
-        // FULL: every row of the chunk is a Jacobian tangent of this group
-        // (t in [2, T)), so the per-row range checks drop out
-        auto compute = [&](auto full_tag) {
-          constexpr bool FULLc = decltype(full_tag)::value;
+        // MODE 1: every row of the chunk is a Jacobian tangent or a padding
+        // row (T <= t < Tp) of this group: padding rows have zero
+        // accumulators, broadcast terms and residuals, so they come out as
+        // the zeros they must be stored as with no per-row checks.  MODE 2:
+        // the group's first chunk with off = 0, the same plus the value row
+        // t = 0 and the Laplacian row t = 1 in fragment slot (rb 0, e 0 / 1)
+        // of quad lane 0.  MODE 0: chunks that reach into a neighbouring
+        // group (off > 0, or Tp not a multiple of 16), rows checked one by
+        // one.
+        auto compute = [&](auto mode_tag) {
+          constexpr int MODE = decltype(mode_tag)::value;
           // pre-activations z of this thread's 16 elements [rb][e][fb]
           float z[2][2][4];
   #pragma unroll
@@ -529,7 +536,7 @@ struct EpiTcLayer : ContigTiles {
             for (int e = 0; e < 2; ++e) {
               const int sr = 8 * rb + T2 + e;
               const int t = 16 * c - off + sr;
-              const bool real = FULLc || (t >= 0 && t < T);
+              const bool real = MODE != 0 || (t >= 0 && t < T);
   #pragma unroll
               for (int fb = 0; fb < 4; ++fb) {
                 const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
@@ -552,7 +559,7 @@ struct EpiTcLayer : ContigTiles {
                 res[rb][0][fb] = res[rb][1][fb] = 0.f;
               }
             }
-          if (!FULLc && c == 0) {
+          if (MODE == 2 || (MODE == 0 && c == 0)) {
             // value row: h = tanh(z + b) on the source lane, then shared by the quad
   #pragma unroll
             for (int fb = 0; fb < 4; ++fb) {
@@ -563,6 +570,7 @@ struct EpiTcLayer : ContigTiles {
               res1[fb] = res[0][1][fb];
             }
           }
+          const bool head = MODE == 2 && (lane & 3) == 0;  // this lane holds t = 0 and t = 1
           uint32_t oh[2][4], ol[2][4];
   #pragma unroll
           for (int rb = 0; rb < 2; ++rb)
@@ -574,14 +582,23 @@ struct EpiTcLayer : ContigTiles {
                 const int t = 16 * c - off + 8 * rb + T2 + e;
                 const float zz = z[rb][e][fb];
                 float v;
-                if (!FULLc && t == 0) {
-                  v = h[fb];
+                if (MODE == 0) {
+                  if (t == 0) {
+                    v = h[fb];
+                  } else {
+                    if (t >= 2) S[fb] = fmaf(zz, zz, S[fb]);  // zero for padding rows
+                    v = d1[fb] * zz;                          // t = 1 rewritten at the end
+                  }
+                } else if (MODE == 2 && rb == 0) {
+                  const float zs = head ? 0.f : zz;
+                  S[fb] = fmaf(zs, zs, S[fb]);
+                  v = (e == 0 && head) ? h[fb] : d1[fb] * zz;  // t = 1 rewritten at the end
                 } else {
-                  if (FULLc || t >= 2) S[fb] = fmaf(zz, zz, S[fb]);  // zero for padding rows
-                  v = d1[fb] * zz;                                   // t = 1 rewritten at the end
+                  S[fb] = fmaf(zz, zz, S[fb]);
+                  v = d1[fb] * zz;
                 }
                 if (RESID) v = (v + res[rb][e][fb]) * kRsqrt2;
-                y[e] = (!FULLc && t >= T) ? 0.f : v;
+                y[e] = (MODE == 0 && t >= T) ? 0.f : v;
               }
               const __nv_bfloat162 hi = __floats2bfloat162_rn(y[0], y[1]);
               const float2 hf = __bfloat1622float2(hi);
@@ -597,8 +614,10 @@ struct EpiTcLayer : ContigTiles {
           }
         };
         const int tc0 = 16 * c - off;
-        if (c > 0 && tc0 >= 2 && tc0 + 16 <= T) compute(std::true_type{});
-        else compute(std::false_type{});
+        const bool inside = tc0 >= 0 && tc0 + 16 <= Tp;
+        if (inside && c > 0) compute(std::integral_constant<int, 1>{});
+        else if (inside && off == 0) compute(std::integral_constant<int, 2>{});
+        else compute(std::integral_constant<int, 0>{});
         __syncwarp();
         // rows of this group except the Laplacian row (written below)
         store_rows_sw(out, (long long)r0 + 16 * c - off, sr_lo(c), sr_hi(c), c == 0 ? off + 1 : -1, col0, nvec, lane,
