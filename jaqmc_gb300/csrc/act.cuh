@@ -10,6 +10,18 @@
 
 namespace qmc {
 
+// tanh for the split-BF16 (mixed) form's value-only activations: from
+// tanh|x| = (1 - e) / (1 + e), e = 2^(-2 log2(e) |x|), with the hardware
+// base-2 exponential (ex2.approx, relative error ~2^-22) and a fast divide.
+// Absolute error a few 1e-7, below the ~1e-5 relative error of the form's
+// split-BF16 GEMM operands; saturates to +-1 for large |x| and keeps the sign
+// of x (tanh(+-0) = +-0).
+__device__ __forceinline__ float split_tanh(float x) {
+  float e;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(fabsf(x) * -2.8853900817779268f));
+  return copysignf(__fdividef(1.f - e, 1.f + e), x);
+}
+
 struct StF32 {
   float* p;
   int ld;

@@ -552,19 +552,12 @@ __device__ __forceinline__ void pair_fma8(float x, const float* __restrict__ w, 
   }
 }
 
-// tanh for the two-electron stream.  FAST (mixed form): from
-// tanh|x| = (1 - e) / (1 + e), e = 2^(-2 log2(e) |x|), with the hardware
-// base-2 exponential and a fast divide; absolute error a few 1e-7, below the
-// ~1e-5 relative error of the form's split-BF16 operands.  Otherwise tanhf.
+// tanh for the two-electron stream: split_tanh in the mixed form (FAST),
+// otherwise tanhf.
 template <bool FAST>
 __device__ __forceinline__ float pair_tanh(float x) {
-  if constexpr (FAST) {
-    float e;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(fabsf(x) * -2.8853900817779268f));
-    return copysignf(__fdividef(1.f - e, 1.f + e), x);
-  } else {
-    return tanhf(x);
-  }
+  if constexpr (FAST) return split_tanh(x);
+  else return tanhf(x);
 }
 
 template <class Out>

@@ -425,8 +425,8 @@ struct EpiTcLayer : ContigTiles {
           for (int fb = 0; fb < 4; ++fb) {
             // accumulator registers of (fb, rb): lane half fb / 2, rows even/odd at q = 2 (fb & 1) + e
             const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
-            float y0 = tanhf(__uint_as_float(ra[0]) + gb[rb][0][fb] + bq[fb]);
-            float y1 = tanhf(__uint_as_float(ra[1]) + gb[rb][1][fb] + bq[fb]);
+            float y0 = split_tanh(__uint_as_float(ra[0]) + gb[rb][0][fb] + bq[fb]);
+            float y1 = split_tanh(__uint_as_float(ra[1]) + gb[rb][1][fb] + bq[fb]);
             if (RESID) {
               const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[fb]));
               const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[fb]));
