@@ -425,17 +425,16 @@ struct EpiTcLayer : ContigTiles {
           for (int fb = 0; fb < 4; ++fb) {
             // accumulator registers of (fb, rb): lane half fb / 2, rows even/odd at q = 2 (fb & 1) + e
             const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
-            float y0 = split_tanh(__uint_as_float(ra[0]) + gb[rb][0][fb] + bq[fb]);
-            float y1 = split_tanh(__uint_as_float(ra[1]) + gb[rb][1][fb] + bq[fb]);
+            float2 y = make_float2(split_tanh(__uint_as_float(ra[0]) + gb[rb][0][fb] + bq[fb]),
+                                   split_tanh(__uint_as_float(ra[1]) + gb[rb][1][fb] + bq[fb]));
             if (RESID) {
               const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[fb]));
               const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[fb]));
-              y0 = (y0 + (h2.x + l2.x)) * kRsqrt2;
-              y1 = (y1 + (h2.y + l2.y)) * kRsqrt2;
+              y = __fmul2_rn(__fadd2_rn(y, __fadd2_rn(h2, l2)), make_float2(kRsqrt2, kRsqrt2));
             }
-            const __nv_bfloat162 hi = __floats2bfloat162_rn(y0, y1);
-            const float2 hf = __bfloat1622float2(hi);
-            const __nv_bfloat162 lo = __floats2bfloat162_rn(y0 - hf.x, y1 - hf.y);
+            const __nv_bfloat162 hi = __floats2bfloat162_rn(y.x, y.y);
+            const float2 lo2 = __ffma2_rn(__bfloat1622float2(hi), make_float2(-1.f, -1.f), y);  // y - hi, exact
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(lo2.x, lo2.y);
             oh[fb] = *reinterpret_cast<const uint32_t*>(&hi);
             ol[fb] = *reinterpret_cast<const uint32_t*>(&lo);
           }
@@ -488,6 +487,9 @@ struct EpiTcLayer : ContigTiles {
       };
       prefetch(0, 0);
       float h[4], d1[4], S[4] = {0.f, 0.f, 0.f, 0.f}, zL[4] = {0.f, 0.f, 0.f, 0.f}, res1[4] = {0.f, 0.f, 0.f, 0.f};
+      // |grad z|^2 partial sums: S from the checked chunks, S2 (rows e = 0, 1
+      // apart) from the unchecked ones
+      float2 S2[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       const int src = (lane & ~3) | (off >> 1);  // quad lane holding t = 0 and t = 1
       int k = 0;
       for (int c = 0; c < nch; ++c, k ^= 1) {
@@ -528,21 +530,33 @@ struct EpiTcLayer : ContigTiles {
         // one.
         auto compute = [&](auto mode_tag) {
           constexpr int MODE = decltype(mode_tag)::value;
-          // pre-activations z of this thread's 16 elements [rb][e][fb]
+          // pre-activations z of this thread's 16 elements [rb][e][fb]; the two
+          // rows e = 0, 1 of a (rb, fb) slot are one packed f32x2 operand in
+          // the unchecked modes
           float z[2][2][4];
   #pragma unroll
           for (int rb = 0; rb < 2; ++rb)
   #pragma unroll
-            for (int e = 0; e < 2; ++e) {
-              const int sr = 8 * rb + T2 + e;
-              const int t = 16 * c - off + sr;
-              const bool real = MODE != 0 || (t >= 0 && t < T);
+            for (int fb = 0; fb < 4; ++fb) {
+              const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
+              float gv[2];
   #pragma unroll
-              for (int fb = 0; fb < 4; ++fb) {
-                const uint32_t* ra = r + 4 * (2 * (fb >> 1) + rb) + 2 * (fb & 1);
+              for (int e = 0; e < 2; ++e) {
+                const int sr = 8 * rb + T2 + e;
                 const int pz = ((T4 >> 2) + 2 * fb) ^ (((sr >> 1) & 3) << 1);
-                const float gv = gbuf[sr * 32 + 4 * pz + (T4 & 3)];
-                z[rb][e][fb] = real ? __uint_as_float(ra[e]) + gv : 0.f;
+                gv[e] = gbuf[sr * 32 + 4 * pz + (T4 & 3)];
+              }
+              if (MODE != 0) {
+                const float2 zp = __fadd2_rn(make_float2(__uint_as_float(ra[0]), __uint_as_float(ra[1])),
+                                             make_float2(gv[0], gv[1]));
+                z[rb][0][fb] = zp.x;
+                z[rb][1][fb] = zp.y;
+              } else {
+  #pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                  const int t = 16 * c - off + 8 * rb + T2 + e;
+                  z[rb][e][fb] = (t >= 0 && t < T) ? __uint_as_float(ra[e]) + gv[e] : 0.f;
+                }
               }
             }
           float res[2][2][4];
@@ -553,8 +567,9 @@ struct EpiTcLayer : ContigTiles {
               if (RESID) {
                 const float2 h2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rh[rb][fb]));
                 const float2 l2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&rl[rb][fb]));
-                res[rb][0][fb] = h2.x + l2.x;
-                res[rb][1][fb] = h2.y + l2.y;
+                const float2 rs = __fadd2_rn(h2, l2);
+                res[rb][0][fb] = rs.x;
+                res[rb][1][fb] = rs.y;
               } else {
                 res[rb][0][fb] = res[rb][1][fb] = 0.f;
               }
@@ -576,33 +591,38 @@ struct EpiTcLayer : ContigTiles {
           for (int rb = 0; rb < 2; ++rb)
   #pragma unroll
             for (int fb = 0; fb < 4; ++fb) {
-              float y[2];
+              float2 y;
+              if (MODE == 0) {
+                float ys[2];
   #pragma unroll
-              for (int e = 0; e < 2; ++e) {
-                const int t = 16 * c - off + 8 * rb + T2 + e;
-                const float zz = z[rb][e][fb];
-                float v;
-                if (MODE == 0) {
+                for (int e = 0; e < 2; ++e) {
+                  const int t = 16 * c - off + 8 * rb + T2 + e;
+                  const float zz = z[rb][e][fb];
+                  float v;
                   if (t == 0) {
                     v = h[fb];
                   } else {
                     if (t >= 2) S[fb] = fmaf(zz, zz, S[fb]);  // zero for padding rows
                     v = d1[fb] * zz;                          // t = 1 rewritten at the end
                   }
-                } else if (MODE == 2 && rb == 0) {
-                  const float zs = head ? 0.f : zz;
-                  S[fb] = fmaf(zs, zs, S[fb]);
-                  v = (e == 0 && head) ? h[fb] : d1[fb] * zz;  // t = 1 rewritten at the end
-                } else {
-                  S[fb] = fmaf(zz, zz, S[fb]);
-                  v = d1[fb] * zz;
+                  if (RESID) v = (v + res[rb][e][fb]) * kRsqrt2;
+                  ys[e] = t >= T ? 0.f : v;
                 }
-                if (RESID) v = (v + res[rb][e][fb]) * kRsqrt2;
-                y[e] = (MODE == 0 && t >= T) ? 0.f : v;
+                y = make_float2(ys[0], ys[1]);
+              } else {
+                const float2 zz = make_float2(z[rb][0][fb], z[rb][1][fb]);
+                // MODE 2, rb 0: the head lane's rows t = 0, 1 stay out of |grad z|^2
+                const float2 zs = (MODE == 2 && rb == 0 && head) ? make_float2(0.f, 0.f) : zz;
+                S2[fb] = __ffma2_rn(zs, zs, S2[fb]);
+                y = __fmul2_rn(make_float2(d1[fb], d1[fb]), zz);  // t = 1 rewritten at the end
+                if (MODE == 2 && rb == 0 && head) y.x = h[fb];
+                if (RESID)
+                  y = __fmul2_rn(__fadd2_rn(y, make_float2(res[rb][0][fb], res[rb][1][fb])),
+                                 make_float2(kRsqrt2, kRsqrt2));
               }
-              const __nv_bfloat162 hi = __floats2bfloat162_rn(y[0], y[1]);
-              const float2 hf = __bfloat1622float2(hi);
-              const __nv_bfloat162 lo = __floats2bfloat162_rn(y[0] - hf.x, y[1] - hf.y);
+              const __nv_bfloat162 hi = __floats2bfloat162_rn(y.x, y.y);
+              const float2 lo2 = __ffma2_rn(__bfloat1622float2(hi), make_float2(-1.f, -1.f), y);  // y - hi, exact
+              const __nv_bfloat162 lo = __floats2bfloat162_rn(lo2.x, lo2.y);
               oh[rb][fb] = *reinterpret_cast<const uint32_t*>(&hi);
               ol[rb][fb] = *reinterpret_cast<const uint32_t*>(&lo);
             }
@@ -628,7 +648,7 @@ struct EpiTcLayer : ContigTiles {
       // y = tanh'' |grad z|^2 + tanh' lap z  (tanh'' = -2 h tanh')
 #pragma unroll
       for (int fb = 0; fb < 4; ++fb) {
-        float st = S[fb];
+        float st = S[fb] + (S2[fb].x + S2[fb].y);
         st += __shfl_xor_sync(0xffffffffu, st, 1);
         st += __shfl_xor_sync(0xffffffffu, st, 2);
         float y1 = d1[fb] * zL[fb] - 2.f * h[fb] * d1[fb] * st;
