@@ -57,7 +57,7 @@ def normalize_masked(x: torch.Tensor, mask: torch.Tensor, mode: str = "mean") ->
         cnt = mask.to(x.dtype).sum()
         norm = s / cnt if cnt > 0 else torch.ones((), dtype=x.dtype, device=x.device)
     else:
-        raise ValueError(f"Unsupported normalization mode: {mode}")
+        raise ValueError(f"normalisation mode must be 'sum' or 'mean' (got {mode!r})")
     norm = norm if norm > 0 else torch.ones((), dtype=x.dtype, device=x.device)
     return torch.where(mask, x / norm, x)
 
@@ -128,131 +128,29 @@ def lift_null_space(gram: torch.Tensor) -> torch.Tensor:
     return centred + 1.0 / B
 
 
-def estimate_required_damping(gram: torch.Tensor, target_cond_num: float, num_iters: int = 10,
-                              rtol: float = 1e-6) -> torch.Tensor:
+def estimate_required_damping(gram: torch.Tensor, target_cond_num: float, num_iters: int = 10) -> torch.Tensor:
     """Smallest damping lam >= 0 with (eig_max + lam) / lam <= target_cond_num,
     taking the smallest eigenvalue of the (positive semi-definite) Gram
-    matrix as 0.  eig_max is a Rayleigh quotient after at most ``num_iters``
-    multiplications, started from the square roots of the diagonal (a vector
-    with a large component along the dominant eigenvector of a Gram matrix),
-    stopping early once the estimate moves by less than ``rtol``."""
+    matrix as 0.  eig_max is the Rayleigh quotient after ``num_iters``
+    multiplications, started from the square roots of the diagonal scaled by
+    1 + 0.5 frac(i phi) (phi the golden ratio): the diagonal weights the
+    walkers with large scores, and the deterministic scatter keeps a
+    component along every eigenvector, which a centred Gram matrix's own
+    rows or diagonal can lack."""
     if not target_cond_num > 1.0:
         raise ValueError(f"the target condition number has to exceed 1 (got {target_cond_num})")
-    v = torch.sqrt(torch.clamp(torch.diagonal(gram), min=0.0)) + 1e-30
+    B = gram.shape[0]
+    idx = torch.arange(B, dtype=gram.dtype, device=gram.device)
+    scatter = 1.0 + 0.5 * torch.frac(idx * 0.6180339887498949)
+    v = torch.sqrt(torch.clamp(torch.diagonal(gram), min=0.0)) * scatter + 1e-30
     v = v / torch.linalg.norm(v)
-    est = torch.dot(v, gram @ v)
     for _ in range(num_iters):
         w = gram @ v
         nrm = torch.linalg.norm(w)
         if not float(nrm) > 0.0:
             break
         v = w / nrm
-        new = torch.dot(v, gram @ v)
-        done = abs(float(new - est)) <= rtol * abs(float(new))
-        est = new
-        if done:
-            break
-    return torch.clamp(est / (target_cond_num - 1.0), min=0.0)
-
-
-class RobustSRState(NamedTuple):
-    count: int                 # preconditioner steps (FisherInverseState.counter)
-    prev_delta: torch.Tensor   # (P,) previous preconditioned direction
-    acc_var: torch.Tensor      # (P,) MARCH accumulator (ones when unused)
-    norm_count: int            # constrained-norm schedule step
-
-
-def normalize_masked(x: torch.Tensor, mask: torch.Tensor, mode: str = "mean") -> torch.Tensor:
-    """``x / norm`` on the masked entries, norm = their sum or mean (1 if <= 0)."""
-    s = torch.where(mask, x, torch.zeros_like(x)).sum()
-    if mode == "sum":
-        norm = s
-    elif mode == "mean":
-        cnt = mask.to(x.dtype).sum()
-        norm = s / cnt if cnt > 0 else torch.ones((), dtype=x.dtype, device=x.device)
-    else:
-        raise ValueError(f"Unsupported normalization mode: {mode}")
-    norm = norm if norm > 0 else torch.ones((), dtype=x.dtype, device=x.device)
-    return torch.where(mask, x / norm, x)
-
-
-def gram_matrix(score: torch.Tensor, scale, block: int = 1024, precision: str = "f64") -> torch.Tensor:
-    """FP64 ``(O diag(s) O^T)`` of an already centred score matrix (used by
-    the tests and callers holding O): see :func:`_centred_gram`."""
-    B, P = score.shape
-    zero = torch.zeros(P, dtype=torch.float64, device=score.device)
-    sc = scale if torch.is_tensor(scale) else torch.full((P,), float(scale), dtype=torch.float64,
-                                                         device=score.device)
-    return _centred_gram(score, zero, torch.ones(B, dtype=torch.float64, device=score.device), 1.0, sc,
-                         block, precision)
-
-
-def _blocks(P: int, block: int):
-    return [(c0, min(P, c0 + block)) for c0 in range(0, P, block)]
-
-
-def _centred_block(S, mean, rescale, inv_sqrt_b, c0, c1) -> torch.Tensor:
-    """FP64 column block ``(rescale * S - mean) / sqrt(B)`` of the centred
-    score (centring in FP64, so columns with a large mean keep their spread)."""
-    return (S[:, c0:c1].double() * rescale[:, None] - mean[c0:c1]) * inv_sqrt_b
-
-
-def _centred_gram(S, mean, rescale, inv_sqrt_b, scale, block: int, precision: str) -> torch.Tensor:
-    """FP64 ``O diag(scale) O^T`` for O = centred score: rows normalised by
-    their max |entry| (clipped at 1e-4; the reference's calc_gram_matrix),
-    products in FP64 (``"f64"``) or in FP32 over ``block``-column pieces summed
-    in FP64 (``"f32"``), row scales put back, symmetrised."""
-    B, P = S.shape
-    big = _blocks(P, 16384)
-    rf = torch.zeros(B, dtype=torch.float64, device=S.device)
-    for c0, c1 in big:
-        ob = _centred_block(S, mean, rescale, inv_sqrt_b, c0, c1) * torch.sqrt(scale[c0:c1])
-        rf = torch.maximum(rf, ob.abs().amax(dim=1))
-    rf = rf.clamp(min=1e-4)
-    gram = torch.zeros((B, B), dtype=torch.float64, device=S.device)
-    prev = torch.backends.cuda.matmul.allow_tf32
-    torch.backends.cuda.matmul.allow_tf32 = False
-    try:
-        for c0, c1 in big:
-            ob = _centred_block(S, mean, rescale, inv_sqrt_b, c0, c1) * torch.sqrt(scale[c0:c1]) / rf[:, None]
-            if precision == "f64":
-                gram += ob @ ob.T
-            else:
-                obf = ob.float()
-                for d0 in range(0, c1 - c0, block):
-                    piece = obf[:, d0:d0 + block]
-                    gram += (piece @ piece.T).double()
-    finally:
-        torch.backends.cuda.matmul.allow_tf32 = prev
-    gram = gram * (rf[:, None] * rf[None, :])
-    return (gram + gram.T) / 2
-
-
-def lift_null_space(gram: torch.Tensor) -> torch.Tensor:
-    """Double-centre the Gram matrix and add back the constant direction
-    (real scores, one device): full rank while centred scores leave the
-    solution unchanged."""
-    B = gram.shape[0]
-    mean_vec = torch.full((1, B), B ** -0.5, dtype=gram.dtype, device=gram.device)
-    shift = torch.full((B, B), 1.0 / B, dtype=gram.dtype, device=gram.device)
-    mean_one = (gram @ mean_vec.T) @ mean_vec
-    mean_all = mean_vec.T @ (mean_vec @ mean_one)
-    return gram - mean_one - mean_one.T + mean_all + shift
-
-
-def estimate_required_damping(gram: torch.Tensor, target_cond_num: float, num_iters: int = 10) -> torch.Tensor:
-    """Damping that bounds the condition number, from a power-iteration
-    estimate of the largest eigenvalue (the smallest taken as 0)."""
-    if target_cond_num <= 1.0:
-        raise ValueError(f"target_cond_num must be greater than 1, got {target_cond_num}")
-    gen = torch.Generator(device=gram.device).manual_seed(42)
-    v = torch.rand(gram.shape[0], dtype=gram.dtype, device=gram.device, generator=gen)
-    v = v / torch.linalg.norm(v)
-    for _ in range(num_iters):
-        v = gram @ v
-        v = v / torch.linalg.norm(v)
-    eig_max = torch.dot(v, gram @ v)
-    return torch.clamp(eig_max / (target_cond_num - 1.0), min=0.0)
+    return torch.clamp(torch.dot(v, gram @ v) / (target_cond_num - 1.0), min=0.0)
 
 
 class RobustSR:
