@@ -277,11 +277,14 @@ static bool pair_stream(const Dims& d, const Plan& p) {
   return (size_t)(d.L - 1) * p.g2_plane * 4 <= p.g1 - p.h2[1];
 }
 
-// Value-only mixed passes on the fused two-electron path take every input of
-// the first layer (split features, pair-mean rows, broadcast term) from one
-// launch_inputs_value call.
+// Mixed passes take every input of the first layer (split features,
+// pair-mean rows, broadcast term) from one per-walker kernel: value-only
+// passes on the fused two-electron path (launch_inputs_value), tangent passes
+// with the compact pair tangents (launch_inputs_fl).
 static bool inputs_fused(const Dims& d, const Plan& p) {
-  return p.mixed && p.T == 1 && pair_fused(d, p.T) && inputs_value_smem(d.n, d.A, d.g1_p[0]) <= 48 * 1024;
+  if (!p.mixed) return false;
+  if (p.T == 1) return pair_fused(d, p.T) && inputs_value_smem(d.n, d.A, d.g1_p[0]) <= 48 * 1024;
+  return p.P2 == 5 && d.d2_in[0] == 4 && inputs_fl_supported(d.n, d.A, p.Tp, d.g1_p[0]);
 }
 
 // The means after pair layer l - 1 (input of one-electron layer l >= 1) on
@@ -605,13 +608,21 @@ qmc_status evaluate(qmc_model* m, const Plan& p, void* ws, const float* electron
   const bool fused = pair_fused(d, p.T);
   if (inputs_fused(d, p)) {
     typedef __nv_bfloat16 bf;
-    const size_t rows = (size_t)p.B * d.n;
-    QMC_PROF(QMC_KC_FEATURES,
-             launch_inputs_value(s, p.B, d.n, d.A, d.n_up, d.C, p.K0p, d.g1_p[0], d.g2_p[0], d.d1[0], electrons,
-                                 ar + m->a.atoms, ar + m->a.charges, m->nuclear_repulsion, ar + m->a.w_g1[0],
-                                 at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, p.h2[0]),
-                                 StSplit{at<bf>(ws, p.x0s), p.K0p, rows * p.K0p},
-                                 StSplit{at<bf>(ws, p.g2s0), d.g2_p[0], rows * d.g2_p[0]}, at<float>(ws, p.gb), pe));
+    const size_t rows = (size_t)p.B * d.n * p.Tp;
+    const StSplit x0s{at<bf>(ws, p.x0s), p.K0p, rows * p.K0p};
+    const StSplit g2s{at<bf>(ws, p.g2s0), d.g2_p[0], rows * d.g2_p[0]};
+    if (p.T == 1)
+      QMC_PROF(QMC_KC_FEATURES,
+               launch_inputs_value(s, p.B, d.n, d.A, d.n_up, d.C, p.K0p, d.g1_p[0], d.g2_p[0], d.d1[0], electrons,
+                                   ar + m->a.atoms, ar + m->a.charges, m->nuclear_repulsion, ar + m->a.w_g1[0],
+                                   at<float>(ws, p.rae), at<float>(ws, p.aevec), at<float>(ws, p.h2[0]), x0s, g2s,
+                                   at<float>(ws, p.gb), pe));
+    else
+      QMC_PROF(QMC_KC_FEATURES,
+               launch_inputs_fl(s, p.B, d.n, d.A, d.n_up, d.C, p.Tp, p.T, p.K0p, d.g1_p[0], d.g2_p[0], d.d1[0],
+                                electrons, ar + m->a.atoms, ar + m->a.charges, m->nuclear_repulsion,
+                                ar + m->a.w_g1[0], at<float>(ws, p.rae), at<float>(ws, p.aevec),
+                                at<float>(ws, p.h2[0]), x0s, g2s, at<float>(ws, p.gb), pe));
   } else {
     QMC_PROF(QMC_KC_FEATURES, launch_features(s, p.B, d.n, d.A, p.Tp, p.T, p.K0p, electrons, ar + m->a.atoms,
                                               ar + m->a.charges, m->nuclear_repulsion, at<float>(ws, p.x0),

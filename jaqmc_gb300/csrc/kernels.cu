@@ -1155,9 +1155,13 @@ __global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, 
   __syncthreads();
   const size_t row0 = (size_t)w * n;
   const int A4 = 4 * A;
-  for (int e = threadIdx.x; e < n * K0p; e += blockDim.x) {
-    const int i = e / K0p, f = e - i * K0p;
-    X0s.put(row0 + i, f, f < A4 ? f4_comp(ea[i * A + (f >> 2)], f & 3) : 0.f);
+  const int k8 = K0p / 8;  // 8 features per thread, 16-byte stores
+  for (int e = threadIdx.x; e < n * k8; e += blockDim.x) {
+    const int i = e / k8, f0 = 8 * (e - i * k8);
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = f0 + q < A4 ? f4_comp(ea[i * A + ((f0 + q) >> 2)], (f0 + q) & 3) : 0.f;
+    store8(X0s, row0 + i, f0, v);
   }
   for (int col = threadIdx.x; col < g1p; col += blockDim.x) {
     float acc = 0.f;
@@ -1170,19 +1174,26 @@ __global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, 
     }
     g1[col] = acc;
   }
-  for (int e = threadIdx.x; e < n * g2p; e += blockDim.x) {
-    const int i = e / g2p, col = e - i * g2p;
-    float v = 0.f;
-    if (col < 4 * C) {
-      const int sc = col >> 2, c4 = col & 3;
-      int a0, a1;
-      channel_range(sc, C, n, n_up, &a0, &a1);
-      float acc = 0.f;
-      for (int a = a0; a < a1; ++a)
-        if (a != i) acc += f4_comp(pr[a * n + i], c4);  // pair (a, i): r_a - r_i
-      v = acc / (float)(a1 - a0);
+  const int c8 = g2p / 8;
+  for (int e = threadIdx.x; e < n * c8; e += blockDim.x) {
+    const int i = e / c8, col0 = 8 * (e - i * c8);
+    float vv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int col = col0 + q;
+      float v = 0.f;
+      if (col < 4 * C) {
+        const int sc = col >> 2, c4 = col & 3;
+        int a0, a1;
+        channel_range(sc, C, n, n_up, &a0, &a1);
+        float acc = 0.f;
+        for (int a = a0; a < a1; ++a)
+          if (a != i) acc += f4_comp(pr[a * n + i], c4);  // pair (a, i): r_a - r_i
+        v = acc / (float)(a1 - a0);
+      }
+      vv[q] = v;
     }
-    G2s.put(row0 + i, col, v);
+    store8(G2s, row0 + i, col0, vv);
   }
   __syncthreads();
   for (int f = threadIdx.x; f < dout; f += blockDim.x) {
@@ -1200,6 +1211,227 @@ __global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, 
       if (threadIdx.x == 0) pe[w] = (float)(v + nuc);
     }
   }
+}
+
+// Forward-Laplacian passes of the mixed form: the same per-walker fusion with
+// T tangent rows (value, Laplacian, 3n Jacobian rows; Tp padded) -- the rows
+// k_features writes (X0 as split bf16, H2 with P2 = 5 tangent planes), the
+// first layer's broadcast term Gb[w, t] = g1[w, t] W_g1 with g1 the spin means
+// of X0 (k_mean_h1_vec's order: electrons in index order, then times 1/n_s),
+// and the spin means of the pair rows with their tangent rules (k_mean_h2):
+// rows t = 0, 1 average pair values and Laplacians (the latter doubled), a
+// Jacobian row of electron el either subtracts the gradients of every pair
+// (el, i) with i the row's electron, or takes the one pair (el, i) of el's
+// channel.  W_g1's column of a thread stays in registers (g1p <= kFlG1Max).
+constexpr int kFlG1Max = 32;
+
+__global__ void __launch_bounds__(256, 1) k_inputs_fl(int n, int A, int n_up, int C, int Tp, int T, int K0p, int g1p,
+                                                   int g2p, int dout, const float* __restrict__ elec,
+                                                   const float* __restrict__ atoms, const float* __restrict__ charges,
+                                                   double nuc, const float* __restrict__ Wg1,
+                                                   float* __restrict__ rae_g, float* __restrict__ aevec_g,
+                                                   float* __restrict__ H2, StSplit X0s, StSplit G2s,
+                                                   float* __restrict__ Gb, float* __restrict__ pe) {
+  // shared tables of the walker (every quotient formed once):
+  //   ea [n][A]      (|r_i - R_I|, r_i - R_I)
+  //   ed [n][A]      (2 / |r_i - R_I|, (r_i - R_I) / |r_i - R_I|)
+  //   pl [n][n][5]   the five planes of pair (a, b) (r_a - r_b), rows of H2
+  //   ps [C][n][5]   per channel s and electron b: sum over a in s of pl[a][b]
+  //   g1 [Tp][g1p]   spin means of the one-electron rows
+  extern __shared__ float4 shfl4[];
+  float4* ea = shfl4;
+  float4* ed = ea + n * A;
+  float4* pl = ed + n * A;
+  float4* ps = pl + (size_t)n * n * 5;
+  float* g1 = reinterpret_cast<float*>(ps + (size_t)C * n * 5);
+  float* xs = g1 + Tp * g1p;
+  __shared__ double red[8];
+  const int w = blockIdx.x;
+  const float* ew = elec + (size_t)w * n * 3;
+  for (int e = threadIdx.x; e < 3 * n; e += blockDim.x) xs[e] = ew[e];
+  __syncthreads();
+  double vpot = 0.0;
+  for (int e = threadIdx.x; e < n * A; e += blockDim.x) {
+    const int i = e / A, I = e - i * A;
+    const float dx = xs[3 * i] - atoms[3 * I], dy = xs[3 * i + 1] - atoms[3 * I + 1],
+                dz = xs[3 * i + 2] - atoms[3 * I + 2];
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    ea[e] = make_float4(r, dx, dy, dz);
+    ed[e] = make_float4(2.0f / r, dx / r, dy / r, dz / r);
+    const size_t gi = (size_t)w * n * A + e;
+    rae_g[gi] = r;
+    aevec_g[3 * gi] = dx;
+    aevec_g[3 * gi + 1] = dy;
+    aevec_g[3 * gi + 2] = dz;
+    if (pe) vpot -= (double)charges[I] / (double)r;
+  }
+  float4* h2w = reinterpret_cast<float4*>(H2) + (size_t)w * n * n * 5;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;
+    float4 v[5];
+#pragma unroll
+    for (int p = 0; p < 5; ++p) v[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i != j) {
+      const float d0 = xs[3 * i] - xs[3 * j], d1 = xs[3 * i + 1] - xs[3 * j + 1], d2 = xs[3 * i + 2] - xs[3 * j + 2];
+      const float r = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+      v[0] = make_float4(r, d0, d1, d2);
+      v[1] = make_float4(2.0f / r, 0.f, 0.f, 0.f);
+      v[2] = make_float4(d0 / r, 1.f, 0.f, 0.f);
+      v[3] = make_float4(d1 / r, 0.f, 1.f, 0.f);
+      v[4] = make_float4(d2 / r, 0.f, 0.f, 1.f);
+      if (pe && i < j) vpot += 1.0 / (double)r;
+    }
+#pragma unroll
+    for (int p = 0; p < 5; ++p) {
+      pl[(size_t)e * 5 + p] = v[p];
+      h2w[(size_t)e * 5 + p] = v[p];
+    }
+  }
+  __syncthreads();
+  // channel sums of the pair planes over the first electron, in electron order
+  for (int e = threadIdx.x; e < C * n * 5; e += blockDim.x) {
+    const int sc = e / (n * 5), rem = e - sc * n * 5;
+    const int b = rem / 5, p = rem - b * 5;
+    int a0, a1;
+    channel_range(sc, C, n, n_up, &a0, &a1);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int a = a0; a < a1; ++a) {
+      const float4 v = pl[((size_t)a * n + b) * 5 + p];
+      acc.x += v.x;
+      acc.y += v.y;
+      acc.z += v.z;
+      acc.w += v.w;
+    }
+    ps[e] = acc;
+  }
+  const int A4 = 4 * A;
+  // one-electron feature f of electron i, tangent row t (k_features' rows)
+  auto x0v = [&](int i, int t, int f) -> float {
+    if (f >= A4 || t >= T) return 0.f;
+    const int I = f >> 2, comp = f & 3;
+    if (t == 0) return f4_comp(ea[i * A + I], comp);
+    if (t == 1) return comp == 0 ? ed[i * A + I].x : 0.f;
+    const int dd = t - 2, el = dd / 3, c = dd - 3 * el;
+    if (el != i) return 0.f;
+    return comp == 0 ? f4_comp(ed[i * A + I], 1 + c) : (comp - 1 == c ? 1.f : 0.f);
+  };
+  const size_t rowb = (size_t)w * n * Tp;
+  const int k8 = K0p / 8;  // one-electron rows: 8 features per thread, 16-byte stores
+  for (int e = threadIdx.x; e < n * Tp * k8; e += blockDim.x) {
+    const int it = e / k8, f0 = 8 * (e - it * k8);
+    const int i = it / Tp, t = it - i * Tp;
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = x0v(i, t, f0 + q);
+    store8(X0s, rowb + it, f0, v);
+  }
+  // spin means of the one-electron rows: rows t <= 1 sum the channel's
+  // electrons; a Jacobian row of electron el has el's row alone (the other
+  // electrons' rows are zero)
+  for (int e = threadIdx.x; e < Tp * g1p; e += blockDim.x) {
+    const int t = e / g1p, col = e - t * g1p;
+    float acc = 0.f;
+    if (col < C * A4 && t < T) {
+      const int sc = col / A4, f = col - sc * A4;
+      int a0, a1;
+      channel_range(sc, C, n, n_up, &a0, &a1);
+      if (t <= 1) {
+        for (int a = a0; a < a1; ++a) acc += x0v(a, t, f);
+      } else {
+        const int el = (t - 2) / 3;
+        if (el >= a0 && el < a1) acc = x0v(el, t, f);
+      }
+      acc *= 1.0f / (float)(a1 - a0);
+    }
+    g1[e] = acc;
+  }
+  // pair rows' spin means over the first electron a of pair (a, i), per
+  // tangent row (k_mean_h2's rules), 8 columns per thread
+  const int c8 = g2p / 8;
+  for (int e = threadIdx.x; e < n * Tp * c8; e += blockDim.x) {
+    const int it = e / c8, col0 = 8 * (e - it * c8);
+    const int i = it / Tp, t = it - i * Tp;
+    const int dd = t - 2, el = t >= 2 ? dd / 3 : -1, c = t >= 2 ? dd - 3 * el : 0;
+    float vv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int col = col0 + q;
+      float v = 0.f;
+      if (col < 4 * C && t < T) {
+        const int sc = col >> 2, f = col & 3;
+        int a0, a1;
+        channel_range(sc, C, n, n_up, &a0, &a1);
+        const float inv = 1.0f / (float)(a1 - a0);
+        if (t == 0) {
+          v = f4_comp(ps[((size_t)sc * n + i) * 5], f) * inv;
+        } else if (t == 1) {
+          v = 2.0f * f4_comp(ps[((size_t)sc * n + i) * 5 + 1], f) * inv;
+        } else if (el == i) {
+          v = -f4_comp(ps[((size_t)sc * n + i) * 5 + 2 + c], f) * inv;
+        } else if (el >= a0 && el < a1) {
+          v = f4_comp(pl[((size_t)el * n + i) * 5 + 2 + c], f) * inv;
+        }
+      }
+      vv[q] = v;
+    }
+    store8(G2s, rowb + it, col0, vv);
+  }
+  __syncthreads();
+  // broadcast term of the first layer: one output column per thread, its
+  // weights in registers, the spin-mean rows read four at a time
+  for (int f = threadIdx.x; f < dout; f += blockDim.x) {
+    float wc[kFlG1Max];
+#pragma unroll
+    for (int k = 0; k < kFlG1Max; ++k) wc[k] = k < g1p ? __ldg(Wg1 + (size_t)k * dout + f) : 0.f;
+    float* gbw = Gb + (size_t)w * Tp * dout + f;
+    for (int t = 0; t < Tp; ++t) {
+      const float4* gr = reinterpret_cast<const float4*>(g1 + t * g1p);
+      float acc = 0.f;
+#pragma unroll
+      for (int k4 = 0; k4 < kFlG1Max / 4; ++k4) {
+        if (4 * k4 < g1p) {
+          const float4 gv = gr[k4];
+          acc = fmaf(gv.x, wc[4 * k4], acc);
+          acc = fmaf(gv.y, wc[4 * k4 + 1], acc);
+          acc = fmaf(gv.z, wc[4 * k4 + 2], acc);
+          acc = fmaf(gv.w, wc[4 * k4 + 3], acc);
+        }
+      }
+      gbw[(size_t)t * dout] = acc;
+    }
+  }
+  if (pe) {
+    for (int o = 16; o > 0; o >>= 1) vpot += __shfl_xor_sync(0xffffffffu, vpot, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vpot;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) pe[w] = (float)(v + nuc);
+    }
+  }
+}
+
+size_t inputs_fl_smem(int n, int A, int Tp, int g1p, int C) {
+  return sizeof(float4) * (2 * (size_t)n * A + (size_t)n * n * 5 + (size_t)C * n * 5) +
+         sizeof(float) * ((size_t)Tp * g1p + 3 * n);
+}
+
+bool inputs_fl_supported(int n, int A, int Tp, int g1p) {
+  return g1p <= kFlG1Max && g1p % 4 == 0 && inputs_fl_smem(n, A, Tp, g1p, 2) <= 48 * 1024;
+}
+// (K0p and g2p are multiples of 8 and the split planes 16-byte aligned: the
+// rows go out as 16-byte stores)
+
+cudaError_t launch_inputs_fl(cudaStream_t s, int B, int n, int A, int n_up, int C, int Tp, int T, int K0p, int g1p,
+                             int g2p, int dout, const float* electrons, const float* atoms, const float* charges,
+                             double nuc, const float* Wg1, float* rae, float* aevec, float* H2, StSplit X0s,
+                             StSplit G2s, float* Gb, float* pe) {
+  if (!inputs_fl_supported(n, A, Tp, g1p)) return cudaErrorNotSupported;
+  k_inputs_fl<<<B, 256, inputs_fl_smem(n, A, Tp, g1p, C), s>>>(n, A, n_up, C, Tp, T, K0p, g1p, g2p, dout, electrons,
+                                                            atoms, charges, nuc, Wg1, rae, aevec, H2, X0s, G2s, Gb,
+                                                            pe);
+  return cudaGetLastError();
 }
 
 size_t inputs_value_smem(int n, int A, int g1p) {

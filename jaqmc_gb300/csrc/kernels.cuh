@@ -50,6 +50,16 @@ cudaError_t launch_inputs_value(cudaStream_t s, int B, int n, int A, int n_up, i
                                 double nuc, const float* Wg1, float* rae, float* aevec, float* H2, StSplit X0s,
                                 StSplit G2s, float* Gb, float* pe);
 
+// Forward-Laplacian inputs of the mixed form's first layer, one block per
+// walker: rae / aevec / pe and H2 (P2 = 5) as launch_features; X0 as split
+// bf16 [(w*n+i)*Tp + t][K0p]; the pair rows' spin means G2 (split) with their
+// tangent rules as launch_mean_h2; Gb [w*Tp + t][dout] = (spin means of X0) W_g1.
+bool inputs_fl_supported(int n, int A, int Tp, int g1p);
+cudaError_t launch_inputs_fl(cudaStream_t s, int B, int n, int A, int n_up, int C, int Tp, int T, int K0p, int g1p,
+                             int g2p, int dout, const float* electrons, const float* atoms, const float* charges,
+                             double nuc, const float* Wg1, float* rae, float* aevec, float* H2, StSplit X0s,
+                             StSplit G2s, float* Gb, float* pe);
+
 // Two-electron layer h2' = residual(tanh(h2 W + b)) on compact tangent rows.
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout);
