@@ -287,6 +287,16 @@ static bool inputs_fused(const Dims& d, const Plan& p) {
   return p.P2 == 5 && d.d2_in[0] == 4 && inputs_fl_supported(d.n, d.A, p.Tp, d.g1_p[0]);
 }
 
+// Tangent passes fuse each two-electron layer with the next one-electron
+// layer's pair means (launch_pair_layer_mean_fl) for the widths and electron
+// counts that kernel covers.
+static bool pair_means_fused(const Dims& d, const Plan& p) {
+  if (p.T == 1 || p.P2 != 5 || d.n > 32 || p.T != 3 * d.n + 2) return false;
+  for (int l = 0; l < d.L; ++l)
+    if (d.upd2[l] && (d.d2[l] != 32 || (d.d2_in[l] != 4 && d.d2_in[l] != 32))) return false;
+  return true;
+}
+
 // The means after pair layer l - 1 (input of one-electron layer l >= 1) on
 // the fused two-electron path: f32 [B*n][g2_p[l]], or two bf16 planes.
 static size_t stream_g2(const Plan& p, int l) { return p.h2[1] + (size_t)(l - 1) * p.g2_plane * 4; }
@@ -325,6 +335,7 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
   const Dims& d = m->d;
   const bool fused = pair_fused(d, p.T);
   const bool stream = pair_stream(d, p);
+  const bool fl_means = pair_means_fused(d, p);
   if (stream) QMC_TRY(run_pair_stream<StF32>(m, p, ws, s));
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
@@ -344,7 +355,7 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
                                           d.g1_p[l], StF32{G1, d.g1_p[l]}));
     QMC_PROF(QMC_KC_BROADCAST, launch_gemm_simt(s, B, wt_map, G1, d.g1_p[l], d.g1_p[l], nullptr, 0, 0,
                                                 ar + a.w_g1[l], dout, dout, EpiStore{Gb, dout, nullptr}));
-    if (!fused && !stream)
+    if (!fused && !stream && !(l > 0 && fl_means))
       QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
                                             StF32{G2, d.g2_p[l]}));
     EpiLayer<StF32> epi{Gb, ar + a.b1[l], StF32{nullptr, dout}, StF32{out, dout}, T};
@@ -357,6 +368,11 @@ static qmc_status run_backbone_plain(qmc_model* m, const Plan& p, void* ws, cuda
       if (fused)
         QMC_PROF(QMC_KC_PAIR, launch_pair_layer_mean(s, B, n, d.n_up, d.C, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
                                                      ar + a.b2[l], h2o, d.g2_p[l + 1], StF32{G2, d.g2_p[l + 1]}));
+      else if (fl_means)  // the pair output is read again only by a later pair layer
+        QMC_PROF(QMC_KC_PAIR,
+                 launch_pair_layer_mean_fl(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                           ar + a.b2[l], d.upd2[l + 1] ? h2o : nullptr, d.g2_p[l + 1],
+                                           StF32{at<float>(ws, p.g2), d.g2_p[l + 1]}));
       else
         QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
                                                 ar + a.b2[l], h2o));
@@ -374,6 +390,7 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
   const Dims& d = m->d;
   const bool fused = pair_fused(d, p.T);
   const bool stream = pair_stream(d, p);
+  const bool fl_means = pair_means_fused(d, p);
   if (stream) QMC_TRY(run_pair_stream<StSplit>(m, p, ws, s));
   const float* ar = m->arena;
   const ArenaLayout& a = m->a;
@@ -439,7 +456,7 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
                                             d.g1_p[l], StSplit{G1, d.g1_p[l], p.g1_plane}));
       TcStoreArgs sa{B * Tp, G1, d.g1_p[l], p.g1_plane, m->arena_bf16 + a.t_g1[l], dout, Gb, m->dev_err};
       QMC_PROF_TRY(QMC_KC_BROADCAST, tc_store_gemm(s, sa));
-      if (!fused && !stream)
+      if (!fused && !stream && !fl_means)
         QMC_PROF(QMC_KC_MEANS, launch_mean_h2(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], p.P2, H2, d.g2_p[l],
                                               StSplit{G2, d.g2_p[l], p.g2_plane}));
       TcLayerArgs la{};
@@ -470,6 +487,11 @@ static qmc_status run_backbone_mixed(qmc_model* m, const Plan& p, void* ws, cuda
         QMC_PROF(QMC_KC_PAIR, launch_pair_layer_mean(s, B, n, d.n_up, d.C, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
                                                      ar + a.b2[l], h2o, d.g2_p[l + 1],
                                                      StSplit{at<bf>(ws, p.g2), d.g2_p[l + 1], p.g2_plane}));
+      else if (fl_means)  // the pair output is read again only by a later pair layer
+        QMC_PROF(QMC_KC_PAIR,
+                 launch_pair_layer_mean_fl(s, B, n, d.n_up, d.C, Tp, T, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
+                                           ar + a.b2[l], d.upd2[l + 1] ? h2o : nullptr, d.g2_p[l + 1],
+                                           StSplit{at<bf>(ws, p.g2), d.g2_p[l + 1], p.g2_plane}));
       else
         QMC_PROF(QMC_KC_PAIR, launch_pair_layer(s, B * n * n, p.P2, d.d2_in[l], d.d2[l], H2, ar + a.w2[l],
                                                 ar + a.b2[l], h2o));

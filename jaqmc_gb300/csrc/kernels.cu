@@ -947,6 +947,159 @@ __global__ void __launch_bounds__(256) k_pair_layer_t5(int npairs, const float* 
   }
 }
 
+// Tangent pair layer fused with the next one-electron layer's pair means
+// (k_pair_layer_t5 followed by k_mean_h2 on its output), one block of 16 n
+// threads per walker: thread (i, q) owns features 2q, 2q+1 of every pair
+// (a, i) and walks a in electron order, with pair row a (all i) staged in
+// shared memory.  It writes the pair outputs (same arithmetic order as
+// k_pair_layer_t5), scatters each pair's gradient planes into the Jacobian
+// rows t = 2 + 3a + c of row i of G2 (channel of a, times 1/n_s; zeros in
+// the other channel), and keeps the channel sums of the five planes over a
+// in registers for rows t = 0 (mean), 1 (twice the mean Laplacian) and the
+// rows of electron i itself (minus the mean gradient), as k_mean_h2 forms
+// them.  Padding rows T..Tp-1 are written as zeros.  Every G2 element is
+// written once, so no atomics and no ordering between threads are involved.
+// Two adjacent features of one row (c even): one 8-byte (FP32) or two 4-byte
+// (split bf16 planes) stores.
+__device__ __forceinline__ void put2(const StF32& Y, size_t r, int c, float x0, float x1) {
+  *reinterpret_cast<float2*>(Y.p + r * Y.ld + c) = make_float2(x0, x1);
+}
+__device__ __forceinline__ void put2(const StSplit& Y, size_t r, int c, float x0, float x1) {
+  const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
+  const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - __low2float(hi), x1 - __high2float(hi));
+  __nv_bfloat16* p = Y.p + r * Y.ld + c;
+  *reinterpret_cast<__nv_bfloat162*>(p) = hi;
+  *reinterpret_cast<__nv_bfloat162*>(p + Y.plane) = lo;
+}
+
+template <int DIN, class Out>
+__global__ void __launch_bounds__(512) k_pair_layer_t5_mean(int n, int n_up, int C, int Tp, int T,
+                                                             const float* __restrict__ Hin,
+                                                             const float* __restrict__ W,
+                                                             const float* __restrict__ b, float* __restrict__ Hout,
+                                                             int g2p, Out G2) {
+  constexpr int P2 = 5, DO = 32;
+  constexpr int RS = P2 * DIN + 4;  // staged pair stride (floats)
+  extern __shared__ __align__(16) float smp[];
+  float* Ws = smp;               // [DIN][32]
+  float* Is = Ws + DIN * DO;     // [n][RS]: pairs (a, i) of the current a
+  const int w = blockIdx.x;
+  const int i = threadIdx.x >> 4, q = threadIdx.x & 15, f0 = 2 * q;
+  for (int e = threadIdx.x; e < DIN * DO; e += blockDim.x) Ws[e] = W[e];
+  const float b0 = b[f0], b1 = b[f0 + 1];
+  // channel sums of the five planes (channel 0 / 1 of the first electron)
+  float acc0[P2][2], acc1[P2][2];
+#pragma unroll
+  for (int p = 0; p < P2; ++p) acc0[p][0] = acc0[p][1] = acc1[p][0] = acc1[p][1] = 0.f;
+  const size_t row_i = ((size_t)w * n + i) * Tp;  // G2 rows of electron i
+  const float inv0 = 1.0f / (float)(C == 1 ? n : n_up), inv1 = C == 1 ? 0.f : 1.0f / (float)(n - n_up);
+  constexpr int V4 = P2 * DIN / 4;
+  for (int a = 0; a < n; ++a) {
+    __syncthreads();  // the previous row's reads are done
+    const float4* src = reinterpret_cast<const float4*>(Hin + ((size_t)w * n + a) * n * P2 * DIN);
+    for (int e = threadIdx.x; e < n * V4; e += blockDim.x) {
+      const int pi = e / V4, qq = e - pi * V4;
+      *reinterpret_cast<float4*>(Is + pi * RS + 4 * qq) = __ldg(src + e);
+    }
+    __syncthreads();
+    const float* in = Is + i * RS;
+    float z[P2][2];
+#pragma unroll
+    for (int p = 0; p < P2; ++p) z[p][0] = z[p][1] = 0.f;
+#pragma unroll
+    for (int k0 = 0; k0 < DIN; k0 += 4) {
+      float4 x[P2];
+#pragma unroll
+      for (int p = 0; p < P2; ++p) x[p] = *reinterpret_cast<const float4*>(in + p * DIN + k0);
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const float2 wv = *reinterpret_cast<const float2*>(Ws + (k0 + kk) * DO + f0);
+#pragma unroll
+        for (int p = 0; p < P2; ++p) {
+          const float xv = kk == 0 ? x[p].x : kk == 1 ? x[p].y : kk == 2 ? x[p].z : x[p].w;
+          z[p][0] = fmaf(xv, wv.x, z[p][0]);
+          z[p][1] = fmaf(xv, wv.y, z[p][1]);
+        }
+      }
+    }
+    float out[P2][2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const float h = tanhf(z[0][c] + (c == 0 ? b0 : b1));
+      const float d1 = 1.f - h * h, d2 = -2.f * h * d1;
+      const float S = z[2][c] * z[2][c] + z[3][c] * z[3][c] + z[4][c] * z[4][c];
+      out[0][c] = h;
+      out[1][c] = d1 * z[1][c] + d2 * S;
+      out[2][c] = d1 * z[2][c];
+      out[3][c] = d1 * z[3][c];
+      out[4][c] = d1 * z[4][c];
+    }
+    float* o = Hout ? Hout + (((size_t)w * n + a) * n + i) * P2 * DO + f0 : nullptr;
+    const int sa = (C == 2 && a >= n_up) ? 1 : 0;
+    const float inva = sa ? inv1 : inv0;
+#pragma unroll
+    for (int p = 0; p < P2; ++p) {
+      float2 v = make_float2(out[p][0], out[p][1]);
+      if (DIN == DO) {
+        const float2 r = *reinterpret_cast<const float2*>(in + p * DIN + f0);
+        v.x = (v.x + r.x) * kRsqrt2;
+        v.y = (v.y + r.y) * kRsqrt2;
+      }
+      if (o) *reinterpret_cast<float2*>(o + p * DO) = v;
+      if (sa == 0) {  // uniform over the block: keeps both sums in registers
+        acc0[p][0] += v.x;
+        acc0[p][1] += v.y;
+      } else {
+        acc1[p][0] += v.x;
+        acc1[p][1] += v.y;
+      }
+      if (p >= 2 && a != i && 2 + 3 * a + (p - 2) < T) {
+        // Jacobian row of electron a, direction p - 2: the pair's gradient
+        const size_t r = row_i + 2 + 3 * a + (p - 2);
+        put2(G2, r, sa * DO + f0, v.x * inva, v.y * inva);
+        if (C == 2) put2(G2, r, (1 - sa) * DO + f0, 0.f, 0.f);
+      }
+    }
+  }
+  // rows 0 (value), 1 (Laplacian) and electron i's own Jacobian rows
+  auto emit = [&](const float (&A)[P2][2], int sc, float inv) {
+    const int col = sc * DO + f0;
+    put2(G2, row_i, col, A[0][0] * inv, A[0][1] * inv);
+    put2(G2, row_i + 1, col, 2.0f * A[1][0] * inv, 2.0f * A[1][1] * inv);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (2 + 3 * i + d < T) put2(G2, row_i + 2 + 3 * i + d, col, -A[2 + d][0] * inv, -A[2 + d][1] * inv);
+  };
+  emit(acc0, 0, inv0);
+  if (C == 2) emit(acc1, 1, inv1);
+  // padding columns and rows (g2p is even)
+  for (int col = C * DO + 2 * q; col < g2p; col += 32)
+    for (int t = 0; t < T; ++t) put2(G2, row_i + t, col, 0.f, 0.f);
+  for (int t = T; t < Tp; ++t)
+    for (int col = 2 * q; col < g2p; col += 32) put2(G2, row_i + t, col, 0.f, 0.f);
+}
+
+template <class Out>
+cudaError_t launch_pair_layer_mean_fl(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d_in,
+                                      int d_out, const float* Hin, const float* W, const float* b, float* Hout,
+                                      int g2p, Out G2) {
+  if (d_out != 32 || (d_in != 4 && d_in != 32) || n < 1 || 16 * n > 512 || T != 3 * n + 2 ||
+      ((uintptr_t)Hin & 15) != 0)
+    return cudaErrorNotSupported;
+  const size_t sm = sizeof(float) * ((size_t)d_in * 32 + (size_t)n * (5 * d_in + 4));
+  if (sm > 48 * 1024) return cudaErrorNotSupported;
+  if (d_in == 4)
+    k_pair_layer_t5_mean<4, Out><<<B, 16 * n, sm, s>>>(n, n_up, C, Tp, T, Hin, W, b, Hout, g2p, G2);
+  else
+    k_pair_layer_t5_mean<32, Out><<<B, 16 * n, sm, s>>>(n, n_up, C, Tp, T, Hin, W, b, Hout, g2p, G2);
+  return cudaGetLastError();
+}
+template cudaError_t launch_pair_layer_mean_fl<StF32>(cudaStream_t, int, int, int, int, int, int, int, int,
+                                                      const float*, const float*, const float*, float*, int, StF32);
+template cudaError_t launch_pair_layer_mean_fl<StSplit>(cudaStream_t, int, int, int, int, int, int, int, int,
+                                                        const float*, const float*, const float*, float*, int,
+                                                        StSplit);
+
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout) {
   if (P2 == 5 && d_out == 32 && (d_in == 4 || d_in == 32) && ((uintptr_t)Hin & 15) == 0 &&

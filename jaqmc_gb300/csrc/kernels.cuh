@@ -60,6 +60,16 @@ cudaError_t launch_inputs_fl(cudaStream_t s, int B, int n, int A, int n_up, int 
                              double nuc, const float* Wg1, float* rae, float* aevec, float* H2, StSplit X0s,
                              StSplit G2s, float* Gb, float* pe);
 
+// Tangent two-electron layer (P2 = 5, 32 outputs) fused with the next
+// one-electron layer's pair means: Hout as launch_pair_layer (skipped when
+// null), G2 [(w*n+i)*Tp + t][g2p] as launch_mean_h2 on Hout; one block per
+// walker (16 n threads, n <= 32).  cudaErrorNotSupported for shapes it does
+// not cover.
+template <class Out>
+cudaError_t launch_pair_layer_mean_fl(cudaStream_t s, int B, int n, int n_up, int C, int Tp, int T, int d_in,
+                                      int d_out, const float* Hin, const float* W, const float* b, float* Hout,
+                                      int g2p, Out G2);
+
 // Two-electron layer h2' = residual(tanh(h2 W + b)) on compact tangent rows.
 cudaError_t launch_pair_layer(cudaStream_t s, int npairs, int P2, int d_in, int d_out,
                               const float* Hin, const float* W, const float* b, float* Hout);
