@@ -1308,13 +1308,11 @@ __global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, 
   __syncthreads();
   const size_t row0 = (size_t)w * n;
   const int A4 = 4 * A;
-  const int k8 = K0p / 8;  // 8 features per thread, 16-byte stores
-  for (int e = threadIdx.x; e < n * k8; e += blockDim.x) {
-    const int i = e / k8, f0 = 8 * (e - i * k8);
-    float v[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] = f0 + q < A4 ? f4_comp(ea[i * A + ((f0 + q) >> 2)], (f0 + q) & 3) : 0.f;
-    store8(X0s, row0 + i, f0, v);
+  const int k2 = K0p / 2;  // two features per thread, paired stores
+  for (int e = threadIdx.x; e < n * k2; e += blockDim.x) {
+    const int i = e / k2, f0 = 2 * (e - i * k2);
+    put2(X0s, row0 + i, f0, f0 < A4 ? f4_comp(ea[i * A + (f0 >> 2)], f0 & 3) : 0.f,
+         f0 + 1 < A4 ? f4_comp(ea[i * A + ((f0 + 1) >> 2)], (f0 + 1) & 3) : 0.f);
   }
   for (int col = threadIdx.x; col < g1p; col += blockDim.x) {
     float acc = 0.f;
@@ -1327,12 +1325,12 @@ __global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, 
     }
     g1[col] = acc;
   }
-  const int c8 = g2p / 8;
-  for (int e = threadIdx.x; e < n * c8; e += blockDim.x) {
-    const int i = e / c8, col0 = 8 * (e - i * c8);
-    float vv[8];
+  const int c2 = g2p / 2;  // two columns per thread, paired stores
+  for (int e = threadIdx.x; e < n * c2; e += blockDim.x) {
+    const int i = e / c2, col0 = 2 * (e - i * c2);
+    float vv[2];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < 2; ++q) {
       const int col = col0 + q;
       float v = 0.f;
       if (col < 4 * C) {
@@ -1346,7 +1344,7 @@ __global__ void k_inputs_value(int n, int A, int n_up, int C, int K0p, int g1p, 
       }
       vv[q] = v;
     }
-    store8(G2s, row0 + i, col0, vv);
+    put2(G2s, row0 + i, col0, vv[0], vv[1]);
   }
   __syncthreads();
   for (int f = threadIdx.x; f < dout; f += blockDim.x) {
@@ -1469,6 +1467,8 @@ __global__ void __launch_bounds__(256, 1) k_inputs_fl(int n, int A, int n_up, in
     return comp == 0 ? f4_comp(ed[i * A + I], 1 + c) : (comp - 1 == c ? 1.f : 0.f);
   };
   const size_t rowb = (size_t)w * n * Tp;
+  // 1 / n_s of the two channels (the same quotient every mean kernel forms)
+  const float invc[2] = {1.0f / (float)(C == 1 ? n : n_up), C == 1 ? 0.f : 1.0f / (float)(n - n_up)};
   const int k8 = K0p / 8;  // one-electron rows: 8 features per thread, 16-byte stores
   for (int e = threadIdx.x; e < n * Tp * k8; e += blockDim.x) {
     const int it = e / k8, f0 = 8 * (e - it * k8);
@@ -1494,7 +1494,7 @@ __global__ void __launch_bounds__(256, 1) k_inputs_fl(int n, int A, int n_up, in
         const int el = (t - 2) / 3;
         if (el >= a0 && el < a1) acc = x0v(el, t, f);
       }
-      acc *= 1.0f / (float)(a1 - a0);
+      acc *= invc[sc];
     }
     g1[e] = acc;
   }
@@ -1514,7 +1514,7 @@ __global__ void __launch_bounds__(256, 1) k_inputs_fl(int n, int A, int n_up, in
         const int sc = col >> 2, f = col & 3;
         int a0, a1;
         channel_range(sc, C, n, n_up, &a0, &a1);
-        const float inv = 1.0f / (float)(a1 - a0);
+        const float inv = invc[sc];
         if (t == 0) {
           v = f4_comp(ps[((size_t)sc * n + i) * 5], f) * inv;
         } else if (t == 1) {
