@@ -524,18 +524,22 @@ def run_gradient(dev, steps, warmup, walkers=4096, budget_gb=8, burn_in=200, fd_
 
 
 # ----------------------------------------------------------------- serving
-def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
-    """Poisson(rate) arrivals of neutral-atom jobs (Z ~ U{2..18}, Hund spins,
-    walkers ~ U{256..4096}, parameters seed 0 so that jobs of one element
-    share a model), each ``requests`` requests of 20 MH steps + E_L
+def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150, z_range=(2, 18),
+                walker_choices=(256, 512, 1024, 2048, 4096), group_max=8):
+    """Poisson(rate) arrivals of neutral-atom jobs (Z ~ U{z_range}, Hund
+    spins, walkers ~ U{walker_choices}, parameters seed 0 so that jobs of one
+    element share a model), each ``requests`` requests of 20 MH steps + E_L
     mean/variance in the mixed form, served with ``slots`` concurrent slots;
-    queued requests of jobs sharing a model are packed into one launch set."""
+    queued requests of jobs sharing a model are packed into one launch set
+    (up to ``group_max`` requests; 1: no packing)."""
     from jaqmc_gb300 import serving as SV
     be = SV.CudaBackend(precision="mixed", mh_steps=20, stddev=0.02, device=dev)
     warm = SV.Server(be, n_slots=2, hbm_budget=budget_gb << 30)
-    warm.run_arrivals(SV.atom_job_specs(3, rate=0.0, seed=10_000, requests=2, walker_choices=(256,)))
-    srv = SV.Server(be, n_slots=slots, hbm_budget=budget_gb << 30)
-    specs = SV.atom_job_specs(n_jobs, rate, seed=seed, requests=requests)
+    warm.run_arrivals(SV.atom_job_specs(3, rate=0.0, seed=10_000, requests=2, walker_choices=(256,),
+                                        z_range=z_range))
+    srv = SV.Server(be, n_slots=slots, hbm_budget=budget_gb << 30, group_max=group_max)
+    specs = SV.atom_job_specs(n_jobs, rate, seed=seed, requests=requests, z_range=z_range,
+                              walker_choices=walker_choices)
     srv.run_arrivals(specs)
     first = min(sp.arrival for sp in specs)
     span = max(st.finished for st in srv.finished_jobs) - first
@@ -543,6 +547,7 @@ def run_serving(dev, rate, n_jobs, requests, slots=8, seed=0, budget_gb=150):
     ws = sum(sp.walkers * 20 * requests for sp in specs)
     bad = [st.spec.job_id for st in srv.finished_jobs if not np.all(np.isfinite(np.stack(st.results)[:, :2]))]
     return {"arrival_rate_jobs_per_s": rate, "jobs": n_jobs, "requests_per_job": requests, "slots": slots,
+            "elements_z": list(z_range), "walker_choices": list(walker_choices), "group_max": group_max,
             "hbm_budget_gb": budget_gb, "jobs_per_s": n_jobs / span, "requests_per_s": n_jobs * requests / span,
             "walker_steps_per_s": ws / span, "request_p50_ms": float(np.percentile(lat, 50)),
             "request_p99_ms": float(np.percentile(lat, 99)), "job_p50_ms": float(np.percentile(jl, 50)),
@@ -738,7 +743,12 @@ def run_ours(args, wl):
     serve = None
     if not args.no_serve:
         serve = {"by_arrival_rate": [run_serving(dev, float(r), args.serve_jobs, args.serve_requests,
-                                                 slots=args.serve_slots) for r in args.serve_rates.split(",")]}
+                                                 slots=args.serve_slots) for r in args.serve_rates.split(",")],
+                 # a burst of small jobs of one model (nitrogen atoms), served without and with
+                 # packing of queued requests into one launch set
+                 "same_model_burst": [run_serving(dev, 200.0, 64, 2, slots=args.serve_slots, seed=1,
+                                                  z_range=(7, 7), walker_choices=(256, 512, 1024), group_max=g)
+                                      for g in (1, 8)]}
     cpu = None
     if rank == 0 and not args.no_cpu:
         r, cores, desc = cpu_request_rate(wl)
