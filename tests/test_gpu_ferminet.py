@@ -55,6 +55,9 @@ CASES = {
     "H-small": (S.hydrogen, lambda: small_cfg((1, 0)), 16),
     "He-triplet": (lambda: S.make_molecule("He", [2], [[0, 0, 0]], (2, 0)), lambda: small_cfg((2, 0)), 16),
     "He-down": (lambda: S.make_molecule("He", [2], [[0, 0, 0]], (0, 2)), lambda: small_cfg((0, 2)), 16),
+    # one spin channel at the full widths: the single-channel branches of the
+    # fused input and pair-mean kernels
+    "He-triplet-full": (lambda: S.make_molecule("He", [2], [[0, 0, 0]], (2, 0)), lambda: full_cfg((2, 0)), 16),
     "CH4-full": (S.methane, lambda: full_cfg((5, 5)), 32),
     "N2-full": (S.nitrogen_dimer, lambda: full_cfg((7, 7)), 32),
     "N2-isotropic": (S.nitrogen_dimer, lambda: full_cfg((7, 7), envelope="isotropic", ndets=4), 32),
@@ -357,10 +360,12 @@ def test_local_energy_on_equilibrated_walkers(case, cuda_device):
 MIXED_EXTRA = {
     "P-full": (lambda: S.atom(15), lambda: full_cfg(S.atom(15).nspins), 64),
     "Ar-full": (lambda: S.atom(18), lambda: full_cfg(S.atom(18).nspins), 64),
+    # one spin channel (and, for H, one electron) at the full widths
+    "H-full": (S.hydrogen, lambda: full_cfg((1, 0)), 64),
 }
 
 
-@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full", "P-full", "Ar-full"])
+@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full", "P-full", "Ar-full", "He-triplet-full", "H-full"])
 def test_mixed_form_on_equilibrated_walkers(case, cuda_device):
     molf, cfgf, _ = {**CASES, **MIXED_EXTRA}[case]
     mol, cfg = molf(), cfgf()
