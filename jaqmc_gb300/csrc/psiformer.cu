@@ -588,13 +588,12 @@ static qmc_status psi_backbone_fl(qmc_model* m, const PsiPlan& pp, void* ws, cud
   const int groups = p.B * d.n, rows = groups * p.Tp, Tp = p.Tp, D = d.D;
   float* x = at<float>(ws, pp.x);
   float* z = at<float>(ws, pp.z);
-  {
-    const RowMap map{1, 0, 1, 1};
-    QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, rows, map, at<float>(ws, p.x0), d.K0p, d.K0p, nullptr, 0, 0,
-                                             ar + a.w_in, D, D, EpiStore{z, D, nullptr}));
-  }
-  QMC_PROF(QMC_KC_LAYER0, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + P.in_b, 0, x, 1, ar + P.ln0_s[0],
-                                              ar + P.ln0_b[0], fmt(ws, pp, pp.xn, D)));
+  (void)rows;
+  // input Dense fused into its group pass (the inputs' tangent rows are
+  // sparse: an electron's features depend on its own position only)
+  QMC_PROF(QMC_KC_LAYER0, launch_psi_input_fl(s, groups, d.n, Tp, D, at<float>(ws, p.x0), d.K0, d.K0p,
+                                              ar + a.w_in, ar + P.in_b, x, ar + P.ln0_s[0], ar + P.ln0_b[0],
+                                              fmt(ws, pp, pp.xn, D)));
   for (int l = 0; l < d.L; ++l) {
     QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn, D, a.w_qkv[l], a.t_qkv[l], 3 * D));
     QMC_PROF(QMC_KC_PAIR, launch_psi_attention_fl(s, p.B, d.n, Tp, p.T, d.H, d.Dh, z, ar + a.b_qkv[l],
@@ -641,14 +640,13 @@ static qmc_status lapnet_backbone_fl(qmc_model* m, const PsiPlan& pp, void* ws, 
   float* x2 = at<float>(ws, pp.x2);
   float* z = at<float>(ws, pp.z);
   float* z2 = at<float>(ws, pp.z2);
-  {
-    const RowMap map{1, 0, 1, 1};
-    QMC_PROF(QMC_KC_LAYER0, launch_gemm_simt(s, rows, map, at<float>(ws, p.x0), d.K0p, d.K0p, nullptr, 0, 0,
-                                             ar + a.w_in, D, D, EpiStore{z, D, nullptr}));
-  }
-  QMC_PROF(QMC_KC_LAYER0, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + a.lb_in, 0, x, 1, nullptr, nullptr,
+  (void)rows;
+  // the input Dense of both streams fused into their group passes
+  QMC_PROF(QMC_KC_LAYER0, launch_psi_input_fl(s, groups, d.n, Tp, D, at<float>(ws, p.x0), d.K0, d.K0p,
+                                              ar + a.w_in, ar + a.lb_in, x, nullptr, nullptr,
                                               fmt(ws, pp, pp.xn, D)));
-  QMC_PROF(QMC_KC_LAYER0, launch_psi_group_fl(s, groups, Tp, D, z, D, ar + a.lb_in, 0, x2, 1, nullptr, nullptr,
+  QMC_PROF(QMC_KC_LAYER0, launch_psi_input_fl(s, groups, d.n, Tp, D, at<float>(ws, p.x0), d.K0, d.K0p,
+                                              ar + a.w_in, ar + a.lb_in, x2, nullptr, nullptr,
                                               fmt(ws, pp, pp.xn2, D)));
   for (int l = 0; l < d.L; ++l) {
     QMC_TRY(psi_gemm(m, pp, ws, s, pp.xn2, D, P.qk_k[l], a.t_qkv[l], 2 * D, z, 3 * D));

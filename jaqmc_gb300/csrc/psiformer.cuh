@@ -110,6 +110,13 @@ template <class Out>
 cudaError_t launch_psi_group_fl(cudaStream_t s, int groups, int Tp, int D, const float* z, int ldz,
                                 const float* bias, int act, float* x, int xmode, const float* ln_s,
                                 const float* ln_b, Out out);
+// The input layer of a tangent pass in one kernel: z = x0 W_in formed per
+// electron for its nonzero tangent rows (value, Laplacian, its own three
+// Jacobian rows), then launch_psi_group_fl's act 0 / xmode 1 rules.
+template <class Out>
+cudaError_t launch_psi_input_fl(cudaStream_t s, int groups, int n, int Tp, int D, const float* x0, int k0,
+                                int k0p, const float* w_in, const float* bias, float* x, const float* ln_s,
+                                const float* ln_b, Out out);
 template <class Out>
 cudaError_t launch_psi_attention_fl(cudaStream_t s, int B, int n, int Tp, int T, int H, int Dh, const float* qkv,
                                     const float* bqkv, Out out);

@@ -232,12 +232,44 @@ __device__ __forceinline__ void put4(const StSplit& o, size_t r, int c, float4 v
 // Jacobian rows t >= 2 (J h = h' J z, accumulating sum_d (J_d z)^2 per
 // feature), then the Laplacian row, which needs that sum.  A warp takes
 // whole rows, a lane four consecutive features per 128 (16-byte accesses).
+//
+// Input layer (in.x0 set): z = x0 W_in is formed here instead of read.  An
+// electron's input features depend on its own position only, so of its
+// tangent rows only the value row, the Laplacian row and its own three
+// Jacobian rows t = 2 + 3i + c are nonzero; the others have z = 0 exactly.
+struct PsiInput {
+  const float* x0;  // [group * Tp + t][k0p] input features with tangents (null: read z)
+  const float* w;   // [k0][D] input Dense kernel
+  int k0, k0p, n;   // features, their row stride, electrons per walker
+};
+
+__device__ __forceinline__ float xw_dot(const float* __restrict__ xr, const float* __restrict__ W, int k0, int D,
+                                        int c) {
+  float acc = 0.f;
+  for (int k = 0; k < k0; ++k) acc = fmaf(__ldg(xr + k), __ldg(W + (size_t)k * D + c), acc);
+  return acc;
+}
+__device__ __forceinline__ float4 xw_dot4(const float* __restrict__ xr, const float* __restrict__ W, int k0, int D,
+                                          int c) {
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k = 0; k < k0; ++k) {
+    const float xv = __ldg(xr + k);
+    const float4 w = __ldg(reinterpret_cast<const float4*>(W + (size_t)k * D + c));
+    acc.x = fmaf(xv, w.x, acc.x);
+    acc.y = fmaf(xv, w.y, acc.y);
+    acc.z = fmaf(xv, w.z, acc.z);
+    acc.w = fmaf(xv, w.w, acc.w);
+  }
+  return acc;
+}
+
 template <class Out>
 __global__ void __launch_bounds__(kGrpWarps * 32) k_psi_group_fl(int Tp, int D, const float* __restrict__ z,
                                                                   int ldz, const float* __restrict__ bias, int act,
                                                                   float* __restrict__ x, int xmode,
                                                                   const float* __restrict__ ln_s,
-                                                                  const float* __restrict__ ln_b, Out out) {
+                                                                  const float* __restrict__ ln_b, Out out,
+                                                                  PsiInput in) {
   constexpr int kV = kGrpMaxD / 128;
   __shared__ __align__(16) float colacc[kGrpWarps][kGrpMaxD];
   __shared__ __align__(16) float hv[2][kGrpMaxD];  // h, h' of the value row
@@ -247,10 +279,11 @@ __global__ void __launch_bounds__(kGrpWarps * 32) k_psi_group_fl(int Tp, int D, 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t r0 = (size_t)blockIdx.x * Tp;
   const float invD = 1.f / (float)D;
+  const int t_own = in.x0 ? 2 + 3 * (int)(blockIdx.x % (unsigned)in.n) : 0;  // first nonzero Jacobian row
   // value row
   float s = 0.f;
   for (int c = threadIdx.x; c < D; c += blockDim.x) {
-    float v = z[r0 * ldz + c] + bias[c];
+    float v = (in.x0 ? xw_dot(in.x0 + r0 * in.k0p, in.w, in.k0, D, c) : z[r0 * ldz + c]) + bias[c];
     if (act) {
       v = tanhf(v);
       hv[0][c] = v;
@@ -279,11 +312,14 @@ __global__ void __launch_bounds__(kGrpWarps * 32) k_psi_group_fl(int Tp, int D, 
     const float* zr = z + (r0 + t) * ldz;
     float* xr = x + (r0 + t) * D;
     float s1 = 0.f, s2 = 0.f;
+    const bool live = !in.x0 || (unsigned)(t - t_own) < 3u;
 #pragma unroll
     for (int k = 0; k < kV; ++k) {
       const int c = 4 * lane + 128 * k;
       if (c < D) {
-        const float4 zz = *reinterpret_cast<const float4*>(zr + c);
+        const float4 zz = !in.x0 ? *reinterpret_cast<const float4*>(zr + c)
+                                 : (live ? xw_dot4(in.x0 + (r0 + t) * in.k0p, in.w, in.k0, D, c)
+                                         : make_float4(0.f, 0.f, 0.f, 0.f));
         float4 v = zz;
         if (act) {
           const float4 h1 = *reinterpret_cast<const float4*>(&hv[1][c]);
@@ -328,7 +364,7 @@ __global__ void __launch_bounds__(kGrpWarps * 32) k_psi_group_fl(int Tp, int D, 
   __syncthreads();
   float s1 = 0.f, s2 = 0.f;
   for (int c = threadIdx.x; c < D; c += blockDim.x) {
-    float v = z[(r0 + 1) * ldz + c];
+    float v = in.x0 ? xw_dot(in.x0 + (r0 + 1) * in.k0p, in.w, in.k0, D, c) : z[(r0 + 1) * ldz + c];
     if (act) {
       float q = 0.f;
 #pragma unroll
@@ -417,7 +453,8 @@ cudaError_t launch_psi_group_fl(cudaStream_t s, int groups, int Tp, int D, const
                                 const float* bias, int act, float* x, int xmode, const float* ln_s,
                                 const float* ln_b, Out out) {
   if (D % 64 || D > kGrpMaxD || Tp > kGrpMaxTp || Tp < 2 || ldz % 4 || (ln_s && !xmode)) return cudaErrorInvalidValue;
-  k_psi_group_fl<Out><<<groups, kGrpWarps * 32, 0, s>>>(Tp, D, z, ldz, bias, act, x, xmode, ln_s, ln_b, out);
+  k_psi_group_fl<Out><<<groups, kGrpWarps * 32, 0, s>>>(Tp, D, z, ldz, bias, act, x, xmode, ln_s, ln_b, out,
+                                                        PsiInput{nullptr, nullptr, 0, 0, 1});
   return cudaGetLastError();
 }
 
@@ -731,6 +768,24 @@ __global__ void __launch_bounds__(kAttnFlThreads, 2) k_psi_attention_fl(int n, i
     out.put(grow + (size_t)i * Tp + T + r / Dh, h * Dh + r % Dh, 0.f);
   }
 }
+
+template <class Out>
+cudaError_t launch_psi_input_fl(cudaStream_t s, int groups, int n, int Tp, int D, const float* x0, int k0,
+                                int k0p, const float* w_in, const float* bias, float* x, const float* ln_s,
+                                const float* ln_b, Out out) {
+  if (D % 64 || D > kGrpMaxD || Tp > kGrpMaxTp || Tp < 5 || n < 1 || k0 > k0p ||
+      ((uintptr_t)w_in & 15) != 0)
+    return cudaErrorInvalidValue;
+  k_psi_group_fl<Out><<<groups, kGrpWarps * 32, 0, s>>>(Tp, D, nullptr, 0, bias, 0, x, 1, ln_s, ln_b, out,
+                                                        PsiInput{x0, w_in, k0, k0p, n});
+  return cudaGetLastError();
+}
+template cudaError_t launch_psi_input_fl<StF32>(cudaStream_t, int, int, int, int, const float*, int, int,
+                                                const float*, const float*, float*, const float*, const float*,
+                                                StF32);
+template cudaError_t launch_psi_input_fl<StSplit>(cudaStream_t, int, int, int, int, const float*, int, int,
+                                                  const float*, const float*, float*, const float*, const float*,
+                                                  StSplit);
 
 template <class Out>
 cudaError_t launch_psi_attention_fl(cudaStream_t s, int B, int n, int Tp, int T, int H, int Dh, const float* qkv,
