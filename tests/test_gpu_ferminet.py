@@ -58,6 +58,8 @@ CASES = {
     # one spin channel at the full widths: the single-channel branches of the
     # fused input and pair-mean kernels
     "He-triplet-full": (lambda: S.make_molecule("He", [2], [[0, 0, 0]], (2, 0)), lambda: full_cfg((2, 0)), 16),
+    # 16-wide two-electron layers: the paths around the fused 32-wide pair kernels
+    "N2-pair16": (S.nitrogen_dimer, lambda: full_cfg((7, 7), hidden_dims_double=[16, 16, 16, 16]), 32),
     "CH4-full": (S.methane, lambda: full_cfg((5, 5)), 32),
     "N2-full": (S.nitrogen_dimer, lambda: full_cfg((7, 7)), 32),
     "N2-isotropic": (S.nitrogen_dimer, lambda: full_cfg((7, 7), envelope="isotropic", ndets=4), 32),
@@ -365,7 +367,8 @@ MIXED_EXTRA = {
 }
 
 
-@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full", "P-full", "Ar-full", "He-triplet-full", "H-full"])
+@pytest.mark.parametrize("case", ["N2-full", "CH4-full", "Li-full", "P-full", "Ar-full", "He-triplet-full", "H-full",
+                                  "N2-pair16"])
 def test_mixed_form_on_equilibrated_walkers(case, cuda_device):
     molf, cfgf, _ = {**CASES, **MIXED_EXTRA}[case]
     mol, cfg = molf(), cfgf()
