@@ -3,6 +3,7 @@
 #include <algorithm>
 
 #include "kernels.cuh"
+#include "tc_ptx.cuh"
 
 namespace qmc {
 
@@ -951,7 +952,7 @@ __global__ void __launch_bounds__(256) k_pair_layer_t5(int npairs, const float* 
 // (k_pair_layer_t5 followed by k_mean_h2 on its output), one block of 16 n
 // threads per walker: thread (i, q) owns features 2q, 2q+1 of every pair
 // (a, i) and walks a in electron order, with pair row a (all i) staged in
-// shared memory.  It writes the pair outputs (same arithmetic order as
+// shared memory by cp.async one row ahead (two buffers).  It writes the pair outputs (same arithmetic order as
 // k_pair_layer_t5), scatters each pair's gradient planes into the Jacobian
 // rows t = 2 + 3a + c of row i of G2 (channel of a, times 1/n_s; zeros in
 // the other channel), and keeps the channel sums of the five planes over a
@@ -982,7 +983,7 @@ __global__ void __launch_bounds__(512) k_pair_layer_t5_mean(int n, int n_up, int
   constexpr int RS = P2 * DIN + 4;  // staged pair stride (floats)
   extern __shared__ __align__(16) float smp[];
   float* Ws = smp;               // [DIN][32]
-  float* Is = Ws + DIN * DO;     // [n][RS]: pairs (a, i) of the current a
+  float* Is0 = Ws + DIN * DO;    // [2][n][RS]: pairs (a, i) of rows a and a + 1
   const int w = blockIdx.x;
   const int i = threadIdx.x >> 4, q = threadIdx.x & 15, f0 = 2 * q;
   for (int e = threadIdx.x; e < DIN * DO; e += blockDim.x) Ws[e] = W[e];
@@ -994,15 +995,22 @@ __global__ void __launch_bounds__(512) k_pair_layer_t5_mean(int n, int n_up, int
   const size_t row_i = ((size_t)w * n + i) * Tp;  // G2 rows of electron i
   const float inv0 = 1.0f / (float)(C == 1 ? n : n_up), inv1 = C == 1 ? 0.f : 1.0f / (float)(n - n_up);
   constexpr int V4 = P2 * DIN / 4;
-  for (int a = 0; a < n; ++a) {
-    __syncthreads();  // the previous row's reads are done
-    const float4* src = reinterpret_cast<const float4*>(Hin + ((size_t)w * n + a) * n * P2 * DIN);
+  auto stage = [&](int a, float* dst) {
+    const float* src = Hin + ((size_t)w * n + a) * n * P2 * DIN;
     for (int e = threadIdx.x; e < n * V4; e += blockDim.x) {
       const int pi = e / V4, qq = e - pi * V4;
-      *reinterpret_cast<float4*>(Is + pi * RS + 4 * qq) = __ldg(src + e);
+      ptx::cp_async16(dst + pi * RS + 4 * qq, src + 4 * e);
     }
-    __syncthreads();
-    const float* in = Is + i * RS;
+  };
+  stage(0, Is0);
+  ptx::cp_async_commit();
+  for (int a = 0; a < n; ++a) {
+    __syncthreads();  // every thread is done with row a - 1, whose buffer row a + 1 takes
+    if (a + 1 < n) stage(a + 1, Is0 + ((a + 1) & 1) * n * RS);
+    ptx::cp_async_commit();  // (possibly empty) group of row a + 1
+    ptx::cp_async_wait<1>();  // this thread's copies of row a have landed
+    __syncthreads();          // and every thread's
+    const float* in = Is0 + (a & 1) * n * RS + i * RS;
     float z[P2][2];
 #pragma unroll
     for (int p = 0; p < P2; ++p) z[p][0] = z[p][1] = 0.f;
@@ -1086,7 +1094,7 @@ cudaError_t launch_pair_layer_mean_fl(cudaStream_t s, int B, int n, int n_up, in
   if (d_out != 32 || (d_in != 4 && d_in != 32) || n < 1 || 16 * n > 512 || T != 3 * n + 2 ||
       ((uintptr_t)Hin & 15) != 0)
     return cudaErrorNotSupported;
-  const size_t sm = sizeof(float) * ((size_t)d_in * 32 + (size_t)n * (5 * d_in + 4));
+  const size_t sm = sizeof(float) * ((size_t)d_in * 32 + 2 * (size_t)n * (5 * d_in + 4));
   if (sm > 48 * 1024) return cudaErrorNotSupported;
   if (d_in == 4)
     k_pair_layer_t5_mean<4, Out><<<B, 16 * n, sm, s>>>(n, n_up, C, Tp, T, Hin, W, b, Hout, g2p, G2);
