@@ -696,16 +696,20 @@ struct EpiTcOrbital {
   // electrons of channel s (4-D activation maps), tpc4[s] tiles per channel
   int chan4d, B;
   int W4[2], tpc4[2];
+  // channel selects (a runtime index into a kernel-parameter array would
+  // copy the struct to local memory)
+  __device__ __forceinline__ const float* pis(int s) const { return s ? pi[1] : pi[0]; }
+  __device__ __forceinline__ const float* sigs(int s) const { return s ? sigma[1] : sigma[0]; }
   __device__ TileInfo tile(int tx, const TcArgs& g) const {
     TileInfo t{};
     if (g.T == 1 && chan4d) {
       const int s = tx < tpc4[0] ? 0 : 1;
       const int ns = s ? n - n_up : n_up;
       t.a_sel = s;
-      t.w = (s ? tx - tpc4[0] : tx) * W4[s];
+      t.w = (s ? tx - tpc4[0] : tx) * (s ? W4[1] : W4[0]);
       t.row0 = t.w;
       t.i0 = s ? n_up : 0;
-      t.ng = min(W4[s], B - t.w) * ns;
+      t.ng = min(s ? W4[1] : W4[0], B - t.w) * ns;
       return t;
     }
     if (g.T == 1) {
@@ -743,8 +747,8 @@ struct EpiTcOrbital {
     for (int I = 0; I < kEnvRegs; ++I) {
       float pv = 0.f, se = 0.f;
       if (I < natom && !unit_env) {
-        pv = pi[s][((size_t)j * natom + I) * K + k];
-        float sv = sigma[s][((size_t)j * natom + I) * K + k];
+        pv = pis(s)[((size_t)j * natom + I) * K + k];
+        float sv = sigs(s)[((size_t)j * natom + I) * K + k];
         se = env_abs ? fabsf(sv) : sv;
       }
       ep.pv[I] = pv;
@@ -760,16 +764,7 @@ struct EpiTcOrbital {
     const float* ra = rae + ((size_t)w * n + i) * natom;
     const float* av = aevec + ((size_t)w * n + i) * natom * 3;
     float e0 = 0.f, ex = 0.f, ey = 0.f, ez = 0.f, el = 0.f;
-    for (int I = 0; I < natom; ++I) {
-      float pv, se;
-      if (I < kEnvRegs) {
-        pv = ep.pv[I];
-        se = ep.se[I];
-      } else {
-        pv = pi[s][((size_t)j * natom + I) * K + k];
-        float sv = sigma[s][((size_t)j * natom + I) * K + k];
-        se = env_abs ? fabsf(sv) : sv;
-      }
+    auto term = [&](int I, float pv, float se) {
       float r = ra[I];
       float ev = pv * expf(-se * r);
       e0 += ev;
@@ -780,6 +775,14 @@ struct EpiTcOrbital {
         ez = fmaf(gr, av[3 * I + 2], ez);
         el += ev * (se * se - 2.0f * se / r);
       }
+    };
+    // constant indices keep the register-held parameters out of local memory
+#pragma unroll
+    for (int I = 0; I < kEnvRegs; ++I)
+      if (I < natom) term(I, ep.pv[I], ep.se[I]);
+    for (int I = kEnvRegs; I < natom; ++I) {
+      float sv = sigs(s)[((size_t)j * natom + I) * K + k];
+      term(I, pis(s)[((size_t)j * natom + I) * K + k], env_abs ? fabsf(sv) : sv);
     }
     e[0] = e0; e[1] = ex; e[2] = ey; e[3] = ez; e[4] = el;
   }
@@ -788,14 +791,36 @@ struct EpiTcOrbital {
     const int k = fok ? f / n : 0, j = fok ? f % n : 0;
     const size_t ts = amat_tangent_stride(n, K);
     EnvParams ep;
-    load_params(ti.a_sel, k, j, ep);
+    if (g.T == 1 && raw) {  // value-only raw stores use no envelope
+#pragma unroll
+      for (int I = 0; I < kEnvRegs; ++I) ep.pv[I] = ep.se[I] = 0.f;
+    } else {
+      load_params(ti.a_sel, k, j, ep);
+    }
     if (g.T == 1 && chan4d) {
       const int ns = ti.a_sel ? n - n_up : n_up;
+      // raw stores of whole chunks walk one pointer: column (wq, iq) of the
+      // tile lands at base + wq*K*n*n + iq*n for this thread's (k, j)
+      const int wstride = K * n * n;
+      float* base = A + amat_index(1, n, K, ti.w, k, 0, ti.i0, j);
       for (int c0 = 16 * half; c0 < g.n_cols; c0 += 32) {
         float v[16];
         ptx::tmem_ld16(taddr + c0, v);
         if (!fok || c0 >= ti.ng) continue;
         int wq = c0 / ns, iq = c0 - wq * ns;
+        if (raw && c0 + 16 <= ti.ng) {
+          int off = wq * wstride + iq * n;
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) {
+            base[off] = v[jj];
+            off += n;
+            if (++iq == ns) {
+              iq = 0;
+              off += wstride - ns * n;
+            }
+          }
+          continue;
+        }
 #pragma unroll
         for (int jj = 0; jj < 16; ++jj) {
           if (c0 + jj < ti.ng) {
@@ -824,6 +849,22 @@ struct EpiTcOrbital {
         if (!fok || c0 >= ti.ng) continue;
         const int gi0 = ti.g0 + c0;
         int w = gi0 / n, i = gi0 - w * n;
+        if (raw && c0 + 16 <= ti.ng) {
+          // column (w, i) lands at base + w*K*n*n + i*n for this thread's (k, j)
+          float* base = A + amat_index(1, n, K, w, k, 0, 0, j);
+          const int wstep = K * n * n - n * n;
+          int off = i * n;
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) {
+            if (!split || (i < n_up ? 0 : 1) == ti.a_sel) base[off] = v[jj];
+            off += n;
+            if (++i == n) {
+              i = 0;
+              off += wstep;
+            }
+          }
+          continue;
+        }
 #pragma unroll
         for (int jj = 0; jj < 16; ++jj) {
           if (c0 + jj < ti.ng && (!split || (i < n_up ? 0 : 1) == ti.a_sel)) {
